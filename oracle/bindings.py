@@ -1,0 +1,177 @@
+"""ctypes bindings for the CPU oracle -- TEST INFRASTRUCTURE.
+
+Loads either the plain-C restatement (oracle/liboracle.so, built from
+tm_oracle.c) or the reference's own functions compiled from its sources
+(oracle/_ref/libtimothy_ref.so, reference flags, or libtimothy_ref_strict.so).
+Both export the same run signature (tm_oracle.h, ref_driver.c), so a caller
+picks one by name.  Only tests, __graft_entry__.smoke() and bench.py's CPU legs
+use this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBS = {
+    "oracle": os.path.join(HERE, "liboracle.so"),
+    "ref": os.path.join(HERE, "_ref", "libtimothy_ref.so"),
+    "ref_strict": os.path.join(HERE, "_ref", "libtimothy_ref_strict.so"),
+}
+
+_P = C.c_void_p
+_cache: dict[str, C.CDLL] = {}
+
+
+def build(ref: bool | None = None) -> None:
+    """Compile the restatement; also the reference library when its sources exist."""
+    subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+    refsrc = os.environ.get("TM_REFSRC", "/root/reference/src")
+    if ref is None:
+        ref = os.path.isdir(refsrc)
+    if ref:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REFSRC={refsrc}"], check=True)
+
+
+def available(which: str) -> bool:
+    return os.path.exists(LIBS[which])
+
+
+def load(which: str = "oracle") -> C.CDLL:
+    if which in _cache:
+        return _cache[which]
+    path = LIBS[which]
+    if not os.path.exists(path):
+        raise FileNotFoundError(f"{path} is not built (oracle.bindings.build())")
+    lib = C.CDLL(path)
+    fn = lib.tmo_run if which == "oracle" else lib.ref_run
+    argt = [C.c_int64, C.c_int, C.c_int] + [_P] * 6 + [_P] * 7 + [C.c_int, C.c_int, C.c_double] + [_P] * 6 + \
+        [_P, _P, _P, _P] + [C.c_int, C.c_float, _P, C.c_int64, _P, _P]
+    if which == "oracle":
+        argt = argt + [C.c_int]
+        lib.tmo_neighbours.restype = C.c_int
+        lib.tmo_neighbours.argtypes = [C.c_int64, C.c_int, C.c_int, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
+                                       C.c_int]
+        lib.tm_mix64.restype = C.c_uint64
+        lib.tm_mix64.argtypes = [C.c_uint64]
+    else:
+        lib.ref_sizeof.restype = C.c_int64
+        lib.ref_sizeof.argtypes = [C.c_int]
+    fn.restype = C.c_int
+    fn.argtypes = argt
+    _cache[which] = lib
+    return lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+@dataclass
+class RunResult:
+    x: np.ndarray
+    y: np.ndarray
+    z: np.ndarray
+    density: np.ndarray
+    v: np.ndarray
+    mindist: np.ndarray
+    fx: np.ndarray
+    fy: np.ndarray
+    fz: np.ndarray
+    removecell: np.ndarray
+    removecount: int
+    octsize: int
+    aff: np.ndarray
+    grid: np.ndarray | None
+    timing: np.ndarray
+
+
+def run(col, nsteps: int = 1, *, which: str = "oracle", update_mode: int = 0, dt: float = 1.0,
+        cic: bool = False, gfh: float = 8.0, nthreads: int = 0) -> RunResult:
+    """Run the oracle (or the reference) on a copy of ``col``'s cells."""
+    lib = load(which)
+    n = col.n
+    t = col.types
+    x, y, z = col.x.copy(), col.y.copy(), col.z.copy()
+    size = np.ascontiguousarray(col.size, np.float64)
+    young = np.ascontiguousarray(col.young, np.float32)
+    ctype = np.ascontiguousarray(col.ctype, np.int32)
+    phase = np.ascontiguousarray(col.phase, np.int32)
+    outs = {k: np.zeros(max(n, 1)) for k in ("density", "v", "mindist", "fx", "fy", "fz")}
+    rem = np.zeros(max(n, 1), np.uint8)
+    remc = np.zeros(1, np.int64)
+    octsize = np.zeros(1, np.int64)
+    aff = np.zeros(4)
+    timing = np.zeros(5)
+    gdims = np.zeros(3, np.int64)
+    grid = None
+    gcap = 0
+    if cic:
+        g = int((2049.0 + 1) / gfh) + 1
+        gcap = g * g * (g if col.dim == 3 else 1)
+        grid = np.zeros(gcap)
+    th, th2, th3, th4 = (np.ascontiguousarray(a, np.float64) for a in (t.h, t.h2, t.h3, t.h4))
+    tsize = np.ascontiguousarray(t.size, np.float64)
+    trm = np.ascontiguousarray(t.randommove, np.float32)
+    args = [n, col.dim, t.ntypes, _ptr(th), _ptr(th2), _ptr(th3), _ptr(th4), _ptr(tsize), _ptr(trm),
+            _ptr(x), _ptr(y), _ptr(z), _ptr(size), _ptr(young), _ptr(ctype), _ptr(phase),
+            nsteps, update_mode, dt,
+            _ptr(outs["density"]), _ptr(outs["v"]), _ptr(outs["mindist"]),
+            _ptr(outs["fx"]), _ptr(outs["fy"]), _ptr(outs["fz"]),
+            _ptr(rem), _ptr(remc), _ptr(octsize), _ptr(aff),
+            1 if cic else 0, gfh, _ptr(grid), gcap, _ptr(gdims), _ptr(timing)]
+    if which == "oracle":
+        rc = lib.tmo_run(*args, nthreads)
+    else:
+        rc = lib.ref_run(*args)
+    if rc != 0:
+        raise RuntimeError(f"{which} run failed with code {rc}")
+    if cic:
+        gx, gy, gz = (int(v) for v in gdims)
+        grid = grid[:gx * gy * gz].reshape(gx, gy, gz)
+    return RunResult(x, y, z, outs["density"][:n], outs["v"][:n], outs["mindist"][:n], outs["fx"][:n],
+                     outs["fy"][:n], outs["fz"][:n], rem[:n], int(remc[0]), int(octsize[0]), aff, grid, timing)
+
+
+@dataclass
+class Neighbours:
+    count: np.ndarray
+    hash: np.ndarray
+    vcand: np.ndarray
+    ncand: np.ndarray
+    offsets: np.ndarray | None
+    lists: np.ndarray | None
+
+
+def neighbours(col, *, lists: bool = False, nthreads: int = 0) -> Neighbours:
+    """Per-cell neighbour-set diagnostics of one octree walk (tm_oracle.h)."""
+    lib = load("oracle")
+    n = col.n
+    t = col.types
+    th = np.ascontiguousarray(t.h, np.float64)
+    cnt = np.zeros(max(n, 1), np.int32)
+    hsh = np.zeros(max(n, 1), np.uint64)
+    vc = np.zeros(max(n, 1), np.int64)
+    nc = np.zeros(max(n, 1), np.int32)
+    offs = np.zeros(n + 1, np.int64) if lists else None
+    ctype = np.ascontiguousarray(col.ctype, np.int32)
+    rc = lib.tmo_neighbours(n, col.dim, t.ntypes, _ptr(th), _ptr(col.x), _ptr(col.y), _ptr(col.z), _ptr(ctype),
+                            _ptr(cnt), _ptr(hsh), _ptr(vc), _ptr(nc), _ptr(offs), None, nthreads)
+    if rc != 0:
+        raise RuntimeError(f"tmo_neighbours failed with code {rc}")
+    lst = None
+    if lists:
+        lst = np.zeros(max(int(offs[n]), 1), np.int64)
+        rc = lib.tmo_neighbours(n, col.dim, t.ntypes, _ptr(th), _ptr(col.x), _ptr(col.y), _ptr(col.z),
+                                _ptr(ctype), None, None, None, None, _ptr(offs), _ptr(lst), nthreads)
+        if rc != 0:
+            raise RuntimeError(f"tmo_neighbours failed with code {rc}")
+    return Neighbours(cnt[:n], hsh[:n], vc[:n], nc[:n], offs, lst)
+
+
+def mix64(z: int) -> int:
+    return int(load("oracle").tm_mix64(z))

@@ -1,0 +1,235 @@
+/* Test-infrastructure driver around the reference's own hot-path functions.
+ *
+ * Compiled only into oracle/_ref/libtimothy_ref*.so, together with the
+ * unmodified reference sources (octree.c, potential.c, cells.c, patches.c,
+ * grid.c, utils.c) and the single-rank MPI shim.  It replays the hot part of
+ * the reference step loop (main.c:67-79, step.c:41-100) on structure-of-arrays
+ * inputs and copies the outputs back, so tests and the CPU baseline can call
+ * the reference through ctypes.  Nothing in the product links against it.
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <math.h>
+#include <omp.h>
+#include <sys/time.h>
+
+#include "global.h"
+#include "potential.h"
+#include "patches.h"
+#include "grid.h"
+
+/* defined in octree.c with external linkage (octree.h:24-27) */
+extern double3dv_t affShift;
+extern double affScale;
+void octbuild(systeminfo_t systeminfo, cellsinfo_t *cellsinfo, celltype_t *celltype);
+void octfree(cellsinfo_t *cellsinfo);
+/* cells.c:342 and patches.c:156 have no prototype in the reference headers */
+void updatepositions(settings_t settings, celltype_t *celltype, cellsinfo_t *cellsinfo,
+                     unsigned char *removecell, int64_t *removecount);
+void patches_cells2envinfo(systeminfo_t systeminfo, settings_t settings, patches_t *patches,
+                           cellsinfo_t *cellsinfo, grid_t *grid);
+void patches_commcells2envinit(systeminfo_t systeminfo, settings_t settings, patches_t *patches);
+int patches_commcells2envwait(systeminfo_t systeminfo, patches_t *patches);
+int patches_applycells2env(systeminfo_t systeminfo, settings_t settings, patches_t *patches,
+                           grid_t *grid, environment_t **environment);
+
+static double wall(void)
+{
+    struct timeval tv;
+    gettimeofday(&tv, NULL);
+    return tv.tv_sec + 1e-6 * tv.tv_usec;
+}
+
+/* Size of the reference structs, for the ABI checks in the tests. */
+int64_t ref_sizeof(int which)
+{
+    switch (which) {
+    case 0: return sizeof(celldata_t);
+    case 1: return sizeof(cellsinfo_t);
+    case 2: return sizeof(celltype_t);
+    case 3: return sizeof(systeminfo_t);
+    case 4: return sizeof(settings_t);
+    case 5: return sizeof(cellcommdata_t);
+    case 6: return sizeof(grid_t);
+    case 7: return sizeof(patches_t);
+    case 8: return sizeof(octnode_t);
+    case 9: return sizeof(environment_t);
+    default: return -1;
+    }
+}
+
+/*
+ * Run `nsteps` steps of the reference hot path.
+ *
+ * update_mode 0: the reference's updatepositions (x += F, cells.c:342-365);
+ * update_mode 1: the harness restatement x += dt*F with the same removal rule;
+ * update_mode 2: no position update.
+ * The density/v/mindist/force outputs are those of the last step, computed
+ * before its position update; x/y/z return the positions after all steps.
+ * With do_cic the CIC deposit of the last step (field 0 of
+ * environment[0].production, grid.c:37-136 geometry at one rank) is copied to
+ * grid_out (x-major, z fastest) when grid_cap is large enough.
+ * timing[0..4] accumulate seconds for octbuild, computepotential,
+ * computegradient, position update and CIC.
+ */
+int ref_run(int64_t n, int dim, int ntypes,
+            const double *th, const double *th2, const double *th3, const double *th4,
+            const double *tsize, const float *trandommove,
+            double *x, double *y, double *z, const double *size, const float *young,
+            const int *ctype, const int *phase,
+            int nsteps, int update_mode, double dt,
+            double *density, double *v, double *mindist,
+            double *fx, double *fy, double *fz,
+            unsigned char *removecell, int64_t *removecount,
+            int64_t *octsize, double *aff,
+            int do_cic, float gfh, double *grid_out, int64_t grid_cap, int64_t *grid_dims,
+            double *timing)
+{
+    systeminfo_t si;
+    settings_t st;
+    cellsinfo_t ci;
+    celltype_t *ct;
+    cellcommdata_t cc;
+    grid_t grid;
+    environment_t *env = NULL;
+    int64_t i;
+    int s, t;
+
+    memset(&si, 0, sizeof(si));
+    memset(&st, 0, sizeof(st));
+    memset(&ci, 0, sizeof(ci));
+    memset(&cc, 0, sizeof(cc));
+    memset(&grid, 0, sizeof(grid));
+    si.rank = 0;
+    si.size = 1;
+    si.nthreads = omp_get_max_threads();
+    si.dim[0] = si.dim[1] = si.dim[2] = 1;
+    si.coords = (int **)malloc(sizeof(int *));
+    si.coords[0] = (int *)calloc(3, sizeof(int));
+
+    st.dimension = dim;
+    st.numberofcelltypes = ntypes;
+    st.numberoffields = do_cic ? 1 : 0;
+    st.gfh = gfh;
+    st.maxlocalcells = n > 0 ? n : 1;
+
+    ct = (celltype_t *)calloc((size_t)ntypes, sizeof(celltype_t));
+    for (t = 0; t < ntypes; t++) {
+        ct[t].h = th[t];
+        ct[t].h2 = th2[t];
+        ct[t].h3 = th3[t];
+        ct[t].h4 = th4[t];
+        ct[t].size = tsize[t];
+        ct[t].randommove = trandommove ? trandommove[t] : 0.0f;
+    }
+
+    ci.dimension = dim;
+    ci.localcount.n = (uint64_t)n;
+    ci.cells = (celldata_t *)calloc((size_t)(n > 0 ? n : 1), sizeof(celldata_t));
+    ci.forces = (double3dv_t *)calloc((size_t)(n > 0 ? n : 1), sizeof(double3dv_t));
+    for (i = 0; i < n; i++) {
+        ci.cells[i].x = x[i];
+        ci.cells[i].y = y[i];
+        ci.cells[i].z = z[i];
+        ci.cells[i].size = size[i];
+        ci.cells[i].young = young[i];
+        ci.cells[i].ctype = ctype[i];
+        ci.cells[i].phase = phase ? phase[i] : 1;
+        ci.cells[i].gid = (int)i;
+    }
+    for (i = 0; i < n; i++) removecell[i] = 0;
+    *removecount = 0;
+
+    if (do_cic) {
+        allocategrid(si, st, &grid);
+        env = (environment_t *)calloc(1, sizeof(environment_t));
+        env[0].production = (double *)calloc((size_t)(grid.localsize.x * grid.localsize.y * grid.localsize.z),
+                                             sizeof(double));
+        grid_dims[0] = grid.localsize.x;
+        grid_dims[1] = grid.localsize.y;
+        grid_dims[2] = grid.localsize.z;
+    }
+
+    for (s = 0; s < nsteps; s++) {
+        patches_t patches;
+        double t0 = wall();
+        octbuild(si, &ci, ct);
+        double t1 = wall();
+        if (do_cic) {
+            patches_alloc(si, st, &patches, &ci, &grid);
+            patches_cells2envinit(si, st, &patches, &ci, &grid);
+        }
+        double t2 = wall();
+        computepotential(si, &ci, ct, cc);
+        double t3 = wall();
+        if (do_cic) {
+            patches_cells2envwait(si, st, &patches, &grid, &env);
+            patches_free(&patches);
+        }
+        double t4 = wall();
+        computegradient(si, &ci, ct, cc);
+        double t5 = wall();
+        if (update_mode == 0) {
+            updatepositions(st, ct, &ci, removecell, removecount);
+        } else if (update_mode == 1) {
+            for (i = 0; i < n; i++) {
+                celldata_t *c = &ci.cells[i];
+                c->x += dt * ci.forces[i].x;
+                c->y += dt * ci.forces[i].y;
+                if (dim == 3) c->z += dt * ci.forces[i].z;
+                if ((c->x - c->size <= -BOXSIZEX / 2.0 || c->x + c->size >= BOXSIZEX / 2.0 ||
+                     c->y - c->size <= -BOXSIZEY / 2.0 || c->y + c->size >= BOXSIZEY / 2.0 ||
+                     (dim == 3 && (c->z - c->size <= -BOXSIZEZ / 2.0 || c->z + c->size >= BOXSIZEZ / 2.0))) &&
+                    removecell[i] == 0) {
+                    removecell[i] = 1;
+                    (*removecount)++;
+                }
+            }
+        }
+        double t6 = wall();
+        if (octsize) *octsize = ci.octsize;
+        octfree(&ci);
+        if (timing) {
+            timing[0] += t1 - t0;
+            timing[1] += t3 - t2;
+            timing[2] += t5 - t4;
+            timing[3] += t6 - t5;
+            timing[4] += (t2 - t1) + (t4 - t3);
+        }
+    }
+
+    for (i = 0; i < n; i++) {
+        x[i] = ci.cells[i].x;
+        y[i] = ci.cells[i].y;
+        z[i] = ci.cells[i].z;
+        if (density) density[i] = ci.cells[i].density;
+        if (v) v[i] = ci.cells[i].v;
+        if (mindist) mindist[i] = ci.cells[i].mindist;
+        if (fx) fx[i] = ci.forces[i].x;
+        if (fy) fy[i] = ci.forces[i].y;
+        if (fz) fz[i] = ci.forces[i].z;
+    }
+    if (aff) {
+        aff[0] = affShift.x;
+        aff[1] = affShift.y;
+        aff[2] = affShift.z;
+        aff[3] = affScale;
+    }
+    if (do_cic) {
+        int64_t g = grid.localsize.x * grid.localsize.y * grid.localsize.z;
+        if (grid_out && grid_cap >= g) memcpy(grid_out, env[0].production, (size_t)g * sizeof(double));
+        free(env[0].production);
+        free(env);
+        free(grid.loweridx);
+        free(grid.upperidx);
+        free(grid.lowleftnear);
+        free(grid.uprightfar);
+    }
+    free(ci.cells);
+    free(ci.forces);
+    free(ct);
+    free(si.coords[0]);
+    free(si.coords);
+    return 0;
+}

@@ -1,0 +1,1 @@
+/* Empty stand-in: the hot-path sources use no Hypre declarations. */

@@ -1,0 +1,86 @@
+/* Single-rank MPI calls for the oracle build of the reference sources.
+ * A send to self is held until the matching receive is posted (or the
+ * reverse), which is all that the reference's patch exchange does at
+ * world size 1 (patches.c:242-315). */
+#include <stdio.h>
+#include <string.h>
+#include "mpi.h"
+
+static size_t type_bytes(MPI_Datatype t)
+{
+    switch (t) {
+    case MPI_INT: return sizeof(int);
+    case MPI_BYTE: case MPI_CHAR: return 1;
+    case MPI_DOUBLE: return sizeof(double);
+    case MPI_DOUBLE_INT: return sizeof(double) + sizeof(int) + 4;
+    case MPI_UINT64_T: case MPI_LONG_LONG: return 8;
+    default: return 1;
+    }
+}
+
+int MPI_Allreduce(const void *s, void *r, int n, MPI_Datatype t, MPI_Op op, MPI_Comm c)
+{
+    (void)op; (void)c;
+    if (s != MPI_IN_PLACE) memmove(r, s, (size_t)n * type_bytes(t));
+    return MPI_SUCCESS;
+}
+
+int MPI_Alltoall(const void *s, int sn, MPI_Datatype st, void *r, int rn, MPI_Datatype rt, MPI_Comm c)
+{
+    (void)rn; (void)rt; (void)c;
+    memmove(r, s, (size_t)sn * type_bytes(st));
+    return MPI_SUCCESS;
+}
+
+int MPI_Allgather(const void *s, int sn, MPI_Datatype st, void *r, int rn, MPI_Datatype rt, MPI_Comm c)
+{
+    return MPI_Alltoall(s, sn, st, r, rn, rt, c);
+}
+
+/* one pending message in each direction is enough for the reference's usage */
+static const void *pend_send; static size_t pend_send_n;
+static void *pend_recv; static size_t pend_recv_n;
+
+int MPI_Isend(const void *b, int n, MPI_Datatype t, int dst, int tag, MPI_Comm c, MPI_Request *q)
+{
+    (void)dst; (void)tag; (void)c;
+    size_t bytes = (size_t)n * type_bytes(t);
+    if (pend_recv) {
+        memcpy(pend_recv, b, bytes < pend_recv_n ? bytes : pend_recv_n);
+        pend_recv = NULL;
+    } else {
+        pend_send = b; pend_send_n = bytes;
+    }
+    if (q) *q = 0;
+    return MPI_SUCCESS;
+}
+
+int MPI_Irecv(void *b, int n, MPI_Datatype t, int src, int tag, MPI_Comm c, MPI_Request *q)
+{
+    (void)src; (void)tag; (void)c;
+    size_t bytes = (size_t)n * type_bytes(t);
+    if (pend_send) {
+        memcpy(b, pend_send, bytes < pend_send_n ? bytes : pend_send_n);
+        pend_send = NULL;
+    } else {
+        pend_recv = b; pend_recv_n = bytes;
+    }
+    if (q) *q = 0;
+    return MPI_SUCCESS;
+}
+
+int MPI_Wait(MPI_Request *q, MPI_Status *st) { (void)q; (void)st; return MPI_SUCCESS; }
+
+int MPI_Abort(MPI_Comm c, int code)
+{
+    (void)c;
+    fprintf(stderr, "MPI_Abort(%d) called by the reference oracle\n", code);
+    exit(code);
+}
+
+int MPI_Get_processor_name(char *name, int *len)
+{
+    strcpy(name, "oracle");
+    *len = 6;
+    return MPI_SUCCESS;
+}

@@ -1,0 +1,74 @@
+/* CPU oracle for the Timothy cell-mechanics hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference
+ * algorithm (pointer octree built by insertion, per-cell depth-first walk,
+ * FP64 pair maths in the reference's operation order, x += F update, CIC
+ * deposit).  Only tests/, __graft_entry__.smoke() and bench.py's CPU legs may
+ * load it, and only as the checker or the timed CPU baseline; the GPU product
+ * never calls it.
+ *
+ * Parity pin: tests/golden/ holds outputs of the reference's own functions
+ * (compiled unmodified from its sources by oracle/Makefile into oracle/_ref),
+ * and tests/test_oracle_golden.py checks this restatement against them.
+ */
+#ifndef TM_ORACLE_H
+#define TM_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Runs nsteps steps of the hot path on structure-of-arrays cells.
+ *
+ * Arguments mirror ref_run() in oracle/ref_driver.c so that tests can call
+ * the reference and the restatement interchangeably:
+ *   th..tsize, trandommove  per-type h, h2, h3, h4, size, randommove (the
+ *                           celltype_t fields, global.h:315-335)
+ *   update_mode             0 reference updatepositions (cells.c:342-365),
+ *                           1 x += dt*F with the same removal rule, 2 none
+ *   density..fz             outputs of the last step (before its update)
+ *   octsize, aff            node count of the last octree, affShift/affScale
+ *   do_cic, gfh, grid_out   CIC deposit of the last step into the one-rank
+ *                           grid (grid.c:37-136), x-major with z fastest
+ *   timing[5]               seconds spent in build, potential, gradient,
+ *                           update, CIC (accumulated)
+ *   nthreads                OpenMP threads (<= 0: runtime default)
+ * Returns 0, or a negative code: -1 bad arguments, -2 two cells share a
+ * lattice code down to the last two levels (the reference's insertion is
+ * undefined there, octree.c:101-107), -3 out of memory.
+ */
+int tmo_run(int64_t n, int dim, int ntypes,
+            const double *th, const double *th2, const double *th3, const double *th4,
+            const double *tsize, const float *trandommove,
+            double *x, double *y, double *z, const double *size, const float *young,
+            const int *ctype, const int *phase,
+            int nsteps, int update_mode, double dt,
+            double *density, double *v, double *mindist,
+            double *fx, double *fy, double *fz,
+            unsigned char *removecell, int64_t *removecount,
+            int64_t *octsize, double *aff,
+            int do_cic, float gfh, double *grid_out, int64_t grid_cap, int64_t *grid_dims,
+            double *timing, int nthreads);
+
+/* One octree build plus one walk per cell, returning per-cell diagnostics:
+ * nbcount/nbhash  size and order-free fingerprint (sum of tm_mix64(j+1)) of
+ *                 the set {j != p : candidate, dist(p,j) <= h_p}
+ * vcand           the candidate whose potential the reference assigns to v
+ *                 (the last one visited, potential.c:118-125), or -1
+ * ncand           number of candidates visited (leaves intersecting the box)
+ * If nb_offsets/nb_list are non-NULL the neighbour lists are written in
+ * visiting order (CSR; nb_list must hold nb_offsets[n] entries, which a
+ * first call with nb_list == NULL returns). */
+int tmo_neighbours(int64_t n, int dim, int ntypes, const double *th,
+                   const double *x, const double *y, const double *z, const int *ctype,
+                   int32_t *nbcount, uint64_t *nbhash, int64_t *vcand, int32_t *ncand,
+                   int64_t *nb_offsets, int64_t *nb_list, int nthreads);
+
+/* The fingerprint mixer shared with the GPU diagnostics (SplitMix64 final mix). */
+uint64_t tm_mix64(uint64_t z);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

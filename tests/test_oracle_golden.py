@@ -1,0 +1,68 @@
+"""Pin the CPU oracle to the reference's own outputs (tests/golden/*.npz).
+
+The fixtures hold outputs of the reference's unmodified functions; the oracle
+restatement must reproduce the strict build bit for bit and stay within the
+reference's own fast-math spread of the shipped build.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from timothy_gb300 import colonies as C
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+CASES = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+
+
+def load_case(name):
+    d = np.load(os.path.join(GOLDEN, name + ".npz"))
+    t = C.CellTypes(d["th"], d["th2"], d["th3"], d["th4"], d["tsize"], d["trandommove"])
+    col = C.Colony(d["x"], d["y"], d["z"], d["size"], d["young"], d["ctype"], d["phase"], t, int(d["dim"]))
+    return d, col
+
+
+def golden_grid(d, tag):
+    shape = tuple(int(s) for s in d[f"{tag}_grid_shape"])
+    g = np.zeros(shape)
+    idx = d[f"{tag}_grid_idx"]
+    if len(idx):
+        g[idx[:, 0], idx[:, 1], idx[:, 2]] = d[f"{tag}_grid_val"]
+    return g
+
+
+def test_cases_present():
+    assert len(CASES) >= 10
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_matches_reference_strict_bitwise(oracle_lib, name):
+    d, col = load_case(name)
+    r = oracle_lib.run(col, int(d["steps"]), which="oracle", update_mode=int(d["update_mode"]),
+                       dt=float(d["dt"]), cic=bool(d["cic"]), gfh=float(d["gfh"]))
+    for k in ("x", "y", "z", "density", "v", "mindist", "fx", "fy", "fz", "removecell"):
+        assert np.array_equal(getattr(r, k), d[f"strict_{k}"]), k
+    if col.n > 0:
+        assert r.octsize == int(d["strict_octsize"])
+        assert np.array_equal(r.aff, d["strict_aff"])
+    assert r.removecount == int(d["strict_removecount"])
+    if int(d["cic"]):
+        assert np.array_equal(r.grid, golden_grid(d, "strict"))
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_within_fast_math_spread(oracle_lib, name):
+    """The shipped build uses -ffast-math; its outputs differ only in rounding."""
+    d, col = load_case(name)
+    r = oracle_lib.run(col, int(d["steps"]), which="oracle", update_mode=int(d["update_mode"]),
+                       dt=float(d["dt"]), cic=bool(d["cic"]), gfh=float(d["gfh"]))
+    if col.n == 0:
+        return
+    fmax = max(np.max(np.abs(d["fast_fx"])), np.max(np.abs(d["fast_fy"])), np.max(np.abs(d["fast_fz"])), 1e-300)
+    for k in ("fx", "fy", "fz"):
+        assert np.max(np.abs(getattr(r, k) - d[f"fast_{k}"])) <= 1e-9 * fmax, k
+    for k in ("density", "mindist", "x", "y", "z"):
+        ref = d[f"fast_{k}"]
+        rel = np.abs(getattr(r, k) - ref) / np.maximum(np.abs(ref), 1e-300)
+        assert np.max(rel, initial=0.0) <= 1e-9, k
