@@ -1,0 +1,146 @@
+/* timothy_gb300 -- GB300-native cell-mechanics hot path of Timothy.
+ *
+ * Two C interfaces, both exported by libtimothy_gb300.so:
+ *
+ *  1. The device-resident session API (tm_*): colonies live in HBM across
+ *     steps; one call advances every active colony.  This is what batching,
+ *     serving and the benchmarks use.
+ *
+ *  2. The reference-signature drop-ins (octbuild, computepotential, ...):
+ *     declared in timothy_refabi.h with the exact signatures of the reference
+ *     functions they replace, so the reference step loop links against them
+ *     unchanged.
+ *
+ * Errors: every tm_* function returns TM_OK (0) or a negative TM_E* code;
+ * tm_last_error() describes the most recent failure of the calling thread.
+ * No function falls back to a CPU implementation: without a usable CUDA
+ * device the session cannot be created.
+ */
+#ifndef TIMOTHY_GB300_H
+#define TIMOTHY_GB300_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TM_OK 0
+#define TM_EINVAL (-1)    /* bad argument */
+#define TM_ENOMEM (-2)    /* device or host allocation failed, or no room */
+#define TM_ECUDA (-3)     /* CUDA runtime error */
+#define TM_EDEVICE (-4)   /* a kernel flagged an input it cannot handle */
+#define TM_ENODEV (-5)    /* no CUDA device */
+#define TM_ENOENT (-6)    /* unknown colony id */
+
+/* device-side error bits reported by tm_colony_stats / TM_EDEVICE */
+#define TM_DEVERR_BIGBIN 1u   /* > 2048 cells in one Morton bin */
+#define TM_DEVERR_STACK 2u    /* octree walk deeper than its stack */
+#define TM_DEVERR_CODES 4u    /* two cells share a lattice code (coincident cells) */
+
+#define TM_PREC_FP64 0        /* plain FP64, the reference's arithmetic */
+#define TM_PREC_FP32C 1       /* FP32 pair maths, Kahan sums, FP64 cutoff band + FP64 positions */
+
+#define TM_UPDATE_REFERENCE 0 /* x += F (+ random move), cells.c:342-365 */
+#define TM_UPDATE_DT 1        /* x += dt * F */
+#define TM_UPDATE_NONE 2
+
+typedef struct tm_session tm_session;
+
+/* Per-type constants (the celltype_t fields the path reads, global.h:315-335).
+ * h2/h3/h4 are used as given, never derived from h. */
+typedef struct {
+    int ntypes;               /* 1..8 */
+    const double *h, *h2, *h3, *h4, *size;
+    const float *randommove;  /* may be NULL: no random move */
+} tm_celltypes;
+
+typedef struct {
+    int dimension;            /* 2 or 3 */
+    int device;               /* CUDA device ordinal */
+    int64_t max_slots;        /* total cells over all colonies (padded to 32 per colony) */
+    int max_colonies;
+    int64_t max_bin_entries;  /* 0: derived from max_slots */
+    int64_t max_grid_entries; /* 0: one 257^3 grid */
+    int diagnostics;          /* fill neighbour counts/fingerprints and v candidates */
+} tm_session_config;
+
+/* One colony's cells in caller order (host memory). */
+typedef struct {
+    int64_t n;
+    const double *x, *y, *z, *size;
+    const float *young;
+    const int *ctype;
+    const int *phase;         /* may be NULL (all 1) */
+} tm_colony_input;
+
+typedef struct {
+    int precision;            /* TM_PREC_* */
+    int update_mode;          /* TM_UPDATE_* */
+    double dt;                /* TM_UPDATE_DT only */
+    int cic;                  /* deposit onto a grid each step */
+    float gfh;                /* grid resolution (settings.gfh) */
+    int lcap;                 /* deepest bin level, 0: from the colony's extent */
+} tm_colony_options;
+
+/* Outputs in caller order (host memory); any pointer may be NULL. */
+typedef struct {
+    double *x, *y, *z;
+    double *density, *v, *mindist;
+    double *fx, *fy, *fz;
+    unsigned char *removecell;
+    int32_t *nbcount;         /* diagnostics: neighbours within h */
+    uint64_t *nbhash;         /* diagnostics: sum of mix64(j+1) over them */
+    int32_t *vcand;           /* diagnostics: caller index of v's candidate or -1 */
+    double *grid;             /* CIC grid, x-major with z fastest */
+} tm_colony_output;
+
+typedef struct {
+    double aff_shift[3], aff_scale;   /* affShift / affScale of the last step */
+    int64_t octsize;                  /* node count of the reference octree */
+    int64_t removecount;              /* cells newly marked for removal */
+    int64_t patch_lower[3], patch_upper[3];   /* CIC patch corners (patches.c:61-132) */
+    int64_t grid_size[3];
+    uint32_t device_errors;           /* TM_DEVERR_* */
+    int bin_level;
+    int64_t n;
+} tm_colony_info;
+
+const char *tm_last_error(void);
+const char *tm_version(void);
+int tm_device_count(void);
+
+int tm_session_create(tm_session **out, const tm_session_config *cfg, const tm_celltypes *types);
+int tm_session_destroy(tm_session *s);
+/* cudaStream_t the session launches on */
+void *tm_session_stream(tm_session *s);
+
+/* Add a colony; its id is written to *id.  Uploads the cells. */
+int tm_colony_add(tm_session *s, const tm_colony_input *in, const tm_colony_options *opt, int *id);
+int tm_colony_remove(tm_session *s, int id);
+/* Replace the cells of an existing colony (same n or fewer). */
+int tm_colony_upload(tm_session *s, int id, const tm_colony_input *in);
+int tm_colony_set_active(tm_session *s, int id, int active);
+int tm_colony_download(tm_session *s, int id, const tm_colony_output *out);
+int tm_colony_stats(tm_session *s, int id, tm_colony_info *st);
+
+/* Enqueue nsteps steps of every active colony on the session stream.
+ * Returns without waiting; tm_session_sync waits and reports device errors. */
+int tm_session_step(tm_session *s, int nsteps);
+int tm_session_sync(tm_session *s);
+
+/* Capture one step into a CUDA graph and replay it from then on (0: off). */
+int tm_session_use_graph(tm_session *s, int on);
+
+/* Per-phase timing with CUDA events on the session stream: phase 0 build,
+ * 1 pair kernel, 2 octree kernel, 3 update, 4 CIC.  ms[k] = mean per step
+ * since profiling was switched on. */
+int tm_session_profile(tm_session *s, int on);
+int tm_session_profile_read(tm_session *s, double *ms, int nphase, int64_t *steps);
+
+/* Slots and memory still free (admission control). */
+int tm_session_capacity(tm_session *s, int64_t *free_slots, int64_t *free_bins, int *free_colonies);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -29,7 +29,7 @@ _cache: dict[str, C.CDLL] = {}
 
 def build(ref: bool | None = None) -> None:
     """Compile the restatement; also the reference library when its sources exist."""
-    subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+    subprocess.run(["make", "-s", "-B", "-C", HERE, "liboracle.so"], check=True)
     refsrc = os.environ.get("TM_REFSRC", "/root/reference/src")
     if ref is None:
         ref = os.path.isdir(refsrc)

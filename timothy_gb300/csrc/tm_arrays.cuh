@@ -1,0 +1,67 @@
+// Packed multi-colony state shared by all kernels.
+//
+// Colony c owns the slot range [desc[c].off, desc[c].off + desc[c].nslots),
+// nslots = n rounded up to a multiple of 32, so a warp never straddles two
+// colonies; slots past n are padding that every kernel skips.  Its bins live
+// at [desc[c].binoff, desc[c].binoff + 8^Lcap + 1) of the shared bin table.
+// One exclusive scan runs over the whole table; a colony turns the scanned
+// value of its bin b into a slot as frame.bin_base + bin_start[b], so slot
+// ranges and bin ranges can be allocated independently.
+#pragma once
+#include "tm_core.cuh"
+
+struct tm_desc {
+    long long off;       // first slot
+    long long binoff;    // first bin-table entry
+    long long gridoff;   // first CIC grid entry (-1: no deposit)
+    int n;               // live cells
+    int nslots;          // padded slot count
+    int Lcap;            // deepest bin level this colony's table holds
+    int precision;       // 0 plain FP64, 1 FP32 + compensated
+    int update_mode;     // 0 reference x += F (+ random move), 1 x += dt*F, 2 none
+    int active;          // 0: skipped by every kernel
+    double dt;
+    // CIC grid geometry (grid.c:37-136 at one rank)
+    double glower[3];
+    float gres;
+    int gsize[3];
+};
+
+struct tm_arrays {
+    // state, current order (double-buffered by the host)
+    double *x, *y, *z, *size;
+    float *young;
+    int *ctype, *phase, *perm;
+    unsigned char *rem;  // removal marks (cells.c:80-83)
+    // state, the other buffer (gather target)
+    double *x2, *y2, *z2, *size2;
+    float *young2;
+    int *ctype2, *phase2, *perm2;
+    unsigned char *rem2;
+    // per slot, constant after upload
+    int *col;
+    // build scratch
+    uint4 *code;         // lattice codes in the pre-sort order
+    uint4 *codes;        // lattice codes in Morton order
+    uint32_t *bin;       // global bin-table index of each pre-sort slot
+    int *tmp;            // new slot -> old slot
+    float4 *hi, *lo;     // FP32 split positions (hi.w = size)
+    double *mass;        // FP64 density weights sc_t * (size / csize_t), [type][slot]
+    // bin table
+    uint32_t *bin_count, *bin_cursor, *bin_start;
+    long long nbin_total;
+    int *bigbins;
+    // outputs (Morton order)
+    double *density, *v, *mindist, *fx, *fy, *fz;
+    int *nbcount;
+    unsigned long long *nbhash;
+    int *vcand;
+    // CIC grids
+    double *grid;
+    // frames / descriptors
+    tm_desc *desc;
+    tm_frame *frame;
+    int ncol;
+    long long nslots_total;
+    int want_diag;       // fill nbcount/nbhash/vcand
+};

@@ -1,0 +1,344 @@
+// Build phase of one step: bounding box and affine map, lattice codes, Morton
+// bins, counting sort into Morton order, gather of the cell state.
+//
+// Replaces octbuild (octree.c:145-207).  The reference inserts cells one by one
+// into a pointer octree; here the same octree is implicit in the Morton order
+// of the same lattice codes: a node is a contiguous run of sorted cells that
+// share a prefix, and a cell's leaf is the largest node holding only it.
+#include "tm_arrays.cuh"
+#include "tm_kernels.cuh"
+
+#define FULL 0xffffffffu
+
+// ---------------------------------------------------------------------------
+// per-step reset of the frames and the bin table's padding entries
+
+__global__ void k_step_init(tm_arrays a)
+{
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= a.ncol) return;
+    tm_frame &f = a.frame[c];
+    for (int t = 0; t < TM_MAX_TYPES; t++) {
+        for (int k = 0; k < 3; k++) {
+            f.bbox[t][k] = 0xffffffffffffffffull;
+            f.bbox[t][3 + k] = 0ull;
+        }
+    }
+    f.error = 0;
+    f.nbig = 0;
+    f.boundary_pairs = 0;
+    for (int k = 0; k < 3; k++) {
+        f.patch_lo[k] = 2147483647ll;
+        f.patch_hi[k] = -2147483648ll;
+    }
+    f.step_counter++;
+}
+
+// slot of the colony's first bin (after the scan)
+__global__ void k_binbase(tm_arrays a)
+{
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= a.ncol) return;
+    const tm_desc &d = a.desc[c];
+    a.frame[c].bin_base = d.off - (long long)a.bin_start[d.binoff];
+}
+
+// ---------------------------------------------------------------------------
+// bounding box with the per-type pad h + 0.01 (octree.c:155-174).
+// min over cells of fl(x - e) equals fl(min x - e) because rounding is
+// monotone, so per-type minima/maxima of x suffice; they are reduced on the
+// order-preserving integer image of the doubles (no FP64 instructions).
+
+__global__ void k_bbox(tm_arrays a, int ntypes)
+{
+    long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    bool live = false;
+    int c = 0;
+    if (s < a.nslots_total) {
+        c = a.col[s];
+        const tm_desc &d = a.desc[c];
+        live = d.active && (s - d.off) < d.n;
+    }
+    unsigned long long v[6];
+    int t = -1;
+    if (live) {
+        t = a.ctype[s];
+        v[0] = tm_ordered(a.x[s]);
+        v[1] = tm_ordered(a.y[s]);
+        v[2] = tm_ordered(a.z[s]);
+        v[3] = v[0];
+        v[4] = v[1];
+        v[5] = v[2];
+    }
+    // a warp never straddles two colonies (32-aligned slot ranges)
+    for (int tt = 0; tt < ntypes; tt++) {
+        bool mine = live && t == tt;
+        unsigned any = __ballot_sync(FULL, mine);
+        if (!any) continue;
+        unsigned long long r[6];
+        for (int k = 0; k < 3; k++) {
+            r[k] = mine ? v[k] : 0xffffffffffffffffull;
+            r[3 + k] = mine ? v[3 + k] : 0ull;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            for (int k = 0; k < 3; k++) {
+                unsigned long long q = __shfl_xor_sync(FULL, r[k], o);
+                r[k] = q < r[k] ? q : r[k];
+                unsigned long long w = __shfl_xor_sync(FULL, r[3 + k], o);
+                r[3 + k] = w > r[3 + k] ? w : r[3 + k];
+            }
+        }
+        int leader = __ffs(any) - 1;
+        if ((threadIdx.x & 31) == leader) {
+            tm_frame &f = a.frame[c];
+            for (int k = 0; k < 3; k++) {
+                atomicMin(&f.bbox[tt][k], r[k]);
+                atomicMax(&f.bbox[tt][3 + k], r[3 + k]);
+            }
+        }
+    }
+}
+
+// affShift / affScale (octree.c:175-180) and the bin depth of each colony
+__global__ void k_frame(tm_arrays a, const tm_consts *K)
+{
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= a.ncol) return;
+    tm_frame &f = a.frame[c];
+    const tm_desc &d = a.desc[c];
+    f.n = d.n;
+    if (!d.active || d.n == 0) return;   // octbuild returns early: the previous map stays
+    double bmin[3] = {1.7976931348623157e308, 1.7976931348623157e308, 1.7976931348623157e308};
+    double bmax[3] = {-1.7976931348623157e308, -1.7976931348623157e308, -1.7976931348623157e308};
+    double hmax = 0.0;
+    for (int t = 0; t < K->ntypes; t++) {
+        if (f.bbox[t][3] == 0ull) continue;   // no cell of this type
+        double e = K->t[t].e;
+        hmax = K->t[t].h > hmax ? K->t[t].h : hmax;
+        for (int k = 0; k < 3; k++) {
+            double lo = sub64(tm_unordered(f.bbox[t][k]), e);
+            double hi = add64(tm_unordered(f.bbox[t][3 + k]), e);
+            bmin[k] = lo < bmin[k] ? lo : bmin[k];
+            bmax[k] = hi > bmax[k] ? hi : bmax[k];
+        }
+    }
+    double sc = sub64(bmax[0], bmin[0]);
+    sc = (sc > sub64(bmax[1], bmin[1]) ? sc : sub64(bmax[1], bmin[1]));
+    sc = (sc > sub64(bmax[2], bmin[2]) ? sc : sub64(bmax[2], bmin[2]));
+    f.scale = sc;
+    for (int k = 0; k < 3; k++) {
+        f.shift[k] = bmin[k];
+        f.shiftf[k] = (float)bmin[k];
+    }
+    // deepest level whose bins are at least h/2 wide
+    int L = 1;
+    while (L < d.Lcap && sc / (double)(1 << (L + 1)) >= 0.5 * hmax) L++;
+    f.L = L;
+    f.nbins = 1u << (3 * L);
+    f.binscale = (float)((double)(1 << L) / sc);
+}
+
+// exact lattice codes (octree.c:187-191) and bin occupancy
+__global__ void k_codes(tm_arrays a)
+{
+    long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= a.nslots_total) return;
+    int c = a.col[s];
+    const tm_desc &d = a.desc[c];
+    if (!d.active || (s - d.off) >= d.n) return;
+    const tm_frame &f = a.frame[c];
+    uint4 q;
+    q.x = tm_lattice(a.x[s], f.shift[0], f.scale);
+    q.y = tm_lattice(a.y[s], f.shift[1], f.scale);
+    q.z = tm_lattice(a.z[s], f.shift[2], f.scale);
+    q.w = 0;
+    a.code[s] = q;
+    uint32_t b = (uint32_t)(d.binoff) + tm_prefix(q, f.L);
+    a.bin[s] = b;
+    // one atomic per distinct bin in the warp
+    unsigned peers = __match_any_sync(__activemask(), b);
+    int leader = __ffs(peers) - 1;
+    if ((int)(threadIdx.x & 31) == leader) atomicAdd(&a.bin_count[b], (uint32_t)__popc(peers));
+}
+
+__global__ void k_scatter(tm_arrays a)
+{
+    long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= a.nslots_total) return;
+    int c = a.col[s];
+    const tm_desc &d = a.desc[c];
+    if (!d.active || (s - d.off) >= d.n) return;
+    uint32_t b = a.bin[s];
+    long long pos = a.frame[c].bin_base + a.bin_start[b] + atomicAdd(&a.bin_cursor[b], 1u);
+    a.tmp[pos] = (int)s;
+}
+
+// sort each bin's slots by full Morton order; bins of up to 32 cells by one
+// thread, larger ones are queued for k_binsort_big
+__global__ void k_binsort_small(tm_arrays a)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.nslots_total) return;
+    int c = a.col[i];
+    const tm_desc &d = a.desc[c];
+    if (!d.active || (i - d.off) >= d.n) return;
+    int r = a.tmp[i];
+    uint32_t b = a.bin[r];
+    long long st = a.frame[c].bin_base + a.bin_start[b];
+    if (st != i) return;                    // not the first slot of its bin
+    uint32_t cnt = a.bin_start[b + 1] - a.bin_start[b];
+    if (cnt <= 1) return;
+    if (cnt > 32) {
+        atomicAdd(&a.frame[c].nbig, 1);
+        int q = atomicAdd(&a.bigbins[0], 1);
+        a.bigbins[1 + 2 * q] = (int)b;
+        a.bigbins[2 + 2 * q] = c;
+        return;
+    }
+    int idx[32];
+    uint4 key[32];
+    for (uint32_t k = 0; k < cnt; k++) {
+        idx[k] = a.tmp[st + k];
+        key[k] = a.code[idx[k]];
+    }
+    for (uint32_t k = 1; k < cnt; k++) {
+        uint4 kk = key[k];
+        int ii = idx[k];
+        int m = (int)k - 1;
+        while (m >= 0 && tm_morton_less(kk, key[m])) {
+            key[m + 1] = key[m];
+            idx[m + 1] = idx[m];
+            m--;
+        }
+        key[m + 1] = kk;
+        idx[m + 1] = ii;
+    }
+    for (uint32_t k = 0; k < cnt; k++) {
+        if (k > 0 && tm_code_eq(key[k], key[k - 1])) atomicOr(&a.frame[c].error, TM_ERR_CODES);
+        a.tmp[st + k] = idx[k];
+    }
+}
+
+// one block per large bin: bitonic sort of up to TM_BIG_BIN cells in shared memory
+__global__ void k_binsort_big(tm_arrays a)
+{
+    __shared__ uint4 key[TM_BIG_BIN];
+    __shared__ int idx[TM_BIG_BIN];
+    int nbig = a.bigbins[0];
+    for (int q = blockIdx.x; q < nbig; q += gridDim.x) {
+        uint32_t b = (uint32_t)a.bigbins[1 + 2 * q];
+        int c = a.bigbins[2 + 2 * q];
+        long long st = a.frame[c].bin_base + a.bin_start[b];
+        uint32_t cnt = a.bin_start[b + 1] - a.bin_start[b];
+        if (cnt > TM_BIG_BIN) {
+            if (threadIdx.x == 0) atomicOr(&a.frame[c].error, TM_ERR_BIGBIN);
+            continue;
+        }
+        uint32_t p2 = 1;
+        while (p2 < cnt) p2 <<= 1;
+        for (uint32_t k = threadIdx.x; k < p2; k += blockDim.x) {
+            if (k < cnt) {
+                idx[k] = a.tmp[st + k];
+                key[k] = a.code[idx[k]];
+            } else {
+                idx[k] = -1;
+                key[k] = make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
+            }
+        }
+        __syncthreads();
+        for (uint32_t size = 2; size <= p2; size <<= 1) {
+            for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+                for (uint32_t k = threadIdx.x; k < p2; k += blockDim.x) {
+                    uint32_t m = k ^ stride;
+                    if (m > k) {
+                        bool up = (k & size) == 0;
+                        uint4 ka = key[k], kb = key[m];
+                        // padding keys (idx -1) sort last
+                        bool a_pad = idx[k] < 0, b_pad = idx[m] < 0;
+                        bool gt = a_pad ? !b_pad : (b_pad ? false : tm_morton_less(kb, ka));
+                        if (gt == up) {
+                            key[k] = kb;
+                            key[m] = ka;
+                            int t = idx[k];
+                            idx[k] = idx[m];
+                            idx[m] = t;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        for (uint32_t k = threadIdx.x; k < cnt; k += blockDim.x) {
+            a.tmp[st + k] = idx[k];
+            if (k > 0 && tm_code_eq(key[k], key[k - 1])) atomicOr(&a.frame[c].error, TM_ERR_CODES);
+        }
+        __syncthreads();
+    }
+}
+
+// move the state into Morton order; split positions for the FP32 path and
+// precompute the FP64 density weights sc_t * (size_j / csize_t) of
+// potential.c:62 for every query type t
+__global__ void k_gather(tm_arrays a, const tm_consts *K)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.nslots_total) return;
+    int c = a.col[i];
+    const tm_desc &d = a.desc[c];
+    if (!d.active || (i - d.off) >= d.n) return;
+    int r = a.tmp[i];
+    double x = a.x[r], y = a.y[r], z = a.z[r], sz = a.size[r];
+    a.x2[i] = x;
+    a.y2[i] = y;
+    a.z2[i] = z;
+    a.size2[i] = sz;
+    a.young2[i] = a.young[r];
+    a.ctype2[i] = a.ctype[r];
+    a.phase2[i] = a.phase[r];
+    a.perm2[i] = a.perm[r];
+    a.rem2[i] = a.rem[r];
+    a.codes[i] = a.code[r];
+    float hx, hy, hz, lx, ly, lz;
+    tm_split(x, hx, lx);
+    tm_split(y, hy, ly);
+    tm_split(z, hz, lz);
+    a.hi[i] = make_float4(hx, hy, hz, (float)sz);
+    a.lo[i] = make_float4(lx, ly, lz, 0.0f);
+    if (d.precision == 0) {
+        for (int t = 0; t < K->ntypes; t++)
+            a.mass[(long long)t * a.nslots_total + i] = mul64(K->t[t].sc, div64(sz, K->t[t].csize));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// node count of the reference octree, for cellsinfo->octsize:
+// 1 + sum_k (leafdepth_k - lcp(k-1, k)) over the Morton-sorted cells, where
+// leafdepth_k = 1 + max(lcp(k-1,k), lcp(k,k+1)) and lcp counts shared levels.
+
+__device__ inline int tm_lcp(uint4 a, uint4 b)
+{
+    uint32_t x = (a.x ^ b.x) | (a.y ^ b.y) | (a.z ^ b.z);
+    if (x == 0) return TM_ROOT_LEVEL;
+    return 28 - (31 - __clz(x));
+}
+
+__global__ void k_octsize(tm_arrays a, unsigned long long *out)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long term = 0;
+    int c = 0;
+    if (i < a.nslots_total) {
+        c = a.col[i];
+        const tm_desc &d = a.desc[c];
+        long long k = i - d.off;
+        if (d.active && k < d.n && d.n >= 2) {
+            uint4 me = a.codes[i];
+            int lp = k > 0 ? tm_lcp(a.codes[i - 1], me) : 0;
+            int ln = (k + 1 < d.n) ? tm_lcp(me, a.codes[i + 1]) : 0;
+            int leaf = 1 + (lp > ln ? lp : ln);
+            term = (unsigned long long)(leaf - lp);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) term += __shfl_xor_sync(FULL, term, o);
+    if ((threadIdx.x & 31) == 0 && term) atomicAdd(&out[c], term);
+}

@@ -1,0 +1,211 @@
+// Shared device-side definitions for the GB300 cell-mechanics path.
+//
+// Data layout in HBM (one colony; every array indexed by "slot", the cell's
+// position in the current Morton order unless stated otherwise):
+//   x, y, z, size          FP64 positions and radii (celldata_t, global.h:100-120)
+//   young                  FP32;  ctype, phase  int32;  perm  caller index
+//   hi[slot], lo[slot]     float4 split of (x, y, z): hi = x rounded to 24 bits,
+//                          lo = x - hi; hi.w = size as float
+//   code[slot]             uint4 (cx, cy, cz, 0) lattice codes of octree.c:187-191
+//   bin_start[b]           first slot of Morton bin b (depth-L octree node), b in
+//                          [0, 8^L]; bin_start[8^L] = n
+// Outputs (same slot order): density, v, mindist, fx, fy, fz, nbcount, nbhash.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#define TM_MAX_TYPES 8
+#define TM_ROOT_LEVEL 29          // global.h:65-66: codes are 29-bit
+#define TM_LMAX 8                 // deepest bin level: 8^8 bins
+#define TM_WARPS_PER_BLOCK 4
+#define TM_BIG_BIN 2048           // largest bin the in-bin sort handles
+
+// error bits written by kernels into tm_frame::error
+#define TM_ERR_BIGBIN 1u          // a bin held more than TM_BIG_BIN cells
+#define TM_ERR_STACK 2u           // octree walk deeper than its stack
+#define TM_ERR_CODES 4u           // two cells share a lattice code
+#define TM_ERR_LIST 8u            // pair list overflow (internal)
+
+// Per-type constants, computed on the host with the reference's expressions
+// (inline.h:45-46, 71-72; potential.c:60) so the FP64 values are bit-identical.
+struct tm_type {
+    double h, h2, h3, h4, csize;
+    double sc;       // density scale: h3 (3-D) or h2 (2-D)
+    double cW;       // sphkernel constant 8/(pi h3) or 40/(7 pi h2)
+    double cG;       // sphgradient constant 48/(pi h4) or 320/(7 pi h3)
+    double e;        // bounding-box pad h + 0.01 (octree.c:167)
+    float randommove;
+    // FP32 forms for the compensated path
+    float hf, h2f, inv_hf, cWf, cGf, kmassf;   // kmassf = sc / csize
+    float thr_lo, thr_hi;                      // squared-distance band around h^2
+};
+
+struct tm_consts {
+    int ntypes;
+    int dim;
+    tm_type t[TM_MAX_TYPES];
+};
+
+// Per-step frame, written on the device (no host round trip inside a step).
+struct tm_frame {
+    double shift[3];     // affShift (octree.c:178-180)
+    double scale;        // affScale (octree.c:175-177)
+    unsigned long long bbox[TM_MAX_TYPES][6];   // order-preserving min x,y,z / max x,y,z
+    int L;               // bin depth
+    uint32_t nbins;      // 8^L
+    float shiftf[3];     // FP32 copies for culling
+    float binscale;      // 2^L / scale
+    int n;               // cells in this colony
+    uint32_t error;      // TM_ERR_* bits
+    unsigned long long removecount;
+    unsigned long long boundary_pairs;   // within-h pairs outside the lattice box (diagnostic)
+    int nbig;            // bins needing the block sort
+    int pad_;
+    long long bin_base;      // slot of a bin = bin_base + bin_start[bin]
+    unsigned long long step_counter;
+    long long patch_lo[3];   // CIC patch corners (patches.c:61-132); INT_MAX/INT_MIN when empty
+    long long patch_hi[3];
+};
+
+// ---------------------------------------------------------------------------
+// small helpers
+
+__host__ __device__ inline unsigned long long tm_ordered(double d)
+{
+    unsigned long long b;
+#ifdef __CUDA_ARCH__
+    b = (unsigned long long)__double_as_longlong(d);
+#else
+    union { double d; unsigned long long u; } c; c.d = d; b = c.u;
+#endif
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+__host__ __device__ inline double tm_unordered(unsigned long long o)
+{
+    unsigned long long b = (o >> 63) ? (o & 0x7fffffffffffffffull) : ~o;
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double((long long)b);
+#else
+    union { double d; unsigned long long u; } c; c.u = b; return c.d;
+#endif
+}
+
+__host__ __device__ inline uint64_t tm_mix64(uint64_t z)
+{
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
+// spread the low 10 bits of v so that bit i lands at bit 3i
+__host__ __device__ inline uint32_t tm_spread3(uint32_t v)
+{
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000ffu;
+    v = (v | (v << 8)) & 0x0300f00fu;
+    v = (v | (v << 4)) & 0x030c30c3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+// Morton index of a node at depth d (d <= 10) from its per-axis prefixes;
+// the child digit is x + 2y + 4z (octree.c:105-107), so z is the most
+// significant bit of every level.
+__host__ __device__ inline uint32_t tm_morton(uint32_t px, uint32_t py, uint32_t pz)
+{
+    return tm_spread3(px) | (tm_spread3(py) << 1) | (tm_spread3(pz) << 2);
+}
+
+// Morton prefix of depth d (<= 10) of a cell's lattice codes
+__host__ __device__ inline uint32_t tm_prefix(uint4 c, int d)
+{
+    int s = TM_ROOT_LEVEL - d;
+    return tm_morton(c.x >> s, c.y >> s, c.z >> s);
+}
+
+// digit of a cell at depth d (1..29): the bits at position 29 - d
+__device__ inline int tm_digit(uint4 c, int d)
+{
+    int s = TM_ROOT_LEVEL - d;
+    return (int)(((c.x >> s) & 1u) | (((c.y >> s) & 1u) << 1) | (((c.z >> s) & 1u) << 2));
+}
+
+__device__ inline bool tm_less_msb(uint32_t a, uint32_t b) { return a < b && a < (a ^ b); }
+
+// true when code a precedes code b in Morton order (z, then y, then x at each level)
+__device__ inline bool tm_morton_less(uint4 a, uint4 b)
+{
+    uint32_t xz = a.z ^ b.z, xy = a.y ^ b.y, xx = a.x ^ b.x;
+    uint32_t best = xz;
+    int dim = 2;
+    if (tm_less_msb(best, xy)) { best = xy; dim = 1; }
+    if (tm_less_msb(best, xx)) { best = xx; dim = 0; }
+    if (dim == 2) return a.z < b.z;
+    if (dim == 1) return a.y < b.y;
+    return a.x < b.x;
+}
+
+__device__ inline bool tm_code_eq(uint4 a, uint4 b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
+
+// FP64 arithmetic without contraction, so every product and sum rounds
+// separately as in the reference's C expressions.
+__device__ __forceinline__ double mul64(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double add64(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub64(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double div64(double a, double b) { return __ddiv_rn(a, b); }
+
+// (unsigned int)(((x - shift) / scale) * 2^29), octree.c:188-190
+__device__ inline uint32_t tm_lattice(double x, double shift, double scale)
+{
+    double q = div64(sub64(x, shift), scale);
+    return (uint32_t)mul64(q, 536870912.0);
+}
+
+// query-box corners of octcomputebox, octree.c:251-263: ((x -/+ h) - shift) / scale
+__device__ inline uint32_t tm_lattice_off(double x, double off, double shift, double scale)
+{
+    double q = div64(sub64(add64(x, off), shift), scale);
+    return (uint32_t)mul64(q, 536870912.0);
+}
+
+// Split a double into hi (x truncated to 24 significant bits) + lo (float of
+// the remainder) with integer operations only, so no FP64 instruction runs.
+// |x| < 2^-70 flushes to zero; |x| must stay below 2^100.
+__device__ inline void tm_split(double x, float &hi, float &lo)
+{
+    unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    uint32_t sgn = (uint32_t)(b >> 32) & 0x80000000u;
+    int e = (int)((b >> 52) & 0x7ff);
+    if (e < 1023 - 70) { hi = 0.0f; lo = 0.0f; return; }
+    unsigned long long m = b & 0xfffffffffffffull;               // 52 fraction bits
+    uint32_t fb = sgn | ((uint32_t)(e - 1023 + 127) << 23) | (uint32_t)(m >> 29);
+    hi = __uint_as_float(fb);
+    uint32_t ml = (uint32_t)(m & ((1ull << 29) - 1));              // remainder = ml * 2^(e-1075)
+    float r = __uint2float_rn(ml);                                 // 24 of 29 bits kept
+    float p2 = __int_as_float((e - 1075 + 127) << 23);             // 2^(e-1075), normal for e >= 953
+    lo = __fmul_rn(r, p2);
+    if (sgn) lo = -lo;
+}
+
+// Knuth's TwoSum: s + err == a + b exactly
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &err)
+{
+    s = __fadd_rn(a, b);
+    float bb = __fsub_rn(s, a);
+    err = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// Kahan-compensated accumulation in FP32
+struct kahan {
+    float s, c;
+    __device__ void init() { s = 0.0f; c = 0.0f; }
+    __device__ __forceinline__ void add(float v)
+    {
+        float y = __fsub_rn(v, c);
+        float t = __fadd_rn(s, y);
+        c = __fsub_rn(__fsub_rn(t, s), y);
+        s = t;
+    }
+    __device__ __forceinline__ float value() const { return __fsub_rn(s, c); }
+};

@@ -1,0 +1,21 @@
+// Kernel entry points of the hot path (host-callable launchers).
+#pragma once
+#include "tm_arrays.cuh"
+
+__global__ void k_step_init(tm_arrays a);
+__global__ void k_bbox(tm_arrays a, int ntypes);
+__global__ void k_frame(tm_arrays a, const tm_consts *K);
+__global__ void k_codes(tm_arrays a);
+__global__ void k_binbase(tm_arrays a);
+__global__ void k_scatter(tm_arrays a);
+__global__ void k_binsort_small(tm_arrays a);
+__global__ void k_binsort_big(tm_arrays a);
+__global__ void k_gather(tm_arrays a, const tm_consts *K);
+__global__ void k_octsize(tm_arrays a, unsigned long long *out);
+
+cudaError_t tm_scan_exclusive(const uint32_t *in, uint32_t *out, long long n, uint32_t *tmp, cudaStream_t st);
+long long tm_scan_tmp_words(long long n);
+cudaError_t tm_launch_pair(const tm_arrays &a, const tm_consts *K, int prec, cudaStream_t st);
+cudaError_t tm_launch_octree(const tm_arrays &a, const tm_consts *K, cudaStream_t st);
+cudaError_t tm_launch_update(const tm_arrays &a, const tm_consts *K, cudaStream_t st);
+cudaError_t tm_launch_cic(const tm_arrays &a, const tm_consts *K, cudaStream_t st);

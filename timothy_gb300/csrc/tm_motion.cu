@@ -1,0 +1,149 @@
+// Position update (updatepositions + outsidethebox, cells.c:41-58, 342-365)
+// and the Cloud-In-Cell deposit of cells onto field 0 of the grid
+// (patches_alloc / patches_cells2envinfo / patches_applycells2env at one rank,
+// patches.c:47-234, 321-367; grid geometry grid.c:37-136).
+#include "tm_arrays.cuh"
+#include "tm_kernels.cuh"
+
+// uniform float in [0, 1] from a counter (stands in for (float)rand()/RAND_MAX)
+__device__ inline float tm_uniform(unsigned long long step, unsigned long long cell, int axis)
+{
+    unsigned long long z = tm_mix64(step * 0x9e3779b97f4a7c15ull ^ (cell * 3ull + (unsigned long long)axis));
+    return (float)(uint32_t)(z >> 40) * (1.0f / 16777215.0f);
+}
+
+__device__ inline bool tm_outside(double x, double y, double z, double r, int dim)
+{
+    // x - r <= -BOXSIZEX/2.0 || x + r >= BOXSIZEX/2.0 (global.h:59-61)
+    if (sub64(x, r) <= -1024.0 || add64(x, r) >= 1024.0) return true;
+    if (sub64(y, r) <= -1024.0 || add64(y, r) >= 1024.0) return true;
+    if (dim == 3 && (sub64(z, r) <= -1024.0 || add64(z, r) >= 1024.0)) return true;
+    return false;
+}
+
+__global__ void k_update(tm_arrays a, const tm_consts *K)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.nslots_total) return;
+    const int c = a.col[i];
+    const tm_desc &d = a.desc[c];
+    if (!d.active || (i - d.off) >= d.n || d.update_mode == 2) return;
+    const int dim = K->dim;
+    double x = a.x[i], y = a.y[i], z = a.z[i];
+    const double fx = a.fx[i], fy = a.fy[i], fz = a.fz[i];
+    if (d.update_mode == 0) {
+        x = add64(x, fx);
+        y = add64(y, fy);
+        if (dim == 3) z = add64(z, fz);
+        const float rm = K->t[a.ctype[i]].randommove;
+        if (rm != 0.0f) {
+            const unsigned long long id = (unsigned long long)a.perm[i];
+            x = add64(x, mul64((double)rm, sub64(mul64((double)tm_uniform(a.frame[c].step_counter, id, 0), 2.0), 1.0)));
+            y = add64(y, mul64((double)rm, sub64(mul64((double)tm_uniform(a.frame[c].step_counter, id, 1), 2.0), 1.0)));
+            if (dim == 3) z = add64(z, mul64((double)rm, sub64(mul64((double)tm_uniform(a.frame[c].step_counter, id, 2), 2.0), 1.0)));
+        }
+    } else {
+        x = add64(x, mul64(d.dt, fx));
+        y = add64(y, mul64(d.dt, fy));
+        if (dim == 3) z = add64(z, mul64(d.dt, fz));
+    }
+    a.x[i] = x;
+    a.y[i] = y;
+    a.z[i] = z;
+    if (tm_outside(x, y, z, a.size[i], dim) && a.rem[i] == 0) {
+        a.rem[i] = 1;
+        atomicAdd(&a.frame[c].removecount, 1ull);
+    }
+}
+
+// CIC weights onto field 0; the patch bounding box (patches.c:81-132) is
+// reduced alongside for the drop-in's patches_alloc.  Morton-ordered cells of
+// one warp mostly share grid nodes, so each distinct node of a corner gets a
+// warp-wide sum and one atomic.
+__global__ void k_cic(tm_arrays a, const tm_consts *K)
+{
+    const unsigned FULLM = 0xffffffffu;
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (((i >> 5) << 5) >= a.nslots_total) return;            // whole warp beyond the slots
+    const int c = a.col[(i >> 5) << 5];
+    const tm_desc &d = a.desc[c];
+    if (!d.active || d.gridoff < 0) return;                    // uniform per warp
+    const bool live = (i - d.off) < d.n;
+    const int dim = K->dim;
+    const int lane = threadIdx.x & 31;
+    long long ci[3] = {0, 0, 0};
+    double dd[3] = {0, 0, 0}, tt[3] = {0, 0, 0};
+    int ph = 5;
+    if (live) {
+        const double pos[3] = {a.x[i], a.y[i], a.z[i]};
+        const double res = (double)d.gres;
+        for (int k = 0; k < 3; k++) {
+            ci[k] = (long long)div64(sub64(pos[k], d.glower[k]), res);
+            // grid->lowercorner + cellIdx * resolution: an int64 * float product is a float
+            const double cic = add64(d.glower[k], (double)__fmul_rn((float)ci[k], d.gres));
+            dd[k] = div64(sub64(pos[k], cic), res);
+            tt[k] = sub64(1.0, dd[k]);
+        }
+        ph = a.phase[i];
+    }
+    const long long up[3] = {d.gsize[0] - 1, d.gsize[1] - 1, dim == 3 ? d.gsize[2] - 1 : 0};
+    const double wph = ph == 0 ? 0.75 : 1.0;
+    long long lo[3] = {0x7fffffffll, 0x7fffffffll, 0x7fffffffll}, hi[3] = {-0x7fffffffll - 1, -0x7fffffffll - 1, -0x7fffffffll - 1};
+    for (int corner = 0; corner < 8; corner++) {
+        const int ax = corner >> 2, ay = (corner >> 1) & 1, az = corner & 1;
+        const long long gx = ci[0] + ax, gy = ci[1] + ay, gz = ci[2] + az;
+        const bool inb = live && gx >= 0 && gy >= 0 && gz >= 0 && gx <= up[0] && gy <= up[1] && gz <= up[2];
+        if (inb) {
+            lo[0] = gx < lo[0] ? gx : lo[0];
+            lo[1] = gy < lo[1] ? gy : lo[1];
+            lo[2] = gz < lo[2] ? gz : lo[2];
+            hi[0] = gx > hi[0] ? gx : hi[0];
+            hi[1] = gy > hi[1] ? gy : hi[1];
+            hi[2] = gz > hi[2] ? gz : hi[2];
+        }
+        const bool dep = inb && ph != 5;                       // necrotic cells deposit nothing
+        const double w = dep ? mul64(mul64(mul64(wph, ax ? dd[0] : tt[0]), ay ? dd[1] : tt[1]), az ? dd[2] : tt[2]) : 0.0;
+        const long long gi = dep ? d.gridoff + ((long long)d.gsize[1] * gx + gy) * d.gsize[2] + gz : -1;
+        unsigned pending = __ballot_sync(FULLM, dep);
+        while (pending) {
+            const int ldr = __ffs(pending) - 1;
+            const long long key = __shfl_sync(FULLM, gi, ldr);
+            const bool mine = dep && gi == key;
+            double sum = mine ? w : 0.0;
+            for (int o = 16; o > 0; o >>= 1) sum = add64(sum, __shfl_xor_sync(FULLM, sum, o));
+            if (lane == ldr) atomicAdd(&a.grid[key], sum);
+            pending &= ~__ballot_sync(FULLM, mine);
+        }
+    }
+    for (int k = 0; k < 3; k++) {
+        for (int o = 16; o > 0; o >>= 1) {
+            const long long ql = __shfl_xor_sync(FULLM, lo[k], o), qh = __shfl_xor_sync(FULLM, hi[k], o);
+            lo[k] = ql < lo[k] ? ql : lo[k];
+            hi[k] = qh > hi[k] ? qh : hi[k];
+        }
+    }
+    if (lane == 0 && hi[0] >= lo[0]) {
+        tm_frame &f = a.frame[c];
+        const int nd = dim == 3 ? 3 : 2;
+        for (int k = 0; k < nd; k++) {
+            atomicMin(&f.patch_lo[k], lo[k]);
+            atomicMax(&f.patch_hi[k], hi[k]);
+        }
+    }
+}
+
+cudaError_t tm_launch_update(const tm_arrays &a, const tm_consts *K, cudaStream_t st)
+{
+    unsigned grid = (unsigned)((a.nslots_total + 255) / 256);
+    if (grid == 0) return cudaSuccess;
+    k_update<<<grid, 256, 0, st>>>(a, K);
+    return cudaGetLastError();
+}
+
+cudaError_t tm_launch_cic(const tm_arrays &a, const tm_consts *K, cudaStream_t st)
+{
+    unsigned grid = (unsigned)((a.nslots_total + 255) / 256);
+    if (grid == 0) return cudaSuccess;
+    k_cic<<<grid, 256, 0, st>>>(a, K);
+    return cudaGetLastError();
+}

@@ -1,0 +1,275 @@
+// Pair kernel: SPH density, nearest distance and SPH-gradient force of every
+// cell (computepotential potential.c:87-138 with potential() :39-78 and
+// sphkernel inline.h:40-51; computegradient potential.c:209-259 with
+// sphgradient inline.h:59-83), fused into one pass because the force does not
+// depend on the density.  v (the potential of the last walked candidate) is
+// produced by the octree kernel.
+//
+// Work decomposition: a warp owns 32 Morton-consecutive slots of one colony.
+//  1. stage: the Morton bins covering the union of the 32 query spheres are
+//     enumerated 32 at a time (one bin per lane), their cell runs are copied
+//     into a shared-memory tile as group-relative FP32 coordinates;
+//  2. test: every lane tests every tile entry against its own cell with a
+//     conservative FP32 squared-distance bound and appends hits to its own
+//     list in shared memory (no divergence: predicated append);
+//  3. drain: each lane walks its own list with the exact pair maths, so the
+//     expensive part runs with all lanes busy.
+// PREC 0 is the plain FP64 path: every reference expression is evaluated in
+// the same order with separate roundings (no contraction), the cutoff test is
+// fl(sqrt(.)) <= h and the kernel value is rounded to float (inline.h:40).
+// PREC 1 is the FP32 path: distances from double-float group-relative
+// coordinates, kernel and gradient in FP32, Kahan-compensated sums, and an
+// FP64 recheck of the cutoff for pairs within 1e-5 h of h, so the neighbour
+// sets equal the FP64 ones.
+#include "tm_arrays.cuh"
+#include "tm_kernels.cuh"
+
+#define FULL 0xffffffffu
+#define PAIR_TILE 128
+#define PAIR_LCAP 64
+
+template <int PREC>
+struct pair_acc;
+
+template <>
+struct pair_acc<0> {
+    double dens, mind, fx, fy, fz;
+    __device__ void init() { dens = 0.0; mind = 1.7976931348623157e308; fx = fy = fz = 0.0; }
+};
+
+template <>
+struct pair_acc<1> {
+    kahan dens, fx, fy, fz;
+    float mins;
+    __device__ void init() { dens.init(); fx.init(); fy.init(); fz.init(); mins = 3.0e38f; }
+};
+
+template <int PREC>
+__global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, const tm_consts *K)
+{
+    __shared__ float4 tile_s[TM_WARPS_PER_BLOCK][PAIR_TILE];
+    __shared__ int list_s[TM_WARPS_PER_BLOCK][PAIR_LCAP][32];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long base = w * 32;
+    if (base >= a.nslots_total) return;
+    const int c = a.col[base];
+    const tm_desc &d = a.desc[c];
+    if (!d.active || d.precision != PREC || d.n <= 1) return;   // potential.c:89
+    const tm_frame &f = a.frame[c];
+    const int dim = K->dim;
+    float4 *tile = tile_s[wib];
+    int(*list)[32] = list_s[wib];
+
+    const long long i = base + lane;
+    const bool live = (i - d.off) < d.n;
+    const int t = live ? a.ctype[i] : 0;
+    const tm_type &T = K->t[t];
+
+    // group origin: the float position of the warp's first cell
+    float4 h0 = a.hi[base];
+    const float ox = __shfl_sync(FULL, h0.x, 0), oy = __shfl_sync(FULL, h0.y, 0), oz = __shfl_sync(FULL, h0.z, 0);
+    float4 hi_i = live ? a.hi[i] : h0;
+    float4 lo_i = live ? a.lo[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    // double-float group-relative coordinates (s + e == x - o up to ~2^-47 |x|)
+    float sx, sy, sz, ex, ey, ez;
+    two_sum(hi_i.x, -ox, sx, ex);
+    two_sum(hi_i.y, -oy, sy, ey);
+    two_sum(hi_i.z, -oz, sz, ez);
+    ex += lo_i.x;
+    ey += lo_i.y;
+    ez += lo_i.z;
+    const float gx = sx + ex, gy = sy + ey, gz = sz + ez;   // single-float form for the test
+    // conservative test radius: FP32 staging errors are < 1e-5 here
+    const float hr = T.hf * 1.00002f + 1e-4f;
+    const float thr = live ? hr * hr : -1.0f;
+
+    // union of the query boxes, in group-relative coordinates
+    float mnx = live ? gx - hr : 3e38f, mny = live ? gy - hr : 3e38f, mnz = live ? gz - hr : 3e38f;
+    float mxx = live ? gx + hr : -3e38f, mxy = live ? gy + hr : -3e38f, mxz = live ? gz + hr : -3e38f;
+    for (int o = 16; o > 0; o >>= 1) {
+        mnx = fminf(mnx, __shfl_xor_sync(FULL, mnx, o));
+        mny = fminf(mny, __shfl_xor_sync(FULL, mny, o));
+        mnz = fminf(mnz, __shfl_xor_sync(FULL, mnz, o));
+        mxx = fmaxf(mxx, __shfl_xor_sync(FULL, mxx, o));
+        mxy = fmaxf(mxy, __shfl_xor_sync(FULL, mxy, o));
+        mxz = fmaxf(mxz, __shfl_xor_sync(FULL, mxz, o));
+    }
+    const int L = f.L;
+    const int nside = 1 << L;
+    const float bs = f.binscale;
+    auto binof = [&](float g, float o, float sh, float eps) {
+        float v = (o - sh + g) * bs + eps;
+        int b = (int)floorf(v);
+        return b < 0 ? 0 : (b >= nside ? nside - 1 : b);
+    };
+    const int bx0 = binof(mnx, ox, f.shiftf[0], -0.01f), bx1 = binof(mxx, ox, f.shiftf[0], 0.01f);
+    const int by0 = binof(mny, oy, f.shiftf[1], -0.01f), by1 = binof(mxy, oy, f.shiftf[1], 0.01f);
+    const int bz0 = binof(mnz, oz, f.shiftf[2], -0.01f), bz1 = binof(mxz, oz, f.shiftf[2], 0.01f);
+    const int nbx = bx1 - bx0 + 1, nby = by1 - by0 + 1, nbz = bz1 - bz0 + 1;
+    const int nb = nbx * nby * nbz;
+    const uint32_t *bstart = a.bin_start + d.binoff;
+    const long long bbase = f.bin_base;
+
+    // FP64 data of the own cell (plain path and band rechecks)
+    const double xi = live ? a.x[i] : 0.0, yi = live ? a.y[i] : 0.0, zi = live ? a.z[i] : 0.0;
+    pair_acc<PREC> acc;
+    acc.init();
+    int cnt_nb = 0;
+    unsigned long long hash = 0;
+    int nl = 0;
+
+    auto drain = [&]() {
+        int m = nl;
+        for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(FULL, m, o));
+        for (int q = 0; q < m; q++) {
+            if (q >= nl) continue;
+            const int j = list[q][lane];
+            if constexpr (PREC == 0) {
+                const double xj = a.x[j], yj = a.y[j], zj = a.z[j];
+                const double dx = sub64(xi, xj), dy = sub64(yi, yj), dz = sub64(zi, zj);
+                const double dist = __dsqrt_rn(add64(add64(mul64(dx, dx), mul64(dy, dy)), mul64(dz, dz)));
+                acc.mind = (dist < acc.mind ? dist : acc.mind);
+                if (dist <= T.h) {
+                    const double u = div64(dist, T.h);
+                    const double omu = sub64(1.0, u);
+                    double wk, wg;
+                    if (u <= 0.5) {
+                        const double six_uu = mul64(mul64(6.0, u), u);
+                        wk = mul64(T.cW, add64(sub64(1.0, six_uu), mul64(six_uu, u)));
+                        wg = add64(mul64(-2.0, u), mul64(mul64(3.0, u), u));
+                    } else {
+                        wk = mul64(T.cW, mul64(mul64(mul64(2.0, omu), omu), omu));
+                        wg = mul64(-omu, omu);
+                    }
+                    const double mj = a.mass[(long long)t * a.nslots_total + j];
+                    acc.dens = add64(acc.dens, mul64(mj, (double)__double2float_rn(wk)));
+                    const double wc = mul64(wg, T.cG);
+                    acc.fx = add64(acc.fx, div64(mul64(wc, sub64(xj, xi)), dist));
+                    acc.fy = add64(acc.fy, div64(mul64(wc, sub64(yj, yi)), dist));
+                    if (dim == 3) acc.fz = add64(acc.fz, div64(mul64(wc, sub64(zj, zi)), dist));
+                    cnt_nb++;
+                    if (a.want_diag) hash += tm_mix64((unsigned long long)a.perm[j] + 1ull);
+                }
+            } else {
+                const float4 hj = a.hi[j], lj = a.lo[j];
+                float s2, e2;
+                two_sum(hj.x, -ox, s2, e2);
+                const float dx = (s2 - sx) + ((e2 + lj.x) - ex);
+                two_sum(hj.y, -oy, s2, e2);
+                const float dy = (s2 - sy) + ((e2 + lj.y) - ey);
+                two_sum(hj.z, -oz, s2, e2);
+                const float dz = (s2 - sz) + ((e2 + lj.z) - ez);
+                const float s = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                bool in = s <= T.thr_lo;
+                if (!in && s <= T.thr_hi) {
+                    // band |r - h| < 1e-5 h: decide with the FP64 distance
+                    const double ddx = sub64(xi, a.x[j]), ddy = sub64(yi, a.y[j]), ddz = sub64(zi, a.z[j]);
+                    in = __dsqrt_rn(add64(add64(mul64(ddx, ddx), mul64(ddy, ddy)), mul64(ddz, ddz))) <= T.h;
+                }
+                if (in) {
+                    acc.mins = fminf(acc.mins, s);
+                    const float rs = s > 0.0f ? rsqrtf(s) : 0.0f;
+                    const float dist = s * rs;
+                    const float u = dist * T.inv_hf;
+                    const float omu = 1.0f - u;
+                    float wk, wg;
+                    if (u <= 0.5f) {
+                        wk = T.cWf * fmaf(6.0f * u * u, u - 1.0f, 1.0f);
+                        wg = u * fmaf(3.0f, u, -2.0f);
+                    } else {
+                        wk = T.cWf * (2.0f * omu * omu * omu);
+                        wg = -omu * omu;
+                    }
+                    acc.dens.add(T.kmassf * hj.w * wk);
+                    const float g = wg * T.cGf * rs;
+                    acc.fx.add(g * dx);
+                    acc.fy.add(g * dy);
+                    if (dim == 3) acc.fz.add(g * dz);
+                    cnt_nb++;
+                    if (a.want_diag) hash += tm_mix64((unsigned long long)a.perm[j] + 1ull);
+                }
+            }
+        }
+        nl = 0;
+    };
+
+    for (int chunk = 0; chunk < nb; chunk += 32) {
+        const int q = chunk + lane;
+        long long st = 0;
+        uint32_t cnt = 0;
+        if (q < nb) {
+            const int bx = bx0 + q % nbx;
+            const int by = by0 + (q / nbx) % nby;
+            const int bz = bz0 + q / (nbx * nby);
+            const uint32_t m = tm_morton((uint32_t)bx, (uint32_t)by, (uint32_t)bz);
+            const uint32_t s0 = bstart[m];
+            st = bbase + s0;
+            cnt = bstart[m + 1] - s0;
+        }
+        uint32_t incl = cnt;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const uint32_t total = __shfl_sync(FULL, incl, 31);
+        const uint32_t off = incl - cnt;
+        for (uint32_t wb = 0; wb < total; wb += PAIR_TILE) {
+            const uint32_t k0 = max(off, wb), k1 = min(off + cnt, wb + PAIR_TILE);
+            for (uint32_t k = k0; k < k1; k++) {
+                const long long j = st + (k - off);
+                const float4 hj = a.hi[j], lj = a.lo[j];
+                tile[k - wb] = make_float4((hj.x - ox) + lj.x, (hj.y - oy) + lj.y, (hj.z - oz) + lj.z,
+                                           __int_as_float((int)j));
+            }
+            __syncwarp();
+            const int wn = (int)min((uint32_t)PAIR_TILE, total - wb);
+            for (int tb = 0; tb < wn; tb += 32) {
+                const int te = min(wn, tb + 32);
+#pragma unroll 8
+                for (int tt = tb; tt < te; tt++) {
+                    const float4 cc = tile[tt];
+                    const float dx = cc.x - gx, dy = cc.y - gy, dz = cc.z - gz;
+                    const float s = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    const int j = __float_as_int(cc.w);
+                    if (s <= thr && (long long)j != i) {
+                        list[nl][lane] = j;
+                        nl++;
+                    }
+                }
+                if (__any_sync(FULL, nl > PAIR_LCAP - 32)) drain();
+            }
+            __syncwarp();
+        }
+    }
+    drain();
+
+    if (!live) return;
+    if constexpr (PREC == 0) {
+        a.density[i] = acc.dens;
+        a.mindist[i] = acc.mind;
+        a.fx[i] = acc.fx;
+        a.fy[i] = acc.fy;
+        a.fz[i] = acc.fz;
+    } else {
+        a.density[i] = (double)acc.dens.value();
+        a.mindist[i] = cnt_nb ? (double)sqrtf(acc.mins) : 1.7976931348623157e308;
+        a.fx[i] = (double)acc.fx.value();
+        a.fy[i] = (double)acc.fy.value();
+        a.fz[i] = (double)acc.fz.value();
+    }
+    a.nbcount[i] = cnt_nb;
+    if (a.want_diag) a.nbhash[i] = hash;
+}
+
+cudaError_t tm_launch_pair(const tm_arrays &a, const tm_consts *K, int prec, cudaStream_t st)
+{
+    long long warps = a.nslots_total / 32;
+    long long threads = warps * 32;
+    int bt = TM_WARPS_PER_BLOCK * 32;
+    unsigned grid = (unsigned)((threads + bt - 1) / bt);
+    if (grid == 0) return cudaSuccess;
+    if (prec == 0) k_pair<0><<<grid, bt, 0, st>>>(a, K);
+    else k_pair<1><<<grid, bt, 0, st>>>(a, K);
+    return cudaGetLastError();
+}

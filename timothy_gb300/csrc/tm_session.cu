@@ -1,0 +1,816 @@
+// Device-resident sessions: colonies packed in HBM, one launch sequence per
+// step for all of them, downloads in caller order.  Implements the tm_* API
+// of include/timothy_gb300.h.
+#include "tm_kernels.cuh"
+#include "timothy_gb300.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+static thread_local std::string g_err;
+
+static int tm_fail(int code, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CK(call)                                                                                     \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess)                                                                       \
+            return tm_fail(TM_ECUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)
+
+extern "C" const char *tm_last_error(void) { return g_err.c_str(); }
+extern "C" const char *tm_version(void) { return "timothy_gb300 0.1 sm_103a"; }
+
+extern "C" int tm_device_count(void)
+{
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
+    return n;
+}
+
+// ---------------------------------------------------------------------------
+// first-fit range allocator
+
+struct range_alloc {
+    long long cap = 0, hwm = 0;
+    std::vector<std::pair<long long, long long>> freel;   // (start, len), sorted by start
+    void init(long long c)
+    {
+        cap = c;
+        hwm = 0;
+        freel.clear();
+        if (c > 0) freel.push_back({0, c});
+    }
+    bool alloc(long long len, long long &start)
+    {
+        for (size_t k = 0; k < freel.size(); k++) {
+            if (freel[k].second >= len) {
+                start = freel[k].first;
+                freel[k].first += len;
+                freel[k].second -= len;
+                if (freel[k].second == 0) freel.erase(freel.begin() + (long)k);
+                hwm = std::max(hwm, start + len);
+                return true;
+            }
+        }
+        return false;
+    }
+    void release(long long start, long long len)
+    {
+        if (len <= 0) return;
+        auto it = std::lower_bound(freel.begin(), freel.end(), std::make_pair(start, 0ll));
+        it = freel.insert(it, {start, len});
+        size_t k = (size_t)(it - freel.begin());
+        if (k + 1 < freel.size() && freel[k].first + freel[k].second == freel[k + 1].first) {
+            freel[k].second += freel[k + 1].second;
+            freel.erase(freel.begin() + (long)k + 1);
+        }
+        if (k > 0 && freel[k - 1].first + freel[k - 1].second == freel[k].first) {
+            freel[k - 1].second += freel[k].second;
+            freel.erase(freel.begin() + (long)k);
+        }
+        // lower the high-water mark when the tail is free
+        if (!freel.empty() && freel.back().first + freel.back().second == cap) hwm = std::min(hwm, freel.back().first);
+    }
+    long long free_total() const
+    {
+        long long s = 0;
+        for (auto &f : freel) s += f.second;
+        return s;
+    }
+};
+
+struct colony_host {
+    bool used = false;
+    int n = 0, nslots = 0, lcap = 1;
+    long long off = 0, binoff = 0, nbin = 0, gridoff = -1, ngrid = 0;
+    int gsize[3] = {0, 0, 0};
+    tm_colony_options opt{};
+    int active = 1;
+};
+
+struct tm_session {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    tm_session_config cfg{};
+    tm_consts K{};
+    tm_consts *dK = nullptr;
+    tm_arrays A{};
+    range_alloc slots, bins, grids;
+    std::vector<colony_host> cols;
+    tm_desc *h_desc = nullptr;
+    tm_frame *h_frame = nullptr;
+    uint32_t *scan_tmp = nullptr;
+    unsigned long long *d_octsize = nullptr;
+    void *d_scratch = nullptr;
+    // profiling
+    bool prof = false;
+    std::vector<cudaEvent_t> evpool;
+    size_t evused = 0;
+    long long prof_steps = 0;
+    // graphs (one per buffer parity)
+    bool use_graph = false;
+    bool graph_valid[2] = {false, false};
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+    int parity = 0;   // 0: A.x is current, 1: A.x2 is current
+};
+
+// ---------------------------------------------------------------------------
+// helper kernels
+
+__global__ void k_colony_init(tm_arrays a, int c, long long off, int n, int nslots, int has_phase)
+{
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nslots) return;
+    long long i = off + k;
+    a.col[i] = c;
+    if (k < n) {
+        a.perm[i] = (int)k;
+        if (!has_phase) a.phase[i] = 1;
+    }
+    a.rem[i] = 0;
+    a.density[i] = 0.0;
+    a.v[i] = 0.0;
+    a.mindist[i] = 0.0;
+    a.fx[i] = 0.0;
+    a.fy[i] = 0.0;
+    a.fz[i] = 0.0;
+    a.nbcount[i] = 0;
+    if (a.nbhash) a.nbhash[i] = 0;
+    if (a.vcand) a.vcand[i] = -1;
+}
+
+template <typename T>
+__global__ void k_unsort(const T *src, const int *perm, long long off, int n, T *dst)
+{
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    dst[perm[off + k]] = src[off + k];
+}
+
+static unsigned blocks_for(long long n, int bt) { return (unsigned)std::max(1ll, (n + bt - 1) / bt); }
+
+// the arrays as the kernels of one step see them (parity 1 swaps the buffers)
+static tm_arrays view(const tm_session *s, int parity)
+{
+    tm_arrays a = s->A;
+    if (parity) {
+        std::swap(a.x, a.x2);
+        std::swap(a.y, a.y2);
+        std::swap(a.z, a.z2);
+        std::swap(a.size, a.size2);
+        std::swap(a.young, a.young2);
+        std::swap(a.ctype, a.ctype2);
+        std::swap(a.phase, a.phase2);
+        std::swap(a.perm, a.perm2);
+        std::swap(a.rem, a.rem2);
+    }
+    a.nslots_total = s->slots.hwm * 32;
+    a.ncol = (int)s->cols.size();
+    return a;
+}
+
+static cudaEvent_t next_event(tm_session *s)
+{
+    if (s->evused == s->evpool.size()) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+        s->evpool.push_back(e);
+    }
+    return s->evpool[s->evused++];
+}
+
+static void mark(tm_session *s)
+{
+    if (!s->prof) return;
+    cudaEvent_t e = next_event(s);
+    if (e) cudaEventRecord(e, s->stream);
+}
+
+// one full step for buffer parity p; the result is current in parity 1 - p
+static int enqueue_step(tm_session *s, int p)
+{
+    cudaStream_t st = s->stream;
+    tm_arrays a = view(s, p);
+    const long long nsl = a.nslots_total;
+    const long long nbin = s->bins.hwm;
+    const int ncol = a.ncol;
+    if (nsl == 0 || ncol == 0) return TM_OK;
+    mark(s);
+    CK(cudaMemsetAsync(a.bin_count, 0, (size_t)(nbin + 1) * sizeof(uint32_t), st));
+    CK(cudaMemsetAsync(a.bin_cursor, 0, (size_t)(nbin + 1) * sizeof(uint32_t), st));
+    CK(cudaMemsetAsync(a.bigbins, 0, sizeof(int), st));
+    k_step_init<<<blocks_for(ncol, 128), 128, 0, st>>>(a);
+    k_bbox<<<blocks_for(nsl, 256), 256, 0, st>>>(a, s->K.ntypes);
+    k_frame<<<blocks_for(ncol, 128), 128, 0, st>>>(a, s->dK);
+    k_codes<<<blocks_for(nsl, 256), 256, 0, st>>>(a);
+    CK(cudaGetLastError());
+    CK(tm_scan_exclusive(a.bin_count, a.bin_start, nbin + 1, s->scan_tmp, st));
+    k_binbase<<<blocks_for(ncol, 128), 128, 0, st>>>(a);
+    k_scatter<<<blocks_for(nsl, 256), 256, 0, st>>>(a);
+    k_binsort_small<<<blocks_for(nsl, 128), 128, 0, st>>>(a);
+    k_binsort_big<<<64, 256, 0, st>>>(a);
+    k_gather<<<blocks_for(nsl, 256), 256, 0, st>>>(a, s->dK);
+    CK(cudaGetLastError());
+    mark(s);
+    // from here on the gathered (Morton-ordered) buffers are current
+    tm_arrays b = view(s, 1 - p);
+    bool any_cic = false, any64 = false, any32 = false;
+    for (auto &c : s->cols) {
+        if (!c.used || !c.active) continue;
+        if (c.gridoff >= 0) any_cic = true;
+        if (c.opt.precision == TM_PREC_FP64) any64 = true;
+        else any32 = true;
+    }
+    if (any_cic) {
+        CK(cudaMemsetAsync(b.grid, 0, (size_t)s->grids.hwm * sizeof(double), st));
+        CK(tm_launch_cic(b, s->dK, st));
+    }
+    mark(s);
+    if (any64) CK(tm_launch_pair(b, s->dK, 0, st));
+    if (any32) CK(tm_launch_pair(b, s->dK, 1, st));
+    mark(s);
+    CK(tm_launch_octree(b, s->dK, st));
+    mark(s);
+    CK(tm_launch_update(b, s->dK, st));
+    mark(s);
+    return TM_OK;
+}
+
+static void drop_graphs(tm_session *s)
+{
+    for (int k = 0; k < 2; k++) {
+        if (s->gexec[k]) cudaGraphExecDestroy(s->gexec[k]);
+        s->gexec[k] = nullptr;
+        s->graph_valid[k] = false;
+    }
+}
+
+static int push_desc(tm_session *s, int c)
+{
+    CK(cudaMemcpyAsync(&s->A.desc[c], &s->h_desc[c], sizeof(tm_desc), cudaMemcpyHostToDevice, s->stream));
+    return TM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// session lifetime
+
+template <typename T>
+static int dalloc(T **p, long long count)
+{
+    if (count <= 0) count = 1;
+    CK(cudaMalloc((void **)p, (size_t)count * sizeof(T)));
+    return TM_OK;
+}
+
+static double host_type_const(int dim, int which, double h, double h2, double h3, double h4)
+{
+    // the reference's own expressions (inline.h:45-46, 71-72)
+    if (which == 0) return dim == 2 ? 40 / (7 * M_PI * h2) : 8 / (M_PI * h3);
+    return dim == 2 ? (40 * 8) / (7 * M_PI * h3) : 48 / (M_PI * h4);
+}
+
+extern "C" int tm_session_destroy(tm_session *s);
+
+extern "C" int tm_session_create(tm_session **out, const tm_session_config *cfg, const tm_celltypes *types)
+{
+    if (!out || !cfg || !types) return tm_fail(TM_EINVAL, "null argument");
+    *out = nullptr;
+    if (cfg->dimension != 2 && cfg->dimension != 3) return tm_fail(TM_EINVAL, "dimension must be 2 or 3");
+    if (types->ntypes < 1 || types->ntypes > TM_MAX_TYPES) return tm_fail(TM_EINVAL, "ntypes must be 1..%d", TM_MAX_TYPES);
+    if (cfg->max_slots <= 0 || cfg->max_colonies <= 0) return tm_fail(TM_EINVAL, "max_slots and max_colonies must be positive");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return tm_fail(TM_ENODEV, "no CUDA device");
+    if (cfg->device < 0 || cfg->device >= ndev) return tm_fail(TM_EINVAL, "device %d out of range", cfg->device);
+    CK(cudaSetDevice(cfg->device));
+
+    tm_session *s = new tm_session();
+    s->device = cfg->device;
+    s->cfg = *cfg;
+    tm_consts &K = s->K;
+    K.ntypes = types->ntypes;
+    K.dim = cfg->dimension;
+    for (int t = 0; t < K.ntypes; t++) {
+        tm_type &T = K.t[t];
+        T.h = types->h[t];
+        T.h2 = types->h2[t];
+        T.h3 = types->h3[t];
+        T.h4 = types->h4[t];
+        T.csize = types->size[t];
+        T.sc = cfg->dimension == 2 ? T.h2 : T.h3;
+        T.cW = host_type_const(cfg->dimension, 0, T.h, T.h2, T.h3, T.h4);
+        T.cG = host_type_const(cfg->dimension, 1, T.h, T.h2, T.h3, T.h4);
+        T.e = T.h + 0.01;
+        T.randommove = types->randommove ? types->randommove[t] : 0.0f;
+        T.hf = (float)T.h;
+        T.h2f = (float)(T.h * T.h);
+        T.inv_hf = (float)(1.0 / T.h);
+        T.cWf = (float)T.cW;
+        T.cGf = (float)T.cG;
+        T.kmassf = (float)(T.sc / T.csize);
+        T.thr_lo = (float)(T.h * (1.0 - 1e-5) * T.h * (1.0 - 1e-5));
+        T.thr_hi = (float)(T.h * (1.0 + 1e-5) * T.h * (1.0 + 1e-5));
+        if (!(T.h > 0.0) || !(T.csize > 0.0)) {
+            delete s;
+            return tm_fail(TM_EINVAL, "type %d: h and size must be positive", t);
+        }
+    }
+
+    const long long S = ((cfg->max_slots + 31) / 32) * 32;
+    const long long B = cfg->max_bin_entries > 0 ? cfg->max_bin_entries
+                                                  : std::max<long long>(1 << 12, 2 * S) + (1ll << (3 * TM_LMAX)) + 2;
+    const long long G = cfg->max_grid_entries > 0 ? cfg->max_grid_entries : 257ll * 257 * 257;
+    const int C = cfg->max_colonies;
+    s->slots.init(S / 32);
+    s->bins.init(B);
+    s->grids.init(G);
+    s->cols.reserve((size_t)C);
+
+    int rc = TM_OK;
+    cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete s;
+        return tm_fail(TM_ECUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+    }
+    tm_arrays &a = s->A;
+#define AL(p, cnt)                                   \
+    if (rc == TM_OK) rc = dalloc(&(p), (cnt));
+    AL(a.x, S) AL(a.y, S) AL(a.z, S) AL(a.size, S) AL(a.young, S) AL(a.ctype, S) AL(a.phase, S) AL(a.perm, S)
+    AL(a.rem, S)
+    AL(a.x2, S) AL(a.y2, S) AL(a.z2, S) AL(a.size2, S) AL(a.young2, S) AL(a.ctype2, S) AL(a.phase2, S)
+    AL(a.perm2, S) AL(a.rem2, S)
+    AL(a.col, S) AL(a.code, S) AL(a.codes, S) AL(a.bin, S) AL(a.tmp, S) AL(a.hi, S) AL(a.lo, S)
+    AL(a.mass, S * K.ntypes)
+    AL(a.bin_count, B + 1) AL(a.bin_cursor, B + 1) AL(a.bin_start, B + 1) AL(a.bigbins, 2 * (S / 33) + 4)
+    AL(a.density, S) AL(a.v, S) AL(a.mindist, S) AL(a.fx, S) AL(a.fy, S) AL(a.fz, S) AL(a.nbcount, S)
+    AL(a.grid, G) AL(a.desc, C) AL(a.frame, C)
+    AL(s->scan_tmp, tm_scan_tmp_words(B + 1)) AL(s->d_octsize, C) AL(s->dK, 1)
+    if (rc == TM_OK) rc = dalloc((double **)&s->d_scratch, S);
+    if (cfg->diagnostics) {
+        AL(a.nbhash, S) AL(a.vcand, S)
+    }
+#undef AL
+    if (rc == TM_OK) {
+        if (cudaMallocHost((void **)&s->h_desc, sizeof(tm_desc) * (size_t)C) != cudaSuccess ||
+            cudaMallocHost((void **)&s->h_frame, sizeof(tm_frame) * (size_t)C) != cudaSuccess)
+            rc = tm_fail(TM_ENOMEM, "pinned host allocation failed");
+    }
+    if (rc != TM_OK) {
+        std::string msg = g_err;
+        tm_session_destroy(s);
+        g_err = msg;
+        return rc == TM_ECUDA ? TM_ENOMEM : rc;
+    }
+    a.want_diag = cfg->diagnostics ? 1 : 0;
+    a.nbin_total = B;
+    memset(s->h_desc, 0, sizeof(tm_desc) * (size_t)C);
+    memset(s->h_frame, 0, sizeof(tm_frame) * (size_t)C);
+    e = cudaMemcpy(s->dK, &s->K, sizeof(tm_consts), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(a.desc, 0, sizeof(tm_desc) * (size_t)C);
+    if (e == cudaSuccess) e = cudaMemset(a.frame, 0, sizeof(tm_frame) * (size_t)C);
+    if (e != cudaSuccess) {
+        tm_session_destroy(s);
+        return tm_fail(TM_ECUDA, "session init: %s", cudaGetErrorString(e));
+    }
+    *out = s;
+    return TM_OK;
+}
+
+extern "C" int tm_session_destroy(tm_session *s)
+{
+    if (!s) return TM_OK;
+    cudaSetDevice(s->device);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    drop_graphs(s);
+    tm_arrays &a = s->A;
+    void *ptrs[] = {a.x, a.y, a.z, a.size, a.young, a.ctype, a.phase, a.perm, a.rem, a.x2, a.y2, a.z2, a.size2,
+                    a.young2, a.ctype2, a.phase2, a.perm2, a.rem2, a.col, a.code, a.codes, a.bin, a.tmp, a.hi, a.lo,
+                    a.mass, a.bin_count, a.bin_cursor, a.bin_start, a.bigbins, a.density, a.v, a.mindist, a.fx,
+                    a.fy, a.fz, a.nbcount, a.nbhash, a.vcand, a.grid, a.desc, a.frame, s->scan_tmp, s->d_octsize,
+                    s->dK, s->d_scratch};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    for (auto ev : s->evpool) cudaEventDestroy(ev);
+    if (s->h_desc) cudaFreeHost(s->h_desc);
+    if (s->h_frame) cudaFreeHost(s->h_frame);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+    return TM_OK;
+}
+
+extern "C" void *tm_session_stream(tm_session *s) { return s ? (void *)s->stream : nullptr; }
+
+// ---------------------------------------------------------------------------
+// colonies
+
+static int grid_geometry(int dim, float gfh, int gsize[3], double lower[3])
+{
+    // computegridsize at one rank, grid.c:37-77 (float arithmetic as written there)
+    if (!(gfh > 0.0f)) return TM_EINVAL;
+    float gx = (float)(1024.0 - (-1024.0) + 1), gz = dim == 3 ? gx : 0.0f;
+    long long sx = (long long)((gx + 1) / gfh);
+    long long sz = dim == 3 ? (long long)((gz + 1) / gfh) : 0;
+    sx += 1 - sx % 1;
+    if (dim == 3) sz += 1 - sz % 1;
+    else sz = 1;
+    gsize[0] = (int)sx;
+    gsize[1] = (int)sx;
+    gsize[2] = (int)sz;
+    lower[0] = -1024.0;
+    lower[1] = -1024.0;
+    lower[2] = dim == 3 ? -1024.0 : 0.0;
+    return TM_OK;
+}
+
+static int copy_cells_in(tm_session *s, const colony_host &c, const tm_colony_input *in)
+{
+    const tm_arrays a = view(s, s->parity);
+    const long long o = c.off;
+    const size_t n = (size_t)in->n;
+    cudaStream_t st = s->stream;
+    if (n) {
+        CK(cudaMemcpyAsync(a.x + o, in->x, n * 8, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(a.y + o, in->y, n * 8, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(a.z + o, in->z, n * 8, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(a.size + o, in->size, n * 8, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(a.young + o, in->young, n * 4, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(a.ctype + o, in->ctype, n * 4, cudaMemcpyHostToDevice, st));
+        if (in->phase) CK(cudaMemcpyAsync(a.phase + o, in->phase, n * 4, cudaMemcpyHostToDevice, st));
+    }
+    k_colony_init<<<blocks_for(c.nslots, 256), 256, 0, st>>>(a, (int)(&c - s->cols.data()), o, (int)n, c.nslots,
+                                                             in->phase ? 1 : 0);
+    CK(cudaGetLastError());
+    // synchronous: the caller may free its buffers on return
+    CK(cudaStreamSynchronize(st));
+    return TM_OK;
+}
+
+static int check_input(const tm_session *s, const tm_colony_input *in)
+{
+    if (!in || in->n < 0) return tm_fail(TM_EINVAL, "bad colony input");
+    if (in->n > 0 && (!in->x || !in->y || !in->z || !in->size || !in->young || !in->ctype))
+        return tm_fail(TM_EINVAL, "colony input arrays missing");
+    if (in->n > 0x7fffffffll) return tm_fail(TM_EINVAL, "colony too large");
+    for (long long k = 0; k < in->n; k++)
+        if (in->ctype[k] < 0 || in->ctype[k] >= s->K.ntypes)
+            return tm_fail(TM_EINVAL, "cell %lld has cell type %d outside 0..%d", k, in->ctype[k], s->K.ntypes - 1);
+    return TM_OK;
+}
+
+static int auto_lcap(const tm_session *s, const tm_colony_input *in)
+{
+    if (in->n <= 1) return 1;
+    double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
+    const double *p[3] = {in->x, in->y, in->z};
+    for (long long k = 0; k < in->n; k++)
+        for (int d = 0; d < 3; d++) {
+            mn[d] = std::min(mn[d], p[d][k]);
+            mx[d] = std::max(mx[d], p[d][k]);
+        }
+    double hmax = 0.0;
+    for (int t = 0; t < s->K.ntypes; t++) hmax = std::max(hmax, s->K.t[t].h);
+    double ext = std::max(mx[0] - mn[0], std::max(mx[1] - mn[1], mx[2] - mn[2])) + 2 * (hmax + 0.01);
+    int L = (int)std::floor(std::log2(2.0 * ext / hmax)) + 1;   // one level of headroom for growth
+    return std::max(1, std::min(TM_LMAX, L));
+}
+
+extern "C" int tm_colony_add(tm_session *s, const tm_colony_input *in, const tm_colony_options *opt, int *id)
+{
+    if (!s || !opt || !id) return tm_fail(TM_EINVAL, "null argument");
+    int rc = check_input(s, in);
+    if (rc) return rc;
+    if (opt->precision != TM_PREC_FP64 && opt->precision != TM_PREC_FP32C) return tm_fail(TM_EINVAL, "bad precision");
+    if (opt->update_mode < 0 || opt->update_mode > 2) return tm_fail(TM_EINVAL, "bad update mode");
+    CK(cudaSetDevice(s->device));
+    int c = -1;
+    for (size_t k = 0; k < s->cols.size(); k++)
+        if (!s->cols[k].used) { c = (int)k; break; }
+    if (c < 0) {
+        if ((int)s->cols.size() >= s->cfg.max_colonies) return tm_fail(TM_ENOMEM, "no free colony entry");
+        s->cols.push_back(colony_host());
+        c = (int)s->cols.size() - 1;
+    }
+    colony_host ch;
+    ch.n = (int)in->n;
+    ch.nslots = (int)(((std::max<long long>(in->n, 1) + 31) / 32) * 32);
+    ch.opt = *opt;
+    ch.lcap = opt->lcap > 0 ? std::min(opt->lcap, TM_LMAX) : auto_lcap(s, in);
+    ch.nbin = (1ll << (3 * ch.lcap)) + 2;
+    long long soff;
+    if (!s->slots.alloc(ch.nslots / 32, soff)) return tm_fail(TM_ENOMEM, "no room for %d slots", ch.nslots);
+    ch.off = soff * 32;
+    if (!s->bins.alloc(ch.nbin, ch.binoff)) {
+        s->slots.release(soff, ch.nslots / 32);
+        return tm_fail(TM_ENOMEM, "no room for %lld bin entries", ch.nbin);
+    }
+    double glower[3] = {0, 0, 0};
+    if (opt->cic) {
+        if (grid_geometry(s->K.dim, opt->gfh, ch.gsize, glower)) {
+            s->slots.release(soff, ch.nslots / 32);
+            s->bins.release(ch.binoff, ch.nbin);
+            return tm_fail(TM_EINVAL, "bad grid resolution");
+        }
+        ch.ngrid = (long long)ch.gsize[0] * ch.gsize[1] * ch.gsize[2];
+        if (!s->grids.alloc(ch.ngrid, ch.gridoff)) {
+            s->slots.release(soff, ch.nslots / 32);
+            s->bins.release(ch.binoff, ch.nbin);
+            return tm_fail(TM_ENOMEM, "no room for a %lld-node grid", ch.ngrid);
+        }
+    }
+    ch.used = true;
+    ch.active = 1;
+    s->cols[c] = ch;
+    tm_desc &d = s->h_desc[c];
+    memset(&d, 0, sizeof d);
+    d.off = ch.off;
+    d.binoff = ch.binoff;
+    d.gridoff = opt->cic ? ch.gridoff : -1;
+    d.n = ch.n;
+    d.nslots = ch.nslots;
+    d.Lcap = ch.lcap;
+    d.precision = opt->precision;
+    d.update_mode = opt->update_mode;
+    d.active = 1;
+    d.dt = opt->dt;
+    for (int k = 0; k < 3; k++) {
+        d.glower[k] = glower[k];
+        d.gsize[k] = ch.gsize[k];
+    }
+    d.gres = opt->gfh;
+    tm_frame &f = s->h_frame[c];
+    memset(&f, 0, sizeof f);
+    f.scale = 1.0;
+    f.L = 1;
+    f.nbins = 8;
+    f.binscale = 2.0f;
+    CK(cudaMemcpyAsync(&s->A.frame[c], &f, sizeof f, cudaMemcpyHostToDevice, s->stream));
+    rc = push_desc(s, c);
+    if (rc == TM_OK) rc = copy_cells_in(s, s->cols[c], in);
+    if (rc != TM_OK) return rc;
+    drop_graphs(s);
+    *id = c;
+    return TM_OK;
+}
+
+static int lookup(tm_session *s, int id)
+{
+    if (!s) return tm_fail(TM_EINVAL, "null session");
+    if (id < 0 || id >= (int)s->cols.size() || !s->cols[id].used) return tm_fail(TM_ENOENT, "no colony %d", id);
+    return TM_OK;
+}
+
+extern "C" int tm_colony_remove(tm_session *s, int id)
+{
+    int rc = lookup(s, id);
+    if (rc) return rc;
+    CK(cudaSetDevice(s->device));
+    CK(cudaStreamSynchronize(s->stream));
+    colony_host &c = s->cols[id];
+    s->h_desc[id].active = 0;
+    s->h_desc[id].n = 0;
+    rc = push_desc(s, id);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(s->stream));
+    s->slots.release(c.off / 32, c.nslots / 32);
+    s->bins.release(c.binoff, c.nbin);
+    if (c.gridoff >= 0) s->grids.release(c.gridoff, c.ngrid);
+    c = colony_host();
+    while (!s->cols.empty() && !s->cols.back().used) s->cols.pop_back();
+    drop_graphs(s);
+    return TM_OK;
+}
+
+extern "C" int tm_colony_upload(tm_session *s, int id, const tm_colony_input *in)
+{
+    int rc = lookup(s, id);
+    if (rc) return rc;
+    rc = check_input(s, in);
+    if (rc) return rc;
+    colony_host &c = s->cols[id];
+    if (in->n > c.nslots) return tm_fail(TM_EINVAL, "colony %d holds at most %d cells", id, c.nslots);
+    CK(cudaSetDevice(s->device));
+    CK(cudaStreamSynchronize(s->stream));
+    c.n = (int)in->n;
+    s->h_desc[id].n = c.n;
+    rc = push_desc(s, id);
+    if (rc) return rc;
+    rc = copy_cells_in(s, c, in);
+    if (rc) return rc;
+    drop_graphs(s);
+    return TM_OK;
+}
+
+extern "C" int tm_colony_set_active(tm_session *s, int id, int active)
+{
+    int rc = lookup(s, id);
+    if (rc) return rc;
+    s->cols[id].active = active ? 1 : 0;
+    s->h_desc[id].active = active ? 1 : 0;
+    rc = push_desc(s, id);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(s->stream));
+    drop_graphs(s);
+    return TM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// stepping
+
+static int run_step_graph(tm_session *s)
+{
+    int p = s->parity;
+    if (!s->graph_valid[p]) {
+        cudaGraph_t g;
+        CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = enqueue_step(s, p);
+        cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+        if (rc) return rc;
+        if (e != cudaSuccess) return tm_fail(TM_ECUDA, "graph capture: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&s->gexec[p], g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return tm_fail(TM_ECUDA, "graph instantiate: %s", cudaGetErrorString(e));
+        s->graph_valid[p] = true;
+    }
+    CK(cudaGraphLaunch(s->gexec[p], s->stream));
+    return TM_OK;
+}
+
+extern "C" int tm_session_step(tm_session *s, int nsteps)
+{
+    if (!s || nsteps < 0) return tm_fail(TM_EINVAL, "bad arguments");
+    CK(cudaSetDevice(s->device));
+    for (int k = 0; k < nsteps; k++) {
+        int rc = (s->use_graph && !s->prof) ? run_step_graph(s) : enqueue_step(s, s->parity);
+        if (rc) return rc;
+        s->parity ^= 1;
+        if (s->prof) s->prof_steps++;
+    }
+    return TM_OK;
+}
+
+extern "C" int tm_session_sync(tm_session *s)
+{
+    if (!s) return tm_fail(TM_EINVAL, "null session");
+    CK(cudaSetDevice(s->device));
+    CK(cudaStreamSynchronize(s->stream));
+    const int ncol = (int)s->cols.size();
+    if (ncol == 0) return TM_OK;
+    CK(cudaMemcpy(s->h_frame, s->A.frame, sizeof(tm_frame) * (size_t)ncol, cudaMemcpyDeviceToHost));
+    for (int c = 0; c < ncol; c++) {
+        if (!s->cols[c].used) continue;
+        uint32_t e = s->h_frame[c].error;
+        if (e)
+            return tm_fail(TM_EDEVICE, "colony %d: device error 0x%x (%s%s%s)", c, e,
+                           (e & TM_ERR_BIGBIN) ? "more than 2048 cells in one bin; " : "",
+                           (e & TM_ERR_STACK) ? "octree walk too deep; " : "",
+                           (e & TM_ERR_CODES) ? "coincident lattice codes; " : "");
+    }
+    return TM_OK;
+}
+
+extern "C" int tm_session_use_graph(tm_session *s, int on)
+{
+    if (!s) return tm_fail(TM_EINVAL, "null session");
+    s->use_graph = on != 0;
+    if (!on) drop_graphs(s);
+    return TM_OK;
+}
+
+extern "C" int tm_session_profile(tm_session *s, int on)
+{
+    if (!s) return tm_fail(TM_EINVAL, "null session");
+    CK(cudaStreamSynchronize(s->stream));
+    s->prof = on != 0;
+    s->evused = 0;
+    s->prof_steps = 0;
+    return TM_OK;
+}
+
+extern "C" int tm_session_profile_read(tm_session *s, double *ms, int nphase, int64_t *steps)
+{
+    if (!s || !ms) return tm_fail(TM_EINVAL, "null argument");
+    CK(cudaStreamSynchronize(s->stream));
+    const int per = 6;   // marks per step
+    double acc[5] = {0, 0, 0, 0, 0};
+    long long nst = (long long)(s->evused / per);
+    for (long long k = 0; k < nst; k++) {
+        for (int ph = 0; ph < 5; ph++) {
+            float t = 0.0f;
+            CK(cudaEventElapsedTime(&t, s->evpool[k * per + ph], s->evpool[k * per + ph + 1]));
+            acc[ph] += t;
+        }
+    }
+    // phases in recording order: build, cic, pair, octree, update -> report build, pair, octree, update, cic
+    const double order[5] = {acc[0], acc[2], acc[3], acc[4], acc[1]};
+    for (int k = 0; k < nphase && k < 5; k++) ms[k] = nst ? order[k] / (double)nst : 0.0;
+    if (steps) *steps = nst;
+    return TM_OK;
+}
+
+extern "C" int tm_session_capacity(tm_session *s, int64_t *free_slots, int64_t *free_bins, int *free_colonies)
+{
+    if (!s) return tm_fail(TM_EINVAL, "null session");
+    if (free_slots) *free_slots = s->slots.free_total() * 32;
+    if (free_bins) *free_bins = s->bins.free_total();
+    if (free_colonies) {
+        int used = 0;
+        for (auto &c : s->cols) used += c.used ? 1 : 0;
+        *free_colonies = s->cfg.max_colonies - used;
+    }
+    return TM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// downloads
+
+template <typename T>
+static int unsort_to_host(tm_session *s, const T *src, const colony_host &c, T *host)
+{
+    if (!host || c.n == 0) return TM_OK;
+    const tm_arrays a = view(s, s->parity);
+    T *tmp = (T *)s->d_scratch;
+    k_unsort<T><<<blocks_for(c.n, 256), 256, 0, s->stream>>>(src, a.perm, c.off, c.n, tmp);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(host, tmp, sizeof(T) * (size_t)c.n, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return TM_OK;
+}
+
+extern "C" int tm_colony_download(tm_session *s, int id, const tm_colony_output *out)
+{
+    int rc = lookup(s, id);
+    if (rc) return rc;
+    if (!out) return tm_fail(TM_EINVAL, "null output");
+    CK(cudaSetDevice(s->device));
+    CK(cudaStreamSynchronize(s->stream));
+    const colony_host &c = s->cols[id];
+    const tm_arrays a = view(s, s->parity);
+    if ((rc = unsort_to_host(s, (const double *)a.x, c, out->x))) return rc;
+    if ((rc = unsort_to_host(s, (const double *)a.y, c, out->y))) return rc;
+    if ((rc = unsort_to_host(s, (const double *)a.z, c, out->z))) return rc;
+    if ((rc = unsort_to_host(s, (const double *)a.density, c, out->density))) return rc;
+    if ((rc = unsort_to_host(s, (const double *)a.v, c, out->v))) return rc;
+    if ((rc = unsort_to_host(s, (const double *)a.mindist, c, out->mindist))) return rc;
+    if ((rc = unsort_to_host(s, (const double *)a.fx, c, out->fx))) return rc;
+    if ((rc = unsort_to_host(s, (const double *)a.fy, c, out->fy))) return rc;
+    if ((rc = unsort_to_host(s, (const double *)a.fz, c, out->fz))) return rc;
+    if ((rc = unsort_to_host(s, (const unsigned char *)a.rem, c, out->removecell))) return rc;
+    if ((rc = unsort_to_host(s, (const int32_t *)a.nbcount, c, out->nbcount))) return rc;
+    if (a.nbhash && (rc = unsort_to_host(s, (const unsigned long long *)a.nbhash, c,
+                                         (unsigned long long *)out->nbhash)))
+        return rc;
+    if (a.vcand && (rc = unsort_to_host(s, (const int32_t *)a.vcand, c, out->vcand))) return rc;
+    if (out->grid && c.gridoff >= 0)
+        CK(cudaMemcpy(out->grid, a.grid + c.gridoff, sizeof(double) * (size_t)c.ngrid, cudaMemcpyDeviceToHost));
+    return TM_OK;
+}
+
+extern "C" int tm_colony_stats(tm_session *s, int id, tm_colony_info *st)
+{
+    int rc = lookup(s, id);
+    if (rc) return rc;
+    if (!st) return tm_fail(TM_EINVAL, "null output");
+    CK(cudaSetDevice(s->device));
+    const colony_host &c = s->cols[id];
+    const tm_arrays a = view(s, s->parity);
+    CK(cudaMemsetAsync(s->d_octsize + id, 0, sizeof(unsigned long long), s->stream));
+    k_octsize<<<blocks_for(a.nslots_total, 256), 256, 0, s->stream>>>(a, s->d_octsize);
+    CK(cudaGetLastError());
+    unsigned long long octs = 0;
+    CK(cudaMemcpyAsync(&octs, s->d_octsize + id, sizeof octs, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpyAsync(&s->h_frame[id], &a.frame[id], sizeof(tm_frame), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    const tm_frame &f = s->h_frame[id];
+    memset(st, 0, sizeof *st);
+    for (int k = 0; k < 3; k++) st->aff_shift[k] = f.shift[k];
+    st->aff_scale = f.scale;
+    st->octsize = c.n >= 2 ? (int64_t)(1 + octs) : (int64_t)c.n;
+    st->removecount = (int64_t)f.removecount;
+    for (int k = 0; k < 3; k++) {
+        st->patch_lower[k] = f.patch_lo[k];
+        st->patch_upper[k] = f.patch_hi[k];
+        st->grid_size[k] = c.gsize[k];
+    }
+    if (s->K.dim == 2) {
+        st->patch_lower[2] = 0;
+        st->patch_upper[2] = 0;
+    }
+    st->device_errors = f.error;
+    st->bin_level = f.L;
+    st->n = c.n;
+    return TM_OK;
+}

@@ -1,0 +1,258 @@
+"""Python binding of the device-resident session API (include/timothy_gb300.h).
+
+A thin ctypes layer over libtimothy_gb300.so: every call goes to the CUDA
+library; there is no Python or CPU implementation behind it.  If the library
+is missing, loading raises instead of falling back.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .colonies import CellTypes, Colony
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libtimothy_gb300.so")
+
+PREC = {"fp64": 0, "fp32c": 1}
+UPDATE = {"reference": 0, "dt": 1, "none": 2}
+
+
+class TimothyError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"timothy_gb300 error {code}: {msg}")
+        self.code = code
+
+
+class _CellTypes(C.Structure):
+    _fields_ = [("ntypes", C.c_int), ("h", C.c_void_p), ("h2", C.c_void_p), ("h3", C.c_void_p),
+                ("h4", C.c_void_p), ("size", C.c_void_p), ("randommove", C.c_void_p)]
+
+
+class _Config(C.Structure):
+    _fields_ = [("dimension", C.c_int), ("device", C.c_int), ("max_slots", C.c_int64), ("max_colonies", C.c_int),
+                ("max_bin_entries", C.c_int64), ("max_grid_entries", C.c_int64), ("diagnostics", C.c_int)]
+
+
+class _Input(C.Structure):
+    _fields_ = [("n", C.c_int64), ("x", C.c_void_p), ("y", C.c_void_p), ("z", C.c_void_p), ("size", C.c_void_p),
+                ("young", C.c_void_p), ("ctype", C.c_void_p), ("phase", C.c_void_p)]
+
+
+class _Options(C.Structure):
+    _fields_ = [("precision", C.c_int), ("update_mode", C.c_int), ("dt", C.c_double), ("cic", C.c_int),
+                ("gfh", C.c_float), ("lcap", C.c_int)]
+
+
+class _Output(C.Structure):
+    _fields_ = [(k, C.c_void_p) for k in ("x", "y", "z", "density", "v", "mindist", "fx", "fy", "fz", "removecell",
+                                           "nbcount", "nbhash", "vcand", "grid")]
+
+
+class _Info(C.Structure):
+    _fields_ = [("aff_shift", C.c_double * 3), ("aff_scale", C.c_double), ("octsize", C.c_int64),
+                ("removecount", C.c_int64), ("patch_lower", C.c_int64 * 3), ("patch_upper", C.c_int64 * 3),
+                ("grid_size", C.c_int64 * 3), ("device_errors", C.c_uint32), ("bin_level", C.c_int),
+                ("n", C.c_int64)]
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH) -> C.CDLL:
+    """Load the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise FileNotFoundError(f"{path} missing: build it with `python -m timothy_gb300.build`")
+    lib = C.CDLL(path)
+    P = C.c_void_p
+    sigs = {
+        "tm_last_error": (C.c_char_p, []),
+        "tm_version": (C.c_char_p, []),
+        "tm_device_count": (C.c_int, []),
+        "tm_session_create": (C.c_int, [C.POINTER(P), C.POINTER(_Config), C.POINTER(_CellTypes)]),
+        "tm_session_destroy": (C.c_int, [P]),
+        "tm_session_stream": (P, [P]),
+        "tm_colony_add": (C.c_int, [P, C.POINTER(_Input), C.POINTER(_Options), C.POINTER(C.c_int)]),
+        "tm_colony_remove": (C.c_int, [P, C.c_int]),
+        "tm_colony_upload": (C.c_int, [P, C.c_int, C.POINTER(_Input)]),
+        "tm_colony_set_active": (C.c_int, [P, C.c_int, C.c_int]),
+        "tm_colony_download": (C.c_int, [P, C.c_int, C.POINTER(_Output)]),
+        "tm_colony_stats": (C.c_int, [P, C.c_int, C.POINTER(_Info)]),
+        "tm_session_step": (C.c_int, [P, C.c_int]),
+        "tm_session_sync": (C.c_int, [P]),
+        "tm_session_use_graph": (C.c_int, [P, C.c_int]),
+        "tm_session_profile": (C.c_int, [P, C.c_int]),
+        "tm_session_profile_read": (C.c_int, [P, P, C.c_int, P]),
+        "tm_session_capacity": (C.c_int, [P, P, P, P]),
+    }
+    for name, (res, args) in sigs.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _check(rc: int):
+    if rc != 0:
+        raise TimothyError(rc, load_library().tm_last_error().decode())
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def device_count() -> int:
+    return int(load_library().tm_device_count())
+
+
+class Session:
+    """A set of colonies resident on one GPU."""
+
+    def __init__(self, types: CellTypes | None = None, *, dim: int = 3, max_slots: int = 1 << 16,
+                 max_colonies: int = 1, diagnostics: bool = False, device: int = 0, max_bin_entries: int = 0,
+                 max_grid_entries: int = 0):
+        lib = load_library()
+        self.types = types or CellTypes.consistent()
+        self._keep = [np.ascontiguousarray(a, dt) for a, dt in
+                      ((self.types.h, np.float64), (self.types.h2, np.float64), (self.types.h3, np.float64),
+                       (self.types.h4, np.float64), (self.types.size, np.float64),
+                       (self.types.randommove, np.float32))]
+        ct = _CellTypes(self.types.ntypes, *[_p(a) for a in self._keep])
+        cfg = _Config(dim, device, int(max_slots), int(max_colonies), int(max_bin_entries), int(max_grid_entries),
+                      1 if diagnostics else 0)
+        h = C.c_void_p()
+        _check(lib.tm_session_create(C.byref(h), C.byref(cfg), C.byref(ct)))
+        self._h = h
+        self.dim = dim
+        self.diagnostics = diagnostics
+        self._n = {}
+        self._grid = {}
+
+    # -- lifetime ---------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            load_library().tm_session_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        return int(load_library().tm_session_stream(self._h) or 0)
+
+    # -- colonies -----------------------------------------------------------
+    @staticmethod
+    def _input(col: Colony):
+        arrs = [np.ascontiguousarray(col.x, np.float64), np.ascontiguousarray(col.y, np.float64),
+                np.ascontiguousarray(col.z, np.float64), np.ascontiguousarray(col.size, np.float64),
+                np.ascontiguousarray(col.young, np.float32), np.ascontiguousarray(col.ctype, np.int32),
+                np.ascontiguousarray(col.phase, np.int32)]
+        return _Input(col.n, *[_p(a) for a in arrs]), arrs
+
+    def add_colony(self, col: Colony, *, precision: str = "fp64", update: str = "reference", dt: float = 1.0,
+                   cic: bool = False, gfh: float = 8.0, lcap: int = 0) -> int:
+        inp, keep = self._input(col)
+        opt = _Options(PREC[precision], UPDATE[update], float(dt), 1 if cic else 0, float(gfh), int(lcap))
+        cid = C.c_int(-1)
+        _check(load_library().tm_colony_add(self._h, C.byref(inp), C.byref(opt), C.byref(cid)))
+        self._n[cid.value] = col.n
+        if cic:
+            g = int((2049.0 + 1) / gfh) + 1
+            self._grid[cid.value] = (g, g, g if self.dim == 3 else 1)
+        return cid.value
+
+    def remove_colony(self, cid: int):
+        _check(load_library().tm_colony_remove(self._h, cid))
+        self._n.pop(cid, None)
+        self._grid.pop(cid, None)
+
+    def upload(self, cid: int, col: Colony):
+        inp, keep = self._input(col)
+        _check(load_library().tm_colony_upload(self._h, cid, C.byref(inp)))
+        self._n[cid] = col.n
+
+    def set_active(self, cid: int, active: bool):
+        _check(load_library().tm_colony_set_active(self._h, cid, 1 if active else 0))
+
+    # -- stepping -----------------------------------------------------------
+    def step(self, nsteps: int = 1):
+        _check(load_library().tm_session_step(self._h, int(nsteps)))
+
+    def sync(self):
+        _check(load_library().tm_session_sync(self._h))
+
+    def use_graph(self, on: bool = True):
+        _check(load_library().tm_session_use_graph(self._h, 1 if on else 0))
+
+    def profile(self, on: bool = True):
+        _check(load_library().tm_session_profile(self._h, 1 if on else 0))
+
+    def profile_read(self) -> dict:
+        ms = np.zeros(5)
+        steps = np.zeros(1, np.int64)
+        _check(load_library().tm_session_profile_read(self._h, _p(ms), 5, _p(steps)))
+        return {"build_ms": ms[0], "pair_ms": ms[1], "octree_ms": ms[2], "update_ms": ms[3], "cic_ms": ms[4],
+                "steps": int(steps[0])}
+
+    def capacity(self) -> dict:
+        fs = np.zeros(1, np.int64)
+        fb = np.zeros(1, np.int64)
+        fc = np.zeros(1, np.int32)
+        _check(load_library().tm_session_capacity(self._h, _p(fs), _p(fb), _p(fc)))
+        return {"free_slots": int(fs[0]), "free_bins": int(fb[0]), "free_colonies": int(fc[0])}
+
+    # -- results ------------------------------------------------------------
+    def download(self, cid: int, fields=None) -> dict:
+        n = self._n[cid]
+        want = fields or ("x", "y", "z", "density", "v", "mindist", "fx", "fy", "fz", "removecell", "nbcount")
+        out = {}
+        dtypes = {"removecell": np.uint8, "nbcount": np.int32, "nbhash": np.uint64, "vcand": np.int32}
+        for k in want:
+            if k == "grid":
+                continue
+            out[k] = np.zeros(n, dtypes.get(k, np.float64))
+        if "grid" in want and cid in self._grid:
+            out["grid"] = np.zeros(self._grid[cid])
+        o = _Output(*[_p(out.get(k)) for k, _ in _Output._fields_])
+        _check(load_library().tm_colony_download(self._h, cid, C.byref(o)))
+        return out
+
+    def stats(self, cid: int) -> dict:
+        info = _Info()
+        _check(load_library().tm_colony_stats(self._h, cid, C.byref(info)))
+        return {"aff": np.array(list(info.aff_shift) + [info.aff_scale]), "octsize": int(info.octsize),
+                "removecount": int(info.removecount), "patch_lower": list(info.patch_lower),
+                "patch_upper": list(info.patch_upper), "device_errors": int(info.device_errors),
+                "bin_level": int(info.bin_level), "n": int(info.n)}
+
+
+def run_colony(col: Colony, nsteps: int, *, precision: str = "fp64", update: str = "reference", dt: float = 1.0,
+               cic: bool = False, gfh: float = 8.0, diagnostics: bool = False, fields=None):
+    """Upload one colony, advance it nsteps, return (outputs, stats)."""
+    with Session(col.types, dim=col.dim, max_slots=max(col.n, 1) + 64, diagnostics=diagnostics) as s:
+        cid = s.add_colony(col, precision=precision, update=update, dt=dt, cic=cic, gfh=gfh)
+        s.step(nsteps)
+        s.sync()
+        f = fields
+        if f is None:
+            f = ["x", "y", "z", "density", "v", "mindist", "fx", "fy", "fz", "removecell", "nbcount"]
+            if diagnostics:
+                f += ["nbhash", "vcand"]
+            if cic:
+                f += ["grid"]
+        return s.download(cid, f), s.stats(cid)
