@@ -1,0 +1,369 @@
+#!/usr/bin/env python
+"""Benchmark of the Timothy cell-mechanics hot path on GB300.
+
+Prints ONE JSON line (rank 0).  Metric: cell-updates/s, where one cell-update
+is one cell advanced by one full step of the path (neighbour search + SPH
+density/potential + force + FP64 position update; plus the CIC deposit for the
+workload that has it).
+
+Workloads (seeded synthetic colonies; the reference ships no datasets):
+  precision16m  16,000,000 cells, clustered spheroid (seed 3), FP32 +
+                compensated path; the plain FP64 path runs on the same colony
+                and GPU for the ratio and the error report.  Default.
+  scale1m       1,000,000 cells, clustered spheroid (seed 2), plain FP64 path
+                with a CIC deposit onto a 257^3 FP64 grid each step.
+  uniform10k    10,000 cells uniform in a ball (seed 1), plain FP64 path.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload precision16m|scale1m|uniform10k]
+Under torchrun each rank runs an independent replica (the path has no
+cross-colony exchange), so scaling is weak and value is the total over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from timothy_gb300 import colonies as C  # noqa: E402
+
+METRIC = "cell-updates/s at 16M cells (FP64 vs FP32+comp, same GPU); p50/p99 latency"
+UNIT = "cell-updates/s"
+# Algorithmic bytes per cell-update: reads x,y,z,size (4x8) + young (4) + ctype (4);
+# writes density, v, mindist, Fx, Fy, Fz, x, y, z (9x8).  The CIC workload adds
+# the phase (4) per cell and one write of the grid per step.
+B_CELL = 112
+# Colony radii giving a mean of 40 neighbours within h = 2.5 (bisected with
+# full-size neighbour counts; the bench reports the measured mean each run).
+RADIUS = {
+    ("uniform", 10_000, 1): 15.256856463570728,
+    ("clustered", 1_000_000, 2): 76.3271427172167,
+    ("clustered", 16_000_000, 3): 192.68257233787858,
+}
+WORKLOADS = {
+    "precision16m": dict(kind="clustered", n=16_000_000, seed=3, precision="fp32c", cic=False, dt=0.01),
+    "scale1m": dict(kind="clustered", n=1_000_000, seed=2, precision="fp64", cic=True, dt=0.01),
+    "uniform10k": dict(kind="uniform", n=10_000, seed=1, precision="fp64", cic=False, dt=0.01),
+}
+
+
+def radius_for(kind, n, seed):
+    """Calibrated radius, or the calibrated one of the same generator scaled by n^(1/3)."""
+    r = RADIUS.get((kind, n, seed))
+    if r is None:
+        base = {"uniform": (10_000, RADIUS[("uniform", 10_000, 1)]),
+                "clustered": (1_000_000, RADIUS[("clustered", 1_000_000, 2)])}[kind]
+        r = base[1] * (n / base[0]) ** (1 / 3)
+    return r
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=2)
+        except Exception:
+            self.proc.kill()
+        rows = self.rows
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, nm in enumerate(names):
+                if r[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(rows),
+                "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit())
+                if any(r[3].replace(".", "").isdigit() for r in rows) else None}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl"
+        try:
+            import torch
+
+            torch.cuda.set_device(local)
+        except Exception:
+            backend = "gloo"
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return world, rank, local, pg
+
+
+def dist_max(pg, value: float) -> float:
+    if pg is None:
+        return value
+    import torch
+
+    dev = "cuda" if pg.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def cpu_sample(workload, threads=0, seconds_cap=30.0):
+    """Time the CPU implementation of the path on a bounded sample of the workload."""
+    from oracle import bindings
+
+    kind = workload["kind"]
+    n = min(workload["n"], 1_000_000 if kind == "clustered" else workload["n"])
+    seed = workload["seed"]
+    col = C.make_colony(kind, n, seed, radius_for(kind, n, seed))
+    which = "ref" if bindings.available("ref") else "oracle"
+    try:
+        bindings.load(which)
+    except OSError:
+        which = "oracle"
+    if which == "oracle" and not bindings.available("oracle"):
+        bindings.build(ref=False)
+    threads = threads or os.cpu_count() or 1
+    steps = 1
+    t0 = time.perf_counter()
+    kw = dict(which=which, update_mode=1, dt=workload["dt"], cic=workload["cic"])
+    if which == "oracle":
+        kw["nthreads"] = threads
+    else:
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+    bindings.run(col, steps, **kw)
+    dt = time.perf_counter() - t0
+    return {"value": n * steps / dt, "unit": UNIT, "cores": threads,
+            "kind": "reference" if which == "ref" else "port",
+            "sample": f"{n} cells of the {kind} generator (seed {seed}), {steps} step, {dt:.2f} s"}
+
+
+def run_reference_arm(args, workload):
+    world, rank, local, pg = dist_setup()
+    if rank != 0:
+        return
+    samples = []
+    cb = None
+    for _ in range(args.warmup):
+        cpu_sample(workload)
+    for _ in range(args.steps):
+        cb = cpu_sample(workload)
+        samples.append(cb["value"])
+    value = float(np.mean(samples))
+    cb["value"] = value
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": args.workload, **{k: workload[k] for k in ("kind", "n", "seed")}},
+            "cpu_baseline": cb, "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                                        "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="precision16m", choices=sorted(WORKLOADS))
+    ap.add_argument("--n", type=int, default=0, help="override the cell count")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    wl = dict(WORKLOADS[args.workload])
+    if args.n:
+        wl["n"] = args.n
+    if args.impl == "reference":
+        return run_reference_arm(args, wl)
+
+    world, rank, local, pg = dist_setup()
+    from timothy_gb300 import session as S
+
+    kind, n, seed = wl["kind"], wl["n"], wl["seed"]
+    radius = radius_for(kind, n, seed)
+    col = C.make_colony(kind, n, seed, radius)
+    prec = wl["precision"]
+
+    def new_session(p):
+        s = S.Session(col.types, dim=3, max_slots=n + 64, device=local)
+        cid = s.add_colony(col, precision=p, update="dt", dt=wl["dt"], cic=wl["cic"])
+        return s, cid
+
+    s, cid = new_session(prec)
+    s.step(args.warmup)
+    s.sync()
+    nbc = s.download(cid, ["nbcount"])["nbcount"]
+    mean_nb, max_nb = float(nbc.mean()), int(nbc.max())
+    s.profile(True)
+    clocks = ClockSampler(local)
+    clocks.start()
+    dist_barrier(pg)
+    l0 = s.launches
+    s.timer_start()
+    s.step(args.steps)
+    ms = s.timer_stop()
+    launches = s.launches - l0
+    clk = clocks.stop()
+    s.sync()
+    prof = s.profile_read()
+    s.profile(False)
+    ms_max = dist_max(pg, ms)
+    ms_per_step = ms_max / args.steps
+    value = n * world * args.steps / (ms_max * 1e-3)
+
+    peak, peak_kind = measured_peaks()
+    pair_ms = prof["pair_ms"]
+    achieved = B_CELL * n / (pair_ms * 1e-3) / 1e9 if pair_ms > 0 else None
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak if achieved else None, "traffic": None, "peak_source": peak_kind,
+                "kernel": "k_pair<%d>" % (1 if prec == "fp32c" else 0),
+                "kernel_ms": pair_ms, "phases_ms": {k: prof[k] for k in ("build_ms", "pair_ms", "octree_ms",
+                                                                          "update_ms", "cic_ms")}}
+    out_fast = s.download(cid, ["x", "y", "z", "density", "fx", "fy", "fz"]) if prec == "fp32c" else None
+
+    # end to end through the public API with host buffers: per step the cells go
+    # host -> device, one step runs, the step's results come back
+    e2e = None
+    if not args.no_e2e:
+        host = [np.ascontiguousarray(a).copy() for a in (col.x, col.y, col.z, col.size, col.young, col.ctype,
+                                                             col.phase)]
+        fields = ["x", "y", "z", "density", "v", "mindist", "fx", "fy", "fz", "removecell"]
+        res = {k: np.zeros(n, np.uint8 if k == "removecell" else np.float64) for k in fields}
+        pinned = host + list(res.values())
+        for a in pinned:
+            S.host_register(a)
+        ecol = C.Colony(*host, col.types, 3)
+        ke = max(2, min(args.steps, 5))
+        s.upload(cid, ecol)
+        s.step(1)
+        s.sync()
+        s.timer_start()
+        for _ in range(ke):
+            s.upload(cid, ecol)
+            s.step(1)
+            s.download(cid, fields, out=res)
+        ems = s.timer_stop()
+        for a in pinned:
+            S.host_unregister(a)
+        ems = dist_max(pg, ems)
+        e2e = {"value": n * world * ke / (ems * 1e-3), "unit": UNIT, "h2d_bytes_per_step": n * 44,
+               "d2h_bytes_per_step": n * 73, "steps": ke, "ms_per_step": ems / ke,
+               "api": "tm_colony_upload + tm_session_step + tm_colony_download"}
+    s.close()
+
+    extra = {}
+    if prec == "fp32c" and not args.no_fp64:
+        # plain FP64 path on the same colony and GPU: rate and the error of the
+        # compensated path against it after the same number of steps
+        s64, c64 = new_session("fp64")
+        s64.step(args.warmup)
+        s64.sync()
+        k64 = max(2, min(args.steps, 5))
+        s64.timer_start()
+        s64.step(k64)
+        ms64 = s64.timer_stop()
+        rest = args.steps - k64
+        if rest > 0:
+            s64.step(rest)
+        s64.sync()
+        ref = s64.download(c64, ["x", "y", "z", "density", "fx", "fy", "fz"])
+        s64.close()
+        ms64 = dist_max(pg, ms64)
+        v64 = n * world * k64 / (ms64 * 1e-3)
+        pos = ref["density"] > 0
+        drel = np.abs(out_fast["density"][pos] - ref["density"][pos]) / ref["density"][pos]
+        f64 = np.stack([ref["fx"], ref["fy"], ref["fz"]])
+        f32 = np.stack([out_fast["fx"], out_fast["fy"], out_fast["fz"]])
+        fscale = np.max(np.abs(f64))
+        ferr = np.abs(f32 - f64) / fscale
+        xerr = np.max([np.max(np.abs(out_fast[k] - ref[k])) for k in ("x", "y", "z")])
+        extra["fp64"] = {"value": v64, "ms_per_step": ms64 / k64, "steps": k64}
+        extra["fp32c_over_fp64"] = value / v64
+        extra["error_vs_fp64"] = {
+            "steps": args.warmup + args.steps, "density_max_rel": float(drel.max()),
+            "density_rms_rel": float(np.sqrt(np.mean(drel ** 2))), "force_max_rel_to_max": float(ferr.max()),
+            "force_rms_rel_to_max": float(np.sqrt(np.mean(ferr ** 2))), "position_max_abs": float(xerr)}
+
+    cpu = None
+    if not args.no_cpu and rank == 0 and world == 1:
+        cpu = cpu_sample(wl)
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+kahan (f64 positions)" if prec == "fp32c" else "f64",
+            "data": "synthetic",
+            "config": {"workload": args.workload, "kind": kind, "cells": n, "seed": seed, "radius": radius,
+                       "h": 2.5, "dt": wl["dt"], "cic": wl["cic"], "precision": prec,
+                       "mean_neighbours": mean_nb, "max_neighbours": max_nb,
+                       "l2": "inputs larger than L2 (state %.1f GB)" % (n * 250 / 1e9),
+                       "parallelism": f"replicas x{world}"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk}
+    line.update(extra)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -137,6 +137,18 @@ int tm_session_use_graph(tm_session *s, int on);
 int tm_session_profile(tm_session *s, int on);
 int tm_session_profile_read(tm_session *s, double *ms, int nphase, int64_t *steps);
 
+/* Device timer on the session stream: op 0 records the start event; op 1
+ * records the stop event, waits for it and writes the elapsed milliseconds. */
+int tm_session_timer(tm_session *s, int op, double *ms);
+
+/* Number of kernels the session has launched (graph replays included). */
+int64_t tm_session_launches(tm_session *s);
+
+/* Page-lock caller memory so host<->device copies run at full speed
+ * (cudaHostRegister); tm_host_unregister undoes it. */
+int tm_host_register(void *ptr, int64_t bytes);
+int tm_host_unregister(void *ptr);
+
 /* Slots and memory still free (admission control). */
 int tm_session_capacity(tm_session *s, int64_t *free_slots, int64_t *free_bins, int *free_colonies);
 

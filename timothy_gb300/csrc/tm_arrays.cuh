@@ -51,6 +51,8 @@ struct tm_arrays {
     uint32_t *bin_count, *bin_cursor, *bin_start;
     long long nbin_total;
     int *bigbins;
+    int *fix_count;      // cells whose FP32 density is redone in FP64
+    int *fix_list;
     // outputs (Morton order)
     double *density, *v, *mindist, *fx, *fy, *fz;
     int *nbcount;

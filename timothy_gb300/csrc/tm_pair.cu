@@ -40,8 +40,8 @@ struct pair_acc<0> {
 template <>
 struct pair_acc<1> {
     kahan dens, fx, fy, fz;
-    float mins;
-    __device__ void init() { dens.init(); fx.init(); fy.init(); fz.init(); mins = 3.0e38f; }
+    float mins, err2;
+    __device__ void init() { dens.init(); fx.init(); fy.init(); fz.init(); mins = 3.0e38f; err2 = 0.0f; }
 };
 
 template <int PREC>
@@ -169,10 +169,11 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
                 }
                 if (in) {
                     acc.mins = fminf(acc.mins, s);
+                    const float dist = sqrtf(s);
                     const float rs = s > 0.0f ? rsqrtf(s) : 0.0f;
-                    const float dist = s * rs;
                     const float u = dist * T.inv_hf;
-                    const float omu = 1.0f - u;
+                    // 1 - u as (h - dist) / h: the subtraction is exact near the cutoff
+                    const float omu = (T.hf - dist) * T.inv_hf;
                     float wk, wg;
                     if (u <= 0.5f) {
                         wk = T.cWf * fmaf(6.0f * u * u, u - 1.0f, 1.0f);
@@ -181,7 +182,12 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
                         wk = T.cWf * (2.0f * omu * omu * omu);
                         wg = -omu * omu;
                     }
-                    acc.dens.add(T.kmassf * hj.w * wk);
+                    const float term = T.kmassf * hj.w * wk;
+                    acc.dens.add(term);
+                    // one-sigma rounding estimate of this term: W ~ (1-u)^3 amplifies
+                    // the FP32 error of (1 - u) near the cutoff
+                    const float ek = term * fmaf(1.0e-7f, __frcp_rn(fmaxf(omu, 1.0e-3f)), 1.2e-7f);
+                    acc.err2 = fmaf(ek, ek, acc.err2);
                     const float g = wg * T.cGf * rs;
                     acc.fx.add(g * dx);
                     acc.fy.add(g * dy);
@@ -252,7 +258,14 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
         a.fy[i] = acc.fy;
         a.fz[i] = acc.fz;
     } else {
-        a.density[i] = (double)acc.dens.value();
+        const float rho = acc.dens.value();
+        a.density[i] = (double)rho;
+        // cells whose estimated relative density error exceeds 3e-7 (almost only
+        // cells whose neighbours all sit near the cutoff) are redone in FP64
+        if (acc.err2 > 9.0e-14f * rho * rho) {
+            const int q = atomicAdd(a.fix_count, 1);
+            a.fix_list[q] = (int)i;
+        }
         a.mindist[i] = cnt_nb ? (double)sqrtf(acc.mins) : 1.7976931348623157e308;
         a.fx[i] = (double)acc.fx.value();
         a.fy[i] = (double)acc.fy.value();
@@ -262,6 +275,56 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
     if (a.want_diag) a.nbhash[i] = hash;
 }
 
+// FP64 density of the cells flagged by the FP32 path: the same neighbour set
+// (exact FP64 cutoff) and the reference expression of potential.c:62.
+__global__ void __launch_bounds__(128) k_density_fix64(tm_arrays a, const tm_consts *K)
+{
+    const int nfix = *a.fix_count;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nfix; q += gridDim.x * blockDim.x) {
+        const long long i = a.fix_list[q];
+        const int c = a.col[i];
+        const tm_desc &d = a.desc[c];
+        const tm_frame &f = a.frame[c];
+        const tm_type &T = K->t[a.ctype[i]];
+        const double xi = a.x[i], yi = a.y[i], zi = a.z[i];
+        const int nside = 1 << f.L;
+        int lo[3], hi[3];
+        const double pos[3] = {xi, yi, zi};
+        for (int k = 0; k < 3; k++) {
+            const float v0 = ((float)pos[k] - f.shiftf[k] - (float)T.h) * f.binscale - 0.01f;
+            const float v1 = ((float)pos[k] - f.shiftf[k] + (float)T.h) * f.binscale + 0.01f;
+            lo[k] = max(0, min(nside - 1, (int)floorf(v0)));
+            hi[k] = max(0, min(nside - 1, (int)floorf(v1)));
+        }
+        const uint32_t *bst = a.bin_start + d.binoff;
+        double dens = 0.0;
+        for (int bz = lo[2]; bz <= hi[2]; bz++)
+            for (int by = lo[1]; by <= hi[1]; by++)
+                for (int bx = lo[0]; bx <= hi[0]; bx++) {
+                    const uint32_t m = tm_morton((uint32_t)bx, (uint32_t)by, (uint32_t)bz);
+                    const long long j0 = f.bin_base + bst[m], j1 = f.bin_base + bst[m + 1];
+                    for (long long j = j0; j < j1; j++) {
+                        if (j == i) continue;
+                        const double dx = sub64(xi, a.x[j]), dy = sub64(yi, a.y[j]), dz = sub64(zi, a.z[j]);
+                        const double dist = __dsqrt_rn(add64(add64(mul64(dx, dx), mul64(dy, dy)), mul64(dz, dz)));
+                        if (!(dist <= T.h)) continue;
+                        const double u = div64(dist, T.h);
+                        double wk;
+                        if (u <= 0.5) {
+                            const double six_uu = mul64(mul64(6.0, u), u);
+                            wk = mul64(T.cW, add64(sub64(1.0, six_uu), mul64(six_uu, u)));
+                        } else {
+                            const double omu = sub64(1.0, u);
+                            wk = mul64(T.cW, mul64(mul64(mul64(2.0, omu), omu), omu));
+                        }
+                        const double mj = mul64(T.sc, div64(a.size[j], T.csize));
+                        dens = add64(dens, mul64(mj, (double)__double2float_rn(wk)));
+                    }
+                }
+        a.density[i] = dens;
+    }
+}
+
 cudaError_t tm_launch_pair(const tm_arrays &a, const tm_consts *K, int prec, cudaStream_t st)
 {
     long long warps = a.nslots_total / 32;
@@ -269,7 +332,11 @@ cudaError_t tm_launch_pair(const tm_arrays &a, const tm_consts *K, int prec, cud
     int bt = TM_WARPS_PER_BLOCK * 32;
     unsigned grid = (unsigned)((threads + bt - 1) / bt);
     if (grid == 0) return cudaSuccess;
-    if (prec == 0) k_pair<0><<<grid, bt, 0, st>>>(a, K);
-    else k_pair<1><<<grid, bt, 0, st>>>(a, K);
+    if (prec == 0) {
+        k_pair<0><<<grid, bt, 0, st>>>(a, K);
+    } else {
+        k_pair<1><<<grid, bt, 0, st>>>(a, K);
+        k_density_fix64<<<256, 128, 0, st>>>(a, K);
+    }
     return cudaGetLastError();
 }

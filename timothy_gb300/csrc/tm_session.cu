@@ -127,6 +127,9 @@ struct tm_session {
     bool graph_valid[2] = {false, false};
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};
     int parity = 0;   // 0: A.x is current, 1: A.x2 is current
+    long long launches = 0;
+    int kernels_per_step = 0;
+    cudaEvent_t tstart = nullptr, tstop = nullptr;
 };
 
 // ---------------------------------------------------------------------------
@@ -201,19 +204,30 @@ static void mark(tm_session *s)
     if (e) cudaEventRecord(e, s->stream);
 }
 
-// one full step for buffer parity p; the result is current in parity 1 - p
-static int enqueue_step(tm_session *s, int p)
+static void colony_mix(const tm_session *s, bool &any_cic, bool &any64, bool &any32)
+{
+    any_cic = any64 = any32 = false;
+    for (auto &c : s->cols) {
+        if (!c.used || !c.active) continue;
+        if (c.gridoff >= 0) any_cic = true;
+        if (c.opt.precision == TM_PREC_FP64) any64 = true;
+        else any32 = true;
+    }
+}
+
+// Build phase for buffer parity p (octbuild): frames, codes, counting sort,
+// gather.  Afterwards the Morton-ordered buffers (parity 1 - p) are current.
+static int enqueue_build(tm_session *s, int p, int &nk)
 {
     cudaStream_t st = s->stream;
     tm_arrays a = view(s, p);
     const long long nsl = a.nslots_total;
     const long long nbin = s->bins.hwm;
     const int ncol = a.ncol;
-    if (nsl == 0 || ncol == 0) return TM_OK;
-    mark(s);
     CK(cudaMemsetAsync(a.bin_count, 0, (size_t)(nbin + 1) * sizeof(uint32_t), st));
     CK(cudaMemsetAsync(a.bin_cursor, 0, (size_t)(nbin + 1) * sizeof(uint32_t), st));
     CK(cudaMemsetAsync(a.bigbins, 0, sizeof(int), st));
+    CK(cudaMemsetAsync(a.fix_count, 0, sizeof(int), st));
     k_step_init<<<blocks_for(ncol, 128), 128, 0, st>>>(a);
     k_bbox<<<blocks_for(nsl, 256), 256, 0, st>>>(a, s->K.ntypes);
     k_frame<<<blocks_for(ncol, 128), 128, 0, st>>>(a, s->dK);
@@ -226,28 +240,67 @@ static int enqueue_step(tm_session *s, int p)
     k_binsort_big<<<64, 256, 0, st>>>(a);
     k_gather<<<blocks_for(nsl, 256), 256, 0, st>>>(a, s->dK);
     CK(cudaGetLastError());
-    mark(s);
-    // from here on the gathered (Morton-ordered) buffers are current
-    tm_arrays b = view(s, 1 - p);
-    bool any_cic = false, any64 = false, any32 = false;
-    for (auto &c : s->cols) {
-        if (!c.used || !c.active) continue;
-        if (c.gridoff >= 0) any_cic = true;
-        if (c.opt.precision == TM_PREC_FP64) any64 = true;
-        else any32 = true;
+    nk += 12;   // step_init, bbox, frame, codes, 3 scan passes, binbase, scatter, 2 bin sorts, gather
+    return TM_OK;
+}
+
+// CIC deposit of the current positions (patches_cells2envinfo)
+static int enqueue_cic(tm_session *s, int &nk)
+{
+    bool any_cic, any64, any32;
+    colony_mix(s, any_cic, any64, any32);
+    if (!any_cic) return TM_OK;
+    tm_arrays b = view(s, s->parity);
+    CK(cudaMemsetAsync(b.grid, 0, (size_t)s->grids.hwm * sizeof(double), s->stream));
+    CK(tm_launch_cic(b, s->dK, s->stream));
+    nk++;
+    return TM_OK;
+}
+
+// pair kernel(s) and octree walk on the current (sorted) buffers
+static int enqueue_compute(tm_session *s, int &nk, bool with_marks)
+{
+    bool any_cic, any64, any32;
+    colony_mix(s, any_cic, any64, any32);
+    tm_arrays b = view(s, s->parity);
+    if (any64) {
+        CK(tm_launch_pair(b, s->dK, 0, s->stream));
+        nk++;
     }
-    if (any_cic) {
-        CK(cudaMemsetAsync(b.grid, 0, (size_t)s->grids.hwm * sizeof(double), st));
-        CK(tm_launch_cic(b, s->dK, st));
+    if (any32) {
+        CK(tm_launch_pair(b, s->dK, 1, s->stream));
+        nk += 2;
     }
+    if (with_marks) mark(s);
+    CK(tm_launch_octree(b, s->dK, s->stream));
+    nk++;
+    return TM_OK;
+}
+
+static int enqueue_update(tm_session *s, int &nk)
+{
+    tm_arrays b = view(s, s->parity);
+    CK(tm_launch_update(b, s->dK, s->stream));
+    nk++;
+    return TM_OK;
+}
+
+// one full step; the parity flips inside (after the build phase)
+static int enqueue_step(tm_session *s)
+{
+    if (s->slots.hwm == 0 || s->cols.empty()) return TM_OK;
+    int nk = 0, rc;
     mark(s);
-    if (any64) CK(tm_launch_pair(b, s->dK, 0, st));
-    if (any32) CK(tm_launch_pair(b, s->dK, 1, st));
+    if ((rc = enqueue_build(s, s->parity, nk))) return rc;
+    s->parity ^= 1;
     mark(s);
-    CK(tm_launch_octree(b, s->dK, st));
+    if ((rc = enqueue_cic(s, nk))) return rc;
     mark(s);
-    CK(tm_launch_update(b, s->dK, st));
+    if ((rc = enqueue_compute(s, nk, true))) return rc;
     mark(s);
+    if ((rc = enqueue_update(s, nk))) return rc;
+    mark(s);
+    s->kernels_per_step = nk;
     return TM_OK;
 }
 
@@ -356,6 +409,7 @@ extern "C" int tm_session_create(tm_session **out, const tm_session_config *cfg,
     AL(a.col, S) AL(a.code, S) AL(a.codes, S) AL(a.bin, S) AL(a.tmp, S) AL(a.hi, S) AL(a.lo, S)
     AL(a.mass, S * K.ntypes)
     AL(a.bin_count, B + 1) AL(a.bin_cursor, B + 1) AL(a.bin_start, B + 1) AL(a.bigbins, 2 * (S / 33) + 4)
+    AL(a.fix_count, 1) AL(a.fix_list, S)
     AL(a.density, S) AL(a.v, S) AL(a.mindist, S) AL(a.fx, S) AL(a.fy, S) AL(a.fz, S) AL(a.nbcount, S)
     AL(a.grid, G) AL(a.desc, C) AL(a.frame, C)
     AL(s->scan_tmp, tm_scan_tmp_words(B + 1)) AL(s->d_octsize, C) AL(s->dK, 1)
@@ -399,12 +453,14 @@ extern "C" int tm_session_destroy(tm_session *s)
     tm_arrays &a = s->A;
     void *ptrs[] = {a.x, a.y, a.z, a.size, a.young, a.ctype, a.phase, a.perm, a.rem, a.x2, a.y2, a.z2, a.size2,
                     a.young2, a.ctype2, a.phase2, a.perm2, a.rem2, a.col, a.code, a.codes, a.bin, a.tmp, a.hi, a.lo,
-                    a.mass, a.bin_count, a.bin_cursor, a.bin_start, a.bigbins, a.density, a.v, a.mindist, a.fx,
+                    a.mass, a.bin_count, a.bin_cursor, a.bin_start, a.bigbins, a.fix_count, a.fix_list, a.density, a.v, a.mindist, a.fx,
                     a.fy, a.fz, a.nbcount, a.nbhash, a.vcand, a.grid, a.desc, a.frame, s->scan_tmp, s->d_octsize,
                     s->dK, s->d_scratch};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (auto ev : s->evpool) cudaEventDestroy(ev);
+    if (s->tstart) cudaEventDestroy(s->tstart);
+    if (s->tstop) cudaEventDestroy(s->tstop);
     if (s->h_desc) cudaFreeHost(s->h_desc);
     if (s->h_frame) cudaFreeHost(s->h_frame);
     if (s->stream) cudaStreamDestroy(s->stream);
@@ -636,7 +692,8 @@ static int run_step_graph(tm_session *s)
     if (!s->graph_valid[p]) {
         cudaGraph_t g;
         CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
-        int rc = enqueue_step(s, p);
+        int rc = enqueue_step(s);   // flips s->parity while recording
+        s->parity = p;
         cudaError_t e = cudaStreamEndCapture(s->stream, &g);
         if (rc) return rc;
         if (e != cudaSuccess) return tm_fail(TM_ECUDA, "graph capture: %s", cudaGetErrorString(e));
@@ -646,6 +703,7 @@ static int run_step_graph(tm_session *s)
         s->graph_valid[p] = true;
     }
     CK(cudaGraphLaunch(s->gexec[p], s->stream));
+    s->parity ^= 1;
     return TM_OK;
 }
 
@@ -654,9 +712,9 @@ extern "C" int tm_session_step(tm_session *s, int nsteps)
     if (!s || nsteps < 0) return tm_fail(TM_EINVAL, "bad arguments");
     CK(cudaSetDevice(s->device));
     for (int k = 0; k < nsteps; k++) {
-        int rc = (s->use_graph && !s->prof) ? run_step_graph(s) : enqueue_step(s, s->parity);
+        int rc = (s->use_graph && !s->prof) ? run_step_graph(s) : enqueue_step(s);
         if (rc) return rc;
-        s->parity ^= 1;
+        s->launches += s->kernels_per_step;
         if (s->prof) s->prof_steps++;
     }
     return TM_OK;
@@ -812,5 +870,39 @@ extern "C" int tm_colony_stats(tm_session *s, int id, tm_colony_info *st)
     st->device_errors = f.error;
     st->bin_level = f.L;
     st->n = c.n;
+    return TM_OK;
+}
+
+extern "C" int tm_session_timer(tm_session *s, int op, double *ms)
+{
+    if (!s) return tm_fail(TM_EINVAL, "null session");
+    CK(cudaSetDevice(s->device));
+    if (!s->tstart) CK(cudaEventCreate(&s->tstart));
+    if (!s->tstop) CK(cudaEventCreate(&s->tstop));
+    if (op == 0) {
+        CK(cudaEventRecord(s->tstart, s->stream));
+        return TM_OK;
+    }
+    CK(cudaEventRecord(s->tstop, s->stream));
+    CK(cudaEventSynchronize(s->tstop));
+    float t = 0.0f;
+    CK(cudaEventElapsedTime(&t, s->tstart, s->tstop));
+    if (ms) *ms = t;
+    return TM_OK;
+}
+
+extern "C" int64_t tm_session_launches(tm_session *s) { return s ? (int64_t)s->launches : 0; }
+
+extern "C" int tm_host_register(void *ptr, int64_t bytes)
+{
+    if (!ptr || bytes <= 0) return tm_fail(TM_EINVAL, "bad host range");
+    CK(cudaHostRegister(ptr, (size_t)bytes, cudaHostRegisterDefault));
+    return TM_OK;
+}
+
+extern "C" int tm_host_unregister(void *ptr)
+{
+    if (!ptr) return tm_fail(TM_EINVAL, "null pointer");
+    CK(cudaHostUnregister(ptr));
     return TM_OK;
 }

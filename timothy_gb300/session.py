@@ -88,6 +88,10 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "tm_session_profile": (C.c_int, [P, C.c_int]),
         "tm_session_profile_read": (C.c_int, [P, P, C.c_int, P]),
         "tm_session_capacity": (C.c_int, [P, P, P, P]),
+        "tm_session_timer": (C.c_int, [P, C.c_int, P]),
+        "tm_session_launches": (C.c_int64, [P]),
+        "tm_host_register": (C.c_int, [P, C.c_int64]),
+        "tm_host_unregister": (C.c_int, [P]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -104,6 +108,15 @@ def _check(rc: int):
 
 def _p(a):
     return None if a is None else a.ctypes.data
+
+
+def host_register(a: np.ndarray):
+    """Page-lock a numpy array for full-speed copies."""
+    _check(load_library().tm_host_register(a.ctypes.data, a.nbytes))
+
+
+def host_unregister(a: np.ndarray):
+    _check(load_library().tm_host_unregister(a.ctypes.data))
 
 
 def device_count() -> int:
@@ -209,6 +222,18 @@ class Session:
         return {"build_ms": ms[0], "pair_ms": ms[1], "octree_ms": ms[2], "update_ms": ms[3], "cic_ms": ms[4],
                 "steps": int(steps[0])}
 
+    def timer_start(self):
+        _check(load_library().tm_session_timer(self._h, 0, None))
+
+    def timer_stop(self) -> float:
+        ms = np.zeros(1)
+        _check(load_library().tm_session_timer(self._h, 1, _p(ms)))
+        return float(ms[0])
+
+    @property
+    def launches(self) -> int:
+        return int(load_library().tm_session_launches(self._h))
+
     def capacity(self) -> dict:
         fs = np.zeros(1, np.int64)
         fb = np.zeros(1, np.int64)
@@ -217,13 +242,14 @@ class Session:
         return {"free_slots": int(fs[0]), "free_bins": int(fb[0]), "free_colonies": int(fc[0])}
 
     # -- results ------------------------------------------------------------
-    def download(self, cid: int, fields=None) -> dict:
+    def download(self, cid: int, fields=None, out: dict | None = None) -> dict:
+        """Copy results to host arrays (caller order); ``out`` may supply them."""
         n = self._n[cid]
         want = fields or ("x", "y", "z", "density", "v", "mindist", "fx", "fy", "fz", "removecell", "nbcount")
-        out = {}
+        out = dict(out or {})
         dtypes = {"removecell": np.uint8, "nbcount": np.int32, "nbhash": np.uint64, "vcand": np.int32}
         for k in want:
-            if k == "grid":
+            if k == "grid" or k in out:
                 continue
             out[k] = np.zeros(n, dtypes.get(k, np.float64))
         if "grid" in want and cid in self._grid:
