@@ -80,6 +80,7 @@ typedef struct {
     int cic;                  /* deposit onto a grid each step */
     float gfh;                /* grid resolution (settings.gfh) */
     int lcap;                 /* deepest bin level, 0: from the colony's extent */
+    int64_t reserve;          /* slots to reserve (>= n) so later uploads can grow */
 } tm_colony_options;
 
 /* Outputs in caller order (host memory); any pointer may be NULL. */

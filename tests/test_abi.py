@@ -48,3 +48,41 @@ def test_version_and_device_count_callable_without_gpu(lib):
     assert b"sm_103a" in lib.tm_version()
     lib.tm_device_count.restype = ctypes.c_int
     assert lib.tm_device_count() >= 0
+
+
+def test_struct_layout_matches_reference_abi():
+    """The ctypes mirror and include/timothy_refabi.h keep the reference layout."""
+    import ctypes as C
+
+    from timothy_gb300 import refabi as R
+
+    for name, size in R.SIZES.items():
+        assert C.sizeof(getattr(R, name)) == size, name
+    cd = R.celldata_t
+    assert (cd.young.offset, cd.x.offset, cd.size.offset, cd.v.offset, cd.density.offset, cd.mindist.offset,
+            cd.ctype.offset) == (36, 48, 72, 80, 88, 96, 104)
+    assert (R.celltype_t.h.offset, R.celltype_t.size.offset, R.celltype_t.randommove.offset) == (160, 152, 360)
+
+
+def test_header_layout_compiles_to_reference_sizes(tmp_path):
+    """Compile include/timothy_refabi.h and compare with the reference's own structs when built here."""
+    import subprocess
+
+    src = tmp_path / "sz.c"
+    src.write_text('#include <stdio.h>\n#include "timothy_refabi.h"\nint main(void){printf("%zu %zu %zu %zu %zu '
+                   '%zu %zu %zu %zu\\n", sizeof(celldata_t), sizeof(cellsinfo_t), sizeof(celltype_t), '
+                   'sizeof(systeminfo_t), sizeof(settings_t), sizeof(cellcommdata_t), sizeof(grid_t), '
+                   'sizeof(patches_t), sizeof(octnode_t));return 0;}\n')
+    exe = tmp_path / "sz"
+    subprocess.run(["gcc", "-I", INCLUDE, str(src), "-o", str(exe)], check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    assert got[:6] == [112, 192, 368, 56, 336, 104]
+    from oracle import bindings
+
+    if bindings.available("ref"):
+        try:
+            lib = bindings.load("ref")
+        except OSError:
+            return
+        ref = [lib.ref_sizeof(k) for k in (0, 1, 2, 3, 4, 5, 6, 7, 8)]
+        assert got == ref

@@ -1,0 +1,286 @@
+/* Reference-signature drop-ins (include/timothy_refabi.h) on top of one
+ * device-resident colony.
+ *
+ * Flow of one reference step (main.c:67-79, step.c:41-100):
+ *   octbuild            cells (host AoS) -> device, Morton sort = implicit octree
+ *   patches_alloc       CIC deposit on the device + patch bounding box
+ *   patches_cells2envinfo  patch field 0 <- deposit
+ *   computepotential    pair kernel + octree walk; density/v/mindist -> host AoS
+ *   computegradient     forces (from the same fused pass) -> host
+ *   updatepositions     host forces -> device, x += F, positions + marks -> host
+ * The drop-ins assume, as the reference step loop guarantees, that the cells'
+ * positions are not changed by the host between octbuild and updatepositions.
+ */
+#include <stddef.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "timothy_refabi.h"
+#include "tm_dropin_api.h"
+
+double3dv_t affShift;
+double affScale;
+
+/* the host program's error exit (utils.c:103-109) when it has one */
+extern void terminate(systeminfo_t systeminfo, char *msg, char *file, int line) __attribute__((weak));
+
+static tm_session *g_sess;
+static int g_cid = -1;
+static int64_t g_cap;
+static int g_dim;
+static void *g_pinned;
+static size_t g_pinned_bytes;
+static systeminfo_t g_si;
+
+static void die(const char *what, int rc, int line)
+{
+    char msg[640];
+    snprintf(msg, sizeof msg, "timothy_gb300 %s failed (%d): %s", what, rc, tm_last_error());
+    if (terminate) terminate(g_si, msg, (char *)__FILE__, line);
+    fprintf(stderr, "error: %s (%s, line %d)\n", msg, __FILE__, line);
+    abort();
+}
+
+#define TRY(what, call)                                  \
+    do {                                                 \
+        int rc_ = (call);                                \
+        if (rc_ != TM_OK) die(what, rc_, __LINE__);      \
+    } while (0)
+
+static void pin_cells(celldata_t *cells, int64_t n)
+{
+    size_t bytes = (size_t)n * sizeof(celldata_t);
+    if ((void *)cells == g_pinned && bytes <= g_pinned_bytes) return;
+    if (g_pinned) tm_host_unregister(g_pinned);
+    g_pinned = NULL;
+    g_pinned_bytes = 0;
+    if (tm_host_register(cells, (int64_t)bytes) == TM_OK) {
+        g_pinned = cells;
+        g_pinned_bytes = bytes;
+    }
+}
+
+/* session with room for n cells and the colony's options */
+static void ensure_session(int64_t n, int dim)
+{
+    if (g_sess && n <= g_cap && dim == g_dim) return;
+    if (g_sess) {
+        tm_session_destroy(g_sess);
+        g_sess = NULL;
+    }
+    int64_t cap = g_cap > n ? g_cap : n;
+    if (cap < 1024) cap = 1024;
+    if (n > g_cap) cap = n + n / 4;
+    double one = 1.5, sz = 1.0;
+    tm_celltypes t = {1, &one, &one, &one, &one, &sz, NULL};
+    tm_session_config cfg;
+    memset(&cfg, 0, sizeof cfg);
+    cfg.dimension = dim;
+    cfg.device = 0;
+    cfg.max_slots = cap + 64;
+    cfg.max_colonies = 1;
+    TRY("session create", tm_session_create(&g_sess, &cfg, &t));
+    g_cap = cap;
+    g_dim = dim;
+    tm_colony_options opt;
+    memset(&opt, 0, sizeof opt);
+    opt.precision = TM_PREC_FP64;
+    opt.update_mode = TM_UPDATE_REFERENCE;
+    opt.dt = 1.0;
+    opt.gfh = 8.0f;
+    opt.lcap = 8;
+    opt.reserve = cap;
+    tm_colony_input in;
+    memset(&in, 0, sizeof in);
+    TRY("colony add", tm_colony_add(g_sess, &in, &opt, &g_cid));
+}
+
+static void push_types(const cellsinfo_t *ci, const celltype_t *celltype)
+{
+    int maxtype = 0;
+    TRY("cell types", tmi_max_ctype(g_sess, g_cid, &maxtype));
+    int nt = maxtype + 1;
+    if (nt > 8) die("more than 8 cell types", TM_EINVAL, __LINE__);
+    double h[8], h2[8], h3[8], h4[8], sz[8];
+    float rm[8];
+    for (int t = 0; t < nt; t++) {
+        h[t] = celltype[t].h;
+        h2[t] = celltype[t].h2;
+        h3[t] = celltype[t].h3;
+        h4[t] = celltype[t].h4;
+        sz[t] = celltype[t].size;
+        rm[t] = celltype[t].randommove;
+    }
+    tm_celltypes tt = {nt, h, h2, h3, h4, sz, rm};
+    TRY("dimension", tmi_set_dimension(g_sess, ci->dimension));
+    TRY("cell types", tmi_set_types(g_sess, &tt));
+}
+
+void octbuild(systeminfo_t systeminfo, cellsinfo_t *cellsinfo, celltype_t *celltype)
+{
+    g_si = systeminfo;
+    int64_t n = (int64_t)cellsinfo->localcount.n;
+    if (n == 0) return;                                /* octree.c:152-153 */
+    ensure_session(n, cellsinfo->dimension);
+    pin_cells(cellsinfo->cells, n);
+    tmi_aos_layout lay = {(int64_t)sizeof(celldata_t), offsetof(celldata_t, x), offsetof(celldata_t, y),
+                          offsetof(celldata_t, z), offsetof(celldata_t, size), offsetof(celldata_t, young),
+                          offsetof(celldata_t, ctype), offsetof(celldata_t, phase)};
+    TRY("upload", tmi_upload_aos(g_sess, g_cid, cellsinfo->cells, n, &lay));
+    push_types(cellsinfo, celltype);
+    TRY("build", tmi_phase(g_sess, 0));
+    tm_colony_info info;
+    TRY("stats", tm_colony_stats(g_sess, g_cid, &info));
+    if (info.device_errors) die("octree build", TM_EDEVICE, __LINE__);
+    affShift.x = info.aff_shift[0];
+    affShift.y = info.aff_shift[1];
+    affShift.z = info.aff_shift[2];
+    affScale = info.aff_scale;
+    cellsinfo->octree = NULL;                         /* the tree lives on the device */
+    cellsinfo->octsize = info.octsize;
+    cellsinfo->octmaxsize = n * 64;                   /* octree.c:193 */
+}
+
+void octfree(cellsinfo_t *cellsinfo)
+{
+    (void)cellsinfo;                                  /* device memory is reused next step */
+}
+
+void computepotential(systeminfo_t systeminfo, cellsinfo_t *cellsinfo, celltype_t *celltype,
+                      cellcommdata_t cellcommdata)
+{
+    (void)celltype;
+    (void)cellcommdata;
+    g_si = systeminfo;
+    if (cellsinfo->localcount.n <= 1) return;         /* potential.c:89 */
+    TRY("pair kernel", tmi_phase(g_sess, 1));
+    TRY("sync", tm_session_sync(g_sess));
+    TRY("download", tmi_download_aos3(g_sess, g_cid, cellsinfo->cells, (int64_t)sizeof(celldata_t),
+                                      offsetof(celldata_t, v), 0));
+}
+
+static void no_remote(systeminfo_t systeminfo, cellcommdata_t cellcommdata)
+{
+    if (cellcommdata.numimp <= 0) return;
+    g_si = systeminfo;
+    die("halo cells: the GB300 path runs one MPI rank", TM_EINVAL, __LINE__);
+}
+
+void computeremotepotential(systeminfo_t systeminfo, cellsinfo_t *cellsinfo, celltype_t *celltype,
+                            cellcommdata_t cellcommdata)
+{
+    (void)cellsinfo;
+    (void)celltype;
+    no_remote(systeminfo, cellcommdata);
+}
+
+void computegradient(systeminfo_t systeminfo, cellsinfo_t *cellsinfo, celltype_t *celltype,
+                     cellcommdata_t cellcommdata)
+{
+    (void)celltype;
+    (void)cellcommdata;
+    g_si = systeminfo;
+    if (cellsinfo->localcount.n <= 1) return;         /* potential.c:212 */
+    TRY("forces", tmi_download_forces(g_sess, g_cid, (double *)cellsinfo->forces));
+}
+
+void computeremotegradient(systeminfo_t systeminfo, cellsinfo_t *cellsinfo, celltype_t *celltype,
+                           cellcommdata_t cellcommdata)
+{
+    (void)cellsinfo;
+    (void)celltype;
+    no_remote(systeminfo, cellcommdata);
+}
+
+void updatepositions(settings_t settings, celltype_t *celltype, cellsinfo_t *cellsinfo, unsigned char *removecell,
+                     int64_t *removecount)
+{
+    (void)celltype;
+    int64_t n = (int64_t)cellsinfo->localcount.n;
+    if (n == 0 || !g_sess) return;
+    TRY("dimension", tmi_set_dimension(g_sess, settings.dimension));
+    TRY("forces", tmi_upload_forces(g_sess, g_cid, (const double *)cellsinfo->forces));
+    TRY("marks", tmi_upload_removecell(g_sess, g_cid, removecell));
+    TRY("update", tmi_phase(g_sess, 2));
+    TRY("sync", tm_session_sync(g_sess));
+    TRY("positions", tmi_download_aos3(g_sess, g_cid, cellsinfo->cells, (int64_t)sizeof(celldata_t),
+                                       offsetof(celldata_t, x), 1));
+    int64_t marked = 0;
+    TRY("marks", tmi_download_removecell(g_sess, g_cid, removecell, &marked));
+    *removecount += marked;
+}
+
+/* grid of this rank (grid.c:80-136): lower corner, resolution, index box */
+static void grid_setup(systeminfo_t si, const grid_t *grid, int dim)
+{
+    if (si.size != 1) die("CIC patches: the GB300 path runs one MPI rank", TM_EINVAL, __LINE__);
+    double lower[3] = {grid->lowercorner.x, grid->lowercorner.y, grid->lowercorner.z};
+    int64_t gs[3] = {grid->localsize.x, grid->localsize.y, dim == 3 ? grid->localsize.z : 1};
+    TRY("grid", tmi_set_cic(g_sess, g_cid, lower, grid->resolution, gs));
+}
+
+void patches_alloc(systeminfo_t systeminfo, settings_t settings, patches_t *patches, cellsinfo_t *cellsinfo,
+                   grid_t *grid)
+{
+    g_si = systeminfo;
+    int p, size = systeminfo.size;
+    patches->data = (double **)calloc((size_t)size, sizeof(double *));
+    patches->intersect = (int *)calloc((size_t)size, sizeof(int));
+    patches->lowercorner = (int643dv_t *)calloc((size_t)size, sizeof(int643dv_t));
+    patches->uppercorner = (int643dv_t *)calloc((size_t)size, sizeof(int643dv_t));
+    patches->lowercornerR = (int643dv_t *)calloc((size_t)size, sizeof(int643dv_t));
+    patches->uppercornerR = (int643dv_t *)calloc((size_t)size, sizeof(int643dv_t));
+    patches->size = (int643dv_t *)calloc((size_t)size, sizeof(int643dv_t));
+    for (p = 0; p < size; p++) {                      /* patches.c:61-78 */
+        patches->lowercorner[p].x = 2147483647;
+        patches->lowercorner[p].y = 2147483647;
+        patches->lowercorner[p].z = cellsinfo->dimension == 3 ? 2147483647 : 0;
+        patches->uppercorner[p].x = -2147483647 - 1;
+        patches->uppercorner[p].y = -2147483647 - 1;
+        patches->uppercorner[p].z = cellsinfo->dimension == 3 ? -2147483647 - 1 : 0;
+    }
+    if (cellsinfo->localcount.n == 0 || !g_sess) return;
+    grid_setup(systeminfo, grid, cellsinfo->dimension);
+    TRY("CIC", tmi_phase(g_sess, 3));
+    int64_t lo[3], hi[3];
+    TRY("patch box", tmi_patch_box(g_sess, g_cid, lo, hi));
+    if (hi[0] < lo[0]) return;                        /* no node touched */
+    patches->intersect[0] = 1;
+    patches->lowercorner[0].x = lo[0];
+    patches->lowercorner[0].y = lo[1];
+    patches->lowercorner[0].z = lo[2];
+    patches->uppercorner[0].x = hi[0];
+    patches->uppercorner[0].y = hi[1];
+    patches->uppercorner[0].z = hi[2];
+    patches->size[0].x = hi[0] - lo[0] + 1;           /* patches.c:134-145 */
+    patches->size[0].y = hi[1] - lo[1] + 1;
+    patches->size[0].z = cellsinfo->dimension == 3 ? hi[2] - lo[2] + 1 : 1;
+    patches->data[0] = (double *)calloc((size_t)(patches->size[0].x * patches->size[0].y * patches->size[0].z *
+                                                 settings.numberoffields),
+                                        sizeof(double));
+}
+
+void patches_cells2envinfo(systeminfo_t systeminfo, settings_t settings, patches_t *patches,
+                           cellsinfo_t *cellsinfo, grid_t *grid)
+{
+    (void)grid;
+    g_si = systeminfo;
+    if (!patches->intersect || !patches->intersect[0] || !g_sess || cellsinfo->localcount.n == 0) return;
+    const int64_t vol = patches->size[0].x * patches->size[0].y * patches->size[0].z;
+    memset(patches->data[0], 0, (size_t)(vol * settings.numberoffields) * sizeof(double));
+    int64_t lo[3] = {patches->lowercorner[0].x, patches->lowercorner[0].y, patches->lowercorner[0].z};
+    int64_t hi[3] = {patches->uppercorner[0].x, patches->uppercorner[0].y, patches->uppercorner[0].z};
+    if (settings.numberoffields > 0) TRY("patch", tmi_read_patch(g_sess, g_cid, lo, hi, patches->data[0]));
+}
+
+void tm_dropin_shutdown(void)
+{
+    if (g_pinned) tm_host_unregister(g_pinned);
+    g_pinned = NULL;
+    g_pinned_bytes = 0;
+    if (g_sess) tm_session_destroy(g_sess);
+    g_sess = NULL;
+    g_cid = -1;
+    g_cap = 0;
+}

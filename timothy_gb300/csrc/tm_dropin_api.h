@@ -1,0 +1,48 @@
+/* Internal entry points used by the reference-signature drop-ins (tm_dropin.c).
+ * They act on colony `cid` of a session and keep its Morton order in mind:
+ * uploads arrive in caller order and are permuted into slot order, downloads
+ * are permuted back. */
+#ifndef TM_DROPIN_API_H
+#define TM_DROPIN_API_H
+#include <stdint.h>
+#include "timothy_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* field offsets of the caller's array of structures */
+typedef struct {
+    int64_t stride;
+    int64_t x, y, z, size, young, ctype, phase;   /* -1: absent */
+} tmi_aos_layout;
+
+int tmi_set_types(tm_session *s, const tm_celltypes *types);
+int tmi_set_dimension(tm_session *s, int dim);
+/* caller-order AoS cells (host) -> colony state; n may not exceed the colony's slots */
+int tmi_upload_aos(tm_session *s, int cid, const void *cells, int64_t n, const tmi_aos_layout *lay);
+/* largest cell type among the uploaded cells */
+int tmi_max_ctype(tm_session *s, int cid, int *maxtype);
+/* 0 build (octbuild), 1 pair + octree walk, 2 position update, 3 CIC deposit */
+int tmi_phase(tm_session *s, int which);
+/* three doubles per cell, caller order, into the host AoS at byte offset `off`:
+ * which = 0 -> (v, density, mindist), 1 -> (x, y, z) */
+int tmi_download_aos3(tm_session *s, int cid, void *cells, int64_t stride, int64_t off, int which);
+/* forces as packed (x, y, z) triples in caller order */
+int tmi_download_forces(tm_session *s, int cid, double *f3);
+int tmi_upload_forces(tm_session *s, int cid, const double *f3);
+int tmi_upload_removecell(tm_session *s, int cid, const unsigned char *rem);
+int tmi_download_removecell(tm_session *s, int cid, unsigned char *rem, int64_t *newly_marked);
+int tmi_set_update(tm_session *s, int cid, int mode, double dt);
+/* CIC grid geometry (allocates the colony's grid on first use or change) */
+int tmi_set_cic(tm_session *s, int cid, const double lower[3], float res, const int64_t gsize[3]);
+/* patch corners of the last deposit and the deposit over [lo, hi] (x-major, z fastest) */
+int tmi_patch_box(tm_session *s, int cid, int64_t lo[3], int64_t hi[3]);
+int tmi_read_patch(tm_session *s, int cid, const int64_t lo[3], const int64_t hi[3], double *dst);
+/* device scratch large enough for n cells of `stride` bytes */
+int tmi_reserve_stage(tm_session *s, int64_t bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -66,12 +66,32 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
     const int t = live ? a.ctype[i] : 0;
     const tm_type &T = K->t[t];
 
-    // group origin: the float position of the warp's first cell
-    float4 h0 = a.hi[base];
-    const float ox = __shfl_sync(FULL, h0.x, 0), oy = __shfl_sync(FULL, h0.y, 0), oz = __shfl_sync(FULL, h0.z, 0);
-    float4 hi_i = live ? a.hi[i] : h0;
+    // Subgroups: lanes whose cells share a Morton node two levels above the
+    // bins.  32 Morton-consecutive cells can straddle a high-level boundary
+    // (e.g. the last cell of one octant and the first of the next), and a
+    // single union box would then span much of the colony; a node of the
+    // subgroup depth bounds every subgroup's box to a few bins per axis.
+    const int L = f.L;
+    const int Lg = L >= 2 ? L - 2 : 0;
+    const uint32_t key = live ? tm_prefix(a.codes[i], Lg) : 0xffffffffu;
+    const unsigned live_mask = __ballot_sync(FULL, live);
+    int my_leader = 0;
+    {
+        unsigned rem = live_mask;
+        while (rem) {
+            const int ldr = __ffs(rem) - 1;
+            const uint32_t kg = __shfl_sync(FULL, key, ldr);
+            const bool member = live && key == kg;
+            if (member) my_leader = ldr;
+            rem &= ~__ballot_sync(FULL, member);
+        }
+    }
+    float4 hi_i = live ? a.hi[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     float4 lo_i = live ? a.lo[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-    // double-float group-relative coordinates (s + e == x - o up to ~2^-47 |x|)
+    // origin: the float position of the subgroup's first cell
+    const float ox = __shfl_sync(FULL, hi_i.x, my_leader), oy = __shfl_sync(FULL, hi_i.y, my_leader),
+                oz = __shfl_sync(FULL, hi_i.z, my_leader);
+    // double-float origin-relative coordinates (s + e == x - o up to ~2^-47 |x|)
     float sx, sy, sz, ex, ey, ez;
     two_sum(hi_i.x, -ox, sx, ex);
     two_sum(hi_i.y, -oy, sy, ey);
@@ -82,20 +102,6 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
     const float gx = sx + ex, gy = sy + ey, gz = sz + ez;   // single-float form for the test
     // conservative test radius: FP32 staging errors are < 1e-5 here
     const float hr = T.hf * 1.00002f + 1e-4f;
-    const float thr = live ? hr * hr : -1.0f;
-
-    // union of the query boxes, in group-relative coordinates
-    float mnx = live ? gx - hr : 3e38f, mny = live ? gy - hr : 3e38f, mnz = live ? gz - hr : 3e38f;
-    float mxx = live ? gx + hr : -3e38f, mxy = live ? gy + hr : -3e38f, mxz = live ? gz + hr : -3e38f;
-    for (int o = 16; o > 0; o >>= 1) {
-        mnx = fminf(mnx, __shfl_xor_sync(FULL, mnx, o));
-        mny = fminf(mny, __shfl_xor_sync(FULL, mny, o));
-        mnz = fminf(mnz, __shfl_xor_sync(FULL, mnz, o));
-        mxx = fmaxf(mxx, __shfl_xor_sync(FULL, mxx, o));
-        mxy = fmaxf(mxy, __shfl_xor_sync(FULL, mxy, o));
-        mxz = fmaxf(mxz, __shfl_xor_sync(FULL, mxz, o));
-    }
-    const int L = f.L;
     const int nside = 1 << L;
     const float bs = f.binscale;
     auto binof = [&](float g, float o, float sh, float eps) {
@@ -103,11 +109,6 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
         int b = (int)floorf(v);
         return b < 0 ? 0 : (b >= nside ? nside - 1 : b);
     };
-    const int bx0 = binof(mnx, ox, f.shiftf[0], -0.01f), bx1 = binof(mxx, ox, f.shiftf[0], 0.01f);
-    const int by0 = binof(mny, oy, f.shiftf[1], -0.01f), by1 = binof(mxy, oy, f.shiftf[1], 0.01f);
-    const int bz0 = binof(mnz, oz, f.shiftf[2], -0.01f), bz1 = binof(mxz, oz, f.shiftf[2], 0.01f);
-    const int nbx = bx1 - bx0 + 1, nby = by1 - by0 + 1, nbz = bz1 - bz0 + 1;
-    const int nb = nbx * nby * nbz;
     const uint32_t *bstart = a.bin_start + d.binoff;
     const long long bbase = f.bin_base;
 
@@ -200,52 +201,76 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
         nl = 0;
     };
 
-    for (int chunk = 0; chunk < nb; chunk += 32) {
-        const int q = chunk + lane;
-        long long st = 0;
-        uint32_t cnt = 0;
-        if (q < nb) {
-            const int bx = bx0 + q % nbx;
-            const int by = by0 + (q / nbx) % nby;
-            const int bz = bz0 + q / (nbx * nby);
-            const uint32_t m = tm_morton((uint32_t)bx, (uint32_t)by, (uint32_t)bz);
-            const uint32_t s0 = bstart[m];
-            st = bbase + s0;
-            cnt = bstart[m + 1] - s0;
+    unsigned pending = live_mask;
+    while (pending) {
+        const int ldr = __ffs(pending) - 1;
+        const bool member = live && my_leader == ldr;
+        pending &= ~__ballot_sync(FULL, member);
+        const float gox = __shfl_sync(FULL, ox, ldr), goy = __shfl_sync(FULL, oy, ldr), goz = __shfl_sync(FULL, oz, ldr);
+        const float thr = member ? hr * hr : -1.0f;
+        // union of the members' query boxes, relative to the subgroup origin
+        float mnx = member ? gx - hr : 3e38f, mny = member ? gy - hr : 3e38f, mnz = member ? gz - hr : 3e38f;
+        float mxx = member ? gx + hr : -3e38f, mxy = member ? gy + hr : -3e38f, mxz = member ? gz + hr : -3e38f;
+        for (int o = 16; o > 0; o >>= 1) {
+            mnx = fminf(mnx, __shfl_xor_sync(FULL, mnx, o));
+            mny = fminf(mny, __shfl_xor_sync(FULL, mny, o));
+            mnz = fminf(mnz, __shfl_xor_sync(FULL, mnz, o));
+            mxx = fmaxf(mxx, __shfl_xor_sync(FULL, mxx, o));
+            mxy = fmaxf(mxy, __shfl_xor_sync(FULL, mxy, o));
+            mxz = fmaxf(mxz, __shfl_xor_sync(FULL, mxz, o));
         }
-        uint32_t incl = cnt;
-        for (int o = 1; o < 32; o <<= 1) {
-            uint32_t y = __shfl_up_sync(FULL, incl, o);
-            if (lane >= o) incl += y;
-        }
-        const uint32_t total = __shfl_sync(FULL, incl, 31);
-        const uint32_t off = incl - cnt;
-        for (uint32_t wb = 0; wb < total; wb += PAIR_TILE) {
-            const uint32_t k0 = max(off, wb), k1 = min(off + cnt, wb + PAIR_TILE);
-            for (uint32_t k = k0; k < k1; k++) {
-                const long long j = st + (k - off);
-                const float4 hj = a.hi[j], lj = a.lo[j];
-                tile[k - wb] = make_float4((hj.x - ox) + lj.x, (hj.y - oy) + lj.y, (hj.z - oz) + lj.z,
-                                           __int_as_float((int)j));
+        const int bx0 = binof(mnx, gox, f.shiftf[0], -0.01f), bx1 = binof(mxx, gox, f.shiftf[0], 0.01f);
+        const int by0 = binof(mny, goy, f.shiftf[1], -0.01f), by1 = binof(mxy, goy, f.shiftf[1], 0.01f);
+        const int bz0 = binof(mnz, goz, f.shiftf[2], -0.01f), bz1 = binof(mxz, goz, f.shiftf[2], 0.01f);
+        const int nbx = bx1 - bx0 + 1, nby = by1 - by0 + 1, nbz = bz1 - bz0 + 1;
+        const int nb = nbx * nby * nbz;
+        for (int chunk = 0; chunk < nb; chunk += 32) {
+            const int q = chunk + lane;
+            long long st = 0;
+            uint32_t cnt = 0;
+            if (q < nb) {
+                const int bx = bx0 + q % nbx;
+                const int by = by0 + (q / nbx) % nby;
+                const int bz = bz0 + q / (nbx * nby);
+                const uint32_t m = tm_morton((uint32_t)bx, (uint32_t)by, (uint32_t)bz);
+                const uint32_t s0 = bstart[m];
+                st = bbase + s0;
+                cnt = bstart[m + 1] - s0;
             }
-            __syncwarp();
-            const int wn = (int)min((uint32_t)PAIR_TILE, total - wb);
-            for (int tb = 0; tb < wn; tb += 32) {
-                const int te = min(wn, tb + 32);
-#pragma unroll 8
-                for (int tt = tb; tt < te; tt++) {
-                    const float4 cc = tile[tt];
-                    const float dx = cc.x - gx, dy = cc.y - gy, dz = cc.z - gz;
-                    const float s = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                    const int j = __float_as_int(cc.w);
-                    if (s <= thr && (long long)j != i) {
-                        list[nl][lane] = j;
-                        nl++;
-                    }
+            uint32_t incl = cnt;
+            for (int o = 1; o < 32; o <<= 1) {
+                uint32_t y = __shfl_up_sync(FULL, incl, o);
+                if (lane >= o) incl += y;
+            }
+            const uint32_t total = __shfl_sync(FULL, incl, 31);
+            const uint32_t off = incl - cnt;
+            for (uint32_t wb = 0; wb < total; wb += PAIR_TILE) {
+                const uint32_t k0 = max(off, wb), k1 = min(off + cnt, wb + PAIR_TILE);
+                for (uint32_t k = k0; k < k1; k++) {
+                    const long long j = st + (k - off);
+                    const float4 hj = a.hi[j], lj = a.lo[j];
+                    tile[k - wb] = make_float4((hj.x - gox) + lj.x, (hj.y - goy) + lj.y, (hj.z - goz) + lj.z,
+                                               __int_as_float((int)j));
                 }
-                if (__any_sync(FULL, nl > PAIR_LCAP - 32)) drain();
+                __syncwarp();
+                const int wn = (int)min((uint32_t)PAIR_TILE, total - wb);
+                for (int tb = 0; tb < wn; tb += 32) {
+                    const int te = min(wn, tb + 32);
+    #pragma unroll 8
+                    for (int tt = tb; tt < te; tt++) {
+                        const float4 cc = tile[tt];
+                        const float dx = cc.x - gx, dy = cc.y - gy, dz = cc.z - gz;
+                        const float s = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                        const int j = __float_as_int(cc.w);
+                        if (s <= thr && (long long)j != i) {
+                            list[nl][lane] = j;
+                            nl++;
+                        }
+                    }
+                    if (__any_sync(FULL, nl > PAIR_LCAP - 32)) drain();
+                }
+                __syncwarp();
             }
-            __syncwarp();
         }
     }
     drain();

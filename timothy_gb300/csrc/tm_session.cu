@@ -562,7 +562,9 @@ extern "C" int tm_colony_add(tm_session *s, const tm_colony_input *in, const tm_
     }
     colony_host ch;
     ch.n = (int)in->n;
-    ch.nslots = (int)(((std::max<long long>(in->n, 1) + 31) / 32) * 32);
+    const long long want = std::max<long long>(std::max<long long>(in->n, opt->reserve), 1);
+    if (want > 0x7fffffe0ll) return tm_fail(TM_EINVAL, "colony too large");
+    ch.nslots = (int)(((want + 31) / 32) * 32);
     ch.opt = *opt;
     ch.lcap = opt->lcap > 0 ? std::min(opt->lcap, TM_LMAX) : auto_lcap(s, in);
     ch.nbin = (1ll << (3 * ch.lcap)) + 2;
@@ -904,5 +906,349 @@ extern "C" int tm_host_unregister(void *ptr)
 {
     if (!ptr) return tm_fail(TM_EINVAL, "null pointer");
     CK(cudaHostUnregister(ptr));
+    return TM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// internal entry points for the reference-signature drop-ins
+
+#include "tm_dropin_api.h"
+
+struct tm_stage {
+    void *ptr = nullptr;
+    long long bytes = 0;
+};
+static tm_stage g_stage;   // one staging buffer per process (the drop-ins use one session)
+
+extern "C" int tmi_reserve_stage(tm_session *s, int64_t bytes)
+{
+    if (bytes <= g_stage.bytes) return TM_OK;
+    CK(cudaSetDevice(s->device));
+    if (g_stage.ptr) CK(cudaFree(g_stage.ptr));
+    g_stage.ptr = nullptr;
+    g_stage.bytes = 0;
+    CK(cudaMalloc(&g_stage.ptr, (size_t)bytes));
+    g_stage.bytes = bytes;
+    return TM_OK;
+}
+
+__global__ void k_unpack_aos(const unsigned char *aos, tmi_aos_layout lay, long long n, tm_arrays a, long long off)
+{
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const unsigned char *c = aos + k * lay.stride;
+    const long long i = off + k;
+    a.x[i] = *(const double *)(c + lay.x);
+    a.y[i] = *(const double *)(c + lay.y);
+    a.z[i] = *(const double *)(c + lay.z);
+    a.size[i] = *(const double *)(c + lay.size);
+    a.young[i] = *(const float *)(c + lay.young);
+    a.ctype[i] = *(const int *)(c + lay.ctype);
+    a.phase[i] = lay.phase >= 0 ? *(const int *)(c + lay.phase) : 1;
+    a.perm[i] = (int)k;
+}
+
+__global__ void k_max_ctype(const int *ctype, long long off, long long n, int *out)
+{
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int v = k < n ? ctype[off + k] : -1;
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0 && v >= 0) atomicMax(out, v);
+}
+
+__global__ void k_unsort3(const double *s0, const double *s1, const double *s2, const int *perm, long long off,
+                          long long n, double *dst)
+{
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const long long c = perm[off + k];
+    dst[3 * c] = s0[off + k];
+    dst[3 * c + 1] = s1[off + k];
+    dst[3 * c + 2] = s2[off + k];
+}
+
+__global__ void k_sort3(const double *src, const int *perm, long long off, long long n, double *d0, double *d1,
+                        double *d2)
+{
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const long long c = perm[off + k];
+    d0[off + k] = src[3 * c];
+    d1[off + k] = src[3 * c + 1];
+    d2[off + k] = src[3 * c + 2];
+}
+
+__global__ void k_sort_u8(const unsigned char *src, const int *perm, long long off, long long n, unsigned char *dst)
+{
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    dst[off + k] = src[perm[off + k]];
+}
+
+__global__ void k_read_box(const double *grid, int gy, int gz, long long lx, long long ly, long long lz,
+                           long long sx, long long sy, long long sz, double *dst)
+{
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= sx * sy * sz) return;
+    const long long i = k / (sy * sz), j = (k / sz) % sy, l = k % sz;
+    dst[k] = grid[((lx + i) * gy + (ly + j)) * gz + (lz + l)];
+}
+
+extern "C" int tmi_set_types(tm_session *s, const tm_celltypes *types)
+{
+    if (!s || !types || types->ntypes < 1 || types->ntypes > TM_MAX_TYPES) return tm_fail(TM_EINVAL, "bad types");
+    tm_consts &K = s->K;
+    K.ntypes = types->ntypes;
+    for (int t = 0; t < K.ntypes; t++) {
+        tm_type &T = K.t[t];
+        T.h = types->h[t];
+        T.h2 = types->h2[t];
+        T.h3 = types->h3[t];
+        T.h4 = types->h4[t];
+        T.csize = types->size[t];
+        T.sc = K.dim == 2 ? T.h2 : T.h3;
+        T.cW = host_type_const(K.dim, 0, T.h, T.h2, T.h3, T.h4);
+        T.cG = host_type_const(K.dim, 1, T.h, T.h2, T.h3, T.h4);
+        T.e = T.h + 0.01;
+        T.randommove = types->randommove ? types->randommove[t] : 0.0f;
+        T.hf = (float)T.h;
+        T.h2f = (float)(T.h * T.h);
+        T.inv_hf = (float)(1.0 / T.h);
+        T.cWf = (float)T.cW;
+        T.cGf = (float)T.cG;
+        T.kmassf = (float)(T.sc / T.csize);
+        T.thr_lo = (float)(T.h * (1.0 - 1e-5) * T.h * (1.0 - 1e-5));
+        T.thr_hi = (float)(T.h * (1.0 + 1e-5) * T.h * (1.0 + 1e-5));
+    }
+    CK(cudaMemcpyAsync(s->dK, &s->K, sizeof(tm_consts), cudaMemcpyHostToDevice, s->stream));
+    return TM_OK;
+}
+
+extern "C" int tmi_set_dimension(tm_session *s, int dim)
+{
+    if (!s || (dim != 2 && dim != 3)) return tm_fail(TM_EINVAL, "bad dimension");
+    if (s->K.dim == dim) return TM_OK;
+    s->K.dim = dim;
+    CK(cudaMemcpyAsync(s->dK, &s->K, sizeof(tm_consts), cudaMemcpyHostToDevice, s->stream));
+    return TM_OK;
+}
+
+extern "C" int tmi_upload_aos(tm_session *s, int cid, const void *cells, int64_t n, const tmi_aos_layout *lay)
+{
+    int rc = lookup(s, cid);
+    if (rc) return rc;
+    colony_host &c = s->cols[cid];
+    if (n > c.nslots) return tm_fail(TM_EINVAL, "colony %d holds at most %d cells", cid, c.nslots);
+    CK(cudaSetDevice(s->device));
+    if ((rc = tmi_reserve_stage(s, std::max<int64_t>(n * lay->stride, 8)))) return rc;
+    if (n > 0)
+        CK(cudaMemcpyAsync(g_stage.ptr, cells, (size_t)(n * lay->stride), cudaMemcpyHostToDevice, s->stream));
+    const tm_arrays a = view(s, s->parity);
+    if (n > 0)
+        k_unpack_aos<<<blocks_for(n, 256), 256, 0, s->stream>>>((const unsigned char *)g_stage.ptr, *lay, n, a, c.off);
+    // outputs and marks as after an upload
+    c.n = (int)n;
+    s->h_desc[cid].n = c.n;
+    if ((rc = push_desc(s, cid))) return rc;
+    k_colony_init<<<blocks_for(c.nslots, 256), 256, 0, s->stream>>>(a, cid, c.off, (int)n, c.nslots, 1);
+    CK(cudaGetLastError());
+    drop_graphs(s);
+    return TM_OK;
+}
+
+extern "C" int tmi_max_ctype(tm_session *s, int cid, int *maxtype)
+{
+    int rc = lookup(s, cid);
+    if (rc) return rc;
+    const colony_host &c = s->cols[cid];
+    const tm_arrays a = view(s, s->parity);
+    int *d = (int *)s->d_scratch;
+    CK(cudaMemsetAsync(d, 0, sizeof(int), s->stream));
+    if (c.n > 0) k_max_ctype<<<blocks_for(c.n, 256), 256, 0, s->stream>>>(a.ctype, c.off, c.n, d);
+    CK(cudaMemcpyAsync(maxtype, d, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return TM_OK;
+}
+
+extern "C" int tmi_phase(tm_session *s, int which)
+{
+    if (!s) return tm_fail(TM_EINVAL, "null session");
+    CK(cudaSetDevice(s->device));
+    int nk = 0, rc = TM_OK;
+    switch (which) {
+    case 0:
+        rc = enqueue_build(s, s->parity, nk);
+        if (rc == TM_OK) s->parity ^= 1;
+        break;
+    case 1: rc = enqueue_compute(s, nk, false); break;
+    case 2: rc = enqueue_update(s, nk); break;
+    case 3: rc = enqueue_cic(s, nk); break;
+    default: return tm_fail(TM_EINVAL, "bad phase");
+    }
+    s->launches += nk;
+    return rc;
+}
+
+extern "C" int tmi_download_aos3(tm_session *s, int cid, void *cells, int64_t stride, int64_t off, int which)
+{
+    int rc = lookup(s, cid);
+    if (rc) return rc;
+    const colony_host &c = s->cols[cid];
+    if (c.n == 0) return TM_OK;
+    const tm_arrays a = view(s, s->parity);
+    double *tmp = (double *)g_stage.ptr;
+    if ((rc = tmi_reserve_stage(s, (int64_t)c.n * 24))) return rc;
+    tmp = (double *)g_stage.ptr;
+    if (which == 0) k_unsort3<<<blocks_for(c.n, 256), 256, 0, s->stream>>>(a.v, a.density, a.mindist, a.perm, c.off, c.n, tmp);
+    else k_unsort3<<<blocks_for(c.n, 256), 256, 0, s->stream>>>(a.x, a.y, a.z, a.perm, c.off, c.n, tmp);
+    CK(cudaGetLastError());
+    CK(cudaMemcpy2DAsync((char *)cells + off, (size_t)stride, tmp, 24, 24, (size_t)c.n, cudaMemcpyDeviceToHost,
+                         s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return TM_OK;
+}
+
+extern "C" int tmi_download_forces(tm_session *s, int cid, double *f3)
+{
+    int rc = lookup(s, cid);
+    if (rc) return rc;
+    const colony_host &c = s->cols[cid];
+    if (c.n == 0) return TM_OK;
+    const tm_arrays a = view(s, s->parity);
+    if ((rc = tmi_reserve_stage(s, (int64_t)c.n * 24))) return rc;
+    double *tmp = (double *)g_stage.ptr;
+    k_unsort3<<<blocks_for(c.n, 256), 256, 0, s->stream>>>(a.fx, a.fy, a.fz, a.perm, c.off, c.n, tmp);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(f3, tmp, (size_t)c.n * 24, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return TM_OK;
+}
+
+extern "C" int tmi_upload_forces(tm_session *s, int cid, const double *f3)
+{
+    int rc = lookup(s, cid);
+    if (rc) return rc;
+    const colony_host &c = s->cols[cid];
+    if (c.n == 0) return TM_OK;
+    const tm_arrays a = view(s, s->parity);
+    if ((rc = tmi_reserve_stage(s, (int64_t)c.n * 24))) return rc;
+    double *tmp = (double *)g_stage.ptr;
+    CK(cudaMemcpyAsync(tmp, f3, (size_t)c.n * 24, cudaMemcpyHostToDevice, s->stream));
+    k_sort3<<<blocks_for(c.n, 256), 256, 0, s->stream>>>(tmp, a.perm, c.off, c.n, a.fx, a.fy, a.fz);
+    CK(cudaGetLastError());
+    return TM_OK;
+}
+
+extern "C" int tmi_upload_removecell(tm_session *s, int cid, const unsigned char *rem)
+{
+    int rc = lookup(s, cid);
+    if (rc) return rc;
+    const colony_host &c = s->cols[cid];
+    if (c.n == 0) return TM_OK;
+    const tm_arrays a = view(s, s->parity);
+    if ((rc = tmi_reserve_stage(s, (int64_t)c.n))) return rc;
+    CK(cudaMemcpyAsync(g_stage.ptr, rem, (size_t)c.n, cudaMemcpyHostToDevice, s->stream));
+    k_sort_u8<<<blocks_for(c.n, 256), 256, 0, s->stream>>>((const unsigned char *)g_stage.ptr, a.perm, c.off, c.n,
+                                                           a.rem);
+    CK(cudaGetLastError());
+    // the update adds to removecount: count this step's marks only
+    CK(cudaMemsetAsync(&s->A.frame[cid].removecount, 0, sizeof(unsigned long long), s->stream));
+    return TM_OK;
+}
+
+extern "C" int tmi_download_removecell(tm_session *s, int cid, unsigned char *rem, int64_t *newly_marked)
+{
+    int rc = lookup(s, cid);
+    if (rc) return rc;
+    const colony_host &c = s->cols[cid];
+    const tm_arrays a = view(s, s->parity);
+    unsigned long long cnt = 0;
+    CK(cudaMemcpyAsync(&cnt, &s->A.frame[cid].removecount, sizeof cnt, cudaMemcpyDeviceToHost, s->stream));
+    if (c.n > 0) {
+        if ((rc = tmi_reserve_stage(s, (int64_t)c.n))) return rc;
+        k_unsort<unsigned char><<<blocks_for(c.n, 256), 256, 0, s->stream>>>(a.rem, a.perm, c.off, c.n,
+                                                                             (unsigned char *)g_stage.ptr);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(rem, g_stage.ptr, (size_t)c.n, cudaMemcpyDeviceToHost, s->stream));
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    if (newly_marked) *newly_marked = (int64_t)cnt;
+    return TM_OK;
+}
+
+extern "C" int tmi_set_update(tm_session *s, int cid, int mode, double dt)
+{
+    int rc = lookup(s, cid);
+    if (rc) return rc;
+    s->cols[cid].opt.update_mode = mode;
+    s->cols[cid].opt.dt = dt;
+    s->h_desc[cid].update_mode = mode;
+    s->h_desc[cid].dt = dt;
+    return push_desc(s, cid);
+}
+
+extern "C" int tmi_set_cic(tm_session *s, int cid, const double lower[3], float res, const int64_t gsize[3])
+{
+    int rc = lookup(s, cid);
+    if (rc) return rc;
+    colony_host &c = s->cols[cid];
+    const long long ng = gsize[0] * gsize[1] * gsize[2];
+    if (ng <= 0) return tm_fail(TM_EINVAL, "empty grid");
+    if (c.gridoff < 0 || c.ngrid != ng) {
+        if (c.gridoff >= 0) s->grids.release(c.gridoff, c.ngrid);
+        c.gridoff = -1;
+        if (!s->grids.alloc(ng, c.gridoff)) return tm_fail(TM_ENOMEM, "no room for a %lld-node grid", ng);
+        c.ngrid = ng;
+    }
+    for (int k = 0; k < 3; k++) c.gsize[k] = (int)gsize[k];
+    c.opt.cic = 1;
+    c.opt.gfh = res;
+    tm_desc &d = s->h_desc[cid];
+    d.gridoff = c.gridoff;
+    d.gres = res;
+    for (int k = 0; k < 3; k++) {
+        d.glower[k] = lower[k];
+        d.gsize[k] = (int)gsize[k];
+    }
+    drop_graphs(s);
+    return push_desc(s, cid);
+}
+
+extern "C" int tmi_patch_box(tm_session *s, int cid, int64_t lo[3], int64_t hi[3])
+{
+    int rc = lookup(s, cid);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(&s->h_frame[cid], &s->A.frame[cid], sizeof(tm_frame), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    for (int k = 0; k < 3; k++) {
+        lo[k] = s->h_frame[cid].patch_lo[k];
+        hi[k] = s->h_frame[cid].patch_hi[k];
+    }
+    if (s->K.dim == 2) {
+        lo[2] = 0;
+        hi[2] = 0;
+    }
+    return TM_OK;
+}
+
+extern "C" int tmi_read_patch(tm_session *s, int cid, const int64_t lo[3], const int64_t hi[3], double *dst)
+{
+    int rc = lookup(s, cid);
+    if (rc) return rc;
+    const colony_host &c = s->cols[cid];
+    if (c.gridoff < 0) return tm_fail(TM_EINVAL, "colony %d has no grid", cid);
+    long long sz[3];
+    for (int k = 0; k < 3; k++) {
+        sz[k] = hi[k] - lo[k] + 1;
+        if (lo[k] < 0 || sz[k] <= 0 || hi[k] >= c.gsize[k]) return tm_fail(TM_EINVAL, "patch outside the grid");
+    }
+    const long long tot = sz[0] * sz[1] * sz[2];
+    if ((rc = tmi_reserve_stage(s, tot * 8))) return rc;
+    k_read_box<<<blocks_for(tot, 256), 256, 0, s->stream>>>(s->A.grid + c.gridoff, c.gsize[1], c.gsize[2], lo[0],
+                                                            lo[1], lo[2], sz[0], sz[1], sz[2],
+                                                            (double *)g_stage.ptr);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(dst, g_stage.ptr, (size_t)tot * 8, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
     return TM_OK;
 }

@@ -1,0 +1,237 @@
+"""ctypes mirror of include/timothy_refabi.h and a driver for the drop-ins.
+
+``DropinRun`` calls the reference-signature entry points of
+libtimothy_gb300.so in the order of the reference step loop (main.c:67-79,
+step.c:41-100): octbuild, patches_alloc + patches_cells2envinfo,
+computepotential, computegradient, updatepositions, octfree.  Cells live in a
+host array of celldata_t exactly as in the reference program.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from .session import load_library
+
+
+class cellcount_t(C.Structure):
+    _fields_ = [(k, C.c_uint64) for k in ("n", "g0phase", "g1phase", "sphase", "g2phase", "mphase",
+                                          "necroticphase")]
+
+
+class celldata_t(C.Structure):
+    _fields_ = [("lifetime", C.c_int), ("phase", C.c_int), ("age", C.c_int), ("death", C.c_int),
+                ("phasetime", C.c_float), ("g1", C.c_float), ("s", C.c_float), ("g2", C.c_float),
+                ("m", C.c_float), ("young", C.c_float), ("gid", C.c_int), ("x", C.c_double), ("y", C.c_double),
+                ("z", C.c_double), ("size", C.c_double), ("v", C.c_double), ("density", C.c_double),
+                ("mindist", C.c_double), ("ctype", C.c_int)]
+
+
+class double3dv_t(C.Structure):
+    _fields_ = [("x", C.c_double), ("y", C.c_double), ("z", C.c_double)]
+
+
+class int643dv_t(C.Structure):
+    _fields_ = [("x", C.c_int64), ("y", C.c_int64), ("z", C.c_int64)]
+
+
+class octnode_t(C.Structure):
+    _fields_ = [("xcode", C.c_uint), ("ycode", C.c_uint), ("zcode", C.c_uint), ("xlimit", C.c_uint),
+                ("ylimit", C.c_uint), ("zlimit", C.c_uint), ("level", C.c_uint), ("father", C.c_int64),
+                ("child", C.c_int64 * 8), ("data", C.c_int)]
+
+
+class cellsinfo_t(C.Structure):
+    _fields_ = [("localcount", cellcount_t), ("globalcount", cellcount_t), ("localtypecount", C.c_void_p),
+                ("globaltypecount", C.c_void_p), ("cellsperproc", C.c_void_p), ("cells", C.c_void_p),
+                ("forces", C.c_void_p), ("octree", C.c_void_p), ("octsize", C.c_int64), ("octmaxsize", C.c_int64),
+                ("dimension", C.c_int), ("velocity", C.c_void_p)]
+
+
+class grid_t(C.Structure):
+    _fields_ = [("globalsize", int643dv_t), ("lowercorner", double3dv_t), ("uppercorner", double3dv_t),
+                ("localsize", int643dv_t), ("resolution", C.c_float), ("loweridx", C.POINTER(int643dv_t)),
+                ("upperidx", C.POINTER(int643dv_t)), ("lowleftnear", C.c_void_p), ("uprightfar", C.c_void_p)]
+
+
+class cellcommdata_t(C.Structure):
+    _fields_ = [("explist", C.c_void_p), ("explistmaxsize", C.c_int), ("reqsend", C.c_void_p),
+                ("reqrecv", C.c_void_p), ("sendoffset", C.c_void_p), ("recvoffset", C.c_void_p),
+                ("recvcount", C.c_void_p), ("sendcount", C.c_void_p), ("sendcellindata", C.c_void_p),
+                ("recvcellindata", C.c_void_p), ("sendcelloutdata", C.c_void_p), ("recvcelloutdata", C.c_void_p),
+                ("numexp", C.c_int), ("numimp", C.c_int)]
+
+
+class settings_t(C.Structure):
+    _fields_ = [("maxcells", C.c_int64), ("maxlocalcells", C.c_int64), ("numberofsteps", C.c_int),
+                ("secondsperstep", C.c_float), ("numberofcelltypes", C.c_int), ("numberoffields", C.c_int),
+                ("dimension", C.c_int), ("restart", C.c_int), ("rstfilename", C.c_char * 128),
+                ("outdir", C.c_char * 128), ("visoutstep", C.c_int), ("statoutstep", C.c_int),
+                ("rstoutstep", C.c_int), ("maxspeed", C.c_float), ("gfdt", C.c_float), ("gfh", C.c_float),
+                ("simulationstart", C.c_int), ("rseed", C.c_uint), ("step", C.c_int)]
+
+
+class systeminfo_t(C.Structure):
+    _fields_ = [("rank", C.c_int), ("size", C.c_int), ("nthreads", C.c_int), ("dim", C.c_int * 3),
+                ("noderank", C.c_int), ("nodesize", C.c_int), ("memperproc", C.c_int), ("MPI_CART_COMM", C.c_int),
+                ("coords", C.c_void_p), ("endian", C.c_int)]
+
+
+class celltype_t(C.Structure):
+    _fields_ = [("name", C.c_char * 128), ("g1", C.c_float), ("s", C.c_float), ("g2", C.c_float),
+                ("m", C.c_float), ("v", C.c_float), ("rd", C.c_float), ("size", C.c_double), ("h", C.c_double),
+                ("h2", C.c_double), ("h3", C.c_double), ("h4", C.c_double), ("inputfile", C.c_char * 128),
+                ("criticaldensity", C.c_float), ("production", C.c_void_p), ("consumption", C.c_void_p),
+                ("criticallevel1", C.c_void_p), ("criticallevel2", C.c_void_p), ("randommove", C.c_float)]
+
+
+class patches_t(C.Structure):
+    _fields_ = [("data", C.POINTER(C.POINTER(C.c_double))), ("intersect", C.POINTER(C.c_int)),
+                ("receiver", C.c_void_p), ("sender", C.c_void_p), ("recvdata", C.c_void_p),
+                ("reqsend", C.c_void_p), ("reqrecv", C.c_void_p), ("lowercorner", C.POINTER(int643dv_t)),
+                ("uppercorner", C.POINTER(int643dv_t)), ("lowercornerR", C.c_void_p),
+                ("uppercornerR", C.c_void_p), ("size", C.POINTER(int643dv_t)), ("commbuff", C.c_void_p),
+                ("buff", C.c_void_p)]
+
+
+SIZES = {"celldata_t": 112, "cellsinfo_t": 192, "celltype_t": 368, "systeminfo_t": 56, "settings_t": 336,
+         "cellcommdata_t": 104}
+
+CELL_DTYPE = np.dtype({"names": [f for f, _ in celldata_t._fields_],
+                       "formats": ["<i4", "<i4", "<i4", "<i4", "<f4", "<f4", "<f4", "<f4", "<f4", "<f4", "<i4",
+                                   "<f8", "<f8", "<f8", "<f8", "<f8", "<f8", "<f8", "<i4"],
+                       "offsets": [getattr(celldata_t, f).offset for f, _ in celldata_t._fields_],
+                       "itemsize": C.sizeof(celldata_t)})
+
+
+def _bind(lib):
+    if getattr(lib, "_refabi_bound", False):
+        return lib
+    lib.octbuild.argtypes = [systeminfo_t, C.POINTER(cellsinfo_t), C.POINTER(celltype_t)]
+    lib.octfree.argtypes = [C.POINTER(cellsinfo_t)]
+    for f in ("computepotential", "computeremotepotential", "computegradient", "computeremotegradient"):
+        getattr(lib, f).argtypes = [systeminfo_t, C.POINTER(cellsinfo_t), C.POINTER(celltype_t), cellcommdata_t]
+    lib.updatepositions.argtypes = [settings_t, C.POINTER(celltype_t), C.POINTER(cellsinfo_t), C.c_void_p,
+                                    C.POINTER(C.c_int64)]
+    lib.patches_alloc.argtypes = [systeminfo_t, settings_t, C.POINTER(patches_t), C.POINTER(cellsinfo_t),
+                                  C.POINTER(grid_t)]
+    lib.patches_cells2envinfo.argtypes = lib.patches_alloc.argtypes
+    for f in ("octbuild", "octfree", "computepotential", "computeremotepotential", "computegradient",
+              "computeremotegradient", "updatepositions", "patches_alloc", "patches_cells2envinfo",
+              "tm_dropin_shutdown"):
+        getattr(lib, f).restype = None
+    lib._refabi_bound = True
+    return lib
+
+
+def grid_geometry(dim: int, gfh: float):
+    """computegridsize at one rank (grid.c:37-77), float arithmetic as there."""
+    f = np.float32
+    gx = f(f(1024.0 - (-1024.0)) + f(1))
+    sx = int(np.float32((gx + f(1)) / f(gfh)))
+    sx += 1 - sx % 1
+    if dim == 3:
+        sz = sx
+        lower = (-1024.0, -1024.0, -1024.0)
+    else:
+        sz = 1
+        lower = (-1024.0, -1024.0, 0.0)
+    return (sx, sx, sz), lower
+
+
+class DropinRun:
+    """The reference step loop on host celldata_t cells, through the drop-ins."""
+
+    def __init__(self, col, *, cic: bool = False, gfh: float = 8.0, nfields: int = 1):
+        self.lib = _bind(load_library())
+        n = col.n
+        self.n = n
+        self.dim = col.dim
+        cells = np.zeros(max(n, 1), CELL_DTYPE)
+        for k in ("x", "y", "z", "size", "young", "ctype", "phase"):
+            cells[k][:n] = getattr(col, k)
+        cells["gid"][:n] = np.arange(n)
+        self.cells = cells
+        self.forces = np.zeros((max(n, 1), 3))
+        t = col.types
+        self.celltype = (celltype_t * t.ntypes)()
+        for k in range(t.ntypes):
+            ct = self.celltype[k]
+            ct.h, ct.h2, ct.h3, ct.h4 = float(t.h[k]), float(t.h2[k]), float(t.h3[k]), float(t.h4[k])
+            ct.size = float(t.size[k])
+            ct.randommove = float(t.randommove[k])
+        self.si = systeminfo_t()
+        self.si.rank, self.si.size = 0, 1
+        self.si.dim[0] = self.si.dim[1] = self.si.dim[2] = 1
+        self.st = settings_t()
+        self.st.dimension = col.dim
+        self.st.numberofcelltypes = t.ntypes
+        self.st.numberoffields = nfields if cic else 0
+        self.st.gfh = gfh
+        self.ci = cellsinfo_t()
+        self.ci.localcount.n = n
+        self.ci.cells = cells.ctypes.data
+        self.ci.forces = self.forces.ctypes.data
+        self.ci.dimension = col.dim
+        self.cc = cellcommdata_t()
+        self.cic = cic
+        if cic:
+            (gx, gy, gz), lower = grid_geometry(col.dim, gfh)
+            self.gsize = (gx, gy, gz)
+            g = grid_t()
+            g.resolution = gfh
+            g.lowercorner.x, g.lowercorner.y, g.lowercorner.z = lower
+            g.localsize.x, g.localsize.y, g.localsize.z = gx, gy, gz
+            g.globalsize.x, g.globalsize.y, g.globalsize.z = gx, gy, (gz if col.dim == 3 else 0)
+            self._lo = (int643dv_t * 1)()
+            self._hi = (int643dv_t * 1)()
+            self._hi[0].x, self._hi[0].y, self._hi[0].z = gx - 1, gy - 1, gz - 1
+            g.loweridx = self._lo
+            g.upperidx = self._hi
+            self.grid = g
+        self.removecount = C.c_int64(0)
+        self.removecell = np.zeros(max(n, 1), np.uint8)
+        self.octsize = 0
+        self.aff = None
+        self.deposit = None
+
+    def step(self, update: bool = True):
+        lib = self.lib
+        ct = self.celltype
+        lib.octbuild(self.si, C.byref(self.ci), ct)
+        self.octsize = int(self.ci.octsize)
+        if self.cic:
+            p = patches_t()
+            lib.patches_alloc(self.si, self.st, C.byref(p), C.byref(self.ci), C.byref(self.grid))
+            lib.patches_cells2envinfo(self.si, self.st, C.byref(p), C.byref(self.ci), C.byref(self.grid))
+            # at one rank the patch is added into the zeroed grid (patches.c:321-367)
+            dep = np.zeros(self.gsize)
+            if p.intersect and p.intersect[0]:
+                lo = p.lowercorner[0]
+                sz = p.size[0]
+                vol = sz.x * sz.y * sz.z
+                patch = np.ctypeslib.as_array(p.data[0], shape=(vol,)).reshape(sz.x, sz.y, sz.z).copy()
+                dep[lo.x:lo.x + sz.x, lo.y:lo.y + sz.y, lo.z:lo.z + sz.z] += patch
+            self.deposit = dep
+        lib.computepotential(self.si, C.byref(self.ci), ct, self.cc)
+        lib.computeremotepotential(self.si, C.byref(self.ci), ct, self.cc)
+        lib.computegradient(self.si, C.byref(self.ci), ct, self.cc)
+        lib.computeremotegradient(self.si, C.byref(self.ci), ct, self.cc)
+        if update:
+            lib.updatepositions(self.st, ct, C.byref(self.ci), self.removecell.ctypes.data,
+                                C.byref(self.removecount))
+        lib.octfree(C.byref(self.ci))
+        aff = double3dv_t.in_dll(lib, "affShift")
+        self.aff = np.array([aff.x, aff.y, aff.z, C.c_double.in_dll(lib, "affScale").value])
+
+    def outputs(self) -> dict:
+        n = self.n
+        c = self.cells[:n]
+        return {"x": c["x"].copy(), "y": c["y"].copy(), "z": c["z"].copy(), "density": c["density"].copy(),
+                "v": c["v"].copy(), "mindist": c["mindist"].copy(), "fx": self.forces[:n, 0].copy(),
+                "fy": self.forces[:n, 1].copy(), "fz": self.forces[:n, 2].copy(),
+                "removecell": self.removecell[:n].copy()}
+
+    def shutdown(self):
+        self.lib.tm_dropin_shutdown()

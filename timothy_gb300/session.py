@@ -42,7 +42,7 @@ class _Input(C.Structure):
 
 class _Options(C.Structure):
     _fields_ = [("precision", C.c_int), ("update_mode", C.c_int), ("dt", C.c_double), ("cic", C.c_int),
-                ("gfh", C.c_float), ("lcap", C.c_int)]
+                ("gfh", C.c_float), ("lcap", C.c_int), ("reserve", C.c_int64)]
 
 
 class _Output(C.Structure):
@@ -178,9 +178,10 @@ class Session:
         return _Input(col.n, *[_p(a) for a in arrs]), arrs
 
     def add_colony(self, col: Colony, *, precision: str = "fp64", update: str = "reference", dt: float = 1.0,
-                   cic: bool = False, gfh: float = 8.0, lcap: int = 0) -> int:
+                   cic: bool = False, gfh: float = 8.0, lcap: int = 0, reserve: int = 0) -> int:
         inp, keep = self._input(col)
-        opt = _Options(PREC[precision], UPDATE[update], float(dt), 1 if cic else 0, float(gfh), int(lcap))
+        opt = _Options(PREC[precision], UPDATE[update], float(dt), 1 if cic else 0, float(gfh), int(lcap),
+                       int(reserve))
         cid = C.c_int(-1)
         _check(load_library().tm_colony_add(self._h, C.byref(inp), C.byref(opt), C.byref(cid)))
         self._n[cid.value] = col.n
