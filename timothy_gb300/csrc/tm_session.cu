@@ -129,6 +129,7 @@ struct tm_session {
     int parity = 0;   // 0: A.x is current, 1: A.x2 is current
     long long launches = 0;
     int kernels_per_step = 0;
+    int mass_types = 0;   // types the FP64 density-weight array holds
     cudaEvent_t tstart = nullptr, tstop = nullptr;
 };
 
@@ -408,6 +409,7 @@ extern "C" int tm_session_create(tm_session **out, const tm_session_config *cfg,
     AL(a.perm2, S) AL(a.rem2, S)
     AL(a.col, S) AL(a.code, S) AL(a.codes, S) AL(a.bin, S) AL(a.tmp, S) AL(a.hi, S) AL(a.lo, S)
     AL(a.mass, S * K.ntypes)
+    s->mass_types = K.ntypes;
     AL(a.bin_count, B + 1) AL(a.bin_cursor, B + 1) AL(a.bin_start, B + 1) AL(a.bigbins, 2 * (S / 33) + 4)
     AL(a.fix_count, 1) AL(a.fix_list, S)
     AL(a.density, S) AL(a.v, S) AL(a.mindist, S) AL(a.fx, S) AL(a.fy, S) AL(a.fz, S) AL(a.nbcount, S)
@@ -997,6 +999,16 @@ __global__ void k_read_box(const double *grid, int gy, int gz, long long lx, lon
 extern "C" int tmi_set_types(tm_session *s, const tm_celltypes *types)
 {
     if (!s || !types || types->ntypes < 1 || types->ntypes > TM_MAX_TYPES) return tm_fail(TM_EINVAL, "bad types");
+    if (types->ntypes > s->mass_types) {
+        // the per-type density weights need one slot array per type
+        CK(cudaStreamSynchronize(s->stream));
+        double *m = nullptr;
+        CK(cudaMalloc((void **)&m, sizeof(double) * (size_t)(s->slots.cap * 32) * (size_t)types->ntypes));
+        CK(cudaFree(s->A.mass));
+        s->A.mass = m;
+        s->mass_types = types->ntypes;
+        drop_graphs(s);
+    }
     tm_consts &K = s->K;
     K.ntypes = types->ntypes;
     for (int t = 0; t < K.ntypes; t++) {
