@@ -27,6 +27,7 @@ __global__ void k_step_init(tm_arrays a)
     f.error = 0;
     f.nbig = 0;
     f.boundary_pairs = 0;
+    f.codes_slow = 0;
     for (int k = 0; k < 3; k++) {
         f.patch_lo[k] = 2147483647ll;
         f.patch_hi[k] = -2147483648ll;
@@ -49,52 +50,78 @@ __global__ void k_binbase(tm_arrays a)
 // monotone, so per-type minima/maxima of x suffice; they are reduced on the
 // order-preserving integer image of the doubles (no FP64 instructions).
 
-__global__ void k_bbox(tm_arrays a, int ntypes)
+__global__ void __launch_bounds__(256) k_bbox(tm_arrays a, int ntypes)
 {
+    // per-block partial minima/maxima in shared memory, one global atomic per
+    // block and value; a block spans at most 8 colonies (32-aligned ranges)
+    __shared__ unsigned long long red[8][TM_MAX_TYPES][6];
+    __shared__ int colid[8];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int k = threadIdx.x; k < 8 * TM_MAX_TYPES * 6; k += blockDim.x) {
+        const int q = k % 6;
+        (&red[0][0][0])[k] = q < 3 ? 0xffffffffffffffffull : 0ull;
+    }
     long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     bool live = false;
-    int c = 0;
+    int c = -1;
     if (s < a.nslots_total) {
         c = a.col[s];
         const tm_desc &d = a.desc[c];
         live = d.active && (s - d.off) < d.n;
     }
-    unsigned long long v[6];
+    if (lane == 0) colid[w] = (((s >> 5) << 5) < a.nslots_total) ? a.col[(s >> 5) << 5] : -1;
+    __syncthreads();
+    unsigned long long v[3] = {0, 0, 0};
     int t = -1;
     if (live) {
         t = a.ctype[s];
         v[0] = tm_ordered(a.x[s]);
         v[1] = tm_ordered(a.y[s]);
         v[2] = tm_ordered(a.z[s]);
-        v[3] = v[0];
-        v[4] = v[1];
-        v[5] = v[2];
     }
-    // a warp never straddles two colonies (32-aligned slot ranges)
     for (int tt = 0; tt < ntypes; tt++) {
-        bool mine = live && t == tt;
-        unsigned any = __ballot_sync(FULL, mine);
-        if (!any) continue;
+        const bool mine = live && t == tt;
+        if (!__ballot_sync(FULL, mine)) continue;
         unsigned long long r[6];
         for (int k = 0; k < 3; k++) {
             r[k] = mine ? v[k] : 0xffffffffffffffffull;
-            r[3 + k] = mine ? v[3 + k] : 0ull;
+            r[3 + k] = mine ? v[k] : 0ull;
         }
         for (int o = 16; o > 0; o >>= 1) {
             for (int k = 0; k < 3; k++) {
-                unsigned long long q = __shfl_xor_sync(FULL, r[k], o);
+                const unsigned long long q = __shfl_xor_sync(FULL, r[k], o);
                 r[k] = q < r[k] ? q : r[k];
-                unsigned long long w = __shfl_xor_sync(FULL, r[3 + k], o);
-                r[3 + k] = w > r[3 + k] ? w : r[3 + k];
+                const unsigned long long u = __shfl_xor_sync(FULL, r[3 + k], o);
+                r[3 + k] = u > r[3 + k] ? u : r[3 + k];
             }
         }
-        int leader = __ffs(any) - 1;
-        if ((threadIdx.x & 31) == leader) {
-            tm_frame &f = a.frame[c];
+        if (lane == 0) {
             for (int k = 0; k < 3; k++) {
-                atomicMin(&f.bbox[tt][k], r[k]);
-                atomicMax(&f.bbox[tt][3 + k], r[3 + k]);
+                red[w][tt][k] = r[k];
+                red[w][tt][3 + k] = r[3 + k];
             }
+        }
+    }
+    __syncthreads();
+    // warps of the same colony merge into the first such warp, which posts the atomics
+    const int nw = blockDim.x >> 5;
+    for (int k = threadIdx.x; k < nw * ntypes * 6; k += blockDim.x) {
+        const int ww = k / (ntypes * 6), tt = (k / 6) % ntypes, q = k % 6;
+        const int cc = colid[ww];
+        if (cc < 0) continue;
+        bool first = true;
+        for (int u = 0; u < ww; u++)
+            if (colid[u] == cc) first = false;
+        if (!first) continue;
+        unsigned long long best = red[ww][tt][q];
+        for (int u = ww + 1; u < nw; u++) {
+            if (colid[u] != cc) continue;
+            const unsigned long long o = red[u][tt][q];
+            best = q < 3 ? (o < best ? o : best) : (o > best ? o : best);
+        }
+        if (q < 3 ? best != 0xffffffffffffffffull : best != 0ull) {
+            if (q < 3) atomicMin(&a.frame[cc].bbox[tt][q], best);
+            else atomicMax(&a.frame[cc].bbox[tt][q], best);
         }
     }
 }
@@ -136,6 +163,26 @@ __global__ void k_frame(tm_arrays a, const tm_consts *K)
     f.L = L;
     f.nbins = 1u << (3 * L);
     f.binscale = (float)((double)(1 << L) / sc);
+    // integer lattice path: cmul = 2^(78-ck)/scale in [2^62, 2^63)
+    int es = 0;
+    frexp(sc, &es);                       // sc in [2^(es-1), 2^es)
+    const int ck = 16 - es;
+    const bool small_shift = fabs(f.shift[0]) < 16384.0 && fabs(f.shift[1]) < 16384.0 && fabs(f.shift[2]) < 16384.0;
+    if (ck >= 1 && ck <= 40 && small_shift) {
+        f.ck = ck;
+        f.cmul = (unsigned long long)ldexp(1.0 / sc, 78 - ck);
+        for (int k = 0; k < 3; k++) f.sh_fx[k] = (long long)ldexp(f.shift[k], 47);
+        // bound of |integer value - FP64 value| in lattice units, doubled:
+        // FP64 roundings of x -+ h and - shift on values below 2^15 (2^-37 each
+        // after two operations) and of the division (2^-24), plus the three
+        // fixed-point truncations (2^-47 each) and the product (2^-31)
+        const double eps = 2.0 * (ldexp(1.0, -8) / sc + 3.0 * ldexp(1.0, -18) / sc + ldexp(1.0, -23));
+        f.ceps = eps >= 0.25 ? 0x40000000u : (uint32_t)ldexp(eps, 32) + 1u;
+    } else {
+        f.ck = 1;
+        f.cmul = 0;
+        f.ceps = 0xffffffffu;             // never accept: exact FP64 path for every code
+    }
 }
 
 // exact lattice codes (octree.c:187-191) and bin occupancy
@@ -148,10 +195,15 @@ __global__ void k_codes(tm_arrays a)
     if (!d.active || (s - d.off) >= d.n) return;
     const tm_frame &f = a.frame[c];
     uint4 q;
-    q.x = tm_lattice(a.x[s], f.shift[0], f.scale);
-    q.y = tm_lattice(a.y[s], f.shift[1], f.scale);
-    q.z = tm_lattice(a.z[s], f.shift[2], f.scale);
+    const double px = a.x[s], py = a.y[s], pz = a.z[s];
+    long long X, Y, Z;
+    const bool okx = tm_fix47(px, X), oky = tm_fix47(py, Y), okz = tm_fix47(pz, Z);
+    unsigned slow = 0;
+    q.x = tm_lattice_fast(px, X, okx, 0, 0.0, f, 0, slow);
+    q.y = tm_lattice_fast(py, Y, oky, 0, 0.0, f, 1, slow);
+    q.z = tm_lattice_fast(pz, Z, okz, 0, 0.0, f, 2, slow);
     q.w = 0;
+    if (slow) atomicAdd(&a.frame[c].codes_slow, (unsigned long long)slow);
     a.code[s] = q;
     uint32_t b = (uint32_t)(d.binoff) + tm_prefix(q, f.L);
     a.bin[s] = b;

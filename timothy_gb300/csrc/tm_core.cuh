@@ -35,6 +35,7 @@ struct tm_type {
     double cG;       // sphgradient constant 48/(pi h4) or 320/(7 pi h3)
     double e;        // bounding-box pad h + 0.01 (octree.c:167)
     float randommove;
+    long long h_fx;  // h * 2^47, truncated
     // FP32 forms for the compensated path
     float hf, h2f, inv_hf, cWf, cGf, kmassf;   // kmassf = sc / csize
     float thr_lo, thr_hi;                      // squared-distance band around h^2
@@ -62,6 +63,12 @@ struct tm_frame {
     int nbig;            // bins needing the block sort
     int pad_;
     long long bin_base;      // slot of a bin = bin_base + bin_start[bin]
+    // fixed-point form of the affine map for the integer lattice-code path
+    long long sh_fx[3];      // shift * 2^47, truncated
+    unsigned long long cmul; // ~ 2^(78-ck) / scale
+    int ck;                  // left shift restoring 2^32 * code
+    uint32_t ceps;           // 2^32 * error bound of the integer path
+    unsigned long long codes_slow;   // codes that took the FP64 path (diagnostic)
     unsigned long long step_counter;
     long long patch_lo[3];   // CIC patch corners (patches.c:61-132); INT_MAX/INT_MIN when empty
     long long patch_hi[3];
@@ -169,6 +176,54 @@ __device__ inline uint32_t tm_lattice_off(double x, double off, double shift, do
     return (uint32_t)mul64(q, 536870912.0);
 }
 
+// Lattice codes without FP64 arithmetic in the common case.
+//
+// A position x (|x| < 2^13) becomes the 2^-47 fixed-point integer X by bit
+// manipulation (truncation).  With D = X + OFF - SHIFT (OFF = 0 or +-h, all
+// truncated the same way) the real code value is D * 2^-18 / scale; it is
+// formed as the 128-bit product D * cmul, cmul ~ 2^(78-ck) / scale, giving
+// 2^32 * code.  Its distance to the value the reference computes,
+// (unsigned)(((x - h - shift) / scale) * 2^29) in FP64 (octree.c:188-190,
+// 251-263), is bounded in k_frame (ceps); when the fraction lies farther than
+// that from an integer the truncations agree, otherwise the exact FP64
+// expression decides.
+__device__ __forceinline__ bool tm_fix47(double x, long long &X)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7ff);
+    if (e > 1035) return false;                              // |x| >= 2^13, inf, nan
+    const unsigned long long m = (b & 0xfffffffffffffull) | (e ? 0x10000000000000ull : 0ull);
+    const int sh = e - 1028;                                  // x * 2^47 = m * 2^(e - 1075 + 47)
+    unsigned long long v = sh >= 0 ? (m << sh) : (sh > -64 ? (m >> (-sh)) : 0ull);
+    X = (b >> 63) ? -(long long)v : (long long)v;
+    return true;
+}
+
+// 2^32 * code from D (D >= 0); ok = false when the integer path cannot decide
+__device__ __forceinline__ uint32_t tm_code_fix(long long D, unsigned long long cmul, int ck, uint32_t ceps,
+                                                bool &ok)
+{
+    if (D < 0) { ok = false; return 0; }
+    const unsigned long long lo = (unsigned long long)D * cmul;
+    const unsigned long long hi = __umul64hi((unsigned long long)D, cmul);
+    const unsigned long long q = (hi << ck) | (lo >> (64 - ck));
+    const uint32_t frac = (uint32_t)q;
+    ok = (hi >> (64 - ck)) == 0 && (q >> 61) == 0 && frac > ceps && frac < 0xffffffffu - ceps;
+    return (uint32_t)(q >> 32);
+}
+
+// the code of x + off (off in {0, -h, +h}) with the exact FP64 fallback
+__device__ __forceinline__ uint32_t tm_lattice_fast(double x, long long Xfx, bool xok, long long offfx, double off,
+                                                    const tm_frame &f, int k, unsigned &slow)
+{
+    bool ok = xok;
+    uint32_t c = 0;
+    if (ok) c = tm_code_fix(Xfx + offfx - f.sh_fx[k], f.cmul, f.ck, f.ceps, ok);
+    if (ok) return c;
+    slow++;
+    return off == 0.0 ? tm_lattice(x, f.shift[k], f.scale) : tm_lattice_off(x, off, f.shift[k], f.scale);
+}
+
 // Split a double into hi (x truncated to 24 significant bits) + lo (float of
 // the remainder) with integer operations only, so no FP64 instruction runs.
 // |x| < 2^-70 flushes to zero; |x| must stay below 2^100.
@@ -208,4 +263,12 @@ struct kahan {
         s = t;
     }
     __device__ __forceinline__ float value() const { return __fsub_rn(s, c); }
+    // add another compensated sum (s2 - c2): TwoSum keeps the rounding of s + s2
+    __device__ __forceinline__ void merge(float s2, float c2)
+    {
+        float t, e;
+        two_sum(s, s2, t, e);
+        c = __fsub_rn(__fadd_rn(c, c2), e);
+        s = t;
+    }
 };

@@ -104,12 +104,17 @@ __global__ void __launch_bounds__(128) k_octree(tm_arrays a, const tm_consts *K)
 
     // query box in lattice codes, octree.c:251-263; half-open [bmin, bmax)
     uint32_t bmin[3], bmax[3];
-    bmin[0] = tm_lattice_off(xp, -T.h, f.shift[0], f.scale);
-    bmin[1] = tm_lattice_off(yp, -T.h, f.shift[1], f.scale);
-    bmin[2] = tm_lattice_off(zp, -T.h, f.shift[2], f.scale);
-    bmax[0] = tm_lattice_off(xp, T.h, f.shift[0], f.scale);
-    bmax[1] = tm_lattice_off(yp, T.h, f.shift[1], f.scale);
-    bmax[2] = tm_lattice_off(zp, T.h, f.shift[2], f.scale);
+    {
+        const double pos[3] = {xp, yp, zp};
+        unsigned slow = 0;
+        for (int k = 0; k < 3; k++) {
+            long long P;
+            const bool ok = tm_fix47(pos[k], P) && T.h < 8192.0;
+            bmin[k] = tm_lattice_fast(pos[k], P, ok, -T.h_fx, -T.h, f, k, slow);
+            bmax[k] = tm_lattice_fast(pos[k], P, ok, T.h_fx, T.h, f, k, slow);
+        }
+        if (slow) atomicAdd(&a.frame[c].codes_slow, (unsigned long long)slow);
+    }
 
     // octlocateregion: the highest differing bit over the three axes
     uint32_t diff = (bmin[0] ^ bmax[0]) | (bmin[1] ^ bmax[1]) | (bmin[2] ^ bmax[2]);

@@ -5,15 +5,17 @@
 // depend on the density.  v (the potential of the last walked candidate) is
 // produced by the octree kernel.
 //
-// Work decomposition: a warp owns 32 Morton-consecutive slots of one colony.
-//  1. stage: the Morton bins covering the union of the 32 query spheres are
+// Work decomposition: a warp owns 8 Morton-consecutive slots of one colony,
+// four lanes per cell.
+//  1. stage: the Morton bins covering the union of the 8 query spheres are
 //     enumerated 32 at a time (one bin per lane), their cell runs are copied
 //     into a shared-memory tile as group-relative FP32 coordinates;
-//  2. test: every lane tests every tile entry against its own cell with a
-//     conservative FP32 squared-distance bound and appends hits to its own
-//     list in shared memory (no divergence: predicated append);
+//  2. test: the four lanes of a cell take every fourth tile entry and test it
+//     against their cell with a conservative FP32 squared-distance bound,
+//     appending hits to their own list in shared memory (predicated append);
 //  3. drain: each lane walks its own list with the exact pair maths, so the
-//     expensive part runs with all lanes busy.
+//     expensive part runs with all lanes busy; the four partial sums of a
+//     cell are combined with shuffles at the end.
 // PREC 0 is the plain FP64 path: every reference expression is evaluated in
 // the same order with separate roundings (no contraction), the cutoff test is
 // fl(sqrt(.)) <= h and the kernel value is rounded to float (inline.h:40).
@@ -27,6 +29,8 @@
 #define FULL 0xffffffffu
 #define PAIR_TILE 128
 #define PAIR_LCAP 64
+#define PAIR_LPC 4                      // lanes per cell
+#define PAIR_CPW (32 / PAIR_LPC)        // cells per warp
 
 template <int PREC>
 struct pair_acc;
@@ -51,7 +55,7 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
     __shared__ int list_s[TM_WARPS_PER_BLOCK][PAIR_LCAP][32];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const long long base = w * 32;
+    const long long base = w * PAIR_CPW;   // colonies are 32-aligned, so a warp stays in one
     if (base >= a.nslots_total) return;
     const int c = a.col[base];
     const tm_desc &d = a.desc[c];
@@ -61,7 +65,8 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
     float4 *tile = tile_s[wib];
     int(*list)[32] = list_s[wib];
 
-    const long long i = base + lane;
+    const int quarter = lane % PAIR_LPC;   // this lane's share of the cell's candidates
+    const long long i = base + lane / PAIR_LPC;
     const bool live = (i - d.off) < d.n;
     const int t = live ? a.ctype[i] : 0;
     const tm_type &T = K->t[t];
@@ -254,10 +259,10 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
                 }
                 __syncwarp();
                 const int wn = (int)min((uint32_t)PAIR_TILE, total - wb);
-                for (int tb = 0; tb < wn; tb += 32) {
-                    const int te = min(wn, tb + 32);
+                for (int tb = 0; tb < wn; tb += 32 * PAIR_LPC) {
+                    const int te = min(wn, tb + 32 * PAIR_LPC);
     #pragma unroll 8
-                    for (int tt = tb; tt < te; tt++) {
+                    for (int tt = tb + quarter; tt < te; tt += PAIR_LPC) {
                         const float4 cc = tile[tt];
                         const float dx = cc.x - gx, dy = cc.y - gy, dz = cc.z - gz;
                         const float s = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
@@ -275,7 +280,27 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
     }
     drain();
 
-    if (!live) return;
+    // combine the partial results of the four lanes of each cell
+    for (int o = 1; o < PAIR_LPC; o <<= 1) {
+        if constexpr (PREC == 0) {
+            acc.dens = add64(acc.dens, __shfl_xor_sync(FULL, acc.dens, o));
+            acc.fx = add64(acc.fx, __shfl_xor_sync(FULL, acc.fx, o));
+            acc.fy = add64(acc.fy, __shfl_xor_sync(FULL, acc.fy, o));
+            acc.fz = add64(acc.fz, __shfl_xor_sync(FULL, acc.fz, o));
+            const double om = __shfl_xor_sync(FULL, acc.mind, o);
+            acc.mind = om < acc.mind ? om : acc.mind;
+        } else {
+            acc.dens.merge(__shfl_xor_sync(FULL, acc.dens.s, o), __shfl_xor_sync(FULL, acc.dens.c, o));
+            acc.fx.merge(__shfl_xor_sync(FULL, acc.fx.s, o), __shfl_xor_sync(FULL, acc.fx.c, o));
+            acc.fy.merge(__shfl_xor_sync(FULL, acc.fy.s, o), __shfl_xor_sync(FULL, acc.fy.c, o));
+            acc.fz.merge(__shfl_xor_sync(FULL, acc.fz.s, o), __shfl_xor_sync(FULL, acc.fz.c, o));
+            acc.mins = fminf(acc.mins, __shfl_xor_sync(FULL, acc.mins, o));
+            acc.err2 += __shfl_xor_sync(FULL, acc.err2, o);
+        }
+        cnt_nb += __shfl_xor_sync(FULL, cnt_nb, o);
+        hash += __shfl_xor_sync(FULL, hash, o);
+    }
+    if (!live || quarter != 0) return;
     if constexpr (PREC == 0) {
         a.density[i] = acc.dens;
         a.mindist[i] = acc.mind;
@@ -352,7 +377,7 @@ __global__ void __launch_bounds__(128) k_density_fix64(tm_arrays a, const tm_con
 
 cudaError_t tm_launch_pair(const tm_arrays &a, const tm_consts *K, int prec, cudaStream_t st)
 {
-    long long warps = a.nslots_total / 32;
+    long long warps = a.nslots_total / PAIR_CPW;
     long long threads = warps * 32;
     int bt = TM_WARPS_PER_BLOCK * 32;
     unsigned grid = (unsigned)((threads + bt - 1) / bt);

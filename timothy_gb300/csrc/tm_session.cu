@@ -369,6 +369,7 @@ extern "C" int tm_session_create(tm_session **out, const tm_session_config *cfg,
         T.cW = host_type_const(cfg->dimension, 0, T.h, T.h2, T.h3, T.h4);
         T.cG = host_type_const(cfg->dimension, 1, T.h, T.h2, T.h3, T.h4);
         T.e = T.h + 0.01;
+        T.h_fx = std::fabs(T.h) < 8192.0 ? (long long)std::ldexp(T.h, 47) : 0;
         T.randommove = types->randommove ? types->randommove[t] : 0.0f;
         T.hf = (float)T.h;
         T.h2f = (float)(T.h * T.h);
@@ -1022,6 +1023,7 @@ extern "C" int tmi_set_types(tm_session *s, const tm_celltypes *types)
         T.cW = host_type_const(K.dim, 0, T.h, T.h2, T.h3, T.h4);
         T.cG = host_type_const(K.dim, 1, T.h, T.h2, T.h3, T.h4);
         T.e = T.h + 0.01;
+        T.h_fx = std::fabs(T.h) < 8192.0 ? (long long)std::ldexp(T.h, 47) : 0;
         T.randommove = types->randommove ? types->randommove[t] : 0.0f;
         T.hf = (float)T.h;
         T.h2f = (float)(T.h * T.h);
