@@ -27,7 +27,7 @@
 #include "tm_kernels.cuh"
 
 #define FULL 0xffffffffu
-#define PAIR_TILE 128
+#define PAIR_TILE 256
 #define PAIR_LCAP 64
 #define PAIR_LPC 4                      // lanes per cell
 #define PAIR_CPW (32 / PAIR_LPC)        // cells per warp
@@ -51,8 +51,12 @@ struct pair_acc<1> {
 template <int PREC>
 __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, const tm_consts *K)
 {
-    __shared__ float4 tile_s[TM_WARPS_PER_BLOCK][PAIR_TILE];
-    __shared__ int list_s[TM_WARPS_PER_BLOCK][PAIR_LCAP][32];
+    // per warp: tile of staged candidates (A: hi part of the origin-relative
+    // position + slot, B: lo part + radius) and one hit list per lane holding
+    // tile indices
+    __shared__ float4 tA_s[TM_WARPS_PER_BLOCK][PAIR_TILE];
+    __shared__ float4 tB_s[TM_WARPS_PER_BLOCK][PAIR_TILE];
+    __shared__ unsigned short list_s[TM_WARPS_PER_BLOCK][PAIR_LCAP][32];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long long base = w * PAIR_CPW;   // colonies are 32-aligned, so a warp stays in one
@@ -62,8 +66,9 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
     if (!d.active || d.precision != PREC || d.n <= 1) return;   // potential.c:89
     const tm_frame &f = a.frame[c];
     const int dim = K->dim;
-    float4 *tile = tile_s[wib];
-    int(*list)[32] = list_s[wib];
+    float4 *tA = tA_s[wib];
+    float4 *tB = tB_s[wib];
+    unsigned short(*list)[32] = list_s[wib];
 
     const int quarter = lane % PAIR_LPC;   // this lane's share of the cell's candidates
     const long long i = base + lane / PAIR_LPC;
@@ -71,11 +76,10 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
     const int t = live ? a.ctype[i] : 0;
     const tm_type &T = K->t[t];
 
-    // Subgroups: lanes whose cells share a Morton node two levels above the
-    // bins.  32 Morton-consecutive cells can straddle a high-level boundary
-    // (e.g. the last cell of one octant and the first of the next), and a
-    // single union box would then span much of the colony; a node of the
-    // subgroup depth bounds every subgroup's box to a few bins per axis.
+    // Subgroups: cells sharing a Morton node two levels above the bins.
+    // Morton-consecutive cells can straddle a high-level boundary (the last
+    // cell of one octant and the first of the next), and one union box would
+    // then span much of the colony; the subgroup node bounds every box.
     const int L = f.L;
     const int Lg = L >= 2 ? L - 2 : 0;
     const uint32_t key = live ? tm_prefix(a.codes[i], Lg) : 0xffffffffu;
@@ -91,12 +95,12 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
             rem &= ~__ballot_sync(FULL, member);
         }
     }
-    float4 hi_i = live ? a.hi[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-    float4 lo_i = live ? a.lo[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 hi_i = live ? a.hi[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 lo_i = live ? a.lo[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     // origin: the float position of the subgroup's first cell
     const float ox = __shfl_sync(FULL, hi_i.x, my_leader), oy = __shfl_sync(FULL, hi_i.y, my_leader),
                 oz = __shfl_sync(FULL, hi_i.z, my_leader);
-    // double-float origin-relative coordinates (s + e == x - o up to ~2^-47 |x|)
+    // double-float origin-relative position: s (exact sum) + e (its error + lo part)
     float sx, sy, sz, ex, ey, ez;
     two_sum(hi_i.x, -ox, sx, ex);
     two_sum(hi_i.y, -oy, sy, ey);
@@ -104,8 +108,7 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
     ex += lo_i.x;
     ey += lo_i.y;
     ez += lo_i.z;
-    const float gx = sx + ex, gy = sy + ey, gz = sz + ez;   // single-float form for the test
-    // conservative test radius: FP32 staging errors are < 1e-5 here
+    // conservative test radius: the test uses s only (|e| < 1e-5 here)
     const float hr = T.hf * 1.00002f + 1e-4f;
     const int nside = 1 << L;
     const float bs = f.binscale;
@@ -125,12 +128,15 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
     unsigned long long hash = 0;
     int nl = 0;
 
+    // exact pair maths over this lane's hit list (tile indices)
     auto drain = [&]() {
         int m = nl;
         for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(FULL, m, o));
         for (int q = 0; q < m; q++) {
             if (q >= nl) continue;
-            const int j = list[q][lane];
+            const int ti = list[q][lane];
+            const float4 A = tA[ti];
+            const int j = __float_as_int(A.w);
             if constexpr (PREC == 0) {
                 const double xj = a.x[j], yj = a.y[j], zj = a.z[j];
                 const double dx = sub64(xi, xj), dy = sub64(yi, yj), dz = sub64(zi, zj);
@@ -158,14 +164,10 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
                     if (a.want_diag) hash += tm_mix64((unsigned long long)a.perm[j] + 1ull);
                 }
             } else {
-                const float4 hj = a.hi[j], lj = a.lo[j];
-                float s2, e2;
-                two_sum(hj.x, -ox, s2, e2);
-                const float dx = (s2 - sx) + ((e2 + lj.x) - ex);
-                two_sum(hj.y, -oy, s2, e2);
-                const float dy = (s2 - sy) + ((e2 + lj.y) - ey);
-                two_sum(hj.z, -oz, s2, e2);
-                const float dz = (s2 - sz) + ((e2 + lj.z) - ez);
+                const float4 B = tB[ti];
+                const float dx = (A.x - sx) + (B.x - ex);
+                const float dy = (A.y - sy) + (B.y - ey);
+                const float dz = (A.z - sz) + (B.z - ez);
                 const float s = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
                 bool in = s <= T.thr_lo;
                 if (!in && s <= T.thr_hi) {
@@ -188,7 +190,7 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
                         wk = T.cWf * (2.0f * omu * omu * omu);
                         wg = -omu * omu;
                     }
-                    const float term = T.kmassf * hj.w * wk;
+                    const float term = T.kmassf * B.w * wk;
                     acc.dens.add(term);
                     // one-sigma rounding estimate of this term: W ~ (1-u)^3 amplifies
                     // the FP32 error of (1 - u) near the cutoff
@@ -206,6 +208,26 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
         nl = 0;
     };
 
+    // test the staged tile [0, fill) and drain; the tile is refilled afterwards
+    auto test_tile = [&](int fill, float thr) {
+        for (int tb = 0; tb < fill; tb += 32 * PAIR_LPC) {
+            const int te = min(fill, tb + 32 * PAIR_LPC);
+#pragma unroll 8
+            for (int tt = tb + quarter; tt < te; tt += PAIR_LPC) {
+                const float4 cc = tA[tt];
+                const float dx = cc.x - sx, dy = cc.y - sy, dz = cc.z - sz;
+                const float s = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                if (s <= thr && (long long)__float_as_int(cc.w) != i) {
+                    list[nl][lane] = (unsigned short)tt;
+                    nl++;
+                }
+            }
+            if (__any_sync(FULL, nl > PAIR_LCAP - 32)) drain();
+        }
+        drain();
+        __syncwarp();
+    };
+
     unsigned pending = live_mask;
     while (pending) {
         const int ldr = __ffs(pending) - 1;
@@ -214,8 +236,8 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
         const float gox = __shfl_sync(FULL, ox, ldr), goy = __shfl_sync(FULL, oy, ldr), goz = __shfl_sync(FULL, oz, ldr);
         const float thr = member ? hr * hr : -1.0f;
         // union of the members' query boxes, relative to the subgroup origin
-        float mnx = member ? gx - hr : 3e38f, mny = member ? gy - hr : 3e38f, mnz = member ? gz - hr : 3e38f;
-        float mxx = member ? gx + hr : -3e38f, mxy = member ? gy + hr : -3e38f, mxz = member ? gz + hr : -3e38f;
+        float mnx = member ? sx - hr : 3e38f, mny = member ? sy - hr : 3e38f, mnz = member ? sz - hr : 3e38f;
+        float mxx = member ? sx + hr : -3e38f, mxy = member ? sy + hr : -3e38f, mxz = member ? sz + hr : -3e38f;
         for (int o = 16; o > 0; o >>= 1) {
             mnx = fminf(mnx, __shfl_xor_sync(FULL, mnx, o));
             mny = fminf(mny, __shfl_xor_sync(FULL, mny, o));
@@ -229,6 +251,7 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
         const int bz0 = binof(mnz, goz, f.shiftf[2], -0.01f), bz1 = binof(mxz, goz, f.shiftf[2], 0.01f);
         const int nbx = bx1 - bx0 + 1, nby = by1 - by0 + 1, nbz = bz1 - bz0 + 1;
         const int nb = nbx * nby * nbz;
+        int fill = 0;   // entries staged in the tile
         for (int chunk = 0; chunk < nb; chunk += 32) {
             const int q = chunk + lane;
             long long st = 0;
@@ -244,41 +267,49 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
             }
             uint32_t incl = cnt;
             for (int o = 1; o < 32; o <<= 1) {
-                uint32_t y = __shfl_up_sync(FULL, incl, o);
+                const uint32_t y = __shfl_up_sync(FULL, incl, o);
                 if (lane >= o) incl += y;
             }
             const uint32_t total = __shfl_sync(FULL, incl, 31);
             const uint32_t off = incl - cnt;
-            for (uint32_t wb = 0; wb < total; wb += PAIR_TILE) {
-                const uint32_t k0 = max(off, wb), k1 = min(off + cnt, wb + PAIR_TILE);
-                for (uint32_t k = k0; k < k1; k++) {
-                    const long long j = st + (k - off);
+            // copy the chunk's candidates [0, total) into the tile with parallel,
+            // coalesced loads: candidate k lives in the bin of the first lane whose
+            // inclusive count exceeds k
+            for (uint32_t k0 = 0; k0 < total; k0 += 32) {
+                const uint32_t k = min(k0 + lane, total - 1);
+                int b = 0;
+#pragma unroll
+                for (int step = 16; step >= 1; step >>= 1) {
+                    const uint32_t v = __shfl_sync(FULL, incl, b + step - 1);
+                    if (v <= k) b += step;
+                }
+                const long long stb = __shfl_sync(FULL, st, b);
+                const uint32_t offb = __shfl_sync(FULL, off, b);
+                const int slot = fill + lane;
+                const bool valid = k0 + lane < total;
+                if (valid) {
+                    const long long j = stb + (k - offb);
                     const float4 hj = a.hi[j], lj = a.lo[j];
-                    tile[k - wb] = make_float4((hj.x - gox) + lj.x, (hj.y - goy) + lj.y, (hj.z - goz) + lj.z,
-                                               __int_as_float((int)j));
+                    float s1, e1, s2, e2, s3, e3;
+                    two_sum(hj.x, -gox, s1, e1);
+                    two_sum(hj.y, -goy, s2, e2);
+                    two_sum(hj.z, -goz, s3, e3);
+                    tA[slot] = make_float4(s1, s2, s3, __int_as_float((int)j));
+                    tB[slot] = make_float4(e1 + lj.x, e2 + lj.y, e3 + lj.z, hj.w);
                 }
-                __syncwarp();
-                const int wn = (int)min((uint32_t)PAIR_TILE, total - wb);
-                for (int tb = 0; tb < wn; tb += 32 * PAIR_LPC) {
-                    const int te = min(wn, tb + 32 * PAIR_LPC);
-    #pragma unroll 8
-                    for (int tt = tb + quarter; tt < te; tt += PAIR_LPC) {
-                        const float4 cc = tile[tt];
-                        const float dx = cc.x - gx, dy = cc.y - gy, dz = cc.z - gz;
-                        const float s = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                        const int j = __float_as_int(cc.w);
-                        if (s <= thr && (long long)j != i) {
-                            list[nl][lane] = j;
-                            nl++;
-                        }
-                    }
-                    if (__any_sync(FULL, nl > PAIR_LCAP - 32)) drain();
+                fill += min(32u, total - k0);
+                if (fill > PAIR_TILE - 32) {
+                    __syncwarp();
+                    test_tile(fill, thr);
+                    fill = 0;
                 }
-                __syncwarp();
             }
         }
+        if (fill > 0) {
+            __syncwarp();
+            test_tile(fill, thr);
+        }
     }
-    drain();
 
     // combine the partial results of the four lanes of each cell
     for (int o = 1; o < PAIR_LPC; o <<= 1) {
