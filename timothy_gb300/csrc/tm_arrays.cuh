@@ -56,6 +56,7 @@ struct tm_arrays {
     // outputs (Morton order)
     double *density, *v, *mindist, *fx, *fy, *fz;
     int *nbcount;
+    int *nbmin;          // first (Morton) slot within h, -1 if none
     unsigned long long *nbhash;
     int *vcand;
     // CIC grids

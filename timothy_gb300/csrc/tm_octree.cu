@@ -101,6 +101,24 @@ __global__ void __launch_bounds__(128) k_octree(tm_arrays a, const tm_consts *K)
     const int t = a.ctype[p];
     const tm_type &T = K->t[t];
     const double xp = a.x[p], yp = a.y[p], zp = a.z[p];
+    const bool isolated = a.nbcount[p] == 0;
+    // v is potential(p, j*) and j* precedes every within-h neighbour in Morton
+    // order, so v can only be non-zero when j* is the first within-h
+    // neighbour m and m overlaps p (xc > 0, potential.c:63-65); otherwise v = 0
+    // without walking.  The overlap is excluded with a margin in FP32.
+    bool need_walk = isolated || a.want_diag;
+    if (!need_walk) {
+        const int m = a.nbmin[p];
+        const float4 hp = a.hi[p], lp = a.lo[p], hm = a.hi[m], lm = a.lo[m];
+        const float dx = (hp.x - hm.x) + (lp.x - lm.x), dy = (hp.y - hm.y) + (lp.y - lm.y),
+                    dz = (hp.z - hm.z) + (lp.z - lm.z);
+        const float rs = (hp.w + hm.w) * 1.0001f + 1e-5f;
+        need_walk = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < rs * rs;
+    }
+    if (!need_walk) {
+        a.v[p] = 0.0;
+        return;
+    }
 
     // query box in lattice codes, octree.c:251-263; half-open [bmin, bmax)
     uint32_t bmin[3], bmax[3];
@@ -146,7 +164,6 @@ __global__ void __launch_bounds__(128) k_octree(tm_arrays a, const tm_consts *K)
         }
     }
 
-    const bool isolated = a.nbcount[p] == 0;
     long long jstar = -1;
     double mind = 1.7976931348623157e308;
     if (a1 > a0 && a1 - a0 >= 2) {

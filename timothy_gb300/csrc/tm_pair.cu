@@ -30,6 +30,9 @@
 #define PAIR_TILE 256
 #define PAIR_LCAP 64
 #define PAIR_LPC 4                      // lanes per cell
+#ifndef PAIR_LSHIFT
+#define PAIR_LSHIFT 1                   // candidate nodes one level above the bins
+#endif
 #define PAIR_CPW (32 / PAIR_LPC)        // cells per warp
 
 template <int PREC>
@@ -82,6 +85,10 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
     // then span much of the colony; the subgroup node bounds every box.
     const int L = f.L;
     const int Lg = L >= 2 ? L - 2 : 0;
+    // candidate ranges come from nodes PAIR_LSHIFT levels above the bins: each
+    // is one contiguous run of 8^PAIR_LSHIFT bins in Morton order
+    const int ls = L > PAIR_LSHIFT ? PAIR_LSHIFT : 0;
+    const int Lp = L - ls;
     const uint32_t key = live ? tm_prefix(a.codes[i], Lg) : 0xffffffffu;
     const unsigned live_mask = __ballot_sync(FULL, live);
     int my_leader = 0;
@@ -110,8 +117,8 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
     ez += lo_i.z;
     // conservative test radius: the test uses s only (|e| < 1e-5 here)
     const float hr = T.hf * 1.00002f + 1e-4f;
-    const int nside = 1 << L;
-    const float bs = f.binscale;
+    const int nside = 1 << Lp;
+    const float bs = f.binscale * (1.0f / (float)(1 << ls));
     auto binof = [&](float g, float o, float sh, float eps) {
         float v = (o - sh + g) * bs + eps;
         int b = (int)floorf(v);
@@ -125,6 +132,7 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
     pair_acc<PREC> acc;
     acc.init();
     int cnt_nb = 0;
+    int nbmin = 0x7fffffff;   // smallest slot (= first in Morton order) within h
     unsigned long long hash = 0;
     int nl = 0;
 
@@ -161,6 +169,7 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
                     acc.fy = add64(acc.fy, div64(mul64(wc, sub64(yj, yi)), dist));
                     if (dim == 3) acc.fz = add64(acc.fz, div64(mul64(wc, sub64(zj, zi)), dist));
                     cnt_nb++;
+                    nbmin = min(nbmin, j);
                     if (a.want_diag) hash += tm_mix64((unsigned long long)a.perm[j] + 1ull);
                 }
             } else {
@@ -201,6 +210,7 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
                     acc.fy.add(g * dy);
                     if (dim == 3) acc.fz.add(g * dz);
                     cnt_nb++;
+                    nbmin = min(nbmin, j);
                     if (a.want_diag) hash += tm_mix64((unsigned long long)a.perm[j] + 1ull);
                 }
             }
@@ -250,20 +260,30 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
         const int by0 = binof(mny, goy, f.shiftf[1], -0.01f), by1 = binof(mxy, goy, f.shiftf[1], 0.01f);
         const int bz0 = binof(mnz, goz, f.shiftf[2], -0.01f), bz1 = binof(mxz, goz, f.shiftf[2], 0.01f);
         const int nbx = bx1 - bx0 + 1, nby = by1 - by0 + 1, nbz = bz1 - bz0 + 1;
-        const int nb = nbx * nby * nbz;
         int fill = 0;   // entries staged in the tile
-        for (int chunk = 0; chunk < nb; chunk += 32) {
-            const int q = chunk + lane;
+        // lanes cover whole rows of nbx bins (nbx <= 32; wider boxes use one
+        // row per chunk pass over bx in steps of 32)
+        const int rowlen = min(nbx, 32);
+        const int rows_per = 32 / rowlen;
+        const int my_row = lane / rowlen, my_col = lane % rowlen;
+        const int nrows = nby * nbz;
+        const int xpasses = (nbx + 31) / 32;
+        const float inv_nby = 1.0f / (float)nby;
+        for (int chunk = 0; chunk < nrows * xpasses; chunk += rows_per) {
+            const int rr = chunk + my_row;               // row-pass index
+            const int xp = xpasses == 1 ? 0 : rr % xpasses;
+            const int row = xpasses == 1 ? rr : rr / xpasses;
+            const int bxo = xp * 32 + my_col;
             long long st = 0;
             uint32_t cnt = 0;
-            if (q < nb) {
-                const int bx = bx0 + q % nbx;
-                const int by = by0 + (q / nbx) % nby;
-                const int bz = bz0 + q / (nbx * nby);
-                const uint32_t m = tm_morton((uint32_t)bx, (uint32_t)by, (uint32_t)bz);
+            if (my_row < rows_per && row < nrows && bxo < nbx) {
+                const int bz = bz0 + (int)(((float)row + 0.5f) * inv_nby);
+                const int by = by0 + row - (bz - bz0) * nby;
+                const int bx = bx0 + bxo;
+                const uint32_t m = tm_morton((uint32_t)bx, (uint32_t)by, (uint32_t)bz) << (3 * ls);
                 const uint32_t s0 = bstart[m];
                 st = bbase + s0;
-                cnt = bstart[m + 1] - s0;
+                cnt = bstart[m + (1u << (3 * ls))] - s0;
             }
             uint32_t incl = cnt;
             for (int o = 1; o < 32; o <<= 1) {
@@ -329,6 +349,7 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
             acc.err2 += __shfl_xor_sync(FULL, acc.err2, o);
         }
         cnt_nb += __shfl_xor_sync(FULL, cnt_nb, o);
+        nbmin = min(nbmin, __shfl_xor_sync(FULL, nbmin, o));
         hash += __shfl_xor_sync(FULL, hash, o);
     }
     if (!live || quarter != 0) return;
@@ -353,6 +374,7 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
         a.fz[i] = (double)acc.fz.value();
     }
     a.nbcount[i] = cnt_nb;
+    a.nbmin[i] = cnt_nb ? nbmin : -1;
     if (a.want_diag) a.nbhash[i] = hash;
 }
 

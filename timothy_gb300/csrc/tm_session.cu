@@ -154,6 +154,7 @@ __global__ void k_colony_init(tm_arrays a, int c, long long off, int n, int nslo
     a.fy[i] = 0.0;
     a.fz[i] = 0.0;
     a.nbcount[i] = 0;
+    a.nbmin[i] = -1;
     if (a.nbhash) a.nbhash[i] = 0;
     if (a.vcand) a.vcand[i] = -1;
 }
@@ -413,7 +414,7 @@ extern "C" int tm_session_create(tm_session **out, const tm_session_config *cfg,
     s->mass_types = K.ntypes;
     AL(a.bin_count, B + 1) AL(a.bin_cursor, B + 1) AL(a.bin_start, B + 1) AL(a.bigbins, 2 * (S / 33) + 4)
     AL(a.fix_count, 1) AL(a.fix_list, S)
-    AL(a.density, S) AL(a.v, S) AL(a.mindist, S) AL(a.fx, S) AL(a.fy, S) AL(a.fz, S) AL(a.nbcount, S)
+    AL(a.density, S) AL(a.v, S) AL(a.mindist, S) AL(a.fx, S) AL(a.fy, S) AL(a.fz, S) AL(a.nbcount, S) AL(a.nbmin, S)
     AL(a.grid, G) AL(a.desc, C) AL(a.frame, C)
     AL(s->scan_tmp, tm_scan_tmp_words(B + 1)) AL(s->d_octsize, C) AL(s->dK, 1)
     if (rc == TM_OK) rc = dalloc((double **)&s->d_scratch, S);
@@ -457,7 +458,7 @@ extern "C" int tm_session_destroy(tm_session *s)
     void *ptrs[] = {a.x, a.y, a.z, a.size, a.young, a.ctype, a.phase, a.perm, a.rem, a.x2, a.y2, a.z2, a.size2,
                     a.young2, a.ctype2, a.phase2, a.perm2, a.rem2, a.col, a.code, a.codes, a.bin, a.tmp, a.hi, a.lo,
                     a.mass, a.bin_count, a.bin_cursor, a.bin_start, a.bigbins, a.fix_count, a.fix_list, a.density, a.v, a.mindist, a.fx,
-                    a.fy, a.fz, a.nbcount, a.nbhash, a.vcand, a.grid, a.desc, a.frame, s->scan_tmp, s->d_octsize,
+                    a.fy, a.fz, a.nbcount, a.nbmin, a.nbhash, a.vcand, a.grid, a.desc, a.frame, s->scan_tmp, s->d_octsize,
                     s->dK, s->d_scratch};
     for (void *p : ptrs)
         if (p) cudaFree(p);
