@@ -150,6 +150,26 @@ int64_t tm_session_launches(tm_session *s);
 int tm_host_register(void *ptr, int64_t bytes);
 int tm_host_unregister(void *ptr);
 
+/* No counterpart in the reference.  CIC deposit of n cells onto field 0 of a
+ * grid, the work of patches_alloc + patches_cells2envinfo at one rank, for
+ * callers that cannot allocate device memory: code running while a CUDA
+ * graph is captured, host programs with a fixed device-memory budget, or
+ * real-time loops where an allocation may block.  Every input and output is
+ * the caller's device memory: x, y, z (double), phase (int) in caller order;
+ * grid (double, gsize[0]*gsize[1]*gsize[2], x-major with z fastest), zeroed
+ * and then deposited; corners (int64[6]: lower x,y,z then upper x,y,z of the
+ * touched nodes).  The call is asynchronous on `stream` (a cudaStream_t, 0
+ * for the default stream) and allocates nothing: its scratch is a fixed
+ * 3 MiB array in device memory, held by every GPU that loads the library
+ * until the process exits, which limits n to 16,777,216 cells (larger n
+ * returns TM_EINVAL).  The first call on a device looks up that array's
+ * address; make it before any stream capture.  All calls share the array,
+ * so calls that overlap on the GPU (other streams, other host threads)
+ * race and must be serialised by the caller. */
+int tm_cic_deposit_noalloc(const double *x, const double *y, const double *z, const int *phase, int64_t n,
+                           int dimension, const double lower[3], float resolution, const int64_t gsize[3],
+                           double *grid, int64_t *corners, void *stream);
+
 /* Slots and memory still free (admission control). */
 int tm_session_capacity(tm_session *s, int64_t *free_slots, int64_t *free_bins, int *free_colonies);
 

@@ -207,8 +207,11 @@ class DropinRun:
             lib.patches_cells2envinfo(self.si, self.st, C.byref(p), C.byref(self.ci), C.byref(self.grid))
             # at one rank the patch is added into the zeroed grid (patches.c:321-367)
             dep = np.zeros(self.gsize)
+            self.patch_corners = None
             if p.intersect and p.intersect[0]:
                 lo = p.lowercorner[0]
+                up = p.uppercorner[0]
+                self.patch_corners = (lo.x, lo.y, lo.z, up.x, up.y, up.z)
                 sz = p.size[0]
                 vol = sz.x * sz.y * sz.z
                 patch = np.ctypeslib.as_array(p.data[0], shape=(vol,)).reshape(sz.x, sz.y, sz.z).copy()
