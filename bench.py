@@ -228,6 +228,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--list-capacity", type=int, default=256,
+                    help="neighbour-list entries per cell (0: search the bins every step)")
+    ap.add_argument("--rmax", type=int, default=16, help="rebuild the neighbour lists at least every rmax steps")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     wl = dict(WORKLOADS[args.workload])
@@ -245,8 +248,9 @@ def main():
     prec = wl["precision"]
 
     def new_session(p):
-        s = S.Session(col.types, dim=3, max_slots=n + 64, device=local)
-        cid = s.add_colony(col, precision=p, update="dt", dt=wl["dt"], cic=wl["cic"])
+        s = S.Session(col.types, dim=3, max_slots=n + 64, device=local, list_capacity=args.list_capacity)
+        cid = s.add_colony(col, precision=p, update="dt", dt=wl["dt"], cic=wl["cic"],
+                           verlet=args.list_capacity > 0, rmax=args.rmax)
         return s, cid
 
     s, cid = new_session(prec)
@@ -254,6 +258,7 @@ def main():
     s.sync()
     nbc = s.download(cid, ["nbcount"])["nbcount"]
     mean_nb, max_nb = float(nbc.mean()), int(nbc.max())
+    rb0 = s.stats(cid)["list_rebuilds"]
     s.profile(True)
     clocks = ClockSampler(local)
     clocks.start()
@@ -267,6 +272,7 @@ def main():
     s.sync()
     prof = s.profile_read()
     s.profile(False)
+    rebuilds = s.stats(cid)["list_rebuilds"] - rb0
     ms_max = dist_max(pg, ms)
     ms_per_step = ms_max / args.steps
     value = n * world * args.steps / (ms_max * 1e-3)
@@ -355,6 +361,8 @@ def main():
             "config": {"workload": args.workload, "kind": kind, "cells": n, "seed": seed, "radius": radius,
                        "h": 2.5, "dt": wl["dt"], "cic": wl["cic"], "precision": prec,
                        "mean_neighbours": mean_nb, "max_neighbours": max_nb,
+                       "neighbour_lists": {"capacity": args.list_capacity, "skin": 0.25, "rmax": args.rmax,
+                                           "rebuilds_in_timed_steps": rebuilds},
                        "l2": "inputs larger than L2 (state %.1f GB)" % (n * 250 / 1e9),
                        "parallelism": f"replicas x{world}"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk}

@@ -62,6 +62,7 @@ typedef struct {
     int64_t max_bin_entries;  /* 0: derived from max_slots */
     int64_t max_grid_entries; /* 0: one 257^3 grid */
     int diagnostics;          /* fill neighbour counts/fingerprints and v candidates */
+    int list_capacity;        /* neighbour-list entries per cell (multiple of 4); 0: none */
 } tm_session_config;
 
 /* One colony's cells in caller order (host memory). */
@@ -81,6 +82,9 @@ typedef struct {
     float gfh;                /* grid resolution (settings.gfh) */
     int lcap;                 /* deepest bin level, 0: from the colony's extent */
     int64_t reserve;          /* slots to reserve (>= n) so later uploads can grow */
+    int verlet;               /* 1: keep neighbour lists within h + skin between rebuilds */
+    float skin;               /* list margin (0: 0.1 h) */
+    int rmax;                 /* rebuild the lists at least every rmax steps (0: 16) */
 } tm_colony_options;
 
 /* Outputs in caller order (host memory); any pointer may be NULL. */
@@ -104,6 +108,8 @@ typedef struct {
     uint32_t device_errors;           /* TM_DEVERR_* */
     int bin_level;
     int64_t n;
+    int64_t list_rebuilds;            /* steps that rebuilt the neighbour lists */
+    int64_t codes_slow;               /* lattice codes of the last step decided in FP64 */
 } tm_colony_info;
 
 const char *tm_last_error(void);

@@ -1,0 +1,93 @@
+"""Neighbour lists (Verlet mode): steps between rebuilds reuse lists of
+neighbours within h + skin but decide the cutoff every step, so every step's
+results must equal the search-every-step path and the oracle."""
+import numpy as np
+import pytest
+
+from timothy_gb300 import colonies as C
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b, floor=1e-300):
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), floor), initial=0.0))
+
+
+def check64(out, ref, tag):
+    for k in ("x", "y", "z"):
+        assert rel(out[k], getattr(ref, k), 1.0) <= 1e-12, (tag, k)
+    assert rel(out["density"], ref.density) <= 1e-12, tag
+    fin = ref.mindist < 1e300
+    assert rel(out["mindist"][fin], ref.mindist[fin]) <= 1e-12, tag
+    vs = max(np.max(np.abs(ref.v)), 1e-300)
+    assert np.max(np.abs(out["v"] - ref.v)) <= 1e-12 * vs, tag
+    fs = np.max(np.abs(np.stack([ref.fx, ref.fy, ref.fz])))
+    for k in ("fx", "fy", "fz"):
+        assert np.max(np.abs(out[k] - getattr(ref, k))) <= 1e-12 * fs, (tag, k)
+
+
+@pytest.mark.parametrize("dt,steps", [(0.01, 30), (0.5, 12)])
+def test_verlet_fp64_multistep_matches_oracle(oracle_lib, dt, steps):
+    from timothy_gb300 import session as S
+
+    col = C.make_colony("clustered", 30000, 31, C.initial_radius("clustered", 30000))
+    out, st = S.run_colony(col, steps, precision="fp64", update="dt", dt=dt, verlet=True, rmax=16)
+    ref = oracle_lib.run(col, steps, which="oracle", update_mode=1, dt=dt)
+    check64(out, ref, f"dt={dt}")
+    assert st["octsize"] == ref.octsize
+    assert st["list_rebuilds"] >= 2          # first step + age or displacement
+    assert st["list_rebuilds"] < steps or dt > 0.1
+
+
+def test_verlet_neighbour_sets_exact_between_rebuilds(oracle_lib):
+    from timothy_gb300 import session as S
+
+    col = C.make_colony("uniform", 20000, 32, C.initial_radius("uniform", 20000))
+    with S.Session(col.types, max_slots=col.n + 64, diagnostics=True, list_capacity=256) as s:
+        cid = s.add_colony(col, precision="fp64", update="dt", dt=0.01, verlet=True, rmax=16)
+        s.step(5)
+        s.sync()
+        pos = s.download(cid, ["x", "y", "z"])
+        s.set_active(cid, True)
+        # one more step without moving, then compare on the same positions
+        s.step(1)
+        s.sync()
+        st = s.stats(cid)
+    assert st["list_rebuilds"] == 1
+    moved = C.Colony(pos["x"], pos["y"], pos["z"], col.size, col.young, col.ctype, col.phase, col.types)
+    out, _ = S.run_colony(moved, 1, precision="fp64", update="none", diagnostics=True)
+    nb = oracle_lib.neighbours(moved)
+    assert np.array_equal(out["nbcount"], nb.count)
+    assert np.array_equal(out["nbhash"], nb.hash)
+    assert np.array_equal(out["vcand"], nb.vcand)
+
+
+def test_verlet_step_outputs_equal_search_every_step():
+    from timothy_gb300 import session as S
+
+    col = C.make_colony("clustered", 25000, 33, C.initial_radius("clustered", 25000))
+    a, sa = S.run_colony(col, 10, precision="fp64", update="dt", dt=0.02, verlet=True, diagnostics=True)
+    b, sb = S.run_colony(col, 10, precision="fp64", update="dt", dt=0.02, verlet=False, diagnostics=True)
+    assert sa["list_rebuilds"] < 10
+    assert np.array_equal(a["nbcount"], b["nbcount"])
+    assert np.array_equal(a["nbhash"], b["nbhash"])
+    assert np.array_equal(a["vcand"], b["vcand"])
+    assert rel(a["density"], b["density"]) <= 1e-13
+    fs = np.max(np.abs(np.stack([b["fx"], b["fy"], b["fz"]])))
+    for k in ("fx", "fy", "fz"):
+        assert np.max(np.abs(a[k] - b[k])) <= 1e-13 * fs
+
+
+def test_verlet_fp32_against_fp64():
+    from timothy_gb300 import session as S
+
+    col = C.make_colony("clustered", 40000, 34, C.initial_radius("clustered", 40000))
+    o64, _ = S.run_colony(col, 8, precision="fp64", update="dt", dt=0.01, verlet=True, diagnostics=True)
+    o32, s32 = S.run_colony(col, 8, precision="fp32c", update="dt", dt=0.01, verlet=True, diagnostics=True)
+    assert s32["list_rebuilds"] < 8
+    assert np.array_equal(o32["nbcount"], o64["nbcount"])
+    pos = o64["density"] > 0
+    assert rel(o32["density"][pos], o64["density"][pos]) <= 1e-6
+    f64 = np.stack([o64["fx"], o64["fy"], o64["fz"]])
+    f32 = np.stack([o32["fx"], o32["fy"], o32["fz"]])
+    assert np.max(np.abs(f32 - f64)) <= 1e-6 * np.max(np.abs(f64))

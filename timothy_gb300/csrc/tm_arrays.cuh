@@ -20,6 +20,9 @@ struct tm_desc {
     int precision;       // 0 plain FP64, 1 FP32 + compensated
     int update_mode;     // 0 reference x += F (+ random move), 1 x += dt*F, 2 none
     int active;          // 0: skipped by every kernel
+    int verlet;          // 1: reuse neighbour lists between rebuilds
+    float skin;          // list radius is h + skin
+    int rmax;            // rebuild at least every rmax steps
     double dt;
     // CIC grid geometry (grid.c:37-136 at one rank)
     double glower[3];
@@ -44,7 +47,8 @@ struct tm_arrays {
     uint4 *code;         // lattice codes in the pre-sort order
     uint4 *codes;        // lattice codes in Morton order
     uint32_t *bin;       // global bin-table index of each pre-sort slot
-    int *tmp;            // new slot -> old slot
+    int *tmp;            // Morton position -> slot
+    int *rank;           // slot -> Morton position
     float4 *hi, *lo;     // FP32 split positions (hi.w = size)
     double *mass;        // FP64 density weights sc_t * (size / csize_t), [type][slot]
     // bin table
@@ -56,7 +60,14 @@ struct tm_arrays {
     // outputs (Morton order)
     double *density, *v, *mindist, *fx, *fy, *fz;
     int *nbcount;
-    int *nbmin;          // first (Morton) slot within h, -1 if none
+    int *nbmin;          // first Morton position within h, -1 if none
+    // neighbour lists: quarter q of cell `slot` holds vcount[q*lstride+slot]
+    // entries vlist[(q*qcap + k)*lstride + slot] (slots), k-major for coalescing
+    int *vlist;
+    int *vcount;
+    float4 *x0;          // float position at the last rebuild (displacement test)
+    long long lstride;
+    int qcap;
     unsigned long long *nbhash;
     int *vcand;
     // CIC grids

@@ -28,6 +28,23 @@ __global__ void k_step_init(tm_arrays a)
     f.nbig = 0;
     f.boundary_pairs = 0;
     f.codes_slow = 0;
+    // Neighbour lists stay valid while no pair can have come from beyond
+    // h + skin to within h: every cell moved less than skin/2 since the lists
+    // were built (maxdisp carries a float-rounding margin).
+    const tm_desc &d = a.desc[c];
+    const bool rb = !d.verlet || f.force_rebuild || !f.list_ok || f.age + 1 >= d.rmax ||
+                    2.0f * __uint_as_float(f.maxdisp) + 1e-3f >= d.skin;
+    f.rebuild = rb ? 1 : 0;
+    f.ident = f.rebuild;
+    if (rb) {
+        f.age = 0;
+        f.rebuilds++;
+        f.list_ok = d.verlet;      // cleared again if a list overflows
+    } else {
+        f.age++;
+    }
+    f.force_rebuild = 0;
+    f.maxdisp = 0u;
     for (int k = 0; k < 3; k++) {
         f.patch_lo[k] = 2147483647ll;
         f.patch_hi[k] = -2147483648ll;
@@ -328,38 +345,66 @@ __global__ void k_binsort_big(tm_arrays a)
     }
 }
 
-// move the state into Morton order; split positions for the FP32 path and
-// precompute the FP64 density weights sc_t * (size_j / csize_t) of
-// potential.c:62 for every query type t
+// Morton order bookkeeping of every step, and for colonies that rebuild their
+// neighbour lists the move of the state into Morton order (into the scratch
+// buffers; k_copyback brings it back).  Positions are split for the FP32 path
+// and the FP64 density weights sc_t * (size_j / csize_t) of potential.c:62 are
+// precomputed for every query type t.
 __global__ void k_gather(tm_arrays a, const tm_consts *K)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;   // Morton position
+    if (i >= a.nslots_total) return;
+    int c = a.col[i];
+    const tm_desc &d = a.desc[c];
+    if (!d.active || (i - d.off) >= d.n) return;
+    const int r = a.tmp[i];                 // slot of the cell at this position
+    a.codes[i] = a.code[r];
+    const double x = a.x[r], y = a.y[r], z = a.z[r], sz = a.size[r];
+    long long s;                            // slot the split positions go to
+    if (a.frame[c].rebuild) {
+        a.x2[i] = x;
+        a.y2[i] = y;
+        a.z2[i] = z;
+        a.size2[i] = sz;
+        a.young2[i] = a.young[r];
+        a.ctype2[i] = a.ctype[r];
+        a.phase2[i] = a.phase[r];
+        a.perm2[i] = a.perm[r];
+        a.rem2[i] = a.rem[r];
+        a.rank[i] = (int)i;
+        s = i;
+        if (d.precision == 0) {
+            for (int t = 0; t < K->ntypes; t++)
+                a.mass[(long long)t * a.nslots_total + i] = mul64(K->t[t].sc, div64(sz, K->t[t].csize));
+        }
+    } else {
+        a.rank[r] = (int)i;
+        s = r;
+    }
+    float hx, hy, hz, lx, ly, lz;
+    tm_split(x, hx, lx);
+    tm_split(y, hy, ly);
+    tm_split(z, hz, lz);
+    a.hi[s] = make_float4(hx, hy, hz, (float)sz);
+    a.lo[s] = make_float4(lx, ly, lz, 0.0f);
+}
+
+__global__ void k_copyback(tm_arrays a)
 {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.nslots_total) return;
     int c = a.col[i];
     const tm_desc &d = a.desc[c];
-    if (!d.active || (i - d.off) >= d.n) return;
-    int r = a.tmp[i];
-    double x = a.x[r], y = a.y[r], z = a.z[r], sz = a.size[r];
-    a.x2[i] = x;
-    a.y2[i] = y;
-    a.z2[i] = z;
-    a.size2[i] = sz;
-    a.young2[i] = a.young[r];
-    a.ctype2[i] = a.ctype[r];
-    a.phase2[i] = a.phase[r];
-    a.perm2[i] = a.perm[r];
-    a.rem2[i] = a.rem[r];
-    a.codes[i] = a.code[r];
-    float hx, hy, hz, lx, ly, lz;
-    tm_split(x, hx, lx);
-    tm_split(y, hy, ly);
-    tm_split(z, hz, lz);
-    a.hi[i] = make_float4(hx, hy, hz, (float)sz);
-    a.lo[i] = make_float4(lx, ly, lz, 0.0f);
-    if (d.precision == 0) {
-        for (int t = 0; t < K->ntypes; t++)
-            a.mass[(long long)t * a.nslots_total + i] = mul64(K->t[t].sc, div64(sz, K->t[t].csize));
-    }
+    if (!d.active || (i - d.off) >= d.n || !a.frame[c].rebuild) return;
+    a.x[i] = a.x2[i];
+    a.y[i] = a.y2[i];
+    a.z[i] = a.z2[i];
+    a.size[i] = a.size2[i];
+    a.young[i] = a.young2[i];
+    a.ctype[i] = a.ctype2[i];
+    a.phase[i] = a.phase2[i];
+    a.perm[i] = a.perm2[i];
+    a.rem[i] = a.rem2[i];
 }
 
 // ---------------------------------------------------------------------------

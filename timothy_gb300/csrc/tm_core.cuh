@@ -69,6 +69,14 @@ struct tm_frame {
     int ck;                  // left shift restoring 2^32 * code
     uint32_t ceps;           // 2^32 * error bound of the integer path
     unsigned long long codes_slow;   // codes that took the FP64 path (diagnostic)
+    // neighbour lists (Verlet): built when cells may have moved half the skin
+    int rebuild;             // this step searches bins and rebuilds the lists
+    int age;                 // steps since the last rebuild
+    int list_ok;             // 0: the lists are missing or overflowed
+    int force_rebuild;       // set by uploads
+    int ident;               // 1: slots are in this step's Morton order
+    unsigned maxdisp;        // float bits of max |x - x_build| after the last update
+    unsigned long long rebuilds;     // rebuild steps so far (diagnostic)
     unsigned long long step_counter;
     long long patch_lo[3];   // CIC patch corners (patches.c:61-132); INT_MAX/INT_MIN when empty
     long long patch_hi[3];

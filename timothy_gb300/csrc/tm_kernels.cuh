@@ -11,6 +11,7 @@ __global__ void k_scatter(tm_arrays a);
 __global__ void k_binsort_small(tm_arrays a);
 __global__ void k_binsort_big(tm_arrays a);
 __global__ void k_gather(tm_arrays a, const tm_consts *K);
+__global__ void k_copyback(tm_arrays a);
 __global__ void k_octsize(tm_arrays a, unsigned long long *out);
 
 cudaError_t tm_scan_exclusive(const uint32_t *in, uint32_t *out, long long n, uint32_t *tmp, cudaStream_t st);

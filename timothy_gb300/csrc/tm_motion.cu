@@ -54,6 +54,19 @@ __global__ void k_update(tm_arrays a, const tm_consts *K)
         a.rem[i] = 1;
         atomicAdd(&a.frame[c].removecount, 1ull);
     }
+    if (d.verlet) {
+        // displacement since the lists were built, in FP32 from the split
+        // positions (the rebuild test adds a margin for this rounding)
+        float hx, hy, hz, lx, ly, lz;
+        tm_split(x, hx, lx);
+        tm_split(y, hy, ly);
+        tm_split(z, hz, lz);
+        const float4 o = a.x0[i];
+        const float ex = hx - o.x, ey = hy - o.y, ez = hz - o.z;
+        const unsigned bits = __float_as_uint(sqrtf(fmaf(ex, ex, fmaf(ey, ey, ez * ez))));
+        const unsigned m = __reduce_max_sync(__activemask(), bits);
+        if (bits == m) atomicMax(&a.frame[c].maxdisp, m);
+    }
 }
 
 // CIC weights onto field 0; the patch bounding box (patches.c:81-132) is

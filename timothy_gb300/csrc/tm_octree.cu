@@ -106,9 +106,14 @@ __global__ void __launch_bounds__(128) k_octree(tm_arrays a, const tm_consts *K)
     // order, so v can only be non-zero when j* is the first within-h
     // neighbour m and m overlaps p (xc > 0, potential.c:63-65); otherwise v = 0
     // without walking.  The overlap is excluded with a margin in FP32.
+    // slots and Morton positions coincide on rebuild steps; otherwise rank and
+    // tmp translate between them
+    const bool ident = f.ident != 0;
+    const long long ps = ident ? p : (long long)a.rank[p];   // p's Morton position
+    auto slot_of = [&](long long k) -> long long { return ident ? k : (long long)a.tmp[k]; };
     bool need_walk = isolated || a.want_diag;
     if (!need_walk) {
-        const int m = a.nbmin[p];
+        const long long m = slot_of(a.nbmin[p]);
         const float4 hp = a.hi[p], lp = a.lo[p], hm = a.hi[m], lm = a.lo[m];
         const float dx = (hp.x - hm.x) + (lp.x - lm.x), dy = (hp.y - hm.y) + (lp.y - lm.y),
                     dz = (hp.z - hm.z) + (lp.z - lm.z);
@@ -201,12 +206,13 @@ __global__ void __launch_bounds__(128) k_octree(tm_arrays a, const tm_consts *K)
             if (bmax[1] <= ly || bmin[1] >= ly + len) continue;
             if (bmax[2] <= lz || bmin[2] >= lz + len) continue;
             if (e - k == 1) {
-                if ((long long)k == p) continue;
+                if ((long long)k == ps) continue;
                 if (jstar < 0) jstar = k;
                 if (!isolated) {
                     done = true;
                 } else {
-                    const double dx = sub64(xp, a.x[k]), dy = sub64(yp, a.y[k]), dz = sub64(zp, a.z[k]);
+                    const long long sk = slot_of(k);
+                    const double dx = sub64(xp, a.x[sk]), dy = sub64(yp, a.y[sk]), dz = sub64(zp, a.z[sk]);
                     const double dist = __dsqrt_rn(add64(add64(mul64(dx, dx), mul64(dy, dy)), mul64(dz, dz)));
                     mind = (dist < mind ? dist : mind);
                 }
@@ -222,6 +228,7 @@ __global__ void __launch_bounds__(128) k_octree(tm_arrays a, const tm_consts *K)
     }
 
     double vv = 0.0;
+    if (jstar >= 0) jstar = slot_of(jstar);
     if (jstar >= 0) {
         if (d.precision == 0) {
             vv = pair_potential64(xp, yp, zp, a.size[p], a.young[p], a.x[jstar], a.y[jstar], a.z[jstar],

@@ -51,6 +51,107 @@ struct pair_acc<1> {
     __device__ void init() { dens.init(); fx.init(); fy.init(); fz.init(); mins = 3.0e38f; err2 = 0.0f; }
 };
 
+// Exact FP64 pair of potential.c:39-78 / inline.h:40-83 (density and force
+// parts; v comes from the octree walk).  Returns the distance.
+__device__ __forceinline__ double pair64(const tm_type &T, int dim, double xi, double yi, double zi, double xj,
+                                         double yj, double zj, double mj, pair_acc<0> &acc, bool &in)
+{
+    const double dx = sub64(xi, xj), dy = sub64(yi, yj), dz = sub64(zi, zj);
+    const double dist = __dsqrt_rn(add64(add64(mul64(dx, dx), mul64(dy, dy)), mul64(dz, dz)));
+    acc.mind = (dist < acc.mind ? dist : acc.mind);
+    in = dist <= T.h;
+    if (in) {
+        const double u = div64(dist, T.h);
+        const double omu = sub64(1.0, u);
+        double wk, wg;
+        if (u <= 0.5) {
+            const double six_uu = mul64(mul64(6.0, u), u);
+            wk = mul64(T.cW, add64(sub64(1.0, six_uu), mul64(six_uu, u)));
+            wg = add64(mul64(-2.0, u), mul64(mul64(3.0, u), u));
+        } else {
+            wk = mul64(T.cW, mul64(mul64(mul64(2.0, omu), omu), omu));
+            wg = mul64(-omu, omu);
+        }
+        acc.dens = add64(acc.dens, mul64(mj, (double)__double2float_rn(wk)));
+        const double wc = mul64(wg, T.cG);
+        acc.fx = add64(acc.fx, div64(mul64(wc, sub64(xj, xi)), dist));
+        acc.fy = add64(acc.fy, div64(mul64(wc, sub64(yj, yi)), dist));
+        if (dim == 3) acc.fz = add64(acc.fz, div64(mul64(wc, sub64(zj, zi)), dist));
+    }
+    return dist;
+}
+
+// FP32 cutoff decision for squared distance s: FP64 only in the band
+// |r - h| < 1e-5 h, so the neighbour set equals the FP64 one
+__device__ __forceinline__ bool within32(const tm_type &T, float s, double xi, double yi, double zi, double xj,
+                                        double yj, double zj)
+{
+    if (s <= T.thr_lo) return true;
+    if (s > T.thr_hi) return false;
+    const double dx = sub64(xi, xj), dy = sub64(yi, yj), dz = sub64(zi, zj);
+    return __dsqrt_rn(add64(add64(mul64(dx, dx), mul64(dy, dy)), mul64(dz, dz))) <= T.h;
+}
+
+// FP32 + compensated pair (caller decided it is within h)
+__device__ __forceinline__ void pair32(const tm_type &T, int dim, float dx, float dy, float dz, float s,
+                                       float sizej, pair_acc<1> &acc)
+{
+    acc.mins = fminf(acc.mins, s);
+    const float dist = sqrtf(s);
+    const float rs = s > 0.0f ? rsqrtf(s) : 0.0f;
+    const float u = dist * T.inv_hf;
+    // 1 - u as (h - dist) / h: the subtraction is exact near the cutoff
+    const float omu = (T.hf - dist) * T.inv_hf;
+    float wk, wg;
+    if (u <= 0.5f) {
+        wk = T.cWf * fmaf(6.0f * u * u, u - 1.0f, 1.0f);
+        wg = u * fmaf(3.0f, u, -2.0f);
+    } else {
+        wk = T.cWf * (2.0f * omu * omu * omu);
+        wg = -omu * omu;
+    }
+    const float term = T.kmassf * sizej * wk;
+    acc.dens.add(term);
+    // one-sigma rounding estimate of this term: W ~ (1-u)^3 amplifies the FP32
+    // error of (1 - u) near the cutoff
+    const float ek = term * fmaf(1.0e-7f, __frcp_rn(fmaxf(omu, 1.0e-3f)), 1.2e-7f);
+    acc.err2 = fmaf(ek, ek, acc.err2);
+    const float g = wg * T.cGf * rs;
+    acc.fx.add(g * dx);
+    acc.fy.add(g * dy);
+    if (dim == 3) acc.fz.add(g * dz);
+}
+
+// write one cell's results (both pair kernels)
+template <int PREC>
+__device__ __forceinline__ void pair_store(const tm_arrays &a, long long i, pair_acc<PREC> &acc, int cnt_nb,
+                                           int nbmin, unsigned long long hash)
+{
+    if constexpr (PREC == 0) {
+        a.density[i] = acc.dens;
+        a.mindist[i] = acc.mind;
+        a.fx[i] = acc.fx;
+        a.fy[i] = acc.fy;
+        a.fz[i] = acc.fz;
+    } else {
+        const float rho = acc.dens.value();
+        a.density[i] = (double)rho;
+        // cells whose estimated relative density error exceeds 3e-7 (almost only
+        // cells whose neighbours all sit near the cutoff) are redone in FP64
+        if (acc.err2 > 9.0e-14f * rho * rho) {
+            const int q = atomicAdd(a.fix_count, 1);
+            a.fix_list[q] = (int)i;
+        }
+        a.mindist[i] = cnt_nb ? (double)sqrtf(acc.mins) : 1.7976931348623157e308;
+        a.fx[i] = (double)acc.fx.value();
+        a.fy[i] = (double)acc.fy.value();
+        a.fz[i] = (double)acc.fz.value();
+    }
+    a.nbcount[i] = cnt_nb;
+    a.nbmin[i] = cnt_nb ? nbmin : -1;
+    if (a.want_diag) a.nbhash[i] = hash;
+}
+
 template <int PREC>
 __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, const tm_consts *K)
 {
@@ -68,7 +169,9 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
     const tm_desc &d = a.desc[c];
     if (!d.active || d.precision != PREC || d.n <= 1) return;   // potential.c:89
     const tm_frame &f = a.frame[c];
+    if (!f.rebuild) return;                 // the list kernel handles this step
     const int dim = K->dim;
+    const bool build = d.verlet != 0;       // also write the neighbour lists
     float4 *tA = tA_s[wib];
     float4 *tB = tB_s[wib];
     unsigned short(*list)[32] = list_s[wib];
@@ -115,8 +218,12 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
     ex += lo_i.x;
     ey += lo_i.y;
     ez += lo_i.z;
-    // conservative test radius: the test uses s only (|e| < 1e-5 here)
-    const float hr = T.hf * 1.00002f + 1e-4f;
+    // conservative test radius (the test uses s only, |e| < 1e-5 here); with
+    // lists it reaches h + skin
+    const float rlist = T.hf + (build ? d.skin : 0.0f);
+    const float hr = rlist * 1.00002f + 1e-4f;
+    const float rl2 = rlist * rlist * 1.00002f;
+    int vc = 0;   // this lane's list entries
     const int nside = 1 << Lp;
     const float bs = f.binscale * (1.0f / (float)(1 << ls));
     auto binof = [&](float g, float o, float sh, float eps) {
@@ -132,11 +239,16 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
     pair_acc<PREC> acc;
     acc.init();
     int cnt_nb = 0;
-    int nbmin = 0x7fffffff;   // smallest slot (= first in Morton order) within h
+    int nbmin = 0x7fffffff;   // first Morton position within h (slots are positions here)
     unsigned long long hash = 0;
     int nl = 0;
 
-    // exact pair maths over this lane's hit list (tile indices)
+    // exact pair maths over this lane's hit list (tile indices); on rebuild
+    // steps entries within h + skin also go to this lane's quarter of the list
+    auto append = [&](int j) {
+        if (vc < a.qcap) a.vlist[((long long)quarter * a.qcap + vc) * a.lstride + i] = j;
+        vc++;
+    };
     auto drain = [&]() {
         int m = nl;
         for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(FULL, m, o));
@@ -146,69 +258,24 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
             const float4 A = tA[ti];
             const int j = __float_as_int(A.w);
             if constexpr (PREC == 0) {
-                const double xj = a.x[j], yj = a.y[j], zj = a.z[j];
-                const double dx = sub64(xi, xj), dy = sub64(yi, yj), dz = sub64(zi, zj);
-                const double dist = __dsqrt_rn(add64(add64(mul64(dx, dx), mul64(dy, dy)), mul64(dz, dz)));
-                acc.mind = (dist < acc.mind ? dist : acc.mind);
-                if (dist <= T.h) {
-                    const double u = div64(dist, T.h);
-                    const double omu = sub64(1.0, u);
-                    double wk, wg;
-                    if (u <= 0.5) {
-                        const double six_uu = mul64(mul64(6.0, u), u);
-                        wk = mul64(T.cW, add64(sub64(1.0, six_uu), mul64(six_uu, u)));
-                        wg = add64(mul64(-2.0, u), mul64(mul64(3.0, u), u));
-                    } else {
-                        wk = mul64(T.cW, mul64(mul64(mul64(2.0, omu), omu), omu));
-                        wg = mul64(-omu, omu);
-                    }
-                    const double mj = a.mass[(long long)t * a.nslots_total + j];
-                    acc.dens = add64(acc.dens, mul64(mj, (double)__double2float_rn(wk)));
-                    const double wc = mul64(wg, T.cG);
-                    acc.fx = add64(acc.fx, div64(mul64(wc, sub64(xj, xi)), dist));
-                    acc.fy = add64(acc.fy, div64(mul64(wc, sub64(yj, yi)), dist));
-                    if (dim == 3) acc.fz = add64(acc.fz, div64(mul64(wc, sub64(zj, zi)), dist));
+                bool in;
+                const double dist = pair64(T, dim, xi, yi, zi, a.x[j], a.y[j], a.z[j],
+                                           a.mass[(long long)t * a.nslots_total + j], acc, in);
+                if (in) {
                     cnt_nb++;
                     nbmin = min(nbmin, j);
                     if (a.want_diag) hash += tm_mix64((unsigned long long)a.perm[j] + 1ull);
                 }
+                if (build && dist <= (double)rlist * 1.000001) append(j);
             } else {
                 const float4 B = tB[ti];
                 const float dx = (A.x - sx) + (B.x - ex);
                 const float dy = (A.y - sy) + (B.y - ey);
                 const float dz = (A.z - sz) + (B.z - ez);
                 const float s = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                bool in = s <= T.thr_lo;
-                if (!in && s <= T.thr_hi) {
-                    // band |r - h| < 1e-5 h: decide with the FP64 distance
-                    const double ddx = sub64(xi, a.x[j]), ddy = sub64(yi, a.y[j]), ddz = sub64(zi, a.z[j]);
-                    in = __dsqrt_rn(add64(add64(mul64(ddx, ddx), mul64(ddy, ddy)), mul64(ddz, ddz))) <= T.h;
-                }
-                if (in) {
-                    acc.mins = fminf(acc.mins, s);
-                    const float dist = sqrtf(s);
-                    const float rs = s > 0.0f ? rsqrtf(s) : 0.0f;
-                    const float u = dist * T.inv_hf;
-                    // 1 - u as (h - dist) / h: the subtraction is exact near the cutoff
-                    const float omu = (T.hf - dist) * T.inv_hf;
-                    float wk, wg;
-                    if (u <= 0.5f) {
-                        wk = T.cWf * fmaf(6.0f * u * u, u - 1.0f, 1.0f);
-                        wg = u * fmaf(3.0f, u, -2.0f);
-                    } else {
-                        wk = T.cWf * (2.0f * omu * omu * omu);
-                        wg = -omu * omu;
-                    }
-                    const float term = T.kmassf * B.w * wk;
-                    acc.dens.add(term);
-                    // one-sigma rounding estimate of this term: W ~ (1-u)^3 amplifies
-                    // the FP32 error of (1 - u) near the cutoff
-                    const float ek = term * fmaf(1.0e-7f, __frcp_rn(fmaxf(omu, 1.0e-3f)), 1.2e-7f);
-                    acc.err2 = fmaf(ek, ek, acc.err2);
-                    const float g = wg * T.cGf * rs;
-                    acc.fx.add(g * dx);
-                    acc.fy.add(g * dy);
-                    if (dim == 3) acc.fz.add(g * dz);
+                if (build && s <= rl2) append(j);
+                if (s <= T.thr_hi && within32(T, s, xi, yi, zi, a.x[j], a.y[j], a.z[j])) {
+                    pair32(T, dim, dx, dy, dz, s, B.w, acc);
                     cnt_nb++;
                     nbmin = min(nbmin, j);
                     if (a.want_diag) hash += tm_mix64((unsigned long long)a.perm[j] + 1ull);
@@ -352,30 +419,64 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
         nbmin = min(nbmin, __shfl_xor_sync(FULL, nbmin, o));
         hash += __shfl_xor_sync(FULL, hash, o);
     }
-    if (!live || quarter != 0) return;
-    if constexpr (PREC == 0) {
-        a.density[i] = acc.dens;
-        a.mindist[i] = acc.mind;
-        a.fx[i] = acc.fx;
-        a.fy[i] = acc.fy;
-        a.fz[i] = acc.fz;
-    } else {
-        const float rho = acc.dens.value();
-        a.density[i] = (double)rho;
-        // cells whose estimated relative density error exceeds 3e-7 (almost only
-        // cells whose neighbours all sit near the cutoff) are redone in FP64
-        if (acc.err2 > 9.0e-14f * rho * rho) {
-            const int q = atomicAdd(a.fix_count, 1);
-            a.fix_list[q] = (int)i;
-        }
-        a.mindist[i] = cnt_nb ? (double)sqrtf(acc.mins) : 1.7976931348623157e308;
-        a.fx[i] = (double)acc.fx.value();
-        a.fy[i] = (double)acc.fy.value();
-        a.fz[i] = (double)acc.fz.value();
+    if (build && live) {
+        a.vcount[(long long)quarter * a.lstride + i] = min(vc, a.qcap);
+        if (vc > a.qcap) atomicExch(&a.frame[c].list_ok, 0);   // rebuild again next step
+        if (quarter == 0) a.x0[i] = hi_i;
     }
-    a.nbcount[i] = cnt_nb;
-    a.nbmin[i] = cnt_nb ? nbmin : -1;
-    if (a.want_diag) a.nbhash[i] = hash;
+    if (!live || quarter != 0) return;
+    pair_store<PREC>(a, i, acc, cnt_nb, nbmin, hash);
+}
+
+// Pair kernel on the neighbour lists (steps between rebuilds): one thread per
+// cell walks the entries of its four quarters with the same exact maths; the
+// cutoff is decided each step, so the neighbour sets are those of this step.
+template <int PREC>
+__global__ void __launch_bounds__(256) k_plist(tm_arrays a, const tm_consts *K)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (((i >> 5) << 5) >= a.nslots_total) return;
+    const int c = a.col[(i >> 5) << 5];
+    const tm_desc &d = a.desc[c];
+    if (!d.active || d.precision != PREC || d.n <= 1 || !d.verlet) return;
+    const tm_frame &f = a.frame[c];
+    if (f.rebuild) return;
+    if ((i - d.off) >= d.n) return;
+    const int dim = K->dim;
+    const int t = a.ctype[i];
+    const tm_type &T = K->t[t];
+    const double xi = a.x[i], yi = a.y[i], zi = a.z[i];
+    const float4 hi_i = a.hi[i], lo_i = a.lo[i];
+    pair_acc<PREC> acc;
+    acc.init();
+    int cnt_nb = 0, nbmin = 0x7fffffff;
+    unsigned long long hash = 0;
+    for (int q = 0; q < 4; q++) {
+        const int cnt = a.vcount[(long long)q * a.lstride + i];
+        const int *lst = a.vlist + (long long)q * a.qcap * a.lstride + i;
+        for (int k = 0; k < cnt; k++) {
+            const int j = lst[(long long)k * a.lstride];
+            bool in;
+            if constexpr (PREC == 0) {
+                pair64(T, dim, xi, yi, zi, a.x[j], a.y[j], a.z[j], a.mass[(long long)t * a.nslots_total + j], acc,
+                       in);
+            } else {
+                const float4 hj = a.hi[j], lj = a.lo[j];
+                const float dx = (hj.x - hi_i.x) + (lj.x - lo_i.x);
+                const float dy = (hj.y - hi_i.y) + (lj.y - lo_i.y);
+                const float dz = (hj.z - hi_i.z) + (lj.z - lo_i.z);
+                const float s = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                in = s <= T.thr_hi && within32(T, s, xi, yi, zi, a.x[j], a.y[j], a.z[j]);
+                if (in) pair32(T, dim, dx, dy, dz, s, hj.w, acc);
+            }
+            if (in) {
+                cnt_nb++;
+                nbmin = min(nbmin, a.rank[j]);
+                if (a.want_diag) hash += tm_mix64((unsigned long long)a.perm[j] + 1ull);
+            }
+        }
+    }
+    pair_store<PREC>(a, i, acc, cnt_nb, nbmin, hash);
 }
 
 // FP64 density of the cells flagged by the FP32 path: the same neighbour set
@@ -400,13 +501,15 @@ __global__ void __launch_bounds__(128) k_density_fix64(tm_arrays a, const tm_con
             hi[k] = max(0, min(nside - 1, (int)floorf(v1)));
         }
         const uint32_t *bst = a.bin_start + d.binoff;
+        const bool ident = f.ident != 0;
         double dens = 0.0;
         for (int bz = lo[2]; bz <= hi[2]; bz++)
             for (int by = lo[1]; by <= hi[1]; by++)
                 for (int bx = lo[0]; bx <= hi[0]; bx++) {
                     const uint32_t m = tm_morton((uint32_t)bx, (uint32_t)by, (uint32_t)bz);
                     const long long j0 = f.bin_base + bst[m], j1 = f.bin_base + bst[m + 1];
-                    for (long long j = j0; j < j1; j++) {
+                    for (long long jk = j0; jk < j1; jk++) {
+                        const long long j = ident ? jk : (long long)a.tmp[jk];   // slot of position jk
                         if (j == i) continue;
                         const double dx = sub64(xi, a.x[j]), dy = sub64(yi, a.y[j]), dz = sub64(zi, a.z[j]);
                         const double dist = __dsqrt_rn(add64(add64(mul64(dx, dx), mul64(dy, dy)), mul64(dz, dz)));
@@ -435,10 +538,13 @@ cudaError_t tm_launch_pair(const tm_arrays &a, const tm_consts *K, int prec, cud
     int bt = TM_WARPS_PER_BLOCK * 32;
     unsigned grid = (unsigned)((threads + bt - 1) / bt);
     if (grid == 0) return cudaSuccess;
+    const unsigned lgrid = (unsigned)((a.nslots_total + 255) / 256);
     if (prec == 0) {
         k_pair<0><<<grid, bt, 0, st>>>(a, K);
+        k_plist<0><<<lgrid, 256, 0, st>>>(a, K);
     } else {
         k_pair<1><<<grid, bt, 0, st>>>(a, K);
+        k_plist<1><<<lgrid, 256, 0, st>>>(a, K);
         k_density_fix64<<<256, 128, 0, st>>>(a, K);
     }
     return cudaGetLastError();

@@ -122,11 +122,11 @@ struct tm_session {
     std::vector<cudaEvent_t> evpool;
     size_t evused = 0;
     long long prof_steps = 0;
-    // graphs (one per buffer parity)
+    // graph of one step
     bool use_graph = false;
     bool graph_valid[2] = {false, false};
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};
-    int parity = 0;   // 0: A.x is current, 1: A.x2 is current
+    int parity = 0;   // always 0: the state stays in place between steps
     long long launches = 0;
     int kernels_per_step = 0;
     int mass_types = 0;   // types the FP64 density-weight array holds
@@ -141,6 +141,10 @@ __global__ void k_colony_init(tm_arrays a, int c, long long off, int n, int nslo
     long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nslots) return;
     long long i = off + k;
+    if (k == 0) {
+        a.frame[c].force_rebuild = 1;   // the slots no longer match the lists
+        a.frame[c].list_ok = 0;
+    }
     a.col[i] = c;
     if (k < n) {
         a.perm[i] = (int)k;
@@ -169,21 +173,10 @@ __global__ void k_unsort(const T *src, const int *perm, long long off, int n, T 
 
 static unsigned blocks_for(long long n, int bt) { return (unsigned)std::max(1ll, (n + bt - 1) / bt); }
 
-// the arrays as the kernels of one step see them (parity 1 swaps the buffers)
-static tm_arrays view(const tm_session *s, int parity)
+// the arrays as the kernels of one step see them
+static tm_arrays view(const tm_session *s, int /*unused*/ = 0)
 {
     tm_arrays a = s->A;
-    if (parity) {
-        std::swap(a.x, a.x2);
-        std::swap(a.y, a.y2);
-        std::swap(a.z, a.z2);
-        std::swap(a.size, a.size2);
-        std::swap(a.young, a.young2);
-        std::swap(a.ctype, a.ctype2);
-        std::swap(a.phase, a.phase2);
-        std::swap(a.perm, a.perm2);
-        std::swap(a.rem, a.rem2);
-    }
     a.nslots_total = s->slots.hwm * 32;
     a.ncol = (int)s->cols.size();
     return a;
@@ -217,8 +210,9 @@ static void colony_mix(const tm_session *s, bool &any_cic, bool &any64, bool &an
     }
 }
 
-// Build phase for buffer parity p (octbuild): frames, codes, counting sort,
-// gather.  Afterwards the Morton-ordered buffers (parity 1 - p) are current.
+// Build phase (octbuild): frames, lattice codes, counting sort into Morton
+// order.  Colonies that rebuild their neighbour lists this step also move
+// their state into Morton order (gather into scratch, copy back).
 static int enqueue_build(tm_session *s, int p, int &nk)
 {
     cudaStream_t st = s->stream;
@@ -241,8 +235,9 @@ static int enqueue_build(tm_session *s, int p, int &nk)
     k_binsort_small<<<blocks_for(nsl, 128), 128, 0, st>>>(a);
     k_binsort_big<<<64, 256, 0, st>>>(a);
     k_gather<<<blocks_for(nsl, 256), 256, 0, st>>>(a, s->dK);
+    k_copyback<<<blocks_for(nsl, 256), 256, 0, st>>>(a);
     CK(cudaGetLastError());
-    nk += 12;   // step_init, bbox, frame, codes, 3 scan passes, binbase, scatter, 2 bin sorts, gather
+    nk += 13;   // step_init, bbox, frame, codes, 3 scan passes, binbase, scatter, 2 bin sorts, gather, copyback
     return TM_OK;
 }
 
@@ -267,11 +262,11 @@ static int enqueue_compute(tm_session *s, int &nk, bool with_marks)
     tm_arrays b = view(s, s->parity);
     if (any64) {
         CK(tm_launch_pair(b, s->dK, 0, s->stream));
-        nk++;
+        nk += 2;
     }
     if (any32) {
         CK(tm_launch_pair(b, s->dK, 1, s->stream));
-        nk += 2;
+        nk += 3;
     }
     if (with_marks) mark(s);
     CK(tm_launch_octree(b, s->dK, s->stream));
@@ -294,7 +289,6 @@ static int enqueue_step(tm_session *s)
     int nk = 0, rc;
     mark(s);
     if ((rc = enqueue_build(s, s->parity, nk))) return rc;
-    s->parity ^= 1;
     mark(s);
     if ((rc = enqueue_cic(s, nk))) return rc;
     mark(s);
@@ -409,7 +403,7 @@ extern "C" int tm_session_create(tm_session **out, const tm_session_config *cfg,
     AL(a.rem, S)
     AL(a.x2, S) AL(a.y2, S) AL(a.z2, S) AL(a.size2, S) AL(a.young2, S) AL(a.ctype2, S) AL(a.phase2, S)
     AL(a.perm2, S) AL(a.rem2, S)
-    AL(a.col, S) AL(a.code, S) AL(a.codes, S) AL(a.bin, S) AL(a.tmp, S) AL(a.hi, S) AL(a.lo, S)
+    AL(a.col, S) AL(a.code, S) AL(a.codes, S) AL(a.bin, S) AL(a.tmp, S) AL(a.rank, S) AL(a.hi, S) AL(a.lo, S)
     AL(a.mass, S * K.ntypes)
     s->mass_types = K.ntypes;
     AL(a.bin_count, B + 1) AL(a.bin_cursor, B + 1) AL(a.bin_start, B + 1) AL(a.bigbins, 2 * (S / 33) + 4)
@@ -420,6 +414,11 @@ extern "C" int tm_session_create(tm_session **out, const tm_session_config *cfg,
     if (rc == TM_OK) rc = dalloc((double **)&s->d_scratch, S);
     if (cfg->diagnostics) {
         AL(a.nbhash, S) AL(a.vcand, S)
+    }
+    a.lstride = S;
+    a.qcap = cfg->list_capacity > 0 ? (cfg->list_capacity + 3) / 4 : 0;
+    if (a.qcap > 0) {
+        AL(a.vlist, S * 4 * (long long)a.qcap) AL(a.vcount, S * 4) AL(a.x0, S)
     }
 #undef AL
     if (rc == TM_OK) {
@@ -456,7 +455,7 @@ extern "C" int tm_session_destroy(tm_session *s)
     drop_graphs(s);
     tm_arrays &a = s->A;
     void *ptrs[] = {a.x, a.y, a.z, a.size, a.young, a.ctype, a.phase, a.perm, a.rem, a.x2, a.y2, a.z2, a.size2,
-                    a.young2, a.ctype2, a.phase2, a.perm2, a.rem2, a.col, a.code, a.codes, a.bin, a.tmp, a.hi, a.lo,
+                    a.young2, a.ctype2, a.phase2, a.perm2, a.rem2, a.col, a.code, a.codes, a.bin, a.tmp, a.rank, a.hi, a.lo, a.vlist, a.vcount, a.x0,
                     a.mass, a.bin_count, a.bin_cursor, a.bin_start, a.bigbins, a.fix_count, a.fix_list, a.density, a.v, a.mindist, a.fx,
                     a.fy, a.fz, a.nbcount, a.nbmin, a.nbhash, a.vcand, a.grid, a.desc, a.frame, s->scan_tmp, s->d_octsize,
                     s->dK, s->d_scratch};
@@ -608,6 +607,13 @@ extern "C" int tm_colony_add(tm_session *s, const tm_colony_input *in, const tm_
     d.update_mode = opt->update_mode;
     d.active = 1;
     d.dt = opt->dt;
+    d.verlet = (opt->verlet && s->A.qcap > 0) ? 1 : 0;
+    {
+        double hmax = 0.0;
+        for (int t = 0; t < s->K.ntypes; t++) hmax = std::max(hmax, s->K.t[t].h);
+        d.skin = opt->skin > 0.0f ? opt->skin : (float)(0.1 * hmax);
+    }
+    d.rmax = opt->rmax > 0 ? opt->rmax : 16;
     for (int k = 0; k < 3; k++) {
         d.glower[k] = glower[k];
         d.gsize[k] = ch.gsize[k];
@@ -615,6 +621,7 @@ extern "C" int tm_colony_add(tm_session *s, const tm_colony_input *in, const tm_
     d.gres = opt->gfh;
     tm_frame &f = s->h_frame[c];
     memset(&f, 0, sizeof f);
+    f.force_rebuild = 1;
     f.scale = 1.0;
     f.L = 1;
     f.nbins = 8;
@@ -698,8 +705,7 @@ static int run_step_graph(tm_session *s)
     if (!s->graph_valid[p]) {
         cudaGraph_t g;
         CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
-        int rc = enqueue_step(s);   // flips s->parity while recording
-        s->parity = p;
+        int rc = enqueue_step(s);
         cudaError_t e = cudaStreamEndCapture(s->stream, &g);
         if (rc) return rc;
         if (e != cudaSuccess) return tm_fail(TM_ECUDA, "graph capture: %s", cudaGetErrorString(e));
@@ -709,7 +715,6 @@ static int run_step_graph(tm_session *s)
         s->graph_valid[p] = true;
     }
     CK(cudaGraphLaunch(s->gexec[p], s->stream));
-    s->parity ^= 1;
     return TM_OK;
 }
 
@@ -876,6 +881,8 @@ extern "C" int tm_colony_stats(tm_session *s, int id, tm_colony_info *st)
     st->device_errors = f.error;
     st->bin_level = f.L;
     st->n = c.n;
+    st->list_rebuilds = (int64_t)f.rebuilds;
+    st->codes_slow = (int64_t)f.codes_slow;
     return TM_OK;
 }
 
@@ -1091,10 +1098,7 @@ extern "C" int tmi_phase(tm_session *s, int which)
     CK(cudaSetDevice(s->device));
     int nk = 0, rc = TM_OK;
     switch (which) {
-    case 0:
-        rc = enqueue_build(s, s->parity, nk);
-        if (rc == TM_OK) s->parity ^= 1;
-        break;
+    case 0: rc = enqueue_build(s, s->parity, nk); break;
     case 1: rc = enqueue_compute(s, nk, false); break;
     case 2: rc = enqueue_update(s, nk); break;
     case 3: rc = enqueue_cic(s, nk); break;

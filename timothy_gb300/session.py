@@ -32,7 +32,8 @@ class _CellTypes(C.Structure):
 
 class _Config(C.Structure):
     _fields_ = [("dimension", C.c_int), ("device", C.c_int), ("max_slots", C.c_int64), ("max_colonies", C.c_int),
-                ("max_bin_entries", C.c_int64), ("max_grid_entries", C.c_int64), ("diagnostics", C.c_int)]
+                ("max_bin_entries", C.c_int64), ("max_grid_entries", C.c_int64), ("diagnostics", C.c_int),
+                ("list_capacity", C.c_int)]
 
 
 class _Input(C.Structure):
@@ -42,7 +43,8 @@ class _Input(C.Structure):
 
 class _Options(C.Structure):
     _fields_ = [("precision", C.c_int), ("update_mode", C.c_int), ("dt", C.c_double), ("cic", C.c_int),
-                ("gfh", C.c_float), ("lcap", C.c_int), ("reserve", C.c_int64)]
+                ("gfh", C.c_float), ("lcap", C.c_int), ("reserve", C.c_int64), ("verlet", C.c_int),
+                ("skin", C.c_float), ("rmax", C.c_int)]
 
 
 class _Output(C.Structure):
@@ -54,7 +56,7 @@ class _Info(C.Structure):
     _fields_ = [("aff_shift", C.c_double * 3), ("aff_scale", C.c_double), ("octsize", C.c_int64),
                 ("removecount", C.c_int64), ("patch_lower", C.c_int64 * 3), ("patch_upper", C.c_int64 * 3),
                 ("grid_size", C.c_int64 * 3), ("device_errors", C.c_uint32), ("bin_level", C.c_int),
-                ("n", C.c_int64)]
+                ("n", C.c_int64), ("list_rebuilds", C.c_int64), ("codes_slow", C.c_int64)]
 
 
 _lib = None
@@ -128,7 +130,7 @@ class Session:
 
     def __init__(self, types: CellTypes | None = None, *, dim: int = 3, max_slots: int = 1 << 16,
                  max_colonies: int = 1, diagnostics: bool = False, device: int = 0, max_bin_entries: int = 0,
-                 max_grid_entries: int = 0):
+                 max_grid_entries: int = 0, list_capacity: int = 0):
         lib = load_library()
         self.types = types or CellTypes.consistent()
         self._keep = [np.ascontiguousarray(a, dt) for a, dt in
@@ -137,7 +139,7 @@ class Session:
                        (self.types.randommove, np.float32))]
         ct = _CellTypes(self.types.ntypes, *[_p(a) for a in self._keep])
         cfg = _Config(dim, device, int(max_slots), int(max_colonies), int(max_bin_entries), int(max_grid_entries),
-                      1 if diagnostics else 0)
+                      1 if diagnostics else 0, int(list_capacity))
         h = C.c_void_p()
         _check(lib.tm_session_create(C.byref(h), C.byref(cfg), C.byref(ct)))
         self._h = h
@@ -178,10 +180,11 @@ class Session:
         return _Input(col.n, *[_p(a) for a in arrs]), arrs
 
     def add_colony(self, col: Colony, *, precision: str = "fp64", update: str = "reference", dt: float = 1.0,
-                   cic: bool = False, gfh: float = 8.0, lcap: int = 0, reserve: int = 0) -> int:
+                   cic: bool = False, gfh: float = 8.0, lcap: int = 0, reserve: int = 0, verlet: bool = False,
+                   skin: float = 0.0, rmax: int = 0) -> int:
         inp, keep = self._input(col)
         opt = _Options(PREC[precision], UPDATE[update], float(dt), 1 if cic else 0, float(gfh), int(lcap),
-                       int(reserve))
+                       int(reserve), 1 if verlet else 0, float(skin), int(rmax))
         cid = C.c_int(-1)
         _check(load_library().tm_colony_add(self._h, C.byref(inp), C.byref(opt), C.byref(cid)))
         self._n[cid.value] = col.n
@@ -265,14 +268,18 @@ class Session:
         return {"aff": np.array(list(info.aff_shift) + [info.aff_scale]), "octsize": int(info.octsize),
                 "removecount": int(info.removecount), "patch_lower": list(info.patch_lower),
                 "patch_upper": list(info.patch_upper), "device_errors": int(info.device_errors),
-                "bin_level": int(info.bin_level), "n": int(info.n)}
+                "bin_level": int(info.bin_level), "n": int(info.n), "list_rebuilds": int(info.list_rebuilds),
+                "codes_slow": int(info.codes_slow)}
 
 
 def run_colony(col: Colony, nsteps: int, *, precision: str = "fp64", update: str = "reference", dt: float = 1.0,
-               cic: bool = False, gfh: float = 8.0, diagnostics: bool = False, fields=None):
+               cic: bool = False, gfh: float = 8.0, diagnostics: bool = False, fields=None, verlet: bool = False,
+               skin: float = 0.0, rmax: int = 0, list_capacity: int = 256):
     """Upload one colony, advance it nsteps, return (outputs, stats)."""
-    with Session(col.types, dim=col.dim, max_slots=max(col.n, 1) + 64, diagnostics=diagnostics) as s:
-        cid = s.add_colony(col, precision=precision, update=update, dt=dt, cic=cic, gfh=gfh)
+    with Session(col.types, dim=col.dim, max_slots=max(col.n, 1) + 64, diagnostics=diagnostics,
+                 list_capacity=list_capacity if verlet else 0) as s:
+        cid = s.add_colony(col, precision=precision, update=update, dt=dt, cic=cic, gfh=gfh, verlet=verlet,
+                           skin=skin, rmax=rmax)
         s.step(nsteps)
         s.sync()
         f = fields
