@@ -228,9 +228,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
-    ap.add_argument("--list-capacity", type=int, default=256,
+    ap.add_argument("--list-capacity", type=int, default=384,
                     help="neighbour-list entries per cell (0: search the bins every step)")
     ap.add_argument("--rmax", type=int, default=16, help="rebuild the neighbour lists at least every rmax steps")
+    ap.add_argument("--skin", type=float, default=0.1, help="neighbour-list skin as a fraction of h")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     wl = dict(WORKLOADS[args.workload])
@@ -250,7 +251,7 @@ def main():
     def new_session(p):
         s = S.Session(col.types, dim=3, max_slots=n + 64, device=local, list_capacity=args.list_capacity)
         cid = s.add_colony(col, precision=p, update="dt", dt=wl["dt"], cic=wl["cic"],
-                           verlet=args.list_capacity > 0, rmax=args.rmax)
+                           verlet=args.list_capacity > 0, skin=args.skin * float(max(col.types.h)), rmax=args.rmax)
         return s, cid
 
     s, cid = new_session(prec)
@@ -361,7 +362,7 @@ def main():
             "config": {"workload": args.workload, "kind": kind, "cells": n, "seed": seed, "radius": radius,
                        "h": 2.5, "dt": wl["dt"], "cic": wl["cic"], "precision": prec,
                        "mean_neighbours": mean_nb, "max_neighbours": max_nb,
-                       "neighbour_lists": {"capacity": args.list_capacity, "skin": 0.25, "rmax": args.rmax,
+                       "neighbour_lists": {"capacity": args.list_capacity, "skin_over_h": args.skin, "rmax": args.rmax,
                                            "rebuilds_in_timed_steps": rebuilds},
                        "l2": "inputs larger than L2 (state %.1f GB)" % (n * 250 / 1e9),
                        "parallelism": f"replicas x{world}"},
