@@ -220,7 +220,7 @@ def run_reference_arm(args, workload):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="precision16m", choices=sorted(WORKLOADS))
@@ -230,7 +230,7 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--list-capacity", type=int, default=384,
                     help="neighbour-list entries per cell (0: search the bins every step)")
-    ap.add_argument("--rmax", type=int, default=16, help="rebuild the neighbour lists at least every rmax steps")
+    ap.add_argument("--rmax", type=int, default=64, help="rebuild the neighbour lists at least every rmax steps")
     ap.add_argument("--skin", type=float, default=0.1, help="neighbour-list skin as a fraction of h")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)

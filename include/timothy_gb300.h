@@ -84,7 +84,7 @@ typedef struct {
     int64_t reserve;          /* slots to reserve (>= n) so later uploads can grow */
     int verlet;               /* 1: keep neighbour lists within h + skin between rebuilds */
     float skin;               /* list margin (0: 0.1 h) */
-    int rmax;                 /* rebuild the lists at least every rmax steps (0: 16) */
+    int rmax;                 /* rebuild the lists at least every rmax steps (0: 64) */
 } tm_colony_options;
 
 /* Outputs in caller order (host memory); any pointer may be NULL. */
@@ -124,7 +124,12 @@ void *tm_session_stream(tm_session *s);
 /* Add a colony; its id is written to *id.  Uploads the cells. */
 int tm_colony_add(tm_session *s, const tm_colony_input *in, const tm_colony_options *opt, int *id);
 int tm_colony_remove(tm_session *s, int id);
-/* Replace the cells of an existing colony (same n or fewer). */
+/* Replace the cells of an existing colony (at most the slots it holds).  With
+ * the same n the cells are taken as the same cells in the same order as the
+ * colony's input: they keep their slots, and neighbour lists stay valid unless
+ * a cell moved too far, changed size or changed type.  Cell types are checked
+ * on the device; one outside the table returns TM_EDEVICE and leaves the
+ * colony empty. */
 int tm_colony_upload(tm_session *s, int id, const tm_colony_input *in);
 int tm_colony_set_active(tm_session *s, int id, int active);
 int tm_colony_download(tm_session *s, int id, const tm_colony_output *out);

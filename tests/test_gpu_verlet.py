@@ -91,3 +91,85 @@ def test_verlet_fp32_against_fp64():
     f64 = np.stack([o64["fx"], o64["fy"], o64["fz"]])
     f32 = np.stack([o32["fx"], o32["fy"], o32["fz"]])
     assert np.max(np.abs(f32 - f64)) <= 1e-6 * np.max(np.abs(f64))
+
+
+def _upload_case(oracle_lib, change):
+    from timothy_gb300 import session as S
+
+    col = C.make_colony("clustered", 20000, 35, C.initial_radius("clustered", 20000))
+    with S.Session(col.types, max_slots=col.n + 64, list_capacity=384) as s:
+        cid = s.add_colony(col, precision="fp64", update="dt", dt=0.01, verlet=True)
+        s.step(3)
+        s.sync()
+        pos = s.download(cid, ["x", "y", "z"])
+        moved = C.Colony(pos["x"].copy(), pos["y"].copy(), pos["z"].copy(), col.size.copy(), col.young, col.ctype,
+                         col.phase, col.types)
+        change(moved)
+        rb = s.stats(cid)["list_rebuilds"]
+        s.upload(cid, moved)
+        s.step(2)
+        s.sync()
+        out = s.download(cid, ["x", "y", "z", "density", "v", "mindist", "fx", "fy", "fz"])
+        rebuilt = s.stats(cid)["list_rebuilds"] - rb
+    ref = oracle_lib.run(moved, 2, which="oracle", update_mode=1, dt=0.01)
+    check64(out, ref, "upload")
+    return rebuilt
+
+
+def test_upload_same_cells_keeps_lists(oracle_lib):
+    assert _upload_case(oracle_lib, lambda c: None) == 0
+
+
+def test_upload_far_move_rebuilds(oracle_lib):
+    def move(c):
+        c.x[123] += 0.3      # beyond half the skin (0.25)
+    assert _upload_case(oracle_lib, move) == 1
+
+
+def test_upload_size_change_rebuilds(oracle_lib):
+    def grow(c):
+        c.size[7] *= 1.05
+    assert _upload_case(oracle_lib, grow) == 1
+
+
+def test_upload_bad_cell_type_empties_colony():
+    from timothy_gb300 import session as S
+
+    col = C.make_colony("uniform", 2000, 36, C.initial_radius("uniform", 2000))
+    with S.Session(col.types, max_slots=col.n + 64, list_capacity=384) as s:
+        cid = s.add_colony(col, precision="fp64", update="dt", dt=0.01, verlet=True)
+        s.step(1)
+        bad = col.copy()
+        bad.ctype[5] = 3
+        with pytest.raises(S.TimothyError):
+            s.upload(cid, bad)
+        assert s.stats(cid)["n"] == 0
+        s.step(1)
+        s.sync()
+        s.upload(cid, col)
+        s.step(1)
+        s.sync()
+        assert s.stats(cid)["n"] == col.n
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+def test_list_overflow_falls_back_to_search(oracle_lib, precision):
+    """Lists too short for the densest cells: every step searches instead, with the same results."""
+    from timothy_gb300 import session as S
+
+    col = C.make_colony("clustered", 20000, 37, C.initial_radius("clustered", 20000))
+    with S.Session(col.types, max_slots=col.n + 64, list_capacity=32) as s:
+        cid = s.add_colony(col, precision=precision, update="dt", dt=0.01, verlet=True)
+        s.step(4)
+        s.sync()
+        out = s.download(cid, ["x", "y", "z", "density", "v", "mindist", "fx", "fy", "fz"])
+        st = s.stats(cid)
+    assert st["list_rebuilds"] == 4
+    ref = oracle_lib.run(col, 4, which="oracle", update_mode=1, dt=0.01)
+    if precision == "fp64":
+        check64(out, ref, "overflow")
+    else:
+        pos = ref.density > 0
+        assert rel(out["density"][pos], ref.density[pos]) <= 1e-6
+        f = np.stack([ref.fx, ref.fy, ref.fz])
+        assert np.max(np.abs(np.stack([out["fx"], out["fy"], out["fz"]]) - f)) <= 1e-6 * np.max(np.abs(f))

@@ -57,6 +57,9 @@ struct tm_arrays {
     int *bigbins;
     int *fix_count;      // cells whose FP32 density is redone in FP64
     int *fix_list;
+    // per step: work[0] colonies that search (or build lists), work[1]
+    // colonies whose lists overflowed; lets the pair grid leave at once
+    int *work;
     // outputs (Morton order)
     double *density, *v, *mindist, *fx, *fy, *fz;
     int *nbcount;

@@ -43,6 +43,7 @@ __global__ void k_step_init(tm_arrays a)
     } else {
         f.age++;
     }
+    if (rb && d.active && d.n > 1) atomicAdd(&a.work[0], 1);
     f.force_rebuild = 0;
     f.maxdisp = 0u;
     for (int k = 0; k < 3; k++) {
@@ -386,7 +387,8 @@ __global__ void k_gather(tm_arrays a, const tm_consts *K)
     tm_split(y, hy, ly);
     tm_split(z, hz, lz);
     a.hi[s] = make_float4(hx, hy, hz, (float)sz);
-    a.lo[s] = make_float4(lx, ly, lz, 0.0f);
+    // .w carries the Morton position of this step (what rank[s] holds)
+    a.lo[s] = make_float4(lx, ly, lz, __int_as_float((int)i));
 }
 
 __global__ void k_copyback(tm_arrays a)

@@ -26,6 +26,8 @@
 #include "tm_arrays.cuh"
 #include "tm_kernels.cuh"
 
+#include <algorithm>
+
 #define FULL 0xffffffffu
 #define PAIR_TILE 256
 #define PAIR_LCAP 64
@@ -92,6 +94,37 @@ __device__ __forceinline__ bool within32(const tm_type &T, float s, double xi, d
     return __dsqrt_rn(add64(add64(mul64(dx, dx), mul64(dy, dy)), mul64(dz, dz))) <= T.h;
 }
 
+// FP64 density term of cell j at distance dist <= h from a cell of type T
+// (potential.c:60-62 with sphkernel inline.h:40-51, W rounded to float)
+__device__ __forceinline__ double dens_term64(const tm_type &T, double dist, double sizej)
+{
+    const double u = div64(dist, T.h);
+    double wk;
+    if (u <= 0.5) {
+        const double six_uu = mul64(mul64(6.0, u), u);
+        wk = mul64(T.cW, add64(sub64(1.0, six_uu), mul64(six_uu, u)));
+    } else {
+        const double omu = sub64(1.0, u);
+        wk = mul64(T.cW, mul64(mul64(mul64(2.0, omu), omu), omu));
+    }
+    const double mj = mul64(T.sc, div64(sizej, T.csize));
+    return mul64(mj, (double)__double2float_rn(wk));
+}
+
+__device__ __forceinline__ double dist64(const tm_arrays &a, long long i, long long j)
+{
+    const double dx = sub64(a.x[i], a.x[j]), dy = sub64(a.y[i], a.y[j]), dz = sub64(a.z[i], a.z[j]);
+    return __dsqrt_rn(add64(add64(mul64(dx, dx), mul64(dy, dy)), mul64(dz, dz)));
+}
+
+// within32 with both cells' FP64 positions read only inside the band
+__device__ __forceinline__ bool within32_at(const tm_type &T, float s, const tm_arrays &a, long long i, long long j)
+{
+    if (s <= T.thr_lo) return true;
+    if (s > T.thr_hi) return false;
+    return dist64(a, i, j) <= T.h;
+}
+
 // FP32 + compensated pair (caller decided it is within h)
 __device__ __forceinline__ void pair32(const tm_type &T, int dim, float dx, float dy, float dz, float s,
                                        float sizej, pair_acc<1> &acc)
@@ -114,7 +147,7 @@ __device__ __forceinline__ void pair32(const tm_type &T, int dim, float dx, floa
     acc.dens.add(term);
     // one-sigma rounding estimate of this term: W ~ (1-u)^3 amplifies the FP32
     // error of (1 - u) near the cutoff
-    const float ek = term * fmaf(1.0e-7f, __frcp_rn(fmaxf(omu, 1.0e-3f)), 1.2e-7f);
+    const float ek = term * fmaf(1.0e-7f, __fdividef(1.0f, fmaxf(omu, 1.0e-3f)), 1.2e-7f);
     acc.err2 = fmaf(ek, ek, acc.err2);
     const float g = wg * T.cGf * rs;
     acc.fx.add(g * dx);
@@ -123,9 +156,19 @@ __device__ __forceinline__ void pair32(const tm_type &T, int dim, float dx, floa
 }
 
 // write one cell's results (both pair kernels)
+// cells whose estimated relative FP32 density error exceeds 3e-7 (almost
+// only cells whose neighbours all sit near the cutoff) are redone in FP64
+__device__ __forceinline__ bool needs_fix64(const pair_acc<1> &acc)
+{
+    const float rho = acc.dens.value();
+    return acc.err2 > 9.0e-14f * rho * rho;
+}
+
+// queue: flagged cells go to the FP64 fix-up kernel (otherwise the caller
+// redoes them)
 template <int PREC>
 __device__ __forceinline__ void pair_store(const tm_arrays &a, long long i, pair_acc<PREC> &acc, int cnt_nb,
-                                           int nbmin, unsigned long long hash)
+                                           int nbmin, unsigned long long hash, bool queue = true)
 {
     if constexpr (PREC == 0) {
         a.density[i] = acc.dens;
@@ -136,9 +179,7 @@ __device__ __forceinline__ void pair_store(const tm_arrays &a, long long i, pair
     } else {
         const float rho = acc.dens.value();
         a.density[i] = (double)rho;
-        // cells whose estimated relative density error exceeds 3e-7 (almost only
-        // cells whose neighbours all sit near the cutoff) are redone in FP64
-        if (acc.err2 > 9.0e-14f * rho * rho) {
+        if (queue && needs_fix64(acc)) {
             const int q = atomicAdd(a.fix_count, 1);
             a.fix_list[q] = (int)i;
         }
@@ -152,29 +193,24 @@ __device__ __forceinline__ void pair_store(const tm_arrays &a, long long i, pair
     if (a.want_diag) a.nbhash[i] = hash;
 }
 
+// one warp, one group of PAIR_CPW Morton-consecutive slots starting at base
 template <int PREC>
-__global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, const tm_consts *K)
+__device__ __forceinline__ void pair_group(const tm_arrays &a, const tm_consts *K, int fallback, long long base,
+                                           int lane, float4 *tA, float4 *tB, unsigned short (*list)[32])
 {
-    // per warp: tile of staged candidates (A: hi part of the origin-relative
-    // position + slot, B: lo part + radius) and one hit list per lane holding
-    // tile indices
-    __shared__ float4 tA_s[TM_WARPS_PER_BLOCK][PAIR_TILE];
-    __shared__ float4 tB_s[TM_WARPS_PER_BLOCK][PAIR_TILE];
-    __shared__ unsigned short list_s[TM_WARPS_PER_BLOCK][PAIR_LCAP][32];
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const long long base = w * PAIR_CPW;   // colonies are 32-aligned, so a warp stays in one
     if (base >= a.nslots_total) return;
-    const int c = a.col[base];
+    const int c = a.col[base];             // colonies are 32-aligned, so a group stays in one
     const tm_desc &d = a.desc[c];
     if (!d.active || d.precision != PREC || d.n <= 1) return;   // potential.c:89
     const tm_frame &f = a.frame[c];
     if (!f.rebuild) return;                 // the list kernel handles this step
+    // first pass: colonies with lists build them (the list kernel then does
+    // the pair maths), the others search and evaluate here; second pass
+    // (fallback): colonies whose lists overflowed search and evaluate
+    if (fallback && (!d.verlet || f.list_ok)) return;
+    if ((base - d.off) >= d.n) return;      // group beyond the colony's cells
+    const bool build = !fallback && d.verlet;
     const int dim = K->dim;
-    const bool build = d.verlet != 0;       // also write the neighbour lists
-    float4 *tA = tA_s[wib];
-    float4 *tB = tB_s[wib];
-    unsigned short(*list)[32] = list_s[wib];
 
     const int quarter = lane % PAIR_LPC;   // this lane's share of the cell's candidates
     const long long i = base + lane / PAIR_LPC;
@@ -266,14 +302,12 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
                     nbmin = min(nbmin, j);
                     if (a.want_diag) hash += tm_mix64((unsigned long long)a.perm[j] + 1ull);
                 }
-                if (build && dist <= (double)rlist * 1.000001) append(j);
             } else {
                 const float4 B = tB[ti];
                 const float dx = (A.x - sx) + (B.x - ex);
                 const float dy = (A.y - sy) + (B.y - ey);
                 const float dz = (A.z - sz) + (B.z - ez);
                 const float s = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                if (build && s <= rl2) append(j);
                 if (s <= T.thr_hi && within32(T, s, xi, yi, zi, a.x[j], a.y[j], a.z[j])) {
                     pair32(T, dim, dx, dy, dz, s, B.w, acc);
                     cnt_nb++;
@@ -287,6 +321,20 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
 
     // test the staged tile [0, fill) and drain; the tile is refilled afterwards
     auto test_tile = [&](int fill, float thr) {
+        if (build) {
+            // list build only: every entry within the conservative radius goes
+            // to this lane's quarter; the list kernel does the pair maths
+#pragma unroll 4
+            for (int tt = quarter; tt < fill; tt += PAIR_LPC) {
+                const float4 cc = tA[tt];
+                const float dx = cc.x - sx, dy = cc.y - sy, dz = cc.z - sz;
+                const float s = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                const int j = __float_as_int(cc.w);
+                if (s <= thr && (long long)j != i) append(j);
+            }
+            __syncwarp();
+            return;
+        }
         for (int tb = 0; tb < fill; tb += 32 * PAIR_LPC) {
             const int te = min(fill, tb + 32 * PAIR_LPC);
 #pragma unroll 8
@@ -419,20 +467,76 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
         nbmin = min(nbmin, __shfl_xor_sync(FULL, nbmin, o));
         hash += __shfl_xor_sync(FULL, hash, o);
     }
-    if (build && live) {
-        a.vcount[(long long)quarter * a.lstride + i] = min(vc, a.qcap);
-        if (vc > a.qcap) atomicExch(&a.frame[c].list_ok, 0);   // rebuild again next step
-        if (quarter == 0) a.x0[i] = hi_i;
+    if (build) {
+        if (live) {
+            a.vcount[(long long)quarter * a.lstride + i] = min(vc, a.qcap);
+            if (quarter == 0) a.x0[i] = hi_i;
+        }
+        // an overflowing list cannot serve this step: flag the colony, whose
+        // results the list kernel then leaves to a search pass
+        if (__any_sync(FULL, live && vc > a.qcap) && lane == 0)
+            if (atomicExch(&a.frame[c].list_ok, 0) == 1) atomicAdd(&a.work[1], 1);
+        return;
     }
     if (!live || quarter != 0) return;
     pair_store<PREC>(a, i, acc, cnt_nb, nbmin, hash);
 }
 
-// Pair kernel on the neighbour lists (steps between rebuilds): one thread per
-// cell walks the entries of its four quarters with the same exact maths; the
-// cutoff is decided each step, so the neighbour sets are those of this step.
+// Grid-stride over the groups: the grid is sized to the resident blocks, and
+// on a step where no colony searches (all evaluate their lists) or no list
+// overflowed (fallback pass) every block leaves after one load.
 template <int PREC>
-__global__ void __launch_bounds__(256) k_plist(tm_arrays a, const tm_consts *K)
+__global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, const tm_consts *K, int fallback)
+{
+    // per warp: tile of staged candidates (A: hi part of the origin-relative
+    // position + slot, B: lo part + radius) and one hit list per lane holding
+    // tile indices
+    __shared__ float4 tA_s[TM_WARPS_PER_BLOCK][PAIR_TILE];
+    __shared__ float4 tB_s[TM_WARPS_PER_BLOCK][PAIR_TILE];
+    __shared__ unsigned short list_s[TM_WARPS_PER_BLOCK][PAIR_LCAP][32];
+    if (a.work[fallback ? 1 : 0] == 0) return;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const long long ngroups = (a.nslots_total + PAIR_CPW - 1) / PAIR_CPW;
+    const long long stride = (long long)gridDim.x * TM_WARPS_PER_BLOCK;
+    for (long long w = (long long)blockIdx.x * TM_WARPS_PER_BLOCK + wib; w < ngroups; w += stride) {
+        pair_group<PREC>(a, K, fallback, w * PAIR_CPW, lane, tA_s[wib], tB_s[wib], list_s[wib]);
+        __syncwarp();
+    }
+}
+
+// Pair kernel on the neighbour lists (every step of a colony with lists): one
+// thread per cell walks the entries of its four quarters with the same exact
+// maths; the cutoff is decided each step, so the neighbour sets are those of
+// this step.
+// Entries are taken two at a time with both gathers issued before either is
+// used (the walk is bound by the latency of the dependent index -> position
+// loads, not by arithmetic).
+template <int PREC>
+__device__ __forceinline__ void plist_one(const tm_arrays &a, const tm_type &T, int dim, int t, long long i,
+                                          float4 hi_i, float4 lo_i, int j, float4 hj, float4 lj, pair_acc<PREC> &acc,
+                                          int &cnt_nb, int &nbmin, unsigned long long &hash)
+{
+    bool in;
+    if constexpr (PREC == 0) {
+        pair64(T, dim, a.x[i], a.y[i], a.z[i], a.x[j], a.y[j], a.z[j], a.mass[(long long)t * a.nslots_total + j],
+               acc, in);
+    } else {
+        const float dx = (hj.x - hi_i.x) + (lj.x - lo_i.x);
+        const float dy = (hj.y - hi_i.y) + (lj.y - lo_i.y);
+        const float dz = (hj.z - hi_i.z) + (lj.z - lo_i.z);
+        const float s = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        in = within32_at(T, s, a, i, j);
+        if (in) pair32(T, dim, dx, dy, dz, s, hj.w, acc);
+    }
+    if (in) {
+        cnt_nb++;
+        nbmin = min(nbmin, PREC == 0 ? a.rank[j] : __float_as_int(lj.w));
+        if (a.want_diag) hash += tm_mix64((unsigned long long)a.perm[j] + 1ull);
+    }
+}
+
+template <int PREC>
+__global__ void __launch_bounds__(256, 4) k_plist(tm_arrays a, const tm_consts *K)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (((i >> 5) << 5) >= a.nslots_total) return;
@@ -440,43 +544,54 @@ __global__ void __launch_bounds__(256) k_plist(tm_arrays a, const tm_consts *K)
     const tm_desc &d = a.desc[c];
     if (!d.active || d.precision != PREC || d.n <= 1 || !d.verlet) return;
     const tm_frame &f = a.frame[c];
-    if (f.rebuild) return;
+    if (!f.list_ok) return;                 // overflowed: the search pass evaluates
     if ((i - d.off) >= d.n) return;
     const int dim = K->dim;
     const int t = a.ctype[i];
     const tm_type &T = K->t[t];
-    const double xi = a.x[i], yi = a.y[i], zi = a.z[i];
     const float4 hi_i = a.hi[i], lo_i = a.lo[i];
+    const float4 *__restrict__ hi = a.hi;
+    const float4 *__restrict__ lo = a.lo;
     pair_acc<PREC> acc;
     acc.init();
     int cnt_nb = 0, nbmin = 0x7fffffff;
     unsigned long long hash = 0;
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int q = 0; q < 4; q++) {
-        const int cnt = a.vcount[(long long)q * a.lstride + i];
-        const int *lst = a.vlist + (long long)q * a.qcap * a.lstride + i;
-        for (int k = 0; k < cnt; k++) {
-            const int j = lst[(long long)k * a.lstride];
-            bool in;
-            if constexpr (PREC == 0) {
-                pair64(T, dim, xi, yi, zi, a.x[j], a.y[j], a.z[j], a.mass[(long long)t * a.nslots_total + j], acc,
-                       in);
-            } else {
-                const float4 hj = a.hi[j], lj = a.lo[j];
-                const float dx = (hj.x - hi_i.x) + (lj.x - lo_i.x);
-                const float dy = (hj.y - hi_i.y) + (lj.y - lo_i.y);
-                const float dz = (hj.z - hi_i.z) + (lj.z - lo_i.z);
-                const float s = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                in = s <= T.thr_hi && within32(T, s, xi, yi, zi, a.x[j], a.y[j], a.z[j]);
-                if (in) pair32(T, dim, dx, dy, dz, s, hj.w, acc);
-            }
-            if (in) {
-                cnt_nb++;
-                nbmin = min(nbmin, a.rank[j]);
-                if (a.want_diag) hash += tm_mix64((unsigned long long)a.perm[j] + 1ull);
-            }
+        const int cnt = __ldg(a.vcount + (long long)q * a.lstride + i);
+        const int *__restrict__ lst = a.vlist + (long long)q * a.qcap * a.lstride + i;
+        int k = 0;
+        for (; k + 1 < cnt; k += 2) {
+            const int j0 = __ldg(lst + (long long)k * a.lstride);
+            const int j1 = __ldg(lst + (long long)(k + 1) * a.lstride);
+            const float4 h0 = PREC ? __ldg(hi + j0) : z4, l0 = PREC ? __ldg(lo + j0) : z4;
+            const float4 h1 = PREC ? __ldg(hi + j1) : z4, l1 = PREC ? __ldg(lo + j1) : z4;
+            plist_one<PREC>(a, T, dim, t, i, hi_i, lo_i, j0, h0, l0, acc, cnt_nb, nbmin, hash);
+            plist_one<PREC>(a, T, dim, t, i, hi_i, lo_i, j1, h1, l1, acc, cnt_nb, nbmin, hash);
+        }
+        if (k < cnt) {
+            const int j0 = __ldg(lst + (long long)k * a.lstride);
+            const float4 h0 = PREC ? __ldg(hi + j0) : z4, l0 = PREC ? __ldg(lo + j0) : z4;
+            plist_one<PREC>(a, T, dim, t, i, hi_i, lo_i, j0, h0, l0, acc, cnt_nb, nbmin, hash);
         }
     }
-    pair_store<PREC>(a, i, acc, cnt_nb, nbmin, hash);
+    pair_store<PREC>(a, i, acc, cnt_nb, nbmin, hash, false);
+    if constexpr (PREC == 1) {
+        if (needs_fix64(acc)) {
+            // FP64 density over the same list, the cutoff decided in FP64
+            double dens = 0.0;
+            for (int q = 0; q < 4; q++) {
+                const int cnt = a.vcount[(long long)q * a.lstride + i];
+                const int *lst = a.vlist + (long long)q * a.qcap * a.lstride + i;
+                for (int k = 0; k < cnt; k++) {
+                    const int j = lst[(long long)k * a.lstride];
+                    const double dist = dist64(a, i, j);
+                    if (dist <= T.h) dens = add64(dens, dens_term64(T, dist, a.size[j]));
+                }
+            }
+            a.density[i] = dens;
+        }
+    }
 }
 
 // FP64 density of the cells flagged by the FP32 path: the same neighbour set
@@ -511,40 +626,53 @@ __global__ void __launch_bounds__(128) k_density_fix64(tm_arrays a, const tm_con
                     for (long long jk = j0; jk < j1; jk++) {
                         const long long j = ident ? jk : (long long)a.tmp[jk];   // slot of position jk
                         if (j == i) continue;
-                        const double dx = sub64(xi, a.x[j]), dy = sub64(yi, a.y[j]), dz = sub64(zi, a.z[j]);
-                        const double dist = __dsqrt_rn(add64(add64(mul64(dx, dx), mul64(dy, dy)), mul64(dz, dz)));
+                        const double dist = dist64(a, i, j);
                         if (!(dist <= T.h)) continue;
-                        const double u = div64(dist, T.h);
-                        double wk;
-                        if (u <= 0.5) {
-                            const double six_uu = mul64(mul64(6.0, u), u);
-                            wk = mul64(T.cW, add64(sub64(1.0, six_uu), mul64(six_uu, u)));
-                        } else {
-                            const double omu = sub64(1.0, u);
-                            wk = mul64(T.cW, mul64(mul64(mul64(2.0, omu), omu), omu));
-                        }
-                        const double mj = mul64(T.sc, div64(a.size[j], T.csize));
-                        dens = add64(dens, mul64(mj, (double)__double2float_rn(wk)));
+                        dens = add64(dens, dens_term64(T, dist, a.size[j]));
                     }
                 }
         a.density[i] = dens;
     }
 }
 
+// resident blocks of the pair kernel on the current device (all SMs)
+static unsigned pair_grid_cap(int prec)
+{
+    static int cached[2][64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1024;
+    if (!cached[prec][dev]) {
+        int sms = 0, per = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (prec == 0)
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pair<0>, TM_WARPS_PER_BLOCK * 32, 0);
+        else
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pair<1>, TM_WARPS_PER_BLOCK * 32, 0);
+        cached[prec][dev] = std::max(1, sms) * std::max(1, per);
+    }
+    return (unsigned)cached[prec][dev];
+}
+
 cudaError_t tm_launch_pair(const tm_arrays &a, const tm_consts *K, int prec, cudaStream_t st)
 {
-    long long warps = a.nslots_total / PAIR_CPW;
-    long long threads = warps * 32;
-    int bt = TM_WARPS_PER_BLOCK * 32;
-    unsigned grid = (unsigned)((threads + bt - 1) / bt);
+    const long long groups = (a.nslots_total + PAIR_CPW - 1) / PAIR_CPW;
+    const int bt = TM_WARPS_PER_BLOCK * 32;
+    const long long need = (groups + TM_WARPS_PER_BLOCK - 1) / TM_WARPS_PER_BLOCK;
+    const unsigned grid = (unsigned)std::min<long long>(need, pair_grid_cap(prec != 0));
     if (grid == 0) return cudaSuccess;
     const unsigned lgrid = (unsigned)((a.nslots_total + 255) / 256);
     if (prec == 0) {
-        k_pair<0><<<grid, bt, 0, st>>>(a, K);
-        k_plist<0><<<lgrid, 256, 0, st>>>(a, K);
+        k_pair<0><<<grid, bt, 0, st>>>(a, K, 0);
+        if (a.qcap > 0) {
+            k_plist<0><<<lgrid, 256, 0, st>>>(a, K);
+            k_pair<0><<<grid, bt, 0, st>>>(a, K, 1);
+        }
     } else {
-        k_pair<1><<<grid, bt, 0, st>>>(a, K);
-        k_plist<1><<<lgrid, 256, 0, st>>>(a, K);
+        k_pair<1><<<grid, bt, 0, st>>>(a, K, 0);
+        if (a.qcap > 0) {
+            k_plist<1><<<lgrid, 256, 0, st>>>(a, K);
+            k_pair<1><<<grid, bt, 0, st>>>(a, K, 1);
+        }
         k_density_fix64<<<256, 128, 0, st>>>(a, K);
     }
     return cudaGetLastError();

@@ -116,6 +116,7 @@ struct tm_session {
     tm_frame *h_frame = nullptr;
     uint32_t *scan_tmp = nullptr;
     unsigned long long *d_octsize = nullptr;
+    int *d_flag = nullptr;   // set by the upload kernels on a cell type outside the table
     void *d_scratch = nullptr;
     // profiling
     bool prof = false;
@@ -161,6 +162,59 @@ __global__ void k_colony_init(tm_arrays a, int c, long long off, int n, int nslo
     a.nbmin[i] = -1;
     if (a.nbhash) a.nbhash[i] = 0;
     if (a.vcand) a.vcand[i] = -1;
+}
+
+// Upload into a colony that keeps its cell count.  The new values arrive in
+// input order in the rebuild scratch and go through perm to the slots the
+// cells occupy now, so the Morton order and the neighbour lists stay valid:
+// the step's rebuild test sees the displacement from the list positions, and
+// a cell that changed size or type (list radius, FP64 density weight) forces a
+// rebuild.  Cell types outside the table are flagged and replaced by 0.
+__global__ void k_upload_keep(tm_arrays a, const tm_consts *K, int c, long long off, int n, int has_phase,
+                              int *bad)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const long long s = off + k;
+    const long long src = off + a.perm[s];
+    const double x = a.x2[src], y = a.y2[src], z = a.z2[src], sz = a.size2[src];
+    int ct = a.ctype2[src];
+    if (ct < 0 || ct >= K->ntypes) {
+        atomicExch(bad, 1);
+        ct = 0;
+    }
+    if (sz != a.size[s] || ct != a.ctype[s]) a.frame[c].force_rebuild = 1;
+    a.x[s] = x;
+    a.y[s] = y;
+    a.z[s] = z;
+    a.size[s] = sz;
+    a.young[s] = a.young2[src];
+    a.ctype[s] = ct;
+    if (has_phase) a.phase[s] = a.phase2[src];
+    a.rem[s] = 0;
+    if (a.desc[c].verlet && a.x0) {
+        float hx, hy, hz, lx, ly, lz;
+        tm_split(x, hx, lx);
+        tm_split(y, hy, ly);
+        tm_split(z, hz, lz);
+        const float4 o = a.x0[s];
+        const float ex = hx - o.x, ey = hy - o.y, ez = hz - o.z;
+        const unsigned bits = __float_as_uint(sqrtf(fmaf(ex, ex, fmaf(ey, ey, ez * ez))));
+        const unsigned m = __reduce_max_sync(__activemask(), bits);
+        if (bits == m) atomicMax(&a.frame[c].maxdisp, m);
+    }
+}
+
+// cell types of a fresh upload (identity order)
+__global__ void k_check_types(tm_arrays a, const tm_consts *K, long long off, int n, int *bad)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int ct = a.ctype[off + k];
+    if (ct < 0 || ct >= K->ntypes) {
+        atomicExch(bad, 1);
+        a.ctype[off + k] = 0;
+    }
 }
 
 template <typename T>
@@ -223,7 +277,7 @@ static int enqueue_build(tm_session *s, int p, int &nk)
     CK(cudaMemsetAsync(a.bin_count, 0, (size_t)(nbin + 1) * sizeof(uint32_t), st));
     CK(cudaMemsetAsync(a.bin_cursor, 0, (size_t)(nbin + 1) * sizeof(uint32_t), st));
     CK(cudaMemsetAsync(a.bigbins, 0, sizeof(int), st));
-    CK(cudaMemsetAsync(a.fix_count, 0, sizeof(int), st));
+    CK(cudaMemsetAsync(a.fix_count, 0, 3 * sizeof(int), st));   // fix count and the two work counters
     k_step_init<<<blocks_for(ncol, 128), 128, 0, st>>>(a);
     k_bbox<<<blocks_for(nsl, 256), 256, 0, st>>>(a, s->K.ntypes);
     k_frame<<<blocks_for(ncol, 128), 128, 0, st>>>(a, s->dK);
@@ -260,13 +314,14 @@ static int enqueue_compute(tm_session *s, int &nk, bool with_marks)
     bool any_cic, any64, any32;
     colony_mix(s, any_cic, any64, any32);
     tm_arrays b = view(s, s->parity);
+    const int lists = b.qcap > 0 ? 2 : 0;   // list kernel + overflow search pass
     if (any64) {
         CK(tm_launch_pair(b, s->dK, 0, s->stream));
-        nk += 2;
+        nk += 1 + lists;
     }
     if (any32) {
         CK(tm_launch_pair(b, s->dK, 1, s->stream));
-        nk += 3;
+        nk += 2 + lists;
     }
     if (with_marks) mark(s);
     CK(tm_launch_octree(b, s->dK, s->stream));
@@ -407,10 +462,11 @@ extern "C" int tm_session_create(tm_session **out, const tm_session_config *cfg,
     AL(a.mass, S * K.ntypes)
     s->mass_types = K.ntypes;
     AL(a.bin_count, B + 1) AL(a.bin_cursor, B + 1) AL(a.bin_start, B + 1) AL(a.bigbins, 2 * (S / 33) + 4)
-    AL(a.fix_count, 1) AL(a.fix_list, S)
+    AL(a.fix_count, 4) AL(a.fix_list, S)
+    if (rc == TM_OK) a.work = a.fix_count + 1;
     AL(a.density, S) AL(a.v, S) AL(a.mindist, S) AL(a.fx, S) AL(a.fy, S) AL(a.fz, S) AL(a.nbcount, S) AL(a.nbmin, S)
     AL(a.grid, G) AL(a.desc, C) AL(a.frame, C)
-    AL(s->scan_tmp, tm_scan_tmp_words(B + 1)) AL(s->d_octsize, C) AL(s->dK, 1)
+    AL(s->scan_tmp, tm_scan_tmp_words(B + 1)) AL(s->d_octsize, C) AL(s->dK, 1) AL(s->d_flag, 1)
     if (rc == TM_OK) rc = dalloc((double **)&s->d_scratch, S);
     if (cfg->diagnostics) {
         AL(a.nbhash, S) AL(a.vcand, S)
@@ -458,7 +514,7 @@ extern "C" int tm_session_destroy(tm_session *s)
                     a.young2, a.ctype2, a.phase2, a.perm2, a.rem2, a.col, a.code, a.codes, a.bin, a.tmp, a.rank, a.hi, a.lo, a.vlist, a.vcount, a.x0,
                     a.mass, a.bin_count, a.bin_cursor, a.bin_start, a.bigbins, a.fix_count, a.fix_list, a.density, a.v, a.mindist, a.fx,
                     a.fy, a.fz, a.nbcount, a.nbmin, a.nbhash, a.vcand, a.grid, a.desc, a.frame, s->scan_tmp, s->d_octsize,
-                    s->dK, s->d_scratch};
+                    s->dK, s->d_scratch, s->d_flag};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (auto ev : s->evpool) cudaEventDestroy(ev);
@@ -495,36 +551,55 @@ static int grid_geometry(int dim, float gfh, int gsize[3], double lower[3])
     return TM_OK;
 }
 
-static int copy_cells_in(tm_session *s, const colony_host &c, const tm_colony_input *in)
+// keep: the colony keeps its cell count, so the cells go to their current
+// slots (k_upload_keep); otherwise slot k takes input cell k and the lists are
+// rebuilt.  Returns TM_EINVAL if a cell type lies outside the table.
+static int copy_cells_in(tm_session *s, const colony_host &c, const tm_colony_input *in, bool keep)
 {
     const tm_arrays a = view(s, s->parity);
     const long long o = c.off;
     const size_t n = (size_t)in->n;
+    const int cid = (int)(&c - s->cols.data());
     cudaStream_t st = s->stream;
+    CK(cudaMemsetAsync(s->d_flag, 0, sizeof(int), st));
+    double *X = keep ? a.x2 : a.x, *Y = keep ? a.y2 : a.y, *Z = keep ? a.z2 : a.z, *SZ = keep ? a.size2 : a.size;
+    float *YG = keep ? a.young2 : a.young;
+    int *CT = keep ? a.ctype2 : a.ctype, *PH = keep ? a.phase2 : a.phase;
     if (n) {
-        CK(cudaMemcpyAsync(a.x + o, in->x, n * 8, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(a.y + o, in->y, n * 8, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(a.z + o, in->z, n * 8, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(a.size + o, in->size, n * 8, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(a.young + o, in->young, n * 4, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(a.ctype + o, in->ctype, n * 4, cudaMemcpyHostToDevice, st));
-        if (in->phase) CK(cudaMemcpyAsync(a.phase + o, in->phase, n * 4, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(X + o, in->x, n * 8, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(Y + o, in->y, n * 8, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(Z + o, in->z, n * 8, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(SZ + o, in->size, n * 8, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(YG + o, in->young, n * 4, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(CT + o, in->ctype, n * 4, cudaMemcpyHostToDevice, st));
+        if (in->phase) CK(cudaMemcpyAsync(PH + o, in->phase, n * 4, cudaMemcpyHostToDevice, st));
     }
-    k_colony_init<<<blocks_for(c.nslots, 256), 256, 0, st>>>(a, (int)(&c - s->cols.data()), o, (int)n, c.nslots,
-                                                             in->phase ? 1 : 0);
+    if (keep) {
+        k_upload_keep<<<blocks_for((long long)n, 256), 256, 0, st>>>(a, s->dK, cid, o, (int)n, in->phase ? 1 : 0,
+                                                                    s->d_flag);
+    } else {
+        k_check_types<<<blocks_for((long long)n, 256), 256, 0, st>>>(a, s->dK, o, (int)n, s->d_flag);
+        k_colony_init<<<blocks_for(c.nslots, 256), 256, 0, st>>>(a, cid, o, (int)n, c.nslots, in->phase ? 1 : 0);
+    }
     CK(cudaGetLastError());
+    int bad = 0;
+    CK(cudaMemcpyAsync(&bad, s->d_flag, sizeof(int), cudaMemcpyDeviceToHost, st));
     // synchronous: the caller may free its buffers on return
     CK(cudaStreamSynchronize(st));
+    if (bad) return tm_fail(TM_EDEVICE, "a cell type lies outside 0..%d", s->K.ntypes - 1);
     return TM_OK;
 }
 
-static int check_input(const tm_session *s, const tm_colony_input *in)
+// scan_types: check the cell types on the host before anything is placed
+// (colony creation); uploads check them on the device
+static int check_input(const tm_session *s, const tm_colony_input *in, bool scan_types = true)
 {
     if (!in || in->n < 0) return tm_fail(TM_EINVAL, "bad colony input");
     if (in->n > 0 && (!in->x || !in->y || !in->z || !in->size || !in->young || !in->ctype))
         return tm_fail(TM_EINVAL, "colony input arrays missing");
     if (in->n > 0x7fffffffll) return tm_fail(TM_EINVAL, "colony too large");
-    for (long long k = 0; k < in->n; k++)
+    if (scan_types)
+        for (long long k = 0; k < in->n; k++)
         if (in->ctype[k] < 0 || in->ctype[k] >= s->K.ntypes)
             return tm_fail(TM_EINVAL, "cell %lld has cell type %d outside 0..%d", k, in->ctype[k], s->K.ntypes - 1);
     return TM_OK;
@@ -613,7 +688,7 @@ extern "C" int tm_colony_add(tm_session *s, const tm_colony_input *in, const tm_
         for (int t = 0; t < s->K.ntypes; t++) hmax = std::max(hmax, s->K.t[t].h);
         d.skin = opt->skin > 0.0f ? opt->skin : (float)(0.1 * hmax);
     }
-    d.rmax = opt->rmax > 0 ? opt->rmax : 16;
+    d.rmax = opt->rmax > 0 ? opt->rmax : 64;
     for (int k = 0; k < 3; k++) {
         d.glower[k] = glower[k];
         d.gsize[k] = ch.gsize[k];
@@ -628,8 +703,13 @@ extern "C" int tm_colony_add(tm_session *s, const tm_colony_input *in, const tm_
     f.binscale = 2.0f;
     CK(cudaMemcpyAsync(&s->A.frame[c], &f, sizeof f, cudaMemcpyHostToDevice, s->stream));
     rc = push_desc(s, c);
-    if (rc == TM_OK) rc = copy_cells_in(s, s->cols[c], in);
-    if (rc != TM_OK) return rc;
+    if (rc == TM_OK) rc = copy_cells_in(s, s->cols[c], in, false);
+    if (rc != TM_OK) {
+        const std::string msg = g_err;
+        tm_colony_remove(s, c);
+        g_err = msg;
+        return rc;
+    }
     drop_graphs(s);
     *id = c;
     return TM_OK;
@@ -667,20 +747,29 @@ extern "C" int tm_colony_upload(tm_session *s, int id, const tm_colony_input *in
 {
     int rc = lookup(s, id);
     if (rc) return rc;
-    rc = check_input(s, in);
+    rc = check_input(s, in, false);
     if (rc) return rc;
     colony_host &c = s->cols[id];
     if (in->n > c.nslots) return tm_fail(TM_EINVAL, "colony %d holds at most %d cells", id, c.nslots);
     CK(cudaSetDevice(s->device));
     CK(cudaStreamSynchronize(s->stream));
-    c.n = (int)in->n;
-    s->h_desc[id].n = c.n;
-    rc = push_desc(s, id);
-    if (rc) return rc;
-    rc = copy_cells_in(s, c, in);
-    if (rc) return rc;
-    drop_graphs(s);
-    return TM_OK;
+    const bool keep = in->n == c.n && c.n > 0;
+    if (!keep) {
+        c.n = (int)in->n;
+        s->h_desc[id].n = c.n;
+        rc = push_desc(s, id);
+        if (rc) return rc;
+        drop_graphs(s);
+    }
+    rc = copy_cells_in(s, c, in, keep);
+    if (rc == TM_EDEVICE) {
+        // a bad cell type: the colony is left empty
+        c.n = 0;
+        s->h_desc[id].n = 0;
+        push_desc(s, id);
+        drop_graphs(s);
+    }
+    return rc;
 }
 
 extern "C" int tm_colony_set_active(tm_session *s, int id, int active)

@@ -200,8 +200,12 @@ class Session:
 
     def upload(self, cid: int, col: Colony):
         inp, keep = self._input(col)
-        _check(load_library().tm_colony_upload(self._h, cid, C.byref(inp)))
-        self._n[cid] = col.n
+        rc = load_library().tm_colony_upload(self._h, cid, C.byref(inp))
+        if rc == 0:
+            self._n[cid] = col.n
+        elif rc == -4:      # a cell type outside the table: the colony was left empty
+            self._n[cid] = 0
+        _check(rc)
 
     def set_active(self, cid: int, active: bool):
         _check(load_library().tm_colony_set_active(self._h, cid, 1 if active else 0))
