@@ -64,13 +64,13 @@ struct tm_arrays {
     double *density, *v, *mindist, *fx, *fy, *fz;
     int *nbcount;
     int *nbmin;          // first Morton position within h, -1 if none
-    // neighbour lists: quarter q of cell `slot` holds vcount[q*lstride+slot]
-    // entries vlist[(q*qcap + k)*lstride + slot] (slots), k-major for coalescing
+    // neighbour lists: cell `slot` holds vcount[slot] entries
+    // vlist[k*lstride + slot] (slots), k-major so a warp's loads coalesce
     int *vlist;
     int *vcount;
     float4 *x0;          // float position at the last rebuild (displacement test)
     long long lstride;
-    int qcap;
+    int vcap;            // entries per cell
     unsigned long long *nbhash;
     int *vcand;
     // CIC grids

@@ -130,19 +130,17 @@ __device__ __forceinline__ void pair32(const tm_type &T, int dim, float dx, floa
                                        float sizej, pair_acc<1> &acc)
 {
     acc.mins = fminf(acc.mins, s);
-    const float dist = sqrtf(s);
     const float rs = s > 0.0f ? rsqrtf(s) : 0.0f;
+    // dist = sqrt(s): s * rsqrt(s) and one Newton step on dist^2 = s
+    float dist = s * rs;
+    dist = fmaf(0.5f * rs, fmaf(-dist, dist, s), dist);
     const float u = dist * T.inv_hf;
     // 1 - u as (h - dist) / h: the subtraction is exact near the cutoff
     const float omu = (T.hf - dist) * T.inv_hf;
-    float wk, wg;
-    if (u <= 0.5f) {
-        wk = T.cWf * fmaf(6.0f * u * u, u - 1.0f, 1.0f);
-        wg = u * fmaf(3.0f, u, -2.0f);
-    } else {
-        wk = T.cWf * (2.0f * omu * omu * omu);
-        wg = -omu * omu;
-    }
+    // both branches of the cubic spline, selected (no divergence)
+    const bool inner = u <= 0.5f;
+    const float wk = T.cWf * (inner ? fmaf(6.0f * u * u, u - 1.0f, 1.0f) : 2.0f * omu * omu * omu);
+    const float wg = inner ? u * fmaf(3.0f, u, -2.0f) : -omu * omu;
     const float term = T.kmassf * sizej * wk;
     acc.dens.add(term);
     // one-sigma rounding estimate of this term: W ~ (1-u)^3 amplifies the FP32
@@ -258,7 +256,6 @@ __device__ __forceinline__ void pair_group(const tm_arrays &a, const tm_consts *
     // lists it reaches h + skin
     const float rlist = T.hf + (build ? d.skin : 0.0f);
     const float hr = rlist * 1.00002f + 1e-4f;
-    const float rl2 = rlist * rlist * 1.00002f;
     int vc = 0;   // this lane's list entries
     const int nside = 1 << Lp;
     const float bs = f.binscale * (1.0f / (float)(1 << ls));
@@ -279,12 +276,7 @@ __device__ __forceinline__ void pair_group(const tm_arrays &a, const tm_consts *
     unsigned long long hash = 0;
     int nl = 0;
 
-    // exact pair maths over this lane's hit list (tile indices); on rebuild
-    // steps entries within h + skin also go to this lane's quarter of the list
-    auto append = [&](int j) {
-        if (vc < a.qcap) a.vlist[((long long)quarter * a.qcap + vc) * a.lstride + i] = j;
-        vc++;
-    };
+    // exact pair maths over this lane's hit list (tile indices)
     auto drain = [&]() {
         int m = nl;
         for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(FULL, m, o));
@@ -322,15 +314,30 @@ __device__ __forceinline__ void pair_group(const tm_arrays &a, const tm_consts *
     // test the staged tile [0, fill) and drain; the tile is refilled afterwards
     auto test_tile = [&](int fill, float thr) {
         if (build) {
-            // list build only: every entry within the conservative radius goes
-            // to this lane's quarter; the list kernel does the pair maths
+            // list build only: every entry within the conservative radius is
+            // appended to the cell's list (the four lanes of a cell take turns
+            // through the tile and place their hits by a ballot prefix); the
+            // list kernel does the pair maths
+            const int cshift = lane & ~(PAIR_LPC - 1);
+            const unsigned below = (1u << quarter) - 1u;
 #pragma unroll 4
-            for (int tt = quarter; tt < fill; tt += PAIR_LPC) {
-                const float4 cc = tA[tt];
-                const float dx = cc.x - sx, dy = cc.y - sy, dz = cc.z - sz;
-                const float s = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                const int j = __float_as_int(cc.w);
-                if (s <= thr && (long long)j != i) append(j);
+            for (int t0 = 0; t0 < fill; t0 += PAIR_LPC) {
+                const int tt = t0 + quarter;
+                bool hit = false;
+                int j = 0;
+                if (tt < fill) {
+                    const float4 cc = tA[tt];
+                    const float dx = cc.x - sx, dy = cc.y - sy, dz = cc.z - sz;
+                    const float s = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    j = __float_as_int(cc.w);
+                    hit = s <= thr && (long long)j != i;
+                }
+                const unsigned cm = (__ballot_sync(FULL, hit) >> cshift) & ((1u << PAIR_LPC) - 1u);
+                if (hit) {
+                    const int slot = vc + __popc(cm & below);
+                    if (slot < a.vcap) a.vlist[(long long)slot * a.lstride + i] = j;
+                }
+                vc += __popc(cm);
             }
             __syncwarp();
             return;
@@ -468,13 +475,13 @@ __device__ __forceinline__ void pair_group(const tm_arrays &a, const tm_consts *
         hash += __shfl_xor_sync(FULL, hash, o);
     }
     if (build) {
-        if (live) {
-            a.vcount[(long long)quarter * a.lstride + i] = min(vc, a.qcap);
-            if (quarter == 0) a.x0[i] = hi_i;
+        if (live && quarter == 0) {
+            a.vcount[i] = min(vc, a.vcap);
+            a.x0[i] = hi_i;
         }
         // an overflowing list cannot serve this step: flag the colony, whose
         // results the list kernel then leaves to a search pass
-        if (__any_sync(FULL, live && vc > a.qcap) && lane == 0)
+        if (__any_sync(FULL, live && vc > a.vcap) && lane == 0)
             if (atomicExch(&a.frame[c].list_ok, 0) == 1) atomicAdd(&a.work[1], 1);
         return;
     }
@@ -505,9 +512,8 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
 }
 
 // Pair kernel on the neighbour lists (every step of a colony with lists): one
-// thread per cell walks the entries of its four quarters with the same exact
-// maths; the cutoff is decided each step, so the neighbour sets are those of
-// this step.
+// thread per cell walks its list with the same exact maths; the cutoff is
+// decided each step, so the neighbour sets are those of this step.
 // Entries are taken two at a time with both gathers issued before either is
 // used (the walk is bound by the latency of the dependent index -> position
 // loads, not by arithmetic).
@@ -557,37 +563,32 @@ __global__ void __launch_bounds__(256, 4) k_plist(tm_arrays a, const tm_consts *
     int cnt_nb = 0, nbmin = 0x7fffffff;
     unsigned long long hash = 0;
     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int q = 0; q < 4; q++) {
-        const int cnt = __ldg(a.vcount + (long long)q * a.lstride + i);
-        const int *__restrict__ lst = a.vlist + (long long)q * a.qcap * a.lstride + i;
-        int k = 0;
-        for (; k + 1 < cnt; k += 2) {
-            const int j0 = __ldg(lst + (long long)k * a.lstride);
-            const int j1 = __ldg(lst + (long long)(k + 1) * a.lstride);
-            const float4 h0 = PREC ? __ldg(hi + j0) : z4, l0 = PREC ? __ldg(lo + j0) : z4;
-            const float4 h1 = PREC ? __ldg(hi + j1) : z4, l1 = PREC ? __ldg(lo + j1) : z4;
-            plist_one<PREC>(a, T, dim, t, i, hi_i, lo_i, j0, h0, l0, acc, cnt_nb, nbmin, hash);
-            plist_one<PREC>(a, T, dim, t, i, hi_i, lo_i, j1, h1, l1, acc, cnt_nb, nbmin, hash);
-        }
-        if (k < cnt) {
-            const int j0 = __ldg(lst + (long long)k * a.lstride);
-            const float4 h0 = PREC ? __ldg(hi + j0) : z4, l0 = PREC ? __ldg(lo + j0) : z4;
-            plist_one<PREC>(a, T, dim, t, i, hi_i, lo_i, j0, h0, l0, acc, cnt_nb, nbmin, hash);
-        }
+    const int cnt = __ldg(a.vcount + i);
+    const long long ls = a.lstride;
+    const int *__restrict__ lst = a.vlist + i;
+    int k = 0;
+    for (; k + 1 < cnt; k += 2, lst += 2 * ls) {
+        const int j0 = __ldg(lst);
+        const int j1 = __ldg(lst + ls);
+        const float4 h0 = PREC ? __ldg(hi + j0) : z4, l0 = PREC ? __ldg(lo + j0) : z4;
+        const float4 h1 = PREC ? __ldg(hi + j1) : z4, l1 = PREC ? __ldg(lo + j1) : z4;
+        plist_one<PREC>(a, T, dim, t, i, hi_i, lo_i, j0, h0, l0, acc, cnt_nb, nbmin, hash);
+        plist_one<PREC>(a, T, dim, t, i, hi_i, lo_i, j1, h1, l1, acc, cnt_nb, nbmin, hash);
+    }
+    if (k < cnt) {
+        const int j0 = __ldg(lst);
+        const float4 h0 = PREC ? __ldg(hi + j0) : z4, l0 = PREC ? __ldg(lo + j0) : z4;
+        plist_one<PREC>(a, T, dim, t, i, hi_i, lo_i, j0, h0, l0, acc, cnt_nb, nbmin, hash);
     }
     pair_store<PREC>(a, i, acc, cnt_nb, nbmin, hash, false);
     if constexpr (PREC == 1) {
         if (needs_fix64(acc)) {
             // FP64 density over the same list, the cutoff decided in FP64
             double dens = 0.0;
-            for (int q = 0; q < 4; q++) {
-                const int cnt = a.vcount[(long long)q * a.lstride + i];
-                const int *lst = a.vlist + (long long)q * a.qcap * a.lstride + i;
-                for (int k = 0; k < cnt; k++) {
-                    const int j = lst[(long long)k * a.lstride];
-                    const double dist = dist64(a, i, j);
-                    if (dist <= T.h) dens = add64(dens, dens_term64(T, dist, a.size[j]));
-                }
+            for (int kk = 0; kk < cnt; kk++) {
+                const int j = a.vlist[(long long)kk * ls + i];
+                const double dist = dist64(a, i, j);
+                if (dist <= T.h) dens = add64(dens, dens_term64(T, dist, a.size[j]));
             }
             a.density[i] = dens;
         }
@@ -663,13 +664,13 @@ cudaError_t tm_launch_pair(const tm_arrays &a, const tm_consts *K, int prec, cud
     const unsigned lgrid = (unsigned)((a.nslots_total + 255) / 256);
     if (prec == 0) {
         k_pair<0><<<grid, bt, 0, st>>>(a, K, 0);
-        if (a.qcap > 0) {
+        if (a.vcap > 0) {
             k_plist<0><<<lgrid, 256, 0, st>>>(a, K);
             k_pair<0><<<grid, bt, 0, st>>>(a, K, 1);
         }
     } else {
         k_pair<1><<<grid, bt, 0, st>>>(a, K, 0);
-        if (a.qcap > 0) {
+        if (a.vcap > 0) {
             k_plist<1><<<lgrid, 256, 0, st>>>(a, K);
             k_pair<1><<<grid, bt, 0, st>>>(a, K, 1);
         }

@@ -314,7 +314,7 @@ static int enqueue_compute(tm_session *s, int &nk, bool with_marks)
     bool any_cic, any64, any32;
     colony_mix(s, any_cic, any64, any32);
     tm_arrays b = view(s, s->parity);
-    const int lists = b.qcap > 0 ? 2 : 0;   // list kernel + overflow search pass
+    const int lists = b.vcap > 0 ? 2 : 0;   // list kernel + overflow search pass
     if (any64) {
         CK(tm_launch_pair(b, s->dK, 0, s->stream));
         nk += 1 + lists;
@@ -472,9 +472,9 @@ extern "C" int tm_session_create(tm_session **out, const tm_session_config *cfg,
         AL(a.nbhash, S) AL(a.vcand, S)
     }
     a.lstride = S;
-    a.qcap = cfg->list_capacity > 0 ? (cfg->list_capacity + 3) / 4 : 0;
-    if (a.qcap > 0) {
-        AL(a.vlist, S * 4 * (long long)a.qcap) AL(a.vcount, S * 4) AL(a.x0, S)
+    a.vcap = cfg->list_capacity > 0 ? cfg->list_capacity : 0;
+    if (a.vcap > 0) {
+        AL(a.vlist, S * (long long)a.vcap) AL(a.vcount, S) AL(a.x0, S)
     }
 #undef AL
     if (rc == TM_OK) {
@@ -682,7 +682,7 @@ extern "C" int tm_colony_add(tm_session *s, const tm_colony_input *in, const tm_
     d.update_mode = opt->update_mode;
     d.active = 1;
     d.dt = opt->dt;
-    d.verlet = (opt->verlet && s->A.qcap > 0) ? 1 : 0;
+    d.verlet = (opt->verlet && s->A.vcap > 0) ? 1 : 0;
     {
         double hmax = 0.0;
         for (int t = 0; t < s->K.ntypes; t++) hmax = std::max(hmax, s->K.t[t].h);
