@@ -83,8 +83,8 @@ typedef struct {
     int lcap;                 /* deepest bin level, 0: from the colony's extent */
     int64_t reserve;          /* slots to reserve (>= n) so later uploads can grow */
     int verlet;               /* 1: keep neighbour lists within h + skin between rebuilds */
-    float skin;               /* list margin (0: 0.1 h) */
-    int rmax;                 /* rebuild the lists at least every rmax steps (0: 64) */
+    float skin;               /* list margin (0: the session's skin_over_h * largest h) */
+    int rmax;                 /* rebuild the lists at least every rmax steps (0: the session's rmax) */
 } tm_colony_options;
 
 /* Outputs in caller order (host memory); any pointer may be NULL. */
@@ -110,6 +110,9 @@ typedef struct {
     int64_t n;
     int64_t list_rebuilds;            /* steps that rebuilt the neighbour lists */
     int64_t codes_slow;               /* lattice codes of the last step decided in FP64 */
+    float list_maxdisp;               /* largest cell displacement since the lists were built */
+    float list_skin;                  /* the colony's list skin */
+    int32_t list_age;                 /* steps since the lists were built */
 } tm_colony_info;
 
 const char *tm_last_error(void);
@@ -120,6 +123,35 @@ int tm_session_create(tm_session **out, const tm_session_config *cfg, const tm_c
 int tm_session_destroy(tm_session *s);
 /* cudaStream_t the session launches on */
 void *tm_session_stream(tm_session *s);
+
+/* Device bytes a session with this configuration allocates (-1 on a bad
+ * configuration); with tm_device_memory, what admission by free HBM uses. */
+int64_t tm_session_bytes(const tm_session_config *cfg, int ntypes);
+/* Free and total bytes of a device (cudaMemGetInfo). */
+int tm_device_memory(int device, int64_t *free_bytes, int64_t *total_bytes);
+
+/* Launch shapes and neighbour-list parameters of a session, as an autotuner
+ * sets them.  Defaults: {1, 1, 128, 0.1, 64}. */
+typedef struct tm_tuning {
+    int pair_lshift;     /* search candidates from Morton nodes 0 or 1 level above the bins */
+    int list_variant;    /* list kernel block/registers: 1 = 256 threads, 64 registers; 2 = 128/64;
+                            3 = 256/80; 4 = 512/64 */
+    int walk_block;      /* octree walk threads per block: 64, 128 or 256 */
+    float skin_over_h;   /* list skin as a fraction of the largest h, in (0, 1] */
+    int rmax;            /* rebuild the lists at least every rmax steps */
+} tm_tuning;
+int tm_session_get_tuning(tm_session *s, tm_tuning *t);
+/* Set all fields (validated; TM_EINVAL leaves the tuning unchanged).  A new
+ * skin_over_h or rmax applies to every colony (overriding its options) and
+ * to colonies added later whose options leave skin / rmax at 0; their lists
+ * are rebuilt at the next step. */
+int tm_session_set_tuning(tm_session *s, const tm_tuning *t);
+
+/* Expected fraction of cells whose neighbour lists are rebuilt per step,
+ * extrapolating each colony's displacement since its last rebuild linearly
+ * (at least 1/rmax), weighted by cells; and the rebuilds so far over all
+ * colonies.  Meaningful after a step. */
+int tm_session_list_rate(tm_session *s, double *rate, int64_t *rebuilds);
 
 /* Add a colony; its id is written to *id.  Uploads the cells. */
 int tm_colony_add(tm_session *s, const tm_colony_input *in, const tm_colony_options *opt, int *id);

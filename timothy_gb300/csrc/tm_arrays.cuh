@@ -82,3 +82,17 @@ struct tm_arrays {
     long long nslots_total;
     int want_diag;       // fill nbcount/nbhash/vcand
 };
+
+// slot i holds a live cell of colony d (unsigned: slots below the colony's
+// range are not live either)
+__device__ __forceinline__ bool tm_live(long long i, const tm_desc &d)
+{
+    return (unsigned long long)(i - d.off) < (unsigned long long)d.n;
+}
+
+// launch shapes chosen per session (tm_tuning)
+struct tm_shapes {
+    int pair_lshift;    // candidate ranges from Morton nodes this many levels above the bins (0 or 1)
+    int list_variant;   // list kernel block size / register budget, 1..4
+    int walk_block;     // octree walk threads per block (64, 128 or 256)
+};

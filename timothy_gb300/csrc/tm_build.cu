@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(256) k_bbox(tm_arrays a, int ntypes)
     if (s < a.nslots_total) {
         c = a.col[s];
         const tm_desc &d = a.desc[c];
-        live = d.active && (s - d.off) < d.n;
+        live = d.active && tm_live(s, d);
     }
     if (lane == 0) colid[w] = (((s >> 5) << 5) < a.nslots_total) ? a.col[(s >> 5) << 5] : -1;
     __syncthreads();
@@ -210,7 +210,7 @@ __global__ void k_codes(tm_arrays a)
     if (s >= a.nslots_total) return;
     int c = a.col[s];
     const tm_desc &d = a.desc[c];
-    if (!d.active || (s - d.off) >= d.n) return;
+    if (!d.active || !tm_live(s, d)) return;
     const tm_frame &f = a.frame[c];
     uint4 q;
     const double px = a.x[s], py = a.y[s], pz = a.z[s];
@@ -237,7 +237,7 @@ __global__ void k_scatter(tm_arrays a)
     if (s >= a.nslots_total) return;
     int c = a.col[s];
     const tm_desc &d = a.desc[c];
-    if (!d.active || (s - d.off) >= d.n) return;
+    if (!d.active || !tm_live(s, d)) return;
     uint32_t b = a.bin[s];
     long long pos = a.frame[c].bin_base + a.bin_start[b] + atomicAdd(&a.bin_cursor[b], 1u);
     a.tmp[pos] = (int)s;
@@ -251,7 +251,7 @@ __global__ void k_binsort_small(tm_arrays a)
     if (i >= a.nslots_total) return;
     int c = a.col[i];
     const tm_desc &d = a.desc[c];
-    if (!d.active || (i - d.off) >= d.n) return;
+    if (!d.active || !tm_live(i, d)) return;
     int r = a.tmp[i];
     uint32_t b = a.bin[r];
     long long st = a.frame[c].bin_base + a.bin_start[b];
@@ -357,7 +357,7 @@ __global__ void k_gather(tm_arrays a, const tm_consts *K)
     if (i >= a.nslots_total) return;
     int c = a.col[i];
     const tm_desc &d = a.desc[c];
-    if (!d.active || (i - d.off) >= d.n) return;
+    if (!d.active || !tm_live(i, d)) return;
     const int r = a.tmp[i];                 // slot of the cell at this position
     a.codes[i] = a.code[r];
     const double x = a.x[r], y = a.y[r], z = a.z[r], sz = a.size[r];
@@ -397,7 +397,7 @@ __global__ void k_copyback(tm_arrays a)
     if (i >= a.nslots_total) return;
     int c = a.col[i];
     const tm_desc &d = a.desc[c];
-    if (!d.active || (i - d.off) >= d.n || !a.frame[c].rebuild) return;
+    if (!d.active || !tm_live(i, d) || !a.frame[c].rebuild) return;
     a.x[i] = a.x2[i];
     a.y[i] = a.y2[i];
     a.z[i] = a.z2[i];
@@ -430,7 +430,7 @@ __global__ void k_octsize(tm_arrays a, unsigned long long *out)
         c = a.col[i];
         const tm_desc &d = a.desc[c];
         long long k = i - d.off;
-        if (d.active && k < d.n && d.n >= 2) {
+        if (d.active && k >= 0 && k < d.n && d.n >= 2) {
             uint4 me = a.codes[i];
             int lp = k > 0 ? tm_lcp(a.codes[i - 1], me) : 0;
             int ln = (k + 1 < d.n) ? tm_lcp(me, a.codes[i + 1]) : 0;

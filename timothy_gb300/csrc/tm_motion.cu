@@ -27,7 +27,7 @@ __global__ void k_update(tm_arrays a, const tm_consts *K)
     if (i >= a.nslots_total) return;
     const int c = a.col[i];
     const tm_desc &d = a.desc[c];
-    if (!d.active || (i - d.off) >= d.n || d.update_mode == 2) return;
+    if (!d.active || !tm_live(i, d) || d.update_mode == 2) return;
     const int dim = K->dim;
     double x = a.x[i], y = a.y[i], z = a.z[i];
     const double fx = a.fx[i], fy = a.fy[i], fz = a.fz[i];
@@ -81,7 +81,7 @@ __global__ void k_cic(tm_arrays a, const tm_consts *K)
     const int c = a.col[(i >> 5) << 5];
     const tm_desc &d = a.desc[c];
     if (!d.active || d.gridoff < 0) return;                    // uniform per warp
-    const bool live = (i - d.off) < d.n;
+    const bool live = tm_live(i, d);
     const int dim = K->dim;
     const int lane = threadIdx.x & 31;
     long long ci[3] = {0, 0, 0};

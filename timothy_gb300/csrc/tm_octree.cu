@@ -90,13 +90,13 @@ __device__ float pair_potential32(float dist, float s1, float y1, float s2, floa
     return (2.0f * xc * xc / (5.0f * D)) * sqrtf((s1 * s2) / (s1 + s2)) + area * 0.1f;
 }
 
-__global__ void __launch_bounds__(128) k_octree(tm_arrays a, const tm_consts *K)
+__global__ void __launch_bounds__(256) k_octree(tm_arrays a, const tm_consts *K)
 {
     long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= a.nslots_total) return;
     const int c = a.col[p];
     const tm_desc &d = a.desc[c];
-    if (!d.active || (p - d.off) >= d.n || d.n <= 1) return;
+    if (!d.active || !tm_live(p, d) || d.n <= 1) return;
     const tm_frame &f = a.frame[c];
     const int t = a.ctype[p];
     const tm_type &T = K->t[t];
@@ -246,10 +246,11 @@ __global__ void __launch_bounds__(128) k_octree(tm_arrays a, const tm_consts *K)
     if (a.want_diag) a.vcand[p] = jstar >= 0 ? a.perm[jstar] : -1;
 }
 
-cudaError_t tm_launch_octree(const tm_arrays &a, const tm_consts *K, cudaStream_t st)
+cudaError_t tm_launch_octree(const tm_arrays &a, const tm_consts *K, int block, cudaStream_t st)
 {
-    unsigned grid = (unsigned)((a.nslots_total + 127) / 128);
+    if (block != 64 && block != 256) block = 128;
+    unsigned grid = (unsigned)((a.nslots_total + block - 1) / block);
     if (grid == 0) return cudaSuccess;
-    k_octree<<<grid, 128, 0, st>>>(a, K);
+    k_octree<<<grid, block, 0, st>>>(a, K);
     return cudaGetLastError();
 }

@@ -32,9 +32,6 @@
 #define PAIR_TILE 256
 #define PAIR_LCAP 64
 #define PAIR_LPC 4                      // lanes per cell
-#ifndef PAIR_LSHIFT
-#define PAIR_LSHIFT 1                   // candidate nodes one level above the bins
-#endif
 #define PAIR_CPW (32 / PAIR_LPC)        // cells per warp
 
 template <int PREC>
@@ -193,8 +190,9 @@ __device__ __forceinline__ void pair_store(const tm_arrays &a, long long i, pair
 
 // one warp, one group of PAIR_CPW Morton-consecutive slots starting at base
 template <int PREC>
-__device__ __forceinline__ void pair_group(const tm_arrays &a, const tm_consts *K, int fallback, long long base,
-                                           int lane, float4 *tA, float4 *tB, unsigned short (*list)[32])
+__device__ __forceinline__ void pair_group(const tm_arrays &a, const tm_consts *K, int fallback, int lshift,
+                                           long long base, int lane, float4 *tA, float4 *tB,
+                                           unsigned short (*list)[32])
 {
     if (base >= a.nslots_total) return;
     const int c = a.col[base];             // colonies are 32-aligned, so a group stays in one
@@ -206,13 +204,13 @@ __device__ __forceinline__ void pair_group(const tm_arrays &a, const tm_consts *
     // the pair maths), the others search and evaluate here; second pass
     // (fallback): colonies whose lists overflowed search and evaluate
     if (fallback && (!d.verlet || f.list_ok)) return;
-    if ((base - d.off) >= d.n) return;      // group beyond the colony's cells
+    if (!tm_live(base, d)) return;      // group beyond the colony's cells
     const bool build = !fallback && d.verlet;
     const int dim = K->dim;
 
     const int quarter = lane % PAIR_LPC;   // this lane's share of the cell's candidates
     const long long i = base + lane / PAIR_LPC;
-    const bool live = (i - d.off) < d.n;
+    const bool live = tm_live(i, d);
     const int t = live ? a.ctype[i] : 0;
     const tm_type &T = K->t[t];
 
@@ -222,9 +220,9 @@ __device__ __forceinline__ void pair_group(const tm_arrays &a, const tm_consts *
     // then span much of the colony; the subgroup node bounds every box.
     const int L = f.L;
     const int Lg = L >= 2 ? L - 2 : 0;
-    // candidate ranges come from nodes PAIR_LSHIFT levels above the bins: each
-    // is one contiguous run of 8^PAIR_LSHIFT bins in Morton order
-    const int ls = L > PAIR_LSHIFT ? PAIR_LSHIFT : 0;
+    // candidate ranges come from nodes lshift levels above the bins: each is
+    // one contiguous run of 8^lshift bins in Morton order
+    const int ls = L > lshift ? lshift : 0;
     const int Lp = L - ls;
     const uint32_t key = live ? tm_prefix(a.codes[i], Lg) : 0xffffffffu;
     const unsigned live_mask = __ballot_sync(FULL, live);
@@ -493,7 +491,8 @@ __device__ __forceinline__ void pair_group(const tm_arrays &a, const tm_consts *
 // on a step where no colony searches (all evaluate their lists) or no list
 // overflowed (fallback pass) every block leaves after one load.
 template <int PREC>
-__global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, const tm_consts *K, int fallback)
+__global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, const tm_consts *K, int fallback,
+                                                                   int lshift)
 {
     // per warp: tile of staged candidates (A: hi part of the origin-relative
     // position + slot, B: lo part + radius) and one hit list per lane holding
@@ -506,7 +505,7 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
     const long long ngroups = (a.nslots_total + PAIR_CPW - 1) / PAIR_CPW;
     const long long stride = (long long)gridDim.x * TM_WARPS_PER_BLOCK;
     for (long long w = (long long)blockIdx.x * TM_WARPS_PER_BLOCK + wib; w < ngroups; w += stride) {
-        pair_group<PREC>(a, K, fallback, w * PAIR_CPW, lane, tA_s[wib], tB_s[wib], list_s[wib]);
+        pair_group<PREC>(a, K, fallback, lshift, w * PAIR_CPW, lane, tA_s[wib], tB_s[wib], list_s[wib]);
         __syncwarp();
     }
 }
@@ -541,8 +540,8 @@ __device__ __forceinline__ void plist_one(const tm_arrays &a, const tm_type &T, 
     }
 }
 
-template <int PREC>
-__global__ void __launch_bounds__(256, 4) k_plist(tm_arrays a, const tm_consts *K)
+template <int PREC, int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) k_plist(tm_arrays a, const tm_consts *K)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (((i >> 5) << 5) >= a.nslots_total) return;
@@ -551,7 +550,7 @@ __global__ void __launch_bounds__(256, 4) k_plist(tm_arrays a, const tm_consts *
     if (!d.active || d.precision != PREC || d.n <= 1 || !d.verlet) return;
     const tm_frame &f = a.frame[c];
     if (!f.list_ok) return;                 // overflowed: the search pass evaluates
-    if ((i - d.off) >= d.n) return;
+    if (!tm_live(i, d)) return;
     const int dim = K->dim;
     const int t = a.ctype[i];
     const tm_type &T = K->t[t];
@@ -654,25 +653,37 @@ static unsigned pair_grid_cap(int prec)
     return (unsigned)cached[prec][dev];
 }
 
-cudaError_t tm_launch_pair(const tm_arrays &a, const tm_consts *K, int prec, cudaStream_t st)
+template <int PREC>
+static void launch_plist(const tm_arrays &a, const tm_consts *K, int variant, cudaStream_t st)
+{
+    const long long n = a.nslots_total;
+    switch (variant) {
+    case 2: k_plist<PREC, 128, 8><<<(unsigned)((n + 127) / 128), 128, 0, st>>>(a, K); break;
+    case 3: k_plist<PREC, 256, 3><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(a, K); break;
+    case 4: k_plist<PREC, 512, 2><<<(unsigned)((n + 511) / 512), 512, 0, st>>>(a, K); break;
+    default: k_plist<PREC, 256, 4><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(a, K); break;
+    }
+}
+
+cudaError_t tm_launch_pair(const tm_arrays &a, const tm_consts *K, int prec, const tm_shapes &sh, cudaStream_t st)
 {
     const long long groups = (a.nslots_total + PAIR_CPW - 1) / PAIR_CPW;
     const int bt = TM_WARPS_PER_BLOCK * 32;
     const long long need = (groups + TM_WARPS_PER_BLOCK - 1) / TM_WARPS_PER_BLOCK;
     const unsigned grid = (unsigned)std::min<long long>(need, pair_grid_cap(prec != 0));
     if (grid == 0) return cudaSuccess;
-    const unsigned lgrid = (unsigned)((a.nslots_total + 255) / 256);
+    const int ls = sh.pair_lshift;
     if (prec == 0) {
-        k_pair<0><<<grid, bt, 0, st>>>(a, K, 0);
+        k_pair<0><<<grid, bt, 0, st>>>(a, K, 0, ls);
         if (a.vcap > 0) {
-            k_plist<0><<<lgrid, 256, 0, st>>>(a, K);
-            k_pair<0><<<grid, bt, 0, st>>>(a, K, 1);
+            launch_plist<0>(a, K, sh.list_variant, st);
+            k_pair<0><<<grid, bt, 0, st>>>(a, K, 1, ls);
         }
     } else {
-        k_pair<1><<<grid, bt, 0, st>>>(a, K, 0);
+        k_pair<1><<<grid, bt, 0, st>>>(a, K, 0, ls);
         if (a.vcap > 0) {
-            k_plist<1><<<lgrid, 256, 0, st>>>(a, K);
-            k_pair<1><<<grid, bt, 0, st>>>(a, K, 1);
+            launch_plist<1>(a, K, sh.list_variant, st);
+            k_pair<1><<<grid, bt, 0, st>>>(a, K, 1, ls);
         }
         k_density_fix64<<<256, 128, 0, st>>>(a, K);
     }

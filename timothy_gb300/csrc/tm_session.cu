@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 static thread_local std::string g_err;
@@ -131,6 +132,7 @@ struct tm_session {
     long long launches = 0;
     int kernels_per_step = 0;
     int mass_types = 0;   // types the FP64 density-weight array holds
+    tm_tuning tune{1, 1, 128, 0.1f, 64};
     cudaEvent_t tstart = nullptr, tstop = nullptr;
 };
 
@@ -215,6 +217,12 @@ __global__ void k_check_types(tm_arrays a, const tm_consts *K, long long off, in
         atomicExch(bad, 1);
         a.ctype[off + k] = 0;
     }
+}
+
+__global__ void k_release_slots(int *col, long long off, int nslots, int none)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nslots) col[off + k] = none;
 }
 
 template <typename T>
@@ -308,6 +316,15 @@ static int enqueue_cic(tm_session *s, int &nk)
     return TM_OK;
 }
 
+static tm_shapes shapes_of(const tm_session *s)
+{
+    tm_shapes sh;
+    sh.pair_lshift = s->tune.pair_lshift;
+    sh.list_variant = s->tune.list_variant;
+    sh.walk_block = s->tune.walk_block;
+    return sh;
+}
+
 // pair kernel(s) and octree walk on the current (sorted) buffers
 static int enqueue_compute(tm_session *s, int &nk, bool with_marks)
 {
@@ -316,15 +333,15 @@ static int enqueue_compute(tm_session *s, int &nk, bool with_marks)
     tm_arrays b = view(s, s->parity);
     const int lists = b.vcap > 0 ? 2 : 0;   // list kernel + overflow search pass
     if (any64) {
-        CK(tm_launch_pair(b, s->dK, 0, s->stream));
+        CK(tm_launch_pair(b, s->dK, 0, shapes_of(s), s->stream));
         nk += 1 + lists;
     }
     if (any32) {
-        CK(tm_launch_pair(b, s->dK, 1, s->stream));
+        CK(tm_launch_pair(b, s->dK, 1, shapes_of(s), s->stream));
         nk += 2 + lists;
     }
     if (with_marks) mark(s);
-    CK(tm_launch_octree(b, s->dK, s->stream));
+    CK(tm_launch_octree(b, s->dK, s->tune.walk_block, s->stream));
     nk++;
     return TM_OK;
 }
@@ -390,6 +407,87 @@ static double host_type_const(int dim, int which, double h, double h2, double h3
 
 extern "C" int tm_session_destroy(tm_session *s);
 
+// Every device buffer of a session: allocates them (alloc) or only adds up
+// their bytes (*bytes), so admission by free memory uses the same list.
+static int session_buffers(tm_session *s, long long S, long long B, long long G, int C, bool alloc,
+                           long long *bytes)
+{
+    tm_arrays &a = s->A;
+    const tm_session_config *cfg = &s->cfg;
+    int rc = TM_OK;
+    long long total = 0;
+    auto AL = [&](auto &p, long long cnt) {
+        using T = typename std::remove_reference<decltype(*p)>::type;
+        total += std::max(cnt, 1ll) * (long long)sizeof(T);
+        if (alloc && rc == TM_OK) rc = dalloc(&p, cnt);
+    };
+    AL(a.x, S); AL(a.y, S); AL(a.z, S); AL(a.size, S); AL(a.young, S); AL(a.ctype, S); AL(a.phase, S);
+    AL(a.perm, S); AL(a.rem, S);
+    AL(a.x2, S); AL(a.y2, S); AL(a.z2, S); AL(a.size2, S); AL(a.young2, S); AL(a.ctype2, S); AL(a.phase2, S);
+    AL(a.perm2, S); AL(a.rem2, S);
+    AL(a.col, S); AL(a.code, S); AL(a.codes, S); AL(a.bin, S); AL(a.tmp, S); AL(a.rank, S); AL(a.hi, S);
+    AL(a.lo, S);
+    AL(a.mass, S * s->K.ntypes);
+    AL(a.bin_count, B + 1); AL(a.bin_cursor, B + 1); AL(a.bin_start, B + 1); AL(a.bigbins, 2 * (S / 33) + 4);
+    AL(a.fix_count, 4); AL(a.fix_list, S);
+    AL(a.density, S); AL(a.v, S); AL(a.mindist, S); AL(a.fx, S); AL(a.fy, S); AL(a.fz, S); AL(a.nbcount, S);
+    AL(a.nbmin, S);
+    AL(a.grid, G); AL(a.desc, C + 1); AL(a.frame, C + 1);   // entry C: never active (freed slots)
+    AL(s->scan_tmp, tm_scan_tmp_words(B + 1)); AL(s->d_octsize, C); AL(s->dK, 1); AL(s->d_flag, 1);
+    {
+        double *scratch = nullptr;
+        AL(scratch, S);
+        s->d_scratch = scratch;
+    }
+    if (cfg->diagnostics) {
+        AL(a.nbhash, S);
+        AL(a.vcand, S);
+    }
+    if (cfg->list_capacity > 0) {
+        AL(a.vlist, S * (long long)cfg->list_capacity);
+        AL(a.vcount, S);
+        AL(a.x0, S);
+    }
+    if (bytes) *bytes = total;
+    return rc;
+}
+
+static void session_extents(const tm_session_config *cfg, long long &S, long long &B, long long &G, int &C)
+{
+    S = ((cfg->max_slots + 31) / 32) * 32;
+    B = cfg->max_bin_entries > 0 ? cfg->max_bin_entries
+                                 : std::max<long long>(1 << 12, 2 * S) + (1ll << (3 * TM_LMAX)) + 2;
+    G = cfg->max_grid_entries > 0 ? cfg->max_grid_entries : 257ll * 257 * 257;
+    C = cfg->max_colonies;
+}
+
+extern "C" int64_t tm_session_bytes(const tm_session_config *cfg, int ntypes)
+{
+    if (!cfg || cfg->max_slots <= 0 || cfg->max_colonies <= 0 || ntypes < 1 || ntypes > TM_MAX_TYPES) return -1;
+    tm_session probe;
+    probe.cfg = *cfg;
+    probe.K.ntypes = ntypes;
+    long long S, B, G, bytes = 0;
+    int C;
+    session_extents(cfg, S, B, G, C);
+    session_buffers(&probe, S, B, G, C, false, &bytes);
+    return (int64_t)bytes;
+}
+
+extern "C" int tm_device_memory(int device, int64_t *free_bytes, int64_t *total_bytes)
+{
+    if (!free_bytes || !total_bytes) return tm_fail(TM_EINVAL, "null argument");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return tm_fail(TM_ENODEV, "no CUDA device");
+    if (device < 0 || device >= ndev) return tm_fail(TM_EINVAL, "device %d out of range", device);
+    CK(cudaSetDevice(device));
+    size_t f = 0, t = 0;
+    CK(cudaMemGetInfo(&f, &t));
+    *free_bytes = (int64_t)f;
+    *total_bytes = (int64_t)t;
+    return TM_OK;
+}
+
 extern "C" int tm_session_create(tm_session **out, const tm_session_config *cfg, const tm_celltypes *types)
 {
     if (!out || !cfg || !types) return tm_fail(TM_EINVAL, "null argument");
@@ -435,11 +533,9 @@ extern "C" int tm_session_create(tm_session **out, const tm_session_config *cfg,
         }
     }
 
-    const long long S = ((cfg->max_slots + 31) / 32) * 32;
-    const long long B = cfg->max_bin_entries > 0 ? cfg->max_bin_entries
-                                                  : std::max<long long>(1 << 12, 2 * S) + (1ll << (3 * TM_LMAX)) + 2;
-    const long long G = cfg->max_grid_entries > 0 ? cfg->max_grid_entries : 257ll * 257 * 257;
-    const int C = cfg->max_colonies;
+    long long S, B, G;
+    int C;
+    session_extents(cfg, S, B, G, C);
     s->slots.init(S / 32);
     s->bins.init(B);
     s->grids.init(G);
@@ -452,31 +548,11 @@ extern "C" int tm_session_create(tm_session **out, const tm_session_config *cfg,
         return tm_fail(TM_ECUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
     }
     tm_arrays &a = s->A;
-#define AL(p, cnt)                                   \
-    if (rc == TM_OK) rc = dalloc(&(p), (cnt));
-    AL(a.x, S) AL(a.y, S) AL(a.z, S) AL(a.size, S) AL(a.young, S) AL(a.ctype, S) AL(a.phase, S) AL(a.perm, S)
-    AL(a.rem, S)
-    AL(a.x2, S) AL(a.y2, S) AL(a.z2, S) AL(a.size2, S) AL(a.young2, S) AL(a.ctype2, S) AL(a.phase2, S)
-    AL(a.perm2, S) AL(a.rem2, S)
-    AL(a.col, S) AL(a.code, S) AL(a.codes, S) AL(a.bin, S) AL(a.tmp, S) AL(a.rank, S) AL(a.hi, S) AL(a.lo, S)
-    AL(a.mass, S * K.ntypes)
+    rc = session_buffers(s, S, B, G, C, true, nullptr);
     s->mass_types = K.ntypes;
-    AL(a.bin_count, B + 1) AL(a.bin_cursor, B + 1) AL(a.bin_start, B + 1) AL(a.bigbins, 2 * (S / 33) + 4)
-    AL(a.fix_count, 4) AL(a.fix_list, S)
     if (rc == TM_OK) a.work = a.fix_count + 1;
-    AL(a.density, S) AL(a.v, S) AL(a.mindist, S) AL(a.fx, S) AL(a.fy, S) AL(a.fz, S) AL(a.nbcount, S) AL(a.nbmin, S)
-    AL(a.grid, G) AL(a.desc, C) AL(a.frame, C)
-    AL(s->scan_tmp, tm_scan_tmp_words(B + 1)) AL(s->d_octsize, C) AL(s->dK, 1) AL(s->d_flag, 1)
-    if (rc == TM_OK) rc = dalloc((double **)&s->d_scratch, S);
-    if (cfg->diagnostics) {
-        AL(a.nbhash, S) AL(a.vcand, S)
-    }
     a.lstride = S;
     a.vcap = cfg->list_capacity > 0 ? cfg->list_capacity : 0;
-    if (a.vcap > 0) {
-        AL(a.vlist, S * (long long)a.vcap) AL(a.vcount, S) AL(a.x0, S)
-    }
-#undef AL
     if (rc == TM_OK) {
         if (cudaMallocHost((void **)&s->h_desc, sizeof(tm_desc) * (size_t)C) != cudaSuccess ||
             cudaMallocHost((void **)&s->h_frame, sizeof(tm_frame) * (size_t)C) != cudaSuccess)
@@ -493,8 +569,8 @@ extern "C" int tm_session_create(tm_session **out, const tm_session_config *cfg,
     memset(s->h_desc, 0, sizeof(tm_desc) * (size_t)C);
     memset(s->h_frame, 0, sizeof(tm_frame) * (size_t)C);
     e = cudaMemcpy(s->dK, &s->K, sizeof(tm_consts), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemset(a.desc, 0, sizeof(tm_desc) * (size_t)C);
-    if (e == cudaSuccess) e = cudaMemset(a.frame, 0, sizeof(tm_frame) * (size_t)C);
+    if (e == cudaSuccess) e = cudaMemset(a.desc, 0, sizeof(tm_desc) * (size_t)(C + 1));
+    if (e == cudaSuccess) e = cudaMemset(a.frame, 0, sizeof(tm_frame) * (size_t)(C + 1));
     if (e != cudaSuccess) {
         tm_session_destroy(s);
         return tm_fail(TM_ECUDA, "session init: %s", cudaGetErrorString(e));
@@ -618,7 +694,9 @@ static int auto_lcap(const tm_session *s, const tm_colony_input *in)
     double hmax = 0.0;
     for (int t = 0; t < s->K.ntypes; t++) hmax = std::max(hmax, s->K.t[t].h);
     double ext = std::max(mx[0] - mn[0], std::max(mx[1] - mn[1], mx[2] - mn[2])) + 2 * (hmax + 0.01);
-    int L = (int)std::floor(std::log2(2.0 * ext / hmax)) + 1;   // one level of headroom for growth
+    // the bin table holds 8^L entries: bins of at least h/2 at the current
+    // extent (a colony that grows later uses coarser bins, see k_frame)
+    int L = (int)std::floor(std::log2(2.0 * ext / hmax));
     return std::max(1, std::min(TM_LMAX, L));
 }
 
@@ -686,9 +764,9 @@ extern "C" int tm_colony_add(tm_session *s, const tm_colony_input *in, const tm_
     {
         double hmax = 0.0;
         for (int t = 0; t < s->K.ntypes; t++) hmax = std::max(hmax, s->K.t[t].h);
-        d.skin = opt->skin > 0.0f ? opt->skin : (float)(0.1 * hmax);
+        d.skin = opt->skin > 0.0f ? opt->skin : (float)(s->tune.skin_over_h * hmax);
     }
-    d.rmax = opt->rmax > 0 ? opt->rmax : 64;
+    d.rmax = opt->rmax > 0 ? opt->rmax : s->tune.rmax;
     for (int k = 0; k < 3; k++) {
         d.glower[k] = glower[k];
         d.gsize[k] = ch.gsize[k];
@@ -733,6 +811,11 @@ extern "C" int tm_colony_remove(tm_session *s, int id)
     s->h_desc[id].n = 0;
     rc = push_desc(s, id);
     if (rc) return rc;
+    // freed slots point at the never-active entry, so no later colony that
+    // reuses this entry sees them as its own
+    k_release_slots<<<blocks_for(c.nslots, 256), 256, 0, s->stream>>>(s->A.col, c.off, c.nslots,
+                                                                       s->cfg.max_colonies);
+    CK(cudaGetLastError());
     CK(cudaStreamSynchronize(s->stream));
     s->slots.release(c.off / 32, c.nslots / 32);
     s->bins.release(c.binoff, c.nbin);
@@ -781,6 +864,85 @@ extern "C" int tm_colony_set_active(tm_session *s, int id, int active)
     rc = push_desc(s, id);
     if (rc) return rc;
     CK(cudaStreamSynchronize(s->stream));
+    drop_graphs(s);
+    return TM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// tuning
+
+__global__ void k_force_rebuild(tm_frame *frame, int ncol)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < ncol) frame[c].force_rebuild = 1;
+}
+
+extern "C" int tm_session_get_tuning(tm_session *s, tm_tuning *t)
+{
+    if (!s || !t) return tm_fail(TM_EINVAL, "null argument");
+    *t = s->tune;
+    return TM_OK;
+}
+
+extern "C" int tm_session_list_rate(tm_session *s, double *rate, int64_t *rebuilds)
+{
+    if (!s || !rate || !rebuilds) return tm_fail(TM_EINVAL, "null argument");
+    CK(cudaSetDevice(s->device));
+    const size_t nc = s->cols.size();
+    if (nc) {
+        CK(cudaMemcpyAsync(s->h_frame, s->A.frame, nc * sizeof(tm_frame), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+    }
+    double num = 0.0, den = 0.0;
+    long long total = 0;
+    for (size_t c = 0; c < nc; c++) {
+        const colony_host &ch = s->cols[c];
+        if (!ch.used) continue;
+        const tm_frame &f = s->h_frame[c];
+        const tm_desc &d = s->h_desc[c];
+        total += (long long)f.rebuilds;
+        if (!ch.active || !d.verlet || ch.n < 2) continue;
+        float md;
+        memcpy(&md, &f.maxdisp, sizeof md);
+        const double grow = 2.0 * (double)md / ((double)f.age + 1.0) / (double)d.skin;
+        num += (double)ch.n * std::max(1.0 / (double)d.rmax, std::min(1.0, grow));
+        den += (double)ch.n;
+    }
+    *rate = den > 0.0 ? num / den : 0.0;
+    *rebuilds = total;
+    return TM_OK;
+}
+
+extern "C" int tm_session_set_tuning(tm_session *s, const tm_tuning *t)
+{
+    if (!s || !t) return tm_fail(TM_EINVAL, "null argument");
+    if (t->pair_lshift < 0 || t->pair_lshift > 1) return tm_fail(TM_EINVAL, "pair_lshift must be 0 or 1");
+    if (t->list_variant < 1 || t->list_variant > 4) return tm_fail(TM_EINVAL, "list_variant must be 1..4");
+    if (t->walk_block != 64 && t->walk_block != 128 && t->walk_block != 256)
+        return tm_fail(TM_EINVAL, "walk_block must be 64, 128 or 256");
+    if (!(t->skin_over_h > 0.0f && t->skin_over_h <= 1.0f)) return tm_fail(TM_EINVAL, "skin_over_h outside (0, 1]");
+    if (t->rmax < 1) return tm_fail(TM_EINVAL, "rmax must be positive");
+    CK(cudaSetDevice(s->device));
+    CK(cudaStreamSynchronize(s->stream));
+    const bool lists_change = t->skin_over_h != s->tune.skin_over_h || t->rmax != s->tune.rmax;
+    s->tune = *t;
+    if (lists_change) {
+        double hmax = 0.0;
+        for (int k = 0; k < s->K.ntypes; k++) hmax = std::max(hmax, s->K.t[k].h);
+        for (size_t c = 0; c < s->cols.size(); c++) {
+            if (!s->cols[c].used) continue;
+            s->h_desc[c].skin = (float)(t->skin_over_h * hmax);
+            s->h_desc[c].rmax = t->rmax;
+            int rc = push_desc(s, (int)c);
+            if (rc) return rc;
+        }
+        if (!s->cols.empty()) {
+            k_force_rebuild<<<blocks_for((long long)s->cols.size(), 128), 128, 0, s->stream>>>(s->A.frame,
+                                                                                            (int)s->cols.size());
+            CK(cudaGetLastError());
+        }
+        CK(cudaStreamSynchronize(s->stream));
+    }
     drop_graphs(s);
     return TM_OK;
 }
@@ -972,6 +1134,9 @@ extern "C" int tm_colony_stats(tm_session *s, int id, tm_colony_info *st)
     st->n = c.n;
     st->list_rebuilds = (int64_t)f.rebuilds;
     st->codes_slow = (int64_t)f.codes_slow;
+    memcpy(&st->list_maxdisp, &f.maxdisp, sizeof(float));   // stored as the float's bits
+    st->list_skin = s->h_desc[id].skin;
+    st->list_age = f.age;
     return TM_OK;
 }
 

@@ -1,0 +1,226 @@
+"""Serving form: a request loop over one device-resident session.
+
+A request is a colony simulation: cells plus a number of steps.  The server
+holds one session whose slot pool is sized at start-up from the device's free
+HBM (``tm_device_memory`` and ``tm_session_bytes``).  Requests queue in
+arrival order and are admitted while the pool has room for their cells (slot
+range, bin table, colony entry); an admitted colony stays resident until its
+last step.  Every engine iteration advances all resident colonies one step in
+the same launches, so a colony admitted now steps alongside colonies that are
+part-way through theirs (continuous batching).  After the step, finished
+colonies are downloaded and removed, which frees room for the queue.
+
+Because a colony's results do not depend on what else is resident (per-colony
+frames, bins, lists; groups aligned to the colony's first slot), a request
+gives the same result alone and in the mix.
+"""
+from __future__ import annotations
+
+import math
+import time
+from collections import deque
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import colonies as C
+
+ENOMEM = -2
+
+
+@dataclass
+class Request:
+    rid: int
+    kind: str
+    n: int
+    steps: int
+    arrival: float                      # seconds after the start (or engine iteration, virtual clock)
+    seed: int = 0
+    colony: C.Colony | None = None      # cells; built on admission when None
+    admitted: float = math.nan
+    finished: float = math.nan
+    result: dict | None = field(default=None, repr=False)
+
+    @property
+    def latency(self) -> float:
+        return self.finished - self.arrival
+
+
+class RequestSource:
+    """Colonies for requests, cut from two pre-generated template colonies.
+
+    A request for n cells of a kind takes n consecutive cells of that kind's
+    template (independent draws, so any n of them are a sample of the same
+    shape) at a seed-chosen offset and shrinks their positions by
+    (n / N_template)^(1/3), which keeps the cell density of a colony drawn
+    directly with n cells.  This keeps the client's cost per request to a few
+    array operations.
+    """
+
+    def __init__(self, n_template: int = 1_000_000, seed: int = 7, types: C.CellTypes | None = None):
+        self.n_template = n_template
+        self.types = types or C.CellTypes.consistent()
+        self.templates = {k: C.make_colony(k, n_template, seed + i, C.initial_radius(k, n_template), types=self.types)
+                          for i, k in enumerate(("uniform", "clustered"))}
+
+    def colony(self, kind: str, n: int, seed: int) -> C.Colony:
+        t = self.templates[kind]
+        n = int(min(n, self.n_template))
+        off = int(np.random.Generator(np.random.PCG64(seed)).integers(0, self.n_template - n + 1))
+        f = (n / self.n_template) ** (1.0 / 3.0)
+        sl = slice(off, off + n)
+        return C.Colony(t.x[sl] * f, t.y[sl] * f, t.z[sl] * f, t.size[sl], t.young[sl], t.ctype[sl], t.phase[sl],
+                        self.types, t.dim, kind, seed, t.radius * f)
+
+
+def poisson_requests(rate: float, duration: float, *, seed: int = 7, lo: int = 1000, hi: int = 1_000_000,
+                     steps=(10, 50, 200)) -> list[Request]:
+    """Arrivals of a Poisson stream over [0, duration): cell counts log-uniform in
+    [lo, hi], uniform or clustered with equal probability, steps uniform over ``steps``."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out, t, rid = [], 0.0, 0
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= duration:
+            break
+        n = int(math.floor(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
+        kind = "clustered" if rng.integers(0, 2) else "uniform"
+        k = int(steps[int(rng.integers(0, len(steps)))])
+        out.append(Request(rid, kind, n, k, t, seed=10_000 + rid))
+        rid += 1
+    return out
+
+
+class Server:
+    """Continuous-batching server over one session (see the module docstring)."""
+
+    def __init__(self, types: C.CellTypes | None = None, *, precision: str = "fp32c", dt: float = 0.01,
+                 hbm_fraction: float = 0.6, max_slots: int | None = None, max_colonies: int = 2048,
+                 list_capacity: int = 384, device: int = 0, graph: bool = True, tuning: dict | None = None,
+                 fields=("x", "y", "z", "density", "fx", "fy", "fz"), keep_results: bool = False):
+        from .session import Session, device_memory, session_bytes
+
+        self.types = types or C.CellTypes.consistent()
+        self.precision, self.dt, self.fields, self.keep = precision, dt, list(fields), keep_results
+        bins_per_slot = 8
+
+        def nbytes(slots):
+            return session_bytes(max_slots=slots, max_colonies=max_colonies, ntypes=self.types.ntypes,
+                                 max_bin_entries=bins_per_slot * slots + (1 << 24), list_capacity=list_capacity)
+
+        free, total = device_memory(device)
+        if max_slots is None:
+            budget = hbm_fraction * free
+            lo, hi = 1 << 15, 1 << 31
+            while hi - lo > 1 << 14:            # largest pool that fits the budget
+                mid = (lo + hi) // 2
+                lo, hi = (mid, hi) if nbytes(mid) <= budget else (lo, mid)
+            max_slots = lo
+        self.max_slots = int(max_slots)
+        self.pool_bytes = nbytes(self.max_slots)
+        self.hbm_free_at_start, self.hbm_total = free, total
+        self.s = Session(self.types, max_slots=self.max_slots, max_colonies=max_colonies, device=device,
+                         max_bin_entries=bins_per_slot * self.max_slots + (1 << 24), list_capacity=list_capacity)
+        if tuning:
+            self.s.set_tuning(**tuning)
+        self.s.use_graph(graph)
+
+    def close(self):
+        self.s.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _admit(self, req: Request, source: RequestSource | None) -> int | None:
+        from .session import TimothyError
+
+        if req.colony is None:
+            req.colony = source.colony(req.kind, req.n, req.seed)
+        try:
+            return self.s.add_colony(req.colony, precision=self.precision, update="dt", dt=self.dt, verlet=True)
+        except TimothyError as e:
+            if e.code == ENOMEM:
+                return None
+            raise
+
+    def run(self, requests: list[Request], *, source: RequestSource | None = None, virtual: bool = False,
+            horizon: float | None = None, log=None) -> dict:
+        """Serve ``requests`` (sorted by arrival).  With ``virtual`` the clock is
+        the engine iteration (deterministic mixes for tests); otherwise wall time
+        in seconds.  With ``horizon`` the run stops at that time, leaving later
+        arrivals and unfinished colonies out."""
+        pending = deque(sorted(requests, key=lambda r: r.arrival))
+        queue: deque[Request] = deque()
+        active: dict[int, list] = {}
+        s = self.s
+        t0 = time.perf_counter()
+        it = 0
+        stepped_cells = 0
+        resident_max = 0
+        clock = (lambda: float(it)) if virtual else (lambda: time.perf_counter() - t0)
+        while pending or queue or active:
+            now = clock()
+            if horizon is not None and now >= horizon:
+                break
+            while pending and pending[0].arrival <= now:
+                queue.append(pending.popleft())
+            while queue:
+                cid = self._admit(queue[0], source)
+                if cid is None:
+                    break
+                req = queue.popleft()
+                req.admitted = clock()
+                active[cid] = [req, req.steps]
+            if not active:
+                if virtual:
+                    it += 1
+                elif pending:
+                    time.sleep(max(0.0, min(pending[0].arrival - clock(), 0.005)))
+                continue
+            resident_max = max(resident_max, sum(r.n for r, _ in active.values()))
+            s.step(1)
+            it += 1
+            stepped_cells += sum(r.n for r, _ in active.values())
+            done = []
+            for cid, entry in active.items():
+                entry[1] -= 1
+                if entry[1] == 0:
+                    done.append(cid)
+            for cid in done:
+                req = active.pop(cid)[0]
+                out = s.download(cid, self.fields)
+                req.finished = clock()
+                req.result = out if self.keep else {"density_sum": float(np.sum(out["density"]))}
+                req.colony = None if not self.keep else req.colony
+                s.remove_colony(cid)
+                if log and len(done):
+                    log(f"t={req.finished:.3f} done rid={req.rid} n={req.n} K={req.steps} lat={req.latency:.3f}")
+        s.sync()
+        wall = clock() if not virtual else time.perf_counter() - t0
+        fin = [r for r in requests if not math.isnan(r.finished)]
+        lat = np.array([r.latency for r in fin]) if fin else np.zeros(0)
+        served = sum(r.n * r.steps for r in fin)
+        return {"requests": len(requests), "finished": len(fin), "wall_s": wall, "iterations": it,
+                "cell_updates_finished": served, "cell_updates_stepped": stepped_cells,
+                "throughput": stepped_cells / wall if wall > 0 else 0.0,
+                "p50": float(np.percentile(lat, 50)) if len(lat) else None,
+                "p99": float(np.percentile(lat, 99)) if len(lat) else None,
+                "max_resident_cells": resident_max, "pool_slots": self.max_slots, "pool_bytes": self.pool_bytes}
+
+
+def run_alone(colony: C.Colony, steps: int, *, precision: str = "fp32c", dt: float = 0.01, list_capacity: int = 384,
+              tuning: dict | None = None, fields=("x", "y", "z", "density", "fx", "fy", "fz"), device: int = 0) -> dict:
+    """The same simulation in a session of its own (the invariance reference)."""
+    from .session import Session
+
+    with Session(colony.types, dim=colony.dim, max_slots=colony.n + 64, device=device,
+                 list_capacity=list_capacity) as s:
+        if tuning:
+            s.set_tuning(**tuning)
+        cid = s.add_colony(colony, precision=precision, update="dt", dt=dt, verlet=True)
+        s.step(steps)
+        s.sync()
+        return s.download(cid, list(fields))

@@ -56,7 +56,13 @@ class _Info(C.Structure):
     _fields_ = [("aff_shift", C.c_double * 3), ("aff_scale", C.c_double), ("octsize", C.c_int64),
                 ("removecount", C.c_int64), ("patch_lower", C.c_int64 * 3), ("patch_upper", C.c_int64 * 3),
                 ("grid_size", C.c_int64 * 3), ("device_errors", C.c_uint32), ("bin_level", C.c_int),
-                ("n", C.c_int64), ("list_rebuilds", C.c_int64), ("codes_slow", C.c_int64)]
+                ("n", C.c_int64), ("list_rebuilds", C.c_int64), ("codes_slow", C.c_int64),
+                ("list_maxdisp", C.c_float), ("list_skin", C.c_float), ("list_age", C.c_int32)]
+
+
+class _Tuning(C.Structure):
+    _fields_ = [("pair_lshift", C.c_int), ("list_variant", C.c_int), ("walk_block", C.c_int),
+                ("skin_over_h", C.c_float), ("rmax", C.c_int)]
 
 
 _lib = None
@@ -92,6 +98,11 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "tm_session_capacity": (C.c_int, [P, P, P, P]),
         "tm_session_timer": (C.c_int, [P, C.c_int, P]),
         "tm_session_launches": (C.c_int64, [P]),
+        "tm_session_list_rate": (C.c_int, [P, P, P]),
+        "tm_session_bytes": (C.c_int64, [C.POINTER(_Config), C.c_int]),
+        "tm_device_memory": (C.c_int, [C.c_int, P, P]),
+        "tm_session_get_tuning": (C.c_int, [P, C.POINTER(_Tuning)]),
+        "tm_session_set_tuning": (C.c_int, [P, C.POINTER(_Tuning)]),
         "tm_host_register": (C.c_int, [P, C.c_int64]),
         "tm_host_unregister": (C.c_int, [P]),
     }
@@ -110,6 +121,25 @@ def _check(rc: int):
 
 def _p(a):
     return None if a is None else a.ctypes.data
+
+
+def session_bytes(*, max_slots: int, max_colonies: int = 1, dim: int = 3, ntypes: int = 1, max_bin_entries: int = 0,
+                  max_grid_entries: int = 0, diagnostics: bool = False, list_capacity: int = 0) -> int:
+    """Device bytes a Session with these arguments allocates."""
+    cfg = _Config(dim, 0, int(max_slots), int(max_colonies), int(max_bin_entries), int(max_grid_entries),
+                  1 if diagnostics else 0, int(list_capacity))
+    b = int(load_library().tm_session_bytes(C.byref(cfg), int(ntypes)))
+    if b < 0:
+        raise ValueError("bad session configuration")
+    return b
+
+
+def device_memory(device: int = 0) -> tuple[int, int]:
+    """(free, total) bytes of a device."""
+    f = np.zeros(1, np.int64)
+    t = np.zeros(1, np.int64)
+    _check(load_library().tm_device_memory(int(device), _p(f), _p(t)))
+    return int(f[0]), int(t[0])
 
 
 def host_register(a: np.ndarray):
@@ -273,7 +303,32 @@ class Session:
                 "removecount": int(info.removecount), "patch_lower": list(info.patch_lower),
                 "patch_upper": list(info.patch_upper), "device_errors": int(info.device_errors),
                 "bin_level": int(info.bin_level), "n": int(info.n), "list_rebuilds": int(info.list_rebuilds),
-                "codes_slow": int(info.codes_slow)}
+                "codes_slow": int(info.codes_slow), "list_maxdisp": float(info.list_maxdisp),
+                "list_skin": float(info.list_skin), "list_age": int(info.list_age)}
+
+    def list_rate(self) -> tuple[float, int]:
+        """(expected fraction of cells rebuilding their lists per step, rebuilds so far)."""
+        r = np.zeros(1, np.float64)
+        n = np.zeros(1, np.int64)
+        _check(load_library().tm_session_list_rate(self._h, _p(r), _p(n)))
+        return float(r[0]), int(n[0])
+
+    # -- tuning -------------------------------------------------------------
+    @property
+    def tuning(self) -> dict:
+        t = _Tuning()
+        _check(load_library().tm_session_get_tuning(self._h, C.byref(t)))
+        return {k: getattr(t, k) for k, _ in _Tuning._fields_}
+
+    def set_tuning(self, **kw):
+        """Change launch shapes / list parameters (see tm_tuning); others keep their values."""
+        cur = self.tuning
+        unknown = set(kw) - set(cur)
+        if unknown:
+            raise ValueError(f"unknown tuning keys {sorted(unknown)}")
+        cur.update(kw)
+        t = _Tuning(**cur)
+        _check(load_library().tm_session_set_tuning(self._h, C.byref(t)))
 
 
 def run_colony(col: Colony, nsteps: int, *, precision: str = "fp64", update: str = "reference", dt: float = 1.0,
