@@ -15,7 +15,12 @@ Workloads (seeded synthetic colonies; the reference ships no datasets):
   uniform10k    10,000 cells uniform in a ball (seed 1), plain FP64 path.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload precision16m|scale1m|uniform10k]
+                  [--workload precision16m|scale1m|uniform10k] [--no-forms]
+
+The line also carries the two other forms ("forms"): the batched form (512
+colonies of 1e3..2e5 cells, autotuned, one step graph per step, FP32+comp and
+FP64) and the serving form (Poisson request streams at the given rates for a
+bounded time; offered and served cell-updates/s, p50/p99 latency).
 Under torchrun each rank runs an independent replica (the path has no
 cross-colony exchange), so scaling is weak and value is the total over ranks.
 """
@@ -165,14 +170,18 @@ def dist_barrier(pg):
         pg.barrier()
 
 
-def cpu_sample(workload, threads=0, seconds_cap=30.0):
-    """Time the CPU implementation of the path on a bounded sample of the workload."""
+def cpu_colony(workload, n_cap=1_000_000):
+    kind, seed = workload["kind"], workload["seed"]
+    n = min(workload["n"], n_cap)
+    return C.make_colony(kind, n, seed, radius_for(kind, n, seed))
+
+
+def cpu_sample(workload, threads=0, col=None):
+    """Time the CPU implementation of the path (the reference compiled here, or
+    the oracle port) for one step on a bounded sample of the workload."""
     from oracle import bindings
 
-    kind = workload["kind"]
-    n = min(workload["n"], 1_000_000 if kind == "clustered" else workload["n"])
-    seed = workload["seed"]
-    col = C.make_colony(kind, n, seed, radius_for(kind, n, seed))
+    col = col if col is not None else cpu_colony(workload)
     which = "ref" if bindings.available("ref") else "oracle"
     try:
         bindings.load(which)
@@ -182,39 +191,96 @@ def cpu_sample(workload, threads=0, seconds_cap=30.0):
         bindings.build(ref=False)
     threads = threads or os.cpu_count() or 1
     steps = 1
-    t0 = time.perf_counter()
     kw = dict(which=which, update_mode=1, dt=workload["dt"], cic=workload["cic"])
     if which == "oracle":
         kw["nthreads"] = threads
     else:
         os.environ["OMP_NUM_THREADS"] = str(threads)
+    t0 = time.perf_counter()
     bindings.run(col, steps, **kw)
     dt = time.perf_counter() - t0
-    return {"value": n * steps / dt, "unit": UNIT, "cores": threads,
+    return {"value": col.n * steps / dt, "unit": UNIT, "cores": threads,
             "kind": "reference" if which == "ref" else "port",
-            "sample": f"{n} cells of the {kind} generator (seed {seed}), {steps} step, {dt:.2f} s"}
+            "sample": f"{col.n} cells of the {col.kind} generator (seed {col.seed}), {steps} step, {dt:.2f} s"}
 
 
-def run_reference_arm(args, workload):
+def run_reference_arm(args, workload, budget_s=150.0):
+    """CPU path of the reference on the host cores, one bounded sample per step;
+    the sample size keeps the whole run near budget_s."""
     world, rank, local, pg = dist_setup()
     if rank != 0:
         return
+    probe = cpu_sample(workload, col=cpu_colony(workload, 100_000))
+    per_step = budget_s / max(1, args.steps + args.warmup)
+    n = int(max(20_000, min(1_000_000, workload["n"], probe["value"] * per_step)))
+    col = cpu_colony(workload, n)
     samples = []
     cb = None
     for _ in range(args.warmup):
-        cpu_sample(workload)
+        cpu_sample(workload, col=col)
     for _ in range(args.steps):
-        cb = cpu_sample(workload)
+        cb = cpu_sample(workload, col=col)
         samples.append(cb["value"])
     value = float(np.mean(samples))
     cb["value"] = value
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": args.workload, **{k: workload[k] for k in ("kind", "n", "seed")}},
+            "warmup": args.warmup, "ms_per_step": col.n / value * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": args.workload, **{k: workload[k] for k in ("kind", "n", "seed")},
+                       "sample_cells": col.n},
             "cpu_baseline": cb, "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                                         "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def batched_form(args, device, log=None):
+    """512 colonies (log-uniform 1e3..2e5 cells, uniform or clustered, seeds
+    1000+i), autotuned, 50 steps per step-graph; FP32+comp, then FP64."""
+    from timothy_gb300 import batch as B
+
+    t0 = time.time()
+    cols = B.make_batch(args.batch_colonies, seed=4)
+    gen_s = time.time() - t0
+    out = {"colonies": len(cols), "cells": int(sum(c.n for c in cols)), "steps": args.batch_steps,
+           "generate_s": gen_s}
+    for prec in ("fp32c", "fp64"):
+        info = B.run_batch(cols, args.batch_steps, precision=prec, warmup=3, tune=True, device=device, log=log)
+        out[prec] = {"value": info["value"], "ms_per_step": info["ms_per_step"], "tuning": info["tuning"],
+                     "tune_s": round(info.get("tune_s", 0.0), 2), "rebuilds": info["rebuilds"],
+                     "gpu_launches_per_step": info["gpu_launches"] / args.batch_steps,
+                     "graph": True}
+    out["fp32c_over_fp64"] = out["fp32c"]["value"] / out["fp64"]["value"]
+    return out
+
+
+def serving_form(args, device, rate, seconds):
+    """Poisson requests (log-uniform 1e3..1e6 cells, uniform or clustered, K in
+    {10, 50, 200}, FP32+comp) for ``seconds``; stops at the horizon."""
+    from timothy_gb300 import serving as SV
+
+    src = SV.RequestSource(n_template=1_000_000, seed=7)
+    reqs = SV.poisson_requests(rate, seconds, seed=7)
+    offered = sum(r.n * r.steps for r in reqs) / seconds
+    with SV.Server(device=device, hbm_fraction=0.5) as srv:
+        st = srv.run(reqs, source=src, horizon=seconds)
+    fin = [r for r in reqs if r.finished == r.finished]
+    unfinished_age = [seconds - r.arrival for r in reqs if r.finished != r.finished]
+    return {"rate_per_s": rate, "seconds": seconds, "requests": len(reqs), "finished": st["finished"],
+            "offered_cell_updates_per_s": offered, "served_cell_updates_per_s": st["throughput"],
+            "p50_s": st["p50"], "p99_s": st["p99"],
+            "p50_by_size": _size_bins(fin),
+            "unfinished_min_age_s": min(unfinished_age) if unfinished_age else None,
+            "max_resident_cells": st["max_resident_cells"], "pool_slots": st["pool_slots"],
+            "pool_gb": st["pool_bytes"] / 1e9}
+
+
+def _size_bins(reqs):
+    out = {}
+    for lo, hi in ((1e3, 1e4), (1e4, 1e5), (1e5, 1e6 + 1)):
+        lat = [r.latency for r in reqs if lo <= r.n < hi]
+        if lat:
+            out[f"{int(lo)}-{int(min(hi, 1e6))}"] = float(np.median(lat))
+    return out
 
 
 def main():
@@ -232,6 +298,11 @@ def main():
                     help="neighbour-list entries per cell (0: search the bins every step)")
     ap.add_argument("--rmax", type=int, default=64, help="rebuild the neighbour lists at least every rmax steps")
     ap.add_argument("--skin", type=float, default=0.1, help="neighbour-list skin as a fraction of h")
+    ap.add_argument("--no-forms", action="store_true", help="skip the batched and serving forms")
+    ap.add_argument("--batch-colonies", type=int, default=512)
+    ap.add_argument("--batch-steps", type=int, default=50)
+    ap.add_argument("--serve-rates", default="200,50", help="request rates (per s) of the serving runs")
+    ap.add_argument("--serve-seconds", type=float, default=20.0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     wl = dict(WORKLOADS[args.workload])
@@ -354,6 +425,12 @@ def main():
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
         cpu = cpu_sample(wl)
+
+    if not args.no_forms and world == 1:
+        forms = {"batched": batched_form(args, local)}
+        forms["serving"] = [serving_form(args, local, float(r), args.serve_seconds)
+                            for r in args.serve_rates.split(",") if r]
+        extra["forms"] = forms
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
