@@ -59,7 +59,8 @@ struct tm_arrays {
     int *fix_list;
     // per step: work[0] colonies that search (or build lists), work[1]
     // colonies whose lists overflowed; lets the pair grid leave at once
-    int *work;
+    int *work;           // work[2], work[3]: cells queued for the octree walk
+    int *walk_list;
     // outputs (Morton order)
     double *density, *v, *mindist, *fx, *fy, *fz;
     int *nbcount;
@@ -88,6 +89,33 @@ struct tm_arrays {
 __device__ __forceinline__ bool tm_live(long long i, const tm_desc &d)
 {
     return (unsigned long long)(i - d.off) < (unsigned long long)d.n;
+}
+
+// Queue cell i for the octree walk, or set its v = 0 when it needs none.
+// Cells with neighbours within h fill the walk list from the front
+// (work[2]), isolated cells -- whose walks visit every candidate -- from the
+// back (work[3]), so warps of the walk hold walks of similar length.
+__device__ __forceinline__ void tm_queue_walk(const tm_arrays &a, long long i, bool isolated, bool walk)
+{
+    if (!walk) a.v[i] = 0.0;
+    const unsigned am = __activemask();
+    const unsigned mf = __ballot_sync(am, walk && !isolated), mb = __ballot_sync(am, walk && isolated);
+    const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    if (mf) {
+        const int leader = __ffs(mf) - 1;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(&a.work[2], __popc(mf));
+        base = __shfl_sync(am, base, leader);
+        if (walk && !isolated) a.walk_list[base + __popc(mf & below)] = (int)i;
+    }
+    if (mb) {
+        const int leader = __ffs(mb) - 1;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(&a.work[3], __popc(mb));
+        base = __shfl_sync(am, base, leader);
+        if (walk && isolated) a.walk_list[a.nslots_total - 1 - (base + __popc(mb & below))] = (int)i;
+    }
 }
 
 // launch shapes chosen per session (tm_tuning)

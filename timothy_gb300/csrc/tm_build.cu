@@ -414,13 +414,6 @@ __global__ void k_copyback(tm_arrays a)
 // 1 + sum_k (leafdepth_k - lcp(k-1, k)) over the Morton-sorted cells, where
 // leafdepth_k = 1 + max(lcp(k-1,k), lcp(k,k+1)) and lcp counts shared levels.
 
-__device__ inline int tm_lcp(uint4 a, uint4 b)
-{
-    uint32_t x = (a.x ^ b.x) | (a.y ^ b.y) | (a.z ^ b.z);
-    if (x == 0) return TM_ROOT_LEVEL;
-    return 28 - (31 - __clz(x));
-}
-
 __global__ void k_octsize(tm_arrays a, unsigned long long *out)
 {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;

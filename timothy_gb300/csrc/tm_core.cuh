@@ -280,3 +280,12 @@ struct kahan {
         s = t;
     }
 };
+
+// levels two lattice codes share (the depth of their deepest common octree
+// node; TM_ROOT_LEVEL when equal)
+__device__ inline int tm_lcp(uint4 a, uint4 b)
+{
+    uint32_t x = (a.x ^ b.x) | (a.y ^ b.y) | (a.z ^ b.z);
+    if (x == 0) return TM_ROOT_LEVEL;
+    return 28 - (31 - __clz(x));
+}

@@ -17,6 +17,8 @@
 #include "tm_arrays.cuh"
 #include "tm_kernels.cuh"
 
+#include <algorithm>
+
 #define WALK_STACK 32
 
 struct walk_frame {
@@ -90,40 +92,27 @@ __device__ float pair_potential32(float dist, float s1, float y1, float s2, floa
     return (2.0f * xc * xc / (5.0f * D)) * sqrtf((s1 * s2) / (s1 + s2)) + area * 0.1f;
 }
 
-__global__ void __launch_bounds__(256) k_octree(tm_arrays a, const tm_consts *K)
+// squared distance of two cells from their split (hi + lo) positions
+__device__ __forceinline__ float dist2_split(const tm_arrays &a, long long p, long long j)
 {
-    long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= a.nslots_total) return;
+    const float4 hp = a.hi[p], lp = a.lo[p], hj = a.hi[j], lj = a.lo[j];
+    const float dx = (hp.x - hj.x) + (lp.x - lj.x), dy = (hp.y - hj.y) + (lp.y - lj.y),
+                dz = (hp.z - hj.z) + (lp.z - lj.z);
+    return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+}
+
+// the walk of one cell p (octlocateregion + the DFS of computepotential)
+__device__ __noinline__ void octree_walk(const tm_arrays &a, const tm_consts *K, long long p)
+{
     const int c = a.col[p];
     const tm_desc &d = a.desc[c];
-    if (!d.active || !tm_live(p, d) || d.n <= 1) return;
     const tm_frame &f = a.frame[c];
-    const int t = a.ctype[p];
-    const tm_type &T = K->t[t];
+    const tm_type &T = K->t[a.ctype[p]];
     const double xp = a.x[p], yp = a.y[p], zp = a.z[p];
     const bool isolated = a.nbcount[p] == 0;
-    // v is potential(p, j*) and j* precedes every within-h neighbour in Morton
-    // order, so v can only be non-zero when j* is the first within-h
-    // neighbour m and m overlaps p (xc > 0, potential.c:63-65); otherwise v = 0
-    // without walking.  The overlap is excluded with a margin in FP32.
-    // slots and Morton positions coincide on rebuild steps; otherwise rank and
-    // tmp translate between them
     const bool ident = f.ident != 0;
     const long long ps = ident ? p : (long long)a.rank[p];   // p's Morton position
     auto slot_of = [&](long long k) -> long long { return ident ? k : (long long)a.tmp[k]; };
-    bool need_walk = isolated || a.want_diag;
-    if (!need_walk) {
-        const long long m = slot_of(a.nbmin[p]);
-        const float4 hp = a.hi[p], lp = a.lo[p], hm = a.hi[m], lm = a.lo[m];
-        const float dx = (hp.x - hm.x) + (lp.x - lm.x), dy = (hp.y - hm.y) + (lp.y - lm.y),
-                    dz = (hp.z - hm.z) + (lp.z - lm.z);
-        const float rs = (hp.w + hm.w) * 1.0001f + 1e-5f;
-        need_walk = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < rs * rs;
-    }
-    if (!need_walk) {
-        a.v[p] = 0.0;
-        return;
-    }
 
     // query box in lattice codes, octree.c:251-263; half-open [bmin, bmax)
     uint32_t bmin[3], bmax[3];
@@ -169,6 +158,26 @@ __global__ void __launch_bounds__(256) k_octree(tm_arrays a, const tm_consts *K)
         }
     }
 
+    // The walk visits candidates in Morton order, and the first within-h
+    // neighbour m is itself a candidate when its leaf meets the box; then no
+    // candidate after position m can be j*, and the walk stops on reaching it.
+    long long mpos = -1;
+    if (!isolated) {
+        const long long m = a.nbmin[p];
+        if (m >= (long long)a0 && m < (long long)a1) {
+            const uint4 cm = codes[m];
+            const int lp = m > d.off ? tm_lcp(codes[m - 1], cm) : 0;
+            const int ln = m + 1 < d.off + d.n ? tm_lcp(cm, codes[m + 1]) : 0;
+            const int dl = 1 + (lp > ln ? lp : ln);         // m's leaf depth
+            const int s = TM_ROOT_LEVEL - dl;
+            const uint32_t len = 1u << s;
+            const uint32_t lx = (cm.x >> s) << s, ly = (cm.y >> s) << s, lz = (cm.z >> s) << s;
+            const bool meets = !(bmax[0] <= lx || bmin[0] >= lx + len || bmax[1] <= ly || bmin[1] >= ly + len ||
+                                 bmax[2] <= lz || bmin[2] >= lz + len);
+            if (meets && dl > dT && m != ps) mpos = m;
+        }
+    }
+
     long long jstar = -1;
     double mind = 1.7976931348623157e308;
     if (a1 > a0 && a1 - a0 >= 2) {
@@ -183,6 +192,11 @@ __global__ void __launch_bounds__(256) k_octree(tm_arrays a, const tm_consts *K)
                 continue;
             }
             const uint32_t k = top.cur;
+            if (mpos >= 0 && (long long)k >= mpos) {
+                jstar = mpos;                   // every later candidate follows m
+                done = true;
+                continue;
+            }
             const uint4 ck = codes[k];
             const int dc = top.depth + 1;
             uint32_t e;
@@ -212,8 +226,13 @@ __global__ void __launch_bounds__(256) k_octree(tm_arrays a, const tm_consts *K)
                     done = true;
                 } else {
                     const long long sk = slot_of(k);
-                    const double dx = sub64(xp, a.x[sk]), dy = sub64(yp, a.y[sk]), dz = sub64(zp, a.z[sk]);
-                    const double dist = __dsqrt_rn(add64(add64(mul64(dx, dx), mul64(dy, dy)), mul64(dz, dz)));
+                    double dist;
+                    if (d.precision == 0) {
+                        const double dx = sub64(xp, a.x[sk]), dy = sub64(yp, a.y[sk]), dz = sub64(zp, a.z[sk]);
+                        dist = __dsqrt_rn(add64(add64(mul64(dx, dx), mul64(dy, dy)), mul64(dz, dz)));
+                    } else {
+                        dist = (double)sqrtf(dist2_split(a, p, sk));   // FP32 path: no FP64 work
+                    }
                     mind = (dist < mind ? dist : mind);
                 }
                 continue;
@@ -234,10 +253,16 @@ __global__ void __launch_bounds__(256) k_octree(tm_arrays a, const tm_consts *K)
             vv = pair_potential64(xp, yp, zp, a.size[p], a.young[p], a.x[jstar], a.y[jstar], a.z[jstar],
                                   a.size[jstar], a.young[jstar], T.h);
         } else {
-            const double dx = sub64(xp, a.x[jstar]), dy = sub64(yp, a.y[jstar]), dz = sub64(zp, a.z[jstar]);
-            const double dist = __dsqrt_rn(add64(add64(mul64(dx, dx), mul64(dy, dy)), mul64(dz, dz)));
-            if (dist <= T.h)
-                vv = (double)pair_potential32((float)dist, (float)a.size[p], a.young[p], (float)a.size[jstar],
+            // distance from the split positions; the cutoff in FP64 only within
+            // 1e-5 h of h
+            const float dist = sqrtf(dist2_split(a, p, jstar));
+            bool in = dist <= T.hf;
+            if (fabsf(dist - T.hf) <= 1.0e-5f * T.hf) {
+                const double dx = sub64(xp, a.x[jstar]), dy = sub64(yp, a.y[jstar]), dz = sub64(zp, a.z[jstar]);
+                in = __dsqrt_rn(add64(add64(mul64(dx, dx), mul64(dy, dy)), mul64(dz, dz))) <= T.h;
+            }
+            if (in)
+                vv = (double)pair_potential32(dist, (float)a.size[p], a.young[p], (float)a.size[jstar],
                                               a.young[jstar]);
         }
     }
@@ -246,11 +271,64 @@ __global__ void __launch_bounds__(256) k_octree(tm_arrays a, const tm_consts *K)
     if (a.want_diag) a.vcand[p] = jstar >= 0 ? a.perm[jstar] : -1;
 }
 
+// Pass 1 over the cells of colonies the list kernel did not evaluate (it
+// does this pass itself).  v is potential(p, j*) and j* precedes every
+// within-h neighbour in Morton order, so v can only be non-zero when j* is
+// the first within-h neighbour m and m overlaps p (xc > 0, potential.c:63-65);
+// otherwise v = 0 without walking (the overlap is excluded with a margin in
+// FP32).  Cells that must walk -- those, isolated cells (mindist comes from
+// the walk) and every cell in diagnostics mode -- are queued, so the walk
+// runs with full warps.
+__global__ void __launch_bounds__(256) k_octree_mark(tm_arrays a)
+{
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (((p >> 5) << 5) >= a.nslots_total) return;
+    const int c = a.col[(p >> 5) << 5];                  // colonies are 32-aligned
+    const tm_desc &d = a.desc[c];
+    if (!d.active || d.n <= 1) return;
+    const tm_frame &f = a.frame[c];
+    if (d.verlet && f.list_ok) return;                   // done by the list kernel
+    if (!tm_live(p, d)) return;
+    const bool isolated = a.nbcount[p] == 0;
+    bool walk = isolated || a.want_diag;
+    if (!walk) {
+        // slots and Morton positions coincide on rebuild steps; otherwise tmp
+        // translates a position to its slot
+        const long long m = f.ident ? (long long)a.nbmin[p] : (long long)a.tmp[a.nbmin[p]];
+        const float4 hp = a.hi[p], lp = a.lo[p], hm = a.hi[m], lm = a.lo[m];
+        const float dx = (hp.x - hm.x) + (lp.x - lm.x), dy = (hp.y - hm.y) + (lp.y - lm.y),
+                    dz = (hp.z - hm.z) + (lp.z - lm.z);
+        const float rs = (hp.w + hm.w) * 1.0001f + 1e-5f;
+        walk = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < rs * rs;
+    }
+    tm_queue_walk(a, p, isolated, walk);
+}
+
+// Pass 2: the walk of every queued cell (grid-stride over both queues)
+__global__ void __launch_bounds__(256) k_octree(tm_arrays a, const tm_consts *K)
+{
+    const int nf = a.work[2], nq = nf + a.work[3];
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nq;
+         q += (long long)gridDim.x * blockDim.x) {
+        const long long p = q < nf ? a.walk_list[q] : a.walk_list[a.nslots_total - 1 - (q - nf)];
+        octree_walk(a, K, p);
+    }
+}
+
 cudaError_t tm_launch_octree(const tm_arrays &a, const tm_consts *K, int block, cudaStream_t st)
 {
     if (block != 64 && block != 256) block = 128;
-    unsigned grid = (unsigned)((a.nslots_total + block - 1) / block);
+    unsigned grid = (unsigned)((a.nslots_total + 255) / 256);
     if (grid == 0) return cudaSuccess;
-    k_octree<<<grid, block, 0, st>>>(a, K);
+    k_octree_mark<<<grid, 256, 0, st>>>(a);
+    // the queue length is known on the device only: a grid of resident size
+    static int sms[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < 64 && !sms[dev]) cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
+    const int nsm = (dev >= 0 && dev < 64 && sms[dev] > 0) ? sms[dev] : 152;
+    const long long cap = (long long)nsm * (2048 / block);
+    const unsigned wgrid = (unsigned)std::min<long long>(cap, (a.nslots_total + block - 1) / block);
+    k_octree<<<wgrid, block, 0, st>>>(a, K);
     return cudaGetLastError();
 }

@@ -580,6 +580,18 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_plist(tm_arrays a, const tm_con
         plist_one<PREC>(a, T, dim, t, i, hi_i, lo_i, j0, h0, l0, acc, cnt_nb, nbmin, hash);
     }
     pair_store<PREC>(a, i, acc, cnt_nb, nbmin, hash, false);
+    // the octree walk's first pass for this cell (see k_octree_mark): walk if
+    // the first within-h neighbour in Morton order may overlap it
+    bool walk = cnt_nb == 0 || a.want_diag;
+    if (!walk) {
+        const long long m = f.ident ? (long long)nbmin : (long long)a.tmp[nbmin];
+        const float4 hm = hi[m], lm = lo[m];
+        const float dx = (hi_i.x - hm.x) + (lo_i.x - lm.x), dy = (hi_i.y - hm.y) + (lo_i.y - lm.y),
+                    dz = (hi_i.z - hm.z) + (lo_i.z - lm.z);
+        const float rs = (hi_i.w + hm.w) * 1.0001f + 1e-5f;
+        walk = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < rs * rs;
+    }
+    tm_queue_walk(a, i, cnt_nb == 0, walk);
     if constexpr (PREC == 1) {
         if (needs_fix64(acc)) {
             // FP64 density over the same list, the cutoff decided in FP64

@@ -285,7 +285,7 @@ static int enqueue_build(tm_session *s, int p, int &nk)
     CK(cudaMemsetAsync(a.bin_count, 0, (size_t)(nbin + 1) * sizeof(uint32_t), st));
     CK(cudaMemsetAsync(a.bin_cursor, 0, (size_t)(nbin + 1) * sizeof(uint32_t), st));
     CK(cudaMemsetAsync(a.bigbins, 0, sizeof(int), st));
-    CK(cudaMemsetAsync(a.fix_count, 0, 3 * sizeof(int), st));   // fix count and the two work counters
+    CK(cudaMemsetAsync(a.fix_count, 0, 5 * sizeof(int), st));   // fix count and the four work counters
     k_step_init<<<blocks_for(ncol, 128), 128, 0, st>>>(a);
     k_bbox<<<blocks_for(nsl, 256), 256, 0, st>>>(a, s->K.ntypes);
     k_frame<<<blocks_for(ncol, 128), 128, 0, st>>>(a, s->dK);
@@ -342,7 +342,7 @@ static int enqueue_compute(tm_session *s, int &nk, bool with_marks)
     }
     if (with_marks) mark(s);
     CK(tm_launch_octree(b, s->dK, s->tune.walk_block, s->stream));
-    nk++;
+    nk += 2;   // mark + walk
     return TM_OK;
 }
 
@@ -429,7 +429,7 @@ static int session_buffers(tm_session *s, long long S, long long B, long long G,
     AL(a.lo, S);
     AL(a.mass, S * s->K.ntypes);
     AL(a.bin_count, B + 1); AL(a.bin_cursor, B + 1); AL(a.bin_start, B + 1); AL(a.bigbins, 2 * (S / 33) + 4);
-    AL(a.fix_count, 4); AL(a.fix_list, S);
+    AL(a.fix_count, 8); AL(a.fix_list, S); AL(a.walk_list, S);
     AL(a.density, S); AL(a.v, S); AL(a.mindist, S); AL(a.fx, S); AL(a.fy, S); AL(a.fz, S); AL(a.nbcount, S);
     AL(a.nbmin, S);
     AL(a.grid, G); AL(a.desc, C + 1); AL(a.frame, C + 1);   // entry C: never active (freed slots)
@@ -588,7 +588,7 @@ extern "C" int tm_session_destroy(tm_session *s)
     tm_arrays &a = s->A;
     void *ptrs[] = {a.x, a.y, a.z, a.size, a.young, a.ctype, a.phase, a.perm, a.rem, a.x2, a.y2, a.z2, a.size2,
                     a.young2, a.ctype2, a.phase2, a.perm2, a.rem2, a.col, a.code, a.codes, a.bin, a.tmp, a.rank, a.hi, a.lo, a.vlist, a.vcount, a.x0,
-                    a.mass, a.bin_count, a.bin_cursor, a.bin_start, a.bigbins, a.fix_count, a.fix_list, a.density, a.v, a.mindist, a.fx,
+                    a.mass, a.bin_count, a.bin_cursor, a.bin_start, a.bigbins, a.fix_count, a.fix_list, a.walk_list, a.density, a.v, a.mindist, a.fx,
                     a.fy, a.fz, a.nbcount, a.nbmin, a.nbhash, a.vcand, a.grid, a.desc, a.frame, s->scan_tmp, s->d_octsize,
                     s->dK, s->d_scratch, s->d_flag};
     for (void *p : ptrs)
