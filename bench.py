@@ -47,6 +47,11 @@ UNIT = "cell-updates/s"
 # writes density, v, mindist, Fx, Fy, Fz, x, y, z (9x8).  The CIC workload adds
 # the phase (4) per cell and one write of the grid per step.
 B_CELL = 112
+# DRAM bytes per cell of one list-pass launch (dram__bytes_read.sum +
+# dram__bytes_write.sum over the cells of the launch), from the ncu capture
+# summarised in profiles/k_plist_fp32_clustered2m.txt; traffic grows with the
+# cell count, so a launch over n cells moves n times this.
+TRAFFIC_PER_CELL = {"k_plist<1>": 375.0}
 # Colony radii giving a mean of 40 neighbours within h = 2.5 (bisected with
 # full-size neighbour counts; the bench reports the measured mean each run).
 RADIUS = {
@@ -163,6 +168,11 @@ def dist_max(pg, value: float) -> float:
     t = torch.tensor([value], dtype=torch.float64, device=dev)
     pg.all_reduce(t, op=pg.ReduceOp.MAX)
     return float(t.item())
+
+
+def aggregate_value(n, world, steps, ms_max):
+    """Whole-job cell-updates/s: every replica's cells over the slowest rank's time."""
+    return n * world * steps / (ms_max * 1e-3)
 
 
 def dist_barrier(pg):
@@ -347,16 +357,20 @@ def main():
     rebuilds = s.stats(cid)["list_rebuilds"] - rb0
     ms_max = dist_max(pg, ms)
     ms_per_step = ms_max / args.steps
-    value = n * world * args.steps / (ms_max * 1e-3)
+    value = aggregate_value(n, world, args.steps, ms_max)
 
     peak, peak_kind = measured_peaks()
-    pair_ms = prof["pair_ms"]
-    achieved = B_CELL * n / (pair_ms * 1e-3) / 1e9 if pair_ms > 0 else None
+    # dominant kernel: the list pass (k_plist), one launch per step
+    list_ms = prof["list_ms"] if prof["list_ms"] > 0 else prof["pair_ms"]
+    achieved = B_CELL * n / (list_ms * 1e-3) / 1e9 if list_ms > 0 else None
+    kname = "k_plist<%d>" % (1 if prec == "fp32c" else 0)
+    traffic = TRAFFIC_PER_CELL.get(kname)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak if achieved else None, "traffic": None, "peak_source": peak_kind,
-                "kernel": "k_pair<%d>" % (1 if prec == "fp32c" else 0),
-                "kernel_ms": pair_ms, "phases_ms": {k: prof[k] for k in ("build_ms", "pair_ms", "octree_ms",
-                                                                          "update_ms", "cic_ms")}}
+                "frac": achieved / peak if achieved else None,
+                "traffic": traffic * n / 1e9 if traffic else None, "traffic_unit": "GB per launch",
+                "peak_source": peak_kind, "kernel": kname, "kernel_ms": list_ms,
+                "phases_ms": {k: prof[k] for k in ("build_ms", "search_ms", "list_ms", "fix_ms", "octree_ms",
+                                                   "update_ms", "cic_ms")}}
     out_fast = s.download(cid, ["x", "y", "z", "density", "fx", "fy", "fz"]) if prec == "fp32c" else None
 
     # end to end through the public API with host buffers: per step the cells go

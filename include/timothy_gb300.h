@@ -176,8 +176,9 @@ int tm_session_sync(tm_session *s);
 int tm_session_use_graph(tm_session *s, int on);
 
 /* Per-phase timing with CUDA events on the session stream: phase 0 build,
- * 1 pair kernel, 2 octree kernel, 3 update, 4 CIC.  ms[k] = mean per step
- * since profiling was switched on. */
+ * 1 search / list-build passes, 2 list passes, 3 overflow searches and the
+ * FP64 density fix-up, 4 octree walk, 5 update, 6 CIC.  ms[k] = mean per
+ * step since profiling was switched on (k < nphase <= 7). */
 int tm_session_profile(tm_session *s, int on);
 int tm_session_profile_read(tm_session *s, double *ms, int nphase, int64_t *steps);
 

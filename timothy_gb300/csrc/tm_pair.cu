@@ -677,27 +677,39 @@ static void launch_plist(const tm_arrays &a, const tm_consts *K, int variant, cu
     }
 }
 
-cudaError_t tm_launch_pair(const tm_arrays &a, const tm_consts *K, int prec, const tm_shapes &sh, cudaStream_t st)
+static unsigned pair_grid(const tm_arrays &a, int prec)
 {
     const long long groups = (a.nslots_total + PAIR_CPW - 1) / PAIR_CPW;
-    const int bt = TM_WARPS_PER_BLOCK * 32;
     const long long need = (groups + TM_WARPS_PER_BLOCK - 1) / TM_WARPS_PER_BLOCK;
-    const unsigned grid = (unsigned)std::min<long long>(need, pair_grid_cap(prec != 0));
+    return (unsigned)std::min<long long>(need, pair_grid_cap(prec != 0));
+}
+
+// search pass (fallback 0: list builds and searches of colonies without lists;
+// fallback 1: searches of colonies whose lists overflowed)
+cudaError_t tm_launch_search(const tm_arrays &a, const tm_consts *K, int prec, const tm_shapes &sh, int fallback,
+                             cudaStream_t st)
+{
+    const unsigned grid = pair_grid(a, prec);
     if (grid == 0) return cudaSuccess;
-    const int ls = sh.pair_lshift;
-    if (prec == 0) {
-        k_pair<0><<<grid, bt, 0, st>>>(a, K, 0, ls);
-        if (a.vcap > 0) {
-            launch_plist<0>(a, K, sh.list_variant, st);
-            k_pair<0><<<grid, bt, 0, st>>>(a, K, 1, ls);
-        }
-    } else {
-        k_pair<1><<<grid, bt, 0, st>>>(a, K, 0, ls);
-        if (a.vcap > 0) {
-            launch_plist<1>(a, K, sh.list_variant, st);
-            k_pair<1><<<grid, bt, 0, st>>>(a, K, 1, ls);
-        }
-        k_density_fix64<<<256, 128, 0, st>>>(a, K);
-    }
+    if (fallback && a.vcap == 0) return cudaSuccess;
+    const int bt = TM_WARPS_PER_BLOCK * 32;
+    if (prec == 0) k_pair<0><<<grid, bt, 0, st>>>(a, K, fallback, sh.pair_lshift);
+    else k_pair<1><<<grid, bt, 0, st>>>(a, K, fallback, sh.pair_lshift);
+    return cudaGetLastError();
+}
+
+// list pass (colonies with valid lists)
+cudaError_t tm_launch_list(const tm_arrays &a, const tm_consts *K, int prec, const tm_shapes &sh, cudaStream_t st)
+{
+    if (a.vcap == 0 || a.nslots_total == 0) return cudaSuccess;
+    if (prec == 0) launch_plist<0>(a, K, sh.list_variant, st);
+    else launch_plist<1>(a, K, sh.list_variant, st);
+    return cudaGetLastError();
+}
+
+// FP64 density of the FP32 cells the search passes flagged
+cudaError_t tm_launch_fix(const tm_arrays &a, const tm_consts *K, cudaStream_t st)
+{
+    k_density_fix64<<<256, 128, 0, st>>>(a, K);
     return cudaGetLastError();
 }

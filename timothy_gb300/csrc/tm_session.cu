@@ -331,14 +331,28 @@ static int enqueue_compute(tm_session *s, int &nk, bool with_marks)
     bool any_cic, any64, any32;
     colony_mix(s, any_cic, any64, any32);
     tm_arrays b = view(s, s->parity);
-    const int lists = b.vcap > 0 ? 2 : 0;   // list kernel + overflow search pass
-    if (any64) {
-        CK(tm_launch_pair(b, s->dK, 0, shapes_of(s), s->stream));
-        nk += 1 + lists;
+    const tm_shapes sh = shapes_of(s);
+    const bool lists = b.vcap > 0;
+    // search / list-build passes, then the list passes, then the searches of
+    // colonies whose lists overflowed and the FP64 density fix-up
+    if (any64) CK(tm_launch_search(b, s->dK, 0, sh, 0, s->stream));
+    if (any32) CK(tm_launch_search(b, s->dK, 1, sh, 0, s->stream));
+    nk += (any64 ? 1 : 0) + (any32 ? 1 : 0);
+    if (with_marks) mark(s);
+    if (lists) {
+        if (any64) CK(tm_launch_list(b, s->dK, 0, sh, s->stream));
+        if (any32) CK(tm_launch_list(b, s->dK, 1, sh, s->stream));
+        nk += (any64 ? 1 : 0) + (any32 ? 1 : 0);
+    }
+    if (with_marks) mark(s);
+    if (lists) {
+        if (any64) CK(tm_launch_search(b, s->dK, 0, sh, 1, s->stream));
+        if (any32) CK(tm_launch_search(b, s->dK, 1, sh, 1, s->stream));
+        nk += (any64 ? 1 : 0) + (any32 ? 1 : 0);
     }
     if (any32) {
-        CK(tm_launch_pair(b, s->dK, 1, shapes_of(s), s->stream));
-        nk += 2 + lists;
+        CK(tm_launch_fix(b, s->dK, s->stream));
+        nk++;
     }
     if (with_marks) mark(s);
     CK(tm_launch_octree(b, s->dK, s->tune.walk_block, s->stream));
@@ -1024,19 +1038,20 @@ extern "C" int tm_session_profile_read(tm_session *s, double *ms, int nphase, in
 {
     if (!s || !ms) return tm_fail(TM_EINVAL, "null argument");
     CK(cudaStreamSynchronize(s->stream));
-    const int per = 6;   // marks per step
-    double acc[5] = {0, 0, 0, 0, 0};
+    const int per = 8;   // marks per step
+    double acc[7] = {0, 0, 0, 0, 0, 0, 0};
     long long nst = (long long)(s->evused / per);
     for (long long k = 0; k < nst; k++) {
-        for (int ph = 0; ph < 5; ph++) {
+        for (int ph = 0; ph < 7; ph++) {
             float t = 0.0f;
             CK(cudaEventElapsedTime(&t, s->evpool[k * per + ph], s->evpool[k * per + ph + 1]));
             acc[ph] += t;
         }
     }
-    // phases in recording order: build, cic, pair, octree, update -> report build, pair, octree, update, cic
-    const double order[5] = {acc[0], acc[2], acc[3], acc[4], acc[1]};
-    for (int k = 0; k < nphase && k < 5; k++) ms[k] = nst ? order[k] / (double)nst : 0.0;
+    // recording order: build, cic, search, list, fallback + fix, octree, update;
+    // reported: build, search, list, fix, octree, update, cic
+    const double order[7] = {acc[0], acc[2], acc[3], acc[4], acc[5], acc[6], acc[1]};
+    for (int k = 0; k < nphase && k < 7; k++) ms[k] = nst ? order[k] / (double)nst : 0.0;
     if (steps) *steps = nst;
     return TM_OK;
 }

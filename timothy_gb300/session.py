@@ -254,11 +254,13 @@ class Session:
         _check(load_library().tm_session_profile(self._h, 1 if on else 0))
 
     def profile_read(self) -> dict:
-        ms = np.zeros(5)
+        ms = np.zeros(7)
         steps = np.zeros(1, np.int64)
-        _check(load_library().tm_session_profile_read(self._h, _p(ms), 5, _p(steps)))
-        return {"build_ms": ms[0], "pair_ms": ms[1], "octree_ms": ms[2], "update_ms": ms[3], "cic_ms": ms[4],
-                "steps": int(steps[0])}
+        _check(load_library().tm_session_profile_read(self._h, _p(ms), 7, _p(steps)))
+        out = {"build_ms": ms[0], "search_ms": ms[1], "list_ms": ms[2], "fix_ms": ms[3], "octree_ms": ms[4],
+               "update_ms": ms[5], "cic_ms": ms[6], "steps": int(steps[0])}
+        out["pair_ms"] = ms[1] + ms[2] + ms[3]
+        return {k: (float(v) if k != "steps" else v) for k, v in out.items()}
 
     def timer_start(self):
         _check(load_library().tm_session_timer(self._h, 0, None))
