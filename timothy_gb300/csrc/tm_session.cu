@@ -119,6 +119,9 @@ struct tm_session {
     unsigned long long *d_octsize = nullptr;
     int *d_flag = nullptr;   // set by the upload kernels on a cell type outside the table
     void *d_scratch = nullptr;
+    void *d_scratch2 = nullptr;              // second download buffer (copies overlap the next gather)
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_ready[2] = {nullptr, nullptr}, ev_copied[2] = {nullptr, nullptr};
     // profiling
     bool prof = false;
     std::vector<cudaEvent_t> evpool;
@@ -132,6 +135,7 @@ struct tm_session {
     long long launches = 0;
     int kernels_per_step = 0;
     int mass_types = 0;   // types the FP64 density-weight array holds
+    int dl_next = 0;      // download buffer the next field uses
     tm_tuning tune{1, 1, 128, 0.1f, 64};
     cudaEvent_t tstart = nullptr, tstop = nullptr;
 };
@@ -452,6 +456,9 @@ static int session_buffers(tm_session *s, long long S, long long B, long long G,
         double *scratch = nullptr;
         AL(scratch, S);
         s->d_scratch = scratch;
+        double *scratch2 = nullptr;
+        AL(scratch2, S);
+        s->d_scratch2 = scratch2;
     }
     if (cfg->diagnostics) {
         AL(a.nbhash, S);
@@ -604,7 +611,7 @@ extern "C" int tm_session_destroy(tm_session *s)
                     a.young2, a.ctype2, a.phase2, a.perm2, a.rem2, a.col, a.code, a.codes, a.bin, a.tmp, a.rank, a.hi, a.lo, a.vlist, a.vcount, a.x0,
                     a.mass, a.bin_count, a.bin_cursor, a.bin_start, a.bigbins, a.fix_count, a.fix_list, a.walk_list, a.density, a.v, a.mindist, a.fx,
                     a.fy, a.fz, a.nbcount, a.nbmin, a.nbhash, a.vcand, a.grid, a.desc, a.frame, s->scan_tmp, s->d_octsize,
-                    s->dK, s->d_scratch, s->d_flag};
+                    s->dK, s->d_scratch, s->d_scratch2, s->d_flag};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (auto ev : s->evpool) cudaEventDestroy(ev);
@@ -612,6 +619,11 @@ extern "C" int tm_session_destroy(tm_session *s)
     if (s->tstop) cudaEventDestroy(s->tstop);
     if (s->h_desc) cudaFreeHost(s->h_desc);
     if (s->h_frame) cudaFreeHost(s->h_frame);
+    for (int k = 0; k < 2; k++) {
+        if (s->ev_ready[k]) cudaEventDestroy(s->ev_ready[k]);
+        if (s->ev_copied[k]) cudaEventDestroy(s->ev_copied[k]);
+    }
+    if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return TM_OK;
@@ -644,6 +656,8 @@ static int grid_geometry(int dim, float gfh, int gsize[3], double lower[3])
 // keep: the colony keeps its cell count, so the cells go to their current
 // slots (k_upload_keep); otherwise slot k takes input cell k and the lists are
 // rebuilt.  Returns TM_EINVAL if a cell type lies outside the table.
+static int download_streams(tm_session *s);
+
 static int copy_cells_in(tm_session *s, const colony_host &c, const tm_colony_input *in, bool keep)
 {
     const tm_arrays a = view(s, s->parity);
@@ -656,13 +670,21 @@ static int copy_cells_in(tm_session *s, const colony_host &c, const tm_colony_in
     float *YG = keep ? a.young2 : a.young;
     int *CT = keep ? a.ctype2 : a.ctype, *PH = keep ? a.phase2 : a.phase;
     if (n) {
+        // two streams, so two copies are in flight at a time
+        int rc = download_streams(s);
+        if (rc) return rc;
+        cudaStream_t st2 = s->copy_stream;
+        CK(cudaEventRecord(s->ev_ready[0], st));
+        CK(cudaStreamWaitEvent(st2, s->ev_ready[0], 0));
         CK(cudaMemcpyAsync(X + o, in->x, n * 8, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(Y + o, in->y, n * 8, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(Y + o, in->y, n * 8, cudaMemcpyHostToDevice, st2));
         CK(cudaMemcpyAsync(Z + o, in->z, n * 8, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(SZ + o, in->size, n * 8, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(SZ + o, in->size, n * 8, cudaMemcpyHostToDevice, st2));
         CK(cudaMemcpyAsync(YG + o, in->young, n * 4, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(CT + o, in->ctype, n * 4, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(CT + o, in->ctype, n * 4, cudaMemcpyHostToDevice, st2));
         if (in->phase) CK(cudaMemcpyAsync(PH + o, in->phase, n * 4, cudaMemcpyHostToDevice, st));
+        CK(cudaEventRecord(s->ev_copied[0], st2));
+        CK(cudaStreamWaitEvent(st, s->ev_copied[0], 0));
     }
     if (keep) {
         k_upload_keep<<<blocks_for((long long)n, 256), 256, 0, st>>>(a, s->dK, cid, o, (int)n, in->phase ? 1 : 0,
@@ -1076,12 +1098,31 @@ template <typename T>
 static int unsort_to_host(tm_session *s, const T *src, const colony_host &c, T *host)
 {
     if (!host || c.n == 0) return TM_OK;
+    // two device buffers: field k is gathered on the session stream into buffer
+    // k % 2 while field k - 1 is copied to the host on the copy stream
+    const int b = s->dl_next;
+    s->dl_next ^= 1;
     const tm_arrays a = view(s, s->parity);
-    T *tmp = (T *)s->d_scratch;
+    T *tmp = (T *)(b ? s->d_scratch2 : s->d_scratch);
+    CK(cudaStreamWaitEvent(s->stream, s->ev_copied[b], 0));     // buffer b is free again
     k_unsort<T><<<blocks_for(c.n, 256), 256, 0, s->stream>>>(src, a.perm, c.off, c.n, tmp);
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(host, tmp, sizeof(T) * (size_t)c.n, cudaMemcpyDeviceToHost, s->stream));
-    CK(cudaStreamSynchronize(s->stream));
+    CK(cudaEventRecord(s->ev_ready[b], s->stream));
+    CK(cudaStreamWaitEvent(s->copy_stream, s->ev_ready[b], 0));
+    CK(cudaMemcpyAsync(host, tmp, sizeof(T) * (size_t)c.n, cudaMemcpyDeviceToHost, s->copy_stream));
+    CK(cudaEventRecord(s->ev_copied[b], s->copy_stream));
+    return TM_OK;
+}
+
+static int download_streams(tm_session *s)
+{
+    if (s->copy_stream) return TM_OK;
+    CK(cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking));
+    for (int k = 0; k < 2; k++) {
+        CK(cudaEventCreateWithFlags(&s->ev_ready[k], cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&s->ev_copied[k], cudaEventDisableTiming));
+        CK(cudaEventRecord(s->ev_copied[k], s->copy_stream));
+    }
     return TM_OK;
 }
 
@@ -1091,7 +1132,7 @@ extern "C" int tm_colony_download(tm_session *s, int id, const tm_colony_output 
     if (rc) return rc;
     if (!out) return tm_fail(TM_EINVAL, "null output");
     CK(cudaSetDevice(s->device));
-    CK(cudaStreamSynchronize(s->stream));
+    if ((rc = download_streams(s))) return rc;
     const colony_host &c = s->cols[id];
     const tm_arrays a = view(s, s->parity);
     if ((rc = unsort_to_host(s, (const double *)a.x, c, out->x))) return rc;
@@ -1109,6 +1150,9 @@ extern "C" int tm_colony_download(tm_session *s, int id, const tm_colony_output 
                                          (unsigned long long *)out->nbhash)))
         return rc;
     if (a.vcand && (rc = unsort_to_host(s, (const int32_t *)a.vcand, c, out->vcand))) return rc;
+    // the caller may read its buffers on return
+    CK(cudaStreamSynchronize(s->stream));
+    CK(cudaStreamSynchronize(s->copy_stream));
     if (out->grid && c.gridoff >= 0)
         CK(cudaMemcpy(out->grid, a.grid + c.gridoff, sizeof(double) * (size_t)c.ngrid, cudaMemcpyDeviceToHost));
     return TM_OK;
