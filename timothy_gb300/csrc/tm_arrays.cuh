@@ -57,8 +57,8 @@ struct tm_arrays {
     int *bigbins;
     int *fix_count;      // cells whose FP32 density is redone in FP64
     int *fix_list;
-    // per step: work[0] colonies that search (or build lists), work[1]
-    // colonies whose lists overflowed; lets the pair grid leave at once
+    // per step: work[0] colonies that search (no lists), work[1] colonies
+    // whose lists overflowed; lets the search grid leave at once
     int *work;           // work[2], work[3]: cells queued for the octree walk
     int *walk_list;
     // outputs (Morton order)

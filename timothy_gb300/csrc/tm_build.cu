@@ -43,7 +43,7 @@ __global__ void k_step_init(tm_arrays a)
     } else {
         f.age++;
     }
-    if (rb && d.active && d.n > 1) atomicAdd(&a.work[0], 1);
+    if (rb && d.active && d.n > 1 && !d.verlet) atomicAdd(&a.work[0], 1);   // colonies the search pass serves
     f.force_rebuild = 0;
     f.maxdisp = 0u;
     for (int k = 0; k < 3; k++) {

@@ -18,6 +18,7 @@ cudaError_t tm_scan_exclusive(const uint32_t *in, uint32_t *out, long long n, ui
 long long tm_scan_tmp_words(long long n);
 cudaError_t tm_launch_search(const tm_arrays &a, const tm_consts *K, int prec, const tm_shapes &sh, int fallback,
                              cudaStream_t st);
+cudaError_t tm_launch_listbuild(const tm_arrays &a, const tm_consts *K, cudaStream_t st);
 cudaError_t tm_launch_list(const tm_arrays &a, const tm_consts *K, int prec, const tm_shapes &sh, cudaStream_t st);
 cudaError_t tm_launch_fix(const tm_arrays &a, const tm_consts *K, cudaStream_t st);
 cudaError_t tm_launch_octree(const tm_arrays &a, const tm_consts *K, int block, cudaStream_t st);

@@ -142,7 +142,8 @@ __device__ __forceinline__ void pair32(const tm_type &T, int dim, float dx, floa
     acc.dens.add(term);
     // one-sigma rounding estimate of this term: W ~ (1-u)^3 amplifies the FP32
     // error of (1 - u) near the cutoff
-    const float ek = term * fmaf(1.0e-7f, __fdividef(1.0f, fmaxf(omu, 1.0e-3f)), 1.2e-7f);
+    // (the constant 1.2e-7 part of the estimate is folded into the threshold)
+    const float ek = __fdividef(term, fmaxf(omu, 1.0e-3f));
     acc.err2 = fmaf(ek, ek, acc.err2);
     const float g = wg * T.cGf * rs;
     acc.fx.add(g * dx);
@@ -151,12 +152,15 @@ __device__ __forceinline__ void pair32(const tm_type &T, int dim, float dx, floa
 }
 
 // write one cell's results (both pair kernels)
-// cells whose estimated relative FP32 density error exceeds 3e-7 (almost
-// only cells whose neighbours all sit near the cutoff) are redone in FP64
+// Cells whose estimated relative FP32 density error exceeds 3e-7 (almost
+// only cells whose neighbours all sit near the cutoff) are redone in FP64.
+// Per term the error is about term * (1e-7 / (1-u) + 1.2e-7); err2 sums
+// (term / (1-u))^2, and (a + b)^2 <= 2a^2 + 2b^2 with sum(term^2) <= rho^2
+// turns the 3e-7 bound into err2 * 1e-14 * 2 + 2.88e-14 rho^2 > 9e-14 rho^2.
 __device__ __forceinline__ bool needs_fix64(const pair_acc<1> &acc)
 {
     const float rho = acc.dens.value();
-    return acc.err2 > 9.0e-14f * rho * rho;
+    return acc.err2 * 2.0e-14f > 6.12e-14f * rho * rho;
 }
 
 // queue: flagged cells go to the FP64 fix-up kernel (otherwise the caller
@@ -200,12 +204,10 @@ __device__ __forceinline__ void pair_group(const tm_arrays &a, const tm_consts *
     if (!d.active || d.precision != PREC || d.n <= 1) return;   // potential.c:89
     const tm_frame &f = a.frame[c];
     if (!f.rebuild) return;                 // the list kernel handles this step
-    // first pass: colonies with lists build them (the list kernel then does
-    // the pair maths), the others search and evaluate here; second pass
-    // (fallback): colonies whose lists overflowed search and evaluate
-    if (fallback && (!d.verlet || f.list_ok)) return;
+    // first pass: colonies without lists; second pass (fallback): colonies
+    // whose lists overflowed
+    if (fallback ? (!d.verlet || f.list_ok) : d.verlet) return;
     if (!tm_live(base, d)) return;      // group beyond the colony's cells
-    const bool build = !fallback && d.verlet;
     const int dim = K->dim;
 
     const int quarter = lane % PAIR_LPC;   // this lane's share of the cell's candidates
@@ -250,11 +252,8 @@ __device__ __forceinline__ void pair_group(const tm_arrays &a, const tm_consts *
     ex += lo_i.x;
     ey += lo_i.y;
     ez += lo_i.z;
-    // conservative test radius (the test uses s only, |e| < 1e-5 here); with
-    // lists it reaches h + skin
-    const float rlist = T.hf + (build ? d.skin : 0.0f);
-    const float hr = rlist * 1.00002f + 1e-4f;
-    int vc = 0;   // this lane's list entries
+    // conservative test radius (the test uses s only, |e| < 1e-5 here)
+    const float hr = T.hf * 1.00002f + 1e-4f;
     const int nside = 1 << Lp;
     const float bs = f.binscale * (1.0f / (float)(1 << ls));
     auto binof = [&](float g, float o, float sh, float eps) {
@@ -311,35 +310,6 @@ __device__ __forceinline__ void pair_group(const tm_arrays &a, const tm_consts *
 
     // test the staged tile [0, fill) and drain; the tile is refilled afterwards
     auto test_tile = [&](int fill, float thr) {
-        if (build) {
-            // list build only: every entry within the conservative radius is
-            // appended to the cell's list (the four lanes of a cell take turns
-            // through the tile and place their hits by a ballot prefix); the
-            // list kernel does the pair maths
-            const int cshift = lane & ~(PAIR_LPC - 1);
-            const unsigned below = (1u << quarter) - 1u;
-#pragma unroll 4
-            for (int t0 = 0; t0 < fill; t0 += PAIR_LPC) {
-                const int tt = t0 + quarter;
-                bool hit = false;
-                int j = 0;
-                if (tt < fill) {
-                    const float4 cc = tA[tt];
-                    const float dx = cc.x - sx, dy = cc.y - sy, dz = cc.z - sz;
-                    const float s = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                    j = __float_as_int(cc.w);
-                    hit = s <= thr && (long long)j != i;
-                }
-                const unsigned cm = (__ballot_sync(FULL, hit) >> cshift) & ((1u << PAIR_LPC) - 1u);
-                if (hit) {
-                    const int slot = vc + __popc(cm & below);
-                    if (slot < a.vcap) a.vlist[(long long)slot * a.lstride + i] = j;
-                }
-                vc += __popc(cm);
-            }
-            __syncwarp();
-            return;
-        }
         for (int tb = 0; tb < fill; tb += 32 * PAIR_LPC) {
             const int te = min(fill, tb + 32 * PAIR_LPC);
 #pragma unroll 8
@@ -472,17 +442,6 @@ __device__ __forceinline__ void pair_group(const tm_arrays &a, const tm_consts *
         nbmin = min(nbmin, __shfl_xor_sync(FULL, nbmin, o));
         hash += __shfl_xor_sync(FULL, hash, o);
     }
-    if (build) {
-        if (live && quarter == 0) {
-            a.vcount[i] = min(vc, a.vcap);
-            a.x0[i] = hi_i;
-        }
-        // an overflowing list cannot serve this step: flag the colony, whose
-        // results the list kernel then leaves to a search pass
-        if (__any_sync(FULL, live && vc > a.vcap) && lane == 0)
-            if (atomicExch(&a.frame[c].list_ok, 0) == 1) atomicAdd(&a.work[1], 1);
-        return;
-    }
     if (!live || quarter != 0) return;
     pair_store<PREC>(a, i, acc, cnt_nb, nbmin, hash);
 }
@@ -516,6 +475,74 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
 // Entries are taken two at a time with both gathers issued before either is
 // used (the walk is bound by the latency of the dependent index -> position
 // loads, not by arithmetic).
+// List build (rebuild steps of colonies with lists): one thread per cell,
+// positions are Morton positions here (the state was just reordered).  The
+// bins covering the cell's box [x - r, x + r] (r = h + skin with a float
+// margin) are visited row by row and every cell in them within r of the cell
+// (double-float distance) is appended to its list; the list kernel then
+// decides the cutoff exactly.  The list order (bins z, y, x, then Morton order
+// inside a bin) depends on the colony's own cells only.
+__global__ void __launch_bounds__(256) k_listbuild(tm_arrays a, const tm_consts *K)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (((i >> 5) << 5) >= a.nslots_total) return;
+    const int c = a.col[(i >> 5) << 5];
+    const tm_desc &d = a.desc[c];
+    if (!d.active || d.n <= 1 || !d.verlet) return;
+    const tm_frame &f = a.frame[c];
+    if (!f.rebuild) return;
+    if (!tm_live(i, d)) return;
+    const tm_type &T = K->t[a.ctype[i]];
+    const float rlist = T.hf + d.skin;
+    const float hr = rlist * 1.00002f + 1e-4f;
+    const float thr = hr * hr;
+    const float4 hi_i = a.hi[i], lo_i = a.lo[i];
+    const int nside = 1 << f.L;
+    const float bs = f.binscale;
+    auto bin_lo = [&](float x, float sh) {
+        const int b = (int)floorf((x - sh - hr) * bs - 0.01f);
+        return b < 0 ? 0 : (b >= nside ? nside - 1 : b);
+    };
+    auto bin_hi = [&](float x, float sh) {
+        const int b = (int)floorf((x - sh + hr) * bs + 0.01f);
+        return b < 0 ? 0 : (b >= nside ? nside - 1 : b);
+    };
+    const int bx0 = bin_lo(hi_i.x, f.shiftf[0]), bx1 = bin_hi(hi_i.x, f.shiftf[0]);
+    const int by0 = bin_lo(hi_i.y, f.shiftf[1]), by1 = bin_hi(hi_i.y, f.shiftf[1]);
+    const int bz0 = bin_lo(hi_i.z, f.shiftf[2]), bz1 = bin_hi(hi_i.z, f.shiftf[2]);
+    const uint32_t *bst = a.bin_start + d.binoff;
+    const long long bbase = f.bin_base;
+    const float4 *__restrict__ hi = a.hi;
+    const float4 *__restrict__ lo = a.lo;
+    const long long ls = a.lstride;
+    int vc = 0;
+    for (int bz = bz0; bz <= bz1; bz++)
+        for (int by = by0; by <= by1; by++) {
+            const uint32_t yz = tm_morton(0u, (uint32_t)by, (uint32_t)bz);
+            for (int bx = bx0; bx <= bx1; bx++) {
+                const uint32_t m = yz | tm_morton((uint32_t)bx, 0u, 0u);
+                const long long j0 = bbase + __ldg(bst + m), j1 = bbase + __ldg(bst + m + 1);
+                for (long long j = j0; j < j1; j++) {
+                    const float4 hj = __ldg(hi + j), lj = __ldg(lo + j);
+                    const float dx = (hj.x - hi_i.x) + (lj.x - lo_i.x);
+                    const float dy = (hj.y - hi_i.y) + (lj.y - lo_i.y);
+                    const float dz = (hj.z - hi_i.z) + (lj.z - lo_i.z);
+                    const float s = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    if (s <= thr && j != i) {
+                        if (vc < a.vcap) a.vlist[(long long)vc * ls + i] = (int)j;
+                        vc++;
+                    }
+                }
+            }
+        }
+    a.vcount[i] = min(vc, a.vcap);
+    a.x0[i] = hi_i;
+    // an overflowing list cannot serve this step: flag the colony, whose
+    // results the fallback search pass then computes
+    if (vc > a.vcap)
+        if (atomicExch(&a.frame[c].list_ok, 0) == 1) atomicAdd(&a.work[1], 1);
+}
+
 template <int PREC>
 __device__ __forceinline__ void plist_one(const tm_arrays &a, const tm_type &T, int dim, int t, long long i,
                                           float4 hi_i, float4 lo_i, int j, float4 hj, float4 lj, pair_acc<PREC> &acc,
@@ -684,8 +711,8 @@ static unsigned pair_grid(const tm_arrays &a, int prec)
     return (unsigned)std::min<long long>(need, pair_grid_cap(prec != 0));
 }
 
-// search pass (fallback 0: list builds and searches of colonies without lists;
-// fallback 1: searches of colonies whose lists overflowed)
+// search pass (fallback 0: searches of colonies without lists; fallback 1:
+// searches of colonies whose lists overflowed)
 cudaError_t tm_launch_search(const tm_arrays &a, const tm_consts *K, int prec, const tm_shapes &sh, int fallback,
                              cudaStream_t st)
 {
@@ -695,6 +722,14 @@ cudaError_t tm_launch_search(const tm_arrays &a, const tm_consts *K, int prec, c
     const int bt = TM_WARPS_PER_BLOCK * 32;
     if (prec == 0) k_pair<0><<<grid, bt, 0, st>>>(a, K, fallback, sh.pair_lshift);
     else k_pair<1><<<grid, bt, 0, st>>>(a, K, fallback, sh.pair_lshift);
+    return cudaGetLastError();
+}
+
+// list build of the colonies that rebuild their lists this step (both precisions)
+cudaError_t tm_launch_listbuild(const tm_arrays &a, const tm_consts *K, cudaStream_t st)
+{
+    if (a.vcap == 0 || a.nslots_total == 0) return cudaSuccess;
+    k_listbuild<<<(unsigned)((a.nslots_total + 255) / 256), 256, 0, st>>>(a, K);
     return cudaGetLastError();
 }
 

@@ -337,11 +337,15 @@ static int enqueue_compute(tm_session *s, int &nk, bool with_marks)
     tm_arrays b = view(s, s->parity);
     const tm_shapes sh = shapes_of(s);
     const bool lists = b.vcap > 0;
-    // search / list-build passes, then the list passes, then the searches of
+    // search and list-build passes, then the list passes, then the searches of
     // colonies whose lists overflowed and the FP64 density fix-up
     if (any64) CK(tm_launch_search(b, s->dK, 0, sh, 0, s->stream));
     if (any32) CK(tm_launch_search(b, s->dK, 1, sh, 0, s->stream));
     nk += (any64 ? 1 : 0) + (any32 ? 1 : 0);
+    if (lists) {
+        CK(tm_launch_listbuild(b, s->dK, s->stream));
+        nk++;
+    }
     if (with_marks) mark(s);
     if (lists) {
         if (any64) CK(tm_launch_list(b, s->dK, 0, sh, s->stream));
