@@ -307,7 +307,8 @@ def main():
     ap.add_argument("--list-capacity", type=int, default=384,
                     help="neighbour-list entries per cell (0: search the bins every step)")
     ap.add_argument("--rmax", type=int, default=64, help="rebuild the neighbour lists at least every rmax steps")
-    ap.add_argument("--skin", type=float, default=0.1, help="neighbour-list skin as a fraction of h")
+    ap.add_argument("--skin", type=float, default=0.1, help="neighbour-list skin as a fraction of h (before tuning)")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (launch shapes, list skin)")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched and serving forms")
     ap.add_argument("--batch-colonies", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=50)
@@ -329,10 +330,25 @@ def main():
     col = C.make_colony(kind, n, seed, radius)
     prec = wl["precision"]
 
+    tuned = {}
+
     def new_session(p):
+        from timothy_gb300 import autotune as AT
+
         s = S.Session(col.types, dim=3, max_slots=n + 64, device=local, list_capacity=args.list_capacity)
-        cid = s.add_colony(col, precision=p, update="dt", dt=wl["dt"], cic=wl["cic"],
-                           verlet=args.list_capacity > 0, skin=args.skin * float(max(col.types.h)), rmax=args.rmax)
+        s.set_tuning(skin_over_h=args.skin, rmax=args.rmax)
+        verlet = args.list_capacity > 0
+
+        def add():
+            return s.add_colony(col, precision=p, update="dt", dt=wl["dt"], cic=wl["cic"], verlet=verlet)
+
+        cid = add()
+        if verlet and not args.no_tune:
+            # launch shapes and list skin for this colony; then a fresh copy of it
+            res = AT.autotune(s)
+            tuned[p] = {"tuning": res["best"], "tune_s": round(res["seconds"], 2)}
+            s.remove_colony(cid)
+            cid = add()
         return s, cid
 
     s, cid = new_session(prec)
@@ -410,13 +426,11 @@ def main():
         s64, c64 = new_session("fp64")
         s64.step(args.warmup)
         s64.sync()
-        k64 = max(2, min(args.steps, 5))
+        # the same timed steps as the compensated path (rebuilds included)
+        k64 = args.steps
         s64.timer_start()
         s64.step(k64)
         ms64 = s64.timer_stop()
-        rest = args.steps - k64
-        if rest > 0:
-            s64.step(rest)
         s64.sync()
         ref = s64.download(c64, ["x", "y", "z", "density", "fx", "fy", "fz"])
         s64.close()
@@ -429,7 +443,7 @@ def main():
         fscale = np.max(np.abs(f64))
         ferr = np.abs(f32 - f64) / fscale
         xerr = np.max([np.max(np.abs(out_fast[k] - ref[k])) for k in ("x", "y", "z")])
-        extra["fp64"] = {"value": v64, "ms_per_step": ms64 / k64, "steps": k64}
+        extra["fp64"] = {"value": v64, "ms_per_step": ms64 / k64, "steps": k64, "tuning": tuned.get("fp64")}
         extra["fp32c_over_fp64"] = value / v64
         extra["error_vs_fp64"] = {
             "steps": args.warmup + args.steps, "density_max_rel": float(drel.max()),
@@ -453,8 +467,8 @@ def main():
             "config": {"workload": args.workload, "kind": kind, "cells": n, "seed": seed, "radius": radius,
                        "h": 2.5, "dt": wl["dt"], "cic": wl["cic"], "precision": prec,
                        "mean_neighbours": mean_nb, "max_neighbours": max_nb,
-                       "neighbour_lists": {"capacity": args.list_capacity, "skin_over_h": args.skin, "rmax": args.rmax,
-                                           "rebuilds_in_timed_steps": rebuilds},
+                       "neighbour_lists": {"capacity": args.list_capacity, "rebuilds_in_timed_steps": rebuilds},
+                       "tuning": tuned.get(prec, {"tuning": None}),
                        "l2": "inputs larger than L2 (state %.1f GB)" % (n * 250 / 1e9),
                        "parallelism": f"replicas x{world}"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk}
