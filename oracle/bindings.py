@@ -53,6 +53,10 @@ def load(which: str = "oracle") -> C.CDLL:
         [_P, _P, _P, _P] + [C.c_int, C.c_float, _P, C.c_int64, _P, _P]
     if which == "oracle":
         argt = argt + [C.c_int]
+        lib.tmo_env2cells.restype = C.c_int
+        lib.tmo_env2cells.argtypes = [C.c_int64, C.c_int, _P, _P, _P, C.c_float, C.c_int, _P, _P, _P]
+        lib.tmo_fieldgradient.restype = C.c_int
+        lib.tmo_fieldgradient.argtypes = [C.c_int, C.c_float, C.c_int, _P, _P, _P]
         lib.tmo_neighbours.restype = C.c_int
         lib.tmo_neighbours.argtypes = [C.c_int64, C.c_int, C.c_int, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
                                        C.c_int]
@@ -61,6 +65,10 @@ def load(which: str = "oracle") -> C.CDLL:
     else:
         lib.ref_sizeof.restype = C.c_int64
         lib.ref_sizeof.argtypes = [C.c_int]
+        lib.ref_env2cells.restype = C.c_int64
+        lib.ref_env2cells.argtypes = [C.c_int64, C.c_int, _P, _P, _P, _P, C.c_float, C.c_int, _P, _P, C.c_int64, _P]
+        lib.ref_fieldgradient.restype = C.c_int64
+        lib.ref_fieldgradient.argtypes = [C.c_int, C.c_float, C.c_int, _P, C.c_int64, _P, _P]
     fn.restype = C.c_int
     fn.argtypes = argt
     _cache[which] = lib
@@ -175,3 +183,52 @@ def neighbours(col, *, lists: bool = False, nthreads: int = 0) -> Neighbours:
 
 def mix64(z: int) -> int:
     return int(load("oracle").tm_mix64(z))
+
+
+def grid_dims(dim: int, gfh: float) -> tuple[int, int, int]:
+    """Size of the one-rank grid (grid.c:37-77) for the given resolution."""
+    g = int((np.float32(2049.0) + np.float32(1.0)) / np.float32(gfh)) + 1
+    return (g, g, g if dim == 3 else 1)
+
+
+def env2cells(col, data: np.ndarray, gradient: np.ndarray, *, gfh: float = 8.0, which: str = "oracle") -> np.ndarray:
+    """Grid -> cell gather (patches_applyenv2cells at one rank).
+
+    data: (nfields, gx, gy, gz) float64; gradient: (nfields, gx, gy, gz, 3).
+    Returns cellenv (nfields, n, 4) = value, gx, gy, gz per field and cell."""
+    lib = load(which)
+    nf = int(data.shape[0])
+    data = np.ascontiguousarray(data, np.float64)
+    gradient = np.ascontiguousarray(gradient, np.float64)
+    out = np.zeros((nf, col.n, 4))
+    x, y, z = (np.ascontiguousarray(a, np.float64) for a in (col.x, col.y, col.z))
+    if which == "oracle":
+        rc = lib.tmo_env2cells(col.n, col.dim, _ptr(x), _ptr(y), _ptr(z), float(gfh), nf, _ptr(data),
+                               _ptr(gradient), _ptr(out))
+    else:
+        ph = np.ascontiguousarray(col.phase, np.int32)
+        rc = lib.ref_env2cells(col.n, col.dim, _ptr(x), _ptr(y), _ptr(z), _ptr(ph), float(gfh), nf, _ptr(data),
+                               _ptr(gradient), int(np.prod(data.shape[1:])), _ptr(out))
+        rc = 0 if rc > 0 else -1
+    if rc:
+        raise RuntimeError(f"env2cells ({which}) failed: {rc}")
+    return out
+
+
+def fieldgradient(data: np.ndarray, *, dim: int = 3, gfh: float = 8.0, which: str = "oracle") -> np.ndarray:
+    """Field gradient (fieldgradient_compute at one rank) of data (nfields, gx, gy, gz);
+    returns (nfields, gx, gy, gz, 3)."""
+    lib = load(which)
+    nf = int(data.shape[0])
+    data = np.ascontiguousarray(data, np.float64)
+    out = np.zeros(data.shape + (3,))
+    dims = np.zeros(3, np.int64)
+    if which == "oracle":
+        rc = lib.tmo_fieldgradient(dim, float(gfh), nf, _ptr(data), _ptr(out), _ptr(dims))
+    else:
+        rc = lib.ref_fieldgradient(dim, float(gfh), nf, _ptr(data), int(np.prod(data.shape[1:])), _ptr(out),
+                                   _ptr(dims))
+        rc = 0 if rc > 0 else -1
+    if rc or tuple(dims) != tuple(data.shape[1:]):
+        raise RuntimeError(f"fieldgradient ({which}) failed: {rc}, grid {tuple(dims)} vs {data.shape[1:]}")
+    return out

@@ -2,7 +2,7 @@
  *
  * Compiled only into oracle/_ref/libtimothy_ref*.so, together with the
  * unmodified reference sources (octree.c, potential.c, cells.c, patches.c,
- * grid.c, utils.c) and the single-rank MPI shim.  It replays the hot part of
+ * grid.c, utils.c, fieldgradient.c) and the single-rank MPI shim.  It replays the hot part of
  * the reference step loop (main.c:67-79, step.c:41-100) on structure-of-arrays
  * inputs and copies the outputs back, so tests and the CPU baseline can call
  * the reference through ctypes.  Nothing in the product links against it.
@@ -18,6 +18,7 @@
 #include "potential.h"
 #include "patches.h"
 #include "grid.h"
+#include "fieldgradient.h"
 
 /* defined in octree.c with external linkage (octree.h:24-27) */
 extern double3dv_t affShift;
@@ -232,4 +233,139 @@ int ref_run(int64_t n, int dim, int ntypes,
     free(si.coords[0]);
     free(si.coords);
     return 0;
+}
+
+/* Grid-to-cell gather (step.c:84-86: patches_env2cellsinit and
+ * patches_env2cellswait, patches.c:380-416, 512-593, 643-657) at one rank:
+ * the patch geometry comes from patches_alloc and the cell-to-grid exchange
+ * that precedes it in the step (step.c:46-47, 58-59).  data holds nfields
+ * fields of the grid (x-major, z fastest), gradient 3 values per node and
+ * field; cellenv receives cellenvdata_t[f][c] = {value, gx, gy, gz}.  Returns
+ * the number of grid nodes per field, or -1 when cap_nodes is too small. */
+int64_t ref_env2cells(int64_t n, int dim, const double *x, const double *y, const double *z, const int *phase,
+                      float gfh, int nfields, const double *data, const double *gradient, int64_t cap_nodes,
+                      double *cellenv)
+{
+    systeminfo_t si;
+    settings_t st;
+    cellsinfo_t ci;
+    grid_t grid;
+    patches_t patches;
+    cellenvdata_t **ce = NULL;
+    environment_t *env;
+    int64_t i, g;
+    int f;
+
+    memset(&si, 0, sizeof(si));
+    memset(&st, 0, sizeof(st));
+    memset(&ci, 0, sizeof(ci));
+    memset(&grid, 0, sizeof(grid));
+    si.rank = 0;
+    si.size = 1;
+    si.nthreads = omp_get_max_threads();
+    si.dim[0] = si.dim[1] = si.dim[2] = 1;
+    si.coords = (int **)malloc(sizeof(int *));
+    si.coords[0] = (int *)calloc(3, sizeof(int));
+    st.dimension = dim;
+    st.numberoffields = nfields;
+    st.gfh = gfh;
+    st.maxlocalcells = n > 0 ? n : 1;
+    st.step = 1;
+
+    allocategrid(si, st, &grid);
+    g = grid.localsize.x * grid.localsize.y * grid.localsize.z;
+    if (g > cap_nodes) return -1;
+
+    ci.dimension = dim;
+    ci.localcount.n = (uint64_t)n;
+    ci.cells = (celldata_t *)calloc((size_t)(n > 0 ? n : 1), sizeof(celldata_t));
+    for (i = 0; i < n; i++) {
+        ci.cells[i].x = x[i];
+        ci.cells[i].y = y[i];
+        ci.cells[i].z = z[i];
+        ci.cells[i].phase = phase ? phase[i] : 1;
+    }
+    env = (environment_t *)calloc((size_t)nfields, sizeof(environment_t));
+    for (f = 0; f < nfields; f++) {
+        env[f].data = (double *)data + (size_t)f * (size_t)g;
+        env[f].gradient = (double *)gradient + (size_t)f * 3 * (size_t)g;
+        env[f].production = (double *)calloc((size_t)g, sizeof(double));
+    }
+
+    patches_alloc(si, st, &patches, &ci, &grid);
+    patches_cells2envinit(si, st, &patches, &ci, &grid);
+    patches_cells2envwait(si, st, &patches, &grid, &env);
+    patches_env2cellsinit(si, st, &patches, &grid, &env);
+    patches_env2cellswait(si, st, &patches, &ci, &grid, &ce);
+    patches_free(&patches);
+
+    for (f = 0; f < nfields; f++) {
+        for (i = 0; i < n; i++) {
+            double *o = cellenv + ((size_t)f * (size_t)n + (size_t)i) * 4;
+            o[0] = ce[f][i].value;
+            o[1] = ce[f][i].gx;
+            o[2] = ce[f][i].gy;
+            o[3] = ce[f][i].gz;
+        }
+        free(ce[f]);
+        free(env[f].production);
+    }
+    free(ce);
+    free(env);
+    free(ci.cells);
+    free(grid.loweridx);
+    free(grid.upperidx);
+    free(grid.lowleftnear);
+    free(grid.uprightfar);
+    free(si.coords[0]);
+    free(si.coords);
+    return g;
+}
+
+/* Field gradient of fieldgradient.c:149-225 (through fieldgradient(),
+ * fieldgradient.c:253-272) at one rank on the grid of the given resolution;
+ * data holds nfields fields, gradient receives 3 values per node and field.
+ * Returns the nodes per field (dims[3] filled), or -1 when cap_nodes is too
+ * small. */
+int64_t ref_fieldgradient(int dim, float gfh, int nfields, const double *data, int64_t cap_nodes, double *gradient,
+                          int64_t *dims)
+{
+    systeminfo_t si;
+    settings_t st;
+    grid_t grid;
+    environment_t *env;
+    int64_t g;
+    int f;
+
+    memset(&si, 0, sizeof(si));
+    memset(&st, 0, sizeof(st));
+    memset(&grid, 0, sizeof(grid));
+    si.rank = 0;
+    si.size = 1;
+    si.dim[0] = si.dim[1] = si.dim[2] = 1;
+    si.coords = (int **)malloc(sizeof(int *));
+    si.coords[0] = (int *)calloc(3, sizeof(int));
+    st.dimension = dim;
+    st.numberoffields = nfields;
+    st.gfh = gfh;
+    allocategrid(si, st, &grid);
+    g = grid.localsize.x * grid.localsize.y * grid.localsize.z;
+    dims[0] = grid.localsize.x;
+    dims[1] = grid.localsize.y;
+    dims[2] = grid.localsize.z;
+    if (g > cap_nodes) return -1;
+    env = (environment_t *)calloc((size_t)nfields, sizeof(environment_t));
+    for (f = 0; f < nfields; f++) {
+        env[f].data = (double *)data + (size_t)f * (size_t)g;
+        env[f].gradient = gradient + (size_t)f * 3 * (size_t)g;
+    }
+    fieldgradient(si, st, &env, &grid);
+    free(env);
+    free(grid.loweridx);
+    free(grid.upperidx);
+    free(grid.lowleftnear);
+    free(grid.uprightfar);
+    free(si.coords[0]);
+    free(si.coords);
+    return g;
 }

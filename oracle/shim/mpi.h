@@ -29,6 +29,7 @@ typedef struct { int MPI_SOURCE, MPI_TAG, MPI_ERROR; } MPI_Status;
 #define MPI_MINLOC 4
 #define MPI_IN_PLACE ((void *)1)
 #define MPI_MAX_PROCESSOR_NAME 256
+#define MPI_PROC_NULL (-2)
 
 int MPI_Allreduce(const void *s, void *r, int n, MPI_Datatype t, MPI_Op op, MPI_Comm c);
 int MPI_Alltoall(const void *s, int sn, MPI_Datatype st, void *r, int rn, MPI_Datatype rt, MPI_Comm c);
@@ -38,4 +39,6 @@ int MPI_Irecv(void *b, int n, MPI_Datatype t, int src, int tag, MPI_Comm c, MPI_
 int MPI_Wait(MPI_Request *q, MPI_Status *st);
 int MPI_Abort(MPI_Comm c, int code);
 int MPI_Get_processor_name(char *name, int *len);
+/* one rank on a non-periodic grid: every neighbour is MPI_PROC_NULL */
+int MPI_Cart_shift(MPI_Comm c, int dir, int disp, int *src, int *dst);
 #endif

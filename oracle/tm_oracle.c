@@ -7,6 +7,7 @@
  *   - pair density + potential                potential.c:39-78, inline.h:40-51
  *   - pair force (SPH kernel gradient)        inline.h:59-83, potential.c:193-202
  *   - position update + removal marks         cells.c:41-58, 342-365
+ *   - grid -> cell gather, field gradient     patches.c:512-593, fieldgradient.c:149-225
  *   - CIC deposit at one rank                 grid.c:37-136, patches.c:47-234,
  *                                             patches.c:321-367
  * Expressions keep the reference's evaluation order (C left-to-right
@@ -453,6 +454,103 @@ static int tmo_cic(int64_t n, int dim, const tmo_grid *g, const double *x, const
                 grid[gi] += patch[ps[2] * ps[1] * (i - plo[0]) + ps[2] * (j - plo[1]) + (k - plo[2])];
             }
     free(patch);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* grid -> cell gather and field gradient at one rank                         */
+/* ------------------------------------------------------------------------ */
+
+/* patches_applyenv2cells, patches.c:512-593, at one rank: the patch holds
+ * every grid node a local cell touches, so each cell gathers its in-grid
+ * corners directly from the grid, in the corner order ax, ay, az and with the
+ * product buff * wx * wy * wz of the reference; field values first, then the
+ * three gradient components of the same corners. */
+int tmo_env2cells(int64_t n, int dim, const double *x, const double *y, const double *z, float gfh, int nfields,
+                  const double *data, const double *gradient, double *cellenv)
+{
+    tmo_grid g;
+    if (n < 0 || nfields < 0 || (dim != 2 && dim != 3) || !(gfh > 0.0f)) return -1;
+    tmo_grid_geometry(dim, gfh, &g);
+    const int64_t up[3] = {g.size[0] - 1, g.size[1] - 1, (dim == 3 ? g.size[2] - 1 : 0)};
+    const int64_t G = g.size[0] * g.size[1] * g.size[2];
+#pragma omp parallel for schedule(static)
+    for (int64_t c = 0; c < n; c++) {
+        const double pos[3] = {x[c], y[c], z[c]};
+        int64_t ci[3];
+        double d[3], t[3];
+        for (int k = 0; k < 3; k++) {
+            ci[k] = (int64_t)((pos[k] - g.lower[k]) / g.res);
+            /* grid->lowercorner + cellIdx * resolution: int64 * float is a float product */
+            const double cic = g.lower[k] + (float)ci[k] * g.res;
+            d[k] = (pos[k] - cic) / g.res;
+            t[k] = 1.0 - d[k];
+        }
+        for (int f = 0; f < nfields; f++) {
+            double *o = cellenv + ((size_t)f * (size_t)n + (size_t)c) * 4;
+            o[0] = o[1] = o[2] = o[3] = 0.0;
+        }
+        for (int ax = 0; ax < 2; ax++)
+            for (int ay = 0; ay < 2; ay++)
+                for (int az = 0; az < 2; az++) {
+                    const int64_t a[3] = {ci[0] + ax, ci[1] + ay, ci[2] + az};
+                    if (!(a[0] >= 0 && a[1] >= 0 && a[2] >= 0 && a[0] <= up[0] && a[1] <= up[1] && a[2] <= up[2]))
+                        continue;
+                    const int64_t node = g.size[1] * g.size[2] * a[0] + g.size[2] * a[1] + a[2];
+                    const double wx = ax * d[0] + (1 - ax) * t[0];
+                    const double wy = ay * d[1] + (1 - ay) * t[1];
+                    const double wz = az * d[2] + (1 - az) * t[2];
+                    for (int f = 0; f < nfields; f++) {
+                        double *o = cellenv + ((size_t)f * (size_t)n + (size_t)c) * 4;
+                        o[0] += data[(size_t)f * G + node] * wx * wy * wz;
+                    }
+                    for (int f = 0; f < nfields; f++) {
+                        double *o = cellenv + ((size_t)f * (size_t)n + (size_t)c) * 4;
+                        const double *gr = gradient + ((size_t)f * G + node) * 3;
+                        o[1] += gr[0] * wx * wy * wz;
+                        o[2] += gr[1] * wx * wy * wz;
+                        o[3] += gr[2] * wx * wy * wz;
+                    }
+                }
+    }
+    return 0;
+}
+
+/* fieldgradient_compute, fieldgradient.c:149-225, with no neighbouring rank:
+ * inside, (data[i+1] - data[i-1]) / resolution (no factor 1/2); on each face
+ * the one-sided (data[1] - data[0]) / resolution and
+ * (data[n-1] - data[n-2]) / resolution.  An axis of one node (the z axis of a
+ * 2-D grid) gets 0: there the reference reads the neighbouring row and, at
+ * the first node, one element before the array. */
+int tmo_fieldgradient(int dim, float gfh, int nfields, const double *data, double *gradient, int64_t *dims)
+{
+    tmo_grid g;
+    if (nfields < 0 || (dim != 2 && dim != 3) || !(gfh > 0.0f)) return -1;
+    tmo_grid_geometry(dim, gfh, &g);
+    const int64_t nx = g.size[0], ny = g.size[1], nz = g.size[2], G = nx * ny * nz;
+    const double res = (double)g.res;
+    dims[0] = nx;
+    dims[1] = ny;
+    dims[2] = nz;
+    for (int f = 0; f < nfields; f++) {
+        const double *u = data + (size_t)f * G;
+        double *gr = gradient + (size_t)f * 3 * G;
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < nx; i++)
+            for (int64_t j = 0; j < ny; j++)
+                for (int64_t k = 0; k < nz; k++) {
+                    const int64_t o = ny * nz * i + nz * j + k;
+                    const int64_t n3[3] = {nx, ny, nz}, ix[3] = {i, j, k}, st[3] = {ny * nz, nz, 1};
+                    for (int c = 0; c < 3; c++) {
+                        double v;
+                        if (n3[c] < 2) v = 0.0;
+                        else if (ix[c] == 0) v = (u[o + st[c]] - u[o]) / res;
+                        else if (ix[c] == n3[c] - 1) v = (u[o] - u[o - st[c]]) / res;
+                        else v = (u[o + st[c]] - u[o - st[c]]) / res;
+                        gr[3 * o + c] = v;
+                    }
+                }
+    }
     return 0;
 }
 

@@ -65,6 +65,17 @@ int tmo_neighbours(int64_t n, int dim, int ntypes, const double *th,
                    int32_t *nbcount, uint64_t *nbhash, int64_t *vcand, int32_t *ncand,
                    int64_t *nb_offsets, int64_t *nb_list, int nthreads);
 
+/* Grid -> cell gather at one rank (patches_applyenv2cells): data holds
+ * nfields fields of the one-rank grid of resolution gfh (x-major, z
+ * fastest), gradient 3 values per node and field; cellenv[(f*n + c)*4 + k]
+ * receives cellenvdata_t {value, gx, gy, gz}.  Returns 0 or -1. */
+int tmo_env2cells(int64_t n, int dim, const double *x, const double *y, const double *z, float gfh, int nfields,
+                  const double *data, const double *gradient, double *cellenv);
+
+/* Field gradient (fieldgradient_compute at one rank) of nfields fields on
+ * the one-rank grid of resolution gfh; dims receives the grid size. */
+int tmo_fieldgradient(int dim, float gfh, int nfields, const double *data, double *gradient, int64_t *dims);
+
 /* The fingerprint mixer shared with the GPU diagnostics (SplitMix64 final mix). */
 uint64_t tm_mix64(uint64_t z);
 

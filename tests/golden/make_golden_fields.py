@@ -1,0 +1,76 @@
+"""Golden fixtures of the grid -> cell gather (patches_applyenv2cells) and the
+field gradient (fieldgradient_compute), from the reference's own functions
+compiled unmodified into oracle/_ref (``make -C oracle ref``).
+
+The fields come from tests/golden/fields.py (deterministic formulas), so only
+cells and outputs are stored; the gradient fixtures keep a seeded sample of
+nodes (always including the faces) plus per-component sums.
+
+    python tests/golden/make_golden_fields.py
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, HERE)
+
+from fields import field, gradient_field  # noqa: E402
+from oracle import bindings as B  # noqa: E402
+from timothy_gb300 import colonies as C  # noqa: E402
+
+
+def sample_nodes(dims, count, seed):
+    gx, gy, gz = dims
+    rng = np.random.Generator(np.random.PCG64(seed))
+    idx = [rng.integers(0, gx, count), rng.integers(0, gy, count), rng.integers(0, gz, count)]
+    faces = []
+    for a in (0, gx - 1):
+        for b in (0, gy - 1):
+            for c in (0, gz - 1):
+                faces.append((a, b, c))
+    for a in range(0, gx, max(1, gx // 16)):
+        faces += [(a, 0, gz // 2), (a, gy - 1, gz // 2), (a, gy // 2, 0), (a, gy // 2, gz - 1)]
+    f = np.array(faces, np.int64).T
+    return tuple(np.concatenate([idx[k], f[k]]) for k in range(3))
+
+
+def main():
+    if not (B.available("ref") and B.available("ref_strict")):
+        raise SystemExit("build the reference first: make -C oracle ref")
+    env_cases = [
+        ("field_env_clustered4k", C.make_colony("clustered", 4000, 2, C.initial_radius("clustered", 4000)), 8.0, 2),
+        ("field_env_uniform2d", C.make_colony("uniform", 2000, 3, C.initial_radius("uniform", 2000, dim=2), dim=2),
+         8.0, 1),
+        ("field_env_coarse", C.make_colony("uniform", 3000, 4, C.initial_radius("uniform", 3000)), 32.0, 3),
+    ]
+    for name, col, gfh, nf in env_cases:
+        dims = B.grid_dims(col.dim, gfh)
+        data, grad = field(nf, dims), gradient_field(nf, dims)
+        rec = {"x": col.x, "y": col.y, "z": col.z, "phase": col.phase, "dim": col.dim, "gfh": gfh, "nfields": nf}
+        for w, tag in (("ref_strict", "strict"), ("ref", "fast")):
+            rec[f"{tag}_cellenv"] = B.env2cells(col, data, grad, gfh=gfh, which=w)
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **rec)
+        print(name, col.n, dims)
+    for name, dim, gfh, nf in (("field_grad_gfh32", 3, 32.0, 2), ("field_grad_gfh8", 3, 8.0, 1),
+                               ("field_grad_2d_gfh8", 2, 8.0, 1)):
+        dims = B.grid_dims(dim, gfh)
+        data = field(nf, dims)
+        idx = sample_nodes(dims, 20000, 11)
+        rec = {"dim": dim, "gfh": gfh, "nfields": nf, "dims": np.array(dims), "ix": idx[0], "iy": idx[1],
+               "iz": idx[2]}
+        for w, tag in (("ref_strict", "strict"), ("ref", "fast")):
+            g = B.fieldgradient(data, dim=dim, gfh=gfh, which=w)
+            rec[f"{tag}_sample"] = g[:, idx[0], idx[1], idx[2], :]
+            rec[f"{tag}_sums"] = g.reshape(nf, -1, 3).sum(axis=1)
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **rec)
+        print(name, dims)
+
+
+if __name__ == "__main__":
+    main()

@@ -13,7 +13,8 @@ import pytest
 from timothy_gb300 import colonies as C
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+CASES = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
+               if not os.path.basename(p).startswith("field_"))
 
 
 def load_case(name):
@@ -66,3 +67,49 @@ def test_oracle_within_fast_math_spread(oracle_lib, name):
         ref = d[f"fast_{k}"]
         rel = np.abs(getattr(r, k) - ref) / np.maximum(np.abs(ref), 1e-300)
         assert np.max(rel, initial=0.0) <= 1e-9, k
+
+
+# -- grid -> cell gather and field gradient ----------------------------------
+
+def _field_colony(rec):
+    from timothy_gb300 import colonies as C
+
+    n = len(rec["x"])
+    return C.Colony(rec["x"], rec["y"], rec["z"], np.full(n, 0.9), np.full(n, 2100.0, np.float32),
+                    np.zeros(n, np.int32), rec["phase"], C.CellTypes.consistent(), int(rec["dim"]))
+
+
+@pytest.mark.parametrize("name", ["field_env_clustered4k", "field_env_uniform2d", "field_env_coarse"])
+def test_oracle_env2cells_matches_reference(oracle_lib, name):
+    import sys
+
+    sys.path.insert(0, GOLDEN)
+    from fields import field, gradient_field
+
+    rec = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    col = _field_colony(rec)
+    gfh, nf = float(rec["gfh"]), int(rec["nfields"])
+    dims = oracle_lib.grid_dims(col.dim, gfh)
+    out = oracle_lib.env2cells(col, field(nf, dims), gradient_field(nf, dims), gfh=gfh, which="oracle")
+    assert np.array_equal(out, rec["strict_cellenv"])
+    scale = np.max(np.abs(rec["fast_cellenv"]))
+    assert np.max(np.abs(out - rec["fast_cellenv"])) <= 1e-13 * scale
+
+
+@pytest.mark.parametrize("name", ["field_grad_gfh32", "field_grad_gfh8", "field_grad_2d_gfh8"])
+def test_oracle_fieldgradient_matches_reference(oracle_lib, name):
+    import sys
+
+    sys.path.insert(0, GOLDEN)
+    from fields import field
+
+    rec = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    dim, gfh, nf = int(rec["dim"]), float(rec["gfh"]), int(rec["nfields"])
+    g = oracle_lib.fieldgradient(field(nf, tuple(rec["dims"])), dim=dim, gfh=gfh, which="oracle")
+    comps = 3 if dim == 3 else 2          # a 2-D grid's z gradient reads outside the array in the reference
+    sample = g[:, rec["ix"], rec["iy"], rec["iz"], :comps]
+    for tag in ("strict", "fast"):
+        assert np.array_equal(sample, rec[f"{tag}_sample"][..., :comps]), tag
+        assert np.array_equal(g.reshape(nf, -1, 3).sum(axis=1)[:, :comps], rec[f"{tag}_sums"][:, :comps]), tag
+    if dim == 2:
+        assert not np.any(g[..., 2])
