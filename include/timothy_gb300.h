@@ -194,6 +194,28 @@ int64_t tm_session_launches(tm_session *s);
 int tm_host_register(void *ptr, int64_t bytes);
 int tm_host_unregister(void *ptr);
 
+/* Grid -> cell gather: patches_applyenv2cells (patches.c:512-593) at one
+ * rank, on device arrays.  data holds nfields fields of the grid (gsize[0] x
+ * gsize[1] x gsize[2] nodes, x-major, z fastest; gsize[2] = 1 in 2-D),
+ * gradient three values per node and field (fieldgradient.c layout);
+ * cellenv receives, per field f and cell c, cellenvdata_t {value, gx, gy, gz}
+ * at cellenv[(f*n + c)*4].  Corners outside the grid are skipped as in the
+ * reference; results match its FP64 roundings bit for bit. */
+int tm_env2cells(const double *x, const double *y, const double *z, int64_t n, int dimension,
+                 const double lower[3], float resolution, const int64_t gsize[3], int nfields,
+                 const double *data, const double *gradient, double *cellenv, void *stream);
+/* Field gradient: fieldgradient_compute (fieldgradient.c:149-225) at one rank
+ * on device arrays: central differences (u[i+1] - u[i-1]) / resolution inside,
+ * one-sided differences on the faces, 0 along an axis of one node. */
+int tm_field_gradient(const double *data, const int64_t gsize[3], float resolution, int nfields,
+                      double *gradient, void *stream);
+/* The gather for the cells of a session colony, written to host memory in
+ * the caller's cell order (cellenv as above, n = the colony's cells); data
+ * and gradient are device arrays of the grid described by lower, resolution
+ * and gsize. */
+int tm_colony_env2cells(tm_session *s, int id, const double lower[3], float resolution, const int64_t gsize[3],
+                        int nfields, const double *data, const double *gradient, double *cellenv);
+
 /* No counterpart in the reference.  CIC deposit of n cells onto field 0 of a
  * grid, the work of patches_alloc + patches_cells2envinfo at one rank, for
  * callers that cannot allocate device memory: code running while a CUDA

@@ -226,6 +226,25 @@ typedef struct patches_t {              /* global.h:337-352 */
     double **buff;
 } patches_t;
 
+typedef struct cellenvdata_t {          /* global.h:122-127 */
+    double value;
+    double gx;
+    double gy;
+    double gz;
+} cellenvdata_t;
+
+typedef struct environment_t {          /* global.h:354-364 */
+    char name[128];
+    double diffusioncoefficient;
+    double boundarycondition;
+    double initialconditionmean;
+    double initialconditionvariance;
+    double lambdadelay;
+    double *data;
+    double *gradient;
+    double *production;
+} environment_t;
+
 #endif /* TM_USE_REFERENCE_GLOBAL_H */
 
 /* affine map of the last octbuild (octree.h:24-25) */
@@ -258,6 +277,14 @@ void patches_alloc(systeminfo_t systeminfo, settings_t settings, patches_t *patc
 /* patches.c:156 -- CIC deposit of the cells into field 0 of the patch */
 void patches_cells2envinfo(systeminfo_t systeminfo, settings_t settings, patches_t *patches,
                            cellsinfo_t *cellsinfo, grid_t *grid);
+
+/* patches.c:512 -- grid -> cell gather of every field and its gradient from
+ * the received patch (patches->buff[0]) into freshly allocated
+ * (*cellenvdata)[f][c]; frees the patch buffers as the reference does */
+void patches_applyenv2cells(systeminfo_t systeminfo, settings_t settings, patches_t *patches,
+                            cellsinfo_t *cellsinfo, grid_t *grid, cellenvdata_t ***cellenvdata);
+/* fieldgradient.c:253 -- gradient of every field (one rank) */
+void fieldgradient(systeminfo_t systeminfo, settings_t settings, environment_t **environment, grid_t *grid);
 
 /* Releases the device session the drop-ins keep between calls (no
  * counterpart in the reference; optional at exit). */

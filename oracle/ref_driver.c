@@ -56,6 +56,7 @@ int64_t ref_sizeof(int which)
     case 7: return sizeof(patches_t);
     case 8: return sizeof(octnode_t);
     case 9: return sizeof(environment_t);
+    case 10: return sizeof(cellenvdata_t);
     default: return -1;
     }
 }

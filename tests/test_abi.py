@@ -70,13 +70,15 @@ def test_header_layout_compiles_to_reference_sizes(tmp_path):
 
     src = tmp_path / "sz.c"
     src.write_text('#include <stdio.h>\n#include "timothy_refabi.h"\nint main(void){printf("%zu %zu %zu %zu %zu '
-                   '%zu %zu %zu %zu\\n", sizeof(celldata_t), sizeof(cellsinfo_t), sizeof(celltype_t), '
+                   '%zu %zu %zu %zu %zu %zu\\n", sizeof(celldata_t), sizeof(cellsinfo_t), sizeof(celltype_t), '
                    'sizeof(systeminfo_t), sizeof(settings_t), sizeof(cellcommdata_t), sizeof(grid_t), '
-                   'sizeof(patches_t), sizeof(octnode_t));return 0;}\n')
+                   'sizeof(patches_t), sizeof(octnode_t), sizeof(environment_t), sizeof(cellenvdata_t));'
+                   'return 0;}\n')
     exe = tmp_path / "sz"
     subprocess.run(["gcc", "-I", INCLUDE, str(src), "-o", str(exe)], check=True)
     got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
     assert got[:6] == [112, 192, 368, 56, 336, 104]
+    assert got[9:] == [192, 32]
     from oracle import bindings
 
     if bindings.available("ref"):
@@ -84,5 +86,5 @@ def test_header_layout_compiles_to_reference_sizes(tmp_path):
             lib = bindings.load("ref")
         except OSError:
             return
-        ref = [lib.ref_sizeof(k) for k in (0, 1, 2, 3, 4, 5, 6, 7, 8)]
+        ref = [lib.ref_sizeof(k) for k in range(11)]
         assert got == ref

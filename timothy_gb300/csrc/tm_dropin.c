@@ -8,6 +8,9 @@
  *   computepotential    pair kernel + octree walk; density/v/mindist -> host AoS
  *   computegradient     forces (from the same fused pass) -> host
  *   updatepositions     host forces -> device, x += F, positions + marks -> host
+ *   patches_applyenv2cells  received patch -> device, gather of every field and
+ *                       its gradient for the cells -> host cellenvdata
+ *   fieldgradient       each field -> device, gradient -> host
  * The drop-ins assume, as the reference step loop guarantees, that the cells'
  * positions are not changed by the host between octbuild and updatepositions.
  */
@@ -272,6 +275,54 @@ void patches_cells2envinfo(systeminfo_t systeminfo, settings_t settings, patches
     int64_t lo[3] = {patches->lowercorner[0].x, patches->lowercorner[0].y, patches->lowercorner[0].z};
     int64_t hi[3] = {patches->uppercorner[0].x, patches->uppercorner[0].y, patches->uppercorner[0].z};
     if (settings.numberoffields > 0) TRY("patch", tmi_read_patch(g_sess, g_cid, lo, hi, patches->data[0]));
+}
+
+void patches_applyenv2cells(systeminfo_t systeminfo, settings_t settings, patches_t *patches,
+                            cellsinfo_t *cellsinfo, grid_t *grid, cellenvdata_t ***cellenvdata)
+{
+    g_si = systeminfo;
+    const int nf = settings.numberoffields;
+    const int64_t n = (int64_t)cellsinfo->localcount.n;
+    int f, p;
+    /* zeroed per-field arrays, patches.c:522-534 */
+    *cellenvdata = (cellenvdata_t **)calloc((size_t)(nf > 0 ? nf : 1), sizeof(cellenvdata_t *));
+    if (!*cellenvdata) die("cellenvdata allocation", TM_ENOMEM, __LINE__);
+    for (f = 0; f < nf; f++) {
+        (*cellenvdata)[f] = (cellenvdata_t *)calloc((size_t)(n > 0 ? n : 1), sizeof(cellenvdata_t));
+        if (!(*cellenvdata)[f]) die("cellenvdata allocation", TM_ENOMEM, __LINE__);
+    }
+    if (systeminfo.size != 1) die("grid-to-cell gather: the GB300 path runs one MPI rank", TM_EINVAL, __LINE__);
+    const int64_t vol = patches->size ? patches->size[0].x * patches->size[0].y * patches->size[0].z : 0;
+    if (n > 0 && nf > 0 && g_sess && vol > 0 && patches->buff && patches->buff[0]) {
+        const int64_t lo[3] = {patches->lowercorner[0].x, patches->lowercorner[0].y, patches->lowercorner[0].z};
+        const int64_t sz[3] = {patches->size[0].x, patches->size[0].y, patches->size[0].z};
+        const double lower[3] = {grid->lowercorner.x, grid->lowercorner.y, grid->lowercorner.z};
+        const int64_t hi[3] = {grid->upperidx[0].x, grid->upperidx[0].y, grid->upperidx[0].z};
+        double **dst = (double **)malloc(sizeof(double *) * (size_t)nf);
+        if (!dst) die("cellenvdata allocation", TM_ENOMEM, __LINE__);
+        for (f = 0; f < nf; f++) dst[f] = (double *)(*cellenvdata)[f];
+        TRY("grid-to-cell gather",
+            tmi_env2cells_patch(g_sess, g_cid, patches->buff[0], nf, lo, sz, lower, grid->resolution, hi, dst));
+        free(dst);
+    }
+    /* the received patches are released here (patches.c:590-592) */
+    if (patches->buff) {
+        for (p = 0; p < systeminfo.size; p++) free(patches->buff[p]);
+        free(patches->buff);
+        patches->buff = NULL;
+    }
+}
+
+void fieldgradient(systeminfo_t systeminfo, settings_t settings, environment_t **environment, grid_t *grid)
+{
+    g_si = systeminfo;
+    if (settings.numberoffields == 0) return;
+    if (systeminfo.size != 1) die("field gradient: the GB300 path runs one MPI rank", TM_EINVAL, __LINE__);
+    if (!g_sess) ensure_session(1, settings.dimension);
+    const int64_t gs[3] = {grid->localsize.x, grid->localsize.y, grid->localsize.z};
+    for (int f = 0; f < settings.numberoffields; f++)
+        TRY("field gradient", tmi_field_gradient_host(g_sess, (*environment)[f].data, gs, grid->resolution,
+                                                      (*environment)[f].gradient));
 }
 
 void tm_dropin_shutdown(void)

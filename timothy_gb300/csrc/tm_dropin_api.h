@@ -41,6 +41,13 @@ int tmi_patch_box(tm_session *s, int cid, int64_t lo[3], int64_t hi[3]);
 int tmi_read_patch(tm_session *s, int cid, const int64_t lo[3], const int64_t hi[3], double *dst);
 /* device scratch large enough for n cells of `stride` bytes */
 int tmi_reserve_stage(tm_session *s, int64_t bytes);
+/* grid -> cell gather from a host patch (fields then gradients) into per-field host arrays */
+int tmi_env2cells_patch(tm_session *s, int cid, const double *patch, int nfields, const int64_t box_lo[3],
+                        const int64_t box_size[3], const double lower[3], float resolution, const int64_t grid_hi[3],
+                        double **cellenv);
+/* gradient of one field, host arrays */
+int tmi_field_gradient_host(tm_session *s, const double *data, const int64_t gsize[3], float resolution,
+                            double *gradient);
 
 #ifdef __cplusplus
 }

@@ -24,3 +24,24 @@ cudaError_t tm_launch_fix(const tm_arrays &a, const tm_consts *K, cudaStream_t s
 cudaError_t tm_launch_octree(const tm_arrays &a, const tm_consts *K, int block, cudaStream_t st);
 cudaError_t tm_launch_update(const tm_arrays &a, const tm_consts *K, cudaStream_t st);
 cudaError_t tm_launch_cic(const tm_arrays &a, const tm_consts *K, cudaStream_t st);
+
+// geometry of a grid -> cell gather or a field gradient (tm_field.cu): the
+// grid's lower corner and resolution, its last node index per axis, and the
+// box of nodes the data arrays hold (the whole grid, or a patch)
+struct tm_envgeom {
+    double lower[3];
+    double res, inv;     // inv = 1 / res when res is a power of two (pow2)
+    float resf;
+    int pow2;
+    long long hi[3];
+    long long blo[3], bsz[3];
+    int nfields;
+};
+tm_envgeom tm_make_envgeom(const double lower[3], float res, const int64_t grid_hi[3], const int64_t box_lo[3],
+                           const int64_t box_size[3], int nfields);
+cudaError_t tm_launch_env2cells(const tm_envgeom &g, const double *x, const double *y, const double *z, long long n,
+                                const double *data, const double *grad, double *out, cudaStream_t st);
+cudaError_t tm_launch_env2cells_colony(const tm_envgeom &g, const tm_arrays &a, long long off, long long n,
+                                       const double *data, const double *grad, double *out, cudaStream_t st);
+cudaError_t tm_launch_field_gradient(const tm_envgeom &g, const int64_t gsize[3], const double *data, double *grad,
+                                     cudaStream_t st);

@@ -136,6 +136,8 @@ struct tm_session {
     int kernels_per_step = 0;
     int mass_types = 0;   // types the FP64 density-weight array holds
     int dl_next = 0;      // download buffer the next field uses
+    double *env_buf = nullptr;   // gather output staging (grows on demand)
+    size_t env_bytes = 0;
     tm_tuning tune{1, 1, 128, 0.1f, 64};
     cudaEvent_t tstart = nullptr, tstop = nullptr;
 };
@@ -627,6 +629,7 @@ extern "C" int tm_session_destroy(tm_session *s)
         if (s->ev_ready[k]) cudaEventDestroy(s->ev_ready[k]);
         if (s->ev_copied[k]) cudaEventDestroy(s->ev_copied[k]);
     }
+    if (s->env_buf) cudaFree(s->env_buf);
     if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
@@ -1585,6 +1588,93 @@ extern "C" int tmi_read_patch(tm_session *s, int cid, const int64_t lo[3], const
                                                             (double *)g_stage.ptr);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(dst, g_stage.ptr, (size_t)tot * 8, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return TM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// grid -> cell gather and field gradient (tm_field.cu) for session colonies
+// and the drop-ins
+
+static int env_reserve(tm_session *s, size_t bytes)
+{
+    if (bytes <= s->env_bytes) return TM_OK;
+    if (s->env_buf) CK(cudaFree(s->env_buf));
+    s->env_buf = nullptr;
+    s->env_bytes = 0;
+    CK(cudaMalloc((void **)&s->env_buf, bytes));
+    s->env_bytes = bytes;
+    return TM_OK;
+}
+
+extern "C" int tm_colony_env2cells(tm_session *s, int id, const double lower[3], float resolution,
+                                   const int64_t gsize[3], int nfields, const double *data, const double *gradient,
+                                   double *cellenv)
+{
+    int rc = lookup(s, id);
+    if (rc) return rc;
+    if (!lower || !gsize || !data || !gradient || !cellenv || nfields < 1 || !(resolution > 0.0f))
+        return tm_fail(TM_EINVAL, "bad gather arguments");
+    if (gsize[0] < 1 || gsize[1] < 1 || gsize[2] < 1 || (s->K.dim == 2 && gsize[2] != 1))
+        return tm_fail(TM_EINVAL, "bad grid size");
+    const colony_host &c = s->cols[id];
+    if (c.n == 0) return TM_OK;
+    CK(cudaSetDevice(s->device));
+    const size_t bytes = (size_t)nfields * (size_t)c.n * 4 * sizeof(double);
+    if ((rc = env_reserve(s, bytes))) return rc;
+    const int64_t hi[3] = {gsize[0] - 1, gsize[1] - 1, s->K.dim == 3 ? gsize[2] - 1 : 0};
+    const int64_t lo[3] = {0, 0, 0};
+    const tm_envgeom g = tm_make_envgeom(lower, resolution, hi, lo, gsize, nfields);
+    CK(tm_launch_env2cells_colony(g, view(s, s->parity), c.off, c.n, data, gradient, s->env_buf, s->stream));
+    CK(cudaMemcpyAsync(cellenv, s->env_buf, bytes, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return TM_OK;
+}
+
+// drop-in patches_applyenv2cells: the host patch (fields, then gradients, the
+// reference's buffer layout) is staged on the device and gathered for the
+// colony's cells; cellenv[f] receives n cellenvdata_t of field f
+extern "C" int tmi_env2cells_patch(tm_session *s, int cid, const double *patch, int nfields, const int64_t box_lo[3],
+                                   const int64_t box_size[3], const double lower[3], float resolution,
+                                   const int64_t grid_hi[3], double **cellenv)
+{
+    int rc = lookup(s, cid);
+    if (rc) return rc;
+    const colony_host &c = s->cols[cid];
+    if (c.n == 0 || nfields < 1) return TM_OK;
+    CK(cudaSetDevice(s->device));
+    const int64_t vol = box_size[0] * box_size[1] * box_size[2];
+    const size_t pbytes = (size_t)(4 * (int64_t)nfields * vol) * sizeof(double);
+    const size_t obytes = (size_t)nfields * (size_t)c.n * 4 * sizeof(double);
+    if ((rc = tmi_reserve_stage(s, (int64_t)pbytes))) return rc;
+    if ((rc = env_reserve(s, obytes))) return rc;
+    CK(cudaMemcpyAsync(g_stage.ptr, patch, pbytes, cudaMemcpyHostToDevice, s->stream));
+    const double *dd = (const double *)g_stage.ptr;
+    const tm_envgeom g = tm_make_envgeom(lower, resolution, grid_hi, box_lo, box_size, nfields);
+    CK(tm_launch_env2cells_colony(g, view(s, s->parity), c.off, c.n, dd, dd + (size_t)nfields * (size_t)vol,
+                                  s->env_buf, s->stream));
+    for (int f = 0; f < nfields; f++)
+        CK(cudaMemcpyAsync(cellenv[f], s->env_buf + (size_t)f * (size_t)c.n * 4, (size_t)c.n * 4 * sizeof(double),
+                           cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return TM_OK;
+}
+
+// drop-in fieldgradient: one field, host data in, host gradient out
+extern "C" int tmi_field_gradient_host(tm_session *s, const double *data, const int64_t gsize[3], float resolution,
+                                       double *gradient)
+{
+    if (!s) return tm_fail(TM_EINVAL, "null session");
+    CK(cudaSetDevice(s->device));
+    const int64_t G = gsize[0] * gsize[1] * gsize[2];
+    if (G <= 0) return TM_OK;
+    int rc = tmi_reserve_stage(s, 4 * G * (int64_t)sizeof(double));
+    if (rc) return rc;
+    double *dd = (double *)g_stage.ptr;
+    CK(cudaMemcpyAsync(dd, data, (size_t)G * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+    const tm_envgeom g = tm_make_envgeom(nullptr, resolution, nullptr, nullptr, gsize, 1);
+    CK(tm_launch_field_gradient(g, gsize, dd, dd + G, s->stream));
+    CK(cudaMemcpyAsync(gradient, dd + G, (size_t)(3 * G) * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     return TM_OK;
 }

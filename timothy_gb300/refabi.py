@@ -92,11 +92,22 @@ class patches_t(C.Structure):
                 ("reqsend", C.c_void_p), ("reqrecv", C.c_void_p), ("lowercorner", C.POINTER(int643dv_t)),
                 ("uppercorner", C.POINTER(int643dv_t)), ("lowercornerR", C.c_void_p),
                 ("uppercornerR", C.c_void_p), ("size", C.POINTER(int643dv_t)), ("commbuff", C.c_void_p),
-                ("buff", C.c_void_p)]
+                ("buff", C.POINTER(C.c_void_p))]
+
+
+class cellenvdata_t(C.Structure):
+    _fields_ = [("value", C.c_double), ("gx", C.c_double), ("gy", C.c_double), ("gz", C.c_double)]
+
+
+class environment_t(C.Structure):
+    _fields_ = [("name", C.c_char * 128), ("diffusioncoefficient", C.c_double), ("boundarycondition", C.c_double),
+                ("initialconditionmean", C.c_double), ("initialconditionvariance", C.c_double),
+                ("lambdadelay", C.c_double), ("data", C.c_void_p), ("gradient", C.c_void_p),
+                ("production", C.c_void_p)]
 
 
 SIZES = {"celldata_t": 112, "cellsinfo_t": 192, "celltype_t": 368, "systeminfo_t": 56, "settings_t": 336,
-         "cellcommdata_t": 104}
+         "cellcommdata_t": 104, "environment_t": 192, "cellenvdata_t": 32}
 
 CELL_DTYPE = np.dtype({"names": [f for f, _ in celldata_t._fields_],
                        "formats": ["<i4", "<i4", "<i4", "<i4", "<f4", "<f4", "<f4", "<f4", "<f4", "<f4", "<i4",
@@ -117,9 +128,12 @@ def _bind(lib):
     lib.patches_alloc.argtypes = [systeminfo_t, settings_t, C.POINTER(patches_t), C.POINTER(cellsinfo_t),
                                   C.POINTER(grid_t)]
     lib.patches_cells2envinfo.argtypes = lib.patches_alloc.argtypes
+    lib.patches_applyenv2cells.argtypes = [systeminfo_t, settings_t, C.POINTER(patches_t), C.POINTER(cellsinfo_t),
+                                           C.POINTER(grid_t), C.POINTER(C.POINTER(C.POINTER(cellenvdata_t)))]
+    lib.fieldgradient.argtypes = [systeminfo_t, settings_t, C.POINTER(C.POINTER(environment_t)), C.POINTER(grid_t)]
     for f in ("octbuild", "octfree", "computepotential", "computeremotepotential", "computegradient",
               "computeremotegradient", "updatepositions", "patches_alloc", "patches_cells2envinfo",
-              "tm_dropin_shutdown"):
+              "patches_applyenv2cells", "fieldgradient", "tm_dropin_shutdown"):
         getattr(lib, f).restype = None
     lib._refabi_bound = True
     return lib
@@ -196,7 +210,11 @@ class DropinRun:
         self.aff = None
         self.deposit = None
 
-    def step(self, update: bool = True):
+    def step(self, update: bool = True, env=None):
+        """One reference step; with env = (data, gradient) (grid arrays of
+        shape (nfields, gx, gy, gz) and (nfields, gx, gy, gz, 3)) the fields are
+        gathered to the cells before the position update, as step.c:84-86 does
+        (self.cellenv, shape (nfields, n, 4))."""
         lib = self.lib
         ct = self.celltype
         lib.octbuild(self.si, C.byref(self.ci), ct)
@@ -221,12 +239,58 @@ class DropinRun:
         lib.computeremotepotential(self.si, C.byref(self.ci), ct, self.cc)
         lib.computegradient(self.si, C.byref(self.ci), ct, self.cc)
         lib.computeremotegradient(self.si, C.byref(self.ci), ct, self.cc)
+        if env is not None and self.cic:
+            self._env2cells(p, *env)
         if update:
             lib.updatepositions(self.st, ct, C.byref(self.ci), self.removecell.ctypes.data,
                                 C.byref(self.removecount))
         lib.octfree(C.byref(self.ci))
         aff = double3dv_t.in_dll(lib, "affShift")
         self.aff = np.array([aff.x, aff.y, aff.z, C.c_double.in_dll(lib, "affScale").value])
+
+    def _env2cells(self, p, data, gradient):
+        # the received patch in the reference's layout (patches.c:380-416):
+        # every field over the patch box, then 3 gradient values per node and field
+        libc = C.CDLL(None)
+        libc.malloc.restype = C.c_void_p
+        libc.malloc.argtypes = [C.c_size_t]
+        nf = int(data.shape[0])
+        lo, sz = p.lowercorner[0], p.size[0]
+        if not (p.intersect and p.intersect[0]):
+            sz = int643dv_t(0, 0, 0)
+        box = (slice(None), slice(lo.x, lo.x + sz.x), slice(lo.y, lo.y + sz.y), slice(lo.z, lo.z + sz.z))
+        packed = np.concatenate([np.ascontiguousarray(data[box]).ravel(),
+                                 np.ascontiguousarray(gradient[box]).ravel()]) if sz.x else np.zeros(1)
+        p.buff = C.cast(libc.malloc(C.sizeof(C.c_void_p)), C.POINTER(C.c_void_p))
+        p.buff[0] = libc.malloc(max(packed.nbytes, 8))
+        C.memmove(p.buff[0], packed.ctypes.data, packed.nbytes)
+        st = settings_t.from_buffer_copy(self.st)
+        st.numberoffields = nf
+        out = C.POINTER(C.POINTER(cellenvdata_t))()
+        self.lib.patches_applyenv2cells(self.si, st, C.byref(p), C.byref(self.ci), C.byref(self.grid),
+                                        C.byref(out))
+        ce = np.zeros((nf, self.n, 4))
+        for f in range(nf):
+            ce[f] = np.ctypeslib.as_array(C.cast(out[f], C.POINTER(C.c_double)), shape=(self.n * 4,)).reshape(-1, 4)
+            libc.free.argtypes = [C.c_void_p]
+            libc.free(C.cast(out[f], C.c_void_p))
+        libc.free(C.cast(out, C.c_void_p))
+        self.cellenv = ce
+
+    def fieldgradient(self, data: np.ndarray) -> np.ndarray:
+        """fieldgradient() drop-in on (nfields, gx, gy, gz) host data."""
+        nf = int(data.shape[0])
+        data = np.ascontiguousarray(data, np.float64)
+        grad = np.zeros(data.shape + (3,))
+        envs = (environment_t * nf)()
+        for f in range(nf):
+            envs[f].data = data[f].ctypes.data
+            envs[f].gradient = grad[f].ctypes.data
+        st = settings_t.from_buffer_copy(self.st)
+        st.numberoffields = nf
+        penv = C.cast(envs, C.POINTER(environment_t))
+        self.lib.fieldgradient(self.si, st, C.byref(penv), C.byref(self.grid))
+        return grad
 
     def outputs(self) -> dict:
         n = self.n

@@ -99,6 +99,9 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "tm_session_timer": (C.c_int, [P, C.c_int, P]),
         "tm_session_launches": (C.c_int64, [P]),
         "tm_session_list_rate": (C.c_int, [P, P, P]),
+        "tm_env2cells": (C.c_int, [P, P, P, C.c_int64, C.c_int, P, C.c_float, P, C.c_int, P, P, P, P]),
+        "tm_field_gradient": (C.c_int, [P, P, C.c_float, C.c_int, P, P]),
+        "tm_colony_env2cells": (C.c_int, [P, C.c_int, P, C.c_float, P, C.c_int, P, P, P]),
         "tm_session_bytes": (C.c_int64, [C.POINTER(_Config), C.c_int]),
         "tm_device_memory": (C.c_int, [C.c_int, P, P]),
         "tm_session_get_tuning": (C.c_int, [P, C.POINTER(_Tuning)]),
@@ -140,6 +143,28 @@ def device_memory(device: int = 0) -> tuple[int, int]:
     t = np.zeros(1, np.int64)
     _check(load_library().tm_device_memory(int(device), _p(f), _p(t)))
     return int(f[0]), int(t[0])
+
+
+def _dptr(a) -> int:
+    """Device address of a CUDA array (anything with data_ptr(), or an int)."""
+    return int(a.data_ptr()) if hasattr(a, "data_ptr") else int(a)
+
+
+def env2cells_device(x, y, z, n: int, dim: int, lower, resolution: float, gsize, nfields: int, data, gradient,
+                     cellenv, stream=None):
+    """tm_env2cells on device arrays (x, y, z, data, gradient, cellenv: CUDA arrays)."""
+    lo = np.ascontiguousarray(lower, np.float64)
+    gs = np.ascontiguousarray(gsize, np.int64)
+    _check(load_library().tm_env2cells(_dptr(x), _dptr(y), _dptr(z), int(n), int(dim), _p(lo), float(resolution),
+                                       _p(gs), int(nfields), _dptr(data), _dptr(gradient), _dptr(cellenv),
+                                       None if stream is None else _dptr(stream)))
+
+
+def field_gradient_device(data, gsize, resolution: float, nfields: int, gradient, stream=None):
+    """tm_field_gradient on device arrays."""
+    gs = np.ascontiguousarray(gsize, np.int64)
+    _check(load_library().tm_field_gradient(_dptr(data), _p(gs), float(resolution), int(nfields), _dptr(gradient),
+                                            None if stream is None else _dptr(stream)))
 
 
 def host_register(a: np.ndarray):
@@ -314,6 +339,16 @@ class Session:
         n = np.zeros(1, np.int64)
         _check(load_library().tm_session_list_rate(self._h, _p(r), _p(n)))
         return float(r[0]), int(n[0])
+
+    def env2cells(self, cid: int, lower, resolution: float, gsize, nfields: int, data, gradient) -> np.ndarray:
+        """Grid -> cell gather for a colony (device field arrays); (nfields, n, 4) in caller order."""
+        n = self._n[cid]
+        out = np.zeros((nfields, n, 4))
+        lo = np.ascontiguousarray(lower, np.float64)
+        gs = np.ascontiguousarray(gsize, np.int64)
+        _check(load_library().tm_colony_env2cells(self._h, cid, _p(lo), float(resolution), _p(gs), int(nfields),
+                                                  _dptr(data), _dptr(gradient), _p(out)))
+        return out
 
     # -- tuning -------------------------------------------------------------
     @property
