@@ -284,6 +284,63 @@ def serving_form(args, device, rate, seconds):
             "pool_gb": st["pool_bytes"] / 1e9}
 
 
+def field_rows(device, peak, steps=10):
+    """The grid -> cell gather and the field gradient on the scale1m layout:
+    1,000,000 clustered cells (seed 2) and one field on the 257^3 FP64 grid of
+    GFH 8.  Each launch is timed alone with CUDA events after a write of 256 MB
+    (flushes L2); achieved bandwidth counts the algorithmic bytes."""
+    import torch
+
+    from oracle import bindings as OB
+    from timothy_gb300 import session as S
+
+    torch.cuda.set_device(device)
+    n, gfh, nf = 1_000_000, 8.0, 1
+    col = C.make_colony("clustered", n, 2, radius_for("clustered", n, 2))
+    dims = OB.grid_dims(3, gfh)
+    G = int(np.prod(dims))
+    rng = np.random.Generator(np.random.PCG64(5))
+    data = torch.from_numpy(rng.random((nf,) + dims)).cuda()
+    grad = torch.zeros((nf,) + dims + (3,), dtype=torch.float64, device="cuda")
+    xs = [torch.from_numpy(np.ascontiguousarray(getattr(col, k))).cuda() for k in ("x", "y", "z")]
+    out = torch.zeros((nf, n, 4), dtype=torch.float64, device="cuda")
+    flush = torch.empty(32 * 1024 * 1024, dtype=torch.float64, device="cuda")
+    lower = (-1024.0, -1024.0, -1024.0)
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        ms = []
+        for _ in range(steps):
+            flush.fill_(1.0)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            torch.cuda.synchronize()
+            ms.append(a.elapsed_time(b))
+        return float(np.mean(ms))
+
+    ms_g = timed(lambda: S.field_gradient_device(data, dims, gfh, nf, grad))
+    ms_e = timed(lambda: S.env2cells_device(*xs, n, 3, lower, gfh, dims, nf, data, grad, out))
+    # grid nodes the cells touch (each read once: its value and 3 gradient components)
+    ci = [np.floor((getattr(col, k) + 1024.0) / gfh).astype(np.int64) for k in ("x", "y", "z")]
+    keys = []
+    for ax in (0, 1):
+        for ay in (0, 1):
+            for az in (0, 1):
+                keys.append(((ci[0] + ax) * dims[1] + ci[1] + ay) * dims[2] + ci[2] + az)
+    touched = int(np.unique(np.concatenate(keys)).size)
+    b_g = 32 * G * nf                              # read u, write 3 components
+    b_e = n * (24 + 32 * nf) + touched * 32 * nf   # positions in, cellenvdata out, touched nodes in
+    return {"config": "1,000,000 clustered cells (seed 2), 257^3 FP64 grid (GFH 8), 1 field; L2 flushed",
+            "field_gradient": {"ms": ms_g, "bytes": b_g, "achieved_gbs": b_g / ms_g / 1e6,
+                               "frac_of_measured_hbm": b_g / ms_g / 1e6 / peak},
+            "env2cells": {"ms": ms_e, "bytes": b_e, "touched_nodes": touched, "achieved_gbs": b_e / ms_e / 1e6,
+                          "frac_of_measured_hbm": b_e / ms_e / 1e6 / peak,
+                          "cell_gathers_per_s": n / (ms_e * 1e-3)}}
+
+
 def _size_bins(reqs):
     out = {}
     for lo, hi in ((1e3, 1e4), (1e4, 1e5), (1e5, 1e6 + 1)):
@@ -455,6 +512,7 @@ def main():
         cpu = cpu_sample(wl)
 
     if not args.no_forms and world == 1:
+        extra["rows"] = {"grid_to_cell": field_rows(local, peak)}
         forms = {"batched": batched_form(args, local)}
         forms["serving"] = [serving_form(args, local, float(r), args.serve_seconds)
                             for r in args.serve_rates.split(",") if r]

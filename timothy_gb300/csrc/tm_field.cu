@@ -9,8 +9,8 @@
 // the reference), one-sided differences on the faces; an axis of one node
 // (the z axis of a 2-D grid) gets 0, where the reference reads outside the
 // row.  Both are FP64 with the reference's roundings: a division by the
-// resolution becomes a multiplication by its reciprocal only when that is a
-// power of two (then both round the same real number).
+// resolution becomes a scaling by its reciprocal only when that is a power of
+// two (then both round the same real number).
 #include "tm_arrays.cuh"
 #include "tm_kernels.cuh"
 #include "timothy_gb300.h"
@@ -18,10 +18,21 @@
 #include <algorithm>
 #include <cmath>
 
+// x * 2^e for a power-of-two scale: the exponent field moves by e, which is
+// the exactly rounded product whenever x and the result are normal numbers
+// (integer work: the FP64 pipe of this GPU is narrow); other cases multiply
+__device__ __forceinline__ double scale_pow2(double x, int e, double factor)
+{
+    const long long b = __double_as_longlong(x);
+    const int ex = (int)((b >> 52) & 0x7ff);
+    if (ex == 0 || ex == 0x7ff || ex + e <= 0 || ex + e >= 0x7ff) return mul64(x, factor);
+    return __longlong_as_double(b + ((long long)e << 52));
+}
+
 // x / res with the reference's rounding
 __device__ __forceinline__ double div_res(double x, const tm_envgeom &g)
 {
-    return g.pow2 ? mul64(x, g.inv) : div64(x, g.res);
+    return g.pow2 ? scale_pow2(x, g.inv_exp, g.inv) : div64(x, g.res);
 }
 
 // gather for one cell at pos; out[(f * out_n + c) * 4 + k]
@@ -83,17 +94,17 @@ __global__ void __launch_bounds__(256) k_env2cells_colony(tm_envgeom g, tm_array
     }
 }
 
-__global__ void __launch_bounds__(256) k_field_gradient(tm_envgeom g, long long nx, long long ny, long long nz,
+// one field per blockIdx.y; node indices fit in 32 bits (checked by the host)
+__global__ void __launch_bounds__(256) k_field_gradient(tm_envgeom g, unsigned nx, unsigned ny, unsigned nz,
                                                         const double *data, double *grad)
 {
-    const long long G = nx * ny * nz, total = G * g.nfields;
-    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < total;
-         q += (long long)gridDim.x * blockDim.x) {
-        const long long f = q / G, o = q - f * G;
-        const long long i = o / (ny * nz), j = (o / nz) % ny, k = o % nz;
-        const double *u = data + f * G;
-        const long long n3[3] = {nx, ny, nz}, ix[3] = {i, j, k}, st[3] = {ny * nz, nz, 1};
-        double *out = grad + (f * G + o) * 3;
+    const unsigned G = nx * ny * nz, nyz = ny * nz;
+    const long long f = blockIdx.y;
+    const double *u = data + f * (long long)G;
+    for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < G; o += gridDim.x * blockDim.x) {
+        const unsigned i = o / nyz, r = o - i * nyz, j = r / nz, k = r - j * nz;
+        const unsigned n3[3] = {nx, ny, nz}, ix[3] = {i, j, k}, st[3] = {nyz, nz, 1u};
+        double *out = grad + (f * (long long)G + o) * 3;
         for (int c = 0; c < 3; c++) {
             double v;
             if (n3[c] < 2) v = 0.0;
@@ -122,6 +133,7 @@ tm_envgeom tm_make_envgeom(const double lower[3], float res, const int64_t grid_
     const double m = std::frexp(g.res, &e);
     g.pow2 = (m == 0.5) ? 1 : 0;             // res = 2^(e-1): its reciprocal is exact
     g.inv = g.pow2 ? std::ldexp(1.0, 1 - e) : 0.0;
+    g.inv_exp = 1 - e;
     g.nfields = nfields;
     return g;
 }
@@ -151,9 +163,12 @@ cudaError_t tm_launch_env2cells_colony(const tm_envgeom &g, const tm_arrays &a, 
 cudaError_t tm_launch_field_gradient(const tm_envgeom &g, const int64_t gsize[3], const double *data, double *grad,
                                      cudaStream_t st)
 {
-    const long long total = (long long)gsize[0] * gsize[1] * gsize[2] * g.nfields;
-    if (total <= 0) return cudaSuccess;
-    k_field_gradient<<<grid_for(total), 256, 0, st>>>(g, gsize[0], gsize[1], gsize[2], data, grad);
+    const long long G = (long long)gsize[0] * gsize[1] * gsize[2];
+    if (G <= 0 || g.nfields <= 0) return cudaSuccess;
+    if (G >= (1ll << 31) || g.nfields > 65535) return cudaErrorInvalidValue;
+    const dim3 blocks(grid_for(G), (unsigned)g.nfields);
+    k_field_gradient<<<blocks, 256, 0, st>>>(g, (unsigned)gsize[0], (unsigned)gsize[1], (unsigned)gsize[2], data,
+                                             grad);
     return cudaGetLastError();
 }
 

@@ -30,9 +30,9 @@ cudaError_t tm_launch_cic(const tm_arrays &a, const tm_consts *K, cudaStream_t s
 // box of nodes the data arrays hold (the whole grid, or a patch)
 struct tm_envgeom {
     double lower[3];
-    double res, inv;     // inv = 1 / res when res is a power of two (pow2)
+    double res, inv;     // inv = 1 / res = 2^inv_exp when res is a power of two (pow2)
     float resf;
-    int pow2;
+    int pow2, inv_exp;
     long long hi[3];
     long long blo[3], bsz[3];
     int nfields;
