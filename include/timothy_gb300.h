@@ -216,6 +216,13 @@ int tm_field_gradient(const double *data, const int64_t gsize[3], float resoluti
 int tm_colony_env2cells(tm_session *s, int id, const double lower[3], float resolution, const int64_t gsize[3],
                         int nfields, const double *data, const double *gradient, double *cellenv);
 
+/* writevtk (io.c:372-516) at one rank for a session colony: writes the
+ * reference's legacy binary VTK file (big-endian float positions, cell type,
+ * rank, cell type index, the density constant 1.0, float forces of the last
+ * step) to path, cells in the caller's order; the file image is assembled on
+ * the device. */
+int tm_colony_write_vtk(tm_session *s, int id, const char *path, int rank);
+
 /* No counterpart in the reference.  CIC deposit of n cells onto field 0 of a
  * grid, the work of patches_alloc + patches_cells2envinfo at one rank, for
  * callers that cannot allocate device memory: code running while a CUDA

@@ -57,6 +57,8 @@ def load(which: str = "oracle") -> C.CDLL:
         lib.tmo_env2cells.argtypes = [C.c_int64, C.c_int, _P, _P, _P, C.c_float, C.c_int, _P, _P, _P]
         lib.tmo_fieldgradient.restype = C.c_int
         lib.tmo_fieldgradient.argtypes = [C.c_int, C.c_float, C.c_int, _P, _P, _P]
+        lib.tmo_write_vtk.restype = C.c_int
+        lib.tmo_write_vtk.argtypes = [C.c_char_p, C.c_int64, _P, _P, _P, _P, _P, _P, _P, C.c_int]
         lib.tmo_neighbours.restype = C.c_int
         lib.tmo_neighbours.argtypes = [C.c_int64, C.c_int, C.c_int, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
                                        C.c_int]
@@ -67,6 +69,8 @@ def load(which: str = "oracle") -> C.CDLL:
         lib.ref_sizeof.argtypes = [C.c_int]
         lib.ref_env2cells.restype = C.c_int64
         lib.ref_env2cells.argtypes = [C.c_int64, C.c_int, _P, _P, _P, _P, C.c_float, C.c_int, _P, _P, C.c_int64, _P]
+        lib.ref_write_vtk.restype = C.c_int
+        lib.ref_write_vtk.argtypes = [C.c_char_p, C.c_int, C.c_int64, _P, _P, _P, _P, _P, _P, _P]
         lib.ref_fieldgradient.restype = C.c_int64
         lib.ref_fieldgradient.argtypes = [C.c_int, C.c_float, C.c_int, _P, C.c_int64, _P, _P]
     fn.restype = C.c_int
@@ -232,3 +236,25 @@ def fieldgradient(data: np.ndarray, *, dim: int = 3, gfh: float = 8.0, which: st
     if rc or tuple(dims) != tuple(data.shape[1:]):
         raise RuntimeError(f"fieldgradient ({which}) failed: {rc}, grid {tuple(dims)} vs {data.shape[1:]}")
     return out
+
+
+def write_vtk(path: str, x, y, z, ctype, fx, fy, fz, *, which: str = "oracle") -> bytes:
+    """writevtk at one rank for cells in caller order; returns the file's bytes.
+    The reference writes vtk/step00000000.vtk under the directory of path."""
+    lib = load(which)
+    arr = [np.ascontiguousarray(a, np.float64) for a in (x, y, z)]
+    ct = np.ascontiguousarray(ctype, np.int32)
+    fs = [np.ascontiguousarray(a, np.float64) for a in (fx, fy, fz)]
+    n = len(arr[0])
+    if which == "oracle":
+        rc = lib.tmo_write_vtk(path.encode(), n, *[_ptr(a) for a in arr], _ptr(ct), *[_ptr(a) for a in fs], 0)
+        out = path
+    else:
+        d = os.path.dirname(os.path.abspath(path))
+        os.makedirs(os.path.join(d, "vtk"), exist_ok=True)
+        rc = lib.ref_write_vtk(d.encode(), 0, n, *[_ptr(a) for a in arr], _ptr(ct), *[_ptr(a) for a in fs])
+        out = os.path.join(d, "vtk", "step00000000.vtk")
+    if rc:
+        raise RuntimeError(f"write_vtk ({which}) failed: {rc}")
+    with open(out, "rb") as f:
+        return f.read()

@@ -2,7 +2,7 @@
  *
  * Compiled only into oracle/_ref/libtimothy_ref*.so, together with the
  * unmodified reference sources (octree.c, potential.c, cells.c, patches.c,
- * grid.c, utils.c, fieldgradient.c) and the single-rank MPI shim.  It replays the hot part of
+ * grid.c, utils.c, fieldgradient.c, io.c) and the single-rank MPI shim.  It replays the hot part of
  * the reference step loop (main.c:67-79, step.c:41-100) on structure-of-arrays
  * inputs and copies the outputs back, so tests and the CPU baseline can call
  * the reference through ctypes.  Nothing in the product links against it.
@@ -13,12 +13,14 @@
 #include <math.h>
 #include <omp.h>
 #include <sys/time.h>
+#include <unistd.h>
 
 #include "global.h"
 #include "potential.h"
 #include "patches.h"
 #include "grid.h"
 #include "fieldgradient.h"
+#include "io.h"
 
 /* defined in octree.c with external linkage (octree.h:24-27) */
 extern double3dv_t affShift;
@@ -369,4 +371,46 @@ int64_t ref_fieldgradient(int dim, float gfh, int nfields, const double *data, i
     free(si.coords[0]);
     free(si.coords);
     return g;
+}
+
+/* writevtk (io.c:372-516) at one rank for cells in caller order: writes
+ * <dir>/vtk/step<step>.vtk (the reference's file name, relative to the
+ * working directory, so the driver runs it from dir).  Returns 0 or -1. */
+int ref_write_vtk(const char *dir, int step, int64_t n, const double *x, const double *y, const double *z,
+                  const int *ctype, const double *fx, const double *fy, const double *fz)
+{
+    systeminfo_t si;
+    settings_t st;
+    cellsinfo_t ci;
+    char cwd[4096];
+    int64_t i;
+    memset(&si, 0, sizeof(si));
+    memset(&st, 0, sizeof(st));
+    memset(&ci, 0, sizeof(ci));
+    si.rank = 0;
+    si.size = 1;
+    si.endian = 1;      /* little-endian host: the file is big-endian (checkendiannes) */
+    st.step = step;
+    ci.localcount.n = (uint64_t)n;
+    ci.globalcount.n = (uint64_t)n;
+    ci.cellsperproc = (uint64_t *)calloc(1, sizeof(uint64_t));
+    ci.cellsperproc[0] = (uint64_t)n;
+    ci.cells = (celldata_t *)calloc((size_t)(n > 0 ? n : 1), sizeof(celldata_t));
+    ci.forces = (double3dv_t *)calloc((size_t)(n > 0 ? n : 1), sizeof(double3dv_t));
+    for (i = 0; i < n; i++) {
+        ci.cells[i].x = x[i];
+        ci.cells[i].y = y[i];
+        ci.cells[i].z = z[i];
+        ci.cells[i].ctype = ctype[i];
+        ci.forces[i].x = fx[i];
+        ci.forces[i].y = fy[i];
+        ci.forces[i].z = fz[i];
+    }
+    if (!getcwd(cwd, sizeof cwd) || chdir(dir) != 0) return -1;
+    writevtk(si, st, ci);
+    int rc = chdir(cwd);
+    free(ci.cells);
+    free(ci.forces);
+    free(ci.cellsperproc);
+    return rc == 0 ? 0 : -1;
 }

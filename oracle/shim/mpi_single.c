@@ -4,6 +4,8 @@
  * world size 1 (patches.c:242-315). */
 #include <stdio.h>
 #include <string.h>
+#include <sys/types.h>
+#include <unistd.h>
 #include "mpi.h"
 
 static size_t type_bytes(MPI_Datatype t)
@@ -14,6 +16,7 @@ static size_t type_bytes(MPI_Datatype t)
     case MPI_DOUBLE: return sizeof(double);
     case MPI_DOUBLE_INT: return sizeof(double) + sizeof(int) + 4;
     case MPI_UINT64_T: case MPI_LONG_LONG: return 8;
+    case MPI_FLOAT: return sizeof(float);
     default: return 1;
     }
 }
@@ -91,4 +94,40 @@ int MPI_Cart_shift(MPI_Comm c, int dir, int disp, int *src, int *dst)
     *src = MPI_PROC_NULL;
     *dst = MPI_PROC_NULL;
     return MPI_SUCCESS;
+}
+
+int MPI_File_open(MPI_Comm c, const char *name, int mode, MPI_Info info, MPI_File *fh)
+{
+    (void)c; (void)info;
+    FILE *f = fopen(name, (mode & MPI_MODE_WRONLY) ? ((mode & MPI_MODE_CREATE) ? "w+b" : "r+b") : "rb");
+    *fh = (MPI_File)f;
+    return f ? MPI_SUCCESS : 1;
+}
+
+int MPI_File_set_size(MPI_File fh, MPI_Offset size)
+{
+    FILE *f = (FILE *)fh;
+    if (!f) return 1;
+    fflush(f);
+    return ftruncate(fileno(f), (off_t)size) == 0 ? MPI_SUCCESS : 1;
+}
+
+int MPI_File_seek(MPI_File fh, MPI_Offset off, int whence)
+{
+    (void)whence;
+    return fseeko((FILE *)fh, (off_t)off, SEEK_SET) == 0 ? MPI_SUCCESS : 1;
+}
+
+int MPI_File_write(MPI_File fh, const void *buf, int n, MPI_Datatype t, MPI_Status *st)
+{
+    (void)st;
+    size_t bytes = (size_t)n * type_bytes(t);
+    return fwrite(buf, 1, bytes, (FILE *)fh) == bytes ? MPI_SUCCESS : 1;
+}
+
+int MPI_File_close(MPI_File *fh)
+{
+    int rc = fclose((FILE *)*fh);
+    *fh = NULL;
+    return rc == 0 ? MPI_SUCCESS : 1;
 }

@@ -8,6 +8,7 @@
  *   - pair force (SPH kernel gradient)        inline.h:59-83, potential.c:193-202
  *   - position update + removal marks         cells.c:41-58, 342-365
  *   - grid -> cell gather, field gradient     patches.c:512-593, fieldgradient.c:149-225
+ *   - VTK writer                              io.c:372-516
  *   - CIC deposit at one rank                 grid.c:37-136, patches.c:47-234,
  *                                             patches.c:321-367
  * Expressions keep the reference's evaluation order (C left-to-right
@@ -18,6 +19,7 @@
 
 #include <float.h>
 #include <math.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #include <sys/time.h>
@@ -552,6 +554,89 @@ int tmo_fieldgradient(int dim, float gfh, int nfields, const double *data, doubl
                 }
     }
     return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* VTK writer at one rank                                                     */
+/* ------------------------------------------------------------------------ */
+
+static void put_be32(unsigned char *p, uint32_t v)
+{
+    p[0] = (unsigned char)(v >> 24);
+    p[1] = (unsigned char)(v >> 16);
+    p[2] = (unsigned char)(v >> 8);
+    p[3] = (unsigned char)v;
+}
+
+static int put_floats_be(FILE *f, const float *v, int64_t count)
+{
+    for (int64_t i = 0; i < count; i++) {
+        unsigned char b[4];
+        uint32_t u;
+        memcpy(&u, &v[i], 4);
+        put_be32(b, u);
+        if (fwrite(b, 1, 4, f) != 4) return -1;
+    }
+    return 0;
+}
+
+/* count big-endian ints: v[i], or `value` for every one when v is NULL */
+static int put_ints_be(FILE *f, int value, const int *v, int64_t count)
+{
+    for (int64_t i = 0; i < count; i++) {
+        unsigned char b[4];
+        put_be32(b, (uint32_t)(v ? v[i] : value));
+        if (fwrite(b, 1, 4, f) != 4) return -1;
+    }
+    return 0;
+}
+
+/* writevtk, io.c:372-516, at one rank: legacy binary VTK with big-endian
+ * float positions, cell type 1 for every cell, the rank, the cell type, a
+ * density of 1.0 (the reference writes the constant) and float forces. */
+int tmo_write_vtk(const char *path, int64_t n, const double *x, const double *y, const double *z, const int *ctype,
+                  const double *fx, const double *fy, const double *fz, int rank)
+{
+    FILE *f = fopen(path, "wb");
+    if (!f) return -1;
+    char head[512];
+    int rc = 0;
+    float *v = (float *)calloc((size_t)(n > 0 ? n : 1) * 3, sizeof(float));
+    if (!v) {
+        fclose(f);
+        return -3;
+    }
+    rc |= fputs("# vtk DataFile Version 2.0\nTimothy output\nBINARY\nDATASET UNSTRUCTURED_GRID", f) < 0;
+    snprintf(head, sizeof head, "\nPOINTS %lld float\n", (long long)n);
+    rc |= fputs(head, f) < 0;
+    for (int64_t i = 0; i < n; i++) {
+        v[3 * i] = (float)x[i];
+        v[3 * i + 1] = (float)y[i];
+        v[3 * i + 2] = (float)z[i];
+    }
+    rc |= put_floats_be(f, v, 3 * n);
+    snprintf(head, sizeof head, "\nCELL_TYPES %lld\n", (long long)n);
+    rc |= fputs(head, f) < 0;
+    rc |= put_ints_be(f, 1, NULL, n);
+    snprintf(head, sizeof head, "\nPOINT_DATA %lld", (long long)n);
+    rc |= fputs(head, f) < 0;
+    rc |= fputs("\nSCALARS rank integer 1\nLOOKUP_TABLE default\n", f) < 0;
+    rc |= put_ints_be(f, rank, NULL, n);
+    rc |= fputs("\nSCALARS type integer 1\nLOOKUP_TABLE default\n", f) < 0;
+    rc |= put_ints_be(f, 0, ctype, n);
+    rc |= fputs("\nSCALARS density float 1\nLOOKUP_TABLE default\n", f) < 0;
+    for (int64_t i = 0; i < n; i++) v[i] = 1.0f;
+    rc |= put_floats_be(f, v, n);
+    rc |= fputs("\nVECTORS force float\n", f) < 0;
+    for (int64_t i = 0; i < n; i++) {
+        v[3 * i] = (float)fx[i];
+        v[3 * i + 1] = (float)fy[i];
+        v[3 * i + 2] = (float)fz[i];
+    }
+    rc |= put_floats_be(f, v, 3 * n);
+    free(v);
+    rc |= fclose(f) != 0;
+    return rc ? -1 : 0;
 }
 
 /* ------------------------------------------------------------------------ */

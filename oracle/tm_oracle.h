@@ -76,6 +76,11 @@ int tmo_env2cells(int64_t n, int dim, const double *x, const double *y, const do
  * the one-rank grid of resolution gfh; dims receives the grid size. */
 int tmo_fieldgradient(int dim, float gfh, int nfields, const double *data, double *gradient, int64_t *dims);
 
+/* writevtk at one rank: the legacy binary VTK file of the cells (caller
+ * order) with their forces.  Returns 0 or a negative code. */
+int tmo_write_vtk(const char *path, int64_t n, const double *x, const double *y, const double *z, const int *ctype,
+                  const double *fx, const double *fy, const double *fz, int rank);
+
 /* The fingerprint mixer shared with the GPU diagnostics (SplitMix64 final mix). */
 uint64_t tm_mix64(uint64_t z);
 

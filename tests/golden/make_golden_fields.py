@@ -1,12 +1,14 @@
-"""Golden fixtures of the grid -> cell gather (patches_applyenv2cells) and the
-field gradient (fieldgradient_compute), from the reference's own functions
+"""Golden fixtures of the grid -> cell gather (patches_applyenv2cells), the
+field gradient (fieldgradient_compute) and the VTK writer (writevtk), from the
+reference's own functions
 compiled unmodified into oracle/_ref (``make -C oracle ref``).
 
 The fields come from tests/golden/fields.py (deterministic formulas), so only
 cells and outputs are stored; the gradient fixtures keep a seeded sample of
 nodes (always including the faces) plus per-component sums.
 
-    python tests/golden/make_golden_fields.py
+    python tests/golden/make_golden_fields.py          # gather and gradient
+    python tests/golden/make_golden_fields.py --vtk    # the VTK writer
 """
 from __future__ import annotations
 
@@ -72,5 +74,25 @@ def main():
         print(name, dims)
 
 
+def make_vtk():
+    """writevtk (io.c:372-516) of a two-type colony with seeded forces."""
+    import hashlib
+    import tempfile
+
+    col = C.make_colony("clustered", 3000, 5, C.initial_radius("clustered", 3000),
+                        types=C.CellTypes.consistent(h=(2.5, 2.5, 2.5), size=(1.0, 1.0, 1.0)))
+    rng = np.random.Generator(np.random.PCG64(9))
+    f = rng.normal(size=(3, col.n))
+    with tempfile.TemporaryDirectory() as d:
+        img = B.write_vtk(os.path.join(d, "x.vtk"), col.x, col.y, col.z, col.ctype, *f, which="ref_strict")
+    np.savez_compressed(os.path.join(HERE, "field_vtk_clustered3k.npz"), x=col.x, y=col.y, z=col.z, ctype=col.ctype,
+                        fx=f[0], fy=f[1], fz=f[2], sha256=np.frombuffer(hashlib.sha256(img).digest(), np.uint8),
+                        nbytes=len(img))
+    print("field_vtk_clustered3k", len(img))
+
+
 if __name__ == "__main__":
-    main()
+    if "--vtk" in sys.argv:
+        make_vtk()
+    else:
+        main()

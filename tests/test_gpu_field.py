@@ -86,10 +86,28 @@ def test_dropin_env2cells_and_fieldgradient(oracle_lib):
     gfh, nf = 8.0, 2
     dims = oracle_lib.grid_dims(3, gfh)
     data, grad = field(nf, dims), gradient_field(nf, dims)
-    run = DropinRun(col, cic=True, gfh=gfh, nfields=nf)
-    run.step(update=False, env=(data, grad))
-    assert np.array_equal(run.cellenv, oracle_lib.env2cells(col, data, grad, gfh=gfh, which="oracle"))
-    run.step(update=True, env=(data, grad))        # again, with the position update after it
-    assert np.array_equal(run.cellenv, oracle_lib.env2cells(col, data, grad, gfh=gfh, which="oracle"))
-    g = run.fieldgradient(data)
+    # the drop-ins page-lock the run's cells until shutdown: leave none behind
+    with DropinRun(col, cic=True, gfh=gfh, nfields=nf) as run:
+        run.step(update=False, env=(data, grad))
+        assert np.array_equal(run.cellenv, oracle_lib.env2cells(col, data, grad, gfh=gfh, which="oracle"))
+        run.step(update=True, env=(data, grad))        # again, with the position update after it
+        assert np.array_equal(run.cellenv, oracle_lib.env2cells(col, data, grad, gfh=gfh, which="oracle"))
+        g = run.fieldgradient(data)
     assert np.array_equal(g, oracle_lib.fieldgradient(data, dim=3, gfh=gfh, which="oracle"))
+
+
+def test_colony_vtk_matches_oracle(oracle_lib, tmp_path):
+    """The reference's VTK file of a resident colony, assembled on the device."""
+    from timothy_gb300 import session as S
+
+    types = C.CellTypes.consistent(h=(2.5, 2.5), size=(1.0, 1.0))
+    col = C.make_colony("clustered", 6000, 64, C.initial_radius("clustered", 6000), types=types)
+    with S.Session(types, max_slots=col.n + 64, list_capacity=384) as s:
+        cid = s.add_colony(col, precision="fp64", update="dt", dt=0.01, verlet=True)
+        s.step(3)
+        s.sync()
+        out = s.download(cid, ["x", "y", "z", "fx", "fy", "fz"])
+        s.write_vtk(cid, str(tmp_path / "gpu.vtk"))
+    ref = oracle_lib.write_vtk(str(tmp_path / "cpu.vtk"), out["x"], out["y"], out["z"], col.ctype, out["fx"],
+                               out["fy"], out["fz"], which="oracle")
+    assert (tmp_path / "gpu.vtk").read_bytes() == ref

@@ -113,3 +113,13 @@ def test_oracle_fieldgradient_matches_reference(oracle_lib, name):
         assert np.array_equal(g.reshape(nf, -1, 3).sum(axis=1)[:, :comps], rec[f"{tag}_sums"][:, :comps]), tag
     if dim == 2:
         assert not np.any(g[..., 2])
+
+
+def test_oracle_vtk_matches_reference(oracle_lib, tmp_path):
+    import hashlib
+
+    rec = np.load(os.path.join(GOLDEN, "field_vtk_clustered3k.npz"))
+    img = oracle_lib.write_vtk(str(tmp_path / "o.vtk"), rec["x"], rec["y"], rec["z"], rec["ctype"], rec["fx"],
+                               rec["fy"], rec["fz"], which="oracle")
+    assert len(img) == int(rec["nbytes"])
+    assert hashlib.sha256(img).digest() == rec["sha256"].tobytes()

@@ -45,3 +45,10 @@ cudaError_t tm_launch_env2cells_colony(const tm_envgeom &g, const tm_arrays &a, 
                                        const double *data, const double *grad, double *out, cudaStream_t st);
 cudaError_t tm_launch_field_gradient(const tm_envgeom &g, const int64_t gsize[3], const double *data, double *grad,
                                      cudaStream_t st);
+
+// byte offsets of the binary sections in a VTK file image (tm_vtk.cu)
+struct tm_vtk_layout {
+    long long points, celltypes, ranks, types, density, forces;
+};
+cudaError_t tm_launch_vtk_pack(const tm_arrays &a, long long off, long long n, int rank, const tm_vtk_layout &L,
+                               unsigned char *img, cudaStream_t st);

@@ -1678,3 +1678,57 @@ extern "C" int tmi_field_gradient_host(tm_session *s, const double *data, const 
     CK(cudaStreamSynchronize(s->stream));
     return TM_OK;
 }
+
+// ---------------------------------------------------------------------------
+// VTK file of a colony (writevtk, io.c:372-516, at one rank)
+
+extern "C" int tm_colony_write_vtk(tm_session *s, int id, const char *path, int rank)
+{
+    int rc = lookup(s, id);
+    if (rc) return rc;
+    if (!path) return tm_fail(TM_EINVAL, "null path");
+    const colony_host &c = s->cols[id];
+    const long long n = c.n;
+    // the text of io.c:397-497, in the same order; n stands for globalcount.n
+    char num[64];
+    std::string img;
+    tm_vtk_layout L;
+    img += "# vtk DataFile Version 2.0\nTimothy output\nBINARY\nDATASET UNSTRUCTURED_GRID";
+    snprintf(num, sizeof num, "\nPOINTS %lld float\n", n);
+    img += num;
+    L.points = (long long)img.size();
+    img.append((size_t)(12 * n), '\0');
+    snprintf(num, sizeof num, "\nCELL_TYPES %lld\n", n);
+    img += num;
+    L.celltypes = (long long)img.size();
+    img.append((size_t)(4 * n), '\0');
+    snprintf(num, sizeof num, "\nPOINT_DATA %lld", n);
+    img += num;
+    img += "\nSCALARS rank integer 1\nLOOKUP_TABLE default\n";
+    L.ranks = (long long)img.size();
+    img.append((size_t)(4 * n), '\0');
+    img += "\nSCALARS type integer 1\nLOOKUP_TABLE default\n";
+    L.types = (long long)img.size();
+    img.append((size_t)(4 * n), '\0');
+    img += "\nSCALARS density float 1\nLOOKUP_TABLE default\n";
+    L.density = (long long)img.size();
+    img.append((size_t)(4 * n), '\0');
+    img += "\nVECTORS force float\n";
+    L.forces = (long long)img.size();
+    img.append((size_t)(12 * n), '\0');
+    if (n > 0) {
+        CK(cudaSetDevice(s->device));
+        if ((rc = env_reserve(s, img.size()))) return rc;
+        unsigned char *dimg = (unsigned char *)s->env_buf;
+        CK(cudaMemcpyAsync(dimg, img.data(), img.size(), cudaMemcpyHostToDevice, s->stream));
+        CK(tm_launch_vtk_pack(view(s, s->parity), c.off, n, rank, L, dimg, s->stream));
+        CK(cudaMemcpyAsync(&img[0], dimg, img.size(), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+    }
+    FILE *f = fopen(path, "wb");
+    if (!f) return tm_fail(TM_EINVAL, "cannot open %s for writing", path);
+    const size_t w = fwrite(img.data(), 1, img.size(), f);
+    const int cl = fclose(f);
+    if (w != img.size() || cl != 0) return tm_fail(TM_EINVAL, "writing %s failed", path);
+    return TM_OK;
+}

@@ -301,4 +301,11 @@ class DropinRun:
                 "removecell": self.removecell[:n].copy()}
 
     def shutdown(self):
+        """Release the drop-ins' device session and the page-locking of this run's cells."""
         self.lib.tm_dropin_shutdown()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.shutdown()

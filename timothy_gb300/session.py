@@ -102,6 +102,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "tm_env2cells": (C.c_int, [P, P, P, C.c_int64, C.c_int, P, C.c_float, P, C.c_int, P, P, P, P]),
         "tm_field_gradient": (C.c_int, [P, P, C.c_float, C.c_int, P, P]),
         "tm_colony_env2cells": (C.c_int, [P, C.c_int, P, C.c_float, P, C.c_int, P, P, P]),
+        "tm_colony_write_vtk": (C.c_int, [P, C.c_int, C.c_char_p, C.c_int]),
         "tm_session_bytes": (C.c_int64, [C.POINTER(_Config), C.c_int]),
         "tm_device_memory": (C.c_int, [C.c_int, P, P]),
         "tm_session_get_tuning": (C.c_int, [P, C.POINTER(_Tuning)]),
@@ -349,6 +350,10 @@ class Session:
         _check(load_library().tm_colony_env2cells(self._h, cid, _p(lo), float(resolution), _p(gs), int(nfields),
                                                   _dptr(data), _dptr(gradient), _p(out)))
         return out
+
+    def write_vtk(self, cid: int, path: str, rank: int = 0):
+        """The reference's VTK file of the colony (positions, types, forces of the last step)."""
+        _check(load_library().tm_colony_write_vtk(self._h, cid, str(path).encode(), int(rank)))
 
     # -- tuning -------------------------------------------------------------
     @property
