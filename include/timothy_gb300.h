@@ -156,6 +156,16 @@ int tm_session_list_rate(tm_session *s, double *rate, int64_t *rebuilds);
 /* Add a colony; its id is written to *id.  Uploads the cells. */
 int tm_colony_add(tm_session *s, const tm_colony_input *in, const tm_colony_options *opt, int *id);
 int tm_colony_remove(tm_session *s, int id);
+/* Remove the colony's cells marked for removal (outside the box after an
+ * update), as cellsdeath does at one rank (cells.c:290-336): the survivors
+ * keep their order, and their caller indices close up (cell k of the caller's
+ * order becomes k minus the removed cells before it).  Nothing is removed
+ * from a colony of one cell (cells.c:294).  *removed receives the count. */
+int tm_colony_compact(tm_session *s, int id, int64_t *removed);
+/* Append cells after the colony's current ones (caller indices n, n+1, ...),
+ * as mitosis appends daughters (cells.c:156-205); the colony must have slots
+ * for them (tm_colony_options.reserve).  Lists are rebuilt at the next step. */
+int tm_colony_append(tm_session *s, int id, const tm_colony_input *in);
 /* Replace the cells of an existing colony (at most the slots it holds).  With
  * the same n the cells are taken as the same cells in the same order as the
  * colony's input: they keep their slots, and neighbour lists stay valid unless

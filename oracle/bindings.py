@@ -69,6 +69,8 @@ def load(which: str = "oracle") -> C.CDLL:
         lib.ref_sizeof.argtypes = [C.c_int]
         lib.ref_env2cells.restype = C.c_int64
         lib.ref_env2cells.argtypes = [C.c_int64, C.c_int, _P, _P, _P, _P, C.c_float, C.c_int, _P, _P, C.c_int64, _P]
+        lib.ref_cellsdeath.restype = C.c_int64
+        lib.ref_cellsdeath.argtypes = [C.c_int64, C.c_int64, _P, C.c_int64, C.c_int64, _P]
         lib.ref_write_vtk.restype = C.c_int
         lib.ref_write_vtk.argtypes = [C.c_char_p, C.c_int, C.c_int64, _P, _P, _P, _P, _P, _P, _P]
         lib.ref_fieldgradient.restype = C.c_int64
@@ -258,3 +260,24 @@ def write_vtk(path: str, x, y, z, ctype, fx, fy, fz, *, which: str = "oracle") -
         raise RuntimeError(f"write_vtk ({which}) failed: {rc}")
     with open(out, "rb") as f:
         return f.read()
+
+
+def survivors(n: int, oldlnc: int, removecell, globalcount: int | None = None) -> np.ndarray:
+    """Order of the cells after cellsdeath (cells.c:290-336): the unmarked
+    cells before oldlnc, then every cell appended after it; nothing is
+    removed when the simulation holds one cell."""
+    removecell = np.asarray(removecell, np.uint8)
+    if (globalcount if globalcount is not None else n) == 1:
+        return np.arange(n)
+    head = np.nonzero(removecell[:oldlnc] == 0)[0]
+    return np.concatenate([head, np.arange(oldlnc, n)])
+
+
+def ref_survivors(n: int, oldlnc: int, removecell, globalcount: int | None = None) -> np.ndarray:
+    """The same through the reference's own cellsdeath."""
+    lib = load("ref_strict")
+    rc = np.ascontiguousarray(np.pad(np.asarray(removecell, np.uint8), (0, max(0, n - len(removecell)))))
+    order = np.zeros(max(n, 1), np.int64)
+    m = lib.ref_cellsdeath(n, oldlnc, _ptr(rc), int(rc[:oldlnc].sum()), globalcount if globalcount else n,
+                           _ptr(order))
+    return order[:m]

@@ -21,6 +21,7 @@
 #include "grid.h"
 #include "fieldgradient.h"
 #include "io.h"
+#include "cells.h"
 
 /* defined in octree.c with external linkage (octree.h:24-27) */
 extern double3dv_t affShift;
@@ -413,4 +414,29 @@ int ref_write_vtk(const char *dir, int step, int64_t n, const double *x, const d
     free(ci.forces);
     free(ci.cellsperproc);
     return rc == 0 ? 0 : -1;
+}
+
+/* cellsdeath (cells.c:290-336) on cells tagged by their index: returns the
+ * new cell count and writes the surviving tags in their new order.  oldlnc
+ * is the count before the step's appends; n the count with them. */
+int64_t ref_cellsdeath(int64_t n, int64_t oldlnc, const unsigned char *removecell, int64_t removecount,
+                       int64_t globalcount, int64_t *order)
+{
+    cellsinfo_t ci;
+    int64_t i;
+    memset(&ci, 0, sizeof(ci));
+    ci.localcount.n = (uint64_t)n;
+    ci.globalcount.n = (uint64_t)globalcount;
+    ci.localtypecount = (cellcount_t *)calloc(1, sizeof(cellcount_t));
+    ci.cells = (celldata_t *)calloc((size_t)(n > 0 ? n : 1), sizeof(celldata_t));
+    for (i = 0; i < n; i++) {
+        ci.cells[i].gid = (ZOLTAN_ID_TYPE)i;
+        ci.cells[i].phase = 1;
+    }
+    cellsdeath((int)oldlnc, &ci, (unsigned char *)removecell, removecount);
+    for (i = 0; i < (int64_t)ci.localcount.n; i++) order[i] = (int64_t)ci.cells[i].gid;
+    int64_t m = (int64_t)ci.localcount.n;
+    free(ci.cells);
+    free(ci.localtypecount);
+    return m;
 }

@@ -123,3 +123,13 @@ def test_oracle_vtk_matches_reference(oracle_lib, tmp_path):
                                rec["fy"], rec["fz"], which="oracle")
     assert len(img) == int(rec["nbytes"])
     assert hashlib.sha256(img).digest() == rec["sha256"].tobytes()
+
+
+def test_cellsdeath_rule_matches_reference(oracle_lib):
+    """The survivor order the session's compaction implements is the reference's cellsdeath."""
+    if not oracle_lib.available("ref_strict"):
+        pytest.skip("reference not built here")
+    rng = np.random.default_rng(7)
+    for n, oldlnc in ((200, 200), (200, 150), (1, 1), (60, 5), (30, 30)):
+        rem = (rng.random(oldlnc) < 0.25).astype(np.uint8)
+        assert np.array_equal(oracle_lib.survivors(n, oldlnc, rem), oracle_lib.ref_survivors(n, oldlnc, rem))

@@ -116,6 +116,7 @@ struct tm_session {
     tm_desc *h_desc = nullptr;
     tm_frame *h_frame = nullptr;
     uint32_t *scan_tmp = nullptr;
+    uint32_t *scan_tmp_slots = nullptr;   // scan scratch for slot-sized scans (compaction)
     unsigned long long *d_octsize = nullptr;
     int *d_flag = nullptr;   // set by the upload kernels on a cell type outside the table
     void *d_scratch = nullptr;
@@ -458,12 +459,13 @@ static int session_buffers(tm_session *s, long long S, long long B, long long G,
     AL(a.nbmin, S);
     AL(a.grid, G); AL(a.desc, C + 1); AL(a.frame, C + 1);   // entry C: never active (freed slots)
     AL(s->scan_tmp, tm_scan_tmp_words(B + 1)); AL(s->d_octsize, C); AL(s->dK, 1); AL(s->d_flag, 1);
+    AL(s->scan_tmp_slots, tm_scan_tmp_words(S + 1));
     {
-        double *scratch = nullptr;
-        AL(scratch, S);
+        double *scratch = nullptr;        // S + 1 doubles: also two (S + 1)-word scans
+        AL(scratch, S + 1);
         s->d_scratch = scratch;
         double *scratch2 = nullptr;
-        AL(scratch2, S);
+        AL(scratch2, S + 1);
         s->d_scratch2 = scratch2;
     }
     if (cfg->diagnostics) {
@@ -616,7 +618,7 @@ extern "C" int tm_session_destroy(tm_session *s)
     void *ptrs[] = {a.x, a.y, a.z, a.size, a.young, a.ctype, a.phase, a.perm, a.rem, a.x2, a.y2, a.z2, a.size2,
                     a.young2, a.ctype2, a.phase2, a.perm2, a.rem2, a.col, a.code, a.codes, a.bin, a.tmp, a.rank, a.hi, a.lo, a.vlist, a.vcount, a.x0,
                     a.mass, a.bin_count, a.bin_cursor, a.bin_start, a.bigbins, a.fix_count, a.fix_list, a.walk_list, a.density, a.v, a.mindist, a.fx,
-                    a.fy, a.fz, a.nbcount, a.nbmin, a.nbhash, a.vcand, a.grid, a.desc, a.frame, s->scan_tmp, s->d_octsize,
+                    a.fy, a.fz, a.nbcount, a.nbmin, a.nbhash, a.vcand, a.grid, a.desc, a.frame, s->scan_tmp, s->scan_tmp_slots, s->d_octsize,
                     s->dK, s->d_scratch, s->d_scratch2, s->d_flag};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -1730,5 +1732,185 @@ extern "C" int tm_colony_write_vtk(tm_session *s, int id, const char *path, int 
     const size_t w = fwrite(img.data(), 1, img.size(), f);
     const int cl = fclose(f);
     if (w != img.size() || cl != 0) return tm_fail(TM_EINVAL, "writing %s failed", path);
+    return TM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// death compaction and appends (cellsdeath, cells.c:290-336, and the
+// appends of mitosis, cells.c:124-205, for resident colonies)
+
+// keep flags in caller order and in slot order
+__global__ void k_keep_flags(tm_arrays a, long long off, int n, uint32_t *keep_caller, uint32_t *keep_slot)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k > n) return;
+    if (k == n) {                              // one past the end: the scans' totals
+        keep_caller[n] = 0;
+        keep_slot[n] = 0;
+        return;
+    }
+    const uint32_t keep = a.rem[off + k] ? 0u : 1u;
+    keep_caller[a.perm[off + k]] = keep;
+    keep_slot[k] = keep;
+}
+
+// survivors move to their compacted slot (scratch copies), with their new
+// caller index; every per-cell field moves with the cell
+__global__ void k_compact_gather(tm_arrays a, long long off, int n, const uint32_t *new_caller,
+                                 const uint32_t *new_slot, double *ob)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const long long s = off + k;
+    if (a.rem[s]) return;
+    const long long d = off + new_slot[k];
+    a.x2[d] = a.x[s];
+    a.y2[d] = a.y[s];
+    a.z2[d] = a.z[s];
+    a.size2[d] = a.size[s];
+    a.young2[d] = a.young[s];
+    a.ctype2[d] = a.ctype[s];
+    a.phase2[d] = a.phase[s];
+    a.perm2[d] = (int)new_caller[a.perm[s]];
+    a.rem2[d] = 0;
+    // outputs, 7 values per cell, into ob (slot-indexed from off)
+    const long long o = (long long)new_slot[k] * 7;
+    ob[o + 0] = a.density[s];
+    ob[o + 1] = a.v[s];
+    ob[o + 2] = a.mindist[s];
+    ob[o + 3] = a.fx[s];
+    ob[o + 4] = a.fy[s];
+    ob[o + 5] = a.fz[s];
+    ob[o + 6] = (double)a.nbcount[s];
+}
+
+__global__ void k_compact_scatter(tm_arrays a, long long off, int m, const double *ob)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m) return;
+    const long long s = off + k;
+    a.x[s] = a.x2[s];
+    a.y[s] = a.y2[s];
+    a.z[s] = a.z2[s];
+    a.size[s] = a.size2[s];
+    a.young[s] = a.young2[s];
+    a.ctype[s] = a.ctype2[s];
+    a.phase[s] = a.phase2[s];
+    a.perm[s] = a.perm2[s];
+    a.rem[s] = 0;
+    const double *o = ob + k * 7;
+    a.density[s] = o[0];
+    a.v[s] = o[1];
+    a.mindist[s] = o[2];
+    a.fx[s] = o[3];
+    a.fy[s] = o[4];
+    a.fz[s] = o[5];
+    a.nbcount[s] = (int)o[6];
+}
+
+__global__ void k_force_rebuild_one(tm_frame *frame, int c)
+{
+    frame[c].force_rebuild = 1;   // slots changed: the lists are rebuilt at the next step
+    frame[c].list_ok = 0;
+}
+
+extern "C" int tm_colony_compact(tm_session *s, int id, int64_t *removed)
+{
+    int rc = lookup(s, id);
+    if (rc) return rc;
+    colony_host &c = s->cols[id];
+    if (removed) *removed = 0;
+    // cells.c:294: with a single cell in the simulation nothing is removed
+    if (c.n <= 1) return TM_OK;
+    CK(cudaSetDevice(s->device));
+    const tm_arrays a = view(s, s->parity);
+    const int n = c.n;
+    uint32_t *keep_caller = (uint32_t *)s->d_scratch;          // n + 1 words
+    uint32_t *new_caller = keep_caller + (n + 1);               // n + 1 words (d_scratch holds 2 S words)
+    uint32_t *keep_slot = (uint32_t *)s->d_scratch2;
+    uint32_t *new_slot = keep_slot + (n + 1);
+    if ((rc = env_reserve(s, (size_t)n * 7 * sizeof(double)))) return rc;
+    cudaStream_t st = s->stream;
+    k_keep_flags<<<blocks_for(n + 1, 256), 256, 0, st>>>(a, c.off, n, keep_caller, keep_slot);
+    CK(cudaGetLastError());
+    CK(tm_scan_exclusive(keep_caller, new_caller, n + 1, s->scan_tmp_slots, st));
+    CK(tm_scan_exclusive(keep_slot, new_slot, n + 1, s->scan_tmp_slots, st));
+    uint32_t survivors = 0;
+    CK(cudaMemcpyAsync(&survivors, new_slot + n, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if ((int)survivors == n) return TM_OK;
+    k_compact_gather<<<blocks_for(n, 256), 256, 0, st>>>(a, c.off, n, new_caller, new_slot, s->env_buf);
+    k_compact_scatter<<<blocks_for(survivors, 256), 256, 0, st>>>(a, c.off, (int)survivors, s->env_buf);
+    k_force_rebuild_one<<<1, 1, 0, st>>>(a.frame, id);
+    CK(cudaGetLastError());
+    c.n = (int)survivors;
+    s->h_desc[id].n = c.n;
+    if ((rc = push_desc(s, id))) return rc;
+    CK(cudaStreamSynchronize(st));
+    drop_graphs(s);
+    if (removed) *removed = n - (int)survivors;
+    return TM_OK;
+}
+
+__global__ void k_append_init(tm_arrays a, long long off, int n0, int m, int has_phase, const tm_consts *K, int *bad)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m) return;
+    const long long s = off + n0 + k;
+    a.perm[s] = n0 + (int)k;
+    a.rem[s] = 0;
+    if (!has_phase) a.phase[s] = 1;
+    const int ct = a.ctype[s];
+    if (ct < 0 || ct >= K->ntypes) {
+        atomicExch(bad, 1);
+        a.ctype[s] = 0;
+    }
+    a.density[s] = 0.0;
+    a.v[s] = 0.0;
+    a.mindist[s] = 0.0;
+    a.fx[s] = 0.0;
+    a.fy[s] = 0.0;
+    a.fz[s] = 0.0;
+    a.nbcount[s] = 0;
+    a.nbmin[s] = -1;
+}
+
+extern "C" int tm_colony_append(tm_session *s, int id, const tm_colony_input *in)
+{
+    int rc = lookup(s, id);
+    if (rc) return rc;
+    rc = check_input(s, in, false);
+    if (rc) return rc;
+    colony_host &c = s->cols[id];
+    const long long m = in->n;
+    if (m == 0) return TM_OK;
+    if (c.n + m > c.nslots)
+        return tm_fail(TM_ENOMEM, "colony %d holds %d slots; %d cells plus %lld appended do not fit", id, c.nslots,
+                       c.n, m);
+    CK(cudaSetDevice(s->device));
+    const tm_arrays a = view(s, s->parity);
+    cudaStream_t st = s->stream;
+    const long long o = c.off + c.n;
+    const size_t n = (size_t)m;
+    CK(cudaMemsetAsync(s->d_flag, 0, sizeof(int), st));
+    CK(cudaMemcpyAsync(a.x + o, in->x, n * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(a.y + o, in->y, n * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(a.z + o, in->z, n * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(a.size + o, in->size, n * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(a.young + o, in->young, n * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(a.ctype + o, in->ctype, n * 4, cudaMemcpyHostToDevice, st));
+    if (in->phase) CK(cudaMemcpyAsync(a.phase + o, in->phase, n * 4, cudaMemcpyHostToDevice, st));
+    k_append_init<<<blocks_for(m, 256), 256, 0, st>>>(a, c.off, c.n, (int)m, in->phase ? 1 : 0, s->dK, s->d_flag);
+    k_force_rebuild_one<<<1, 1, 0, st>>>(a.frame, id);
+    CK(cudaGetLastError());
+    int bad = 0;
+    CK(cudaMemcpyAsync(&bad, s->d_flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    c.n += (int)m;
+    s->h_desc[id].n = c.n;
+    if ((rc = push_desc(s, id))) return rc;
+    CK(cudaStreamSynchronize(st));
+    drop_graphs(s);
+    if (bad) return tm_fail(TM_EDEVICE, "an appended cell type lies outside 0..%d (set to 0)", s->K.ntypes - 1);
     return TM_OK;
 }

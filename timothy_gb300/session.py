@@ -103,6 +103,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "tm_field_gradient": (C.c_int, [P, P, C.c_float, C.c_int, P, P]),
         "tm_colony_env2cells": (C.c_int, [P, C.c_int, P, C.c_float, P, C.c_int, P, P, P]),
         "tm_colony_write_vtk": (C.c_int, [P, C.c_int, C.c_char_p, C.c_int]),
+        "tm_colony_compact": (C.c_int, [P, C.c_int, P]),
+        "tm_colony_append": (C.c_int, [P, C.c_int, C.POINTER(_Input)]),
         "tm_session_bytes": (C.c_int64, [C.POINTER(_Config), C.c_int]),
         "tm_device_memory": (C.c_int, [C.c_int, P, P]),
         "tm_session_get_tuning": (C.c_int, [P, C.POINTER(_Tuning)]),
@@ -261,6 +263,21 @@ class Session:
             self._n[cid] = col.n
         elif rc == -4:      # a cell type outside the table: the colony was left empty
             self._n[cid] = 0
+        _check(rc)
+
+    def compact(self, cid: int) -> int:
+        """Remove the cells marked for removal (cellsdeath); returns how many."""
+        r = np.zeros(1, np.int64)
+        _check(load_library().tm_colony_compact(self._h, cid, _p(r)))
+        self._n[cid] -= int(r[0])
+        return int(r[0])
+
+    def append(self, cid: int, col: Colony):
+        """Append cells after the colony's current ones (needs reserved slots)."""
+        inp, keep = self._input(col)
+        rc = load_library().tm_colony_append(self._h, cid, C.byref(inp))
+        if rc in (0, -4):
+            self._n[cid] += col.n
         _check(rc)
 
     def set_active(self, cid: int, active: bool):
