@@ -59,6 +59,9 @@ def load(which: str = "oracle") -> C.CDLL:
         lib.tmo_fieldgradient.argtypes = [C.c_int, C.c_float, C.c_int, _P, _P, _P]
         lib.tmo_write_vtk.restype = C.c_int
         lib.tmo_write_vtk.argtypes = [C.c_char_p, C.c_int64, _P, _P, _P, _P, _P, _P, _P, C.c_int]
+        lib.tmo_cellcycle.restype = C.c_int
+        lib.tmo_cellcycle.argtypes = [C.c_int64, C.c_int] + [_P] * 8 + [C.c_int, _P, _P, C.c_int, C.c_float, _P, _P,
+                                                                         C.c_int64] + [_P] * 16 + [C.c_int64, _P, _P]
         lib.tmo_neighbours.restype = C.c_int
         lib.tmo_neighbours.argtypes = [C.c_int64, C.c_int, C.c_int, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
                                        C.c_int]
@@ -69,6 +72,10 @@ def load(which: str = "oracle") -> C.CDLL:
         lib.ref_sizeof.argtypes = [C.c_int]
         lib.ref_env2cells.restype = C.c_int64
         lib.ref_env2cells.argtypes = [C.c_int64, C.c_int, _P, _P, _P, _P, C.c_float, C.c_int, _P, _P, C.c_int64, _P]
+        lib.ref_cellcycle.restype = C.c_int
+        lib.ref_cellcycle.argtypes = [C.c_int64, C.c_int, C.c_int] + [_P] * 8 + [C.c_int, _P, _P, C.c_int, C.c_float,
+                                                                                 C.c_uint, _P] + [_P] * 16 + \
+            [C.c_int64, _P]
         lib.ref_cellsdeath.restype = C.c_int64
         lib.ref_cellsdeath.argtypes = [C.c_int64, C.c_int64, _P, C.c_int64, C.c_int64, _P]
         lib.ref_write_vtk.restype = C.c_int
@@ -281,3 +288,68 @@ def ref_survivors(n: int, oldlnc: int, removecell, globalcount: int | None = Non
     m = lib.ref_cellsdeath(n, oldlnc, _ptr(rc), int(rc[:oldlnc].sum()), globalcount if globalcount else n,
                            _ptr(order))
     return order[:m]
+
+
+CYCLE_STATE = (("phase", np.int32), ("phasetime", np.float32), ("g1", np.float32), ("s", np.float32),
+               ("g2", np.float32), ("m", np.float32), ("age", np.int32), ("size", np.float64),
+               ("young", np.float32), ("x", np.float64), ("y", np.float64), ("z", np.float64),
+               ("density", np.float64), ("ctype", np.int32))
+
+
+def libc_draws(seed: int, count: int) -> np.ndarray:
+    """The first count values of the C library's rand() after srand(seed)."""
+    libc = C.CDLL(None)
+    libc.rand.restype = C.c_int
+    libc.srand.argtypes = [C.c_uint]
+    libc.srand(seed)
+    return np.array([libc.rand() for _ in range(count)], np.int32)
+
+
+def cellcycle(state: dict, types: dict, *, dim: int = 3, nfields: int = 0, envvalue=None, cl1=None, cl2=None,
+              simulationstart: int = 1, sps: float = 3600.0, seed: int = 1, cap: int | None = None,
+              removecell=None, which: str = "oracle", draws=None) -> dict:
+    """updatecellcycles with mitosis on caller-ordered cells.
+
+    state: arrays named as in CYCLE_STATE; types: per-type g1, s, g2, m, v, rd,
+    cd (criticaldensity) float arrays and size (float64).  The oracle takes its
+    draws from the C library's rand() after srand(seed) (or from draws); the
+    reference calls rand() itself.  Returns the new state (daughters appended),
+    removecell, removecount, and, for the oracle, the draws used."""
+    lib = load(which)
+    n = len(state["phase"])
+    cap = cap or 2 * n + 1
+    st = {k: np.zeros(cap, dt) for k, dt in CYCLE_STATE}
+    for k, dt in CYCLE_STATE:
+        st[k][:n] = np.asarray(state[k], dt)
+    rem = np.zeros(cap, np.uint8)
+    if removecell is not None:
+        rem[:n] = removecell
+    ntypes = len(types["g1"])
+    ty = [np.ascontiguousarray(types[k], np.float32) for k in ("g1", "s", "g2", "m", "v", "rd", "cd")]
+    tsize = np.ascontiguousarray(types["size"], np.float64)
+    nf = int(nfields)
+    env = np.ascontiguousarray(envvalue if envvalue is not None else np.zeros(max(nf, 1) * max(n, 1)), np.float64)
+    c1 = np.ascontiguousarray(cl1 if cl1 is not None else np.zeros(max(ntypes * nf, 1)), np.float32)
+    c2 = np.ascontiguousarray(cl2 if cl2 is not None else np.zeros(max(ntypes * nf, 1)), np.float32)
+    rc_count = C.c_int64(0)
+    nout = C.c_int64(0)
+    arrays = [_ptr(st[k]) for k, _ in CYCLE_STATE]
+    out = {}
+    if which == "oracle":
+        dr = np.ascontiguousarray(draws if draws is not None else libc_draws(seed, 13 * n + 16), np.int32)
+        used = C.c_int64(0)
+        rc = lib.tmo_cellcycle(n, dim, *[_ptr(a) for a in ty], _ptr(tsize), nf, _ptr(c1), _ptr(c2),
+                               simulationstart, sps, _ptr(env), _ptr(dr), len(dr), *arrays, _ptr(rem),
+                               C.byref(rc_count), cap, C.byref(nout), C.byref(used))
+        out["draws_used"] = int(used.value)
+    else:
+        rc = lib.ref_cellcycle(n, dim, ntypes, *[_ptr(a) for a in ty], _ptr(tsize), nf, _ptr(c1), _ptr(c2),
+                               simulationstart, sps, seed, _ptr(env), *arrays, _ptr(rem), C.byref(rc_count), cap,
+                               C.byref(nout))
+    if rc:
+        raise RuntimeError(f"cellcycle ({which}) failed: {rc}")
+    m = int(nout.value)
+    out.update({k: st[k][:m].copy() for k, _ in CYCLE_STATE})
+    out["removecell"] = rem[:m].copy()
+    out["removecount"] = int(rc_count.value)
+    return out

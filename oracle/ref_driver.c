@@ -440,3 +440,105 @@ int64_t ref_cellsdeath(int64_t n, int64_t oldlnc, const unsigned char *removecel
     free(ci.localtypecount);
     return m;
 }
+
+/* updatecellcycles (cells.c:370-523), with mitosis (cells.c:124-205), on
+ * structure-of-arrays cells, after srand(seed).  The arrays hold room for
+ * cap cells: daughters are appended at [n, *nout).  mitosis reads
+ * cellsinfo->velocity (cells.c:134) only to overwrite the value, so a zeroed
+ * array stands in for the one the reference never allocates. */
+int updatecellcycles(systeminfo_t systeminfo, settings_t settings, celltype_t *celltype, cellsinfo_t *cellsinfo,
+                     cellenvdata_t **cellenvdata, unsigned char *removecell, int64_t *removecount);
+
+int ref_cellcycle(int64_t n, int dim, int ntypes, const float *tg1, const float *ts, const float *tg2,
+                  const float *tm, const float *tv, const float *trd, const float *tcd, const double *tsize,
+                  int nfields, const float *cl1, const float *cl2, int simulationstart, float sps, unsigned seed,
+                  const double *envvalue, int *phase, float *phasetime, float *g1, float *s, float *g2, float *m,
+                  int *age, double *size, float *young, double *x, double *y, double *z, double *density, int *ctype,
+                  unsigned char *removecell, int64_t *removecount, int64_t cap, int64_t *nout)
+{
+    systeminfo_t si;
+    settings_t st;
+    cellsinfo_t ci;
+    celltype_t *ct = (celltype_t *)calloc((size_t)ntypes, sizeof(celltype_t));
+    cellenvdata_t **ce = (cellenvdata_t **)calloc((size_t)(nfields > 0 ? nfields : 1), sizeof(cellenvdata_t *));
+    int64_t i;
+    int t, f;
+    memset(&si, 0, sizeof(si));
+    memset(&st, 0, sizeof(st));
+    memset(&ci, 0, sizeof(ci));
+    si.rank = 0;
+    si.size = 1;
+    st.dimension = dim;
+    st.numberoffields = nfields;
+    st.numberofcelltypes = ntypes;
+    st.simulationstart = simulationstart;
+    st.secondsperstep = sps;
+    st.maxlocalcells = cap;
+    for (t = 0; t < ntypes; t++) {
+        ct[t].g1 = tg1[t];
+        ct[t].s = ts[t];
+        ct[t].g2 = tg2[t];
+        ct[t].m = tm[t];
+        ct[t].v = tv[t];
+        ct[t].rd = trd[t];
+        ct[t].criticaldensity = tcd[t];
+        ct[t].size = tsize[t];
+        ct[t].criticallevel1 = (float *)cl1 + (size_t)t * (size_t)nfields;
+        ct[t].criticallevel2 = (float *)cl2 + (size_t)t * (size_t)nfields;
+    }
+    for (f = 0; f < nfields; f++) {
+        ce[f] = (cellenvdata_t *)calloc((size_t)(n > 0 ? n : 1), sizeof(cellenvdata_t));
+        for (i = 0; i < n; i++) ce[f][i].value = envvalue[(size_t)f * (size_t)n + (size_t)i];
+    }
+    ci.dimension = dim;
+    ci.localcount.n = (uint64_t)n;
+    ci.globalcount.n = (uint64_t)n;
+    ci.localtypecount = (cellcount_t *)calloc((size_t)ntypes, sizeof(cellcount_t));
+    ci.cells = (celldata_t *)calloc((size_t)cap, sizeof(celldata_t));
+    ci.velocity = (double3dv_t *)calloc((size_t)cap, sizeof(double3dv_t));
+    for (i = 0; i < n; i++) {
+        celldata_t *c = &ci.cells[i];
+        c->phase = phase[i];
+        c->phasetime = phasetime[i];
+        c->g1 = g1[i];
+        c->s = s[i];
+        c->g2 = g2[i];
+        c->m = m[i];
+        c->age = age[i];
+        c->size = size[i];
+        c->young = young[i];
+        c->x = x[i];
+        c->y = y[i];
+        c->z = z[i];
+        c->density = density[i];
+        c->ctype = ctype[i];
+        c->gid = (ZOLTAN_ID_TYPE)i;
+    }
+    srand(seed);
+    updatecellcycles(si, st, ct, &ci, ce, removecell, removecount);
+    *nout = (int64_t)ci.localcount.n;
+    for (i = 0; i < *nout; i++) {
+        const celldata_t *c = &ci.cells[i];
+        phase[i] = c->phase;
+        phasetime[i] = c->phasetime;
+        g1[i] = c->g1;
+        s[i] = c->s;
+        g2[i] = c->g2;
+        m[i] = c->m;
+        age[i] = c->age;
+        size[i] = c->size;
+        young[i] = c->young;
+        x[i] = c->x;
+        y[i] = c->y;
+        z[i] = c->z;
+        density[i] = c->density;
+        ctype[i] = c->ctype;
+    }
+    for (f = 0; f < nfields; f++) free(ce[f]);
+    free(ce);
+    free(ci.cells);
+    free(ci.velocity);
+    free(ci.localtypecount);
+    free(ct);
+    return 0;
+}

@@ -9,6 +9,7 @@
  *   - position update + removal marks         cells.c:41-58, 342-365
  *   - grid -> cell gather, field gradient     patches.c:512-593, fieldgradient.c:149-225
  *   - VTK writer                              io.c:372-516
+ *   - cell cycle and mitosis                  cells.c:124-205, 370-523
  *   - CIC deposit at one rank                 grid.c:37-136, patches.c:47-234,
  *                                             patches.c:321-367
  * Expressions keep the reference's evaluation order (C left-to-right
@@ -554,6 +555,128 @@ int tmo_fieldgradient(int dim, float gfh, int nfields, const double *data, doubl
                 }
     }
     return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* cell cycle                                                                 */
+/* ------------------------------------------------------------------------ */
+
+#define TMO_RAND_MAX 2147483647
+
+/* (float)rand()/RAND_MAX with the draw r, as the reference forms it */
+static float tmo_frand(int r) { return (float)r / TMO_RAND_MAX; }
+
+/* updatecellcycles, cells.c:370-523, with mitosis, cells.c:124-205: the
+ * random draws are taken from draws[] in the order the reference calls
+ * rand() (death at G1->S and G2->M; at mitosis three (two in 2-D) shift
+ * components, the parent's g1, g2, s, m, the daughter's young and the
+ * daughter's g1, g2, s, m).  mitosis's read of the unallocated velocity
+ * (cells.c:134) is left out: its value is overwritten before use.  Daughters
+ * are appended after the n cells (caller arrays hold cap entries); *nout is
+ * the new count, *ndraws the draws used.  Returns 0, or -1 when cap is too
+ * small. */
+int tmo_cellcycle(int64_t n, int dim, const float *tg1, const float *ts, const float *tg2, const float *tm,
+                  const float *tv, const float *trd, const float *tcd, const double *tsize, int nfields,
+                  const float *cl1, const float *cl2, int simulationstart, float sps, const double *envvalue,
+                  const int *draws, int64_t ndraws_cap, int *phase, float *phasetime, float *g1, float *s, float *g2,
+                  float *m, int *age, double *size, float *young, double *x, double *y, double *z, double *density,
+                  int *ctype, unsigned char *removecell, int64_t *removecount, int64_t cap, int64_t *nout,
+                  int64_t *ndraws)
+{
+    int64_t nn = n, k = 0;
+    const double shrink = pow(2.0, -(1.0 / 3.0));
+#define DRAW() (k < ndraws_cap ? draws[k++] : (k++, 0))
+    for (int64_t c = 0; c < n; c++) {
+        const int t = ctype[c];
+        const double eps = tcd[t], csize = tsize[t], rd = trd[t];
+        if (removecell[c]) continue;
+        int low1 = 0, low2 = 0;
+        for (int f = 0; f < nfields; f++) {
+            const double val = envvalue[(size_t)f * (size_t)n + (size_t)c];
+            if (val < cl1[t * nfields + f]) { low1 = 1; break; }
+            if (val < cl2[t * nfields + f]) { low2 = 1; break; }
+        }
+        if (!simulationstart) continue;
+        if (phase[c] != 0 && density[c] <= eps) phasetime[c] += sps / 3600.0;
+        switch (phase[c]) {
+        case 0:
+            if (low2) { phase[c] = 5; phasetime[c] = 0; break; }
+            if (density[c] <= eps || n == 1 || !low1) phase[c] = 1;
+            break;
+        case 1:
+            if (density[c] > eps || low1) {
+                if (low2) { phase[c] = 5; phasetime[c] = 0; }
+                else phase[c] = 0;
+                break;
+            }
+            if (size[c] < csize) size[c] += (csize - shrink * csize) * (sps) / (3600.0 * g1[c]);
+            if (size[c] > csize) size[c] = csize;
+            if (phasetime[c] >= g1[c]) {
+                phase[c] = 2;
+                phasetime[c] = 0;
+                if (tmo_frand(DRAW()) < rd && removecell[c] == 0) { removecell[c] = 1; (*removecount)++; }
+            }
+            break;
+        case 2:
+            if (low2) { phase[c] = 5; phasetime[c] = 0; break; }
+            if (phasetime[c] >= s[c]) { phase[c] = 3; phasetime[c] = 0; }
+            break;
+        case 3:
+            if (low2) { phase[c] = 5; phasetime[c] = 0; break; }
+            if (phasetime[c] >= g2[c]) {
+                phase[c] = 4;
+                phasetime[c] = 0;
+                if (tmo_frand(DRAW()) < rd && removecell[c] == 0) { removecell[c] = 1; (*removecount)++; }
+            }
+            break;
+        case 4:
+            if (low2) { phase[c] = 5; phasetime[c] = 0; }
+            else if (phasetime[c] >= m[c]) {
+                if (nn + 1 > cap) return -1;
+                double sh[3];
+                sh[0] = ((double)DRAW() / TMO_RAND_MAX) * 2.0 - 1.0;
+                sh[1] = ((double)DRAW() / TMO_RAND_MAX) * 2.0 - 1.0;
+                sh[2] = dim == 3 ? ((double)DRAW() / TMO_RAND_MAX) * 2.0 - 1.0 : 0.0;
+                double sc = sqrt(sh[0] * sh[0] + sh[1] * sh[1] + sh[2] * sh[2]);
+                sc = size[c] / (2 * sc);
+                for (int q = 0; q < 3; q++) sh[q] = sc * sh[q];
+                const int64_t d = nn;
+                x[d] = x[c] + sh[0];
+                y[d] = y[c] + sh[1];
+                z[d] = z[c] + sh[2];
+                size[d] = shrink * size[c];
+                ctype[d] = ctype[c];
+                age[d] = age[c] + 1;
+                x[c] -= sh[0];
+                y[c] -= sh[1];
+                z[c] -= sh[2];
+                size[c] = size[d];
+                age[c] += 1;
+                g1[c] = tg1[t] * (1 + ((tmo_frand(DRAW())) * 2.0 - 1.0) * tv[t]);
+                g2[c] = tg2[t] * (1 + ((tmo_frand(DRAW())) * 2.0 - 1.0) * tv[t]);
+                s[c] = ts[t] * (1 + ((tmo_frand(DRAW())) * 2.0 - 1.0) * tv[t]);
+                m[c] = tm[t] * (1 + ((tmo_frand(DRAW())) * 2.0 - 1.0) * tv[t]);
+                density[d] = density[c];
+                young[d] = 2100.0 + ((tmo_frand(DRAW())) * 2.0 - 1.0) * 100.0;
+                phase[d] = 1;
+                phasetime[d] = 0.0f;
+                removecell[d] = 0;
+                /* the daughter's own v is 0 (cells.c:184), so its draws do not change its lengths */
+                g1[d] = tg1[t] * (1 + ((tmo_frand(DRAW())) * 2.0 - 1.0) * 0.0);
+                g2[d] = tg2[t] * (1 + ((tmo_frand(DRAW())) * 2.0 - 1.0) * 0.0);
+                s[d] = ts[t] * (1 + ((tmo_frand(DRAW())) * 2.0 - 1.0) * 0.0);
+                m[d] = tm[t] * (1 + ((tmo_frand(DRAW())) * 2.0 - 1.0) * 0.0);
+                nn++;
+                phase[c] = 1;
+                phasetime[c] = 0;
+            }
+            break;
+        }
+    }
+#undef DRAW
+    *nout = nn;
+    *ndraws = k;
+    return k > ndraws_cap ? -2 : 0;
 }
 
 /* ------------------------------------------------------------------------ */

@@ -76,6 +76,16 @@ int tmo_env2cells(int64_t n, int dim, const double *x, const double *y, const do
  * the one-rank grid of resolution gfh; dims receives the grid size. */
 int tmo_fieldgradient(int dim, float gfh, int nfields, const double *data, double *gradient, int64_t *dims);
 
+/* updatecellcycles with mitosis on caller-ordered arrays (room for cap
+ * cells), the rand() values taken from draws[]; see tm_oracle.c. */
+int tmo_cellcycle(int64_t n, int dim, const float *tg1, const float *ts, const float *tg2, const float *tm,
+                  const float *tv, const float *trd, const float *tcd, const double *tsize, int nfields,
+                  const float *cl1, const float *cl2, int simulationstart, float sps, const double *envvalue,
+                  const int *draws, int64_t ndraws_cap, int *phase, float *phasetime, float *g1, float *s, float *g2,
+                  float *m, int *age, double *size, float *young, double *x, double *y, double *z, double *density,
+                  int *ctype, unsigned char *removecell, int64_t *removecount, int64_t cap, int64_t *nout,
+                  int64_t *ndraws);
+
 /* writevtk at one rank: the legacy binary VTK file of the cells (caller
  * order) with their forces.  Returns 0 or a negative code. */
 int tmo_write_vtk(const char *path, int64_t n, const double *x, const double *y, const double *z, const int *ctype,

@@ -9,6 +9,7 @@ nodes (always including the faces) plus per-component sums.
 
     python tests/golden/make_golden_fields.py          # gather and gradient
     python tests/golden/make_golden_fields.py --vtk    # the VTK writer
+    python tests/golden/make_golden_fields.py --cycle  # the cell cycle
 """
 from __future__ import annotations
 
@@ -91,8 +92,43 @@ def make_vtk():
     print("field_vtk_clustered3k", len(img))
 
 
+CYCLE_TYPES = dict(g1=np.array([11.0, 9.0], np.float32), s=np.array([8.0, 7.0], np.float32),
+                   g2=np.array([4.0, 3.0], np.float32), m=np.array([1.0, 1.5], np.float32),
+                   v=np.array([0.2, 0.1], np.float32), rd=np.array([0.1, 0.3], np.float32),
+                   cd=np.array([2.0, 3.0], np.float32), size=np.array([1.0, 0.9]))
+CYCLE_CL1 = np.array([0.3, 0.2, 0.25, 0.1], np.float32)     # [type][field]
+CYCLE_CL2 = np.array([0.1, 0.05, 0.1, 0.02], np.float32)
+
+
+def cycle_state(n, seed):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return dict(phase=rng.integers(0, 6, n), phasetime=rng.uniform(0, 12, n), g1=rng.uniform(8, 12, n),
+                s=rng.uniform(6, 9, n), g2=rng.uniform(2, 5, n), m=rng.uniform(0.5, 2, n), age=rng.integers(0, 5, n),
+                size=rng.uniform(0.7, 1.0, n), young=rng.uniform(2000, 2200, n), x=rng.normal(size=n),
+                y=rng.normal(size=n), z=rng.normal(size=n), density=rng.uniform(0, 4, n),
+                ctype=rng.integers(0, 2, n)), rng.uniform(0, 1, 2 * n), (rng.random(n) < 0.05).astype(np.uint8)
+
+
+def make_cycle():
+    """updatecellcycles with mitosis (cells.c:124-205, 370-523), the reference
+    drawing from rand() after srand(seed); inputs and outputs of each case."""
+    for name, dim, seed in (("field_cycle_3d", 3, 21), ("field_cycle_2d", 2, 22)):
+        st, env, rem = cycle_state(3000, seed)
+        if dim == 2:
+            st["z"] = np.zeros(3000)
+        out = B.cellcycle(st, CYCLE_TYPES, dim=dim, nfields=2, envvalue=env, cl1=CYCLE_CL1, cl2=CYCLE_CL2,
+                          sps=3600.0, seed=seed, removecell=rem, which="ref_strict")
+        rec = {"dim": dim, "seed": seed, "env": env, "rem": rem}
+        rec.update({"in_" + k: v for k, v in st.items()})
+        rec.update({"out_" + k: np.asarray(v) for k, v in out.items()})
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **rec)
+        print(name, len(out["phase"]), out["removecount"])
+
+
 if __name__ == "__main__":
     if "--vtk" in sys.argv:
         make_vtk()
+    elif "--cycle" in sys.argv:
+        make_cycle()
     else:
         main()

@@ -133,3 +133,22 @@ def test_cellsdeath_rule_matches_reference(oracle_lib):
     for n, oldlnc in ((200, 200), (200, 150), (1, 1), (60, 5), (30, 30)):
         rem = (rng.random(oldlnc) < 0.25).astype(np.uint8)
         assert np.array_equal(oracle_lib.survivors(n, oldlnc, rem), oracle_lib.ref_survivors(n, oldlnc, rem))
+
+
+@pytest.mark.parametrize("name", ["field_cycle_3d", "field_cycle_2d"])
+def test_oracle_cellcycle_matches_reference(oracle_lib, name):
+    """updatecellcycles with mitosis: the restatement, fed the C library's
+    rand() stream after the same srand(), reproduces the reference's cells."""
+    import sys
+
+    sys.path.insert(0, GOLDEN)
+    from make_golden_fields import CYCLE_CL1, CYCLE_CL2, CYCLE_TYPES
+
+    rec = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    st = {k[3:]: rec[k] for k in rec.files if k.startswith("in_")}
+    out = oracle_lib.cellcycle(st, CYCLE_TYPES, dim=int(rec["dim"]), nfields=2, envvalue=rec["env"], cl1=CYCLE_CL1,
+                               cl2=CYCLE_CL2, sps=3600.0, seed=int(rec["seed"]), removecell=rec["rem"],
+                               which="oracle")
+    for k in rec.files:
+        if k.startswith("out_"):
+            assert np.array_equal(np.asarray(out[k[4:]]), rec[k]), k
