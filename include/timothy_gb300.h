@@ -166,6 +166,43 @@ int tm_colony_compact(tm_session *s, int id, int64_t *removed);
  * as mitosis appends daughters (cells.c:156-205); the colony must have slots
  * for them (tm_colony_options.reserve).  Lists are rebuilt at the next step. */
 int tm_colony_append(tm_session *s, int id, const tm_colony_input *in);
+/* Cell-cycle parameters of one cell type (celltype_t, global.h:315-335). */
+typedef struct tm_cycle_type {
+    float g1, s, g2, m;       /* phase lengths (hours) */
+    float v;                  /* relative spread of the lengths drawn at division */
+    float rd;                 /* death probability at G1->S and G2->M */
+    float criticaldensity;    /* growth stops above it */
+} tm_cycle_type;
+
+/* One cell-cycle step (updatecellcycles, cells.c:370-523, with mitosis,
+ * cells.c:124-205) for a colony.  draw supplies the random values in the
+ * order the reference calls rand() (NULL: the C library's rand()); to follow
+ * a reference run exactly, the generator first skips the values the
+ * reference's updatepositions takes (2 or 3 per cell, cells.c:353-355). */
+typedef struct tm_cycle_params {
+    const tm_cycle_type *types;   /* one per cell type */
+    int nfields;
+    const float *criticallevel1;  /* [type][field] */
+    const float *criticallevel2;
+    const double *cellenv;        /* device, nfields x n x 4 as tm_colony_env2cells writes; NULL if nfields == 0 */
+    int simulationstart;
+    float secondsperstep;
+    int (*draw)(void *ctx);
+    void *draw_ctx;
+} tm_cycle_params;
+
+/* Cell-cycle state of a colony's cells in the caller's order (n entries):
+ * phase time and lengths (hours), age; get also returns phase, size and young. */
+int tm_colony_set_cycle(tm_session *s, int id, const float *phasetime, const float *g1, const float *sphase,
+                        const float *g2, const float *m, const int *age);
+int tm_colony_get_cycle(tm_session *s, int id, float *phasetime, float *g1, float *sphase, float *g2, float *m,
+                        int *age, int *phase, double *size, float *young);
+/* Runs the step; dividing cells append their daughter (caller indices n, n+1,
+ * ... in the order of their parents; the colony needs reserved slots), dying
+ * cells are marked for removal (tm_colony_compact removes them).  *divided
+ * and *marked receive the counts. */
+int tm_colony_cellcycle(tm_session *s, int id, const tm_cycle_params *p, int64_t *divided, int64_t *marked);
+
 /* Replace the cells of an existing colony (at most the slots it holds).  With
  * the same n the cells are taken as the same cells in the same order as the
  * colony's input: they keep their slots, and neighbour lists stay valid unless

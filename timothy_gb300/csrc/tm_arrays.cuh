@@ -59,6 +59,10 @@ struct tm_arrays {
     int *fix_list;
     // per step: work[0] colonies that search (no lists), work[1] colonies
     // whose lists overflowed; lets the search grid leave at once
+    // cell-cycle state, indexed by colony offset + the caller's cell index
+    // (allocated when a colony first runs the cell cycle)
+    float *cy_pt, *cy_g1, *cy_s, *cy_g2, *cy_m;
+    int *cy_age;
     int *work;           // work[2], work[3]: cells queued for the octree walk
     int *walk_list;
     // outputs (Morton order)

@@ -52,3 +52,21 @@ struct tm_vtk_layout {
 };
 cudaError_t tm_launch_vtk_pack(const tm_arrays &a, long long off, long long n, int rank, const tm_vtk_layout &L,
                                unsigned char *img, cudaStream_t st);
+
+// cell cycle (tm_cycle.cu): per-type parameters and the step's inputs on the device
+#include "timothy_gb300.h"
+struct tm_cycle_dev {
+    const tm_cycle_type *types;    // ntypes
+    const float *cl1, *cl2;        // [type][field]
+    const double *csize;           // celltype size per type
+    const double *cellenv;         // nfields x n x 4, caller order (tm_colony_env2cells layout)
+    long long off;                 // colony offset (cell-cycle arrays are indexed off + caller index)
+    int nfields, simulationstart;
+    float sps;                     // settings.secondsperstep
+    double shrink;                 // pow(2, -1/3)
+};
+cudaError_t tm_launch_cycle_count(const tm_cycle_dev &P, const tm_arrays &a, long long off, long long n, int dim,
+                                  uint32_t *draws, uint32_t *divs, cudaStream_t st);
+cudaError_t tm_launch_cycle_apply(const tm_cycle_dev &P, const tm_arrays &a, long long off, long long n, int dim,
+                                  const uint32_t *draw_off, const uint32_t *div_off, const int *stream,
+                                  unsigned long long *marked, cudaStream_t st);

@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <type_traits>
@@ -139,6 +140,11 @@ struct tm_session {
     int dl_next = 0;      // download buffer the next field uses
     double *env_buf = nullptr;   // gather output staging (grows on demand)
     size_t env_bytes = 0;
+    // cell cycle: per-type parameters on the device, the draw stream, state arrays
+    void *cy_params = nullptr;   // tm_cycle_type[8] + 2 x [8][TM_CYCLE_MAX_FIELDS] floats + double csize[8]
+    int *cy_stream = nullptr;
+    size_t cy_stream_cap = 0;
+    unsigned long long *cy_marked = nullptr;
     tm_tuning tune{1, 1, 128, 0.1f, 64};
     cudaEvent_t tstart = nullptr, tstop = nullptr;
 };
@@ -600,6 +606,8 @@ extern "C" int tm_session_create(tm_session **out, const tm_session_config *cfg,
     e = cudaMemcpy(s->dK, &s->K, sizeof(tm_consts), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(a.desc, 0, sizeof(tm_desc) * (size_t)(C + 1));
     if (e == cudaSuccess) e = cudaMemset(a.frame, 0, sizeof(tm_frame) * (size_t)(C + 1));
+    // the memsets run on the legacy stream, which the session's stream does not wait for
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
         tm_session_destroy(s);
         return tm_fail(TM_ECUDA, "session init: %s", cudaGetErrorString(e));
@@ -632,6 +640,12 @@ extern "C" int tm_session_destroy(tm_session *s)
         if (s->ev_copied[k]) cudaEventDestroy(s->ev_copied[k]);
     }
     if (s->env_buf) cudaFree(s->env_buf);
+    {
+        void *cy[] = {s->A.cy_pt, s->A.cy_g1, s->A.cy_s, s->A.cy_g2, s->A.cy_m, s->A.cy_age, s->cy_params,
+                      s->cy_stream, s->cy_marked};
+        for (void *p : cy)
+            if (p) cudaFree(p);
+    }
     if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
@@ -1808,6 +1822,42 @@ __global__ void k_compact_scatter(tm_arrays a, long long off, int m, const doubl
     a.nbcount[s] = (int)o[6];
 }
 
+// cell-cycle state (caller-indexed) of the survivors, 6 words each, via scratch
+__global__ void k_compact_cycle_gather(tm_arrays a, long long off, int n, const uint32_t *keep_caller,
+                                       const uint32_t *new_caller, double *scratch)
+{
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n || !keep_caller[c]) return;
+    float *w = (float *)scratch + (long long)new_caller[c] * 6;
+    const long long i = off + c;
+    w[0] = a.cy_pt[i];
+    w[1] = a.cy_g1[i];
+    w[2] = a.cy_s[i];
+    w[3] = a.cy_g2[i];
+    w[4] = a.cy_m[i];
+    w[5] = __int_as_float(a.cy_age[i]);
+}
+
+__global__ void k_compact_cycle_scatter(tm_arrays a, long long off, int m, const double *scratch)
+{
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= m) return;
+    const float *w = (const float *)scratch + c * 6;
+    const long long i = off + c;
+    a.cy_pt[i] = w[0];
+    a.cy_g1[i] = w[1];
+    a.cy_s[i] = w[2];
+    a.cy_g2[i] = w[3];
+    a.cy_m[i] = w[4];
+    a.cy_age[i] = __float_as_int(w[5]);
+}
+
+__global__ void k_append_cols(int *col, long long first, int m, int c)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < m) col[first + k] = c;
+}
+
 __global__ void k_force_rebuild_one(tm_frame *frame, int c)
 {
     frame[c].force_rebuild = 1;   // slots changed: the lists are rebuilt at the next step
@@ -1843,6 +1893,13 @@ extern "C" int tm_colony_compact(tm_session *s, int id, int64_t *removed)
     k_compact_scatter<<<blocks_for(survivors, 256), 256, 0, st>>>(a, c.off, (int)survivors, s->env_buf);
     k_force_rebuild_one<<<1, 1, 0, st>>>(a.frame, id);
     CK(cudaGetLastError());
+    if (a.cy_pt) {
+        // cell-cycle state follows the caller indices (after the outputs: env_buf is reused)
+        k_compact_cycle_gather<<<blocks_for(n, 256), 256, 0, st>>>(a, c.off, n, keep_caller, new_caller, s->env_buf);
+        k_compact_cycle_scatter<<<blocks_for(survivors, 256), 256, 0, st>>>(a, c.off, (int)survivors,
+                                                                          s->env_buf);
+        CK(cudaGetLastError());
+    }
     c.n = (int)survivors;
     s->h_desc[id].n = c.n;
     if ((rc = push_desc(s, id))) return rc;
@@ -1901,6 +1958,15 @@ extern "C" int tm_colony_append(tm_session *s, int id, const tm_colony_input *in
     CK(cudaMemcpyAsync(a.ctype + o, in->ctype, n * 4, cudaMemcpyHostToDevice, st));
     if (in->phase) CK(cudaMemcpyAsync(a.phase + o, in->phase, n * 4, cudaMemcpyHostToDevice, st));
     k_append_init<<<blocks_for(m, 256), 256, 0, st>>>(a, c.off, c.n, (int)m, in->phase ? 1 : 0, s->dK, s->d_flag);
+    if (a.cy_pt) {
+        const long long o2 = c.off + c.n;
+        CK(cudaMemsetAsync(a.cy_pt + o2, 0, n * 4, st));
+        CK(cudaMemsetAsync(a.cy_g1 + o2, 0, n * 4, st));
+        CK(cudaMemsetAsync(a.cy_s + o2, 0, n * 4, st));
+        CK(cudaMemsetAsync(a.cy_g2 + o2, 0, n * 4, st));
+        CK(cudaMemsetAsync(a.cy_m + o2, 0, n * 4, st));
+        CK(cudaMemsetAsync(a.cy_age + o2, 0, n * 4, st));
+    }
     k_force_rebuild_one<<<1, 1, 0, st>>>(a.frame, id);
     CK(cudaGetLastError());
     int bad = 0;
@@ -1912,5 +1978,180 @@ extern "C" int tm_colony_append(tm_session *s, int id, const tm_colony_input *in
     CK(cudaStreamSynchronize(st));
     drop_graphs(s);
     if (bad) return tm_fail(TM_EDEVICE, "an appended cell type lies outside 0..%d (set to 0)", s->K.ntypes - 1);
+    return TM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// cell cycle (tm_cycle.cu)
+
+#define TM_CYCLE_MAX_FIELDS 16
+
+static int cycle_alloc(tm_session *s)
+{
+    if (s->A.cy_pt) return TM_OK;
+    const long long S = ((s->cfg.max_slots + 31) / 32) * 32;
+    tm_arrays &a = s->A;
+    int rc = TM_OK;
+    if (rc == TM_OK) rc = dalloc(&a.cy_pt, S);
+    if (rc == TM_OK) rc = dalloc(&a.cy_g1, S);
+    if (rc == TM_OK) rc = dalloc(&a.cy_s, S);
+    if (rc == TM_OK) rc = dalloc(&a.cy_g2, S);
+    if (rc == TM_OK) rc = dalloc(&a.cy_m, S);
+    if (rc == TM_OK) rc = dalloc(&a.cy_age, S);
+    const size_t pbytes = sizeof(tm_cycle_type) * TM_MAX_TYPES + 2 * sizeof(float) * TM_MAX_TYPES * TM_CYCLE_MAX_FIELDS +
+                          sizeof(double) * TM_MAX_TYPES;
+    if (rc == TM_OK) rc = dalloc((unsigned char **)&s->cy_params, (long long)pbytes);
+    if (rc == TM_OK) rc = dalloc(&s->cy_marked, 1);
+    if (rc == TM_OK) {
+        // on the session stream: it does not wait for the legacy default stream
+        CK(cudaMemsetAsync(a.cy_pt, 0, S * 4, s->stream));
+        CK(cudaMemsetAsync(a.cy_g1, 0, S * 4, s->stream));
+        CK(cudaMemsetAsync(a.cy_s, 0, S * 4, s->stream));
+        CK(cudaMemsetAsync(a.cy_g2, 0, S * 4, s->stream));
+        CK(cudaMemsetAsync(a.cy_m, 0, S * 4, s->stream));
+        CK(cudaMemsetAsync(a.cy_age, 0, S * 4, s->stream));
+    }
+    drop_graphs(s);
+    return rc;
+}
+
+extern "C" int tm_colony_set_cycle(tm_session *s, int id, const float *phasetime, const float *g1,
+                                   const float *sphase, const float *g2, const float *m, const int *age)
+{
+    int rc = lookup(s, id);
+    if (rc) return rc;
+    if (!phasetime || !g1 || !sphase || !g2 || !m || !age) return tm_fail(TM_EINVAL, "null cycle array");
+    CK(cudaSetDevice(s->device));
+    if ((rc = cycle_alloc(s))) return rc;
+    const colony_host &c = s->cols[id];
+    const size_t b = (size_t)c.n * 4;
+    const tm_arrays &a = s->A;
+    if (b) {
+        CK(cudaMemcpyAsync(a.cy_pt + c.off, phasetime, b, cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemcpyAsync(a.cy_g1 + c.off, g1, b, cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemcpyAsync(a.cy_s + c.off, sphase, b, cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemcpyAsync(a.cy_g2 + c.off, g2, b, cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemcpyAsync(a.cy_m + c.off, m, b, cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemcpyAsync(a.cy_age + c.off, age, b, cudaMemcpyHostToDevice, s->stream));
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    return TM_OK;
+}
+
+extern "C" int tm_colony_get_cycle(tm_session *s, int id, float *phasetime, float *g1, float *sphase, float *g2,
+                                   float *m, int *age, int *phase, double *size, float *young)
+{
+    int rc = lookup(s, id);
+    if (rc) return rc;
+    CK(cudaSetDevice(s->device));
+    const colony_host &c = s->cols[id];
+    const size_t b = (size_t)c.n * 4;
+    const tm_arrays &a = s->A;
+    CK(cudaStreamSynchronize(s->stream));
+    if (b && a.cy_pt) {
+        float *fl[5] = {phasetime, g1, sphase, g2, m};
+        const float *src[5] = {a.cy_pt, a.cy_g1, a.cy_s, a.cy_g2, a.cy_m};
+        for (int k = 0; k < 5; k++)
+            if (fl[k]) CK(cudaMemcpyAsync(fl[k], src[k] + c.off, b, cudaMemcpyDeviceToHost, s->stream));
+        if (age) CK(cudaMemcpyAsync(age, a.cy_age + c.off, b, cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+    }
+    if ((rc = download_streams(s))) return rc;
+    if (phase && (rc = unsort_to_host(s, (const int32_t *)a.phase, c, (int32_t *)phase))) return rc;
+    if (size && (rc = unsort_to_host(s, (const double *)a.size, c, size))) return rc;
+    if (young && (rc = unsort_to_host(s, (const float *)a.young, c, young))) return rc;
+    CK(cudaStreamSynchronize(s->stream));
+    CK(cudaStreamSynchronize(s->copy_stream));
+    return TM_OK;
+}
+
+extern "C" int tm_colony_cellcycle(tm_session *s, int id, const tm_cycle_params *p, int64_t *divided, int64_t *marked)
+{
+    int rc = lookup(s, id);
+    if (rc) return rc;
+    if (!p || !p->types) return tm_fail(TM_EINVAL, "null cycle parameters");
+    if (p->nfields < 0 || p->nfields > TM_CYCLE_MAX_FIELDS) return tm_fail(TM_EINVAL, "nfields must be 0..%d",
+                                                                         TM_CYCLE_MAX_FIELDS);
+    if (p->nfields > 0 && (!p->cellenv || !p->criticallevel1 || !p->criticallevel2))
+        return tm_fail(TM_EINVAL, "fields need cellenv and critical levels");
+    colony_host &c = s->cols[id];
+    if (divided) *divided = 0;
+    if (marked) *marked = 0;
+    const long long n = c.n;
+    if (n == 0) return TM_OK;
+    CK(cudaSetDevice(s->device));
+    if ((rc = cycle_alloc(s))) return rc;
+    const int nt = s->K.ntypes, nf = p->nfields;
+    // parameters to the device
+    std::vector<unsigned char> hp(sizeof(tm_cycle_type) * TM_MAX_TYPES + 2 * sizeof(float) * TM_MAX_TYPES *
+                                  TM_CYCLE_MAX_FIELDS + sizeof(double) * TM_MAX_TYPES, 0);
+    tm_cycle_type *ht = (tm_cycle_type *)hp.data();
+    float *hc1 = (float *)(ht + TM_MAX_TYPES), *hc2 = hc1 + TM_MAX_TYPES * TM_CYCLE_MAX_FIELDS;
+    double *hcs = (double *)(hc2 + TM_MAX_TYPES * TM_CYCLE_MAX_FIELDS);
+    for (int t = 0; t < nt; t++) {
+        ht[t] = p->types[t];
+        hcs[t] = s->K.t[t].csize;
+        for (int f = 0; f < nf; f++) {
+            hc1[t * nf + f] = p->criticallevel1[t * nf + f];
+            hc2[t * nf + f] = p->criticallevel2[t * nf + f];
+        }
+    }
+    cudaStream_t st = s->stream;
+    CK(cudaMemcpyAsync(s->cy_params, hp.data(), hp.size(), cudaMemcpyHostToDevice, st));
+    tm_cycle_dev P;
+    P.types = (const tm_cycle_type *)s->cy_params;
+    P.cl1 = (const float *)(P.types + TM_MAX_TYPES);
+    P.cl2 = P.cl1 + TM_MAX_TYPES * TM_CYCLE_MAX_FIELDS;
+    P.csize = (const double *)(P.cl2 + TM_MAX_TYPES * TM_CYCLE_MAX_FIELDS);
+    P.cellenv = p->cellenv;
+    P.off = c.off;
+    P.nfields = nf;
+    P.simulationstart = p->simulationstart;
+    P.sps = p->secondsperstep;
+    P.shrink = std::pow(2.0, -(1.0 / 3.0));
+    const tm_arrays a = view(s, s->parity);
+    // pass 1: draws and divisions per cell, in the caller's order; their scans
+    uint32_t *draws = (uint32_t *)s->d_scratch, *draw_off = draws + (n + 1);
+    uint32_t *divs = (uint32_t *)s->d_scratch2, *div_off = divs + (n + 1);
+    CK(tm_launch_cycle_count(P, a, c.off, n, s->K.dim, draws, divs, st));
+    CK(tm_scan_exclusive(draws, draw_off, n + 1, s->scan_tmp_slots, st));
+    CK(tm_scan_exclusive(divs, div_off, n + 1, s->scan_tmp_slots, st));
+    uint32_t tot[2] = {0, 0};
+    CK(cudaMemcpyAsync(&tot[0], draw_off + n, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&tot[1], div_off + n, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (n + (long long)tot[1] > c.nslots)
+        return tm_fail(TM_ENOMEM, "colony %d: %lld cells and %u daughters exceed its %d slots", id, n, tot[1],
+                       c.nslots);
+    // the random values, in the reference's order
+    std::vector<int> hs(tot[0] > 0 ? tot[0] : 1);
+    for (uint32_t k = 0; k < tot[0]; k++) hs[k] = p->draw ? p->draw(p->draw_ctx) : rand();
+    if (s->cy_stream_cap < hs.size()) {
+        if (s->cy_stream) CK(cudaFree(s->cy_stream));
+        s->cy_stream = nullptr;
+        s->cy_stream_cap = 0;
+        if ((rc = dalloc(&s->cy_stream, (long long)hs.size()))) return rc;
+        s->cy_stream_cap = hs.size();
+    }
+    CK(cudaMemcpyAsync(s->cy_stream, hs.data(), hs.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(s->cy_marked, 0, sizeof(unsigned long long), st));
+    // pass 2: the transitions
+    CK(tm_launch_cycle_apply(P, a, c.off, n, s->K.dim, draw_off, div_off, s->cy_stream, s->cy_marked, st));
+    unsigned long long mk = 0;
+    CK(cudaMemcpyAsync(&mk, s->cy_marked, sizeof mk, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (tot[1] > 0) {
+        // daughters joined the colony: their slots need the colony's entry, the lists a rebuild
+        k_append_cols<<<blocks_for(tot[1], 256), 256, 0, st>>>(s->A.col, c.off + n, (int)tot[1], id);
+        k_force_rebuild_one<<<1, 1, 0, st>>>(a.frame, id);
+        CK(cudaGetLastError());
+        c.n += (int)tot[1];
+        s->h_desc[id].n = c.n;
+        if ((rc = push_desc(s, id))) return rc;
+        CK(cudaStreamSynchronize(st));
+        drop_graphs(s);
+    }
+    if (divided) *divided = tot[1];
+    if (marked) *marked = (int64_t)mk;
     return TM_OK;
 }

@@ -60,6 +60,20 @@ class _Info(C.Structure):
                 ("list_maxdisp", C.c_float), ("list_skin", C.c_float), ("list_age", C.c_int32)]
 
 
+class _CycleType(C.Structure):
+    _fields_ = [("g1", C.c_float), ("s", C.c_float), ("g2", C.c_float), ("m", C.c_float), ("v", C.c_float),
+                ("rd", C.c_float), ("criticaldensity", C.c_float)]
+
+
+_DRAW = C.CFUNCTYPE(C.c_int, C.c_void_p)
+
+
+class _CycleParams(C.Structure):
+    _fields_ = [("types", C.POINTER(_CycleType)), ("nfields", C.c_int), ("criticallevel1", C.c_void_p),
+                ("criticallevel2", C.c_void_p), ("cellenv", C.c_void_p), ("simulationstart", C.c_int),
+                ("secondsperstep", C.c_float), ("draw", _DRAW), ("draw_ctx", C.c_void_p)]
+
+
 class _Tuning(C.Structure):
     _fields_ = [("pair_lshift", C.c_int), ("list_variant", C.c_int), ("walk_block", C.c_int),
                 ("skin_over_h", C.c_float), ("rmax", C.c_int)]
@@ -104,6 +118,9 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "tm_colony_env2cells": (C.c_int, [P, C.c_int, P, C.c_float, P, C.c_int, P, P, P]),
         "tm_colony_write_vtk": (C.c_int, [P, C.c_int, C.c_char_p, C.c_int]),
         "tm_colony_compact": (C.c_int, [P, C.c_int, P]),
+        "tm_colony_set_cycle": (C.c_int, [P, C.c_int, P, P, P, P, P, P]),
+        "tm_colony_get_cycle": (C.c_int, [P, C.c_int, P, P, P, P, P, P, P, P, P]),
+        "tm_colony_cellcycle": (C.c_int, [P, C.c_int, C.POINTER(_CycleParams), P, P]),
         "tm_colony_append": (C.c_int, [P, C.c_int, C.POINTER(_Input)]),
         "tm_session_bytes": (C.c_int64, [C.POINTER(_Config), C.c_int]),
         "tm_device_memory": (C.c_int, [C.c_int, P, P]),
@@ -279,6 +296,46 @@ class Session:
         if rc in (0, -4):
             self._n[cid] += col.n
         _check(rc)
+
+    # -- cell cycle -----------------------------------------------------------
+    def set_cycle(self, cid: int, phasetime, g1, sphase, g2, m, age):
+        """Cell-cycle state of the colony's cells (caller order)."""
+        arrs = [np.ascontiguousarray(a, np.float32) for a in (phasetime, g1, sphase, g2, m)]
+        ag = np.ascontiguousarray(age, np.int32)
+        _check(load_library().tm_colony_set_cycle(self._h, cid, *[_p(a) for a in arrs], _p(ag)))
+
+    def get_cycle(self, cid: int) -> dict:
+        n = self._n[cid]
+        out = {k: np.zeros(n, np.float32) for k in ("phasetime", "g1", "s", "g2", "m")}
+        out["age"] = np.zeros(n, np.int32)
+        out["phase"] = np.zeros(n, np.int32)
+        out["size"] = np.zeros(n)
+        out["young"] = np.zeros(n, np.float32)
+        _check(load_library().tm_colony_get_cycle(self._h, cid, *[_p(out[k]) for k in
+                                                                  ("phasetime", "g1", "s", "g2", "m", "age",
+                                                                   "phase", "size", "young")]))
+        return out
+
+    def cellcycle(self, cid: int, types: dict, *, nfields: int = 0, cl1=None, cl2=None, cellenv=None,
+                  simulationstart: int = 1, secondsperstep: float = 3600.0, draw=None) -> tuple[int, int]:
+        """One cell-cycle step; types holds per-type g1, s, g2, m, v, rd, cd arrays.
+        cellenv: device array (nfields, n, 4).  draw: None (the C library's
+        rand()) or a callable returning the next value.  Returns (divided, marked)."""
+        nt = len(types["g1"])
+        tarr = (_CycleType * nt)(*[_CycleType(*(float(types[k][t]) for k in ("g1", "s", "g2", "m", "v", "rd",
+                                                                               "cd"))) for t in range(nt)])
+        c1 = np.ascontiguousarray(cl1 if cl1 is not None else np.zeros(1), np.float32)
+        c2 = np.ascontiguousarray(cl2 if cl2 is not None else np.zeros(1), np.float32)
+        fn = _DRAW(lambda ctx: int(draw())) if draw is not None else _DRAW()
+        prm = _CycleParams(C.cast(tarr, C.POINTER(_CycleType)), int(nfields), _p(c1), _p(c2),
+                           _dptr(cellenv) if cellenv is not None else None, int(simulationstart),
+                           float(secondsperstep), fn, None)
+        d = np.zeros(1, np.int64)
+        mk = np.zeros(1, np.int64)
+        rc = load_library().tm_colony_cellcycle(self._h, cid, C.byref(prm), _p(d), _p(mk))
+        _check(rc)
+        self._n[cid] += int(d[0])
+        return int(d[0]), int(mk[0])
 
     def set_active(self, cid: int, active: bool):
         _check(load_library().tm_colony_set_active(self._h, cid, 1 if active else 0))
