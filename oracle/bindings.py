@@ -76,6 +76,9 @@ def load(which: str = "oracle") -> C.CDLL:
         lib.ref_cellcycle.argtypes = [C.c_int64, C.c_int, C.c_int] + [_P] * 8 + [C.c_int, _P, _P, C.c_int, C.c_float,
                                                                                  C.c_uint, _P] + [_P] * 16 + \
             [C.c_int64, _P]
+        lib.ref_cellsupdate_run.restype = C.c_int
+        lib.ref_cellsupdate_run.argtypes = [_P, _P, C.c_int64, C.c_int, C.c_int] + [_P] * 13 + \
+            [C.c_int, C.c_float, C.c_uint, C.c_int, _P]
         lib.ref_cellsdeath.restype = C.c_int64
         lib.ref_cellsdeath.argtypes = [C.c_int64, C.c_int64, _P, C.c_int64, C.c_int64, _P]
         lib.ref_write_vtk.restype = C.c_int
@@ -353,3 +356,55 @@ def cellcycle(state: dict, types: dict, *, dim: int = 3, nfields: int = 0, envva
     out["removecell"] = rem[:m].copy()
     out["removecount"] = int(rc_count.value)
     return out
+
+
+# celldata_t (global.h:100-120) as the reference lays it out: 112-byte records
+REF_CELL_DTYPE = np.dtype({
+    "names": ["lifetime", "phase", "age", "death", "phasetime", "g1", "s", "g2", "m", "young", "gid", "x", "y", "z",
+              "size", "v", "density", "mindist", "ctype"],
+    "formats": ["<i4", "<i4", "<i4", "<i4", "<f4", "<f4", "<f4", "<f4", "<f4", "<f4", "<i4", "<f8", "<f8", "<f8",
+                "<f8", "<f8", "<f8", "<f8", "<i4"],
+    "offsets": [0, 4, 8, 12, 16, 20, 24, 28, 32, 36, 40, 48, 56, 64, 72, 80, 88, 96, 104],
+    "itemsize": 112})
+
+
+def phase_counts(phase, ctype, ntypes: int) -> np.ndarray:
+    """localcount's 7 values then localtypecount's 7 per type (cellcount_t,
+    global.h:90-98) for cells with the given phases and types."""
+    out = np.zeros(7 + 7 * ntypes, np.uint64)
+    phase = np.asarray(phase)
+    ctype = np.asarray(ctype)
+    out[0] = len(phase)
+    for p in range(6):
+        out[1 + p] = np.count_nonzero(phase == p)
+    for t in range(ntypes):
+        sel = ctype == t
+        out[7 + 7 * t] = np.count_nonzero(sel)
+        for p in range(6):
+            out[7 + 7 * t + 1 + p] = np.count_nonzero(sel & (phase == p))
+    return out
+
+
+def ref_cellsupdate(records: np.ndarray, n: int, types, cycle: dict, *, dim: int = 3, simulationstart: int = 1,
+                    sps: float = 3600.0, seed: int = 1, steps: int = 1, counts=None,
+                    which: str = "ref_strict") -> tuple[np.ndarray, np.ndarray]:
+    """The reference's step loop with its whole cell update (octbuild,
+    computepotential, computegradient, cellsupdate) for ``steps`` steps after
+    srand(seed) on REF_CELL_DTYPE records (len(records) = room for cells).
+    types: a CellTypes; cycle: per-type g1, s, g2, m, v, rd, cd.  Returns the
+    records in use and the counters after the run."""
+    lib = load(which)
+    rec = np.ascontiguousarray(records.copy())
+    cap = len(rec)
+    nt = types.ntypes
+    cnt = np.ascontiguousarray(counts if counts is not None else
+                               phase_counts(rec["phase"][:n], rec["ctype"][:n], nt), np.uint64).copy()
+    tp = [np.ascontiguousarray(a, np.float64) for a in (types.h, types.h2, types.h3, types.h4, types.size)]
+    rm = np.ascontiguousarray(types.randommove, np.float32)
+    cy = [np.ascontiguousarray(cycle[k], np.float32) for k in ("g1", "s", "g2", "m", "v", "rd", "cd")]
+    nn = C.c_int64(n)
+    rc = lib.ref_cellsupdate_run(_ptr(rec), C.byref(nn), cap, dim, nt, *[_ptr(a) for a in tp], _ptr(rm),
+                                 *[_ptr(a) for a in cy], simulationstart, sps, seed, steps, _ptr(cnt))
+    if rc:
+        raise RuntimeError(f"ref_cellsupdate_run failed: {rc}")
+    return rec[:int(nn.value)].copy(), cnt

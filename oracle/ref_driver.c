@@ -22,6 +22,7 @@
 #include "fieldgradient.h"
 #include "io.h"
 #include "cells.h"
+#include "utils.h"
 
 /* defined in octree.c with external linkage (octree.h:24-27) */
 extern double3dv_t affShift;
@@ -539,6 +540,94 @@ int ref_cellcycle(int64_t n, int dim, int ntypes, const float *tg1, const float 
     free(ci.cells);
     free(ci.velocity);
     free(ci.localtypecount);
+    free(ct);
+    return 0;
+}
+
+/* The reference step loop with the whole cell update (main.c:67-79,
+ * step.c:41-100 without fields; cells.c:525-543 cellsupdate: random move,
+ * cell cycle with mitosis, removal, global counts) for nsteps steps after
+ * srand(seed), on the caller's celldata_t records (cap of them, *n in use).
+ * counts holds localcount's 7 values then localtypecount's 7 per type, in
+ * and out.  The velocity array mitosis reads only to overwrite the value is
+ * zeroed. */
+void cellsupdate(systeminfo_t systeminfo, settings_t settings, celltype_t *celltype, cellenvdata_t **cellenvdata,
+                 cellsinfo_t *cellsinfo);
+
+int ref_cellsupdate_run(void *cells, int64_t *n, int64_t cap, int dim, int ntypes, const double *th,
+                        const double *th2, const double *th3, const double *th4, const double *tsize,
+                        const float *trandommove, const float *tg1, const float *ts, const float *tg2,
+                        const float *tm, const float *tv, const float *trd, const float *tcd, int simulationstart,
+                        float sps, unsigned seed, int nsteps, uint64_t *counts)
+{
+    systeminfo_t si;
+    settings_t st;
+    cellsinfo_t ci;
+    cellcommdata_t cc;
+    celltype_t *ct = (celltype_t *)calloc((size_t)ntypes, sizeof(celltype_t));
+    int t, s;
+    memset(&si, 0, sizeof(si));
+    memset(&st, 0, sizeof(st));
+    memset(&ci, 0, sizeof(ci));
+    memset(&cc, 0, sizeof(cc));
+    si.rank = 0;
+    si.size = 1;
+    si.nthreads = omp_get_max_threads();
+    si.dim[0] = si.dim[1] = si.dim[2] = 1;
+    st.dimension = dim;
+    st.numberofcelltypes = ntypes;
+    st.numberoffields = 0;
+    st.simulationstart = simulationstart;
+    st.secondsperstep = sps;
+    st.maxlocalcells = cap;
+    st.maxcells = cap;
+    for (t = 0; t < ntypes; t++) {
+        ct[t].h = th[t];
+        ct[t].h2 = th2[t];
+        ct[t].h3 = th3[t];
+        ct[t].h4 = th4[t];
+        ct[t].size = tsize[t];
+        ct[t].randommove = trandommove[t];
+        ct[t].g1 = tg1[t];
+        ct[t].s = ts[t];
+        ct[t].g2 = tg2[t];
+        ct[t].m = tm[t];
+        ct[t].v = tv[t];
+        ct[t].rd = trd[t];
+        ct[t].criticaldensity = tcd[t];
+    }
+    ci.dimension = dim;
+    ci.cells = (celldata_t *)cells;
+    ci.forces = (double3dv_t *)calloc((size_t)cap, sizeof(double3dv_t));
+    ci.velocity = (double3dv_t *)calloc((size_t)cap, sizeof(double3dv_t));
+    ci.localtypecount = (cellcount_t *)calloc((size_t)ntypes, sizeof(cellcount_t));
+    ci.cellsperproc = (uint64_t *)calloc(1, sizeof(uint64_t));
+    uint64_t *lc = &ci.localcount.n;
+    for (t = 0; t < 7; t++) lc[t] = counts[t];
+    for (t = 0; t < ntypes; t++) {
+        uint64_t *tc = &ci.localtypecount[t].n;
+        for (s = 0; s < 7; s++) tc[s] = counts[7 + 7 * t + s];
+    }
+    updateglobalcounts(&ci);
+    srand(seed);
+    for (s = 0; s < nsteps; s++) {
+        if (ci.localcount.n == 0) break;
+        octbuild(si, &ci, ct);
+        computepotential(si, &ci, ct, cc);
+        computegradient(si, &ci, ct, cc);
+        cellsupdate(si, st, ct, NULL, &ci);
+        octfree(&ci);
+    }
+    *n = (int64_t)ci.localcount.n;
+    for (t = 0; t < 7; t++) counts[t] = lc[t];
+    for (t = 0; t < ntypes; t++) {
+        uint64_t *tc = &ci.localtypecount[t].n;
+        for (s = 0; s < 7; s++) counts[7 + 7 * t + s] = tc[s];
+    }
+    free(ci.forces);
+    free(ci.velocity);
+    free(ci.localtypecount);
+    free(ci.cellsperproc);
     free(ct);
     return 0;
 }

@@ -10,6 +10,7 @@ nodes (always including the faces) plus per-component sums.
     python tests/golden/make_golden_fields.py          # gather and gradient
     python tests/golden/make_golden_fields.py --vtk    # the VTK writer
     python tests/golden/make_golden_fields.py --cycle  # the cell cycle
+    python tests/golden/make_golden_fields.py --chain  # step loop with the whole cell update
 """
 from __future__ import annotations
 
@@ -125,8 +126,56 @@ def make_cycle():
         print(name, len(out["phase"]), out["removecount"])
 
 
+CHAIN_CYCLE = dict(g1=np.array([3.0], np.float32), s=np.array([2.0], np.float32), g2=np.array([1.0], np.float32),
+                   m=np.array([1.0], np.float32), v=np.array([0.2], np.float32), rd=np.array([0.05], np.float32))
+
+
+def chain_records(kind, n, seed, dim, cap):
+    """Records of a colony of n cells for the cell-update chain (room for cap)."""
+    col = C.make_colony(kind, n, seed, C.initial_radius(kind, n), dim=dim)
+    rng = np.random.Generator(np.random.PCG64(seed + 1))
+    rec = np.zeros(cap, B.REF_CELL_DTYPE)
+    for k in ("x", "y", "z", "size", "young", "ctype"):
+        rec[k][:n] = getattr(col, k)
+    rec["phase"][:n] = rng.integers(0, 5, n)
+    rec["phasetime"][:n] = rng.uniform(0, 3, n)
+    for k, lo, hi in (("g1", 2.5, 3.5), ("s", 1.5, 2.5), ("g2", 0.7, 1.3), ("m", 0.7, 1.3)):
+        rec[k][:n] = rng.uniform(lo, hi, n)
+    rec["age"][:n] = rng.integers(0, 4, n)
+    rec["gid"][:n] = np.arange(n)
+    rec["lifetime"][:n] = rng.integers(0, 100, n)
+    return col, rec
+
+
+def make_chain():
+    """The reference step loop with its whole cell update (cellsupdate,
+    cells.c:525-543: random move, cell cycle with mitosis, removal) for a few
+    steps after srand(seed): the records before and after, and the counters."""
+    for name, kind, n, dim, seed, steps in (("chain_clustered3d", "clustered", 2000, 3, 31, 4),
+                                            ("chain_uniform2d", "uniform", 1500, 2, 32, 4)):
+        cap = 4 * n
+        col, rec = chain_records(kind, n, seed, dim, cap)
+        types = C.CellTypes.consistent(randommove=[0.05])
+        # a critical density at the colony's median lets about half the cells grow
+        r = B.run(col, 1, which="ref_strict", update_mode=2)
+        cyc = dict(CHAIN_CYCLE, cd=np.array([np.median(r.density)], np.float32))
+        counts = B.phase_counts(rec["phase"][:n], rec["ctype"][:n], 1)
+        out, cnt = B.ref_cellsupdate(rec, n, types, cyc, dim=dim, sps=3600.0, seed=seed, steps=steps,
+                                     counts=counts)
+        data = {"dim": dim, "seed": seed, "steps": steps, "cap": cap, "n": n, "sps": 3600.0,
+                "randommove": types.randommove, "h": types.h, "tsize": types.size, "counts_in": counts,
+                "counts_out": cnt}
+        data.update({"cy_" + k: v for k, v in cyc.items()})
+        data.update({"in_" + k: rec[k][:n].copy() for k in B.REF_CELL_DTYPE.names})
+        data.update({"out_" + k: out[k].copy() for k in B.REF_CELL_DTYPE.names})
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **data)
+        print(name, n, "->", len(out), "counts", cnt[:7])
+
+
 if __name__ == "__main__":
-    if "--vtk" in sys.argv:
+    if "--chain" in sys.argv:
+        make_chain()
+    elif "--vtk" in sys.argv:
         make_vtk()
     elif "--cycle" in sys.argv:
         make_cycle()

@@ -17,7 +17,7 @@ from timothy_gb300 import colonies as C
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-               if not os.path.basename(p).startswith("field_"))
+               if not os.path.basename(p).startswith(("field_", "chain_")))
 UPDATE = {0: "reference", 1: "dt", 2: "none"}
 
 pytestmark = pytest.mark.gpu

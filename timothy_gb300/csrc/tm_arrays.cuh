@@ -63,6 +63,9 @@ struct tm_arrays {
     // (allocated when a colony first runs the cell cycle)
     float *cy_pt, *cy_g1, *cy_s, *cy_g2, *cy_m;
     int *cy_age;
+    // the C library's rand() values of updatepositions' random move, dim per
+    // cell in the caller's order (drop-in only; null: a counter-based stream)
+    const int *move_draws;
     int *work;           // work[2], work[3]: cells queued for the octree walk
     int *walk_list;
     // outputs (Morton order)

@@ -289,3 +289,7 @@ __device__ inline int tm_lcp(uint4 a, uint4 b)
     if (x == 0) return TM_ROOT_LEVEL;
     return 28 - (31 - __clz(x));
 }
+
+// (float)rand()/RAND_MAX for a value r of the C library's rand() (RAND_MAX
+// = 2^31 - 1 with glibc), as the reference forms its random numbers
+__device__ __forceinline__ float tm_frand(int r) { return __fdiv_rn(__int2float_rn(r), (float)2147483647); }

@@ -18,8 +18,7 @@
 
 #define TM_RAND_MAX_I 2147483647
 
-// (float)rand()/RAND_MAX for the draw r
-__device__ __forceinline__ float frand(int r) { return __fdiv_rn(__int2float_rn(r), (float)TM_RAND_MAX_I); }
+__device__ __forceinline__ float frand(int r) { return tm_frand(r); }
 
 struct cycle_decision {
     int next_phase;       // phase after this step

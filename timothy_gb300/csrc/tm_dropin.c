@@ -120,6 +120,15 @@ static void push_types(const cellsinfo_t *ci, const celltype_t *celltype)
     TRY("cell types", tmi_set_types(g_sess, &tt));
 }
 
+static const tmi_aos_layout *cell_layout(void)
+{
+    static const tmi_aos_layout lay = {(int64_t)sizeof(celldata_t), offsetof(celldata_t, x), offsetof(celldata_t, y),
+                                       offsetof(celldata_t, z), offsetof(celldata_t, size),
+                                       offsetof(celldata_t, young), offsetof(celldata_t, ctype),
+                                       offsetof(celldata_t, phase)};
+    return &lay;
+}
+
 void octbuild(systeminfo_t systeminfo, cellsinfo_t *cellsinfo, celltype_t *celltype)
 {
     g_si = systeminfo;
@@ -127,10 +136,7 @@ void octbuild(systeminfo_t systeminfo, cellsinfo_t *cellsinfo, celltype_t *cellt
     if (n == 0) return;                                /* octree.c:152-153 */
     ensure_session(n, cellsinfo->dimension);
     pin_cells(cellsinfo->cells, n);
-    tmi_aos_layout lay = {(int64_t)sizeof(celldata_t), offsetof(celldata_t, x), offsetof(celldata_t, y),
-                          offsetof(celldata_t, z), offsetof(celldata_t, size), offsetof(celldata_t, young),
-                          offsetof(celldata_t, ctype), offsetof(celldata_t, phase)};
-    TRY("upload", tmi_upload_aos(g_sess, g_cid, cellsinfo->cells, n, &lay));
+    TRY("upload", tmi_upload_aos(g_sess, g_cid, cellsinfo->cells, n, cell_layout()));
     push_types(cellsinfo, celltype);
     TRY("build", tmi_phase(g_sess, 0));
     tm_colony_info info;
@@ -205,13 +211,124 @@ void updatepositions(settings_t settings, celltype_t *celltype, cellsinfo_t *cel
     TRY("dimension", tmi_set_dimension(g_sess, settings.dimension));
     TRY("forces", tmi_upload_forces(g_sess, g_cid, (const double *)cellsinfo->forces));
     TRY("marks", tmi_upload_removecell(g_sess, g_cid, removecell));
+    /* the random move takes dim rand() values per cell in cell order whatever
+     * the cell types' randommove (cells.c:353-356): drawn here, so that the
+     * caller's generator stays where the reference leaves it */
+    const int64_t nd = n * (settings.dimension == 3 ? 3 : 2);
+    int *draws = (int *)malloc((size_t)nd * sizeof(int));
+    if (!draws) die("random move draws", -2, __LINE__);
+    for (int64_t k = 0; k < nd; k++) draws[k] = rand();
+    TRY("random move", tmi_set_move_draws(g_sess, draws, nd));
     TRY("update", tmi_phase(g_sess, 2));
     TRY("sync", tm_session_sync(g_sess));
+    free(draws);
+    TRY("random move", tmi_set_move_draws(g_sess, NULL, 0));
     TRY("positions", tmi_download_aos3(g_sess, g_cid, cellsinfo->cells, (int64_t)sizeof(celldata_t),
                                        offsetof(celldata_t, x), 1));
     int64_t marked = 0;
     TRY("marks", tmi_download_removecell(g_sess, g_cid, removecell, &marked));
     *removecount += marked;
+}
+
+static uint64_t *phase_counter(cellcount_t *c, int phase)
+{
+    switch (phase) {
+    case 0: return &c->g0phase;
+    case 1: return &c->g1phase;
+    case 2: return &c->sphase;
+    case 3: return &c->g2phase;
+    case 4: return &c->mphase;
+    default: return &c->necroticphase;
+    }
+}
+
+/* One cell-cycle step of every local cell (cells.c:370-523) with mitosis
+ * (cells.c:124-205), on the device.  The records go up as they are, the cycle
+ * draws the caller's rand() values in the reference's order and the records,
+ * daughters appended, come back with removecell and the counters.  The colony
+ * count stands in for globalcount.n (the two agree at one rank). */
+int updatecellcycles(systeminfo_t systeminfo, settings_t settings, celltype_t *celltype, cellsinfo_t *cellsinfo,
+                     cellenvdata_t **cellenvdata, unsigned char *removecell, int64_t *removecount)
+{
+    g_si = systeminfo;
+    const int64_t n = (int64_t)cellsinfo->localcount.n;
+    if (n == 0) return 0;
+    /* records the caller's array holds: settings.maxlocalcells (mitosis,
+     * cells.c:130-131, stops beyond it); one division per cell at most */
+    int64_t room = settings.maxlocalcells > n ? settings.maxlocalcells : n;
+    if (room > 2 * n) room = 2 * n;
+    ensure_session(room, settings.dimension);
+    pin_cells(cellsinfo->cells, room);
+    TRY("upload", tmi_upload_aos(g_sess, g_cid, cellsinfo->cells, n, cell_layout()));
+    push_types(cellsinfo, celltype);
+    int maxtype = 0;
+    TRY("cell types", tmi_max_ctype(g_sess, g_cid, &maxtype));
+    const int nt = maxtype + 1, nf = settings.numberoffields;
+    if (nf > 16) die("more than 16 fields", TM_EINVAL, __LINE__);
+    tm_cycle_type ct[8];
+    float cl1[8 * 16], cl2[8 * 16];
+    for (int t = 0; t < nt; t++) {
+        ct[t].g1 = celltype[t].g1;
+        ct[t].s = celltype[t].s;
+        ct[t].g2 = celltype[t].g2;
+        ct[t].m = celltype[t].m;
+        ct[t].v = celltype[t].v;
+        ct[t].rd = celltype[t].rd;
+        ct[t].criticaldensity = celltype[t].criticaldensity;
+        for (int f = 0; f < nf; f++) {
+            cl1[t * nf + f] = celltype[t].criticallevel1[f];
+            cl2[t * nf + f] = celltype[t].criticallevel2[f];
+        }
+    }
+    tm_cycle_params p;
+    memset(&p, 0, sizeof p);
+    p.types = ct;
+    p.nfields = nf;
+    p.criticallevel1 = cl1;
+    p.criticallevel2 = cl2;
+    p.simulationstart = settings.simulationstart;
+    p.secondsperstep = settings.secondsperstep;
+    double *env[16];
+    for (int f = 0; f < nf; f++) env[f] = (double *)cellenvdata[f];
+    int64_t marked = 0, nout = n, counts[16];
+    TRY("cell cycle", tmi_cycle_aos(g_sess, g_cid, cellsinfo->cells, n, room, &p, env, removecell, &marked, &nout,
+                                    counts));
+    *removecount += marked;
+    for (int ph = 0; ph < 6; ph++) *phase_counter(&cellsinfo->localcount, ph) += (uint64_t)counts[ph];
+    for (int t = 0; t < nt; t++) {
+        cellsinfo->localtypecount[t].n += (uint64_t)counts[8 + t];
+        cellsinfo->localtypecount[t].g1phase += (uint64_t)counts[8 + t];
+    }
+    cellsinfo->localcount.n += (uint64_t)(nout - n);
+    cellsinfo->localcount.g1phase += (uint64_t)(nout - n);
+    return 0;
+}
+
+/* Removal of the marked cells (cells.c:290-336): the records are compacted
+ * on the device in the reference's order and the counters of the removed
+ * cells' phases and types are taken down. */
+void cellsdeath(int oldlnc, cellsinfo_t *cellsinfo, unsigned char *removecell, int64_t removecount)
+{
+    if (cellsinfo->globalcount.n == 1) return;
+    const int64_t n = (int64_t)cellsinfo->localcount.n;
+    if (n == 0 || removecount == 0) {
+        cellsinfo->localcount.n -= (uint64_t)removecount;
+        return;
+    }
+    ensure_session(n, cellsinfo->dimension);
+    int64_t nout = n, removed[64];
+    TRY("cell removal", tmi_compact_aos(g_sess, cellsinfo->cells, n, oldlnc, removecell, &nout, removed));
+    for (int t = 0; t < 8; t++)
+        for (int ph = 0; ph < 8; ph++) {
+            const int64_t r = removed[t * 8 + ph];
+            if (!r) continue;
+            if (ph < 5) {
+                *phase_counter(&cellsinfo->localcount, ph) -= (uint64_t)r;
+                *phase_counter(&cellsinfo->localtypecount[t], ph) -= (uint64_t)r;
+            }
+            cellsinfo->localtypecount[t].n -= (uint64_t)r;
+        }
+    cellsinfo->localcount.n -= (uint64_t)removecount;
 }
 
 /* grid of this rank (grid.c:80-136): lower corner, resolution, index box */

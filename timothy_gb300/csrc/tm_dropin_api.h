@@ -45,6 +45,17 @@ int tmi_reserve_stage(tm_session *s, int64_t bytes);
 int tmi_env2cells_patch(tm_session *s, int cid, const double *patch, int nfields, const int64_t box_lo[3],
                         const int64_t box_size[3], const double lower[3], float resolution, const int64_t grid_hi[3],
                         double **cellenv);
+/* the random move's rand() values (dim per cell, caller order); NULL clears */
+int tmi_set_move_draws(tm_session *s, const int *draws, int64_t count);
+/* updatecellcycles on host celldata_t records (after tmi_upload_aos of them);
+ * counts[0..5]: change of the phase counters, counts[8 + t]: daughters of type t */
+int tmi_cycle_aos(tm_session *s, int cid, void *cells, int64_t n, int64_t cap, const tm_cycle_params *p,
+                  double *const *cellenv, unsigned char *removecell, int64_t *marked, int64_t *nout,
+                  int64_t counts[16]);
+/* cellsdeath on host celldata_t records; removed[t * 8 + p]: removed cells of
+ * type t in phase p (p = 7 for the necrotic phase) */
+int tmi_compact_aos(tm_session *s, void *cells, int64_t n, int64_t oldlnc, const unsigned char *removecell,
+                    int64_t *nout, int64_t removed[64]);
 /* gradient of one field, host arrays */
 int tmi_field_gradient_host(tm_session *s, const double *data, const int64_t gsize[3], float resolution,
                             double *gradient);

@@ -36,7 +36,13 @@ __global__ void k_update(tm_arrays a, const tm_consts *K)
         y = add64(y, fy);
         if (dim == 3) z = add64(z, fz);
         const float rm = K->t[a.ctype[i]].randommove;
-        if (rm != 0.0f) {
+        if (a.move_draws) {
+            // the reference's own draws (cells.c:353-355), dim per cell in caller order
+            const int *r = a.move_draws + (long long)dim * a.perm[i];
+            x = add64(x, mul64((double)rm, sub64(mul64((double)tm_frand(r[0]), 2.0), 1.0)));
+            y = add64(y, mul64((double)rm, sub64(mul64((double)tm_frand(r[1]), 2.0), 1.0)));
+            if (dim == 3) z = add64(z, mul64((double)rm, sub64(mul64((double)tm_frand(r[2]), 2.0), 1.0)));
+        } else if (rm != 0.0f) {
             const unsigned long long id = (unsigned long long)a.perm[i];
             x = add64(x, mul64((double)rm, sub64(mul64((double)tm_uniform(a.frame[c].step_counter, id, 0), 2.0), 1.0)));
             y = add64(y, mul64((double)rm, sub64(mul64((double)tm_uniform(a.frame[c].step_counter, id, 1), 2.0), 1.0)));

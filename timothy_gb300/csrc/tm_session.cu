@@ -145,6 +145,8 @@ struct tm_session {
     int *cy_stream = nullptr;
     size_t cy_stream_cap = 0;
     unsigned long long *cy_marked = nullptr;
+    int *move_buf = nullptr;     // the drop-in's random-move draws
+    size_t move_cap = 0;
     tm_tuning tune{1, 1, 128, 0.1f, 64};
     cudaEvent_t tstart = nullptr, tstop = nullptr;
 };
@@ -642,7 +644,7 @@ extern "C" int tm_session_destroy(tm_session *s)
     if (s->env_buf) cudaFree(s->env_buf);
     {
         void *cy[] = {s->A.cy_pt, s->A.cy_g1, s->A.cy_s, s->A.cy_g2, s->A.cy_m, s->A.cy_age, s->cy_params,
-                      s->cy_stream, s->cy_marked};
+                      s->cy_stream, s->cy_marked, s->move_buf};
         for (void *p : cy)
             if (p) cudaFree(p);
     }
@@ -2153,5 +2155,245 @@ extern "C" int tm_colony_cellcycle(tm_session *s, int id, const tm_cycle_params 
     }
     if (divided) *divided = tot[1];
     if (marked) *marked = (int64_t)mk;
+    return TM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// drop-in helpers for cellsupdate (cells.c:525-543): the random move's draws,
+// the cell cycle and the death compaction on the host's celldata_t records
+
+extern "C" int tmi_set_move_draws(tm_session *s, const int *draws, int64_t count)
+{
+    if (!s) return tm_fail(TM_EINVAL, "null session");
+    if (!draws || count <= 0) {
+        if (s->A.move_draws) drop_graphs(s);
+        s->A.move_draws = nullptr;
+        return TM_OK;
+    }
+    CK(cudaSetDevice(s->device));
+    if (s->move_cap < (size_t)count) {
+        if (s->move_buf) CK(cudaFree(s->move_buf));
+        s->move_buf = nullptr;
+        s->move_cap = 0;
+        int rc = dalloc(&s->move_buf, count);
+        if (rc) return rc;
+        s->move_cap = (size_t)count;
+    }
+    CK(cudaMemcpyAsync(s->move_buf, draws, (size_t)count * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+    s->A.move_draws = s->move_buf;
+    drop_graphs(s);
+    return TM_OK;
+}
+
+// celldata_t byte offsets (global.h:100-120, 112-byte records)
+#define CD_PHASE 4
+#define CD_AGE 8
+#define CD_DEATH 12
+#define CD_PT 16
+#define CD_G1 20
+#define CD_S 24
+#define CD_G2 28
+#define CD_M 32
+#define CD_YOUNG 36
+#define CD_GID 40
+#define CD_X 48
+#define CD_Y 56
+#define CD_Z 64
+#define CD_SIZE 72
+#define CD_V 80
+#define CD_DENSITY 88
+#define CD_CTYPE 104
+#define CD_BYTES 112
+
+template <typename T>
+__device__ __forceinline__ T &cd_field(unsigned char *rec, int off)
+{
+    return *(T *)(rec + off);
+}
+
+// records (caller order, identity slots after an upload) -> the cycle's inputs
+__global__ void k_cycle_from_aos(const unsigned char *aos, long long n, tm_arrays a, long long off)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    unsigned char *r = (unsigned char *)aos + k * CD_BYTES;
+    const long long i = off + k;
+    a.density[i] = cd_field<double>(r, CD_DENSITY);
+    a.cy_pt[i] = cd_field<float>(r, CD_PT);
+    a.cy_g1[i] = cd_field<float>(r, CD_G1);
+    a.cy_s[i] = cd_field<float>(r, CD_S);
+    a.cy_g2[i] = cd_field<float>(r, CD_G2);
+    a.cy_m[i] = cd_field<float>(r, CD_M);
+    a.cy_age[i] = cd_field<int>(r, CD_AGE);
+}
+
+// the cycle's results into the records (cells keep every other field;
+// daughters get the fields mitosis sets, cells.c:156-205).  cnt[0..5] gets
+// the change of the phase counters (a cell leaving a phase takes one off it,
+// the phase it enters gets one), cnt[8 + t] the daughters of type t.
+__global__ void k_cycle_to_aos(unsigned char *aos, long long n, long long total, tm_arrays a, long long off,
+                               unsigned long long *cnt)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= total) return;
+    const long long s = off + k;                  // identity order: slot = caller index
+    unsigned char *r = aos + k * CD_BYTES;
+    const int ph = a.phase[s];
+    if (k >= n) {
+        cd_field<int>(r, CD_GID) = (int)k;        // rank * maxlocalcells + index at one rank
+        cd_field<double>(r, CD_V) = 0.0;
+        cd_field<int>(r, CD_DEATH) = 0;
+        cd_field<double>(r, CD_DENSITY) = a.density[s];
+        cd_field<int>(r, CD_CTYPE) = a.ctype[s];
+        atomicAdd(&cnt[8 + a.ctype[s]], 1ull);
+    } else {
+        const int old = cd_field<int>(r, CD_PHASE);
+        if (old != ph) {
+            if (old >= 0 && old < 6) atomicAdd(&cnt[old], ~0ull);    // -1
+            if (ph >= 0 && ph < 6) atomicAdd(&cnt[ph], 1ull);
+        }
+    }
+    cd_field<int>(r, CD_PHASE) = ph;
+    cd_field<int>(r, CD_AGE) = a.cy_age[s];
+    cd_field<float>(r, CD_PT) = a.cy_pt[s];
+    cd_field<float>(r, CD_G1) = a.cy_g1[s];
+    cd_field<float>(r, CD_S) = a.cy_s[s];
+    cd_field<float>(r, CD_G2) = a.cy_g2[s];
+    cd_field<float>(r, CD_M) = a.cy_m[s];
+    cd_field<float>(r, CD_YOUNG) = a.young[s];
+    cd_field<double>(r, CD_X) = a.x[s];
+    cd_field<double>(r, CD_Y) = a.y[s];
+    cd_field<double>(r, CD_Z) = a.z[s];
+    cd_field<double>(r, CD_SIZE) = a.size[s];
+}
+
+__global__ void k_rem_out(const tm_arrays a, long long off, long long n, unsigned char *out)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) out[k] = a.rem[off + k];
+}
+
+static int64_t round256(int64_t b) { return (b + 255) & ~(int64_t)255; }
+
+// updatecellcycles on the host's records: cells[0, n) in, cells[0, *nout)
+// out (the caller's array holds cap records); removecell (n entries) in and
+// out.  The cell types' cycle parameters and levels are in p, the fields'
+// values in cellenv[f][c] (host, cellenvdata_t layout).
+extern "C" int tmi_cycle_aos(tm_session *s, int cid, void *cells, int64_t n, int64_t cap, const tm_cycle_params *p,
+                             double *const *cellenv, unsigned char *removecell, int64_t *marked, int64_t *nout,
+                             int64_t counts[8 + TM_MAX_TYPES])
+{
+    int rc = lookup(s, cid);
+    if (rc) return rc;
+    *nout = n;
+    *marked = 0;
+    for (int k = 0; k < 8 + TM_MAX_TYPES; k++) counts[k] = 0;
+    if (n == 0) return TM_OK;
+    CK(cudaSetDevice(s->device));
+    if ((rc = cycle_alloc(s))) return rc;
+    colony_host &c = s->cols[cid];
+    if (cap > c.nslots) cap = c.nslots;
+    const tm_arrays a = view(s, s->parity);
+    // the marks first: their upload passes through the staging buffer the records use next
+    if ((rc = tmi_upload_removecell(s, cid, removecell))) return rc;
+    // the records' cycle inputs (the positions, sizes, types and phases came with tmi_upload_aos)
+    const int64_t cnt_at = round256(cap * CD_BYTES + cap);
+    if ((rc = tmi_reserve_stage(s, cnt_at + 8 * (8 + TM_MAX_TYPES)))) return rc;
+    unsigned char *st = (unsigned char *)g_stage.ptr, *rem_dev = st + cap * CD_BYTES;
+    unsigned long long *cnt = (unsigned long long *)(st + cnt_at);
+    CK(cudaMemsetAsync(cnt, 0, 8 * (8 + TM_MAX_TYPES), s->stream));
+    CK(cudaMemcpyAsync(st, cells, (size_t)(n * CD_BYTES), cudaMemcpyHostToDevice, s->stream));
+    k_cycle_from_aos<<<blocks_for(n, 256), 256, 0, s->stream>>>(st, n, a, c.off);
+    CK(cudaGetLastError());
+    tm_cycle_params q = *p;
+    if (p->nfields > 0) {
+        if ((rc = env_reserve(s, (size_t)p->nfields * (size_t)n * 4 * sizeof(double)))) return rc;
+        for (int f = 0; f < p->nfields; f++)
+            CK(cudaMemcpyAsync(s->env_buf + (size_t)f * (size_t)n * 4, cellenv[f], (size_t)n * 4 * sizeof(double),
+                               cudaMemcpyHostToDevice, s->stream));
+        q.cellenv = s->env_buf;
+    }
+    int64_t div = 0;
+    if ((rc = tm_colony_cellcycle(s, cid, &q, &div, marked))) return rc;
+    const long long total = n + div;
+    if (total > cap) return tm_fail(TM_ENOMEM, "too many local cells after mitosis");
+    const tm_arrays b = view(s, s->parity);
+    // the daughters' records keep the bytes mitosis does not set (lifetime, mindist)
+    if (div > 0)
+        CK(cudaMemcpyAsync(st + n * CD_BYTES, (const unsigned char *)cells + n * CD_BYTES, (size_t)(div * CD_BYTES),
+                           cudaMemcpyHostToDevice, s->stream));
+    k_cycle_to_aos<<<blocks_for(total, 256), 256, 0, s->stream>>>(st, n, total, b, c.off, cnt);
+    k_rem_out<<<blocks_for(n, 256), 256, 0, s->stream>>>(b, c.off, n, rem_dev);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(cells, st, (size_t)(total * CD_BYTES), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpyAsync(removecell, rem_dev, (size_t)n, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpyAsync(counts, cnt, 8 * (8 + TM_MAX_TYPES), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    *nout = total;
+    return TM_OK;
+}
+
+__global__ void k_keep_records(const unsigned char *rem, const unsigned char *aos, long long oldlnc, long long n,
+                               uint32_t *keep, unsigned long long *removed)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k > n) return;
+    if (k == n || k >= oldlnc) {
+        keep[k] = k == n ? 0u : 1u;
+        return;
+    }
+    keep[k] = rem[k] ? 0u : 1u;
+    if (rem[k]) {
+        // the counters a removed cell leaves (cells.c:308-333): its phase's, if 0..4, and its type's
+        const unsigned char *r = aos + k * CD_BYTES;
+        const int t = *(const int *)(r + CD_CTYPE), ph = *(const int *)(r + CD_PHASE);
+        if (t >= 0 && t < TM_MAX_TYPES) atomicAdd(&removed[t * 8 + (ph >= 0 && ph < 5 ? ph : 7)], 1ull);
+    }
+}
+
+__global__ void k_move_records(const unsigned char *src, const uint32_t *keep, const uint32_t *dst_idx, long long n,
+                               unsigned char *dst)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n || !keep[k]) return;
+    const uint4 *s4 = (const uint4 *)(src + k * CD_BYTES);
+    uint4 *d4 = (uint4 *)(dst + (long long)dst_idx[k] * CD_BYTES);
+    for (int w = 0; w < CD_BYTES / 16; w++) d4[w] = s4[w];
+}
+
+// cellsdeath (cells.c:290-336) on the host's records: the unmarked cells
+// before oldlnc, then every cell from oldlnc on, in order; *nout = count;
+// removed[t * 8 + p] = removed cells of type t in phase p (p = 7: phase 5)
+extern "C" int tmi_compact_aos(tm_session *s, void *cells, int64_t n, int64_t oldlnc, const unsigned char *removecell,
+                               int64_t *nout, int64_t removed[8 * TM_MAX_TYPES])
+{
+    if (!s) return tm_fail(TM_EINVAL, "null session");
+    *nout = n;
+    for (int k = 0; k < 8 * TM_MAX_TYPES; k++) removed[k] = 0;
+    if (n == 0) return TM_OK;
+    if (oldlnc > n) oldlnc = n;
+    if (n + 1 > s->cfg.max_slots + 1) return tm_fail(TM_EINVAL, "more records than the session's slots");
+    CK(cudaSetDevice(s->device));
+    const int64_t rb = n * CD_BYTES, cnt_at = round256(2 * rb + oldlnc);
+    int rc = tmi_reserve_stage(s, cnt_at + 8 * 8 * TM_MAX_TYPES);
+    if (rc) return rc;
+    unsigned char *src = (unsigned char *)g_stage.ptr, *dst = src + rb, *rem = dst + rb;
+    unsigned long long *cnt = (unsigned long long *)(src + cnt_at);
+    uint32_t *keep = (uint32_t *)s->d_scratch, *idx = keep + (n + 1);
+    CK(cudaMemsetAsync(cnt, 0, 8 * 8 * TM_MAX_TYPES, s->stream));
+    CK(cudaMemcpyAsync(src, cells, (size_t)rb, cudaMemcpyHostToDevice, s->stream));
+    if (oldlnc > 0) CK(cudaMemcpyAsync(rem, removecell, (size_t)oldlnc, cudaMemcpyHostToDevice, s->stream));
+    k_keep_records<<<blocks_for(n + 1, 256), 256, 0, s->stream>>>(rem, src, oldlnc, n, keep, cnt);
+    CK(cudaGetLastError());
+    CK(tm_scan_exclusive(keep, idx, n + 1, s->scan_tmp_slots, s->stream));
+    uint32_t m = 0;
+    CK(cudaMemcpyAsync(&m, idx + n, 4, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpyAsync(removed, cnt, 8 * 8 * TM_MAX_TYPES, cudaMemcpyDeviceToHost, s->stream));
+    k_move_records<<<blocks_for(n, 256), 256, 0, s->stream>>>(src, keep, idx, n, dst);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s->stream));
+    if (m > 0) CK(cudaMemcpyAsync(cells, dst, (size_t)m * CD_BYTES, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    *nout = m;
     return TM_OK;
 }

@@ -131,9 +131,13 @@ def _bind(lib):
     lib.patches_applyenv2cells.argtypes = [systeminfo_t, settings_t, C.POINTER(patches_t), C.POINTER(cellsinfo_t),
                                            C.POINTER(grid_t), C.POINTER(C.POINTER(C.POINTER(cellenvdata_t)))]
     lib.fieldgradient.argtypes = [systeminfo_t, settings_t, C.POINTER(C.POINTER(environment_t)), C.POINTER(grid_t)]
+    lib.updatecellcycles.argtypes = [systeminfo_t, settings_t, C.POINTER(celltype_t), C.POINTER(cellsinfo_t),
+                                     C.c_void_p, C.c_void_p, C.POINTER(C.c_int64)]
+    lib.updatecellcycles.restype = C.c_int
+    lib.cellsdeath.argtypes = [C.c_int, C.POINTER(cellsinfo_t), C.c_void_p, C.c_int64]
     for f in ("octbuild", "octfree", "computepotential", "computeremotepotential", "computegradient",
               "computeremotegradient", "updatepositions", "patches_alloc", "patches_cells2envinfo",
-              "patches_applyenv2cells", "fieldgradient", "tm_dropin_shutdown"):
+              "patches_applyenv2cells", "fieldgradient", "cellsdeath", "tm_dropin_shutdown"):
         getattr(lib, f).restype = None
     lib._refabi_bound = True
     return lib
@@ -157,17 +161,21 @@ def grid_geometry(dim: int, gfh: float):
 class DropinRun:
     """The reference step loop on host celldata_t cells, through the drop-ins."""
 
-    def __init__(self, col, *, cic: bool = False, gfh: float = 8.0, nfields: int = 1):
+    def __init__(self, col, *, cic: bool = False, gfh: float = 8.0, nfields: int = 1, cap: int | None = None,
+                 cycle: dict | None = None, sps: float = 3600.0, simulationstart: int = 1):
+        """cap: records the cells array holds (settings.maxlocalcells); cycle:
+        the cell types' g1, s, g2, m, v, rd and cd (criticaldensity), for
+        cellsupdate."""
         self.lib = _bind(load_library())
         n = col.n
         self.n = n
         self.dim = col.dim
-        cells = np.zeros(max(n, 1), CELL_DTYPE)
+        cells = np.zeros(max(n, 1, cap or 0), CELL_DTYPE)
         for k in ("x", "y", "z", "size", "young", "ctype", "phase"):
             cells[k][:n] = getattr(col, k)
         cells["gid"][:n] = np.arange(n)
         self.cells = cells
-        self.forces = np.zeros((max(n, 1), 3))
+        self.forces = np.zeros((len(cells), 3))           # settings.maxlocalcells entries, as main.c allocates
         t = col.types
         self.celltype = (celltype_t * t.ntypes)()
         for k in range(t.ntypes):
@@ -175,6 +183,9 @@ class DropinRun:
             ct.h, ct.h2, ct.h3, ct.h4 = float(t.h[k]), float(t.h2[k]), float(t.h3[k]), float(t.h4[k])
             ct.size = float(t.size[k])
             ct.randommove = float(t.randommove[k])
+            if cycle is not None:
+                ct.g1, ct.s, ct.g2, ct.m = (float(cycle[q][k]) for q in ("g1", "s", "g2", "m"))
+                ct.v, ct.rd, ct.criticaldensity = float(cycle["v"][k]), float(cycle["rd"][k]), float(cycle["cd"][k])
         self.si = systeminfo_t()
         self.si.rank, self.si.size = 0, 1
         self.si.dim[0] = self.si.dim[1] = self.si.dim[2] = 1
@@ -183,8 +194,14 @@ class DropinRun:
         self.st.numberofcelltypes = t.ntypes
         self.st.numberoffields = nfields if cic else 0
         self.st.gfh = gfh
+        self.st.maxlocalcells = len(cells)
+        self.st.maxcells = len(cells)
+        self.st.secondsperstep = sps
+        self.st.simulationstart = simulationstart
         self.ci = cellsinfo_t()
         self.ci.localcount.n = n
+        self.typecount = (cellcount_t * t.ntypes)()
+        self.ci.localtypecount = C.addressof(self.typecount)
         self.ci.cells = cells.ctypes.data
         self.ci.forces = self.forces.ctypes.data
         self.ci.dimension = col.dim
@@ -247,6 +264,51 @@ class DropinRun:
         lib.octfree(C.byref(self.ci))
         aff = double3dv_t.in_dll(lib, "affShift")
         self.aff = np.array([aff.x, aff.y, aff.z, C.c_double.in_dll(lib, "affScale").value])
+
+    COUNT_FIELDS = ("n", "g0phase", "g1phase", "sphase", "g2phase", "mphase", "necroticphase")
+
+    def set_counts(self, counts):
+        """localcount's 7 values then localtypecount's 7 per type; globalcount
+        follows localcount (one rank)."""
+        for k, f in enumerate(self.COUNT_FIELDS):
+            setattr(self.ci.localcount, f, int(counts[k]))
+            for t in range(len(self.typecount)):
+                setattr(self.typecount[t], f, int(counts[7 + 7 * t + k]))
+        self._globalcounts()
+
+    def counts(self) -> np.ndarray:
+        out = [getattr(self.ci.localcount, f) for f in self.COUNT_FIELDS]
+        for t in range(len(self.typecount)):
+            out += [getattr(self.typecount[t], f) for f in self.COUNT_FIELDS]
+        return np.array(out, np.uint64)
+
+    def _globalcounts(self):
+        # updateglobalcounts (utils.c:80-101) at one rank
+        for f in self.COUNT_FIELDS:
+            setattr(self.ci.globalcount, f, getattr(self.ci.localcount, f))
+
+    def cellsupdate(self) -> int:
+        """cellsupdate (cells.c:525-543) over the drop-ins: random move,
+        cell cycle with mitosis, removal, global counts.  Returns the step's
+        removecount."""
+        lib = self.lib
+        oldlnc = int(self.ci.localcount.n)
+        rem = np.zeros(max(oldlnc, 1), np.uint8)
+        rc = C.c_int64(0)
+        lib.updatepositions(self.st, self.celltype, C.byref(self.ci), rem.ctypes.data, C.byref(rc))
+        lib.updatecellcycles(self.si, self.st, self.celltype, C.byref(self.ci), None, rem.ctypes.data, C.byref(rc))
+        lib.cellsdeath(oldlnc, C.byref(self.ci), rem.ctypes.data, rc.value)
+        self._globalcounts()
+        self.n = int(self.ci.localcount.n)
+        return int(rc.value)
+
+    def cycle_step(self) -> int:
+        """One step of the reference loop without fields: octree, potential,
+        gradient, then the whole cell update."""
+        if self.ci.localcount.n == 0:
+            return 0
+        self.step(update=False)
+        return self.cellsupdate()
 
     def _env2cells(self, p, data, gradient):
         # the received patch in the reference's layout (patches.c:380-416):
