@@ -256,6 +256,40 @@ int tm_env2cells(const double *x, const double *y, const double *z, int64_t n, i
  * one-sided differences on the faces, 0 along an axis of one node. */
 int tm_field_gradient(const double *data, const int64_t gsize[3], float resolution, int nfields,
                       double *gradient, void *stream);
+/* Implicit diffusion step: environment_compute (environment.c:131-523) at one
+ * rank on device fields (nfields x gsize[0] x gsize[1] x gsize[2], x-major, z
+ * fastest, as environment_t.data).  Per field: z = dc * gfdt / (res * res)
+ * (res * res in float), the operator (1 + 6 z + lambda gfdt) u_i - z * (the
+ * in-grid neighbours), and as many solves per step as environment_initsystem
+ * picks from secondsperstep / gfdt (environment.c:144-164), each of
+ * A u = u + z bc (once per grid face the node lies on) + source, starting
+ * from data, which receives the result.  source: device, same layout, or
+ * NULL.  Each solve runs preconditioned conjugate gradients (a geometric
+ * multigrid V-cycle preconditions stiff operators) to a relative residual of
+ * tol (the reference asks its Hypre PCG for 1e-12). */
+typedef struct tm_diffusion tm_diffusion;
+typedef struct tm_diffusion_stats {
+    int solves_per_field;          /* numberofiters */
+    int iterations;                /* CG iterations over all solves */
+    int max_iterations;            /* of one solve */
+    int multigrid_fields;          /* fields solved with the multigrid preconditioner */
+    int levels;                    /* multigrid levels of the grid */
+    double max_relative_residual;  /* largest final |b - A u| / |b| */
+} tm_diffusion_stats;
+/* A solver for grids of gsize nodes (its work vectors and multigrid levels
+ * are allocated once). */
+int tm_diffusion_create(tm_diffusion **d, const int64_t gsize[3], int device);
+int tm_diffusion_destroy(tm_diffusion *d);
+int tm_diffusion_levels(const tm_diffusion *d);
+/* One step on data (host parameters dc, bc, lambda: nfields each).  Runs on
+ * stream; the host waits for each CG iteration's residual norm. */
+int tm_diffusion_step(tm_diffusion *d, double *data, float resolution, int nfields, const double *dc,
+                      const double *bc, const double *lambda, float secondsperstep, float gfdt, const double *source,
+                      double tol, tm_diffusion_stats *stats, void *stream);
+/* The same with a solver made and released for the call. */
+int tm_field_diffuse(double *data, const int64_t gsize[3], float resolution, int nfields, const double *dc,
+                     const double *bc, const double *lambda, float secondsperstep, float gfdt, const double *source,
+                     double tol, tm_diffusion_stats *stats, void *stream);
 /* The gather for the cells of a session colony, written to host memory in
  * the caller's cell order (cellenv as above, n = the colony's cells); data
  * and gradient are device arrays of the grid described by lower, resolution

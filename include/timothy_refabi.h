@@ -288,6 +288,28 @@ void fieldgradient(systeminfo_t systeminfo, settings_t settings, environment_t *
 
 /* Releases the device session the drop-ins keep between calls (no
  * counterpart in the reference; optional at exit). */
+/* cells.c:370 -- cell cycle with mitosis of every local cell (one rank);
+ * cells.c:290 -- removal of the marked cells */
+int updatecellcycles(systeminfo_t systeminfo, settings_t settings, celltype_t *celltype, cellsinfo_t *cellsinfo,
+                     cellenvdata_t **cellenvdata, unsigned char *removecell, int64_t *removecount);
+void cellsdeath(int oldlnc, cellsinfo_t *cellsinfo, unsigned char *removecell, int64_t removecount);
+/* environment.c:33, 58, 131, 516 -- the fields without Hypre: allocation,
+ * initial values, (nothing to) set up, and the implicit diffusion step on the
+ * GPU.  solverdata_t / solversettings_t (global.h:366-392, Hypre handles) are
+ * never touched, so they are passed as untyped pointers. */
+void environment_allocate(systeminfo_t systeminfo, settings_t settings, grid_t grid, environment_t **environment,
+                          void *solverdata, void *solversettings);
+void environment_init(systeminfo_t systeminfo, settings_t settings, grid_t grid, environment_t **environment);
+void environment_initsystem(systeminfo_t systeminfo, settings_t settings, grid_t *grid, environment_t **environment,
+                            void *solverdata, void *solversettings);
+void environment_compute(systeminfo_t systeminfo, settings_t settings, grid_t *grid, environment_t **environment,
+                         void *solverdata, void *solversettings);
+/* the solution of field f after the last environment_compute (G values,
+ * environment_t.data layout); TM_OK or a negative code */
+int tm_dropin_env_solution(int field, double *out);
+/* 1: environment_compute also copies the solution into environment[f].data
+ * (the reference leaves data unchanged, environment.c:495-507) */
+void tm_dropin_set_env_writeback(int on);
 void tm_dropin_shutdown(void);
 
 #ifdef __cplusplus

@@ -21,6 +21,7 @@ LIBS = {
     "oracle": os.path.join(HERE, "liboracle.so"),
     "ref": os.path.join(HERE, "_ref", "libtimothy_ref.so"),
     "ref_strict": os.path.join(HERE, "_ref", "libtimothy_ref_strict.so"),
+    "ref_env": os.path.join(HERE, "_ref", "libtimothy_ref_env.so"),
 }
 
 _P = C.c_void_p
@@ -48,6 +49,12 @@ def load(which: str = "oracle") -> C.CDLL:
     if not os.path.exists(path):
         raise FileNotFoundError(f"{path} is not built (oracle.bindings.build())")
     lib = C.CDLL(path)
+    if which == "ref_env":
+        lib.ref_environment.restype = C.c_int64
+        lib.ref_environment.argtypes = [C.c_int, C.c_float, C.c_float, C.c_float, C.c_int, C.c_int] + [_P] * 4 + \
+            [C.c_int, C.c_int64] + [_P] * 7
+        _cache[which] = lib
+        return lib
     fn = lib.tmo_run if which == "oracle" else lib.ref_run
     argt = [C.c_int64, C.c_int, C.c_int] + [_P] * 6 + [_P] * 7 + [C.c_int, C.c_int, C.c_double] + [_P] * 6 + \
         [_P, _P, _P, _P] + [C.c_int, C.c_float, _P, C.c_int64, _P, _P]
@@ -65,6 +72,13 @@ def load(which: str = "oracle") -> C.CDLL:
         lib.tmo_neighbours.restype = C.c_int
         lib.tmo_neighbours.argtypes = [C.c_int64, C.c_int, C.c_int, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
                                        C.c_int]
+        lib.tmo_diffusion_iters.restype = C.c_int
+        lib.tmo_diffusion_iters.argtypes = [C.c_float, C.c_float]
+        lib.tmo_diffusion_z.restype = C.c_double
+        lib.tmo_diffusion_z.argtypes = [C.c_double, C.c_float, C.c_float]
+        lib.tmo_diffuse.restype = C.c_int
+        lib.tmo_diffuse.argtypes = [C.c_int64, C.c_int64, C.c_int64, C.c_float, C.c_float, C.c_float, C.c_int,
+                                    C.c_int] + [_P] * 6 + [C.c_double, _P, _P, _P, _P]
         lib.tm_mix64.restype = C.c_uint64
         lib.tm_mix64.argtypes = [C.c_uint64]
     else:
@@ -408,3 +422,68 @@ def ref_cellsupdate(records: np.ndarray, n: int, types, cycle: dict, *, dim: int
     if rc:
         raise RuntimeError(f"ref_cellsupdate_run failed: {rc}")
     return rec[:int(nn.value)].copy(), cnt
+
+
+def diffuse(gsize, resolution: float, sps: float, gfdt: float, step: int, dc, bc, mean, lam, *, u0=None,
+            source=None, tol: float = 1e-15) -> dict:
+    """environment_compute's diffusion step at one rank (tmo_diffuse): fields
+    of shape (nfields, nx, ny, nz), z fastest.  u0 replaces the mean as the
+    start, source the point source."""
+    lib = load("oracle")
+    nx, ny, nz = (int(v) for v in gsize)
+    nf = len(dc)
+    arr = [np.ascontiguousarray(v, np.float64) for v in (dc, bc, mean, lam)]
+    u = np.zeros((nf, nx, ny, nz))
+    b = np.zeros((nf, nx, ny, nz))
+    it = C.c_int(0)
+    cg = C.c_int(0)
+    u0c = None if u0 is None else np.ascontiguousarray(u0, np.float64)
+    src = None if source is None else np.ascontiguousarray(source, np.float64)
+    rc = lib.tmo_diffuse(nx, ny, nz, resolution, sps, gfdt, step, nf, *[_ptr(a) for a in arr], _ptr(u0c), _ptr(src),
+                         tol, _ptr(u), _ptr(b), C.byref(it), C.byref(cg))
+    if rc:
+        raise RuntimeError(f"tmo_diffuse failed: {rc}")
+    return {"u": u, "b": b, "iters": int(it.value), "cg_iters": int(cg.value)}
+
+
+def diffusion_iters(sps: float, gfdt: float) -> int:
+    return int(load("oracle").tmo_diffusion_iters(sps, gfdt))
+
+
+def diffusion_z(dc: float, gfdt: float, resolution: float) -> float:
+    return float(load("oracle").tmo_diffusion_z(dc, gfdt, resolution))
+
+
+def ref_environment(dim: int, gfh: float, sps: float, gfdt: float, step: int, dc, bc, mean, lam,
+                    ncalls: int = 1) -> dict:
+    """The reference's environment_initsystem + ncalls x environment_compute
+    on the Hypre stand-in (oracle/_ref/libtimothy_ref_env.so).  Returns the
+    grid size, numberofiters, z, the requested tolerance and iteration cap,
+    the solves made, the stencil coefficients (nfields, nx, ny, nz, 7), and
+    the last right-hand side and solution (nfields, nx, ny, nz)."""
+    lib = load("ref_env")
+    nf = len(dc)
+    gx, gy, gz = grid_dims(dim, gfh)
+    cap = gx * gy * gz
+    arr = [np.ascontiguousarray(v, np.float64) for v in (dc, bc, mean, lam)]
+    gs = np.zeros(3, np.int64)
+    info = np.zeros(4, np.int32)
+    z = np.zeros(nf)
+    tol = np.zeros(1)
+    coef = np.zeros(nf * cap * 7)
+    b = np.zeros(nf * cap)
+    x = np.zeros(nf * cap)
+    G = lib.ref_environment(dim, gfh, sps, gfdt, step, nf, *[_ptr(a) for a in arr], ncalls, cap, _ptr(gs),
+                            _ptr(info), _ptr(z), _ptr(tol), _ptr(coef), _ptr(b), _ptr(x))
+    if G < 0:
+        raise RuntimeError("ref_environment: grid larger than expected")
+    nx, ny, nz = (int(v) for v in gs)
+
+    def xmajor(a, extra=()):
+        # box order (x fastest) -> (nx, ny, nz), z fastest
+        a = a.reshape((nf, nz, ny, nx) + extra)
+        return np.ascontiguousarray(np.moveaxis(a, (1, 2, 3), (3, 2, 1)))
+
+    return {"gsize": (nx, ny, nz), "iters": int(info[0]), "maxiter": int(info[1]), "nsolves": int(info[2]),
+            "z": z, "tol": float(tol[0]), "coef": xmajor(coef[:nf * G * 7], (7,)), "b": xmajor(b[:nf * G]),
+            "x": xmajor(x[:nf * G])}

@@ -1,0 +1,2 @@
+/* Stand-in header: see hypre_standin.h. */
+#include "hypre_standin.h"

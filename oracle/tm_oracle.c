@@ -1023,3 +1023,138 @@ int tmo_neighbours(int64_t n, int dim, int ntypes, const double *th,
     free(tree.code);
     return rc;
 }
+
+/* ------------------------------------------------------------------------
+ * Implicit diffusion step (environment.c:131-523) at one rank.
+ *
+ * environment_initsystem (environment.c:144-164) picks the number of solves
+ * per step from secondsperstep / gfdt in float arithmetic, then sets every
+ * field's dt to gfdt (environment.c:221) and z = dc * dt / (res * res), the
+ * product res * res in float (environment.c:222).  The operator is the
+ * 7-point stencil with 1 + 6 z + lambda dt on the diagonal and -z for each
+ * neighbour (environment.c:227-230); the Dirichlet faces (environment.c:
+ * 332-375) move z * bc to the right-hand side once per grid face the node
+ * lies on (x-, x+, y-, y+, z-, z+ in turn; both z faces on a one-layer grid)
+ * and leave the couplings to nodes outside the grid, which no solve uses.
+ * environment_compute starts from u = initialconditionmean (a new solution
+ * vector each call, environment.c:298-316) and, numberofiters times, solves
+ * A u = u + faces + pc (environment.c:438-488), pc being 100 at node
+ * (5, 5, 5) from step 1 on (environment_pcfunction, environment.c:251-266).
+ * The solve here is conjugate gradients to a relative residual of tol (the
+ * reference's Hypre PCG with a BoomerAMG preconditioner stops at 1e-12 or 50
+ * iterations, environment.c:404-422).  u0 (x-major, z fastest, nfields
+ * fields) replaces the mean as the start when given; source replaces pc.
+ * Outputs u and the last right-hand side b_last in the same layout. */
+int tmo_diffusion_iters(float secondsperstep, float gfdt)
+{
+    if ((secondsperstep / gfdt) > 1) {
+        const int intdiv = (int)(secondsperstep / gfdt) + 1;
+        const float a1 = secondsperstep / intdiv;
+        const float a2 = secondsperstep / (intdiv - 1);
+        return (gfdt - a1) < (a2 - gfdt) ? intdiv : intdiv - 1;
+    }
+    return 1;
+}
+
+double tmo_diffusion_z(double dc, float gfdt, float resolution)
+{
+    const double dt = gfdt;
+    const float r2 = resolution * resolution;
+    return dc * dt / r2;
+}
+
+static void diff_apply(int64_t nx, int64_t ny, int64_t nz, double diag, double off, const double *u, double *y)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < nx; i++)
+        for (int64_t j = 0; j < ny; j++)
+            for (int64_t k = 0; k < nz; k++) {
+                const int64_t p = (i * ny + j) * nz + k;
+                double s = diag * u[p];
+                if (i > 0) s += off * u[p - ny * nz];
+                if (i < nx - 1) s += off * u[p + ny * nz];
+                if (j > 0) s += off * u[p - nz];
+                if (j < ny - 1) s += off * u[p + nz];
+                if (k > 0) s += off * u[p - 1];
+                if (k < nz - 1) s += off * u[p + 1];
+                y[p] = s;
+            }
+}
+
+static double diff_dot(const double *a, const double *b, int64_t n)
+{
+    double s = 0.0;
+#pragma omp parallel for reduction(+ : s) schedule(static)
+    for (int64_t i = 0; i < n; i++) s += a[i] * b[i];
+    return s;
+}
+
+int tmo_diffuse(int64_t nx, int64_t ny, int64_t nz, float resolution, float secondsperstep, float gfdt, int step,
+                int nfields, const double *dc, const double *bc, const double *mean, const double *lambda,
+                const double *u0, const double *source, double tol, double *u, double *b_last, int *iters_out,
+                int *cg_iters)
+{
+    const int64_t G = nx * ny * nz;
+    const int iters = tmo_diffusion_iters(secondsperstep, gfdt);
+    double *r = (double *)malloc((size_t)G * sizeof(double)), *p = (double *)malloc((size_t)G * sizeof(double));
+    double *q = (double *)malloc((size_t)G * sizeof(double));
+    if (!r || !p || !q) return -1;
+    *iters_out = iters;
+    int cg_total = 0;
+    for (int f = 0; f < nfields; f++) {
+        const double z = tmo_diffusion_z(dc[f], gfdt, resolution);
+        const double dt = gfdt;
+        const double diag = 1 + 6.0 * z + lambda[f] * dt, off = -z, zb = z * bc[f];
+        double *uf = u + (size_t)f * (size_t)G, *bf = b_last + (size_t)f * (size_t)G;
+        for (int64_t i = 0; i < G; i++) uf[i] = u0 ? u0[(size_t)f * (size_t)G + i] : mean[f];
+        for (int it = 0; it < iters; it++) {
+            /* right-hand side in the reference's order of additions */
+            for (int64_t i = 0; i < nx; i++)
+                for (int64_t j = 0; j < ny; j++)
+                    for (int64_t k = 0; k < nz; k++) {
+                        const int64_t o = (i * ny + j) * nz + k;
+                        double v = uf[o];
+                        if (i == 0) v += zb;
+                        if (i == nx - 1) v += zb;
+                        if (j == 0) v += zb;
+                        if (j == ny - 1) v += zb;
+                        if (k == 0) v += zb;
+                        if (k == nz - 1) v += zb;
+                        if (source) v += source[(size_t)f * (size_t)G + o];
+                        else v += (step != 0 && i == 5 && j == 5 && k == 5) ? 100.0 : 0.0;
+                        bf[o] = v;
+                    }
+            /* conjugate gradients from the current u */
+            diff_apply(nx, ny, nz, diag, off, uf, q);
+            for (int64_t i = 0; i < G; i++) r[i] = bf[i] - q[i];
+            memcpy(p, r, (size_t)G * sizeof(double));
+            const double bb = diff_dot(bf, bf, G);
+            double rr = diff_dot(r, r, G), best = rr;
+            int n = 0, stall = 0;
+            while (rr > tol * tol * bb && n < 100000 && stall < 50) {
+                diff_apply(nx, ny, nz, diag, off, p, q);
+                const double alpha = rr / diff_dot(p, q, G);
+                for (int64_t i = 0; i < G; i++) {
+                    uf[i] += alpha * p[i];
+                    r[i] -= alpha * q[i];
+                }
+                const double rr1 = diff_dot(r, r, G);
+                for (int64_t i = 0; i < G; i++) p[i] = r[i] + (rr1 / rr) * p[i];
+                rr = rr1;
+                if (rr < best) {
+                    best = rr;
+                    stall = 0;
+                } else {
+                    stall++;
+                }
+                n++;
+            }
+            cg_total += n;
+        }
+    }
+    if (cg_iters) *cg_iters = cg_total;
+    free(r);
+    free(p);
+    free(q);
+    return 0;
+}

@@ -94,6 +94,15 @@ int tmo_write_vtk(const char *path, int64_t n, const double *x, const double *y,
 /* The fingerprint mixer shared with the GPU diagnostics (SplitMix64 final mix). */
 uint64_t tm_mix64(uint64_t z);
 
+/* The implicit diffusion step of environment_compute at one rank
+ * (environment.c:131-523).  See tm_oracle.c. */
+int tmo_diffusion_iters(float secondsperstep, float gfdt);
+double tmo_diffusion_z(double dc, float gfdt, float resolution);
+int tmo_diffuse(int64_t nx, int64_t ny, int64_t nz, float resolution, float secondsperstep, float gfdt, int step,
+                int nfields, const double *dc, const double *bc, const double *mean, const double *lambda,
+                const double *u0, const double *source, double tol, double *u, double *b_last, int *iters_out,
+                int *cg_iters);
+
 #ifdef __cplusplus
 }
 #endif

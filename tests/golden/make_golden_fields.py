@@ -11,6 +11,7 @@ nodes (always including the faces) plus per-component sums.
     python tests/golden/make_golden_fields.py --vtk    # the VTK writer
     python tests/golden/make_golden_fields.py --cycle  # the cell cycle
     python tests/golden/make_golden_fields.py --chain  # step loop with the whole cell update
+    python tests/golden/make_golden_fields.py --diffusion  # the implicit diffusion step
 """
 from __future__ import annotations
 
@@ -172,8 +173,39 @@ def make_chain():
         print(name, n, "->", len(out), "counts", cnt[:7])
 
 
+DIFFUSION_CASES = {
+    # name: dim, gfh, secondsperstep, gfdt, step, dc, bc, mean, lambda
+    "field_diffuse_3d_two": (3, 128.0, 16000.0, 4000.0, 1, [4.0, 1.82e-5], [1.0, 0.1575e-6], [0.5, 0.1575e-6],
+                             [0.0, 0.001]),
+    "field_diffuse_3d_stiff": (3, 64.0, 16000.0, 3000.0, 1, [200.0], [0.2], [1.0], [1e-4]),
+    "field_diffuse_2d": (2, 128.0, 16000.0, 16000.0, 1, [2.0], [0.3], [0.7], [0.0]),
+    "field_diffuse_3d_step0": (3, 128.0, 16000.0, 16000.0, 0, [2.0], [0.3], [0.7], [0.0]),
+}
+
+
+def make_diffusion():
+    """environment_initsystem + environment_compute (environment.c:131-523),
+    compiled unmodified on the Hypre stand-in (oracle/shim_hypre), twice per
+    case: the solve count, z, the assembled operator's coefficients, the last
+    right-hand side and the solution (fields x-major, z fastest)."""
+    for name, (dim, gfh, sps, gfdt, step, dc, bc, mean, lam) in DIFFUSION_CASES.items():
+        r = B.ref_environment(dim, gfh, sps, gfdt, step, dc, bc, mean, lam, ncalls=2)
+        nx, ny, nz = r["gsize"]
+        co = r["coef"]
+        rec = {"dim": dim, "gfh": gfh, "sps": sps, "gfdt": gfdt, "step": step, "dc": np.array(dc),
+               "bc": np.array(bc), "mean": np.array(mean), "lam": np.array(lam), "gsize": np.array(r["gsize"]),
+               "iters": r["iters"], "z": r["z"], "tol": r["tol"], "maxiter": r["maxiter"], "nsolves": r["nsolves"],
+               # the diagonal and the -x coupling of an interior node (every in-grid coupling is the same)
+               "diag": co[:, 1, 1, min(1, nz - 1), 0], "off": co[:, 1, 1, min(1, nz - 1), 1],
+               "b": r["b"], "x": r["x"]}
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **rec)
+        print(name, r["gsize"], r["iters"], r["z"])
+
+
 if __name__ == "__main__":
-    if "--chain" in sys.argv:
+    if "--diffusion" in sys.argv:
+        make_diffusion()
+    elif "--chain" in sys.argv:
         make_chain()
     elif "--vtk" in sys.argv:
         make_vtk()

@@ -152,3 +152,46 @@ def test_oracle_cellcycle_matches_reference(oracle_lib, name):
     for k in rec.files:
         if k.startswith("out_"):
             assert np.array_equal(np.asarray(out[k[4:]]), rec[k]), k
+
+
+DIFFUSION = ["field_diffuse_3d_two", "field_diffuse_3d_stiff", "field_diffuse_2d", "field_diffuse_3d_step0"]
+
+
+@pytest.mark.parametrize("name", DIFFUSION)
+def test_oracle_diffusion_matches_reference(oracle_lib, name):
+    """The implicit diffusion step (environment.c:131-523): solve count, z and
+    the assembled operator exactly as the reference's own environment.c builds
+    them (compiled on the Hypre stand-in); the right-hand side bit for bit
+    when the step makes one solve (later solves start from a CG result); the
+    solution within 1e-13 of the largest value (both solve to 1e-15)."""
+    rec = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    gfh, sps, gfdt, step = float(rec["gfh"]), float(rec["sps"]), float(rec["gfdt"]), int(rec["step"])
+    assert oracle_lib.diffusion_iters(sps, gfdt) == int(rec["iters"])
+    assert int(rec["nsolves"]) == 2 * int(rec["iters"])
+    assert float(rec["tol"]) == 1e-12 and int(rec["maxiter"]) == 50
+    for f, dc in enumerate(rec["dc"]):
+        z = oracle_lib.diffusion_z(float(dc), gfdt, gfh)
+        assert z == rec["z"][f]
+        assert rec["diag"][f] == 1 + 6.0 * z + rec["lam"][f] * float(np.float32(gfdt))
+        assert rec["off"][f] == -z
+    out = oracle_lib.diffuse(tuple(rec["gsize"]), gfh, sps, gfdt, step, rec["dc"], rec["bc"], rec["mean"],
+                             rec["lam"])
+    assert out["iters"] == int(rec["iters"])
+    if int(rec["iters"]) == 1:
+        assert np.array_equal(out["b"], rec["b"])
+    else:
+        assert np.max(np.abs(out["b"] - rec["b"])) <= 1e-14 * np.max(np.abs(rec["b"]))
+    assert np.max(np.abs(out["u"] - rec["x"])) <= 1e-13 * np.max(np.abs(rec["x"]))
+
+
+def test_oracle_diffusion_matches_live_reference(oracle_lib):
+    """The same comparison against the reference's environment.c run here, with
+    other parameters (one solve per step, so the right-hand side is exact)."""
+    if not oracle_lib.available("ref_env"):
+        pytest.skip("reference not built here")
+    args = (3, 128.0, 7200.0, 7200.0, 3, [0.7, 30.0], [2.0, 0.0], [1.5, 0.25], [0.002, 0.0])
+    r = oracle_lib.ref_environment(*args, ncalls=1)
+    out = oracle_lib.diffuse(r["gsize"], *args[1:])
+    assert out["iters"] == r["iters"] == 1
+    assert np.array_equal(out["b"], r["b"])
+    assert np.max(np.abs(out["u"] - r["x"])) <= 1e-13 * np.max(np.abs(r["x"]))

@@ -442,8 +442,111 @@ void fieldgradient(systeminfo_t systeminfo, settings_t settings, environment_t *
                                                       (*environment)[f].gradient));
 }
 
+/* ------------------------------------------------------------------------
+ * Fields: environment.c without Hypre.  The reference assembles the implicit
+ * step in environment_initsystem / environment_initboundary and solves it
+ * with Hypre's PCG + BoomerAMG in environment_solve; here the step runs on
+ * the GPU (tm_diffusion).  As in the reference, environment_compute starts
+ * every field from its initialconditionmean and leaves environment[f].data
+ * as it was (the loop meant to copy the solution back is empty,
+ * environment.c:495-507); tm_dropin_env_solution reads the solution, and
+ * tm_dropin_set_env_writeback(1) copies it into data after each step. */
+static tm_diffusion *g_diff;
+static int64_t g_diff_gs[3];
+static int g_env_writeback;
+
+/* environment.c:33-56 without the solver's own arrays */
+void environment_allocate(systeminfo_t systeminfo, settings_t settings, grid_t grid, environment_t **environment,
+                          void *solverdata, void *solversettings)
+{
+    (void)solverdata;
+    (void)solversettings;
+    if (settings.numberoffields == 0) return;
+    const size_t G = (size_t)(grid.localsize.x * grid.localsize.y * grid.localsize.z);
+    for (int i = 0; i < settings.numberoffields; i++)
+        if (!((*environment)[i].data = (double *)calloc(G, sizeof(double))))
+            die("environment->data allocation", TM_ENOMEM, __LINE__);
+    for (int i = 0; i < settings.numberoffields; i++)
+        if (!((*environment)[i].production = (double *)calloc(G, sizeof(double))))
+            die("environment->production allocation", TM_ENOMEM, __LINE__);
+    for (int i = 0; i < settings.numberoffields; i++)
+        if (!((*environment)[i].gradient = (double *)calloc(G * 3, sizeof(double))))
+            die("environment->gradient allocation", TM_ENOMEM, __LINE__);
+    (void)systeminfo;
+}
+
+/* environment.c:58-74: mean + rand() / RAND_MAX * variance per node in the
+ * reference's order (the caller's generator advances as the reference's does) */
+void environment_init(systeminfo_t systeminfo, settings_t settings, grid_t grid, environment_t **environment)
+{
+    (void)systeminfo;
+    if (settings.numberoffields == 0) return;
+    const int64_t yz = grid.localsize.y * grid.localsize.z;
+    for (int f = 0; f < settings.numberoffields; f++)
+        for (int64_t i = 0; i < grid.localsize.x; i++)
+            for (int64_t j = 0; j < grid.localsize.y; j++)
+                for (int64_t k = 0; k < grid.localsize.z; k++)
+                    (*environment)[f].data[yz * i + grid.localsize.z * j + k] =
+                        (*environment)[f].initialconditionmean +
+                        ((double)(rand()) / RAND_MAX) * (*environment)[f].initialconditionvariance;
+}
+
+/* environment.c:131-233: the step's parameters are derived again by
+ * environment_compute; nothing to assemble */
+void environment_initsystem(systeminfo_t systeminfo, settings_t settings, grid_t *grid, environment_t **environment,
+                            void *solverdata, void *solversettings)
+{
+    (void)systeminfo;
+    (void)settings;
+    (void)grid;
+    (void)environment;
+    (void)solverdata;
+    (void)solversettings;
+}
+
+void environment_compute(systeminfo_t systeminfo, settings_t settings, grid_t *grid, environment_t **environment,
+                         void *solverdata, void *solversettings)
+{
+    (void)solverdata;
+    (void)solversettings;
+    g_si = systeminfo;
+    const int nf = settings.numberoffields;
+    if (nf == 0) return;
+    if (systeminfo.size != 1) die("diffusion: the GB300 path runs one MPI rank", TM_EINVAL, __LINE__);
+    if (nf > 64) die("diffusion: more than 64 fields", TM_EINVAL, __LINE__);
+    const int64_t gs[3] = {grid->localsize.x, grid->localsize.y, grid->localsize.z};
+    if (!g_diff || gs[0] != g_diff_gs[0] || gs[1] != g_diff_gs[1] || gs[2] != g_diff_gs[2]) {
+        if (g_diff) tm_diffusion_destroy(g_diff);
+        g_diff = NULL;
+        TRY("diffusion solver", tm_diffusion_create(&g_diff, gs, 0));
+        memcpy(g_diff_gs, gs, sizeof gs);
+    }
+    double mean[64], dc[64], bc[64], lam[64];
+    for (int f = 0; f < nf; f++) {
+        mean[f] = (*environment)[f].initialconditionmean;
+        dc[f] = (*environment)[f].diffusioncoefficient;
+        bc[f] = (*environment)[f].boundarycondition;
+        lam[f] = (*environment)[f].lambdadelay;
+    }
+    tm_diffusion_stats st;
+    TRY("diffusion step", tmi_env_compute(g_diff, nf, mean, dc, bc, lam, grid->resolution, settings.secondsperstep,
+                                          settings.gfdt, settings.step, &st));
+    if (g_env_writeback)
+        for (int f = 0; f < nf; f++) TRY("diffusion result", tmi_env_solution(g_diff, f, (*environment)[f].data));
+}
+
+int tm_dropin_env_solution(int field, double *out)
+{
+    if (!g_diff) return TM_EINVAL;
+    return tmi_env_solution(g_diff, field, out);
+}
+
+void tm_dropin_set_env_writeback(int on) { g_env_writeback = on ? 1 : 0; }
+
 void tm_dropin_shutdown(void)
 {
+    if (g_diff) tm_diffusion_destroy(g_diff);
+    g_diff = NULL;
     if (g_pinned) tm_host_unregister(g_pinned);
     g_pinned = NULL;
     g_pinned_bytes = 0;

@@ -56,6 +56,12 @@ int tmi_cycle_aos(tm_session *s, int cid, void *cells, int64_t n, int64_t cap, c
  * type t in phase p (p = 7 for the necrotic phase) */
 int tmi_compact_aos(tm_session *s, void *cells, int64_t n, int64_t oldlnc, const unsigned char *removecell,
                     int64_t *nout, int64_t removed[64]);
+/* environment_compute's fields on the device (every field from its mean,
+ * the reference's point source); tmi_env_solution reads field f back */
+int tmi_env_compute(tm_diffusion *d, int nfields, const double *mean, const double *dc, const double *bc,
+                    const double *lambda, float resolution, float secondsperstep, float gfdt, int step,
+                    tm_diffusion_stats *stats);
+int tmi_env_solution(tm_diffusion *d, int f, double *host);
 /* gradient of one field, host arrays */
 int tmi_field_gradient_host(tm_session *s, const double *data, const int64_t gsize[3], float resolution,
                             double *gradient);

@@ -34,6 +34,13 @@ static int tm_fail(int code, const char *fmt, ...)
             return tm_fail(TM_ECUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
     } while (0)
 
+// the same message slot for the other translation units
+int tm_report(int code, const char *msg)
+{
+    g_err = msg;
+    return code;
+}
+
 extern "C" const char *tm_last_error(void) { return g_err.c_str(); }
 extern "C" const char *tm_version(void) { return "timothy_gb300 0.1 sm_103a"; }
 

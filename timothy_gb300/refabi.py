@@ -135,9 +135,20 @@ def _bind(lib):
                                      C.c_void_p, C.c_void_p, C.POINTER(C.c_int64)]
     lib.updatecellcycles.restype = C.c_int
     lib.cellsdeath.argtypes = [C.c_int, C.POINTER(cellsinfo_t), C.c_void_p, C.c_int64]
+    PENV = C.POINTER(C.POINTER(environment_t))
+    lib.environment_allocate.argtypes = [systeminfo_t, settings_t, grid_t, PENV, C.c_void_p, C.c_void_p]
+    lib.environment_init.argtypes = [systeminfo_t, settings_t, grid_t, PENV]
+    lib.environment_initsystem.argtypes = [systeminfo_t, settings_t, C.POINTER(grid_t), PENV, C.c_void_p,
+                                           C.c_void_p]
+    lib.environment_compute.argtypes = lib.environment_initsystem.argtypes
+    lib.tm_dropin_env_solution.argtypes = [C.c_int, C.c_void_p]
+    lib.tm_dropin_env_solution.restype = C.c_int
+    lib.tm_dropin_set_env_writeback.argtypes = [C.c_int]
     for f in ("octbuild", "octfree", "computepotential", "computeremotepotential", "computegradient",
               "computeremotegradient", "updatepositions", "patches_alloc", "patches_cells2envinfo",
-              "patches_applyenv2cells", "fieldgradient", "cellsdeath", "tm_dropin_shutdown"):
+              "patches_applyenv2cells", "fieldgradient", "cellsdeath", "environment_allocate", "environment_init",
+              "environment_initsystem", "environment_compute", "tm_dropin_set_env_writeback",
+              "tm_dropin_shutdown"):
         getattr(lib, f).restype = None
     lib._refabi_bound = True
     return lib
@@ -371,3 +382,77 @@ class DropinRun:
 
     def __exit__(self, *exc):
         self.shutdown()
+
+
+class EnvironmentRun:
+    """The reference's field set-up and implicit diffusion step
+    (environment.c:33-523: environment_allocate, environment_init,
+    environment_initsystem, environment_compute) through the drop-ins, at one
+    rank on the grid of the given resolution."""
+
+    def __init__(self, dim: int, gfh: float, fields: list[dict], *, secondsperstep: float, gfdt: float,
+                 step: int = 1):
+        """fields: dicts with dc, bc, mean, variance, lam."""
+        self.lib = _bind(load_library())
+        self.si = systeminfo_t()
+        self.si.rank, self.si.size = 0, 1
+        self.si.dim[0] = self.si.dim[1] = self.si.dim[2] = 1
+        self.st = settings_t()
+        self.st.dimension = dim
+        self.st.numberoffields = len(fields)
+        self.st.gfh = gfh
+        self.st.gfdt = gfdt
+        self.st.secondsperstep = secondsperstep
+        self.st.step = step
+        (gx, gy, gz), lower = grid_geometry(dim, gfh)
+        self.gsize = (gx, gy, gz)
+        g = grid_t()
+        g.resolution = gfh
+        g.lowercorner.x, g.lowercorner.y, g.lowercorner.z = lower
+        g.localsize.x, g.localsize.y, g.localsize.z = gx, gy, gz
+        g.globalsize.x, g.globalsize.y, g.globalsize.z = gx, gy, (gz if dim == 3 else 0)
+        self.grid = g
+        self.envs = (environment_t * len(fields))()
+        for e, f in zip(self.envs, fields):
+            e.diffusioncoefficient = f["dc"]
+            e.boundarycondition = f["bc"]
+            e.initialconditionmean = f["mean"]
+            e.initialconditionvariance = f.get("variance", 0.0)
+            e.lambdadelay = f.get("lam", 0.0)
+        self.penv = C.cast(self.envs, C.POINTER(environment_t))
+        self.lib.environment_allocate(self.si, self.st, self.grid, C.byref(self.penv), None, None)
+        self.lib.environment_init(self.si, self.st, self.grid, C.byref(self.penv))
+        self.lib.environment_initsystem(self.si, self.st, C.byref(self.grid), C.byref(self.penv), None, None)
+
+    def compute(self, writeback: bool = False):
+        self.lib.tm_dropin_set_env_writeback(1 if writeback else 0)
+        self.lib.environment_compute(self.si, self.st, C.byref(self.grid), C.byref(self.penv), None, None)
+
+    def data(self, f: int) -> np.ndarray:
+        n = int(np.prod(self.gsize))
+        return np.ctypeslib.as_array(C.cast(self.envs[f].data, C.POINTER(C.c_double)), shape=(n,)).reshape(
+            self.gsize).copy()
+
+    def solution(self, f: int) -> np.ndarray:
+        out = np.zeros(self.gsize)
+        rc = self.lib.tm_dropin_env_solution(f, out.ctypes.data)
+        if rc:
+            raise RuntimeError(f"tm_dropin_env_solution: {rc}")
+        return out
+
+    def close(self):
+        libc = C.CDLL(None)
+        libc.free.argtypes = [C.c_void_p]
+        for e in self.envs:
+            for k in ("data", "production", "gradient"):
+                if getattr(e, k):
+                    libc.free(getattr(e, k))
+                    setattr(e, k, None)
+        self.lib.tm_dropin_set_env_writeback(0)
+        self.lib.tm_dropin_shutdown()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

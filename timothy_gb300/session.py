@@ -115,6 +115,13 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "tm_session_list_rate": (C.c_int, [P, P, P]),
         "tm_env2cells": (C.c_int, [P, P, P, C.c_int64, C.c_int, P, C.c_float, P, C.c_int, P, P, P, P]),
         "tm_field_gradient": (C.c_int, [P, P, C.c_float, C.c_int, P, P]),
+        "tm_diffusion_create": (C.c_int, [C.POINTER(P), P, C.c_int]),
+        "tm_diffusion_destroy": (C.c_int, [P]),
+        "tm_diffusion_levels": (C.c_int, [P]),
+        "tm_diffusion_step": (C.c_int, [P, P, C.c_float, C.c_int, P, P, P, C.c_float, C.c_float, P, C.c_double, P,
+                                        P]),
+        "tm_field_diffuse": (C.c_int, [P, P, C.c_float, C.c_int, P, P, P, C.c_float, C.c_float, P, C.c_double, P,
+                                       P]),
         "tm_colony_env2cells": (C.c_int, [P, C.c_int, P, C.c_float, P, C.c_int, P, P, P]),
         "tm_colony_write_vtk": (C.c_int, [P, C.c_int, C.c_char_p, C.c_int]),
         "tm_colony_compact": (C.c_int, [P, C.c_int, P]),
@@ -185,6 +192,53 @@ def field_gradient_device(data, gsize, resolution: float, nfields: int, gradient
     gs = np.ascontiguousarray(gsize, np.int64)
     _check(load_library().tm_field_gradient(_dptr(data), _p(gs), float(resolution), int(nfields), _dptr(gradient),
                                             None if stream is None else _dptr(stream)))
+
+
+class DiffusionStats(C.Structure):
+    _fields_ = [("solves_per_field", C.c_int), ("iterations", C.c_int), ("max_iterations", C.c_int),
+                ("multigrid_fields", C.c_int), ("levels", C.c_int), ("max_relative_residual", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Diffusion:
+    """tm_diffusion: the implicit diffusion step of environment_compute on
+    device fields of one grid size (work vectors allocated once)."""
+
+    def __init__(self, gsize, device: int = 0):
+        self.lib = load_library()
+        self.gsize = tuple(int(v) for v in gsize)
+        gs = np.ascontiguousarray(self.gsize, np.int64)
+        h = C.c_void_p()
+        _check(self.lib.tm_diffusion_create(C.byref(h), _p(gs), int(device)))
+        self.h = h
+
+    @property
+    def levels(self) -> int:
+        return int(self.lib.tm_diffusion_levels(self.h))
+
+    def step(self, data, resolution: float, dc, bc, lam, secondsperstep: float, gfdt: float, source=None,
+             tol: float = 1e-12, stream=None) -> dict:
+        """One step on data (CUDA array, nfields x gsize, z fastest), in place."""
+        dcs, bcs, lams = (np.ascontiguousarray(np.atleast_1d(v), np.float64) for v in (dc, bc, lam))
+        st = DiffusionStats()
+        _check(self.lib.tm_diffusion_step(self.h, _dptr(data), float(resolution), len(dcs), _p(dcs), _p(bcs),
+                                          _p(lams), float(secondsperstep), float(gfdt),
+                                          None if source is None else _dptr(source), float(tol), C.byref(st),
+                                          None if stream is None else _dptr(stream)))
+        return st.as_dict()
+
+    def close(self):
+        if self.h:
+            self.lib.tm_diffusion_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 def host_register(a: np.ndarray):
