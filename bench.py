@@ -341,6 +341,86 @@ def field_rows(device, peak, steps=10):
                           "cell_gathers_per_s": n / (ms_e * 1e-3)}}
 
 
+def diffusion_rows(device, steps=3):
+    """The implicit diffusion step (environment_compute) on the 257^3 FP64 grid
+    of GFH 8, one field, from the reference's start (the mean) with its point
+    source: with the reference's sample parameters (DC 1.82e-5, SECPERSTEP =
+    GFDT = 16000: z = 4.6e-3, one solve per step) and with DC 2.0 (z = 500, a
+    stiff operator: the multigrid preconditioner).  Each step is timed with
+    CUDA events on the default stream (it waits for each iteration's norm)."""
+    import torch
+
+    from timothy_gb300 import session as S
+
+    torch.cuda.set_device(device)
+    gs = (257, 257, 257)
+    src = torch.zeros((1,) + gs, dtype=torch.float64, device="cuda")
+    src[0, 5, 5, 5] = 100.0
+    out = {"config": "257^3 FP64 grid (GFH 8), 1 field, mean 0.1575e-6, BC 0.1575e-6, point source 100 at "
+                     "(5,5,5), SECPERSTEP = GFDT = 16000, tolerance 1e-12 (the reference's)"}
+    with S.Diffusion(gs, device=device) as d:
+        for name, dc in (("reference_parameters", 1.82e-5), ("stiff_dc2", 2.0)):
+            ms, st = [], None
+            for k in range(steps + 1):
+                u = torch.full((1,) + gs, 0.1575e-6, dtype=torch.float64, device="cuda")
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record()
+                st = d.step(u, 8.0, [dc], [0.1575e-6], [0.0], 16000.0, 16000.0, source=src, tol=1e-12)
+                b.record()
+                torch.cuda.synchronize()
+                if k:
+                    ms.append(a.elapsed_time(b))
+            out[name] = {"ms_per_step": float(np.mean(ms)), "nodes_per_s": float(np.prod(gs)) / (np.mean(ms) * 1e-3),
+                         "z": dc * 16000.0 / 64.0, **st}
+    return out
+
+
+def cycle_rows(device, reps=5):
+    """The cell cycle with mitosis (tm_colony_cellcycle) and the removal that
+    follows (tm_colony_compact) on a resident colony of 1,000,000 clustered
+    cells (seed 2): phases G0/G1/S/G2/M with probabilities .1/.4/.25/.21/.04,
+    phase times uniform in [0, 12) h, lengths 11/8/4/1 h, death probability
+    0.1, one step of 3600 s, so that the M cells (4 %) divide and about 2 %
+    die; wall time per call (each waits for its draw counts and the C
+    library's rand() values)."""
+    import dataclasses
+    import time
+
+    from timothy_gb300 import session as S
+
+    n = 1_000_000
+    col = C.make_colony("clustered", n, 2, radius_for("clustered", n, 2))
+    rng = np.random.Generator(np.random.PCG64(9))
+    types = {"g1": [11.0], "s": [8.0], "g2": [4.0], "m": [1.0], "v": [0.2], "rd": [0.1], "cd": [1e9]}
+    t_cyc, t_cmp, divided, marked = [], [], [], []
+    with S.Session(col.types, dim=3, max_slots=3 * n, device=device) as s:
+        for k in range(reps + 1):
+            phase = rng.choice(5, size=n, p=[0.1, 0.4, 0.25, 0.21, 0.04]).astype(np.int32)
+            cid = s.add_colony(dataclasses.replace(col, phase=phase), precision="fp64", update="dt", dt=0.01,
+                               reserve=2 * n)
+            s.set_cycle(cid, rng.uniform(0.0, 12.0, n), np.full(n, 11.0), np.full(n, 8.0), np.full(n, 4.0),
+                        np.full(n, 1.0), np.zeros(n, np.int32))
+            s.sync()
+            t0 = time.perf_counter()
+            dv, mk = s.cellcycle(cid, types, secondsperstep=3600.0)
+            s.sync()
+            t1 = time.perf_counter()
+            s.compact(cid)
+            s.sync()
+            t2 = time.perf_counter()
+            s.remove_colony(cid)
+            if k:
+                t_cyc.append((t1 - t0) * 1e3)
+                t_cmp.append((t2 - t1) * 1e3)
+                divided.append(dv)
+                marked.append(mk)
+    return {"config": "1,000,000 clustered cells (seed 2), phases G0/G1/S/G2/M .1/.4/.25/.21/.04, phase times "
+                      "uniform in [0, 12) h, lengths 11/8/4/1 h, rd 0.1, one step of 3600 s",
+            "cellcycle_ms": float(np.mean(t_cyc)), "compact_ms": float(np.mean(t_cmp)),
+            "cells_per_s": n / (np.mean(t_cyc) * 1e-3), "divided": int(np.mean(divided)),
+            "marked": int(np.mean(marked))}
+
+
 def _size_bins(reqs):
     out = {}
     for lo, hi in ((1e3, 1e4), (1e4, 1e5), (1e5, 1e6 + 1)):
@@ -371,8 +451,16 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=50)
     ap.add_argument("--serve-rates", default="200,50", help="request rates (per s) of the serving runs")
     ap.add_argument("--serve-seconds", type=float, default=20.0)
+    ap.add_argument("--row", choices=["grid_to_cell", "diffusion", "cell_cycle"],
+                    help="measure one of the rows beside the path alone and print it (no bench line)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.row:
+        peak = measured_peaks()[0]
+        fn = {"grid_to_cell": lambda: field_rows(0, peak), "diffusion": lambda: diffusion_rows(0),
+              "cell_cycle": lambda: cycle_rows(0)}[args.row]
+        print(json.dumps({args.row: fn()}))
+        return 0
     wl = dict(WORKLOADS[args.workload])
     if args.n:
         wl["n"] = args.n
@@ -512,7 +600,8 @@ def main():
         cpu = cpu_sample(wl)
 
     if not args.no_forms and world == 1:
-        extra["rows"] = {"grid_to_cell": field_rows(local, peak)}
+        extra["rows"] = {"grid_to_cell": field_rows(local, peak), "diffusion": diffusion_rows(local),
+                         "cell_cycle": cycle_rows(local)}
         forms = {"batched": batched_form(args, local)}
         forms["serving"] = [serving_form(args, local, float(r), args.serve_seconds)
                             for r in args.serve_rates.split(",") if r]

@@ -264,14 +264,16 @@ int tm_field_gradient(const double *data, const int64_t gsize[3], float resoluti
  * picks from secondsperstep / gfdt (environment.c:144-164), each of
  * A u = u + z bc (once per grid face the node lies on) + source, starting
  * from data, which receives the result.  source: device, same layout, or
- * NULL.  Each solve runs preconditioned conjugate gradients (a geometric
- * multigrid V-cycle preconditions stiff operators) to a relative residual of
- * tol (the reference asks its Hypre PCG for 1e-12). */
+ * NULL.  Each solve reaches a relative FP64 residual |b - A u| / |b| <= tol
+ * (the reference asks its Hypre PCG for 1e-12) by iterative refinement: FP64
+ * residuals, FP32 corrections by preconditioned conjugate gradients (a
+ * geometric multigrid V-cycle preconditions stiff operators). */
 typedef struct tm_diffusion tm_diffusion;
 typedef struct tm_diffusion_stats {
     int solves_per_field;          /* numberofiters */
-    int iterations;                /* CG iterations over all solves */
+    int iterations;                /* FP32 CG iterations over all solves */
     int max_iterations;            /* of one solve */
+    int refinements;               /* FP64 residual corrections over all solves */
     int multigrid_fields;          /* fields solved with the multigrid preconditioner */
     int levels;                    /* multigrid levels of the grid */
     double max_relative_residual;  /* largest final |b - A u| / |b| */

@@ -1,5 +1,5 @@
 """Implicit diffusion step (environment_compute, environment.c:131-523) on the
-GPU: against the reference's own environment.c run on the Hypre stand-in
+GPU (FP64 residuals, FP32 multigrid-preconditioned corrections): against the reference's own environment.c run on the Hypre stand-in
 (tests/golden/field_diffuse_*.npz), against the oracle on other grids and
 inputs, and at the full grid of the default resolution (GFH 8, 257^3 nodes)
 through the residual of the solution, checked with an independent torch FP64
@@ -113,7 +113,7 @@ def test_diffusion_reproducible_and_multigrid():
         outs.append(data.cpu().numpy())
     assert np.array_equal(outs[0], outs[1])
     assert st["multigrid_fields"] == 1 and st["levels"] == 6
-    assert st["max_iterations"] <= 30
+    assert st["max_iterations"] <= 60 and st["refinements"] <= 6
     assert st["max_relative_residual"] <= 1e-12
 
 

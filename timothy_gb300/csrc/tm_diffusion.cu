@@ -7,14 +7,22 @@
 // "faces" adding z * bc once for each grid face the node lies on, in the
 // reference's order x-, x+, y-, y+, z-, z+ (a one-layer grid lies on both z
 // faces).  The reference hands the system to Hypre's PCG with a BoomerAMG
-// preconditioner (tolerance 1e-12, at most 50 iterations); here it is
-// preconditioned conjugate gradients to a relative residual of tol with a
-// geometric multigrid V(1,1)-cycle as the preconditioner when the operator is
-// stiff (condition bound (1 + 12 z + lambda dt) / (1 + lambda dt) above 30),
-// plain CG otherwise (the diagonal is constant).
+// preconditioner (tolerance 1e-12, at most 50 iterations); here each solve
+// reaches a relative FP64 residual |b - A u| / |b| <= tol.
 //
-// Multigrid: vertex-centred coarsening (n -> (n + 1) / 2 along every axis
-// with more than 3 nodes), the operator rediscretised per level (z_d / 4 along
+// The FP64 pipe of this GPU is narrow, so a solve is iterative refinement:
+// the residual r = b - A u and the update u += |r| d are FP64, and the
+// correction d solves A d = r / |r| in FP32 by preconditioned conjugate
+// gradients to a relative residual of 1e-5 (each refinement gains about five
+// digits; the FP64 residual is the stopping test).  The inner preconditioner
+// is a geometric multigrid V(1,1)-cycle in FP32 when the operator is stiff
+// (condition bound (1 + 12 z + lambda dt) / (1 + lambda dt) above 30), the
+// constant diagonal otherwise.
+//
+// Multigrid: coarsening n -> n / 2 along every axis with more than 3 nodes,
+// coarse node I on fine node 2I + 1, so that the coarse grid's Dirichlet
+// ghost below node 0 is the fine grid's (and, for odd n, the one above the
+// last node too); the operator rediscretised per level (z_d / 4 along
 // a coarsened axis), full weighting (the transpose of trilinear interpolation
 // over 2^dc), red-black Gauss-Seidel (red then black before the coarse
 // correction, black then red after it, so the cycle is symmetric), and on the
@@ -23,9 +31,9 @@
 // couplings to nodes outside the grid are absent.
 //
 // Reductions are deterministic: every reduction kernel runs on a fixed grid
-// and writes one partial per block, and one block adds the partials in a
-// fixed order; the CG scalars (alpha, beta) stay on the device.  The host
-// reads the residual norm once per iteration for the stopping test.
+// and writes one FP64 partial per block, and one block adds the partials in
+// a fixed order; the CG scalars stay on the device.  The host reads a norm
+// once per iteration for the stopping tests.
 #include "tm_kernels.cuh"
 #include "timothy_gb300.h"
 
@@ -42,6 +50,8 @@ constexpr int kThreads = 256;
 constexpr int kRedBlocks = 152 * 4;      // reduction grid: partials per reduction
 constexpr int kCoarseMax = 27;           // at most 3 nodes per axis on the coarsest grid
 constexpr int kCoarseSweeps = 64;
+constexpr double kInnerTol = 1e-5;       // relative residual of one FP32 correction solve
+constexpr int kMaxRefine = 40;
 
 struct level {
     unsigned nx, ny, nz;
@@ -50,9 +60,10 @@ struct level {
     __host__ __device__ unsigned size() const { return nx * ny * nz; }
 };
 
-// CG scalars on the device
+// scalars on the device: outer (FP64 residual) and inner (FP32 CG)
 struct scalars {
-    double bb, rr, rho, rho_new, pq, alpha, beta;
+    double bb, rr;                            // |b|^2, |b - A u|^2
+    double rho, pq, alpha, beta, ss;          // inner CG
 };
 
 __device__ __forceinline__ void coords(const level &L, unsigned o, unsigned &i, unsigned &j, unsigned &k)
@@ -64,25 +75,29 @@ __device__ __forceinline__ void coords(const level &L, unsigned o, unsigned &i, 
     k = r - j * L.nz;
 }
 
-// sum of z_d times the in-grid neighbours of node o
-__device__ __forceinline__ double neighbours(const level &L, const double *u, unsigned o, unsigned i, unsigned j,
-                                             unsigned k)
+// in-grid neighbour sums along x, y, z
+template <typename T>
+__device__ __forceinline__ void nbsums(const level &L, const T *u, unsigned o, unsigned i, unsigned j, unsigned k,
+                                       T &sx, T &sy, T &sz)
 {
     const unsigned nyz = L.ny * L.nz;
-    double sx = 0.0, sy = 0.0, sz = 0.0;
+    sx = T(0);
+    sy = T(0);
+    sz = T(0);
     if (i > 0) sx += u[o - nyz];
     if (i + 1 < L.nx) sx += u[o + nyz];
     if (j > 0) sy += u[o - L.nz];
     if (j + 1 < L.ny) sy += u[o + L.nz];
     if (k > 0) sz += u[o - 1];
     if (k + 1 < L.nz) sz += u[o + 1];
-    return L.zx * sx + L.zy * sy + L.zz * sz;
 }
 
-__device__ __forceinline__ double apply(const level &L, const double *u, unsigned o, unsigned i, unsigned j,
-                                        unsigned k)
+template <typename T>
+__device__ __forceinline__ T neighbours(const level &L, const T *u, unsigned o, unsigned i, unsigned j, unsigned k)
 {
-    return L.diag * u[o] - neighbours(L, u, o, i, j, k);
+    T sx, sy, sz;
+    nbsums(L, u, o, i, j, k, sx, sy, sz);
+    return T(L.zx) * sx + T(L.zy) * sy + T(L.zz) * sz;
 }
 
 // block sum into partial[blockIdx.x] (fixed order for a fixed launch)
@@ -99,9 +114,14 @@ __device__ __forceinline__ void block_partial(double v, double *partial)
     }
 }
 
-// b = u + faces + source; r = b - A u; partials of b.b
+// FP32 sums of one thread, then FP64 across the block
+__device__ __forceinline__ void block_partial32(float v, double *partial) { block_partial((double)v, partial); }
+
+// ------------------------------------------------------------ FP64 outer
+
+// b = u + faces + source; partials of b.b
 __global__ void __launch_bounds__(kThreads) k_rhs(level L, const double *u, const double *src, double zb, double *b,
-                                                  double *r, double *partial)
+                                                  double *partial)
 {
     double acc = 0.0;
     const unsigned G = L.size();
@@ -117,75 +137,118 @@ __global__ void __launch_bounds__(kThreads) k_rhs(level L, const double *u, cons
         if (k == L.nz - 1) v += zb;
         if (src) v += src[o];
         b[o] = v;
-        r[o] = v - apply(L, u, o, i, j, k);
         acc += v * v;
     }
     block_partial(acc, partial);
 }
 
-// partials of x.y
-__global__ void __launch_bounds__(kThreads) k_dot(unsigned G, const double *x, const double *y, double *partial)
+// r = b - A u (the fine operator has one coupling z for every axis); partials
+// of r.r.  FP64 instructions are the cost here: the neighbours outside the
+// grid are selected away, not added as zeros (5 adds for the six), and the
+// rest is two fused multiply-adds.
+__global__ void __launch_bounds__(kThreads) k_residual64(level L, const double *u, const double *b, double *r,
+                                                         double *partial)
 {
     double acc = 0.0;
-    for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < G; o += gridDim.x * blockDim.x) acc += x[o] * y[o];
-    block_partial(acc, partial);
-}
-
-// q = A p; partials of p.q
-__global__ void __launch_bounds__(kThreads) k_apply_dot(level L, const double *p, double *q, double *partial)
-{
-    double acc = 0.0;
-    const unsigned G = L.size();
+    const unsigned G = L.size(), nyz = L.ny * L.nz;
     for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < G; o += gridDim.x * blockDim.x) {
         unsigned i, j, k;
         coords(L, o, i, j, k);
-        const double v = apply(L, p, o, i, j, k);
+        const double xm = i > 0 ? u[o - nyz] : 0.0, xp = i + 1 < L.nx ? u[o + nyz] : 0.0;
+        const double ym = j > 0 ? u[o - L.nz] : 0.0, yp = j + 1 < L.ny ? u[o + L.nz] : 0.0;
+        const double zm = k > 0 ? u[o - 1] : 0.0, zp = k + 1 < L.nz ? u[o + 1] : 0.0;
+        const double s = ((xm + xp) + (ym + yp)) + (zm + zp);
+        const double v = fma(-L.diag, u[o], fma(L.zx, s, b[o]));
+        r[o] = v;
+        acc = fma(v, v, acc);
+    }
+    block_partial(acc, partial);
+}
+
+// s = r / |r| in FP32, d = 0
+__global__ void __launch_bounds__(kThreads) k_scale32(unsigned G, const double *r, const scalars *sc, float *s,
+                                                      float *d)
+{
+    const double inv = sc->rr > 0.0 ? 1.0 / sqrt(sc->rr) : 0.0;
+    for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < G; o += gridDim.x * blockDim.x) {
+        s[o] = (float)(r[o] * inv);
+        d[o] = 0.0f;
+    }
+}
+
+// u += |r| d
+__global__ void __launch_bounds__(kThreads) k_correct64(unsigned G, double *u, const float *d, const scalars *sc)
+{
+    const double nr = sqrt(sc->rr);
+    for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < G; o += gridDim.x * blockDim.x)
+        u[o] += nr * (double)d[o];
+}
+
+// ------------------------------------------------------------ FP32 inner CG
+
+// q = A p; partials of p.q
+__global__ void __launch_bounds__(kThreads) k_apply_dot32(level L, const float *p, float *q, double *partial)
+{
+    float acc = 0.0f;
+    const unsigned G = L.size();
+    const float dg = (float)L.diag;
+    for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < G; o += gridDim.x * blockDim.x) {
+        unsigned i, j, k;
+        coords(L, o, i, j, k);
+        const float v = dg * p[o] - neighbours(L, p, o, i, j, k);
         q[o] = v;
         acc += p[o] * v;
     }
-    block_partial(acc, partial);
+    block_partial32(acc, partial);
 }
 
-// u += alpha p; r -= alpha q; partials of r.r
-__global__ void __launch_bounds__(kThreads) k_update(unsigned G, double *u, double *r, const double *p,
-                                                     const double *q, const scalars *sc, double *partial)
+// d += alpha p; s -= alpha q; partials of s.s
+__global__ void __launch_bounds__(kThreads) k_update32(unsigned G, float *d, float *s, const float *p, const float *q,
+                                                       const scalars *sc, double *partial)
 {
-    const double a = sc->alpha;
-    double acc = 0.0;
+    const float a = (float)sc->alpha;
+    float acc = 0.0f;
     for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < G; o += gridDim.x * blockDim.x) {
-        u[o] += a * p[o];
-        const double v = r[o] - a * q[o];
-        r[o] = v;
+        d[o] += a * p[o];
+        const float v = s[o] - a * q[o];
+        s[o] = v;
         acc += v * v;
     }
-    block_partial(acc, partial);
+    block_partial32(acc, partial);
 }
 
-// p = zv + beta p (beta = 0: p = zv)
-__global__ void __launch_bounds__(kThreads) k_direction(unsigned G, double *p, const double *zv, const scalars *sc,
-                                                        int first)
+// p = zv + beta p (first: p = zv)
+__global__ void __launch_bounds__(kThreads) k_direction32(unsigned G, float *p, const float *zv, const scalars *sc,
+                                                          int first)
 {
-    const double be = first ? 0.0 : sc->beta;
+    const float be = first ? 0.0f : (float)sc->beta;
     for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < G; o += gridDim.x * blockDim.x)
         p[o] = first ? zv[o] : zv[o] + be * p[o];
 }
 
-// zv = r / diag; partials of r.zv
-__global__ void __launch_bounds__(kThreads) k_jacobi_dot(unsigned G, const double *r, double *zv, double inv_diag,
-                                                         double *partial)
+// zv = s / diag; partials of s.zv
+__global__ void __launch_bounds__(kThreads) k_jacobi_dot32(unsigned G, const float *s, float *zv, float inv_diag,
+                                                           double *partial)
 {
-    double acc = 0.0;
+    float acc = 0.0f;
     for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < G; o += gridDim.x * blockDim.x) {
-        const double v = r[o] * inv_diag;
+        const float v = s[o] * inv_diag;
         zv[o] = v;
-        acc += r[o] * v;
+        acc += s[o] * v;
     }
-    block_partial(acc, partial);
+    block_partial32(acc, partial);
+}
+
+// partials of x.y (FP32 vectors)
+__global__ void __launch_bounds__(kThreads) k_dot32(unsigned G, const float *x, const float *y, double *partial)
+{
+    float acc = 0.0f;
+    for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < G; o += gridDim.x * blockDim.x) acc += x[o] * y[o];
+    block_partial32(acc, partial);
 }
 
 // one block adds the partials in a fixed order and updates the scalars:
-// what 0: bb and rr (after k_rhs / k_dot of r); 1: pq -> alpha;
-// 2: rr; 3: rho (first); 4: rho_new -> beta, rho
+// 0: bb; 1: rr; 2: pq -> alpha; 3: ss; 4: rho (first); 5: rho -> beta
 __global__ void __launch_bounds__(kThreads) k_finish(const double *partial, int n, scalars *sc, int what)
 {
     double v = 0.0;
@@ -201,32 +264,32 @@ __global__ void __launch_bounds__(kThreads) k_finish(const double *partial, int 
     const double t = sh[0];
     switch (what) {
     case 0: sc->bb = t; break;
-    case 1:
+    case 1: sc->rr = t; break;
+    case 2:
         sc->pq = t;
         sc->alpha = t != 0.0 ? sc->rho / t : 0.0;
         break;
-    case 2: sc->rr = t; break;
-    case 3: sc->rho = t; break;
-    case 4:
-        sc->rho_new = t;
+    case 3: sc->ss = t; break;
+    case 4: sc->rho = t; break;
+    case 5:
         sc->beta = sc->rho != 0.0 ? t / sc->rho : 0.0;
         sc->rho = t;
         break;
     }
 }
 
-// ---------------------------------------------------------------- multigrid
+// ---------------------------------------------------------------- multigrid (FP32)
 
-__global__ void __launch_bounds__(kThreads) k_zero(unsigned G, double *e)
+__global__ void __launch_bounds__(kThreads) k_zero(unsigned G, float *e)
 {
-    for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < G; o += gridDim.x * blockDim.x) e[o] = 0.0;
+    for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < G; o += gridDim.x * blockDim.x) e[o] = 0.0f;
 }
 
 // Gauss-Seidel on the nodes of one colour ((i + j + k) & 1 == colour)
-__global__ void __launch_bounds__(kThreads) k_rbgs(level L, double *e, const double *f, int colour)
+__global__ void __launch_bounds__(kThreads) k_rbgs(level L, float *e, const float *f, int colour)
 {
     const unsigned G = L.size();
-    const double inv = 1.0 / L.diag;
+    const float inv = (float)(1.0 / L.diag);
     for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < G; o += gridDim.x * blockDim.x) {
         unsigned i, j, k;
         coords(L, o, i, j, k);
@@ -236,44 +299,44 @@ __global__ void __launch_bounds__(kThreads) k_rbgs(level L, double *e, const dou
 }
 
 // res = f - A e
-__global__ void __launch_bounds__(kThreads) k_residual(level L, const double *e, const double *f, double *res)
+__global__ void __launch_bounds__(kThreads) k_residual32(level L, const float *e, const float *f, float *res)
 {
     const unsigned G = L.size();
+    const float dg = (float)L.diag;
     for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < G; o += gridDim.x * blockDim.x) {
         unsigned i, j, k;
         coords(L, o, i, j, k);
-        res[o] = f[o] - apply(L, e, o, i, j, k);
+        res[o] = f[o] - (dg * e[o] - neighbours(L, e, o, i, j, k));
     }
 }
 
-// weights of fine index fi for coarse index I along an axis (coarsened or not)
-__device__ __forceinline__ void axis_taps(unsigned I, unsigned nf, bool coarse, unsigned *idx, double *w, int &n)
+// fine indices and weights restricting to coarse index I along an axis: the
+// coarse node sits on fine node 2I + 1 and takes its two fine neighbours at
+// half weight (the first fine node's other coarse neighbour, and the last's
+// on a grid of odd size, are the Dirichlet ghosts)
+__device__ __forceinline__ void axis_taps(unsigned I, unsigned nf, bool coarse, unsigned *idx, float *w, int &n)
 {
     if (!coarse) {
         idx[0] = I;
-        w[0] = 1.0;
+        w[0] = 1.0f;
         n = 1;
         return;
     }
-    n = 0;
-    const unsigned c = 2 * I;
-    if (c < nf) {
-        idx[n] = c;
-        w[n++] = 1.0;
-    }
-    if (c >= 1 && c - 1 < nf) {
-        idx[n] = c - 1;
-        w[n++] = 0.5;
-    }
+    const unsigned c = 2 * I + 1;       // < nf: I < nf / 2
+    idx[0] = c;
+    w[0] = 1.0f;
+    idx[1] = c - 1;
+    w[1] = 0.5f;
+    n = 2;
     if (c + 1 < nf) {
-        idx[n] = c + 1;
-        w[n++] = 0.5;
+        idx[2] = c + 1;
+        w[2] = 0.5f;
+        n = 3;
     }
 }
 
 // f_c = R res_f (the transpose of interpolation over 2^dc)
-__global__ void __launch_bounds__(kThreads) k_restrict(level Lf, level Lc, const double *res, double *fc,
-                                                       double scale)
+__global__ void __launch_bounds__(kThreads) k_restrict(level Lf, level Lc, const float *res, float *fc, float scale)
 {
     const unsigned G = Lc.size();
     const bool cx = Lc.nx != Lf.nx, cy = Lc.ny != Lf.ny, cz = Lc.nz != Lf.nz;
@@ -281,12 +344,12 @@ __global__ void __launch_bounds__(kThreads) k_restrict(level Lf, level Lc, const
         unsigned I, J, K;
         coords(Lc, o, I, J, K);
         unsigned ix[3], iy[3], iz[3];
-        double wx[3], wy[3], wz[3];
+        float wx[3], wy[3], wz[3];
         int nx, ny, nz;
         axis_taps(I, Lf.nx, cx, ix, wx, nx);
         axis_taps(J, Lf.ny, cy, iy, wy, ny);
         axis_taps(K, Lf.nz, cz, iz, wz, nz);
-        double s = 0.0;
+        float s = 0.0f;
         for (int a = 0; a < nx; a++)
             for (int b = 0; b < ny; b++)
                 for (int c = 0; c < nz; c++)
@@ -295,33 +358,36 @@ __global__ void __launch_bounds__(kThreads) k_restrict(level Lf, level Lc, const
     }
 }
 
-// coarse indices and weights interpolating fine index fi along an axis
-__device__ __forceinline__ void axis_from(unsigned fi, unsigned nc, bool coarse, unsigned *idx, double *w, int &n)
+// coarse indices and weights interpolating fine index fi along an axis (the
+// transpose of axis_taps)
+__device__ __forceinline__ void axis_from(unsigned fi, unsigned nc, bool coarse, unsigned *idx, float *w, int &n)
 {
     if (!coarse) {
         idx[0] = fi;
-        w[0] = 1.0;
+        w[0] = 1.0f;
         n = 1;
         return;
     }
     n = 0;
-    if ((fi & 1u) == 0) {
-        idx[0] = fi >> 1;           // always < nc
-        w[0] = 1.0;
+    if (fi & 1u) {
+        idx[0] = fi >> 1;               // (fi - 1) / 2 < nc
+        w[0] = 1.0f;
         n = 1;
         return;
     }
-    const unsigned lo = fi >> 1, hi = lo + 1;
-    idx[n] = lo;
-    w[n++] = 0.5;
-    if (hi < nc) {                   // beyond the last coarse node: a Dirichlet ghost
+    const unsigned hi = fi >> 1;         // coarse neighbours hi - 1 and hi
+    if (hi >= 1) {
+        idx[n] = hi - 1;
+        w[n++] = 0.5f;
+    }
+    if (hi < nc) {
         idx[n] = hi;
-        w[n++] = 0.5;
+        w[n++] = 0.5f;
     }
 }
 
 // e_f += P e_c
-__global__ void __launch_bounds__(kThreads) k_prolong(level Lf, level Lc, const double *ec, double *ef)
+__global__ void __launch_bounds__(kThreads) k_prolong(level Lf, level Lc, const float *ec, float *ef)
 {
     const unsigned G = Lf.size();
     const bool cx = Lc.nx != Lf.nx, cy = Lc.ny != Lf.ny, cz = Lc.nz != Lf.nz;
@@ -329,12 +395,12 @@ __global__ void __launch_bounds__(kThreads) k_prolong(level Lf, level Lc, const 
         unsigned i, j, k;
         coords(Lf, o, i, j, k);
         unsigned ix[2], iy[2], iz[2];
-        double wx[2], wy[2], wz[2];
+        float wx[2], wy[2], wz[2];
         int nx, ny, nz;
         axis_from(i, Lc.nx, cx, ix, wx, nx);
         axis_from(j, Lc.ny, cy, iy, wy, ny);
         axis_from(k, Lc.nz, cz, iz, wz, nz);
-        double s = 0.0;
+        float s = 0.0f;
         for (int a = 0; a < nx; a++)
             for (int b = 0; b < ny; b++)
                 for (int c = 0; c < nz; c++) s += wx[a] * wy[b] * wz[c] * ec[(ix[a] * Lc.ny + iy[b]) * Lc.nz + iz[c]];
@@ -343,22 +409,23 @@ __global__ void __launch_bounds__(kThreads) k_prolong(level Lf, level Lc, const 
 }
 
 // the coarsest grid (at most kCoarseMax nodes): Jacobi sweeps from zero in one block
-__global__ void __launch_bounds__(32) k_coarse(level L, double *e, const double *f)
+__global__ void __launch_bounds__(32) k_coarse(level L, float *e, const float *f)
 {
-    __shared__ double a[kCoarseMax], b[kCoarseMax];
+    __shared__ float a[kCoarseMax], b[kCoarseMax];
     const unsigned G = L.size();
     const unsigned o = threadIdx.x;
-    if (o < G) a[o] = 0.0;
+    if (o < G) a[o] = 0.0f;
     __syncthreads();
-    double *cur = a, *nxt = b;
+    float *cur = a, *nxt = b;
+    const float inv = (float)(1.0 / L.diag);
     for (int s = 0; s < kCoarseSweeps; s++) {
         if (o < G) {
             unsigned i, j, k;
             coords(L, o, i, j, k);
-            nxt[o] = (f[o] + neighbours(L, cur, o, i, j, k)) / L.diag;
+            nxt[o] = (f[o] + neighbours(L, (const float *)cur, o, i, j, k)) * inv;
         }
         __syncthreads();
-        double *t = cur;
+        float *t = cur;
         cur = nxt;
         nxt = t;
     }
@@ -371,17 +438,24 @@ unsigned blocks_for(unsigned G)
     return b < 152u * 8u ? (b ? b : 1u) : 152u * 8u;
 }
 
+unsigned red_blocks(unsigned G)
+{
+    const unsigned b = blocks_for(G);
+    return b < (unsigned)kRedBlocks ? b : (unsigned)kRedBlocks;
+}
+
 }  // namespace
 
 struct tm_diffusion {
     int device = 0;
     int64_t gsize[3] = {0, 0, 0};
     std::vector<level> lv;              // geometry of the levels (couplings set per solve)
-    std::vector<double *> e, f, res;    // per level (level 0: e, f unused: the CG vectors)
-    double *b = nullptr, *r = nullptr, *p = nullptr, *q = nullptr, *zv = nullptr;
+    std::vector<float *> e, f, res;     // per level (level 0: the inner CG's vectors)
+    double *b = nullptr, *r = nullptr;  // FP64 right-hand side and residual
+    float *s = nullptr, *d = nullptr, *p = nullptr, *q = nullptr, *zv = nullptr;   // FP32 inner CG
     double *partial = nullptr;
     scalars *sc = nullptr;
-    scalars *h_sc = nullptr;            // page-locked copy for the stopping test
+    scalars *h_sc = nullptr;            // page-locked copy for the stopping tests
     double *field = nullptr;            // the drop-in's fields and source (nfields x G)
     double *src = nullptr;
     int field_n = 0;
@@ -399,11 +473,13 @@ struct tm_diffusion {
 
 static void diffusion_free(tm_diffusion *d)
 {
-    for (double *v : d->e) cudaFree(v);
-    for (double *v : d->f) cudaFree(v);
-    for (double *v : d->res) cudaFree(v);
+    for (float *v : d->e) cudaFree(v);
+    for (float *v : d->f) cudaFree(v);
+    for (float *v : d->res) cudaFree(v);
     cudaFree(d->b);
     cudaFree(d->r);
+    cudaFree(d->s);
+    cudaFree(d->d);
     cudaFree(d->p);
     cudaFree(d->q);
     cudaFree(d->zv);
@@ -428,16 +504,18 @@ extern "C" int tm_diffusion_create(tm_diffusion **out, const int64_t gsize[3], i
     level L{(unsigned)gsize[0], (unsigned)gsize[1], (unsigned)gsize[2], 0, 0, 0, 0};
     d->lv.push_back(L);
     while (L.nx > 3 || L.ny > 3 || L.nz > 3) {
-        L.nx = L.nx > 3 ? (L.nx + 1) / 2 : L.nx;
-        L.ny = L.ny > 3 ? (L.ny + 1) / 2 : L.ny;
-        L.nz = L.nz > 3 ? (L.nz + 1) / 2 : L.nz;
+        L.nx = L.nx > 3 ? L.nx / 2 : L.nx;
+        L.ny = L.ny > 3 ? L.ny / 2 : L.ny;
+        L.nz = L.nz > 3 ? L.nz / 2 : L.nz;
         d->lv.push_back(L);
     }
-    auto alloc = [&](double **p, size_t n) { return cudaMalloc((void **)p, n * sizeof(double)) == cudaSuccess; };
+    auto a64 = [&](double **p, size_t n) { return cudaMalloc((void **)p, n * sizeof(double)) == cudaSuccess; };
+    auto a32 = [&](float **p, size_t n) { return cudaMalloc((void **)p, n * sizeof(float)) == cudaSuccess; };
     bool ok = true;
     const size_t n0 = (size_t)G;
-    ok = ok && alloc(&d->b, n0) && alloc(&d->r, n0) && alloc(&d->p, n0) && alloc(&d->q, n0) && alloc(&d->zv, n0);
-    ok = ok && alloc(&d->partial, kRedBlocks);
+    ok = ok && a64(&d->b, n0) && a64(&d->r, n0);
+    ok = ok && a32(&d->s, n0) && a32(&d->d, n0) && a32(&d->p, n0) && a32(&d->q, n0) && a32(&d->zv, n0);
+    ok = ok && a64(&d->partial, kRedBlocks);
     ok = ok && cudaMalloc((void **)&d->sc, sizeof(scalars)) == cudaSuccess;
     ok = ok && cudaMallocHost((void **)&d->h_sc, sizeof(scalars)) == cudaSuccess;
     d->e.assign(d->lv.size(), nullptr);
@@ -445,8 +523,8 @@ extern "C" int tm_diffusion_create(tm_diffusion **out, const int64_t gsize[3], i
     d->res.assign(d->lv.size(), nullptr);
     for (size_t l = 0; ok && l < d->lv.size(); l++) {
         const size_t n = d->lv[l].size();
-        if (l > 0) ok = alloc(&d->e[l], n) && alloc(&d->f[l], n);
-        if (ok && l + 1 < d->lv.size()) ok = alloc(&d->res[l], n);
+        if (l > 0) ok = a32(&d->e[l], n) && a32(&d->f[l], n);
+        if (ok && l + 1 < d->lv.size()) ok = a32(&d->res[l], n);
     }
     if (!ok) {
         diffusion_free(d);
@@ -469,14 +547,13 @@ extern "C" int tm_diffusion_destroy(tm_diffusion *d)
 
 extern "C" int tm_diffusion_levels(const tm_diffusion *d) { return d ? (int)d->lv.size() : 0; }
 
-// the V-cycle applied to the residual r (level 0) into zv
+// the V-cycle applied to the inner residual s (level 0) into zv
 static int vcycle(tm_diffusion *d, const std::vector<level> &lv, cudaStream_t st)
 {
     const int nl = (int)lv.size();
-    // level 0 works on zv (error) and r (right-hand side)
-    std::vector<double *> E(nl), F(nl);
+    std::vector<float *> E(nl), F(nl);
     E[0] = d->zv;
-    F[0] = d->r;
+    F[0] = d->s;
     for (int l = 1; l < nl; l++) {
         E[l] = d->e[l];
         F[l] = d->f[l];
@@ -487,10 +564,10 @@ static int vcycle(tm_diffusion *d, const std::vector<level> &lv, cudaStream_t st
         k_zero<<<gb, kThreads, 0, st>>>(G, E[l]);
         k_rbgs<<<gb, kThreads, 0, st>>>(L, E[l], F[l], 0);
         k_rbgs<<<gb, kThreads, 0, st>>>(L, E[l], F[l], 1);
-        k_residual<<<gb, kThreads, 0, st>>>(L, E[l], F[l], d->res[l]);
+        k_residual32<<<gb, kThreads, 0, st>>>(L, E[l], F[l], d->res[l]);
         const level &C = lv[l + 1];
         const int dc = (C.nx != L.nx) + (C.ny != L.ny) + (C.nz != L.nz);
-        k_restrict<<<blocks_for(C.size()), kThreads, 0, st>>>(L, C, d->res[l], F[l + 1], 1.0 / (double)(1 << dc));
+        k_restrict<<<blocks_for(C.size()), kThreads, 0, st>>>(L, C, d->res[l], F[l + 1], 1.0f / (float)(1 << dc));
     }
     k_coarse<<<1, 32, 0, st>>>(lv[nl - 1], E[nl - 1], F[nl - 1]);
     for (int l = nl - 2; l >= 0; l--) {
@@ -511,50 +588,64 @@ static int read_scalars(tm_diffusion *d, cudaStream_t st)
     return TM_OK;
 }
 
-// solve A u = b (b already in d->b, r = b - A u) by PCG; returns iterations
-static int pcg(tm_diffusion *d, const std::vector<level> &lv, double *u, double tol, int max_iter, bool mg,
-               cudaStream_t st, int *iters, double *relres)
+// A d = s (|s| = 1) in FP32 by PCG to a relative residual of kInnerTol; returns iterations
+static int inner_pcg(tm_diffusion *d, const std::vector<level> &lv, bool mg, int max_iter, cudaStream_t st,
+                     int *iters)
 {
     const level &L0 = lv[0];
-    const unsigned G = L0.size();
-    const unsigned rb = blocks_for(G) < (unsigned)kRedBlocks ? blocks_for(G) : (unsigned)kRedBlocks;
-    const double inv_diag = 1.0 / L0.diag;
-    int rc;
-    *iters = 0;
-    // rr of the initial residual
-    k_dot<<<rb, kThreads, 0, st>>>(G, d->r, d->r, d->partial);
-    k_finish<<<1, kThreads, 0, st>>>(d->partial, rb, d->sc, 2);
-    if ((rc = read_scalars(d, st))) return rc;
-    const double bb = d->h_sc->bb, stop = tol * tol * bb;
-    double rr = d->h_sc->rr;
-    if (bb == 0.0 || rr <= stop) {
-        *relres = bb > 0.0 ? std::sqrt(rr / bb) : 0.0;
-        return TM_OK;
-    }
-    int it = 0;
+    const unsigned G = L0.size(), rb = red_blocks(G), gb = blocks_for(G);
+    const float inv_diag = (float)(1.0 / L0.diag);
+    int rc, it = 0;
     for (; it < max_iter; it++) {
         if (mg) {
             if ((rc = vcycle(d, lv, st))) return rc;
-            k_dot<<<rb, kThreads, 0, st>>>(G, d->r, d->zv, d->partial);
+            k_dot32<<<rb, kThreads, 0, st>>>(G, d->s, d->zv, d->partial);
         } else {
-            k_jacobi_dot<<<rb, kThreads, 0, st>>>(G, d->r, d->zv, inv_diag, d->partial);
+            k_jacobi_dot32<<<rb, kThreads, 0, st>>>(G, d->s, d->zv, inv_diag, d->partial);
         }
-        k_finish<<<1, kThreads, 0, st>>>(d->partial, rb, d->sc, it == 0 ? 3 : 4);
-        k_direction<<<blocks_for(G), kThreads, 0, st>>>(G, d->p, d->zv, d->sc, it == 0);
-        k_apply_dot<<<rb, kThreads, 0, st>>>(L0, d->p, d->q, d->partial);
-        k_finish<<<1, kThreads, 0, st>>>(d->partial, rb, d->sc, 1);
-        k_update<<<rb, kThreads, 0, st>>>(G, u, d->r, d->p, d->q, d->sc, d->partial);
+        k_finish<<<1, kThreads, 0, st>>>(d->partial, rb, d->sc, it == 0 ? 4 : 5);
+        k_direction32<<<gb, kThreads, 0, st>>>(G, d->p, d->zv, d->sc, it == 0);
+        k_apply_dot32<<<rb, kThreads, 0, st>>>(L0, d->p, d->q, d->partial);
         k_finish<<<1, kThreads, 0, st>>>(d->partial, rb, d->sc, 2);
+        k_update32<<<rb, kThreads, 0, st>>>(G, d->d, d->s, d->p, d->q, d->sc, d->partial);
+        k_finish<<<1, kThreads, 0, st>>>(d->partial, rb, d->sc, 3);
         DK(cudaGetLastError());
         if ((rc = read_scalars(d, st))) return rc;
-        rr = d->h_sc->rr;
-        if (rr <= stop) {
+        if (!(d->h_sc->ss > kInnerTol * kInnerTol)) {      // also stops on a NaN
             it++;
             break;
         }
     }
     *iters = it;
-    *relres = std::sqrt(rr / bb);
+    return TM_OK;
+}
+
+// one solve A u = b (b in d->b) by iterative refinement
+static int solve(tm_diffusion *d, const std::vector<level> &lv, double *u, double tol, bool mg, cudaStream_t st,
+                 int *inner, int *refinements, double *relres)
+{
+    const level &L0 = lv[0];
+    const unsigned G = L0.size(), rb = red_blocks(G), gb = blocks_for(G);
+    int rc;
+    *inner = 0;
+    *refinements = 0;
+    double rel = 0.0;
+    for (int k = 0; k <= kMaxRefine; k++) {
+        k_residual64<<<rb, kThreads, 0, st>>>(L0, u, d->b, d->r, d->partial);
+        k_finish<<<1, kThreads, 0, st>>>(d->partial, rb, d->sc, 1);
+        DK(cudaGetLastError());
+        if ((rc = read_scalars(d, st))) return rc;
+        const double bb = d->h_sc->bb, rr = d->h_sc->rr;
+        rel = bb > 0.0 ? std::sqrt(rr / bb) : std::sqrt(rr);
+        if (rr <= tol * tol * bb || rr == 0.0 || k == kMaxRefine) break;
+        k_scale32<<<gb, kThreads, 0, st>>>(G, d->r, d->sc, d->s, d->d);
+        int n = 0;
+        if ((rc = inner_pcg(d, lv, mg, mg ? 60 : 400, st, &n))) return rc;
+        k_correct64<<<gb, kThreads, 0, st>>>(G, u, d->d, d->sc);
+        *inner += n;
+        (*refinements)++;
+    }
+    *relres = rel;
     return TM_OK;
 }
 
@@ -603,16 +694,17 @@ extern "C" int tm_diffusion_step(tm_diffusion *d, double *data, float resolution
         if (mg) S.multigrid_fields++;
         double *u = data + (size_t)fi * G;
         const double *src = source ? source + (size_t)fi * G : nullptr;
-        const unsigned rb = blocks_for(G) < (unsigned)kRedBlocks ? blocks_for(G) : (unsigned)kRedBlocks;
+        const unsigned rb = red_blocks(G);
         for (int s = 0; s < iters; s++) {
-            k_rhs<<<rb, kThreads, 0, st>>>(lv[0], u, src, zb, d->b, d->r, d->partial);
+            k_rhs<<<rb, kThreads, 0, st>>>(lv[0], u, src, zb, d->b, d->partial);
             k_finish<<<1, kThreads, 0, st>>>(d->partial, rb, d->sc, 0);
             DK(cudaGetLastError());
-            int n = 0;
+            int n = 0, nref = 0;
             double rel = 0.0;
-            int rc = pcg(d, lv, u, tol, mg ? 200 : 2000, mg, st, &n, &rel);
+            int rc = solve(d, lv, u, tol, mg, st, &n, &nref, &rel);
             if (rc) return rc;
             S.iterations += n;
+            S.refinements += nref;
             if (n > S.max_iterations) S.max_iterations = n;
             if (rel > S.max_relative_residual) S.max_relative_residual = rel;
         }

@@ -196,7 +196,8 @@ def field_gradient_device(data, gsize, resolution: float, nfields: int, gradient
 
 class DiffusionStats(C.Structure):
     _fields_ = [("solves_per_field", C.c_int), ("iterations", C.c_int), ("max_iterations", C.c_int),
-                ("multigrid_fields", C.c_int), ("levels", C.c_int), ("max_relative_residual", C.c_double)]
+                ("refinements", C.c_int), ("multigrid_fields", C.c_int), ("levels", C.c_int),
+                ("max_relative_residual", C.c_double)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
