@@ -36,6 +36,7 @@ extern "C" {
 #define TM_DEVERR_BIGBIN 1u   /* > 2048 cells in one Morton bin */
 #define TM_DEVERR_STACK 2u    /* octree walk deeper than its stack */
 #define TM_DEVERR_CODES 4u    /* two cells share a lattice code (coincident cells) */
+#define TM_DEVERR_TYPES 8u    /* an asynchronous upload carried a cell type outside the table (read as 0) */
 
 #define TM_PREC_FP64 0        /* plain FP64, the reference's arithmetic */
 #define TM_PREC_FP32C 1       /* FP32 pair maths, Kahan sums, FP64 cutoff band + FP64 positions */
@@ -203,6 +204,15 @@ int tm_colony_get_cycle(tm_session *s, int id, float *phasetime, float *g1, floa
  * and *marked receive the counts. */
 int tm_colony_cellcycle(tm_session *s, int id, const tm_cycle_params *p, int64_t *divided, int64_t *marked);
 
+/* Asynchronous host I/O for pipelined loops (upload of step k + 1 while the
+ * results of step k travel back).  tm_colony_upload_async takes the same
+ * cells in the same order as the colony holds (same n; other uploads go
+ * through tm_colony_upload); a cell type outside the table is read as 0 and
+ * reported as TM_DEVERR_TYPES by the next tm_session_sync.  Both return once
+ * the work is queued: the caller leaves in's arrays unchanged, and reads
+ * out's arrays only, after tm_session_sync. */
+int tm_colony_upload_async(tm_session *s, int id, const tm_colony_input *in);
+int tm_colony_download_async(tm_session *s, int id, const tm_colony_output *out);
 /* Replace the cells of an existing colony (at most the slots it holds).  With
  * the same n the cells are taken as the same cells in the same order as the
  * colony's input: they keep their slots, and neighbour lists stay valid unless

@@ -24,6 +24,7 @@
 #define TM_ERR_BIGBIN 1u          // a bin held more than TM_BIG_BIN cells
 #define TM_ERR_STACK 2u           // octree walk deeper than its stack
 #define TM_ERR_CODES 4u           // two cells share a lattice code
+#define TM_ERR_TYPES 8u           // an asynchronous upload carried a cell type outside the table
 #define TM_ERR_LIST 8u            // pair list overflow (internal)
 
 // Per-type constants, computed on the host with the reference's expressions

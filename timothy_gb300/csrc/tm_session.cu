@@ -130,6 +130,15 @@ struct tm_session {
     void *d_scratch = nullptr;
     void *d_scratch2 = nullptr;              // second download buffer (copies overlap the next gather)
     cudaStream_t copy_stream = nullptr;
+    cudaStream_t h2d_stream = nullptr;    // asynchronous uploads
+    cudaEvent_t ev_h2d = nullptr;
+    // asynchronous I/O: own staging, so copies overlap the steps
+    unsigned char *up_stage = nullptr;    // x, y, z, size (8 B), young, ctype, phase (4 B) per slot
+    unsigned char *dl_stage = nullptr;    // the downloaded fields, 8 B per slot each
+    size_t up_bytes = 0, dl_bytes = 0;
+    cudaEvent_t ev_up_read = nullptr;     // k_upload_keep has read up_stage
+    cudaEvent_t ev_dl_gathered = nullptr, ev_dl_copied = nullptr;
+    bool dl_pending = false, up_pending = false;
     cudaEvent_t ev_ready[2] = {nullptr, nullptr}, ev_copied[2] = {nullptr, nullptr};
     // profiling
     bool prof = false;
@@ -194,17 +203,26 @@ __global__ void k_colony_init(tm_arrays a, int c, long long off, int n, int nslo
 // the step's rebuild test sees the displacement from the list positions, and
 // a cell that changed size or type (list radius, FP64 density weight) forces a
 // rebuild.  Cell types outside the table are flagged and replaced by 0.
+// the cells of an upload in caller order, at [base + caller index]
+struct upload_src {
+    const double *x, *y, *z, *size;
+    const float *young;
+    const int *ctype, *phase;
+    long long base;
+};
+
 __global__ void k_upload_keep(tm_arrays a, const tm_consts *K, int c, long long off, int n, int has_phase,
-                              int *bad)
+                              int *bad, upload_src u)
 {
     const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const long long s = off + k;
-    const long long src = off + a.perm[s];
-    const double x = a.x2[src], y = a.y2[src], z = a.z2[src], sz = a.size2[src];
-    int ct = a.ctype2[src];
+    const long long src = u.base + a.perm[s];
+    const double x = u.x[src], y = u.y[src], z = u.z[src], sz = u.size[src];
+    int ct = u.ctype[src];
     if (ct < 0 || ct >= K->ntypes) {
-        atomicExch(bad, 1);
+        if (bad) atomicExch(bad, 1);
+        else atomicOr(&a.frame[c].error, TM_ERR_TYPES);
         ct = 0;
     }
     if (sz != a.size[s] || ct != a.ctype[s]) a.frame[c].force_rebuild = 1;
@@ -212,9 +230,9 @@ __global__ void k_upload_keep(tm_arrays a, const tm_consts *K, int c, long long 
     a.y[s] = y;
     a.z[s] = z;
     a.size[s] = sz;
-    a.young[s] = a.young2[src];
+    a.young[s] = u.young[src];
     a.ctype[s] = ct;
-    if (has_phase) a.phase[s] = a.phase2[src];
+    if (has_phase) a.phase[s] = u.phase[src];
     a.rem[s] = 0;
     if (a.desc[c].verlet && a.x0) {
         float hx, hy, hz, lx, ly, lz;
@@ -656,6 +674,12 @@ extern "C" int tm_session_destroy(tm_session *s)
             if (p) cudaFree(p);
     }
     if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
+    if (s->h2d_stream) cudaStreamDestroy(s->h2d_stream);
+    if (s->ev_h2d) cudaEventDestroy(s->ev_h2d);
+    for (cudaEvent_t e : {s->ev_up_read, s->ev_dl_gathered, s->ev_dl_copied})
+        if (e) cudaEventDestroy(e);
+    if (s->up_stage) cudaFree(s->up_stage);
+    if (s->dl_stage) cudaFree(s->dl_stage);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return TM_OK;
@@ -719,8 +743,9 @@ static int copy_cells_in(tm_session *s, const colony_host &c, const tm_colony_in
         CK(cudaStreamWaitEvent(st, s->ev_copied[0], 0));
     }
     if (keep) {
+        const upload_src u = {a.x2, a.y2, a.z2, a.size2, a.young2, a.ctype2, a.phase2, o};
         k_upload_keep<<<blocks_for((long long)n, 256), 256, 0, st>>>(a, s->dK, cid, o, (int)n, in->phase ? 1 : 0,
-                                                                    s->d_flag);
+                                                                    s->d_flag, u);
     } else {
         k_check_types<<<blocks_for((long long)n, 256), 256, 0, st>>>(a, s->dK, o, (int)n, s->d_flag);
         k_colony_init<<<blocks_for(c.nslots, 256), 256, 0, st>>>(a, cid, o, (int)n, c.nslots, in->phase ? 1 : 0);
@@ -923,6 +948,69 @@ extern "C" int tm_colony_upload(tm_session *s, int id, const tm_colony_input *in
     return rc;
 }
 
+static int async_io_init(tm_session *s)
+{
+    if (s->h2d_stream) return TM_OK;
+    int rc = download_streams(s);
+    if (rc) return rc;
+    CK(cudaStreamCreateWithFlags(&s->h2d_stream, cudaStreamNonBlocking));
+    for (cudaEvent_t *e : {&s->ev_h2d, &s->ev_up_read, &s->ev_dl_gathered, &s->ev_dl_copied})
+        CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    return TM_OK;
+}
+
+// Upload of the same cells (same n, same order) into the upload staging
+// (44 B per slot, allocated on first use): the copies wait only until the
+// previous asynchronous upload's kernel has read the staging, so they overlap
+// the step before; the kernel that puts the cells into their slots follows on
+// the session stream.
+extern "C" int tm_colony_upload_async(tm_session *s, int id, const tm_colony_input *in)
+{
+    int rc = lookup(s, id);
+    if (rc) return rc;
+    rc = check_input(s, in, false);
+    if (rc) return rc;
+    colony_host &c = s->cols[id];
+    if (in->n != c.n || c.n == 0) return tm_colony_upload(s, id, in);
+    CK(cudaSetDevice(s->device));
+    if ((rc = async_io_init(s))) return rc;
+    const size_t S = (size_t)s->slots.hwm * 32 + 32, need = S * 44;
+    if (s->up_bytes < need) {
+        CK(cudaStreamSynchronize(s->h2d_stream));
+        CK(cudaStreamSynchronize(s->stream));
+        if (s->up_stage) CK(cudaFree(s->up_stage));
+        s->up_stage = nullptr;
+        s->up_bytes = 0;
+        CK(cudaMalloc((void **)&s->up_stage, need));
+        s->up_bytes = need;
+        s->up_pending = false;
+    }
+    double *X = (double *)s->up_stage, *Y = X + S, *Z = Y + S, *SZ = Z + S;
+    float *YG = (float *)(SZ + S);
+    int *CT = (int *)(YG + S), *PH = CT + S;
+    const long long o = c.off;
+    const size_t n = (size_t)in->n;
+    cudaStream_t h = s->h2d_stream;
+    if (s->up_pending) CK(cudaStreamWaitEvent(h, s->ev_up_read, 0));
+    CK(cudaMemcpyAsync(X + o, in->x, n * 8, cudaMemcpyHostToDevice, h));
+    CK(cudaMemcpyAsync(Y + o, in->y, n * 8, cudaMemcpyHostToDevice, h));
+    CK(cudaMemcpyAsync(Z + o, in->z, n * 8, cudaMemcpyHostToDevice, h));
+    CK(cudaMemcpyAsync(SZ + o, in->size, n * 8, cudaMemcpyHostToDevice, h));
+    CK(cudaMemcpyAsync(YG + o, in->young, n * 4, cudaMemcpyHostToDevice, h));
+    CK(cudaMemcpyAsync(CT + o, in->ctype, n * 4, cudaMemcpyHostToDevice, h));
+    if (in->phase) CK(cudaMemcpyAsync(PH + o, in->phase, n * 4, cudaMemcpyHostToDevice, h));
+    CK(cudaEventRecord(s->ev_h2d, h));
+    CK(cudaStreamWaitEvent(s->stream, s->ev_h2d, 0));
+    const tm_arrays a = view(s, s->parity);
+    const upload_src u = {X, Y, Z, SZ, YG, CT, PH, o};
+    k_upload_keep<<<blocks_for((long long)n, 256), 256, 0, s->stream>>>(a, s->dK, id, o, (int)n, in->phase ? 1 : 0,
+                                                                      nullptr, u);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(s->ev_up_read, s->stream));
+    s->up_pending = true;
+    return TM_OK;
+}
+
 extern "C" int tm_colony_set_active(tm_session *s, int id, int active)
 {
     int rc = lookup(s, id);
@@ -1055,6 +1143,8 @@ extern "C" int tm_session_sync(tm_session *s)
     if (!s) return tm_fail(TM_EINVAL, "null session");
     CK(cudaSetDevice(s->device));
     CK(cudaStreamSynchronize(s->stream));
+    if (s->copy_stream) CK(cudaStreamSynchronize(s->copy_stream));
+    if (s->h2d_stream) CK(cudaStreamSynchronize(s->h2d_stream));
     const int ncol = (int)s->cols.size();
     if (ncol == 0) return TM_OK;
     CK(cudaMemcpy(s->h_frame, s->A.frame, sizeof(tm_frame) * (size_t)ncol, cudaMemcpyDeviceToHost));
@@ -1062,10 +1152,11 @@ extern "C" int tm_session_sync(tm_session *s)
         if (!s->cols[c].used) continue;
         uint32_t e = s->h_frame[c].error;
         if (e)
-            return tm_fail(TM_EDEVICE, "colony %d: device error 0x%x (%s%s%s)", c, e,
+            return tm_fail(TM_EDEVICE, "colony %d: device error 0x%x (%s%s%s%s)", c, e,
                            (e & TM_ERR_BIGBIN) ? "more than 2048 cells in one bin; " : "",
                            (e & TM_ERR_STACK) ? "octree walk too deep; " : "",
-                           (e & TM_ERR_CODES) ? "coincident lattice codes; " : "");
+                           (e & TM_ERR_CODES) ? "coincident lattice codes; " : "",
+                           (e & TM_ERR_TYPES) ? "cell type outside the table in an upload; " : "");
     }
     return TM_OK;
 }
@@ -1158,11 +1249,94 @@ static int download_streams(tm_session *s)
     return TM_OK;
 }
 
+static int download_queue(tm_session *s, int id, const tm_colony_output *out, bool wait);
+
 extern "C" int tm_colony_download(tm_session *s, int id, const tm_colony_output *out)
+{
+    return download_queue(s, id, out, true);
+}
+
+extern "C" int tm_colony_download_async(tm_session *s, int id, const tm_colony_output *out)
+{
+    return download_queue(s, id, out, false);
+}
+
+// Asynchronous download: every requested field is gathered into its own part
+// of the download staging (8 B per slot per field, allocated on first use) on
+// the session stream, then copied to the host on the copy stream, so the
+// copies overlap the steps that follow; the next asynchronous download's
+// gathers wait for these copies.
+template <typename T>
+static int gather_async(tm_session *s, const T *src, const colony_host &c, T *host, size_t S, int &slot,
+                        std::vector<std::pair<void *, std::pair<const void *, size_t>>> &copies)
+{
+    if (!host || c.n == 0) return TM_OK;
+    T *dst = (T *)(s->dl_stage + (size_t)slot * S * 8);
+    slot++;
+    const tm_arrays a = view(s, s->parity);
+    k_unsort<T><<<blocks_for(c.n, 256), 256, 0, s->stream>>>(src, a.perm, c.off, c.n, dst);
+    CK(cudaGetLastError());
+    copies.push_back({(void *)host, {(const void *)dst, sizeof(T) * (size_t)c.n}});
+    return TM_OK;
+}
+
+static int download_async_queue(tm_session *s, int id, const tm_colony_output *out)
+{
+    int rc = async_io_init(s);
+    if (rc) return rc;
+    const colony_host &c = s->cols[id];
+    const tm_arrays a = view(s, s->parity);
+    const size_t S = (size_t)s->slots.hwm * 32 + 32, need = S * 8 * 13;
+    if (s->dl_bytes < need) {
+        CK(cudaStreamSynchronize(s->copy_stream));
+        CK(cudaStreamSynchronize(s->stream));
+        if (s->dl_stage) CK(cudaFree(s->dl_stage));
+        s->dl_stage = nullptr;
+        s->dl_bytes = 0;
+        CK(cudaMalloc((void **)&s->dl_stage, need));
+        s->dl_bytes = need;
+        s->dl_pending = false;
+    }
+    if (s->dl_pending) CK(cudaStreamWaitEvent(s->stream, s->ev_dl_copied, 0));
+    std::vector<std::pair<void *, std::pair<const void *, size_t>>> copies;
+    int slot = 0;
+    if ((rc = gather_async(s, (const double *)a.x, c, out->x, S, slot, copies))) return rc;
+    if ((rc = gather_async(s, (const double *)a.y, c, out->y, S, slot, copies))) return rc;
+    if ((rc = gather_async(s, (const double *)a.z, c, out->z, S, slot, copies))) return rc;
+    if ((rc = gather_async(s, (const double *)a.density, c, out->density, S, slot, copies))) return rc;
+    if ((rc = gather_async(s, (const double *)a.v, c, out->v, S, slot, copies))) return rc;
+    if ((rc = gather_async(s, (const double *)a.mindist, c, out->mindist, S, slot, copies))) return rc;
+    if ((rc = gather_async(s, (const double *)a.fx, c, out->fx, S, slot, copies))) return rc;
+    if ((rc = gather_async(s, (const double *)a.fy, c, out->fy, S, slot, copies))) return rc;
+    if ((rc = gather_async(s, (const double *)a.fz, c, out->fz, S, slot, copies))) return rc;
+    if ((rc = gather_async(s, (const unsigned char *)a.rem, c, out->removecell, S, slot, copies))) return rc;
+    if ((rc = gather_async(s, (const int32_t *)a.nbcount, c, out->nbcount, S, slot, copies))) return rc;
+    if (a.nbhash &&
+        (rc = gather_async(s, (const unsigned long long *)a.nbhash, c, (unsigned long long *)out->nbhash, S, slot,
+                           copies)))
+        return rc;
+    if (a.vcand && (rc = gather_async(s, (const int32_t *)a.vcand, c, out->vcand, S, slot, copies))) return rc;
+    CK(cudaEventRecord(s->ev_dl_gathered, s->stream));
+    CK(cudaStreamWaitEvent(s->copy_stream, s->ev_dl_gathered, 0));
+    for (auto &cp : copies)
+        CK(cudaMemcpyAsync(cp.first, cp.second.first, cp.second.second, cudaMemcpyDeviceToHost, s->copy_stream));
+    if (out->grid && c.gridoff >= 0)
+        CK(cudaMemcpyAsync(out->grid, a.grid + c.gridoff, sizeof(double) * (size_t)c.ngrid, cudaMemcpyDeviceToHost,
+                           s->copy_stream));
+    CK(cudaEventRecord(s->ev_dl_copied, s->copy_stream));
+    s->dl_pending = true;
+    return TM_OK;
+}
+
+static int download_queue(tm_session *s, int id, const tm_colony_output *out, bool wait)
 {
     int rc = lookup(s, id);
     if (rc) return rc;
     if (!out) return tm_fail(TM_EINVAL, "null output");
+    if (!wait) {
+        CK(cudaSetDevice(s->device));
+        return download_async_queue(s, id, out);
+    }
     CK(cudaSetDevice(s->device));
     if ((rc = download_streams(s))) return rc;
     const colony_host &c = s->cols[id];
@@ -1182,11 +1356,18 @@ extern "C" int tm_colony_download(tm_session *s, int id, const tm_colony_output 
                                          (unsigned long long *)out->nbhash)))
         return rc;
     if (a.vcand && (rc = unsort_to_host(s, (const int32_t *)a.vcand, c, out->vcand))) return rc;
-    // the caller may read its buffers on return
-    CK(cudaStreamSynchronize(s->stream));
-    CK(cudaStreamSynchronize(s->copy_stream));
-    if (out->grid && c.gridoff >= 0)
-        CK(cudaMemcpy(out->grid, a.grid + c.gridoff, sizeof(double) * (size_t)c.ngrid, cudaMemcpyDeviceToHost));
+    if (out->grid && c.gridoff >= 0) {
+        CK(cudaEventRecord(s->ev_ready[0], s->stream));
+        CK(cudaStreamWaitEvent(s->copy_stream, s->ev_ready[0], 0));
+        CK(cudaMemcpyAsync(out->grid, a.grid + c.gridoff, sizeof(double) * (size_t)c.ngrid, cudaMemcpyDeviceToHost,
+                           s->copy_stream));
+        CK(cudaEventRecord(s->ev_copied[0], s->copy_stream));
+    }
+    if (wait) {
+        // the caller may read its buffers on return
+        CK(cudaStreamSynchronize(s->stream));
+        CK(cudaStreamSynchronize(s->copy_stream));
+    }
     return TM_OK;
 }
 

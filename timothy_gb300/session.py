@@ -103,6 +103,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "tm_colony_upload": (C.c_int, [P, C.c_int, C.POINTER(_Input)]),
         "tm_colony_set_active": (C.c_int, [P, C.c_int, C.c_int]),
         "tm_colony_download": (C.c_int, [P, C.c_int, C.POINTER(_Output)]),
+        "tm_colony_upload_async": (C.c_int, [P, C.c_int, C.POINTER(_Input)]),
+        "tm_colony_download_async": (C.c_int, [P, C.c_int, C.POINTER(_Output)]),
         "tm_colony_stats": (C.c_int, [P, C.c_int, C.POINTER(_Info)]),
         "tm_session_step": (C.c_int, [P, C.c_int]),
         "tm_session_sync": (C.c_int, [P]),
@@ -276,6 +278,7 @@ class Session:
         self.dim = dim
         self.diagnostics = diagnostics
         self._n = {}
+        self._keep_async = []          # arrays of queued asynchronous uploads, held until sync()
         self._grid = {}
 
     # -- lifetime ---------------------------------------------------------
@@ -336,6 +339,23 @@ class Session:
         elif rc == -4:      # a cell type outside the table: the colony was left empty
             self._n[cid] = 0
         _check(rc)
+
+    def upload_async(self, cid: int, col: Colony):
+        """Queue the re-upload of the colony's cells (same n, same order); the
+        arrays must stay unchanged until sync()."""
+        inp, keep = self._input(col)
+        self._keep_async.append(keep)
+        _check(load_library().tm_colony_upload_async(self._h, cid, C.byref(inp)))
+
+    def download_async(self, cid: int, fields, out: dict):
+        """Queue the copy of results into out's arrays (caller order); they are
+        valid after sync()."""
+        n = self._n[cid]
+        for k in fields:
+            if k not in out or len(out[k]) < n:
+                raise ValueError(f"download_async needs an output array for {k} with {n} entries")
+        o = _Output(*[_p(out.get(k)) if k in fields else None for k, _ in _Output._fields_])
+        _check(load_library().tm_colony_download_async(self._h, cid, C.byref(o)))
 
     def compact(self, cid: int) -> int:
         """Remove the cells marked for removal (cellsdeath); returns how many."""
@@ -401,6 +421,7 @@ class Session:
 
     def sync(self):
         _check(load_library().tm_session_sync(self._h))
+        self._keep_async.clear()
 
     def use_graph(self, on: bool = True):
         _check(load_library().tm_session_use_graph(self._h, 1 if on else 0))
