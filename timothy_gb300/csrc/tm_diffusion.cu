@@ -47,7 +47,7 @@ int tm_report(int code, const char *msg);
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kRedBlocks = 152 * 4;      // reduction grid: partials per reduction
+constexpr int kRedBlocks = 152 * 8;      // reduction grid (8 blocks of 256 per SM): partials per reduction
 constexpr int kCoarseMax = 27;           // at most 3 nodes per axis on the coarsest grid
 constexpr int kCoarseSweeps = 64;
 constexpr double kInnerTol = 1e-5;       // relative residual of one FP32 correction solve
@@ -57,6 +57,7 @@ struct level {
     unsigned nx, ny, nz;
     double zx, zy, zz;      // couplings along x, y, z
     double diag;
+    float zxf, zyf, zzf, diagf, invf;   // FP32 copies for the FP32 kernels (set on the host: no FP64 per node)
     __host__ __device__ unsigned size() const { return nx * ny * nz; }
 };
 
@@ -92,25 +93,27 @@ __device__ __forceinline__ void nbsums(const level &L, const T *u, unsigned o, u
     if (k + 1 < L.nz) sz += u[o + 1];
 }
 
-template <typename T>
-__device__ __forceinline__ T neighbours(const level &L, const T *u, unsigned o, unsigned i, unsigned j, unsigned k)
+__device__ __forceinline__ float neighbours(const level &L, const float *u, unsigned o, unsigned i, unsigned j,
+                                            unsigned k)
 {
-    T sx, sy, sz;
+    float sx, sy, sz;
     nbsums(L, u, o, i, j, k, sx, sy, sz);
-    return T(L.zx) * sx + T(L.zy) * sy + T(L.zz) * sz;
+    return L.zxf * sx + L.zyf * sy + L.zzf * sz;
 }
 
-// block sum into partial[blockIdx.x] (fixed order for a fixed launch)
+// block sum into partial[linear block index] (fixed order for a fixed
+// launch; blocks of kThreads threads, of any 1-, 2- or 3-D shape)
 __device__ __forceinline__ void block_partial(double v, double *partial)
 {
     __shared__ double sh[kThreads / 32];
+    const unsigned t = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
     for (int d = 16; d > 0; d >>= 1) v += __shfl_down_sync(0xffffffffu, v, d);
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    if ((t & 31) == 0) sh[t >> 5] = v;
     __syncthreads();
-    if (threadIdx.x < 32) {
-        v = threadIdx.x < kThreads / 32 ? sh[threadIdx.x] : 0.0;
+    if (t < 32) {
+        v = t < kThreads / 32 ? sh[t] : 0.0;
         for (int d = 16; d > 0; d >>= 1) v += __shfl_down_sync(0xffffffffu, v, d);
-        if (threadIdx.x == 0) partial[blockIdx.x] = v;
+        if (t == 0) partial[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = v;
     }
 }
 
@@ -150,18 +153,19 @@ __global__ void __launch_bounds__(kThreads) k_residual64(level L, const double *
                                                          double *partial)
 {
     double acc = 0.0;
-    const unsigned G = L.size(), nyz = L.ny * L.nz;
-    for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < G; o += gridDim.x * blockDim.x) {
-        unsigned i, j, k;
-        coords(L, o, i, j, k);
-        const double xm = i > 0 ? u[o - nyz] : 0.0, xp = i + 1 < L.nx ? u[o + nyz] : 0.0;
-        const double ym = j > 0 ? u[o - L.nz] : 0.0, yp = j + 1 < L.ny ? u[o + L.nz] : 0.0;
-        const double zm = k > 0 ? u[o - 1] : 0.0, zp = k + 1 < L.nz ? u[o + 1] : 0.0;
-        const double s = ((xm + xp) + (ym + yp)) + (zm + zp);
-        const double v = fma(-L.diag, u[o], fma(L.zx, s, b[o]));
-        r[o] = v;
-        acc = fma(v, v, acc);
-    }
+    const unsigned k = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    const unsigned nyz = L.ny * L.nz;
+    if (k < L.nz && j < L.ny)
+        for (unsigned i = blockIdx.z; i < L.nx; i += gridDim.z) {
+            const unsigned o = (i * L.ny + j) * L.nz + k;
+            const double xm = i > 0 ? u[o - nyz] : 0.0, xp = i + 1 < L.nx ? u[o + nyz] : 0.0;
+            const double ym = j > 0 ? u[o - L.nz] : 0.0, yp = j + 1 < L.ny ? u[o + L.nz] : 0.0;
+            const double zm = k > 0 ? u[o - 1] : 0.0, zp = k + 1 < L.nz ? u[o + 1] : 0.0;
+            const double sn = ((xm + xp) + (ym + yp)) + (zm + zp);
+            const double v = fma(-L.diag, u[o], fma(L.zx, sn, b[o]));
+            r[o] = v;
+            acc = fma(v, v, acc);
+        }
     block_partial(acc, partial);
 }
 
@@ -186,19 +190,18 @@ __global__ void __launch_bounds__(kThreads) k_correct64(unsigned G, double *u, c
 
 // ------------------------------------------------------------ FP32 inner CG
 
-// q = A p; partials of p.q
+// q = A p; partials of p.q (column mapping as k_residual64)
 __global__ void __launch_bounds__(kThreads) k_apply_dot32(level L, const float *p, float *q, double *partial)
 {
     float acc = 0.0f;
-    const unsigned G = L.size();
-    const float dg = (float)L.diag;
-    for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < G; o += gridDim.x * blockDim.x) {
-        unsigned i, j, k;
-        coords(L, o, i, j, k);
-        const float v = dg * p[o] - neighbours(L, p, o, i, j, k);
-        q[o] = v;
-        acc += p[o] * v;
-    }
+    const unsigned k = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (k < L.nz && j < L.ny)
+        for (unsigned i = blockIdx.z; i < L.nx; i += gridDim.z) {
+            const unsigned o = (i * L.ny + j) * L.nz + k;
+            const float v = L.diagf * p[o] - neighbours(L, p, o, i, j, k);
+            q[o] = v;
+            acc = fmaf(p[o], v, acc);
+        }
     block_partial32(acc, partial);
 }
 
@@ -208,22 +211,57 @@ __global__ void __launch_bounds__(kThreads) k_update32(unsigned G, float *d, flo
 {
     const float a = (float)sc->alpha;
     float acc = 0.0f;
-    for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < G; o += gridDim.x * blockDim.x) {
-        d[o] += a * p[o];
-        const float v = s[o] - a * q[o];
+    // four nodes per access (the vectors are 256-byte aligned), the tail singly
+    const unsigned G4 = G / 4, stride = gridDim.x * blockDim.x;
+    float4 *d4 = (float4 *)d, *s4 = (float4 *)s;
+    const float4 *p4 = (const float4 *)p, *q4 = (const float4 *)q;
+    for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < G4; o += stride) {
+        float4 dv = d4[o], sv = s4[o];
+        const float4 pv = p4[o], qv = q4[o];
+        dv.x = fmaf(a, pv.x, dv.x);
+        dv.y = fmaf(a, pv.y, dv.y);
+        dv.z = fmaf(a, pv.z, dv.z);
+        dv.w = fmaf(a, pv.w, dv.w);
+        sv.x = fmaf(-a, qv.x, sv.x);
+        sv.y = fmaf(-a, qv.y, sv.y);
+        sv.z = fmaf(-a, qv.z, sv.z);
+        sv.w = fmaf(-a, qv.w, sv.w);
+        d4[o] = dv;
+        s4[o] = sv;
+        acc = fmaf(sv.x, sv.x, fmaf(sv.y, sv.y, fmaf(sv.z, sv.z, fmaf(sv.w, sv.w, acc))));
+    }
+    for (unsigned o = 4 * G4 + blockIdx.x * blockDim.x + threadIdx.x; o < G; o += stride) {
+        d[o] = fmaf(a, p[o], d[o]);
+        const float v = fmaf(-a, q[o], s[o]);
         s[o] = v;
-        acc += v * v;
+        acc = fmaf(v, v, acc);
     }
     block_partial32(acc, partial);
 }
 
-// p = zv + beta p (first: p = zv)
+// p = zv + beta p (first: p = zv); four nodes per access, the tail singly
 __global__ void __launch_bounds__(kThreads) k_direction32(unsigned G, float *p, const float *zv, const scalars *sc,
                                                           int first)
 {
     const float be = first ? 0.0f : (float)sc->beta;
-    for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < G; o += gridDim.x * blockDim.x)
-        p[o] = first ? zv[o] : zv[o] + be * p[o];
+    const unsigned G4 = G / 4, stride = gridDim.x * blockDim.x;
+    float4 *p4 = (float4 *)p;
+    const float4 *z4 = (const float4 *)zv;
+    for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < G4; o += stride) {
+        const float4 z = z4[o];
+        if (first) {
+            p4[o] = z;
+        } else {
+            float4 v = p4[o];
+            v.x = fmaf(be, v.x, z.x);
+            v.y = fmaf(be, v.y, z.y);
+            v.z = fmaf(be, v.z, z.z);
+            v.w = fmaf(be, v.w, z.w);
+            p4[o] = v;
+        }
+    }
+    for (unsigned o = 4 * G4 + blockIdx.x * blockDim.x + threadIdx.x; o < G; o += stride)
+        p[o] = first ? zv[o] : fmaf(be, p[o], zv[o]);
 }
 
 // zv = s / diag; partials of s.zv
@@ -231,10 +269,19 @@ __global__ void __launch_bounds__(kThreads) k_jacobi_dot32(unsigned G, const flo
                                                            double *partial)
 {
     float acc = 0.0f;
-    for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < G; o += gridDim.x * blockDim.x) {
+    const unsigned G4 = G / 4, stride = gridDim.x * blockDim.x;
+    const float4 *s4 = (const float4 *)s;
+    float4 *z4 = (float4 *)zv;
+    for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < G4; o += stride) {
+        const float4 a = s4[o];
+        const float4 v = make_float4(a.x * inv_diag, a.y * inv_diag, a.z * inv_diag, a.w * inv_diag);
+        z4[o] = v;
+        acc = fmaf(a.x, v.x, fmaf(a.y, v.y, fmaf(a.z, v.z, fmaf(a.w, v.w, acc))));
+    }
+    for (unsigned o = 4 * G4 + blockIdx.x * blockDim.x + threadIdx.x; o < G; o += stride) {
         const float v = s[o] * inv_diag;
         zv[o] = v;
-        acc += s[o] * v;
+        acc = fmaf(s[o], v, acc);
     }
     block_partial32(acc, partial);
 }
@@ -243,7 +290,13 @@ __global__ void __launch_bounds__(kThreads) k_jacobi_dot32(unsigned G, const flo
 __global__ void __launch_bounds__(kThreads) k_dot32(unsigned G, const float *x, const float *y, double *partial)
 {
     float acc = 0.0f;
-    for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < G; o += gridDim.x * blockDim.x) acc += x[o] * y[o];
+    const unsigned G4 = G / 4, stride = gridDim.x * blockDim.x;
+    const float4 *x4 = (const float4 *)x, *y4 = (const float4 *)y;
+    for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < G4; o += stride) {
+        const float4 a = x4[o], b = y4[o];
+        acc = fmaf(a.x, b.x, fmaf(a.y, b.y, fmaf(a.z, b.z, fmaf(a.w, b.w, acc))));
+    }
+    for (unsigned o = 4 * G4 + blockIdx.x * blockDim.x + threadIdx.x; o < G; o += stride) acc = fmaf(x[o], y[o], acc);
     block_partial32(acc, partial);
 }
 
@@ -280,132 +333,141 @@ __global__ void __launch_bounds__(kThreads) k_finish(const double *partial, int 
 
 // ---------------------------------------------------------------- multigrid (FP32)
 
-__global__ void __launch_bounds__(kThreads) k_zero(unsigned G, float *e)
+// The stencil kernels of the V-cycle run one thread per node on a 3-D grid:
+// blocks of 256 threads over (z, y), blockIdx.z = x, so no thread divides
+// to find its node (see shape3).
+__device__ __forceinline__ bool node3(const level &L, unsigned &i, unsigned &j, unsigned &k)
 {
-    for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < G; o += gridDim.x * blockDim.x) e[o] = 0.0f;
+    k = blockIdx.x * blockDim.x + threadIdx.x;
+    j = blockIdx.y * blockDim.y + threadIdx.y;
+    i = blockIdx.z;
+    return k < L.nz && j < L.ny;
 }
 
-// Gauss-Seidel on the nodes of one colour ((i + j + k) & 1 == colour)
+// Gauss-Seidel on the nodes of one colour ((i + j + k) & 1 == colour): a
+// thread per node of the colour, two z positions per thread index
 __global__ void __launch_bounds__(kThreads) k_rbgs(level L, float *e, const float *f, int colour)
 {
-    const unsigned G = L.size();
-    const float inv = (float)(1.0 / L.diag);
-    for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < G; o += gridDim.x * blockDim.x) {
-        unsigned i, j, k;
-        coords(L, o, i, j, k);
-        if (((i + j + k) & 1u) != (unsigned)colour) continue;
-        e[o] = (f[o] + neighbours(L, e, o, i, j, k)) * inv;
-    }
+    const unsigned kk = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y,
+                   i = blockIdx.z;
+    const unsigned k = 2 * kk + ((i + j + (unsigned)colour) & 1u);
+    if (k >= L.nz || j >= L.ny) return;
+    const unsigned o = (i * L.ny + j) * L.nz + k;
+    e[o] = (f[o] + neighbours(L, e, o, i, j, k)) * L.invf;
+}
+
+// the first half-sweep from e = 0: red nodes e = f / diag (their neighbours
+// are zero), black nodes 0
+__global__ void __launch_bounds__(kThreads) k_rbgs_first(level L, float *e, const float *f)
+{
+    unsigned i, j, k;
+    if (!node3(L, i, j, k)) return;
+    const unsigned o = (i * L.ny + j) * L.nz + k;
+    e[o] = ((i + j + k) & 1u) ? 0.0f : f[o] * L.invf;
 }
 
 // res = f - A e
 __global__ void __launch_bounds__(kThreads) k_residual32(level L, const float *e, const float *f, float *res)
 {
-    const unsigned G = L.size();
-    const float dg = (float)L.diag;
-    for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < G; o += gridDim.x * blockDim.x) {
-        unsigned i, j, k;
-        coords(L, o, i, j, k);
-        res[o] = f[o] - (dg * e[o] - neighbours(L, e, o, i, j, k));
-    }
+    unsigned i, j, k;
+    if (!node3(L, i, j, k)) return;
+    const unsigned o = (i * L.ny + j) * L.nz + k;
+    res[o] = f[o] - (L.diagf * e[o] - neighbours(L, e, o, i, j, k));
 }
 
-// fine indices and weights restricting to coarse index I along an axis: the
-// coarse node sits on fine node 2I + 1 and takes its two fine neighbours at
-// half weight (the first fine node's other coarse neighbour, and the last's
-// on a grid of odd size, are the Dirichlet ghosts)
-__device__ __forceinline__ void axis_taps(unsigned I, unsigned nf, bool coarse, unsigned *idx, float *w, int &n)
+// Restriction taps of coarse index I along an axis: the coarse node sits on
+// fine node 2I + 1 (weight 1) with its fine neighbours 2I and 2I + 2 at half
+// weight; the last one is a Dirichlet ghost on a grid of odd size (weight 0,
+// index clamped).  An axis that is not coarsened has the single tap I.
+__device__ __forceinline__ void rtaps(unsigned I, unsigned nf, bool coarse, unsigned t[3], float w[3])
 {
     if (!coarse) {
-        idx[0] = I;
+        t[0] = t[1] = t[2] = I;
         w[0] = 1.0f;
-        n = 1;
+        w[1] = w[2] = 0.0f;
         return;
     }
-    const unsigned c = 2 * I + 1;       // < nf: I < nf / 2
-    idx[0] = c;
+    const unsigned c = 2 * I + 1;        // < nf: I < nf / 2
+    t[0] = c;
     w[0] = 1.0f;
-    idx[1] = c - 1;
+    t[1] = c - 1;
     w[1] = 0.5f;
-    n = 2;
-    if (c + 1 < nf) {
-        idx[2] = c + 1;
-        w[2] = 0.5f;
-        n = 3;
-    }
+    const bool has = c + 1 < nf;
+    t[2] = has ? c + 1 : c;
+    w[2] = has ? 0.5f : 0.0f;
 }
 
-// f_c = R res_f (the transpose of interpolation over 2^dc)
+// f_c = R res_f (the transpose of interpolation over 2^dc); one thread per
+// coarse node, 27 fixed taps (absent ones weigh 0)
 __global__ void __launch_bounds__(kThreads) k_restrict(level Lf, level Lc, const float *res, float *fc, float scale)
 {
-    const unsigned G = Lc.size();
-    const bool cx = Lc.nx != Lf.nx, cy = Lc.ny != Lf.ny, cz = Lc.nz != Lf.nz;
-    for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < G; o += gridDim.x * blockDim.x) {
-        unsigned I, J, K;
-        coords(Lc, o, I, J, K);
-        unsigned ix[3], iy[3], iz[3];
-        float wx[3], wy[3], wz[3];
-        int nx, ny, nz;
-        axis_taps(I, Lf.nx, cx, ix, wx, nx);
-        axis_taps(J, Lf.ny, cy, iy, wy, ny);
-        axis_taps(K, Lf.nz, cz, iz, wz, nz);
-        float s = 0.0f;
-        for (int a = 0; a < nx; a++)
-            for (int b = 0; b < ny; b++)
-                for (int c = 0; c < nz; c++)
-                    s += wx[a] * wy[b] * wz[c] * res[(ix[a] * Lf.ny + iy[b]) * Lf.nz + iz[c]];
-        fc[o] = s * scale;
-    }
+    unsigned I, J, K;
+    if (!node3(Lc, I, J, K)) return;
+    unsigned tx[3], ty[3], tz[3];
+    float wx[3], wy[3], wz[3];
+    rtaps(I, Lf.nx, Lc.nx != Lf.nx, tx, wx);
+    rtaps(J, Lf.ny, Lc.ny != Lf.ny, ty, wy);
+    rtaps(K, Lf.nz, Lc.nz != Lf.nz, tz, wz);
+    float s = 0.0f;
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++) {
+            const float wab = wx[a] * wy[b];
+            const float *row = res + (tx[a] * Lf.ny + ty[b]) * Lf.nz;
+#pragma unroll
+            for (int c = 0; c < 3; c++) s = fmaf(wab * wz[c], row[tz[c]], s);
+        }
+    fc[(I * Lc.ny + J) * Lc.nz + K] = s * scale;
 }
 
-// coarse indices and weights interpolating fine index fi along an axis (the
-// transpose of axis_taps)
-__device__ __forceinline__ void axis_from(unsigned fi, unsigned nc, bool coarse, unsigned *idx, float *w, int &n)
+// Interpolation taps of fine index f along an axis (the transpose of rtaps):
+// an odd f is coarse node (f - 1) / 2; an even f lies between coarse nodes
+// f / 2 - 1 and f / 2, each at half weight, either of which may be a ghost
+// (weight 0, index clamped)
+__device__ __forceinline__ void ptaps(unsigned f, unsigned nc, bool coarse, unsigned t[2], float w[2])
 {
     if (!coarse) {
-        idx[0] = fi;
+        t[0] = t[1] = f;
         w[0] = 1.0f;
-        n = 1;
+        w[1] = 0.0f;
         return;
     }
-    n = 0;
-    if (fi & 1u) {
-        idx[0] = fi >> 1;               // (fi - 1) / 2 < nc
+    if (f & 1u) {
+        t[0] = t[1] = f >> 1;            // < nc
         w[0] = 1.0f;
-        n = 1;
+        w[1] = 0.0f;
         return;
     }
-    const unsigned hi = fi >> 1;         // coarse neighbours hi - 1 and hi
-    if (hi >= 1) {
-        idx[n] = hi - 1;
-        w[n++] = 0.5f;
-    }
-    if (hi < nc) {
-        idx[n] = hi;
-        w[n++] = 0.5f;
-    }
+    const unsigned hi = f >> 1;
+    const bool has_lo = hi >= 1, has_hi = hi < nc;
+    t[0] = has_lo ? hi - 1 : 0;
+    w[0] = has_lo ? 0.5f : 0.0f;
+    t[1] = has_hi ? hi : (has_lo ? hi - 1 : 0);
+    w[1] = has_hi ? 0.5f : 0.0f;
 }
 
-// e_f += P e_c
+// e_f += P e_c; one thread per fine node, 8 fixed taps
 __global__ void __launch_bounds__(kThreads) k_prolong(level Lf, level Lc, const float *ec, float *ef)
 {
-    const unsigned G = Lf.size();
-    const bool cx = Lc.nx != Lf.nx, cy = Lc.ny != Lf.ny, cz = Lc.nz != Lf.nz;
-    for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < G; o += gridDim.x * blockDim.x) {
-        unsigned i, j, k;
-        coords(Lf, o, i, j, k);
-        unsigned ix[2], iy[2], iz[2];
-        float wx[2], wy[2], wz[2];
-        int nx, ny, nz;
-        axis_from(i, Lc.nx, cx, ix, wx, nx);
-        axis_from(j, Lc.ny, cy, iy, wy, ny);
-        axis_from(k, Lc.nz, cz, iz, wz, nz);
-        float s = 0.0f;
-        for (int a = 0; a < nx; a++)
-            for (int b = 0; b < ny; b++)
-                for (int c = 0; c < nz; c++) s += wx[a] * wy[b] * wz[c] * ec[(ix[a] * Lc.ny + iy[b]) * Lc.nz + iz[c]];
-        ef[o] += s;
-    }
+    unsigned i, j, k;
+    if (!node3(Lf, i, j, k)) return;
+    unsigned tx[2], ty[2], tz[2];
+    float wx[2], wy[2], wz[2];
+    ptaps(i, Lc.nx, Lc.nx != Lf.nx, tx, wx);
+    ptaps(j, Lc.ny, Lc.ny != Lf.ny, ty, wy);
+    ptaps(k, Lc.nz, Lc.nz != Lf.nz, tz, wz);
+    float s = 0.0f;
+#pragma unroll
+    for (int a = 0; a < 2; a++)
+#pragma unroll
+        for (int b = 0; b < 2; b++) {
+            const float wab = wx[a] * wy[b];
+            const float *row = ec + (tx[a] * Lc.ny + ty[b]) * Lc.nz;
+#pragma unroll
+            for (int c = 0; c < 2; c++) s = fmaf(wab * wz[c], row[tz[c]], s);
+        }
+    ef[(i * Lf.ny + j) * Lf.nz + k] += s;
 }
 
 // the coarsest grid (at most kCoarseMax nodes): Jacobi sweeps from zero in one block
@@ -417,7 +479,7 @@ __global__ void __launch_bounds__(32) k_coarse(level L, float *e, const float *f
     if (o < G) a[o] = 0.0f;
     __syncthreads();
     float *cur = a, *nxt = b;
-    const float inv = (float)(1.0 / L.diag);
+    const float inv = L.invf;
     for (int s = 0; s < kCoarseSweeps; s++) {
         if (o < G) {
             unsigned i, j, k;
@@ -436,6 +498,40 @@ unsigned blocks_for(unsigned G)
 {
     const unsigned b = (G + kThreads - 1) / kThreads;
     return b < 152u * 8u ? (b ? b : 1u) : 152u * 8u;
+}
+
+// launch shape of a 3-D stencil kernel over nx x ny x nzw threads: blocks
+// of 256 threads over (z, y), z-width the power of two covering nzw (at most
+// 32), blockIdx.z = x
+struct shape3 {
+    dim3 grid, block;
+};
+
+shape3 shape_of(unsigned nx, unsigned ny, unsigned nzw)
+{
+    unsigned bx = 1;
+    while (bx < nzw && bx < 32) bx <<= 1;
+    const unsigned by = kThreads / bx;
+    return {dim3((nzw + bx - 1) / bx, (ny + by - 1) / by, nx), dim3(bx, by, 1)};
+}
+
+// column kernels (k_residual64, k_apply_dot32): the (z, y) blocks of
+// shape_of, and as many x-slices as keep the blocks near kRedBlocks
+shape3 column_shape(unsigned nx, unsigned ny, unsigned nz)
+{
+    shape3 sh = shape_of(nx, ny, nz);
+    const unsigned plane = sh.grid.x * sh.grid.y;
+    unsigned gz = plane >= (unsigned)kRedBlocks ? 1u : (unsigned)kRedBlocks / plane;
+    sh.grid.z = gz < nx ? gz : nx;
+    return sh;
+}
+
+// partials a reduction over level L0 writes at most
+size_t partial_count(const level &L0)
+{
+    const shape3 cs = column_shape(L0.nx, L0.ny, L0.nz);
+    const size_t cn = (size_t)cs.grid.x * cs.grid.y * cs.grid.z;
+    return cn > (size_t)kRedBlocks ? cn : (size_t)kRedBlocks;
 }
 
 unsigned red_blocks(unsigned G)
@@ -497,6 +593,7 @@ extern "C" int tm_diffusion_create(tm_diffusion **out, const int64_t gsize[3], i
     if (gsize[0] < 1 || gsize[1] < 1 || gsize[2] < 1) return tm_report(TM_EINVAL, "grid sizes must be >= 1");
     const long long G = (long long)gsize[0] * gsize[1] * gsize[2];
     if (G >= (1ll << 31)) return tm_report(TM_EINVAL, "grid above 2^31 nodes");
+    if (gsize[0] > 65535 || gsize[1] > 65535 * 8) return tm_report(TM_EINVAL, "grid axis too long for the launch shape");
     DK(cudaSetDevice(device));
     tm_diffusion *d = new tm_diffusion();
     d->device = device;
@@ -515,7 +612,7 @@ extern "C" int tm_diffusion_create(tm_diffusion **out, const int64_t gsize[3], i
     const size_t n0 = (size_t)G;
     ok = ok && a64(&d->b, n0) && a64(&d->r, n0);
     ok = ok && a32(&d->s, n0) && a32(&d->d, n0) && a32(&d->p, n0) && a32(&d->q, n0) && a32(&d->zv, n0);
-    ok = ok && a64(&d->partial, kRedBlocks);
+    ok = ok && a64(&d->partial, partial_count(d->lv[0]));
     ok = ok && cudaMalloc((void **)&d->sc, sizeof(scalars)) == cudaSuccess;
     ok = ok && cudaMallocHost((void **)&d->h_sc, sizeof(scalars)) == cudaSuccess;
     d->e.assign(d->lv.size(), nullptr);
@@ -560,22 +657,22 @@ static int vcycle(tm_diffusion *d, const std::vector<level> &lv, cudaStream_t st
     }
     for (int l = 0; l + 1 < nl; l++) {
         const level &L = lv[l];
-        const unsigned G = L.size(), gb = blocks_for(G);
-        k_zero<<<gb, kThreads, 0, st>>>(G, E[l]);
-        k_rbgs<<<gb, kThreads, 0, st>>>(L, E[l], F[l], 0);
-        k_rbgs<<<gb, kThreads, 0, st>>>(L, E[l], F[l], 1);
-        k_residual32<<<gb, kThreads, 0, st>>>(L, E[l], F[l], d->res[l]);
+        const shape3 full = shape_of(L.nx, L.ny, L.nz), half = shape_of(L.nx, L.ny, (L.nz + 1) / 2);
+        k_rbgs_first<<<full.grid, full.block, 0, st>>>(L, E[l], F[l]);
+        k_rbgs<<<half.grid, half.block, 0, st>>>(L, E[l], F[l], 1);
+        k_residual32<<<full.grid, full.block, 0, st>>>(L, E[l], F[l], d->res[l]);
         const level &C = lv[l + 1];
         const int dc = (C.nx != L.nx) + (C.ny != L.ny) + (C.nz != L.nz);
-        k_restrict<<<blocks_for(C.size()), kThreads, 0, st>>>(L, C, d->res[l], F[l + 1], 1.0f / (float)(1 << dc));
+        const shape3 cs = shape_of(C.nx, C.ny, C.nz);
+        k_restrict<<<cs.grid, cs.block, 0, st>>>(L, C, d->res[l], F[l + 1], 1.0f / (float)(1 << dc));
     }
     k_coarse<<<1, 32, 0, st>>>(lv[nl - 1], E[nl - 1], F[nl - 1]);
     for (int l = nl - 2; l >= 0; l--) {
         const level &L = lv[l];
-        const unsigned gb = blocks_for(L.size());
-        k_prolong<<<gb, kThreads, 0, st>>>(L, lv[l + 1], E[l + 1], E[l]);
-        k_rbgs<<<gb, kThreads, 0, st>>>(L, E[l], F[l], 1);
-        k_rbgs<<<gb, kThreads, 0, st>>>(L, E[l], F[l], 0);
+        const shape3 full = shape_of(L.nx, L.ny, L.nz), half = shape_of(L.nx, L.ny, (L.nz + 1) / 2);
+        k_prolong<<<full.grid, full.block, 0, st>>>(L, lv[l + 1], E[l + 1], E[l]);
+        k_rbgs<<<half.grid, half.block, 0, st>>>(L, E[l], F[l], 1);
+        k_rbgs<<<half.grid, half.block, 0, st>>>(L, E[l], F[l], 0);
     }
     DK(cudaGetLastError());
     return TM_OK;
@@ -594,6 +691,8 @@ static int inner_pcg(tm_diffusion *d, const std::vector<level> &lv, bool mg, int
 {
     const level &L0 = lv[0];
     const unsigned G = L0.size(), rb = red_blocks(G), gb = blocks_for(G);
+    const shape3 cs = column_shape(L0.nx, L0.ny, L0.nz);
+    const int cn = (int)(cs.grid.x * cs.grid.y * cs.grid.z);
     const float inv_diag = (float)(1.0 / L0.diag);
     int rc, it = 0;
     for (; it < max_iter; it++) {
@@ -605,8 +704,8 @@ static int inner_pcg(tm_diffusion *d, const std::vector<level> &lv, bool mg, int
         }
         k_finish<<<1, kThreads, 0, st>>>(d->partial, rb, d->sc, it == 0 ? 4 : 5);
         k_direction32<<<gb, kThreads, 0, st>>>(G, d->p, d->zv, d->sc, it == 0);
-        k_apply_dot32<<<rb, kThreads, 0, st>>>(L0, d->p, d->q, d->partial);
-        k_finish<<<1, kThreads, 0, st>>>(d->partial, rb, d->sc, 2);
+        k_apply_dot32<<<cs.grid, cs.block, 0, st>>>(L0, d->p, d->q, d->partial);
+        k_finish<<<1, kThreads, 0, st>>>(d->partial, cn, d->sc, 2);
         k_update32<<<rb, kThreads, 0, st>>>(G, d->d, d->s, d->p, d->q, d->sc, d->partial);
         k_finish<<<1, kThreads, 0, st>>>(d->partial, rb, d->sc, 3);
         DK(cudaGetLastError());
@@ -625,14 +724,16 @@ static int solve(tm_diffusion *d, const std::vector<level> &lv, double *u, doubl
                  int *inner, int *refinements, double *relres)
 {
     const level &L0 = lv[0];
-    const unsigned G = L0.size(), rb = red_blocks(G), gb = blocks_for(G);
+    const unsigned G = L0.size(), gb = blocks_for(G);
+    const shape3 cs = column_shape(L0.nx, L0.ny, L0.nz);
+    const int cn = (int)(cs.grid.x * cs.grid.y * cs.grid.z);
     int rc;
     *inner = 0;
     *refinements = 0;
     double rel = 0.0;
     for (int k = 0; k <= kMaxRefine; k++) {
-        k_residual64<<<rb, kThreads, 0, st>>>(L0, u, d->b, d->r, d->partial);
-        k_finish<<<1, kThreads, 0, st>>>(d->partial, rb, d->sc, 1);
+        k_residual64<<<cs.grid, cs.block, 0, st>>>(L0, u, d->b, d->r, d->partial);
+        k_finish<<<1, kThreads, 0, st>>>(d->partial, cn, d->sc, 1);
         DK(cudaGetLastError());
         if ((rc = read_scalars(d, st))) return rc;
         const double bb = d->h_sc->bb, rr = d->h_sc->rr;
@@ -690,6 +791,11 @@ extern "C" int tm_diffusion_step(tm_diffusion *d, double *data, float resolution
                 L.zz = P.zz * (L.nz != P.nz ? 0.25 : 1.0);
                 L.diag = c0 + 2.0 * (L.zx + L.zy + L.zz);
             }
+            L.zxf = (float)L.zx;
+            L.zyf = (float)L.zy;
+            L.zzf = (float)L.zz;
+            L.diagf = (float)L.diag;
+            L.invf = (float)(1.0 / L.diag);
         }
         if (mg) S.multigrid_fields++;
         double *u = data + (size_t)fi * G;
