@@ -153,19 +153,18 @@ __global__ void __launch_bounds__(kThreads) k_residual64(level L, const double *
                                                          double *partial)
 {
     double acc = 0.0;
-    const unsigned k = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
-    const unsigned nyz = L.ny * L.nz;
-    if (k < L.nz && j < L.ny)
-        for (unsigned i = blockIdx.z; i < L.nx; i += gridDim.z) {
-            const unsigned o = (i * L.ny + j) * L.nz + k;
-            const double xm = i > 0 ? u[o - nyz] : 0.0, xp = i + 1 < L.nx ? u[o + nyz] : 0.0;
-            const double ym = j > 0 ? u[o - L.nz] : 0.0, yp = j + 1 < L.ny ? u[o + L.nz] : 0.0;
-            const double zm = k > 0 ? u[o - 1] : 0.0, zp = k + 1 < L.nz ? u[o + 1] : 0.0;
-            const double sn = ((xm + xp) + (ym + yp)) + (zm + zp);
-            const double v = fma(-L.diag, u[o], fma(L.zx, sn, b[o]));
-            r[o] = v;
-            acc = fma(v, v, acc);
-        }
+    const unsigned G = L.size(), nyz = L.ny * L.nz;
+    for (unsigned o = blockIdx.x * blockDim.x + threadIdx.x; o < G; o += gridDim.x * blockDim.x) {
+        unsigned i, j, k;
+        coords(L, o, i, j, k);
+        const double xm = i > 0 ? u[o - nyz] : 0.0, xp = i + 1 < L.nx ? u[o + nyz] : 0.0;
+        const double ym = j > 0 ? u[o - L.nz] : 0.0, yp = j + 1 < L.ny ? u[o + L.nz] : 0.0;
+        const double zm = k > 0 ? u[o - 1] : 0.0, zp = k + 1 < L.nz ? u[o + 1] : 0.0;
+        const double sn = ((xm + xp) + (ym + yp)) + (zm + zp);
+        const double v = fma(-L.diag, u[o], fma(L.zx, sn, b[o]));
+        r[o] = v;
+        acc = fma(v, v, acc);
+    }
     block_partial(acc, partial);
 }
 
@@ -190,7 +189,8 @@ __global__ void __launch_bounds__(kThreads) k_correct64(unsigned G, double *u, c
 
 // ------------------------------------------------------------ FP32 inner CG
 
-// q = A p; partials of p.q (column mapping as k_residual64)
+// q = A p; partials of p.q; blocks over (z, y), each thread walks x in
+// steps of gridDim.z (no coordinate division; a fixed number of partials)
 __global__ void __launch_bounds__(kThreads) k_apply_dot32(level L, const float *p, float *q, double *partial)
 {
     float acc = 0.0f;
@@ -515,7 +515,7 @@ shape3 shape_of(unsigned nx, unsigned ny, unsigned nzw)
     return {dim3((nzw + bx - 1) / bx, (ny + by - 1) / by, nx), dim3(bx, by, 1)};
 }
 
-// column kernels (k_residual64, k_apply_dot32): the (z, y) blocks of
+// column kernel (k_apply_dot32): the (z, y) blocks of
 // shape_of, and as many x-slices as keep the blocks near kRedBlocks
 shape3 column_shape(unsigned nx, unsigned ny, unsigned nz)
 {
@@ -724,16 +724,14 @@ static int solve(tm_diffusion *d, const std::vector<level> &lv, double *u, doubl
                  int *inner, int *refinements, double *relres)
 {
     const level &L0 = lv[0];
-    const unsigned G = L0.size(), gb = blocks_for(G);
-    const shape3 cs = column_shape(L0.nx, L0.ny, L0.nz);
-    const int cn = (int)(cs.grid.x * cs.grid.y * cs.grid.z);
+    const unsigned G = L0.size(), rb = red_blocks(G), gb = blocks_for(G);
     int rc;
     *inner = 0;
     *refinements = 0;
     double rel = 0.0;
     for (int k = 0; k <= kMaxRefine; k++) {
-        k_residual64<<<cs.grid, cs.block, 0, st>>>(L0, u, d->b, d->r, d->partial);
-        k_finish<<<1, kThreads, 0, st>>>(d->partial, cn, d->sc, 1);
+        k_residual64<<<rb, kThreads, 0, st>>>(L0, u, d->b, d->r, d->partial);
+        k_finish<<<1, kThreads, 0, st>>>(d->partial, rb, d->sc, 1);
         DK(cudaGetLastError());
         if ((rc = read_scalars(d, st))) return rc;
         const double bb = d->h_sc->bb, rr = d->h_sc->rr;
