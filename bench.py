@@ -381,8 +381,9 @@ def cycle_rows(device, reps=5):
     cells (seed 2): phases G0/G1/S/G2/M with probabilities .1/.4/.25/.21/.04,
     phase times uniform in [0, 12) h, lengths 11/8/4/1 h, death probability
     0.1, one step of 3600 s, so that the M cells (4 %) divide and about 2 %
-    die; wall time per call (each waits for its draw counts and the C
-    library's rand() values)."""
+    die; wall time per call (each waits for its draw counts).  The draws come
+    from the C library's stream, generated on the device or, for comparison,
+    by calling rand() on the host."""
     import dataclasses
     import time
 
@@ -391,8 +392,9 @@ def cycle_rows(device, reps=5):
     n = 1_000_000
     col = C.make_colony("clustered", n, 2, radius_for("clustered", n, 2))
     rng = np.random.Generator(np.random.PCG64(9))
+    rng2 = np.random.Generator(np.random.PCG64(10))
     types = {"g1": [11.0], "s": [8.0], "g2": [4.0], "m": [1.0], "v": [0.2], "rd": [0.1], "cd": [1e9]}
-    t_cyc, t_cmp, divided, marked = [], [], [], []
+    t_cyc, t_cmp, t_libc, divided, marked = [], [], [], [], []
     with S.Session(col.types, dim=3, max_slots=3 * n, device=device) as s:
         for k in range(reps + 1):
             phase = rng.choice(5, size=n, p=[0.1, 0.4, 0.25, 0.21, 0.04]).astype(np.int32)
@@ -401,22 +403,38 @@ def cycle_rows(device, reps=5):
             s.set_cycle(cid, rng.uniform(0.0, 12.0, n), np.full(n, 11.0), np.full(n, 8.0), np.full(n, 4.0),
                         np.full(n, 1.0), np.zeros(n, np.int32))
             s.sync()
+            # the C library's stream after srand(k), generated on the device
             t0 = time.perf_counter()
-            dv, mk = s.cellcycle(cid, types, secondsperstep=3600.0)
+            dv, mk = s.cellcycle(cid, types, secondsperstep=3600.0, stream=S.RandStream(k))
             s.sync()
             t1 = time.perf_counter()
             s.compact(cid)
             s.sync()
             t2 = time.perf_counter()
             s.remove_colony(cid)
+            # the same step drawing through the C library's rand() on the host
+            cid = s.add_colony(dataclasses.replace(col, phase=phase), precision="fp64", update="dt", dt=0.01,
+                               reserve=2 * n)
+            s.set_cycle(cid, rng2.uniform(0.0, 12.0, n), np.full(n, 11.0), np.full(n, 8.0), np.full(n, 4.0),
+                        np.full(n, 1.0), np.zeros(n, np.int32))
+            s.sync()
+            t3 = time.perf_counter()
+            s.cellcycle(cid, types, secondsperstep=3600.0)
+            s.sync()
+            t4 = time.perf_counter()
+            s.remove_colony(cid)
             if k:
                 t_cyc.append((t1 - t0) * 1e3)
                 t_cmp.append((t2 - t1) * 1e3)
+                t_libc.append((t4 - t3) * 1e3)
                 divided.append(dv)
                 marked.append(mk)
     return {"config": "1,000,000 clustered cells (seed 2), phases G0/G1/S/G2/M .1/.4/.25/.21/.04, phase times "
                       "uniform in [0, 12) h, lengths 11/8/4/1 h, rd 0.1, one step of 3600 s",
             "cellcycle_ms": float(np.mean(t_cyc)), "compact_ms": float(np.mean(t_cmp)),
+            "cellcycle_host_rand_ms": float(np.mean(t_libc)),
+            "draws": "cellcycle_ms: the C library's rand() stream after srand(step) generated on the device "
+                     "(tm_cycle_params.rand_seeded); cellcycle_host_rand_ms: the same step calling rand() on the host",
             "cells_per_s": n / (np.mean(t_cyc) * 1e-3), "divided": int(np.mean(divided)),
             "marked": int(np.mean(marked))}
 

@@ -190,6 +190,14 @@ typedef struct tm_cycle_params {
     float secondsperstep;
     int (*draw)(void *ctx);
     void *draw_ctx;
+    /* rand_seeded = 1: the values come from the C library's rand() stream
+     * after srand(rand_seed), starting after *rand_offset earlier values,
+     * generated on the device (the same values rand() would return, without
+     * calling it); *rand_offset advances by the values taken.  draw is then
+     * unused. */
+    int rand_seeded;
+    uint32_t rand_seed;
+    int64_t *rand_offset;
 } tm_cycle_params;
 
 /* Cell-cycle state of a colony's cells in the caller's order (n entries):

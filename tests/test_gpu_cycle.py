@@ -83,3 +83,63 @@ def test_cellcycle_matches_oracle(oracle_lib, dim, seed):
     assert removed == marked
     for k in ("phase", "g1", "age", "size"):
         assert np.array_equal(kept[k], ref[k][keep]), k
+
+
+def _cycle_run(types, col, cyc, env, stream_seed=None, libc_seed=None, calls=2):
+    """Cell-cycle steps of one colony; the draws from the C library after
+    srand(libc_seed), or from the device stream of stream_seed."""
+    torch = _torch()
+    from timothy_gb300 import session as S
+
+    n = col.n
+    cellenv = np.zeros((2, n, 4))
+    cellenv[:, :, 0] = env
+    outs = []
+    stream = S.RandStream(stream_seed) if stream_seed is not None else None
+    with S.Session(types, dim=col.dim, max_slots=4 * n + 64, list_capacity=384) as s:
+        cid = s.add_colony(col, precision="fp64", update="none", verlet=True, reserve=4 * n)
+        s.step(1)
+        s.sync()
+        s.set_cycle(cid, cyc["phasetime"], cyc["g1"], cyc["s"], cyc["g2"], cyc["m"], cyc["age"])
+        if libc_seed is not None:
+            srand(libc_seed)
+        for _ in range(calls):
+            m = s._n[cid]
+            env_m = torch.from_numpy(np.ascontiguousarray(np.resize(cellenv, (2, m, 4)))).cuda()
+            res = s.cellcycle(cid, TYPES, nfields=2, cl1=CL1, cl2=CL2, cellenv=env_m, stream=stream)
+            outs.append((res, s.get_cycle(cid), s.download(cid, ["x", "y", "z", "removecell"])))
+    return outs, stream
+
+
+def test_device_rand_stream_matches_libc():
+    """tm_cycle_params.rand_seeded: the values of the C library's stream after
+    srand(seed), generated on the device, give the same cells bit for bit as
+    the library's own rand() calls, over consecutive steps; the stream's
+    offset then points where the library's next rand() would be."""
+    types = C.CellTypes.consistent(h=(2.5, 2.5), size=(1.0, 0.9))
+    n, seed = 6000, 77
+    col = C.make_colony("uniform", n, seed, C.initial_radius("uniform", n), types=types)
+    rng = np.random.default_rng(seed)
+    cyc = dict(phasetime=rng.uniform(0, 12, n).astype(np.float32), g1=rng.uniform(8, 12, n).astype(np.float32),
+               s=rng.uniform(6, 9, n).astype(np.float32), g2=rng.uniform(2, 5, n).astype(np.float32),
+               m=rng.uniform(0.5, 2, n).astype(np.float32), age=rng.integers(0, 5, n).astype(np.int32))
+    col.phase[:] = rng.integers(0, 6, n)
+    env = rng.uniform(0, 1, (2, n))
+    a, _ = _cycle_run(types, col, cyc, env, libc_seed=seed, calls=3)
+    libc = ctypes.CDLL(None)
+    libc.rand.restype = ctypes.c_int
+    next_libc = libc.rand()
+    b, stream = _cycle_run(types, col, cyc, env, stream_seed=seed, calls=3)
+    for (ra, ca, oa), (rb, cb, ob) in zip(a, b):
+        assert ra == rb
+        for k in ca:
+            assert np.array_equal(ca[k], cb[k]), k
+        for k in oa:
+            assert np.array_equal(oa[k], ob[k]), k
+    lib = ctypes.CDLL(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "timothy_gb300",
+                                   "libtimothy_gb300.so"))
+    lib.tmi_libc_rand_host.argtypes = [ctypes.c_uint32, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p]
+    nxt = np.zeros(1, np.int32)
+    lib.tmi_libc_rand_host(seed, stream.offset, 1, nxt.ctypes.data)
+    assert int(nxt[0]) == next_libc
+    assert sum(r[0][0] for r in b) > 0                     # divisions happened

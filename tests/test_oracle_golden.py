@@ -195,3 +195,4 @@ def test_oracle_diffusion_matches_live_reference(oracle_lib):
     assert out["iters"] == r["iters"] == 1
     assert np.array_equal(out["b"], r["b"])
     assert np.max(np.abs(out["u"] - r["x"])) <= 1e-13 * np.max(np.abs(r["x"]))
+

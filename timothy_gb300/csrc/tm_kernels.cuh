@@ -70,3 +70,14 @@ cudaError_t tm_launch_cycle_count(const tm_cycle_dev &P, const tm_arrays &a, lon
 cudaError_t tm_launch_cycle_apply(const tm_cycle_dev &P, const tm_arrays &a, long long off, long long n, int dim,
                                   const uint32_t *draw_off, const uint32_t *div_off, const int *stream,
                                   unsigned long long *marked, cudaStream_t st);
+
+// the C library's rand() stream on the device (tm_libcrand.cu)
+struct tm_rand_cache {
+    int valid;
+    uint32_t seed;
+    int64_t offset;
+    uint32_t window[31];
+};
+int tm_libc_rand_device(uint32_t seed, int64_t offset, int64_t count, int *out, tm_rand_cache *cache,
+                        uint32_t *d_windows, int64_t windows_cap, cudaStream_t st);
+

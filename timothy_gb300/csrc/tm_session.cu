@@ -161,6 +161,9 @@ struct tm_session {
     int *cy_stream = nullptr;
     size_t cy_stream_cap = 0;
     unsigned long long *cy_marked = nullptr;
+    tm_rand_cache rand_cache = {};          // where the last device rand() stream ended
+    uint32_t *rand_windows = nullptr;        // per-chunk starting windows of that stream
+    int64_t rand_windows_cap = 0;
     int *move_buf = nullptr;     // the drop-in's random-move draws
     size_t move_cap = 0;
     tm_tuning tune{1, 1, 128, 0.1f, 64};
@@ -669,7 +672,7 @@ extern "C" int tm_session_destroy(tm_session *s)
     if (s->env_buf) cudaFree(s->env_buf);
     {
         void *cy[] = {s->A.cy_pt, s->A.cy_g1, s->A.cy_s, s->A.cy_g2, s->A.cy_m, s->A.cy_age, s->cy_params,
-                      s->cy_stream, s->cy_marked, s->move_buf};
+                      s->cy_stream, s->cy_marked, s->move_buf, s->rand_windows};
         for (void *p : cy)
             if (p) cudaFree(p);
     }
@@ -2314,16 +2317,34 @@ extern "C" int tm_colony_cellcycle(tm_session *s, int id, const tm_cycle_params 
         return tm_fail(TM_ENOMEM, "colony %d: %lld cells and %u daughters exceed its %d slots", id, n, tot[1],
                        c.nslots);
     // the random values, in the reference's order
-    std::vector<int> hs(tot[0] > 0 ? tot[0] : 1);
-    for (uint32_t k = 0; k < tot[0]; k++) hs[k] = p->draw ? p->draw(p->draw_ctx) : rand();
-    if (s->cy_stream_cap < hs.size()) {
+    const size_t nd = tot[0] > 0 ? tot[0] : 1;
+    if (s->cy_stream_cap < nd) {
         if (s->cy_stream) CK(cudaFree(s->cy_stream));
         s->cy_stream = nullptr;
         s->cy_stream_cap = 0;
-        if ((rc = dalloc(&s->cy_stream, (long long)hs.size()))) return rc;
-        s->cy_stream_cap = hs.size();
+        if ((rc = dalloc(&s->cy_stream, (long long)nd))) return rc;
+        s->cy_stream_cap = nd;
     }
-    CK(cudaMemcpyAsync(s->cy_stream, hs.data(), hs.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    std::vector<int> hs;
+    if (p->rand_seeded && p->rand_offset) {
+        // the C library's stream after srand(rand_seed), generated on the device
+        const int64_t chunks = ((int64_t)tot[0] + 2047) / 2048 + 1;
+        if (s->rand_windows_cap < chunks) {
+            if (s->rand_windows) CK(cudaFree(s->rand_windows));
+            s->rand_windows = nullptr;
+            s->rand_windows_cap = 0;
+            if ((rc = dalloc(&s->rand_windows, chunks * 31))) return rc;
+            s->rand_windows_cap = chunks;
+        }
+        if (tm_libc_rand_device(p->rand_seed, *p->rand_offset, (int64_t)tot[0], s->cy_stream, &s->rand_cache,
+                                s->rand_windows, s->rand_windows_cap, st) != 0)
+            return tm_fail(TM_ECUDA, "device rand() stream failed");
+        *p->rand_offset += (int64_t)tot[0];
+    } else {
+        hs.resize(nd);
+        for (uint32_t k = 0; k < tot[0]; k++) hs[k] = p->draw ? p->draw(p->draw_ctx) : rand();
+        CK(cudaMemcpyAsync(s->cy_stream, hs.data(), hs.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    }
     CK(cudaMemsetAsync(s->cy_marked, 0, sizeof(unsigned long long), st));
     // pass 2: the transitions
     CK(tm_launch_cycle_apply(P, a, c.off, n, s->K.dim, draw_off, div_off, s->cy_stream, s->cy_marked, st));

@@ -71,7 +71,18 @@ _DRAW = C.CFUNCTYPE(C.c_int, C.c_void_p)
 class _CycleParams(C.Structure):
     _fields_ = [("types", C.POINTER(_CycleType)), ("nfields", C.c_int), ("criticallevel1", C.c_void_p),
                 ("criticallevel2", C.c_void_p), ("cellenv", C.c_void_p), ("simulationstart", C.c_int),
-                ("secondsperstep", C.c_float), ("draw", _DRAW), ("draw_ctx", C.c_void_p)]
+                ("secondsperstep", C.c_float), ("draw", _DRAW), ("draw_ctx", C.c_void_p),
+                ("rand_seeded", C.c_int), ("rand_seed", C.c_uint32), ("rand_offset", C.POINTER(C.c_int64))]
+
+
+class RandStream:
+    """The C library's rand() stream after srand(seed), for cellcycle(): the
+    values are generated on the device (tm_cycle_params.rand_seeded);
+    ``offset`` counts the values taken so far."""
+
+    def __init__(self, seed: int, offset: int = 0):
+        self.seed = int(seed) & 0xffffffff
+        self.offset = int(offset)
 
 
 class _Tuning(C.Structure):
@@ -392,7 +403,8 @@ class Session:
         return out
 
     def cellcycle(self, cid: int, types: dict, *, nfields: int = 0, cl1=None, cl2=None, cellenv=None,
-                  simulationstart: int = 1, secondsperstep: float = 3600.0, draw=None) -> tuple[int, int]:
+                  simulationstart: int = 1, secondsperstep: float = 3600.0, draw=None,
+                  stream: RandStream | None = None) -> tuple[int, int]:
         """One cell-cycle step; types holds per-type g1, s, g2, m, v, rd, cd arrays.
         cellenv: device array (nfields, n, 4).  draw: None (the C library's
         rand()) or a callable returning the next value.  Returns (divided, marked)."""
@@ -402,13 +414,17 @@ class Session:
         c1 = np.ascontiguousarray(cl1 if cl1 is not None else np.zeros(1), np.float32)
         c2 = np.ascontiguousarray(cl2 if cl2 is not None else np.zeros(1), np.float32)
         fn = _DRAW(lambda ctx: int(draw())) if draw is not None else _DRAW()
+        off = C.c_int64(stream.offset if stream is not None else 0)
         prm = _CycleParams(C.cast(tarr, C.POINTER(_CycleType)), int(nfields), _p(c1), _p(c2),
                            _dptr(cellenv) if cellenv is not None else None, int(simulationstart),
-                           float(secondsperstep), fn, None)
+                           float(secondsperstep), fn, None, 1 if stream is not None else 0,
+                           stream.seed if stream is not None else 0, C.pointer(off))
         d = np.zeros(1, np.int64)
         mk = np.zeros(1, np.int64)
         rc = load_library().tm_colony_cellcycle(self._h, cid, C.byref(prm), _p(d), _p(mk))
         _check(rc)
+        if stream is not None:
+            stream.offset = int(off.value)
         self._n[cid] += int(d[0])
         return int(d[0]), int(mk[0])
 
