@@ -218,7 +218,9 @@ int tm_colony_cellcycle(tm_session *s, int id, const tm_cycle_params *p, int64_t
  * through tm_colony_upload); a cell type outside the table is read as 0 and
  * reported as TM_DEVERR_TYPES by the next tm_session_sync.  Both return once
  * the work is queued: the caller leaves in's arrays unchanged, and reads
- * out's arrays only, after tm_session_sync. */
+ * out's arrays only, after tm_session_sync.  They stage through device
+ * buffers of their own, 44 and 104 bytes per slot, allocated on first use
+ * (not counted by tm_session_bytes). */
 int tm_colony_upload_async(tm_session *s, int id, const tm_colony_input *in);
 int tm_colony_download_async(tm_session *s, int id, const tm_colony_output *out);
 /* Replace the cells of an existing colony (at most the slots it holds).  With
