@@ -550,6 +550,21 @@ def main():
                 "peak_source": peak_kind, "kernel": kname, "kernel_ms": list_ms,
                 "phases_ms": {k: prof[k] for k in ("build_ms", "search_ms", "list_ms", "fix_ms", "octree_ms",
                                                    "update_ms", "cic_ms")}}
+    # the compute side of the list pass (the path is a gather-reduce: no
+    # tensor cores): pairs within h per second, from this colony's own
+    # neighbour counts, and the algorithmic FP32 flops of those pairs (the
+    # reference's expressions, about 83 flops per pair for density and force)
+    # against the nominal FP32 rate of the part (152 SMs x 128 lanes x 2 x
+    # the maximum SM clock; no measured figure exists for it)
+    nb = s.download(cid, ["nbcount"])["nbcount"]
+    pairs = float(np.sum(nb.astype(np.int64)))
+    if list_ms:
+        fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
+        pair_rate = pairs / (list_ms * 1e-3)
+        roofline["compute"] = {"pairs_within_h_per_launch": pairs, "pairs_per_s": pair_rate,
+                               "algorithmic_tflops": pair_rate * 83 / 1e12, "fp32_peak_tflops": fp32_peak,
+                               "fp32_peak_source": "nominal (152 SMs x 128 FP32 lanes x 2 x 2.07 GHz)",
+                               "frac": pair_rate * 83 / 1e12 / fp32_peak}
     out_fast = s.download(cid, ["x", "y", "z", "density", "fx", "fy", "fz"]) if prec == "fp32c" else None
 
     # end to end through the public API with host buffers: per step the cells go

@@ -97,11 +97,13 @@ class Server:
     def __init__(self, types: C.CellTypes | None = None, *, precision: str = "fp32c", dt: float = 0.01,
                  hbm_fraction: float = 0.6, max_slots: int | None = None, max_colonies: int = 2048,
                  list_capacity: int = 384, device: int = 0, graph: bool = True, tuning: dict | None = None,
-                 fields=("x", "y", "z", "density", "fx", "fy", "fz"), keep_results: bool = False):
+                 fields=("x", "y", "z", "density", "fx", "fy", "fz"), keep_results: bool = False,
+                 prepare_ahead: int = 16):
         from .session import Session, device_memory, session_bytes
 
         self.types = types or C.CellTypes.consistent()
         self.precision, self.dt, self.fields, self.keep = precision, dt, list(fields), keep_results
+        self.prepare_ahead = prepare_ahead
         bins_per_slot = 8
 
         def nbytes(slots):
@@ -184,6 +186,12 @@ class Server:
             s.step(1)
             it += 1
             stepped_cells += sum(r.n for r, _ in active.values())
+            # the step runs on the device: meanwhile build the cells of the
+            # requests that wait, so their admission costs only the upload
+            if source is not None:
+                for req in list(queue)[:self.prepare_ahead]:
+                    if req.colony is None:
+                        req.colony = source.colony(req.kind, req.n, req.seed)
             done = []
             for cid, entry in active.items():
                 entry[1] -= 1
