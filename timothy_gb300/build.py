@@ -22,6 +22,10 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libtimothy_gb300.so")
+# the reference-signature drop-ins as a static archive: a program links them
+# as regular objects, so their definitions replace the reference's (weakened)
+# ones, which a shared library's definitions cannot do
+DROPIN_LIB = os.path.join(PKG, "libtimothy_gb300_dropin.a")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
@@ -72,6 +76,11 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
             logs.append(err)
     if jobs or not os.path.exists(LIB):
         _run([nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"])
+    dropin_obj = os.path.join(BUILD, "tm_dropin.c.o")
+    if jobs or not os.path.exists(DROPIN_LIB):
+        if os.path.exists(DROPIN_LIB):
+            os.remove(DROPIN_LIB)
+        _run(["ar", "rcs", DROPIN_LIB, dropin_obj])
     if verbose or ptxas_info:
         for l in logs:
             if l:
