@@ -51,7 +51,7 @@ B_CELL = 112
 # dram__bytes_write.sum over the cells of the launch), from the ncu capture
 # summarised in profiles/k_plist_fp32_clustered2m.txt; traffic grows with the
 # cell count, so a launch over n cells moves n times this.
-TRAFFIC_PER_CELL = {"k_plist<1>": 375.0}
+TRAFFIC_PER_CELL = {"k_plist<1>": 376.1}
 # Colony radii giving a mean of 40 neighbours within h = 2.5 (bisected with
 # full-size neighbour counts; the bench reports the measured mean each run).
 RADIUS = {
