@@ -171,3 +171,50 @@ def test_environment_dropins_match_reference():
         run.compute(writeback=True)
         for f in range(len(fields)):
             assert np.array_equal(run.data(f), run.solution(f))
+
+
+def test_one_shot_and_two_fields(oracle_lib):
+    """tm_field_diffuse (a solver made for the call) on two fields at once,
+    against the oracle field by field."""
+    torch = _torch()
+    import ctypes as C
+
+    from timothy_gb300 import session as S
+
+    gs = (21, 18, 12)
+    rng = np.random.default_rng(2)
+    u0 = rng.uniform(0.0, 1.0, (2,) + gs)
+    src = rng.uniform(0.0, 0.2, (2,) + gs)
+    # field 0: z = 0.625 (plain CG); field 1: z = 3750 (multigrid)
+    dc, bc, lam, res, sps, gfdt = [0.01, 60.0], [0.3, 0.0], [0.0, 0.002], 4.0, 3000.0, 1000.0
+    ref = oracle_lib.diffuse(gs, res, sps, gfdt, 1, dc, bc, [0.0, 0.0], lam, u0=u0, source=src)
+    data = torch.from_numpy(u0.copy()).cuda()
+    st = S.DiffusionStats()
+    arr = [np.ascontiguousarray(v, np.float64) for v in (dc, bc, lam)]
+    gsz = np.array(gs, np.int64)
+    lib = S.load_library()
+    rc = lib.tm_field_diffuse(data.data_ptr(), gsz.ctypes.data, res, 2, *[a.ctypes.data for a in arr], sps, gfdt,
+                              torch.from_numpy(src).cuda().data_ptr(), 1e-14, C.byref(st), None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    assert st.solves_per_field == ref["iters"] == 3 and st.multigrid_fields == 1
+    got = data.cpu().numpy()
+    for f in range(2):
+        assert np.max(np.abs(got[f] - ref["u"][f])) <= 1e-11 * np.max(np.abs(ref["u"][f])), f
+
+
+def test_environment_dropins_2d():
+    """The drop-ins on a one-layer (2-D) grid: the reference's fixture (the
+    point source lies off the grid there: no z node 5)."""
+    _torch()
+    from timothy_gb300.refabi import EnvironmentRun
+
+    rec = np.load(os.path.join(GOLDEN, "field_diffuse_2d.npz"))
+    fields = [{"dc": float(rec["dc"][0]), "bc": float(rec["bc"][0]), "mean": float(rec["mean"][0]),
+               "lam": float(rec["lam"][0])}]
+    with EnvironmentRun(2, float(rec["gfh"]), fields, secondsperstep=float(rec["sps"]), gfdt=float(rec["gfdt"]),
+                        step=int(rec["step"])) as run:
+        assert run.gsize == tuple(int(v) for v in rec["gsize"])
+        run.compute(writeback=True)
+        sol = run.data(0)
+        assert np.max(np.abs(sol - rec["x"][0])) <= 1e-10 * np.max(np.abs(rec["x"][0]))
