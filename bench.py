@@ -341,6 +341,75 @@ def field_rows(device, peak, steps=10):
                           "cell_gathers_per_s": n / (ms_e * 1e-3)}}
 
 
+def cic_rows(device, peak, steps=10):
+    """The CIC deposit (patches_alloc + patches_cells2envinfo) on the 1,000,000
+    clustered cells of the scale1m workload (seed 2) onto the 257^3 FP64 grid
+    of GFH 8: inside a session step (the deposit phase of an FP32 + compensated
+    step, CUDA events) and through the allocation-free entry point on device
+    arrays (L2 flushed before each call).  Algorithmic bytes: the cells'
+    positions and phases in (28 B/cell) and one write of the grid."""
+    import ctypes
+
+    import torch
+
+    from oracle import bindings as OB
+    from timothy_gb300 import session as S
+
+    torch.cuda.set_device(device)
+    n, gfh = 1_000_000, 8.0
+    col = C.make_colony("clustered", n, 2, radius_for("clustered", n, 2))
+    dims = OB.grid_dims(3, gfh)
+    G = int(np.prod(dims))
+    bytes_ = n * 28 + G * 8
+    out = {"config": "1,000,000 clustered cells (seed 2), 257^3 FP64 grid (GFH 8)", "bytes": bytes_}
+    with S.Session(col.types, dim=3, max_slots=n + 64, list_capacity=384, device=device) as s:
+        s.add_colony(col, precision="fp32c", update="dt", dt=0.01, cic=True, gfh=gfh, verlet=True)
+        s.step(3)
+        s.sync()
+        s.profile(True)
+        s.step(steps)
+        s.sync()
+        prof = s.profile_read()
+        s.profile(False)
+    ms = prof["cic_ms"]
+    out["in_step"] = {"ms": ms, "achieved_gbs": bytes_ / ms / 1e6, "frac_of_measured_hbm": bytes_ / ms / 1e6 / peak}
+    lib = S.load_library()
+    fn = lib.tm_cic_deposit_noalloc
+    P = ctypes.c_void_p
+    fn.restype = ctypes.c_int
+    fn.argtypes = [P, P, P, P, ctypes.c_int64, ctypes.c_int, P, ctypes.c_float, P, P, P, P]
+    xs = [torch.from_numpy(np.ascontiguousarray(getattr(col, k))).cuda() for k in ("x", "y", "z")]
+    ph = torch.from_numpy(np.ascontiguousarray(col.phase, np.int32)).cuda()
+    grid = torch.zeros(G, dtype=torch.float64, device="cuda")
+    corners = torch.zeros(6, dtype=torch.int64, device="cuda")
+    lower = np.array([-1024.0, -1024.0, -1024.0])
+    gs = np.array(dims, np.int64)
+    flush = torch.empty(32 * 1024 * 1024, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+
+    def call():
+        rc = fn(xs[0].data_ptr(), xs[1].data_ptr(), xs[2].data_ptr(), ph.data_ptr(), n, 3, lower.ctypes.data, gfh,
+                gs.ctypes.data, grid.data_ptr(), corners.data_ptr(), stream)
+        if rc:
+            raise RuntimeError(f"tm_cic_deposit_noalloc: {rc}")
+
+    for _ in range(3):
+        call()
+    ts = []
+    for _ in range(steps):
+        flush.fill_(1.0)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        call()
+        b.record()
+        torch.cuda.synchronize()
+        ts.append(a.elapsed_time(b))
+    ms2 = float(np.mean(ts))
+    out["noalloc_call"] = {"ms": ms2, "achieved_gbs": bytes_ / ms2 / 1e6,
+                           "frac_of_measured_hbm": bytes_ / ms2 / 1e6 / peak}
+    return out
+
+
 def diffusion_rows(device, steps=3):
     """The implicit diffusion step (environment_compute) on the 257^3 FP64 grid
     of GFH 8, one field, from the reference's start (the mean) with its point
@@ -469,13 +538,14 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=50)
     ap.add_argument("--serve-rates", default="200,50", help="request rates (per s) of the serving runs")
     ap.add_argument("--serve-seconds", type=float, default=20.0)
-    ap.add_argument("--row", choices=["grid_to_cell", "diffusion", "cell_cycle"],
+    ap.add_argument("--row", choices=["grid_to_cell", "cic_deposit", "diffusion", "cell_cycle"],
                     help="measure one of the rows beside the path alone and print it (no bench line)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.row:
         peak = measured_peaks()[0]
-        fn = {"grid_to_cell": lambda: field_rows(0, peak), "diffusion": lambda: diffusion_rows(0),
+        fn = {"grid_to_cell": lambda: field_rows(0, peak), "cic_deposit": lambda: cic_rows(0, peak),
+              "diffusion": lambda: diffusion_rows(0),
               "cell_cycle": lambda: cycle_rows(0)}[args.row]
         print(json.dumps({args.row: fn()}))
         return 0
@@ -638,8 +708,8 @@ def main():
         cpu = cpu_sample(wl)
 
     if not args.no_forms and world == 1:
-        extra["rows"] = {"grid_to_cell": field_rows(local, peak), "diffusion": diffusion_rows(local),
-                         "cell_cycle": cycle_rows(local)}
+        extra["rows"] = {"grid_to_cell": field_rows(local, peak), "cic_deposit": cic_rows(local, peak),
+                         "diffusion": diffusion_rows(local), "cell_cycle": cycle_rows(local)}
         forms = {"batched": batched_form(args, local)}
         forms["serving"] = [serving_form(args, local, float(r), args.serve_seconds)
                             for r in args.serve_rates.split(",") if r]
