@@ -171,6 +171,47 @@ __device__ __forceinline__ double add64(double a, double b) { return __dadd_rn(a
 __device__ __forceinline__ double sub64(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double div64(double a, double b) { return __ddiv_rn(a, b); }
 
+// x / r (r the grid's float resolution) with the rounding of an FP64
+// division.  When r is a power of two the quotient is x scaled by 2^-e,
+// exact for a normal result, and is made by moving x's exponent field
+// (integer work: this GPU's FP64 pipe is narrow); zero, subnormal or
+// non-finite x, a result leaving the normal range, or any other r take the
+// FP64 division.
+__device__ __forceinline__ double tm_div_res(double x, float r)
+{
+    const unsigned rb = __float_as_uint(r);
+    const unsigned ex = (rb >> 23) & 0xffu;
+    if ((rb & 0x807fffffu) == 0u && ex != 0u && ex != 0xffu) {
+        const int e = (int)ex - 127;                    // r = 2^e
+        const long long b = __double_as_longlong(x);
+        const int xe = (int)((b >> 52) & 0x7ff);
+        if (xe != 0 && xe != 0x7ff && xe - e > 0 && xe - e < 0x7ff) return __longlong_as_double(b - ((long long)e << 52));
+    }
+    return div64(x, (double)r);
+}
+
+// Adds w to grid[gi] for every lane with dep set.  Lanes in a row holding
+// the same node (a run; Morton-ordered cells give long ones) are summed by a
+// segmented scan, ceil(log2(longest run)) shuffle-and-add steps for the whole
+// warp, and the run's last lane issues one atomic.  No FP64 add is spent when
+// every run is one lane long.  All 32 lanes of the warp call it.
+__device__ __forceinline__ void tm_warp_deposit(double *grid, long long gi, double w, bool dep, int lane)
+{
+    const unsigned FULLM = 0xffffffffu;
+    if (!__any_sync(FULLM, dep)) return;
+    const long long prev = __shfl_up_sync(FULLM, gi, 1);
+    const unsigned heads = __ballot_sync(FULLM, lane == 0 || gi != prev);
+    const int span = lane - (31 - __clz(heads & (FULLM >> (31 - lane))));   // lanes before this one in its run
+    const int longest = __reduce_max_sync(FULLM, span);
+    double v = w;
+    for (int d = 1; d <= longest; d <<= 1) {
+        const double u = __shfl_up_sync(FULLM, v, d);
+        if (span >= d) v = add64(v, u);
+    }
+    const bool tail = lane == 31 || ((heads >> (lane + 1)) & 1u);
+    if (dep && tail) atomicAdd(grid + gi, v);
+}
+
 // (unsigned int)(((x - shift) / scale) * 2^29), octree.c:188-190
 __device__ inline uint32_t tm_lattice(double x, double shift, double scale)
 {

@@ -5,6 +5,9 @@
 #include "tm_arrays.cuh"
 #include "tm_kernels.cuh"
 
+#include <algorithm>
+#include <numeric>
+
 // uniform float in [0, 1] from a counter (stands in for (float)rand()/RAND_MAX)
 __device__ inline float tm_uniform(unsigned long long step, unsigned long long cell, int axis)
 {
@@ -77,13 +80,18 @@ __global__ void k_update(tm_arrays a, const tm_consts *K)
 
 // CIC weights onto field 0; the patch bounding box (patches.c:81-132) is
 // reduced alongside for the drop-in's patches_alloc.  Morton-ordered cells of
-// one warp mostly share grid nodes, so each distinct node of a corner gets a
-// warp-wide sum and one atomic.
-__global__ void k_cic(tm_arrays a, const tm_consts *K)
+// one warp mostly share grid nodes, so each distinct node of a corner gets
+// one atomic carrying the sum of the warp's weights on it.  Warps that run
+// together would hit the same few nodes (the same Morton neighbourhood) and
+// queue on them, so the g-th warp launched takes the 32 slots of warp
+// (g * stride) mod nwarps, stride coprime to nwarps: a bijection that puts
+// concurrently running warps far apart in the colony.
+__global__ void __launch_bounds__(256) k_cic(tm_arrays a, const tm_consts *K, long long nwarps, long long stride)
 {
     const unsigned FULLM = 0xffffffffu;
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (((i >> 5) << 5) >= a.nslots_total) return;            // whole warp beyond the slots
+    const long long g = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (g >= nwarps) return;                                   // whole warp beyond the slots
+    const long long i = ((g * stride) % nwarps) * 32 + (threadIdx.x & 31);
     const int c = a.col[(i >> 5) << 5];
     const tm_desc &d = a.desc[c];
     if (!d.active || d.gridoff < 0) return;                    // uniform per warp
@@ -95,12 +103,11 @@ __global__ void k_cic(tm_arrays a, const tm_consts *K)
     int ph = 5;
     if (live) {
         const double pos[3] = {a.x[i], a.y[i], a.z[i]};
-        const double res = (double)d.gres;
         for (int k = 0; k < 3; k++) {
-            ci[k] = (long long)div64(sub64(pos[k], d.glower[k]), res);
+            ci[k] = (long long)tm_div_res(sub64(pos[k], d.glower[k]), d.gres);
             // grid->lowercorner + cellIdx * resolution: an int64 * float product is a float
             const double cic = add64(d.glower[k], (double)__fmul_rn((float)ci[k], d.gres));
-            dd[k] = div64(sub64(pos[k], cic), res);
+            dd[k] = tm_div_res(sub64(pos[k], cic), d.gres);
             tt[k] = sub64(1.0, dd[k]);
         }
         ph = a.phase[i];
@@ -108,8 +115,13 @@ __global__ void k_cic(tm_arrays a, const tm_consts *K)
     const long long up[3] = {d.gsize[0] - 1, d.gsize[1] - 1, dim == 3 ? d.gsize[2] - 1 : 0};
     const double wph = ph == 0 ? 0.75 : 1.0;
     long long lo[3] = {0x7fffffffll, 0x7fffffffll, 0x7fffffffll}, hi[3] = {-0x7fffffffll - 1, -0x7fffffffll - 1, -0x7fffffffll - 1};
+    // the weight ((wphase * wx) * wy) * wz in the reference's order, its
+    // partial products shared between corners
+    const double wx0 = mul64(wph, tt[0]), wx1 = mul64(wph, dd[0]);
+    double wxy = 0.0;
     for (int corner = 0; corner < 8; corner++) {
         const int ax = corner >> 2, ay = (corner >> 1) & 1, az = corner & 1;
+        if (az == 0) wxy = mul64(ax ? wx1 : wx0, ay ? dd[1] : tt[1]);
         const long long gx = ci[0] + ax, gy = ci[1] + ay, gz = ci[2] + az;
         const bool inb = live && gx >= 0 && gy >= 0 && gz >= 0 && gx <= up[0] && gy <= up[1] && gz <= up[2];
         if (inb) {
@@ -121,18 +133,9 @@ __global__ void k_cic(tm_arrays a, const tm_consts *K)
             hi[2] = gz > hi[2] ? gz : hi[2];
         }
         const bool dep = inb && ph != 5;                       // necrotic cells deposit nothing
-        const double w = dep ? mul64(mul64(mul64(wph, ax ? dd[0] : tt[0]), ay ? dd[1] : tt[1]), az ? dd[2] : tt[2]) : 0.0;
+        const double w = dep ? mul64(wxy, az ? dd[2] : tt[2]) : 0.0;
         const long long gi = dep ? d.gridoff + ((long long)d.gsize[1] * gx + gy) * d.gsize[2] + gz : -1;
-        unsigned pending = __ballot_sync(FULLM, dep);
-        while (pending) {
-            const int ldr = __ffs(pending) - 1;
-            const long long key = __shfl_sync(FULLM, gi, ldr);
-            const bool mine = dep && gi == key;
-            double sum = mine ? w : 0.0;
-            for (int o = 16; o > 0; o >>= 1) sum = add64(sum, __shfl_xor_sync(FULLM, sum, o));
-            if (lane == ldr) atomicAdd(&a.grid[key], sum);
-            pending &= ~__ballot_sync(FULLM, mine);
-        }
+        tm_warp_deposit(a.grid, gi, w, dep, lane);
     }
     for (int k = 0; k < 3; k++) {
         for (int o = 16; o > 0; o >>= 1) {
@@ -144,9 +147,12 @@ __global__ void k_cic(tm_arrays a, const tm_consts *K)
     if (lane == 0 && hi[0] >= lo[0]) {
         tm_frame &f = a.frame[c];
         const int nd = dim == 3 ? 3 : 2;
+        // one address per corner for the whole colony: read it first and
+        // touch it only when this warp's box reaches past it (a stale read
+        // only costs an atomic; the corners move one way)
         for (int k = 0; k < nd; k++) {
-            atomicMin(&f.patch_lo[k], lo[k]);
-            atomicMax(&f.patch_hi[k], hi[k]);
+            if (lo[k] < __ldcg(&f.patch_lo[k])) atomicMin(&f.patch_lo[k], lo[k]);
+            if (hi[k] > __ldcg(&f.patch_hi[k])) atomicMax(&f.patch_hi[k], hi[k]);
         }
     }
 }
@@ -163,6 +169,9 @@ cudaError_t tm_launch_cic(const tm_arrays &a, const tm_consts *K, cudaStream_t s
 {
     unsigned grid = (unsigned)((a.nslots_total + 255) / 256);
     if (grid == 0) return cudaSuccess;
-    k_cic<<<grid, 256, 0, st>>>(a, K);
+    const long long nwarps = (a.nslots_total + 31) / 32;
+    long long stride = std::max(1ll, (long long)(0.6180339887 * (double)nwarps));
+    while (std::gcd(stride, nwarps) != 1) stride++;
+    k_cic<<<grid, 256, 0, st>>>(a, K, nwarps, stride);
     return cudaGetLastError();
 }

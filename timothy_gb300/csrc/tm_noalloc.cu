@@ -59,9 +59,9 @@ k_cic_noalloc(const double *x, const double *y, const double *z, const int *phas
     if (live) {
         const double pos[3] = {x[i], y[i], z[i]};
         for (int k = 0; k < 3; k++) {
-            ci[k] = (long long)div64(sub64(pos[k], lower[k]), (double)res);
+            ci[k] = (long long)tm_div_res(sub64(pos[k], lower[k]), res);
             const double cic = add64(lower[k], (double)__fmul_rn((float)ci[k], res));
-            dd[k] = div64(sub64(pos[k], cic), (double)res);
+            dd[k] = tm_div_res(sub64(pos[k], cic), res);
             tt[k] = sub64(1.0, dd[k]);
         }
         ph = phase[i];
@@ -70,8 +70,12 @@ k_cic_noalloc(const double *x, const double *y, const double *z, const int *phas
     const double wph = ph == 0 ? 0.75 : 1.0;
     long long lo[3] = {0x7fffffffll, 0x7fffffffll, 0x7fffffffll};
     long long hi[3] = {-0x7fffffffll - 1, -0x7fffffffll - 1, -0x7fffffffll - 1};
+    // ((wphase * wx) * wy) * wz in the reference's order, partial products shared
+    const double wx0 = mul64(wph, tt[0]), wx1 = mul64(wph, dd[0]);
+    double wxy = 0.0;
     for (int corner = 0; corner < 8; corner++) {
         const int ax = corner >> 2, ay = (corner >> 1) & 1, az = corner & 1;
+        if (az == 0) wxy = mul64(ax ? wx1 : wx0, ay ? dd[1] : tt[1]);
         const long long px = ci[0] + ax, py = ci[1] + ay, pz = ci[2] + az;
         const bool inb = live && px >= 0 && py >= 0 && pz >= 0 && px <= up[0] && py <= up[1] && pz <= up[2];
         if (inb) {
@@ -83,19 +87,9 @@ k_cic_noalloc(const double *x, const double *y, const double *z, const int *phas
             hi[2] = max(hi[2], pz);
         }
         const bool dep = inb && ph != 5;
-        const double wgt =
-            dep ? mul64(mul64(mul64(wph, ax ? dd[0] : tt[0]), ay ? dd[1] : tt[1]), az ? dd[2] : tt[2]) : 0.0;
+        const double wgt = dep ? mul64(wxy, az ? dd[2] : tt[2]) : 0.0;
         const long long gi = dep ? ((long long)gy * px + py) * gz + pz : -1;
-        unsigned pending = __ballot_sync(FULLM, dep);
-        while (pending) {
-            const int ldr = __ffs(pending) - 1;
-            const long long key = __shfl_sync(FULLM, gi, ldr);
-            const bool mine = dep && gi == key;
-            double sum = mine ? wgt : 0.0;
-            for (int o = 16; o > 0; o >>= 1) sum = add64(sum, __shfl_xor_sync(FULLM, sum, o));
-            if (lane == ldr) atomicAdd(&grid[key], sum);
-            pending &= ~__ballot_sync(FULLM, mine);
-        }
+        tm_warp_deposit(grid, gi, wgt, dep, lane);
     }
     for (int k = 0; k < 3; k++) {
         for (int o = 16; o > 0; o >>= 1) {
