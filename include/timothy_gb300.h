@@ -219,16 +219,18 @@ int tm_colony_cellcycle(tm_session *s, int id, const tm_cycle_params *p, int64_t
  * reported as TM_DEVERR_TYPES by the next tm_session_sync.  Both return once
  * the work is queued: the caller leaves in's arrays unchanged, and reads
  * out's arrays only, after tm_session_sync.  They stage through device
- * buffers of their own, 44 and 104 bytes per slot, allocated on first use
+ * buffers of their own, 44 and 112 bytes per slot, allocated on first use
  * (not counted by tm_session_bytes). */
 int tm_colony_upload_async(tm_session *s, int id, const tm_colony_input *in);
 int tm_colony_download_async(tm_session *s, int id, const tm_colony_output *out);
 /* Replace the cells of an existing colony (at most the slots it holds).  With
  * the same n the cells are taken as the same cells in the same order as the
  * colony's input: they keep their slots, and neighbour lists stay valid unless
- * a cell moved too far, changed size or changed type.  Cell types are checked
- * on the device; one outside the table returns TM_EDEVICE and leaves the
- * colony empty. */
+ * a cell moved too far, changed size or changed type.  Such uploads (and
+ * tm_colony_upload_async) reorder the cells through a record buffer of 48
+ * bytes per slot, allocated on first use (not counted by tm_session_bytes).
+ * Cell types are checked on the device; one outside the table returns
+ * TM_EDEVICE and leaves the colony empty. */
 int tm_colony_upload(tm_session *s, int id, const tm_colony_input *in);
 int tm_colony_set_active(tm_session *s, int id, int active);
 int tm_colony_download(tm_session *s, int id, const tm_colony_output *out);

@@ -137,9 +137,11 @@ __global__ void __launch_bounds__(256) k_bbox(tm_arrays a, int ntypes)
             const unsigned long long o = red[u][tt][q];
             best = q < 3 ? (o < best ? o : best) : (o > best ? o : best);
         }
+        // the box only widens during the pass: post only what reaches past its current value
         if (q < 3 ? best != 0xffffffffffffffffull : best != 0ull) {
-            if (q < 3) atomicMin(&a.frame[cc].bbox[tt][q], best);
-            else atomicMax(&a.frame[cc].bbox[tt][q], best);
+            unsigned long long *t = &a.frame[cc].bbox[tt][q];
+            if (q < 3 && best < __ldcg(t)) atomicMin(t, best);
+            else if (q >= 3 && best > __ldcg(t)) atomicMax(t, best);
         }
     }
 }

@@ -74,7 +74,8 @@ __global__ void k_update(tm_arrays a, const tm_consts *K)
         const float ex = hx - o.x, ey = hy - o.y, ez = hz - o.z;
         const unsigned bits = __float_as_uint(sqrtf(fmaf(ex, ex, fmaf(ey, ey, ez * ez))));
         const unsigned m = __reduce_max_sync(__activemask(), bits);
-        if (bits == m) atomicMax(&a.frame[c].maxdisp, m);
+        // one word per colony: only warps past its current value post (it only grows)
+        if (bits == m && m > __ldcg(&a.frame[c].maxdisp)) atomicMax(&a.frame[c].maxdisp, m);
     }
 }
 

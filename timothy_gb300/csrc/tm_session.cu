@@ -134,9 +134,10 @@ struct tm_session {
     cudaEvent_t ev_h2d = nullptr;
     // asynchronous I/O: own staging, so copies overlap the steps
     unsigned char *up_stage = nullptr;    // x, y, z, size (8 B), young, ctype, phase (4 B) per slot
-    unsigned char *dl_stage = nullptr;    // the downloaded fields, 8 B per slot each
-    size_t up_bytes = 0, dl_bytes = 0;
-    cudaEvent_t ev_up_read = nullptr;     // k_upload_keep has read up_stage
+    unsigned char *dl_stage = nullptr;    // the downloaded fields, 8 B per slot each, and the inverse permutation
+    unsigned char *up_rec = nullptr;      // an upload's cells as 48-byte records (caller order)
+    size_t up_bytes = 0, dl_bytes = 0, rec_bytes = 0;
+    cudaEvent_t ev_up_read = nullptr;     // k_upload_pack has read up_stage
     cudaEvent_t ev_dl_gathered = nullptr, ev_dl_copied = nullptr;
     bool dl_pending = false, up_pending = false;
     cudaEvent_t ev_ready[2] = {nullptr, nullptr}, ev_copied[2] = {nullptr, nullptr};
@@ -214,15 +215,54 @@ struct upload_src {
     long long base;
 };
 
+// One cell of an upload, 16-byte aligned.  The slots hold the cells in Morton
+// order and the caller's arrays in caller order, so putting the cells in
+// their slots reads them at random: from seven separate arrays that costs
+// seven DRAM bursts per cell, from one record one or two.  k_upload_pack
+// writes the records from the staged arrays (both sides in caller order,
+// coalesced) and k_upload_keep reads one record per slot.
+union up_rec {
+    struct {
+        double x, y, z, size;
+        float young;
+        int ctype, phase, pad;
+    } f;
+    int4 v[3];
+};
+
+__global__ void k_upload_pack(upload_src u, int n, int has_phase, int4 *rec)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const long long src = u.base + k;
+    up_rec r;
+    r.f.x = u.x[src];
+    r.f.y = u.y[src];
+    r.f.z = u.z[src];
+    r.f.size = u.size[src];
+    r.f.young = u.young[src];
+    r.f.ctype = u.ctype[src];
+    r.f.phase = has_phase ? u.phase[src] : 0;
+    r.f.pad = 0;
+    int4 *d = rec + src * 3;
+    d[0] = r.v[0];
+    d[1] = r.v[1];
+    d[2] = r.v[2];
+}
+
 __global__ void k_upload_keep(tm_arrays a, const tm_consts *K, int c, long long off, int n, int has_phase,
-                              int *bad, upload_src u)
+                              int *bad, const int4 *rec, long long base)
 {
     const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const long long s = off + k;
-    const long long src = u.base + a.perm[s];
-    const double x = u.x[src], y = u.y[src], z = u.z[src], sz = u.size[src];
-    int ct = u.ctype[src];
+    const int4 *p = rec + (base + a.perm[s]) * 3;
+    up_rec r;
+    r.v[0] = p[0];
+    r.v[1] = p[1];
+    r.v[2] = p[2];
+    const double x = r.f.x, y = r.f.y, z = r.f.z, sz = r.f.size;
+    int ct = r.f.ctype;
     if (ct < 0 || ct >= K->ntypes) {
         if (bad) atomicExch(bad, 1);
         else atomicOr(&a.frame[c].error, TM_ERR_TYPES);
@@ -233,9 +273,9 @@ __global__ void k_upload_keep(tm_arrays a, const tm_consts *K, int c, long long 
     a.y[s] = y;
     a.z[s] = z;
     a.size[s] = sz;
-    a.young[s] = u.young[src];
+    a.young[s] = r.f.young;
     a.ctype[s] = ct;
-    if (has_phase) a.phase[s] = u.phase[src];
+    if (has_phase) a.phase[s] = r.f.phase;
     a.rem[s] = 0;
     if (a.desc[c].verlet && a.x0) {
         float hx, hy, hz, lx, ly, lz;
@@ -246,7 +286,8 @@ __global__ void k_upload_keep(tm_arrays a, const tm_consts *K, int c, long long 
         const float ex = hx - o.x, ey = hy - o.y, ez = hz - o.z;
         const unsigned bits = __float_as_uint(sqrtf(fmaf(ex, ex, fmaf(ey, ey, ez * ez))));
         const unsigned m = __reduce_max_sync(__activemask(), bits);
-        if (bits == m) atomicMax(&a.frame[c].maxdisp, m);
+        // one word per colony: only warps past its current value post (it only grows)
+        if (bits == m && m > __ldcg(&a.frame[c].maxdisp)) atomicMax(&a.frame[c].maxdisp, m);
     }
 }
 
@@ -274,6 +315,27 @@ __global__ void k_unsort(const T *src, const int *perm, long long off, int n, T 
     long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     dst[perm[off + k]] = src[off + k];
+}
+
+// Download gathers: the inverse of the slot permutation (iperm[perm[off + s]]
+// = s), then one pass per field that reads the field at random and writes it
+// in caller order (coalesced).  Measured at 16 M cells: 0.17 ms per 8-byte
+// field; scattering the writes instead took 0.3 ms, and packing the fields
+// into 16-byte-aligned records to gather whole records took 2.2 ms for the
+// ten fields against 1.7 ms.
+__global__ void k_invert_perm(const int *perm, long long off, int n, int *iperm)
+{
+    long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    iperm[perm[off + s]] = (int)s;
+}
+
+template <typename T>
+__global__ void k_unsort_gather(const T *src, const int *iperm, long long off, int n, T *dst)
+{
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    dst[k] = src[off + iperm[k]];
 }
 
 static unsigned blocks_for(long long n, int bt) { return (unsigned)std::max(1ll, (n + bt - 1) / bt); }
@@ -683,6 +745,7 @@ extern "C" int tm_session_destroy(tm_session *s)
         if (e) cudaEventDestroy(e);
     if (s->up_stage) cudaFree(s->up_stage);
     if (s->dl_stage) cudaFree(s->dl_stage);
+    if (s->up_rec) cudaFree(s->up_rec);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return TM_OK;
@@ -717,6 +780,22 @@ static int grid_geometry(int dim, float gfh, int gsize[3], double lower[3])
 // rebuilt.  Returns TM_EINVAL if a cell type lies outside the table.
 static int download_streams(tm_session *s);
 
+// the record buffer of uploads into kept slots (48 B per slot, allocated on first use)
+static int upload_records(tm_session *s, int4 **rec)
+{
+    const size_t need = ((size_t)s->slots.hwm * 32 + 32) * sizeof(up_rec);
+    if (s->rec_bytes < need) {
+        CK(cudaStreamSynchronize(s->stream));
+        if (s->up_rec) CK(cudaFree(s->up_rec));
+        s->up_rec = nullptr;
+        s->rec_bytes = 0;
+        CK(cudaMalloc((void **)&s->up_rec, need));
+        s->rec_bytes = need;
+    }
+    *rec = (int4 *)s->up_rec;
+    return TM_OK;
+}
+
 static int copy_cells_in(tm_session *s, const colony_host &c, const tm_colony_input *in, bool keep)
 {
     const tm_arrays a = view(s, s->parity);
@@ -747,8 +826,12 @@ static int copy_cells_in(tm_session *s, const colony_host &c, const tm_colony_in
     }
     if (keep) {
         const upload_src u = {a.x2, a.y2, a.z2, a.size2, a.young2, a.ctype2, a.phase2, o};
+        int4 *rec = nullptr;
+        int rc = upload_records(s, &rec);
+        if (rc) return rc;
+        k_upload_pack<<<blocks_for((long long)n, 256), 256, 0, st>>>(u, (int)n, in->phase ? 1 : 0, rec);
         k_upload_keep<<<blocks_for((long long)n, 256), 256, 0, st>>>(a, s->dK, cid, o, (int)n, in->phase ? 1 : 0,
-                                                                    s->d_flag, u);
+                                                                    s->d_flag, rec, o);
     } else {
         k_check_types<<<blocks_for((long long)n, 256), 256, 0, st>>>(a, s->dK, o, (int)n, s->d_flag);
         k_colony_init<<<blocks_for(c.nslots, 256), 256, 0, st>>>(a, cid, o, (int)n, c.nslots, in->phase ? 1 : 0);
@@ -1006,10 +1089,14 @@ extern "C" int tm_colony_upload_async(tm_session *s, int id, const tm_colony_inp
     CK(cudaStreamWaitEvent(s->stream, s->ev_h2d, 0));
     const tm_arrays a = view(s, s->parity);
     const upload_src u = {X, Y, Z, SZ, YG, CT, PH, o};
-    k_upload_keep<<<blocks_for((long long)n, 256), 256, 0, s->stream>>>(a, s->dK, id, o, (int)n, in->phase ? 1 : 0,
-                                                                      nullptr, u);
+    int4 *rec = nullptr;
+    if ((rc = upload_records(s, &rec))) return rc;
+    k_upload_pack<<<blocks_for((long long)n, 256), 256, 0, s->stream>>>(u, (int)n, in->phase ? 1 : 0, rec);
     CK(cudaGetLastError());
-    CK(cudaEventRecord(s->ev_up_read, s->stream));
+    CK(cudaEventRecord(s->ev_up_read, s->stream));   // the staging is free for the next upload's copies
+    k_upload_keep<<<blocks_for((long long)n, 256), 256, 0, s->stream>>>(a, s->dK, id, o, (int)n, in->phase ? 1 : 0,
+                                                                      nullptr, rec, o);
+    CK(cudaGetLastError());
     s->up_pending = true;
     return TM_OK;
 }
@@ -1264,24 +1351,13 @@ extern "C" int tm_colony_download_async(tm_session *s, int id, const tm_colony_o
     return download_queue(s, id, out, false);
 }
 
-// Asynchronous download: every requested field is gathered into its own part
-// of the download staging (8 B per slot per field, allocated on first use) on
-// the session stream, then copied to the host on the copy stream, so the
-// copies overlap the steps that follow; the next asynchronous download's
-// gathers wait for these copies.
-template <typename T>
-static int gather_async(tm_session *s, const T *src, const colony_host &c, T *host, size_t S, int &slot,
-                        std::vector<std::pair<void *, std::pair<const void *, size_t>>> &copies)
-{
-    if (!host || c.n == 0) return TM_OK;
-    T *dst = (T *)(s->dl_stage + (size_t)slot * S * 8);
-    slot++;
-    const tm_arrays a = view(s, s->parity);
-    k_unsort<T><<<blocks_for(c.n, 256), 256, 0, s->stream>>>(src, a.perm, c.off, c.n, dst);
-    CK(cudaGetLastError());
-    copies.push_back({(void *)host, {(const void *)dst, sizeof(T) * (size_t)c.n}});
-    return TM_OK;
-}
+// Asynchronous download: each requested field is gathered into its own part
+// of the download staging (8 B per slot per field, allocated on first use,
+// the inverse permutation in the last part) on the session stream, then
+// copied to the host on the copy stream, so the copies overlap the steps that
+// follow; the next asynchronous download waits for these copies before it
+// touches the staging.
+#define DL_MAX_FIELDS 13
 
 static int download_async_queue(tm_session *s, int id, const tm_colony_output *out)
 {
@@ -1289,7 +1365,7 @@ static int download_async_queue(tm_session *s, int id, const tm_colony_output *o
     if (rc) return rc;
     const colony_host &c = s->cols[id];
     const tm_arrays a = view(s, s->parity);
-    const size_t S = (size_t)s->slots.hwm * 32 + 32, need = S * 8 * 13;
+    const size_t S = (size_t)s->slots.hwm * 32 + 32, need = S * 8 * (DL_MAX_FIELDS + 1);
     if (s->dl_bytes < need) {
         CK(cudaStreamSynchronize(s->copy_stream));
         CK(cudaStreamSynchronize(s->stream));
@@ -1301,24 +1377,38 @@ static int download_async_queue(tm_session *s, int id, const tm_colony_output *o
         s->dl_pending = false;
     }
     if (s->dl_pending) CK(cudaStreamWaitEvent(s->stream, s->ev_dl_copied, 0));
+    struct want { const void *src; void *host; int size; };
+    const want all[DL_MAX_FIELDS] = {
+        {a.x, out->x, 8}, {a.y, out->y, 8}, {a.z, out->z, 8}, {a.density, out->density, 8}, {a.v, out->v, 8},
+        {a.mindist, out->mindist, 8}, {a.fx, out->fx, 8}, {a.fy, out->fy, 8}, {a.fz, out->fz, 8},
+        {a.rem, out->removecell, 1}, {a.nbcount, out->nbcount, 4},
+        {a.nbhash, a.nbhash ? (void *)out->nbhash : nullptr, 8}, {a.vcand, a.vcand ? (void *)out->vcand : nullptr, 4}};
     std::vector<std::pair<void *, std::pair<const void *, size_t>>> copies;
-    int slot = 0;
-    if ((rc = gather_async(s, (const double *)a.x, c, out->x, S, slot, copies))) return rc;
-    if ((rc = gather_async(s, (const double *)a.y, c, out->y, S, slot, copies))) return rc;
-    if ((rc = gather_async(s, (const double *)a.z, c, out->z, S, slot, copies))) return rc;
-    if ((rc = gather_async(s, (const double *)a.density, c, out->density, S, slot, copies))) return rc;
-    if ((rc = gather_async(s, (const double *)a.v, c, out->v, S, slot, copies))) return rc;
-    if ((rc = gather_async(s, (const double *)a.mindist, c, out->mindist, S, slot, copies))) return rc;
-    if ((rc = gather_async(s, (const double *)a.fx, c, out->fx, S, slot, copies))) return rc;
-    if ((rc = gather_async(s, (const double *)a.fy, c, out->fy, S, slot, copies))) return rc;
-    if ((rc = gather_async(s, (const double *)a.fz, c, out->fz, S, slot, copies))) return rc;
-    if ((rc = gather_async(s, (const unsigned char *)a.rem, c, out->removecell, S, slot, copies))) return rc;
-    if ((rc = gather_async(s, (const int32_t *)a.nbcount, c, out->nbcount, S, slot, copies))) return rc;
-    if (a.nbhash &&
-        (rc = gather_async(s, (const unsigned long long *)a.nbhash, c, (unsigned long long *)out->nbhash, S, slot,
-                           copies)))
-        return rc;
-    if (a.vcand && (rc = gather_async(s, (const int32_t *)a.vcand, c, out->vcand, S, slot, copies))) return rc;
+    if (c.n > 0) {
+        int *iperm = (int *)(s->dl_stage + (size_t)DL_MAX_FIELDS * S * 8);
+        bool inverted = false;
+        int part = 0;
+        for (const want &w : all) {
+            if (!w.host) continue;
+            if (!inverted) {
+                k_invert_perm<<<blocks_for(c.n, 256), 256, 0, s->stream>>>(a.perm, c.off, c.n, iperm);
+                inverted = true;
+            }
+            unsigned char *dst = s->dl_stage + (size_t)part++ * S * 8;
+            const unsigned g = blocks_for(c.n, 256);
+            if (w.size == 8)
+                k_unsort_gather<unsigned long long><<<g, 256, 0, s->stream>>>(
+                    (const unsigned long long *)w.src, iperm, c.off, c.n, (unsigned long long *)dst);
+            else if (w.size == 4)
+                k_unsort_gather<unsigned><<<g, 256, 0, s->stream>>>((const unsigned *)w.src, iperm, c.off, c.n,
+                                                                   (unsigned *)dst);
+            else
+                k_unsort_gather<unsigned char><<<g, 256, 0, s->stream>>>((const unsigned char *)w.src, iperm, c.off,
+                                                                        c.n, dst);
+            copies.push_back({w.host, {(const void *)dst, (size_t)w.size * (size_t)c.n}});
+        }
+        CK(cudaGetLastError());
+    }
     CK(cudaEventRecord(s->ev_dl_gathered, s->stream));
     CK(cudaStreamWaitEvent(s->copy_stream, s->ev_dl_gathered, 0));
     for (auto &cp : copies)
