@@ -649,7 +649,9 @@ def main():
         for a in pinned:
             S.host_register(a)
         ecol = C.Colony(*host, col.types, 3)
-        ke = max(2, min(args.steps, 10))
+        # 30 steps: the first upload and the last download, which nothing
+        # overlaps, are spread over enough steps to show the loop's rate
+        ke = max(2, min(args.steps, 30))
         s.upload(cid, ecol)
         s.step(1)
         s.sync()
