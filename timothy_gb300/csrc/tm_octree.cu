@@ -101,52 +101,74 @@ __device__ __forceinline__ float dist2_split(const tm_arrays &a, long long p, lo
     return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
 }
 
-// the walk of one cell p (octlocateregion + the DFS of computepotential)
-__device__ __noinline__ void octree_walk(const tm_arrays &a, const tm_consts *K, long long p)
+// The walk of one cell p (octlocateregion + the DFS of computepotential),
+// split into a start, single DFS steps and an end.  The kernel runs it as a
+// loop in which a lane whose walk is over takes its next queued cell while
+// the other lanes of the warp keep walking: walks differ in length by a wide
+// margin, and a warp that waited for its longest one kept a third of its
+// lanes busy on average.
+struct walk_state {
+    long long p, ps, mpos, jstar;   // the cell, its Morton position, m's position, j*
+    double mind;                    // mindist of an isolated cell
+    uint32_t bmin[3], bmax[3];      // query box, half-open
+    uint32_t base;                  // the colony's first Morton position
+    int L, c, sp;                   // bin depth, colony, stack depth
+    bool isolated, ident, fp64;
+    const uint32_t *bst;            // the colony's bin starts
+};
+
+// octlocateregion and the first stack frame; false when there is nothing to
+// walk (fewer than two cells in the start node)
+__device__ __forceinline__ bool walk_begin(const tm_arrays &a, const tm_consts *K, long long p, walk_state &w,
+                                           walk_frame *stk)
 {
     const int c = a.col[p];
     const tm_desc &d = a.desc[c];
     const tm_frame &f = a.frame[c];
     const tm_type &T = K->t[a.ctype[p]];
-    const double xp = a.x[p], yp = a.y[p], zp = a.z[p];
-    const bool isolated = a.nbcount[p] == 0;
-    const bool ident = f.ident != 0;
-    const long long ps = ident ? p : (long long)a.rank[p];   // p's Morton position
-    auto slot_of = [&](long long k) -> long long { return ident ? k : (long long)a.tmp[k]; };
+    w.p = p;
+    w.c = c;
+    w.isolated = a.nbcount[p] == 0;
+    w.ident = f.ident != 0;
+    w.fp64 = d.precision == 0;
+    w.ps = w.ident ? p : (long long)a.rank[p];
+    w.jstar = -1;
+    w.mind = 1.7976931348623157e308;
+    w.mpos = -1;
+    w.sp = 0;
 
     // query box in lattice codes, octree.c:251-263; half-open [bmin, bmax)
-    uint32_t bmin[3], bmax[3];
     {
-        const double pos[3] = {xp, yp, zp};
+        const double pos[3] = {a.x[p], a.y[p], a.z[p]};
         unsigned slow = 0;
         for (int k = 0; k < 3; k++) {
             long long P;
             const bool ok = tm_fix47(pos[k], P) && T.h < 8192.0;
-            bmin[k] = tm_lattice_fast(pos[k], P, ok, -T.h_fx, -T.h, f, k, slow);
-            bmax[k] = tm_lattice_fast(pos[k], P, ok, T.h_fx, T.h, f, k, slow);
+            w.bmin[k] = tm_lattice_fast(pos[k], P, ok, -T.h_fx, -T.h, f, k, slow);
+            w.bmax[k] = tm_lattice_fast(pos[k], P, ok, T.h_fx, T.h, f, k, slow);
         }
         if (slow) atomicAdd(&a.frame[c].codes_slow, (unsigned long long)slow);
     }
 
     // octlocateregion: the highest differing bit over the three axes
-    uint32_t diff = (bmin[0] ^ bmax[0]) | (bmin[1] ^ bmax[1]) | (bmin[2] ^ bmax[2]);
+    const uint32_t diff = (w.bmin[0] ^ w.bmax[0]) | (w.bmin[1] ^ w.bmax[1]) | (w.bmin[2] ^ w.bmax[2]);
     int lm = diff ? 31 - __clz(diff) : 0;
     lm++;
     const int dT = TM_ROOT_LEVEL - lm;       // depth of the start node
-    const uint4 mcode = make_uint4(bmin[0], bmin[1], bmin[2], 0);
+    const uint4 mcode = make_uint4(w.bmin[0], w.bmin[1], w.bmin[2], 0);
     const uint4 *codes = a.codes;
-    const uint32_t *bst = a.bin_start + d.binoff;
-    const uint32_t base = (uint32_t)f.bin_base;   // slots fit in 32 bits; wraps consistently
-    const int L = f.L;
+    w.bst = a.bin_start + d.binoff;
+    w.base = (uint32_t)f.bin_base;   // slots fit in 32 bits; wraps consistently
+    w.L = f.L;
     uint32_t a0, a1;
-    if (dT <= L) {
+    if (dT <= w.L) {
         const uint32_t P = tm_prefix(mcode, dT);
-        const int sh = 3 * (L - dT);
-        a0 = base + bst[P << sh];
-        a1 = base + bst[(P + 1) << sh];
+        const int sh = 3 * (w.L - dT);
+        a0 = w.base + w.bst[P << sh];
+        a1 = w.base + w.bst[(P + 1) << sh];
     } else {
-        const uint32_t b = tm_prefix(mcode, L);
-        const uint32_t lo = base + bst[b], hi = base + bst[b + 1];
+        const uint32_t b = tm_prefix(mcode, w.L);
+        const uint32_t lo = w.base + w.bst[b], hi = w.base + w.bst[b + 1];
         a0 = prefix_lower_bound(codes, lo, hi, mcode, dT);
         a1 = run_end(codes, a0, hi, mcode, dT);
         if (a0 < hi) {
@@ -161,8 +183,7 @@ __device__ __noinline__ void octree_walk(const tm_arrays &a, const tm_consts *K,
     // The walk visits candidates in Morton order, and the first within-h
     // neighbour m is itself a candidate when its leaf meets the box; then no
     // candidate after position m can be j*, and the walk stops on reaching it.
-    long long mpos = -1;
-    if (!isolated) {
+    if (!w.isolated) {
         const long long m = a.nbmin[p];
         if (m >= (long long)a0 && m < (long long)a1) {
             const uint4 cm = codes[m];
@@ -172,85 +193,89 @@ __device__ __noinline__ void octree_walk(const tm_arrays &a, const tm_consts *K,
             const int s = TM_ROOT_LEVEL - dl;
             const uint32_t len = 1u << s;
             const uint32_t lx = (cm.x >> s) << s, ly = (cm.y >> s) << s, lz = (cm.z >> s) << s;
-            const bool meets = !(bmax[0] <= lx || bmin[0] >= lx + len || bmax[1] <= ly || bmin[1] >= ly + len ||
-                                 bmax[2] <= lz || bmin[2] >= lz + len);
-            if (meets && dl > dT && m != ps) mpos = m;
+            const bool meets = !(w.bmax[0] <= lx || w.bmin[0] >= lx + len || w.bmax[1] <= ly ||
+                                 w.bmin[1] >= ly + len || w.bmax[2] <= lz || w.bmin[2] >= lz + len);
+            if (meets && dl > dT && m != w.ps) w.mpos = m;
         }
     }
-
-    long long jstar = -1;
-    double mind = 1.7976931348623157e308;
     if (a1 > a0 && a1 - a0 >= 2) {
-        walk_frame stk[WALK_STACK];
-        int sp = 0;
-        stk[sp++] = {a1, a0, dT};
-        bool done = false;
-        while (sp > 0 && !done) {
-            walk_frame &top = stk[sp - 1];
-            if (top.cur >= top.end) {
-                sp--;
-                continue;
-            }
-            const uint32_t k = top.cur;
-            if (mpos >= 0 && (long long)k >= mpos) {
-                jstar = mpos;                   // every later candidate follows m
-                done = true;
-                continue;
-            }
-            const uint4 ck = codes[k];
-            const int dc = top.depth + 1;
-            uint32_t e;
-            if (dc <= L) {
-                const uint32_t P = tm_prefix(ck, dc);
-                e = base + bst[(P + 1) << (3 * (L - dc))];
-                if (e > top.end) e = top.end;
-            } else {
-                e = run_end(codes, k + 1, top.end, ck, dc);
-            }
-            if (e <= k) {                       // inconsistent bins: never loop in place
-                atomicOr(&a.frame[c].error, TM_ERR_STACK);
-                e = k + 1;
-            }
-            top.cur = e;
-            // child node box, tested as octnodeintersection does
-            const int s = TM_ROOT_LEVEL - dc;
-            const uint32_t lx = (ck.x >> s) << s, ly = (ck.y >> s) << s, lz = (ck.z >> s) << s;
-            const uint32_t len = 1u << s;
-            if (bmax[0] <= lx || bmin[0] >= lx + len) continue;
-            if (bmax[1] <= ly || bmin[1] >= ly + len) continue;
-            if (bmax[2] <= lz || bmin[2] >= lz + len) continue;
-            if (e - k == 1) {
-                if ((long long)k == ps) continue;
-                if (jstar < 0) jstar = k;
-                if (!isolated) {
-                    done = true;
-                } else {
-                    const long long sk = slot_of(k);
-                    double dist;
-                    if (d.precision == 0) {
-                        const double dx = sub64(xp, a.x[sk]), dy = sub64(yp, a.y[sk]), dz = sub64(zp, a.z[sk]);
-                        dist = __dsqrt_rn(add64(add64(mul64(dx, dx), mul64(dy, dy)), mul64(dz, dz)));
-                    } else {
-                        dist = (double)sqrtf(dist2_split(a, p, sk));   // FP32 path: no FP64 work
-                    }
-                    mind = (dist < mind ? dist : mind);
-                }
-                continue;
-            }
-            if (sp == WALK_STACK) {
-                atomicOr(&a.frame[c].error, TM_ERR_STACK);
-                done = true;
-                continue;
-            }
-            stk[sp++] = {e, k, dc};
-        }
+        stk[0] = {a1, a0, dT};
+        w.sp = 1;
+        return true;
     }
+    return false;
+}
 
+// one DFS step (the child pop order of computepotential); true when the walk is over
+__device__ __forceinline__ bool walk_step(const tm_arrays &a, walk_state &w, walk_frame *stk)
+{
+    walk_frame &top = stk[w.sp - 1];
+    if (top.cur >= top.end) {
+        w.sp--;
+        return w.sp == 0;
+    }
+    const uint32_t k = top.cur;
+    if (w.mpos >= 0 && (long long)k >= w.mpos) {
+        w.jstar = w.mpos;                   // every later candidate follows m
+        return true;
+    }
+    const uint4 *codes = a.codes;
+    const uint4 ck = codes[k];
+    const int dc = top.depth + 1;
+    uint32_t e;
+    if (dc <= w.L) {
+        const uint32_t P = tm_prefix(ck, dc);
+        e = w.base + w.bst[(P + 1) << (3 * (w.L - dc))];
+        if (e > top.end) e = top.end;
+    } else {
+        e = run_end(codes, k + 1, top.end, ck, dc);
+    }
+    if (e <= k) {                           // inconsistent bins: never loop in place
+        atomicOr(&a.frame[w.c].error, TM_ERR_STACK);
+        e = k + 1;
+    }
+    top.cur = e;
+    // child node box, tested as octnodeintersection does
+    const int s = TM_ROOT_LEVEL - dc;
+    const uint32_t lx = (ck.x >> s) << s, ly = (ck.y >> s) << s, lz = (ck.z >> s) << s;
+    const uint32_t len = 1u << s;
+    if (w.bmax[0] <= lx || w.bmin[0] >= lx + len) return false;
+    if (w.bmax[1] <= ly || w.bmin[1] >= ly + len) return false;
+    if (w.bmax[2] <= lz || w.bmin[2] >= lz + len) return false;
+    if (e - k == 1) {
+        if ((long long)k == w.ps) return false;
+        if (w.jstar < 0) w.jstar = k;
+        if (!w.isolated) return true;
+        const long long sk = w.ident ? (long long)k : (long long)a.tmp[k];
+        double dist;
+        if (w.fp64) {
+            const double dx = sub64(a.x[w.p], a.x[sk]), dy = sub64(a.y[w.p], a.y[sk]), dz = sub64(a.z[w.p], a.z[sk]);
+            dist = __dsqrt_rn(add64(add64(mul64(dx, dx), mul64(dy, dy)), mul64(dz, dz)));
+        } else {
+            dist = (double)sqrtf(dist2_split(a, w.p, sk));   // FP32 path: no FP64 work
+        }
+        w.mind = (dist < w.mind ? dist : w.mind);
+        return false;
+    }
+    if (w.sp == WALK_STACK) {
+        atomicOr(&a.frame[w.c].error, TM_ERR_STACK);
+        return true;
+    }
+    stk[w.sp++] = {e, k, dc};
+    return false;
+}
+
+// v from j*, mindist of an isolated cell, the diagnostics' candidate
+__device__ __forceinline__ void walk_end(const tm_arrays &a, const tm_consts *K, const walk_state &w)
+{
+    const long long p = w.p;
+    long long jstar = w.jstar;
+    if (jstar >= 0 && !w.ident) jstar = (long long)a.tmp[jstar];
     double vv = 0.0;
-    if (jstar >= 0) jstar = slot_of(jstar);
     if (jstar >= 0) {
-        if (d.precision == 0) {
-            vv = pair_potential64(xp, yp, zp, a.size[p], a.young[p], a.x[jstar], a.y[jstar], a.z[jstar],
+        const tm_type &T = K->t[a.ctype[p]];
+        if (w.fp64) {
+            vv = pair_potential64(a.x[p], a.y[p], a.z[p], a.size[p], a.young[p], a.x[jstar], a.y[jstar], a.z[jstar],
                                   a.size[jstar], a.young[jstar], T.h);
         } else {
             // distance from the split positions; the cutoff in FP64 only within
@@ -258,7 +283,8 @@ __device__ __noinline__ void octree_walk(const tm_arrays &a, const tm_consts *K,
             const float dist = sqrtf(dist2_split(a, p, jstar));
             bool in = dist <= T.hf;
             if (fabsf(dist - T.hf) <= 1.0e-5f * T.hf) {
-                const double dx = sub64(xp, a.x[jstar]), dy = sub64(yp, a.y[jstar]), dz = sub64(zp, a.z[jstar]);
+                const double dx = sub64(a.x[p], a.x[jstar]), dy = sub64(a.y[p], a.y[jstar]),
+                             dz = sub64(a.z[p], a.z[jstar]);
                 in = __dsqrt_rn(add64(add64(mul64(dx, dx), mul64(dy, dy)), mul64(dz, dz))) <= T.h;
             }
             if (in)
@@ -267,7 +293,7 @@ __device__ __noinline__ void octree_walk(const tm_arrays &a, const tm_consts *K,
         }
     }
     a.v[p] = vv;
-    if (isolated) a.mindist[p] = mind;
+    if (w.isolated) a.mindist[p] = w.mind;
     if (a.want_diag) a.vcand[p] = jstar >= 0 ? a.perm[jstar] : -1;
 }
 
@@ -304,14 +330,34 @@ __global__ void __launch_bounds__(256) k_octree_mark(tm_arrays a)
     tm_queue_walk(a, p, isolated, walk);
 }
 
-// Pass 2: the walk of every queued cell (grid-stride over both queues)
-__global__ void __launch_bounds__(256) k_octree(tm_arrays a, const tm_consts *K)
+// Pass 2: the walk of every queued cell (grid-stride over both queues).  Each
+// lane runs its own sequence of walks: in one iteration it either takes one
+// step of its current walk or starts its next cell, so the warp's lanes stay
+// busy until their sequences run out.
+__global__ void __launch_bounds__(256, 4) k_octree(tm_arrays a, const tm_consts *K)
 {
     const int nf = a.work[2], nq = nf + a.work[3];
-    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nq;
-         q += (long long)gridDim.x * blockDim.x) {
-        const long long p = q < nf ? a.walk_list[q] : a.walk_list[a.nslots_total - 1 - (q - nf)];
-        octree_walk(a, K, p);
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    walk_state w;
+    walk_frame stk[WALK_STACK];   // the DFS stack (local memory)
+    bool busy = false;
+    for (;;) {
+        bool over;
+        if (busy) {
+            over = walk_step(a, w, stk);
+        } else if (q < nq) {
+            const long long p = q < nf ? a.walk_list[q] : a.walk_list[a.nslots_total - 1 - (q - nf)];
+            q += stride;
+            busy = walk_begin(a, K, p, w, stk);
+            over = !busy;
+        } else {
+            break;
+        }
+        if (over) {
+            walk_end(a, K, w);
+            busy = false;
+        }
     }
 }
 
