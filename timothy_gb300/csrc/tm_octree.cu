@@ -112,7 +112,8 @@ struct walk_state {
     double mind;                    // mindist of an isolated cell
     uint32_t bmin[3], bmax[3];      // query box, half-open
     uint32_t base;                  // the colony's first Morton position
-    int L, c, sp;                   // bin depth, colony, stack depth
+    int L, c, sp;                   // bin depth, colony, frames (the top one in top)
+    walk_frame top;                 // the frame being walked; the ones below it in the stack
     bool isolated, ident, fp64;
     const uint32_t *bst;            // the colony's bin starts
 };
@@ -199,7 +200,7 @@ __device__ __forceinline__ bool walk_begin(const tm_arrays &a, const tm_consts *
         }
     }
     if (a1 > a0 && a1 - a0 >= 2) {
-        stk[0] = {a1, a0, dT};
+        w.top = {a1, a0, dT};
         w.sp = 1;
         return true;
     }
@@ -209,10 +210,11 @@ __device__ __forceinline__ bool walk_begin(const tm_arrays &a, const tm_consts *
 // one DFS step (the child pop order of computepotential); true when the walk is over
 __device__ __forceinline__ bool walk_step(const tm_arrays &a, walk_state &w, walk_frame *stk)
 {
-    walk_frame &top = stk[w.sp - 1];
+    walk_frame &top = w.top;
     if (top.cur >= top.end) {
-        w.sp--;
-        return w.sp == 0;
+        if (--w.sp == 0) return true;
+        top = stk[w.sp - 1];
+        return false;
     }
     const uint32_t k = top.cur;
     if (w.mpos >= 0 && (long long)k >= w.mpos) {
@@ -261,7 +263,9 @@ __device__ __forceinline__ bool walk_step(const tm_arrays &a, walk_state &w, wal
         atomicOr(&a.frame[w.c].error, TM_ERR_STACK);
         return true;
     }
-    stk[w.sp++] = {e, k, dc};
+    stk[w.sp - 1] = top;                // keep the parent (its cursor already past this child)
+    top = {e, k, dc};
+    w.sp++;
     return false;
 }
 
