@@ -8,6 +8,8 @@
 #include "tm_arrays.cuh"
 #include "tm_kernels.cuh"
 
+#include <algorithm>
+
 #define FULL 0xffffffffu
 
 // ---------------------------------------------------------------------------
@@ -68,82 +70,86 @@ __global__ void k_binbase(tm_arrays a)
 // monotone, so per-type minima/maxima of x suffice; they are reduced on the
 // order-preserving integer image of the doubles (no FP64 instructions).
 
+// Each warp streams BBOX_GROUPS groups of 32 slots (a group lies in one
+// colony: colonies are 32-aligned) and keeps running per-type minima and
+// maxima in registers; it reduces them across the lanes and posts them only
+// when the colony changes and at the end of its groups.
+#define BBOX_GROUPS 16
+
+template <int NT>
+__device__ __forceinline__ void bbox_post(tm_arrays &a, int c, unsigned long long (&r)[NT][6], int lane)
+{
+#pragma unroll
+    for (int tt = 0; tt < NT; tt++) {
+#pragma unroll
+        for (int q = 0; q < 6; q++) {
+            unsigned long long v = r[tt][q];
+            for (int o = 16; o > 0; o >>= 1) {
+                const unsigned long long u = __shfl_xor_sync(FULL, v, o);
+                v = q < 3 ? (u < v ? u : v) : (u > v ? u : v);
+            }
+            // the box only widens during the pass: post only what reaches past its current value
+            if (lane == 0 && (q < 3 ? v != 0xffffffffffffffffull : v != 0ull)) {
+                unsigned long long *t = &a.frame[c].bbox[tt][q];
+                if (q < 3 && v < __ldcg(t)) atomicMin(t, v);
+                else if (q >= 3 && v > __ldcg(t)) atomicMax(t, v);
+            }
+            r[tt][q] = q < 3 ? 0xffffffffffffffffull : 0ull;
+        }
+    }
+}
+
+template <int NT>
 __global__ void __launch_bounds__(256) k_bbox(tm_arrays a, int ntypes)
 {
-    // per-block partial minima/maxima in shared memory, one global atomic per
-    // block and value; a block spans at most 8 colonies (32-aligned ranges)
-    __shared__ unsigned long long red[8][TM_MAX_TYPES][6];
-    __shared__ int colid[8];
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int k = threadIdx.x; k < 8 * TM_MAX_TYPES * 6; k += blockDim.x) {
-        const int q = k % 6;
-        (&red[0][0][0])[k] = q < 3 ? 0xffffffffffffffffull : 0ull;
-    }
-    long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    bool live = false;
-    int c = -1;
-    if (s < a.nslots_total) {
-        c = a.col[s];
+    const int lane = threadIdx.x & 31;
+    const long long ngroups = (a.nslots_total + 31) >> 5;
+    const long long g0 = (((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * BBOX_GROUPS;
+    if (g0 >= ngroups) return;                      // whole warp
+    const long long g1 = g0 + BBOX_GROUPS < ngroups ? g0 + BBOX_GROUPS : ngroups;
+    unsigned long long r[NT][6];
+#pragma unroll
+    for (int tt = 0; tt < NT; tt++)
+#pragma unroll
+        for (int q = 0; q < 6; q++) r[tt][q] = q < 3 ? 0xffffffffffffffffull : 0ull;
+    int cur = -1;                                   // the colony being reduced
+    for (long long g = g0; g < g1; g++) {
+        const long long s = (g << 5) + lane;
+        const int c = a.col[g << 5];                // uniform over the group
         const tm_desc &d = a.desc[c];
-        live = d.active && tm_live(s, d);
-    }
-    if (lane == 0) colid[w] = (((s >> 5) << 5) < a.nslots_total) ? a.col[(s >> 5) << 5] : -1;
-    __syncthreads();
-    unsigned long long v[3] = {0, 0, 0};
-    int t = -1;
-    if (live) {
-        t = a.ctype[s];
-        v[0] = tm_ordered(a.x[s]);
-        v[1] = tm_ordered(a.y[s]);
-        v[2] = tm_ordered(a.z[s]);
-    }
-    for (int tt = 0; tt < ntypes; tt++) {
-        const bool mine = live && t == tt;
-        if (!__ballot_sync(FULL, mine)) continue;
-        unsigned long long r[6];
-        for (int k = 0; k < 3; k++) {
-            r[k] = mine ? v[k] : 0xffffffffffffffffull;
-            r[3 + k] = mine ? v[k] : 0ull;
+        if (!d.active) continue;
+        if (c != cur) {
+            if (cur >= 0) bbox_post<NT>(a, cur, r, lane);
+            cur = c;
         }
-        for (int o = 16; o > 0; o >>= 1) {
-            for (int k = 0; k < 3; k++) {
-                const unsigned long long q = __shfl_xor_sync(FULL, r[k], o);
-                r[k] = q < r[k] ? q : r[k];
-                const unsigned long long u = __shfl_xor_sync(FULL, r[3 + k], o);
-                r[3 + k] = u > r[3 + k] ? u : r[3 + k];
-            }
-        }
-        if (lane == 0) {
-            for (int k = 0; k < 3; k++) {
-                red[w][tt][k] = r[k];
-                red[w][tt][3 + k] = r[3 + k];
-            }
+        if (s >= a.nslots_total || !tm_live(s, d)) continue;
+        const int t = a.ctype[s];
+        const unsigned long long v0 = tm_ordered(a.x[s]), v1 = tm_ordered(a.y[s]), v2 = tm_ordered(a.z[s]);
+#pragma unroll
+        for (int tt = 0; tt < NT; tt++) {
+            if (t != tt) continue;
+            r[tt][0] = v0 < r[tt][0] ? v0 : r[tt][0];
+            r[tt][1] = v1 < r[tt][1] ? v1 : r[tt][1];
+            r[tt][2] = v2 < r[tt][2] ? v2 : r[tt][2];
+            r[tt][3] = v0 > r[tt][3] ? v0 : r[tt][3];
+            r[tt][4] = v1 > r[tt][4] ? v1 : r[tt][4];
+            r[tt][5] = v2 > r[tt][5] ? v2 : r[tt][5];
         }
     }
-    __syncthreads();
-    // warps of the same colony merge into the first such warp, which posts the atomics
-    const int nw = blockDim.x >> 5;
-    for (int k = threadIdx.x; k < nw * ntypes * 6; k += blockDim.x) {
-        const int ww = k / (ntypes * 6), tt = (k / 6) % ntypes, q = k % 6;
-        const int cc = colid[ww];
-        if (cc < 0) continue;
-        bool first = true;
-        for (int u = 0; u < ww; u++)
-            if (colid[u] == cc) first = false;
-        if (!first) continue;
-        unsigned long long best = red[ww][tt][q];
-        for (int u = ww + 1; u < nw; u++) {
-            if (colid[u] != cc) continue;
-            const unsigned long long o = red[u][tt][q];
-            best = q < 3 ? (o < best ? o : best) : (o > best ? o : best);
-        }
-        // the box only widens during the pass: post only what reaches past its current value
-        if (q < 3 ? best != 0xffffffffffffffffull : best != 0ull) {
-            unsigned long long *t = &a.frame[cc].bbox[tt][q];
-            if (q < 3 && best < __ldcg(t)) atomicMin(t, best);
-            else if (q >= 3 && best > __ldcg(t)) atomicMax(t, best);
-        }
-    }
+    if (cur >= 0) bbox_post<NT>(a, cur, r, lane);
+    (void)ntypes;
+}
+
+cudaError_t tm_launch_bbox(const tm_arrays &a, int ntypes, cudaStream_t st)
+{
+    const long long ngroups = (a.nslots_total + 31) >> 5;
+    const long long warps = (ngroups + BBOX_GROUPS - 1) / BBOX_GROUPS;
+    const unsigned grid = (unsigned)std::max(1ll, (warps + 7) / 8);
+    if (ntypes <= 1) k_bbox<1><<<grid, 256, 0, st>>>(a, ntypes);
+    else if (ntypes <= 2) k_bbox<2><<<grid, 256, 0, st>>>(a, ntypes);
+    else if (ntypes <= 4) k_bbox<4><<<grid, 256, 0, st>>>(a, ntypes);
+    else k_bbox<TM_MAX_TYPES><<<grid, 256, 0, st>>>(a, ntypes);
+    return cudaGetLastError();
 }
 
 // affShift / affScale (octree.c:175-180) and the bin depth of each colony

@@ -3,7 +3,7 @@
 #include "tm_arrays.cuh"
 
 __global__ void k_step_init(tm_arrays a);
-__global__ void k_bbox(tm_arrays a, int ntypes);
+cudaError_t tm_launch_bbox(const tm_arrays &a, int ntypes, cudaStream_t st);
 __global__ void k_frame(tm_arrays a, const tm_consts *K);
 __global__ void k_codes(tm_arrays a);
 __global__ void k_binbase(tm_arrays a);

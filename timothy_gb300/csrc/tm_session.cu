@@ -392,7 +392,7 @@ static int enqueue_build(tm_session *s, int p, int &nk)
     CK(cudaMemsetAsync(a.bigbins, 0, sizeof(int), st));
     CK(cudaMemsetAsync(a.fix_count, 0, 5 * sizeof(int), st));   // fix count and the four work counters
     k_step_init<<<blocks_for(ncol, 128), 128, 0, st>>>(a);
-    k_bbox<<<blocks_for(nsl, 256), 256, 0, st>>>(a, s->K.ntypes);
+    CK(tm_launch_bbox(a, s->K.ntypes, st));
     k_frame<<<blocks_for(ncol, 128), 128, 0, st>>>(a, s->dK);
     k_codes<<<blocks_for(nsl, 256), 256, 0, st>>>(a);
     CK(cudaGetLastError());
