@@ -248,11 +248,14 @@ __global__ void k_scatter(tm_arrays a)
     if (!d.active || !tm_live(s, d)) return;
     uint32_t b = a.bin[s];
     long long pos = a.frame[c].bin_base + a.bin_start[b] + atomicAdd(&a.bin_cursor[b], 1u);
-    a.tmp[pos] = (int)s;
+    a.rank[pos] = (int)s;   // grouped by bin; rank is free until k_gather rewrites it
 }
 
-// sort each bin's slots by full Morton order; bins of up to 32 cells by one
-// thread, larger ones are queued for k_binsort_big
+// Sort each bin's slots by full Morton order.  k_scatter left them grouped by
+// bin in rank[]; every cell of a bin of up to 32 counts the bin's codes that
+// sort before its own (ties, an error, by position) and writes its slot at
+// that rank into tmp, so all lanes work and nothing is kept in local arrays.
+// Larger bins are queued for k_binsort_big.
 __global__ void k_binsort_small(tm_arrays a)
 {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -260,41 +263,34 @@ __global__ void k_binsort_small(tm_arrays a)
     int c = a.col[i];
     const tm_desc &d = a.desc[c];
     if (!d.active || !tm_live(i, d)) return;
-    int r = a.tmp[i];
-    uint32_t b = a.bin[r];
-    long long st = a.frame[c].bin_base + a.bin_start[b];
-    if (st != i) return;                    // not the first slot of its bin
-    uint32_t cnt = a.bin_start[b + 1] - a.bin_start[b];
-    if (cnt <= 1) return;
+    const int r = a.rank[i];
+    const uint32_t b = a.bin[r];
+    const long long st = a.frame[c].bin_base + a.bin_start[b];
+    const uint32_t cnt = a.bin_start[b + 1] - a.bin_start[b];
     if (cnt > 32) {
-        atomicAdd(&a.frame[c].nbig, 1);
-        int q = atomicAdd(&a.bigbins[0], 1);
-        a.bigbins[1 + 2 * q] = (int)b;
-        a.bigbins[2 + 2 * q] = c;
+        if (st == i) {
+            atomicAdd(&a.frame[c].nbig, 1);
+            int q = atomicAdd(&a.bigbins[0], 1);
+            a.bigbins[1 + 2 * q] = (int)b;
+            a.bigbins[2 + 2 * q] = c;
+        }
         return;
     }
-    int idx[32];
-    uint4 key[32];
+    const uint4 key = a.code[r];
+    uint32_t rk = 0;
+    bool dup = false;
     for (uint32_t k = 0; k < cnt; k++) {
-        idx[k] = a.tmp[st + k];
-        key[k] = a.code[idx[k]];
-    }
-    for (uint32_t k = 1; k < cnt; k++) {
-        uint4 kk = key[k];
-        int ii = idx[k];
-        int m = (int)k - 1;
-        while (m >= 0 && tm_morton_less(kk, key[m])) {
-            key[m + 1] = key[m];
-            idx[m + 1] = idx[m];
-            m--;
+        const long long j = st + (long long)k;
+        if (j == i) continue;
+        const uint4 kj = a.code[a.rank[j]];
+        if (tm_morton_less(kj, key)) rk++;
+        else if (tm_code_eq(kj, key)) {
+            dup = true;
+            if (j < i) rk++;
         }
-        key[m + 1] = kk;
-        idx[m + 1] = ii;
     }
-    for (uint32_t k = 0; k < cnt; k++) {
-        if (k > 0 && tm_code_eq(key[k], key[k - 1])) atomicOr(&a.frame[c].error, TM_ERR_CODES);
-        a.tmp[st + k] = idx[k];
-    }
+    if (dup) atomicOr(&a.frame[c].error, TM_ERR_CODES);
+    a.tmp[st + rk] = r;
 }
 
 // one block per large bin: bitonic sort of up to TM_BIG_BIN cells in shared memory
@@ -316,7 +312,7 @@ __global__ void k_binsort_big(tm_arrays a)
         while (p2 < cnt) p2 <<= 1;
         for (uint32_t k = threadIdx.x; k < p2; k += blockDim.x) {
             if (k < cnt) {
-                idx[k] = a.tmp[st + k];
+                idx[k] = a.rank[st + k];      // grouped by k_scatter
                 key[k] = a.code[idx[k]];
             } else {
                 idx[k] = -1;
