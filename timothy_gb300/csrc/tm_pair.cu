@@ -515,11 +515,30 @@ __global__ void __launch_bounds__(256) k_listbuild(tm_arrays a, const tm_consts 
     const float4 *__restrict__ hi = a.hi;
     const float4 *__restrict__ lo = a.lo;
     const long long ls = a.lstride;
+    // Rows of bins whose y/z gap to the cell already exceeds the radius hold
+    // no cell within it, and the rest are cut to the x range the remaining
+    // radius reaches: the corners of the box are skipped, the lists are the
+    // same.  A bin's extent is widened by the 0.01-bin margin of bin_lo/bin_hi.
+    const float mrg = 0.01f / bs;
+    auto gap = [&](int b, float x, float sh) {
+        const float e0 = sh + (float)b / bs - mrg, e1 = sh + (float)(b + 1) / bs + mrg;
+        return x < e0 ? e0 - x : (x > e1 ? x - e1 : 0.0f);
+    };
     int vc = 0;
-    for (int bz = bz0; bz <= bz1; bz++)
+    for (int bz = bz0; bz <= bz1; bz++) {
+        const float gz = gap(bz, hi_i.z, f.shiftf[2]);
+        if (gz * gz > thr) continue;
         for (int by = by0; by <= by1; by++) {
+            const float gy = gap(by, hi_i.y, f.shiftf[1]);
+            const float r2 = thr - gz * gz - gy * gy;
+            if (r2 < 0.0f) continue;
+            const float rx = sqrtf(r2) * 1.00002f + 1e-4f;
+            int xa = (int)floorf((hi_i.x - f.shiftf[0] - rx) * bs - 0.01f);
+            int xb = (int)floorf((hi_i.x - f.shiftf[0] + rx) * bs + 0.01f);
+            xa = xa < bx0 ? bx0 : xa;
+            xb = xb > bx1 ? bx1 : xb;
             const uint32_t yz = tm_morton(0u, (uint32_t)by, (uint32_t)bz);
-            for (int bx = bx0; bx <= bx1; bx++) {
+            for (int bx = xa; bx <= xb; bx++) {
                 const uint32_t m = yz | tm_morton((uint32_t)bx, 0u, 0u);
                 const long long j0 = bbase + __ldg(bst + m), j1 = bbase + __ldg(bst + m + 1);
                 for (long long j = j0; j < j1; j++) {
@@ -535,6 +554,7 @@ __global__ void __launch_bounds__(256) k_listbuild(tm_arrays a, const tm_consts 
                 }
             }
         }
+    }
     a.vcount[i] = min(vc, a.vcap);
     a.x0[i] = hi_i;
     // an overflowing list cannot serve this step: flag the colony, whose
