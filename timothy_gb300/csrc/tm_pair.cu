@@ -538,11 +538,14 @@ __global__ void __launch_bounds__(256) k_listbuild(tm_arrays a, const tm_consts 
             xa = xa < bx0 ? bx0 : xa;
             xb = xb > bx1 ? bx1 : xb;
             const uint32_t yz = tm_morton(0u, (uint32_t)by, (uint32_t)bz);
-            for (int bx = xa; bx <= xb; bx++) {
+            for (int bx = xa; bx <= xb;) {
+                // x is the lowest Morton bit: an even bin and the next one are
+                // one contiguous range, visited in the same order
                 const uint32_t m = yz | tm_morton((uint32_t)bx, 0u, 0u);
-                const long long j0 = bbase + __ldg(bst + m), j1 = bbase + __ldg(bst + m + 1);
-                for (long long j = j0; j < j1; j++) {
-                    const float4 hj = __ldg(hi + j), lj = __ldg(lo + j);
+                const int w = ((bx & 1) == 0 && bx < xb) ? 2 : 1;
+                bx += w;
+                const long long j0 = bbase + __ldg(bst + m), j1 = bbase + __ldg(bst + m + w);
+                auto test = [&](long long j, float4 hj, float4 lj) {
                     const float dx = (hj.x - hi_i.x) + (lj.x - lo_i.x);
                     const float dy = (hj.y - hi_i.y) + (lj.y - lo_i.y);
                     const float dz = (hj.z - hi_i.z) + (lj.z - lo_i.z);
@@ -551,7 +554,15 @@ __global__ void __launch_bounds__(256) k_listbuild(tm_arrays a, const tm_consts 
                         if (vc < a.vcap) a.vlist[(long long)vc * ls + i] = (int)j;
                         vc++;
                     }
+                };
+                // two candidates' loads in flight, appended in order
+                long long j = j0;
+                for (; j + 1 < j1; j += 2) {
+                    const float4 h0 = __ldg(hi + j), l0 = __ldg(lo + j), h1 = __ldg(hi + j + 1), l1 = __ldg(lo + j + 1);
+                    test(j, h0, l0);
+                    test(j + 1, h1, l1);
                 }
+                if (j < j1) test(j, __ldg(hi + j), __ldg(lo + j));
             }
         }
     }
