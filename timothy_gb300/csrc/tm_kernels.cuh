@@ -72,6 +72,9 @@ cudaError_t tm_launch_cycle_apply(const tm_cycle_dev &P, const tm_arrays &a, lon
                                   unsigned long long *marked, cudaStream_t st);
 
 // the C library's rand() stream on the device (tm_libcrand.cu)
+// values per chunk of the device rand() stream (one thread each); a call of
+// count values needs count / TM_RAND_CHUNK + 2 windows of 31 words
+#define TM_RAND_CHUNK 992
 struct tm_rand_cache {
     int valid;
     uint32_t seed;

@@ -10,22 +10,30 @@
 //
 // The recurrence is linear over the integers mod 2^32, so the window
 // S_t = (r[t-31], ..., r[t-1]) advances by a 31 x 31 matrix M: S_{t+n} =
-// M^n S_t.  The host reaches the requested offset by powers of M (squaring),
-// then gives each of the chunks of kChunk values its starting window by
-// repeated multiplication with M^kChunk; one device thread per chunk runs
-// the recurrence.  A session remembers where its last stream ended, so
-// consecutive calls continue without the powers.
+// M^n S_t.  The host reaches the requested offset by powers of M (squaring);
+// on the device, chunk c of kChunk values starts from M^(c kChunk) S, which
+// its thread builds from a table of M^(kChunk 2^b) (the bits of c), and one
+// thread per chunk runs the recurrence.  The thread of the last chunk leaves
+// the window after the last value, so a session's next call continues from
+// it without any power on the host.
 #include "tm_kernels.cuh"
 #include "timothy_gb300.h"
 
 #include <cstdint>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 namespace {
 
 constexpr int kWin = 31;
-constexpr int kChunk = 2048;
+constexpr int kChunk = TM_RAND_CHUNK;   // 31 x 32: a chunk is whole blocks of 31 steps
+static_assert(kChunk % kWin == 0, "chunks of whole 31-step blocks");
+constexpr int kPowers = 24;   // M^(kChunk 2^b), b < kPowers: up to 2^24 chunks of one call
+
+// the table of jumps, transposed (entry [k * 31 + i] = M[i][k]), copied to
+// each device on first use
+__device__ uint32_t g_jump[kPowers][kWin * kWin];
 
 struct mat31 {
     uint32_t m[kWin][kWin];
@@ -106,23 +114,108 @@ void window_at(uint32_t seed, uint64_t offset, uint32_t w[kWin])
     }
 }
 
-__global__ void k_libc_rand(const uint32_t *windows, int64_t count, int *out)
+struct window31 {
+    uint32_t w[kWin];
+};
+
+// the starting window of every chunk, M^(c kChunk) w0: one warp per chunk,
+// lane i holds entry i, and each jump is a matrix-vector product with the
+// window broadcast lane by lane
+__global__ void __launch_bounds__(128) k_rand_windows(window31 w0, int64_t nchunks, uint32_t *windows)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (c >= nchunks) return;                  // whole warp
+    uint32_t v = 0u;
+#pragma unroll
+    for (int i = 0; i < kWin; i++)
+        if (lane == i) v = w0.w[i];
+    int64_t bits = c;
+    for (int b = 0; bits != 0 && b < kPowers; b++, bits >>= 1) {
+        if (!(bits & 1)) continue;             // uniform over the warp
+        const uint32_t *mt = g_jump[b];
+        uint32_t acc = 0u;
+#pragma unroll
+        for (int k = 0; k < kWin; k++) {
+            const uint32_t vk = __shfl_sync(0xffffffffu, v, k);
+            if (lane < kWin) acc += __ldg(mt + k * kWin + lane) * vk;
+        }
+        v = acc;
+    }
+    if (lane < kWin) windows[c * kWin + lane] = v;
+}
+
+// one thread per chunk runs the recurrence in blocks of 31 steps, the window
+// in registers: at a block's start w[j] = r[t + j - 31], and step j makes
+// r[t + j] = w[j] + (j < 3 ? w[j + 28] : the new w[j - 3]) in place.  The
+// last block stops at the stream's end, and its thread writes the window
+// after the last value (w from the stop, in stream order).
+__global__ void __launch_bounds__(128) k_libc_rand(const uint32_t *windows, int64_t count, int *out, uint32_t *endw)
 {
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t first = c * kChunk;
     if (first >= count) return;
     uint32_t w[kWin];
+#pragma unroll
     for (int i = 0; i < kWin; i++) w[i] = windows[c * kWin + i];
     const int64_t last = first + kChunk < count ? first + kChunk : count;
-    int head = 0;                          // w[head] is the oldest entry, r[t-31]
-    for (int64_t k = first; k < last; k++) {
-        int i3 = head + kWin - 3;
-        if (i3 >= kWin) i3 -= kWin;
-        const uint32_t v = w[head] + w[i3];
-        w[head] = v;
-        head = head + 1 == kWin ? 0 : head + 1;
-        out[k] = (int)(v >> 1);
+    int64_t k0 = first;
+    for (; k0 + kWin <= last; k0 += kWin) {
+#pragma unroll
+        for (int j = 0; j < kWin; j++) {
+            w[j] += w[j < 3 ? j + kWin - 3 : j - 3];
+            out[k0 + j] = (int)(w[j] >> 1);
+        }
     }
+    const int rem = (int)(last - k0);          // 0..30 steps of a last, partial block
+#pragma unroll
+    for (int j = 0; j < kWin; j++) {
+        if (j < rem) {
+            w[j] += w[j < 3 ? j + kWin - 3 : j - 3];
+            out[k0 + j] = (int)(w[j] >> 1);
+        }
+    }
+    if (last == count) {
+        // the oldest entry is w[rem] (w[0] after a whole block): rotate by rem
+        // as fixed rotations by its bits, so every index stays static
+#pragma unroll
+        for (int bit = 1; bit < 32; bit <<= 1) {
+            if (rem & bit) {
+                uint32_t t[kWin];
+#pragma unroll
+                for (int i = 0; i < kWin; i++) t[i] = w[(i + bit) % kWin];
+#pragma unroll
+                for (int i = 0; i < kWin; i++) w[i] = t[i];
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < kWin; i++) endw[i] = w[i];
+    }
+}
+
+// the jump table on the current device (once per device and process)
+int ensure_jumps()
+{
+    static std::mutex mtx;
+    static bool done[64] = {};
+    static std::vector<uint32_t> table;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -2;
+    std::lock_guard<std::mutex> lock(mtx);
+    if (done[dev]) return 0;
+    if (table.empty()) {
+        table.resize((size_t)kPowers * kWin * kWin);
+        mat31 m = power(step_matrix(), kChunk);
+        for (int b = 0; b < kPowers; b++) {
+            uint32_t *t = &table[(size_t)b * kWin * kWin];
+            for (int i = 0; i < kWin; i++)
+                for (int k = 0; k < kWin; k++) t[k * kWin + i] = m.m[i][k];
+            m = mul(m, m);
+        }
+    }
+    if (cudaMemcpyToSymbol(g_jump, table.data(), table.size() * sizeof(uint32_t)) != cudaSuccess) return -2;
+    done[dev] = true;
+    return 0;
 }
 
 }  // namespace
@@ -136,35 +229,28 @@ int tm_libc_rand_device(uint32_t seed, int64_t offset, int64_t count, int *out, 
 {
     if (count <= 0) return 0;
     const int64_t nchunks = (count + kChunk - 1) / kChunk;
-    if (nchunks > windows_cap) return -1;
-    uint32_t w[kWin];
+    if (nchunks + 1 > windows_cap || nchunks > ((int64_t)1 << kPowers)) return -1;
+    if (ensure_jumps() != 0) return -2;
+    window31 w0;
     if (cache && cache->valid && cache->seed == seed && cache->offset == offset) {
-        memcpy(w, cache->window, sizeof w);
+        memcpy(w0.w, cache->window, sizeof w0.w);
     } else {
-        window_at(seed, (uint64_t)offset, w);
+        window_at(seed, (uint64_t)offset, w0.w);
     }
-    std::vector<uint32_t> win((size_t)nchunks * kWin);
-    static const mat31 jump = power(step_matrix(), kChunk);
-    memcpy(win.data(), w, sizeof w);
-    for (int64_t c = 1; c < nchunks; c++) apply(jump, &win[(size_t)(c - 1) * kWin], &win[(size_t)c * kWin]);
-    // the window after the last value, for the next call
+    uint32_t *endw = d_windows + nchunks * kWin;   // the spare window after the chunks'
+    k_rand_windows<<<(unsigned)((nchunks * 32 + 127) / 128), 128, 0, st>>>(w0, nchunks, d_windows);
+    const int threads = 128;
+    k_libc_rand<<<(unsigned)((nchunks + threads - 1) / threads), threads, 0, st>>>(d_windows, count, out, endw);
+    if (cudaGetLastError() != cudaSuccess) return -2;
+    uint32_t end[kWin];
+    if (cudaMemcpyAsync(end, endw, sizeof end, cudaMemcpyDeviceToHost, st) != cudaSuccess) return -2;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return -2;
     if (cache) {
-        uint32_t endw[kWin];
-        const int64_t rest = count - (nchunks - 1) * kChunk;
-        apply(power(step_matrix(), (uint64_t)rest), &win[(size_t)(nchunks - 1) * kWin], endw);
-        memcpy(cache->window, endw, sizeof endw);
+        memcpy(cache->window, end, sizeof end);
         cache->seed = seed;
         cache->offset = offset + count;
         cache->valid = 1;
     }
-    if (cudaMemcpyAsync(d_windows, win.data(), win.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st) !=
-        cudaSuccess)
-        return -2;
-    const int threads = 128;
-    k_libc_rand<<<(unsigned)((nchunks + threads - 1) / threads), threads, 0, st>>>(d_windows, count, out);
-    if (cudaGetLastError() != cudaSuccess) return -2;
-    // the host vector must outlive the copy
-    if (cudaStreamSynchronize(st) != cudaSuccess) return -2;
     return 0;
 }
 

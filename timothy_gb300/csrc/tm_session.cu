@@ -2418,7 +2418,7 @@ extern "C" int tm_colony_cellcycle(tm_session *s, int id, const tm_cycle_params 
     std::vector<int> hs;
     if (p->rand_seeded && p->rand_offset) {
         // the C library's stream after srand(rand_seed), generated on the device
-        const int64_t chunks = ((int64_t)tot[0] + 2047) / 2048 + 1;
+        const int64_t chunks = ((int64_t)tot[0] + TM_RAND_CHUNK - 1) / TM_RAND_CHUNK + 1;
         if (s->rand_windows_cap < chunks) {
             if (s->rand_windows) CK(cudaFree(s->rand_windows));
             s->rand_windows = nullptr;
