@@ -114,7 +114,8 @@ __device__ __forceinline__ float cycle_length(float g, int r, float v)
 
 __global__ void __launch_bounds__(256) k_cycle_apply(tm_cycle_dev P, tm_arrays a, long long off, long long n, int dim,
                                                      const uint32_t *draw_off, const uint32_t *div_off,
-                                                     const int *stream, unsigned long long *marked)
+                                                     const int *stream, unsigned long long *marked,
+                                                     uint32_t *divlist)
 {
     const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
@@ -143,54 +144,72 @@ __global__ void __launch_bounds__(256) k_cycle_apply(tm_cycle_dev P, tm_arrays a
             atomicAdd(marked, 1ull);
         }
     }
-    if (d.divide) {
-        double sh[3];
-        sh[0] = sub64(mul64(div64((double)dr[0], (double)TM_RAND_MAX_I), 2.0), 1.0);
-        sh[1] = sub64(mul64(div64((double)dr[1], (double)TM_RAND_MAX_I), 2.0), 1.0);
-        int q = 2;
-        if (dim == 3) sh[2] = sub64(mul64(div64((double)dr[q++], (double)TM_RAND_MAX_I), 2.0), 1.0);
-        else sh[2] = 0.0;
-        double sc = __dsqrt_rn(add64(add64(mul64(sh[0], sh[0]), mul64(sh[1], sh[1])), mul64(sh[2], sh[2])));
-        const double psize = a.size[s];
-        sc = div64(psize, mul64(2.0, sc));
-        for (int e = 0; e < 3; e++) sh[e] = mul64(sc, sh[e]);
-        const long long j = div_off[c];
-        const long long ds = off + n + j, dc = off + n + j;   // daughter slot and caller index (n + j)
-        const double dsize = mul64(P.shrink, psize);
-        a.x[ds] = add64(a.x[s], sh[0]);
-        a.y[ds] = add64(a.y[s], sh[1]);
-        a.z[ds] = add64(a.z[s], sh[2]);
-        a.size[ds] = dsize;
-        a.ctype[ds] = t;
-        a.cy_age[dc] = a.cy_age[ci] + 1;
-        a.x[s] = sub64(a.x[s], sh[0]);
-        a.y[s] = sub64(a.y[s], sh[1]);
-        a.z[s] = sub64(a.z[s], sh[2]);
-        a.size[s] = dsize;
-        a.cy_age[ci] = a.cy_age[ci] + 1;
-        a.cy_g1[ci] = cycle_length(T.g1, dr[q], T.v);
-        a.cy_g2[ci] = cycle_length(T.g2, dr[q + 1], T.v);
-        a.cy_s[ci] = cycle_length(T.s, dr[q + 2], T.v);
-        a.cy_m[ci] = cycle_length(T.m, dr[q + 3], T.v);
-        a.density[ds] = a.density[s];
-        a.young[ds] = __double2float_rn(add64(2100.0, mul64(sub64(mul64((double)frand(dr[q + 4]), 2.0), 1.0), 100.0)));
-        a.phase[ds] = 1;
-        a.cy_pt[dc] = 0.0f;
-        // the daughter's own v is 0 (cells.c:184): its draws leave the type's lengths
-        a.cy_g1[dc] = cycle_length(T.g1, dr[q + 5], 0.0f);
-        a.cy_g2[dc] = cycle_length(T.g2, dr[q + 6], 0.0f);
-        a.cy_s[dc] = cycle_length(T.s, dr[q + 7], 0.0f);
-        a.cy_m[dc] = cycle_length(T.m, dr[q + 8], 0.0f);
-        a.perm[ds] = (int)(n + j);
-        a.rem[ds] = 0;
-        a.v[ds] = 0.0;
-        a.mindist[ds] = 0.0;
-        a.fx[ds] = 0.0;
-        a.fy[ds] = 0.0;
-        a.fz[ds] = 0.0;
-        a.nbcount[ds] = 0;
-        a.nbmin[ds] = -1;
-    }
+    if (d.divide) divlist[div_off[c]] = (uint32_t)s;   // k_cycle_divide does the rest
+}
+
+// the divisions (cells.c:175-201), one thread per dividing cell from the list
+// k_cycle_apply leaves in daughter order: their FP64 work (draw scaling,
+// sqrt, divisions) runs in full warps instead of in every warp that holds
+// one dividing cell
+__global__ void __launch_bounds__(256) k_cycle_divide(tm_cycle_dev P, tm_arrays a, long long off, long long n, int dim,
+                                                      long long ndiv, const uint32_t *divlist,
+                                                      const uint32_t *draw_off, const uint32_t *div_off,
+                                                      const int *stream)
+{
+    const long long jj = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (jj >= ndiv) return;
+    const long long s = divlist[jj];
+    const long long c = a.perm[s];
+    const long long ci = off + c;
+    const int t = a.ctype[s];
+    const tm_cycle_type &T = P.types[t];
+    const int *dr = stream + draw_off[c];
+    double sh[3];
+    sh[0] = sub64(mul64(div64((double)dr[0], (double)TM_RAND_MAX_I), 2.0), 1.0);
+    sh[1] = sub64(mul64(div64((double)dr[1], (double)TM_RAND_MAX_I), 2.0), 1.0);
+    int q = 2;
+    if (dim == 3) sh[2] = sub64(mul64(div64((double)dr[q++], (double)TM_RAND_MAX_I), 2.0), 1.0);
+    else sh[2] = 0.0;
+    double sc = __dsqrt_rn(add64(add64(mul64(sh[0], sh[0]), mul64(sh[1], sh[1])), mul64(sh[2], sh[2])));
+    const double psize = a.size[s];
+    sc = div64(psize, mul64(2.0, sc));
+    for (int e = 0; e < 3; e++) sh[e] = mul64(sc, sh[e]);
+    const long long j = div_off[c];
+    const long long ds = off + n + j, dc = off + n + j;   // daughter slot and caller index (n + j)
+    const double dsize = mul64(P.shrink, psize);
+    a.x[ds] = add64(a.x[s], sh[0]);
+    a.y[ds] = add64(a.y[s], sh[1]);
+    a.z[ds] = add64(a.z[s], sh[2]);
+    a.size[ds] = dsize;
+    a.ctype[ds] = t;
+    a.cy_age[dc] = a.cy_age[ci] + 1;
+    a.x[s] = sub64(a.x[s], sh[0]);
+    a.y[s] = sub64(a.y[s], sh[1]);
+    a.z[s] = sub64(a.z[s], sh[2]);
+    a.size[s] = dsize;
+    a.cy_age[ci] = a.cy_age[ci] + 1;
+    a.cy_g1[ci] = cycle_length(T.g1, dr[q], T.v);
+    a.cy_g2[ci] = cycle_length(T.g2, dr[q + 1], T.v);
+    a.cy_s[ci] = cycle_length(T.s, dr[q + 2], T.v);
+    a.cy_m[ci] = cycle_length(T.m, dr[q + 3], T.v);
+    a.density[ds] = a.density[s];
+    a.young[ds] = __double2float_rn(add64(2100.0, mul64(sub64(mul64((double)frand(dr[q + 4]), 2.0), 1.0), 100.0)));
+    a.phase[ds] = 1;
+    a.cy_pt[dc] = 0.0f;
+    // the daughter's own v is 0 (cells.c:184): its draws leave the type's lengths
+    a.cy_g1[dc] = cycle_length(T.g1, dr[q + 5], 0.0f);
+    a.cy_g2[dc] = cycle_length(T.g2, dr[q + 6], 0.0f);
+    a.cy_s[dc] = cycle_length(T.s, dr[q + 7], 0.0f);
+    a.cy_m[dc] = cycle_length(T.m, dr[q + 8], 0.0f);
+    a.perm[ds] = (int)(n + j);
+    a.rem[ds] = 0;
+    a.v[ds] = 0.0;
+    a.mindist[ds] = 0.0;
+    a.fx[ds] = 0.0;
+    a.fy[ds] = 0.0;
+    a.fz[ds] = 0.0;
+    a.nbcount[ds] = 0;
+    a.nbmin[ds] = -1;
 }
 
 cudaError_t tm_launch_cycle_count(const tm_cycle_dev &P, const tm_arrays &a, long long off, long long n, int dim,
@@ -202,9 +221,13 @@ cudaError_t tm_launch_cycle_count(const tm_cycle_dev &P, const tm_arrays &a, lon
 
 cudaError_t tm_launch_cycle_apply(const tm_cycle_dev &P, const tm_arrays &a, long long off, long long n, int dim,
                                   const uint32_t *draw_off, const uint32_t *div_off, const int *stream,
-                                  unsigned long long *marked, cudaStream_t st)
+                                  unsigned long long *marked, uint32_t *divlist, long long ndiv, cudaStream_t st)
 {
     if (n <= 0) return cudaSuccess;
-    k_cycle_apply<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(P, a, off, n, dim, draw_off, div_off, stream, marked);
+    k_cycle_apply<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(P, a, off, n, dim, draw_off, div_off, stream, marked,
+                                                               divlist);
+    if (ndiv > 0)
+        k_cycle_divide<<<(unsigned)((ndiv + 255) / 256), 256, 0, st>>>(P, a, off, n, dim, ndiv, divlist, draw_off,
+                                                                       div_off, stream);
     return cudaGetLastError();
 }

@@ -69,7 +69,7 @@ cudaError_t tm_launch_cycle_count(const tm_cycle_dev &P, const tm_arrays &a, lon
                                   uint32_t *draws, uint32_t *divs, cudaStream_t st);
 cudaError_t tm_launch_cycle_apply(const tm_cycle_dev &P, const tm_arrays &a, long long off, long long n, int dim,
                                   const uint32_t *draw_off, const uint32_t *div_off, const int *stream,
-                                  unsigned long long *marked, cudaStream_t st);
+                                  unsigned long long *marked, uint32_t *divlist, long long ndiv, cudaStream_t st);
 
 // the C library's rand() stream on the device (tm_libcrand.cu)
 // values per chunk of the device rand() stream (one thread each); a call of

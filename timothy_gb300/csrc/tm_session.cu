@@ -2437,7 +2437,9 @@ extern "C" int tm_colony_cellcycle(tm_session *s, int id, const tm_cycle_params 
     }
     CK(cudaMemsetAsync(s->cy_marked, 0, sizeof(unsigned long long), st));
     // pass 2: the transitions
-    CK(tm_launch_cycle_apply(P, a, c.off, n, s->K.dim, draw_off, div_off, s->cy_stream, s->cy_marked, st));
+    // the per-cell division counts are spent: their array takes the list of dividing cells
+    CK(tm_launch_cycle_apply(P, a, c.off, n, s->K.dim, draw_off, div_off, s->cy_stream, s->cy_marked, divs,
+                             (long long)tot[1], st));
     unsigned long long mk = 0;
     CK(cudaMemcpyAsync(&mk, s->cy_marked, sizeof mk, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
