@@ -6,7 +6,6 @@
 #include "tm_kernels.cuh"
 
 #include <algorithm>
-#include <numeric>
 
 // uniform float in [0, 1] from a counter (stands in for (float)rand()/RAND_MAX)
 __device__ inline float tm_uniform(unsigned long long step, unsigned long long cell, int axis)
@@ -102,18 +101,13 @@ __global__ void k_update(tm_arrays a, const tm_consts *K)
 
 // CIC weights onto field 0; the patch bounding box (patches.c:81-132) is
 // reduced alongside for the drop-in's patches_alloc.  Morton-ordered cells of
-// one warp mostly share grid nodes, so each distinct node of a corner gets
-// one atomic carrying the sum of the warp's weights on it.  Warps that run
-// together would hit the same few nodes (the same Morton neighbourhood) and
-// queue on them, so the g-th warp launched takes the 32 slots of warp
-// (g * stride) mod nwarps, stride coprime to nwarps: a bijection that puts
-// concurrently running warps far apart in the colony.
-__global__ void __launch_bounds__(256) k_cic(tm_arrays a, const tm_consts *K, long long nwarps, long long stride)
+// one warp mostly share grid nodes, so each run of cells on one node gets
+// one atomic carrying the sum of their weights (tm_warp_deposit).
+__global__ void __launch_bounds__(256) k_cic(tm_arrays a, const tm_consts *K)
 {
     const unsigned FULLM = 0xffffffffu;
-    const long long g = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (g >= nwarps) return;                                   // whole warp beyond the slots
-    const long long i = ((g * stride) % nwarps) * 32 + (threadIdx.x & 31);
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (((i >> 5) << 5) >= a.nslots_total) return;            // whole warp beyond the slots
     const int c = a.col[(i >> 5) << 5];
     const tm_desc &d = a.desc[c];
     if (!d.active || d.gridoff < 0) return;                    // uniform per warp
@@ -191,9 +185,6 @@ cudaError_t tm_launch_cic(const tm_arrays &a, const tm_consts *K, cudaStream_t s
 {
     unsigned grid = (unsigned)((a.nslots_total + 255) / 256);
     if (grid == 0) return cudaSuccess;
-    const long long nwarps = (a.nslots_total + 31) / 32;
-    long long stride = std::max(1ll, (long long)(0.6180339887 * (double)nwarps));
-    while (std::gcd(stride, nwarps) != 1) stride++;
-    k_cic<<<grid, 256, 0, st>>>(a, K, nwarps, stride);
+    k_cic<<<grid, 256, 0, st>>>(a, K);
     return cudaGetLastError();
 }
