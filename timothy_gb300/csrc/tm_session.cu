@@ -202,11 +202,13 @@ __global__ void k_colony_init(tm_arrays a, int c, long long off, int n, int nslo
 }
 
 // Upload into a colony that keeps its cell count.  The new values arrive in
-// input order in the rebuild scratch and go through perm to the slots the
-// cells occupy now, so the Morton order and the neighbour lists stay valid:
-// the step's rebuild test sees the displacement from the list positions, and
-// a cell that changed size or type (list radius, FP64 density weight) forces a
-// rebuild.  Cell types outside the table are flagged and replaced by 0.
+// input order (in the rebuild scratch, or the asynchronous upload's staging)
+// and go through perm to the slots the cells occupy now, so the Morton order
+// and the neighbour lists stay valid: the step's rebuild test sees the
+// displacement from the list positions, and a cell that changed size or type
+// (list radius, FP64 density weight) forces a rebuild.  Cell types outside
+// the table are flagged and replaced by 0.
+
 // the cells of an upload in caller order, at [base + caller index]
 struct upload_src {
     const double *x, *y, *z, *size;
