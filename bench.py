@@ -52,13 +52,6 @@ B_CELL = 112
 # summarised in profiles/k_plist_fp32_clustered2m.txt; traffic grows with the
 # cell count, so a launch over n cells moves n times this.
 TRAFFIC_PER_CELL = {"k_plist<1>": 376.1}
-# Colony radii giving a mean of 40 neighbours within h = 2.5 (bisected with
-# full-size neighbour counts; the bench reports the measured mean each run).
-RADIUS = {
-    ("uniform", 10_000, 1): 15.256856463570728,
-    ("clustered", 1_000_000, 2): 76.3271427172167,
-    ("clustered", 16_000_000, 3): 192.68257233787858,
-}
 WORKLOADS = {
     "precision16m": dict(kind="clustered", n=16_000_000, seed=3, precision="fp32c", cic=False, dt=0.01),
     "scale1m": dict(kind="clustered", n=1_000_000, seed=2, precision="fp64", cic=True, dt=0.01),
@@ -68,12 +61,7 @@ WORKLOADS = {
 
 def radius_for(kind, n, seed):
     """Calibrated radius, or the calibrated one of the same generator scaled by n^(1/3)."""
-    r = RADIUS.get((kind, n, seed))
-    if r is None:
-        base = {"uniform": (10_000, RADIUS[("uniform", 10_000, 1)]),
-                "clustered": (1_000_000, RADIUS[("clustered", 1_000_000, 2)])}[kind]
-        r = base[1] * (n / base[0]) ** (1 / 3)
-    return r
+    return C.configured_radius(kind, n, seed)
 
 
 def measured_peaks():
@@ -181,6 +169,8 @@ def dist_barrier(pg):
 
 
 def cpu_colony(workload, n_cap=1_000_000):
+    """A sample of the workload: n_cap cells of the same generator and seed,
+    the radius scaled so that the mean neighbour count stays 40."""
     kind, seed = workload["kind"], workload["seed"]
     n = min(workload["n"], n_cap)
     return C.make_colony(kind, n, seed, radius_for(kind, n, seed))
@@ -214,15 +204,16 @@ def cpu_sample(workload, threads=0, col=None):
             "sample": f"{col.n} cells of the {col.kind} generator (seed {col.seed}), {steps} step, {dt:.2f} s"}
 
 
-def run_reference_arm(args, workload, budget_s=150.0):
-    """CPU path of the reference on the host cores, one bounded sample per step;
-    the sample size keeps the whole run near budget_s."""
+def run_reference_arm(args, workload, budget_s=200.0):
+    """CPU path of the reference on the host cores, one bounded sample per step:
+    the largest sample of the workload (cells of the same generator, up to
+    the whole colony) that keeps the whole run near budget_s."""
     world, rank, local, pg = dist_setup()
     if rank != 0:
         return
-    probe = cpu_sample(workload, col=cpu_colony(workload, 100_000))
+    probe = cpu_sample(workload, col=cpu_colony(workload, 200_000))
     per_step = budget_s / max(1, args.steps + args.warmup)
-    n = int(max(20_000, min(1_000_000, workload["n"], probe["value"] * per_step)))
+    n = int(max(20_000, min(workload["n"], probe["value"] * per_step)))
     col = cpu_colony(workload, n)
     samples = []
     cb = None
@@ -237,7 +228,8 @@ def run_reference_arm(args, workload, budget_s=150.0):
             "warmup": args.warmup, "ms_per_step": col.n / value * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
             "config": {"workload": args.workload, **{k: workload[k] for k in ("kind", "n", "seed")},
-                       "sample_cells": col.n},
+                       "sample_cells": col.n,
+                       "sample": f"{col.n} of the {workload['n']} cells per step (same generator and density)"},
             "cpu_baseline": cb, "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                                         "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -517,6 +509,171 @@ def _size_bins(reqs):
     return out
 
 
+def r4(v):
+    """4 significant digits (the short line), None kept."""
+    if v is None:
+        return None
+    if isinstance(v, (int, np.integer)):
+        return int(v)
+    v = float(v)
+    return float(f"{v:.4g}") if np.isfinite(v) else None
+
+
+def neighbour_check(s, cid, col, local):
+    """Neighbour sets of the FP32 + compensated colony, evaluated from its
+    Verlet lists (built steps before), against a plain FP64 pass that searches
+    the bins on the same positions with no lists: per cell the count and the
+    fingerprint of the set within h (potential.c:39-78, dist <= h)."""
+    from timothy_gb300 import session as S
+
+    pos = s.download(cid, ["x", "y", "z"])
+    st = s.stats(cid)
+    s.set_diagnostics(True)
+    s.step(1)
+    s.sync()
+    fast = s.download(cid, ["nbcount", "nbhash"])
+    s.set_diagnostics(False)
+    at = col.copy()
+    at.x, at.y, at.z = pos["x"], pos["y"], pos["z"]
+    with S.Session(col.types, dim=3, max_slots=col.n + 64, device=local, diagnostics=True) as s64:
+        c64 = s64.add_colony(at, precision="fp64", update="none")
+        s64.step(1)
+        s64.sync()
+        ref = s64.download(c64, ["nbcount", "nbhash"])
+    bad = (fast["nbcount"] != ref["nbcount"]) | (fast["nbhash"] != ref["nbhash"])
+    return {"cells": int(col.n), "pairs_within_h": int(np.sum(ref["nbcount"].astype(np.int64))),
+            "mismatched_cells": int(np.sum(bad)), "list_age_steps": st["list_age"],
+            "against": "plain FP64 bin search on the same positions, no lists"}
+
+
+def e2e_loop(s, cid, col, steps):
+    """End to end through the public API with host buffers, as a host program
+    that drives the colony step by step: every step uploads the cells from
+    pinned host memory (the positions are the ones the previous step sent
+    back), runs one step and downloads all its results.  The upload of step
+    k + 1 waits on the device for step k's positions to reach the host and
+    overlaps the rest of step k's download."""
+    from timothy_gb300 import session as S
+
+    n = col.n
+    fields = ["x", "y", "z", "density", "v", "mindist", "fx", "fy", "fz", "removecell"]
+    res = {k: np.zeros(n, np.uint8 if k == "removecell" else np.float64) for k in fields}
+    start = s.download(cid, ["x", "y", "z"])
+    for k in ("x", "y", "z"):
+        res[k][:] = start[k]
+    fixed = [np.ascontiguousarray(a).copy() for a in (col.size, col.young, col.ctype, col.phase)]
+    pinned = list(res.values()) + fixed
+    for a in pinned:
+        S.host_register(a)
+    # the upload reads the arrays the previous download writes
+    ecol = C.Colony(res["x"], res["y"], res["z"], *fixed, col.types, 3)
+    rb0 = s.stats(cid)["list_rebuilds"]
+    s.sync()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        s.upload_async(cid, ecol)
+        s.step(1)
+        s.download_async(cid, fields, res)
+    s.sync()
+    ems = (time.perf_counter() - t0) * 1e3
+    for a in pinned:
+        S.host_unregister(a)
+    rebuilds = s.stats(cid)["list_rebuilds"] - rb0
+    return ems, rebuilds
+
+
+def scale1m_record(local, steps, args):
+    """The 1 M-cell configuration: 1,000,000 clustered cells (seed 2), plain
+    FP64 path with neighbour lists and a CIC deposit onto the 257^3 FP64 grid
+    every step: device time over `steps` steps, the CPU implementation on all
+    host cores (one step of the whole colony), and parity after 3 steps
+    against the oracle (the neighbour sets on the same positions)."""
+    from oracle import bindings
+    from timothy_gb300 import autotune as AT
+    from timothy_gb300 import session as S
+
+    n, seed = 1_000_000, 2
+    col = C.make_colony("clustered", n, seed, C.configured_radius("clustered", n, seed))
+    out = {"cells": n, "kind": "clustered", "seed": seed, "cic": "257^3 FP64 grid, GFH 8", "precision": "fp64"}
+    with S.Session(col.types, dim=3, max_slots=n + 64, device=local, list_capacity=384) as s:
+        s.set_tuning(skin_over_h=0.05)
+        cid = s.add_colony(col, precision="fp64", update="dt", dt=0.01, cic=True, verlet=True)
+        res = AT.autotune(s)
+        s.remove_colony(cid)
+        cid = s.add_colony(col, precision="fp64", update="dt", dt=0.01, cic=True, verlet=True)
+        s.step(3)
+        s.sync()
+        rb0 = s.stats(cid)["list_rebuilds"]
+        s.timer_start()
+        s.step(steps)
+        ms = s.timer_stop()
+        out.update({"steps": steps, "ms_per_step": ms / steps, "value": n * steps / (ms * 1e-3),
+                    "rebuilds": s.stats(cid)["list_rebuilds"] - rb0, "tuning": res["best"]})
+    # parity: 3 steps, GPU against the oracle
+    k = 3
+    with S.Session(col.types, dim=3, max_slots=n + 64, device=local, list_capacity=384, diagnostics=True) as s:
+        cid = s.add_colony(col, precision="fp64", update="dt", dt=0.01, cic=True, verlet=True)
+        s.step(k - 1)
+        s.sync()
+        before = s.download(cid, ["x", "y", "z"])
+        s.step(1)
+        s.sync()
+        g = s.download(cid, ["x", "y", "z", "density", "mindist", "v", "fx", "fy", "fz", "grid", "nbcount",
+                             "nbhash"])
+    if not bindings.available("oracle"):
+        bindings.build(ref=False)
+    t0 = time.perf_counter()
+    ref = bindings.run(col, k, which="oracle", update_mode=1, dt=0.01, cic=True)
+    cpu_s = time.perf_counter() - t0
+    at = col.copy()
+    at.x, at.y, at.z = before["x"], before["y"], before["z"]
+    nb = bindings.neighbours(at)
+    fscale = np.max(np.abs(np.stack([ref.fx, ref.fy, ref.fz])))
+    fin = ref.mindist < 1e300
+    out["parity_after_3_steps"] = {
+        "density_max_rel": float(np.max(np.abs(g["density"] - ref.density) / np.abs(ref.density))),
+        "mindist_max_rel": float(np.max(np.abs(g["mindist"][fin] - ref.mindist[fin]) / ref.mindist[fin])),
+        "v_max_abs": float(np.max(np.abs(g["v"] - ref.v))),
+        "force_max_rel_to_max": float(max(np.max(np.abs(g[q] - getattr(ref, q))) for q in ("fx", "fy", "fz"))
+                                      / fscale),
+        "position_max_rel": float(max(np.max(np.abs(g[q] - getattr(ref, q)) / np.maximum(np.abs(getattr(ref, q)),
+                                                                                         1.0))
+                                      for q in ("x", "y", "z"))),
+        "grid_max_rel_to_max": float(np.max(np.abs(g["grid"] - ref.grid)) / np.max(np.abs(ref.grid))),
+        "neighbour_sets_mismatched_cells": int(np.sum((g["nbcount"] != nb.count) | (g["nbhash"] != nb.hash))),
+        "oracle": f"oracle restatement on {os.cpu_count()} host threads"}
+    # the CPU implementation on all host cores, one step of the whole colony
+    if not args.no_cpu:
+        out["cpu_baseline"] = cpu_sample(WORKLOADS["scale1m"], col=col)
+        out["cpu_baseline"]["oracle_3_steps_s"] = cpu_s
+    return out
+
+
+def dropin_record(n, kind, seed, cic, steps, warmup=1):
+    """The reference's own API: the step loop of a host program over the
+    drop-ins (octbuild, patches_alloc, patches_cells2envinfo,
+    computepotential, computegradient, updatepositions, octfree) on host
+    celldata_t records, wall clock per step.  updatepositions draws the
+    caller's rand() for every cell as the reference does (cells.c:353-356)."""
+    from timothy_gb300.refabi import CELL_DTYPE, DropinRun
+
+    col = C.make_colony(kind, n, seed, C.configured_radius(kind, n, seed))
+    run = DropinRun(col, cic=cic)
+    for _ in range(warmup):
+        run.step_loop()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        run.step_loop()
+    dt = time.perf_counter() - t0
+    run.shutdown()
+    rec = CELL_DTYPE.itemsize
+    return {"cells": n, "kind": kind, "cic": cic, "steps": steps, "ms_per_step": dt / steps * 1e3,
+            "value": n * steps / dt, "unit": UNIT,
+            # per step: the records up (octbuild); density, v, mindist and the
+            # forces, then positions and removal marks down; forces and marks up
+            "h2d_bytes_per_step": n * (rec + 24 + 1), "d2h_bytes_per_step": n * (24 + 24 + 24 + 1)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -528,6 +685,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-check", action="store_true", help="skip the neighbour-set check")
+    ap.add_argument("--no-scale1m", action="store_true", help="skip the 1 M-cell FP64 + CIC record")
+    ap.add_argument("--no-dropin", action="store_true", help="skip the drop-in (reference API) record")
+    ap.add_argument("--e2e-steps", type=int, default=30)
     ap.add_argument("--list-capacity", type=int, default=384,
                     help="neighbour-list entries per cell (0: search the bins every step)")
     ap.add_argument("--rmax", type=int, default=64, help="rebuild the neighbour lists at least every rmax steps")
@@ -538,6 +699,7 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=50)
     ap.add_argument("--serve-rates", default="200,50", help="request rates (per s) of the serving runs")
     ap.add_argument("--serve-seconds", type=float, default=20.0)
+    ap.add_argument("--detail", default="", help="also write the full record (rows, forms, ...) to this file")
     ap.add_argument("--row", choices=["grid_to_cell", "cic_deposit", "diffusion", "cell_cycle"],
                     help="measure one of the rows beside the path alone and print it (no bench line)")
     args = ap.parse_args()
@@ -620,73 +782,52 @@ def main():
                 "peak_source": peak_kind, "kernel": kname, "kernel_ms": list_ms,
                 "phases_ms": {k: prof[k] for k in ("build_ms", "search_ms", "list_ms", "fix_ms", "octree_ms",
                                                    "update_ms", "cic_ms")}}
-    # the compute side of the list pass (the path is a gather-reduce: no
-    # tensor cores): pairs within h per second, from this colony's own
-    # neighbour counts, and the algorithmic FP32 flops of those pairs (the
-    # reference's expressions, about 83 flops per pair for density and force)
-    # against the nominal FP32 rate of the part (152 SMs x 128 lanes x 2 x
-    # the maximum SM clock; no measured figure exists for it)
+    detail = {"roofline": dict(roofline)}
+    # the compute side of the list pass (a gather-reduce: no tensor cores):
+    # pairs within h per second, from this colony's own neighbour counts, and
+    # the algorithmic FP32 flops of those pairs (the reference's expressions,
+    # about 83 flops per pair for density and force) against the nominal FP32
+    # rate of the part (152 SMs x 128 lanes x 2 x the maximum SM clock; no
+    # measured figure exists for it)
     nb = s.download(cid, ["nbcount"])["nbcount"]
     pairs = float(np.sum(nb.astype(np.int64)))
     if list_ms:
         fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
         pair_rate = pairs / (list_ms * 1e-3)
-        roofline["compute"] = {"pairs_within_h_per_launch": pairs, "pairs_per_s": pair_rate,
-                               "algorithmic_tflops": pair_rate * 83 / 1e12, "fp32_peak_tflops": fp32_peak,
-                               "fp32_peak_source": "nominal (152 SMs x 128 FP32 lanes x 2 x 2.07 GHz)",
-                               "frac": pair_rate * 83 / 1e12 / fp32_peak}
+        detail["roofline"]["compute"] = {
+            "pairs_within_h_per_launch": pairs, "pairs_per_s": pair_rate, "algorithmic_tflops": pair_rate * 83 / 1e12,
+            "fp32_peak_tflops": fp32_peak, "fp32_peak_source": "nominal (152 SMs x 128 FP32 lanes x 2 x 2.07 GHz)",
+            "frac": pair_rate * 83 / 1e12 / fp32_peak}
     out_fast = s.download(cid, ["x", "y", "z", "density", "fx", "fy", "fz"]) if prec == "fp32c" else None
 
-    # end to end through the public API with host buffers: per step the cells go
-    # host -> device, one step runs, the step's results come back
+    extra = {}
+    if not args.no_check and world == 1:
+        extra["neighbour_check"] = neighbour_check(s, cid, col, local)
+
     e2e = None
     if not args.no_e2e:
-        host = [np.ascontiguousarray(a).copy() for a in (col.x, col.y, col.z, col.size, col.young, col.ctype,
-                                                             col.phase)]
-        fields = ["x", "y", "z", "density", "v", "mindist", "fx", "fy", "fz", "removecell"]
-        res = {k: np.zeros(n, np.uint8 if k == "removecell" else np.float64) for k in fields}
-        pinned = host + list(res.values())
-        for a in pinned:
-            S.host_register(a)
-        ecol = C.Colony(*host, col.types, 3)
-        # 30 steps: the first upload and the last download, which nothing
-        # overlaps, are spread over enough steps to show the loop's rate
-        ke = max(2, min(args.steps, 30))
-        s.upload(cid, ecol)
-        s.step(1)
-        s.sync()
-        # pipelined: step k's upload is queued behind step k - 1's download,
-        # so the two directions of the host link overlap; every copy is in
-        # the timed region, which ends when the last results are on the host
-        t0 = time.perf_counter()
-        for _ in range(ke):
-            s.upload_async(cid, ecol)
-            s.step(1)
-            s.download_async(cid, fields, res)
-        s.sync()
-        ems = (time.perf_counter() - t0) * 1e3
-        for a in pinned:
-            S.host_unregister(a)
+        ke = max(2, args.e2e_steps)
+        ems, erb = e2e_loop(s, cid, col, ke)
         ems = dist_max(pg, ems)
         e2e = {"value": n * world * ke / (ems * 1e-3), "unit": UNIT, "h2d_bytes_per_step": n * 44,
-               "d2h_bytes_per_step": n * 73, "steps": ke, "ms_per_step": ems / ke,
-               "api": "tm_colony_upload_async + tm_session_step + tm_colony_download_async, tm_session_sync at "
-                      "the end (wall clock)"}
+               "d2h_bytes_per_step": n * 73, "steps": ke, "ms_per_step": ems / ke, "rebuilds": erb,
+               "api": "tm_colony_upload_async (positions fed back from the previous step) + tm_session_step + "
+                      "tm_colony_download_async, tm_session_sync at the end (wall clock)"}
     s.close()
 
-    extra = {}
     if prec == "fp32c" and not args.no_fp64:
         # plain FP64 path on the same colony and GPU: rate and the error of the
         # compensated path against it after the same number of steps
         s64, c64 = new_session("fp64")
         s64.step(args.warmup)
         s64.sync()
-        # the same timed steps as the compensated path (rebuilds included)
         k64 = args.steps
+        rb64 = s64.stats(c64)["list_rebuilds"]
         s64.timer_start()
         s64.step(k64)
         ms64 = s64.timer_stop()
         s64.sync()
+        rb64 = s64.stats(c64)["list_rebuilds"] - rb64
         ref = s64.download(c64, ["x", "y", "z", "density", "fx", "fy", "fz"])
         s64.close()
         ms64 = dist_max(pg, ms64)
@@ -698,7 +839,8 @@ def main():
         fscale = np.max(np.abs(f64))
         ferr = np.abs(f32 - f64) / fscale
         xerr = np.max([np.max(np.abs(out_fast[k] - ref[k])) for k in ("x", "y", "z")])
-        extra["fp64"] = {"value": v64, "ms_per_step": ms64 / k64, "steps": k64, "tuning": tuned.get("fp64")}
+        extra["fp64"] = {"value": v64, "ms_per_step": ms64 / k64, "steps": k64, "rebuilds": rb64}
+        detail["fp64_tuning"] = tuned.get("fp64")
         extra["fp32c_over_fp64"] = value / v64
         extra["error_vs_fp64"] = {
             "steps": args.warmup + args.steps, "density_max_rel": float(drel.max()),
@@ -709,29 +851,71 @@ def main():
     if not args.no_cpu and rank == 0 and world == 1:
         cpu = cpu_sample(wl)
 
+    if world == 1 and not args.no_scale1m and args.workload == "precision16m":
+        detail["scale1m"] = scale1m_record(local, 100, args)
+    if world == 1 and not args.no_dropin:
+        detail["e2e_dropin"] = {"1m_cic": dropin_record(1_000_000, "clustered", 2, True, 5)}
+        if n >= 16_000_000:
+            detail["e2e_dropin"]["16m"] = dropin_record(n, kind, seed, False, 2)
+
     if not args.no_forms and world == 1:
-        extra["rows"] = {"grid_to_cell": field_rows(local, peak), "cic_deposit": cic_rows(local, peak),
-                         "diffusion": diffusion_rows(local), "cell_cycle": cycle_rows(local)}
+        detail["rows"] = {"grid_to_cell": field_rows(local, peak), "cic_deposit": cic_rows(local, peak),
+                          "diffusion": diffusion_rows(local), "cell_cycle": cycle_rows(local)}
         forms = {"batched": batched_form(args, local)}
         forms["serving"] = [serving_form(args, local, float(r), args.serve_seconds)
                             for r in args.serve_rates.split(",") if r]
-        extra["forms"] = forms
+        detail["forms"] = forms
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+kahan (f64 positions)" if prec == "fp32c" else "f64",
             "data": "synthetic",
-            "config": {"workload": args.workload, "kind": kind, "cells": n, "seed": seed, "radius": radius,
-                       "h": 2.5, "dt": wl["dt"], "cic": wl["cic"], "precision": prec,
-                       "mean_neighbours": mean_nb, "max_neighbours": max_nb,
-                       "neighbour_lists": {"capacity": args.list_capacity, "rebuilds_in_timed_steps": rebuilds},
-                       "tuning": tuned.get(prec, {"tuning": None}),
+            "config": {"workload": args.workload, "kind": kind, "cells": n, "seed": seed, "h": 2.5, "dt": wl["dt"],
+                       "cic": wl["cic"], "precision": prec, "mean_neighbours": r4(mean_nb),
+                       "max_neighbours": max_nb, "list_capacity": args.list_capacity,
+                       "tuning": (tuned.get(prec) or {}).get("tuning"),
                        "l2": "inputs larger than L2 (state %.1f GB)" % (n * 250 / 1e9),
                        "parallelism": f"replicas x{world}"},
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk}
-    line.update(extra)
+            "roofline": {k: (r4(v) if not isinstance(v, str) else v) for k, v in roofline.items()
+                         if k not in ("phases_ms", "traffic_unit", "peak_source")},
+            "phases_ms": {k[:-3]: r4(v) for k, v in prof.items() if k.endswith("_ms") and k != "pair_ms"},
+            "rebuilds": rebuilds,
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk}
+    line["roofline"]["peak_source"] = peak_kind
+    for k in ("fp64", "fp32c_over_fp64", "error_vs_fp64", "neighbour_check"):
+        if k in extra:
+            v = extra[k]
+            line[k] = {q: r4(w) if not isinstance(w, str) else w for q, w in v.items()} if isinstance(v, dict) \
+                else r4(v)
+    if "scale1m" in detail:
+        sc = detail["scale1m"]
+        par = sc["parity_after_3_steps"]
+        line["scale1m"] = {"ms_per_step": r4(sc["ms_per_step"]), "value": r4(sc["value"]),
+                           "cpu_value": r4(sc.get("cpu_baseline", {}).get("value")),
+                           "density_err": r4(par["density_max_rel"]), "force_err": r4(par["force_max_rel_to_max"]),
+                           "grid_err": r4(par["grid_max_rel_to_max"]),
+                           "nb_mismatch": par["neighbour_sets_mismatched_cells"]}
+    if "e2e_dropin" in detail:
+        line["e2e_dropin"] = {k: {"value": r4(v["value"]), "ms_per_step": r4(v["ms_per_step"])}
+                              for k, v in detail["e2e_dropin"].items()}
+    if "forms" in detail:
+        fb = detail["forms"]["batched"]
+        line["forms"] = {"batched_fp32c": r4(fb["fp32c"]["value"]), "batched_fp64": r4(fb["fp64"]["value"]),
+                         "serving": [{"rate": r4(f["rate_per_s"]), "served": r4(f["served_cell_updates_per_s"]),
+                                      "p50": r4(f["p50_s"]), "p99": r4(f["p99_s"])}
+                                     for f in detail["forms"]["serving"]]}
     if rank == 0:
-        print(json.dumps(line), flush=True)
+        full = dict(line)
+        full.update(detail)
+        full.update(extra)
+        full["e2e_full"] = e2e
+        if args.detail:
+            with open(args.detail, "w") as f:
+                json.dump(full, f, indent=1, default=float)
+        # the full record first (one line, prefixed so it is not the bench line),
+        # then the short bench line last
+        print("detail " + json.dumps(full, default=float), flush=True)
+        print(json.dumps(line, default=float), flush=True)
     if pg is not None:
         pg.destroy_process_group()
 

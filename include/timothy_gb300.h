@@ -218,9 +218,14 @@ int tm_colony_cellcycle(tm_session *s, int id, const tm_cycle_params *p, int64_t
  * through tm_colony_upload); a cell type outside the table is read as 0 and
  * reported as TM_DEVERR_TYPES by the next tm_session_sync.  Both return once
  * the work is queued: the caller leaves in's arrays unchanged, and reads
- * out's arrays only, after tm_session_sync.  They stage through device
- * buffers of their own, 44 and 112 bytes per slot, allocated on first use
- * (not counted by tm_session_bytes). */
+ * out's arrays only, after tm_session_sync.  An asynchronous upload reads
+ * its arrays only after the positions (x, y, z) of the asynchronous download
+ * queued before it have reached the host, so a host loop may pass one step's
+ * downloaded positions to the next step's upload without waiting; the other
+ * fields of that download keep travelling while the upload runs.  They
+ * stage through device buffers of their own, 44 and 112 bytes per slot and,
+ * for a downloaded grid, one copy of the colony's grid, allocated on first
+ * use (not counted by tm_session_bytes). */
 int tm_colony_upload_async(tm_session *s, int id, const tm_colony_input *in);
 int tm_colony_download_async(tm_session *s, int id, const tm_colony_output *out);
 /* Replace the cells of an existing colony (at most the slots it holds).  With
@@ -243,6 +248,21 @@ int tm_session_sync(tm_session *s);
 
 /* Capture one step into a CUDA graph and replay it from then on (0: off). */
 int tm_session_use_graph(tm_session *s, int on);
+
+/* Diagnostics for the following steps (the session configuration's
+ * `diagnostics`, switched at run time): neighbour-set fingerprints (nbhash),
+ * v's candidate (vcand) and the octree walk of every cell.  Its arrays are
+ * allocated on first use and not counted by tm_session_bytes. */
+int tm_session_set_diagnostics(tm_session *s, int on);
+/* With diagnostics on, every following step records the neighbours within h
+ * of the sampled cells (caller indices cells[0..ncells) of colony id) as the
+ * pair kernels decide them: up to lcap caller indices per cell.  ncells = 0
+ * ends the sampling. */
+int tm_colony_sample_neighbours(tm_session *s, int id, const int64_t *cells, int64_t ncells, int lcap);
+/* The sampled lists of the last step: counts[k] neighbours within h of
+ * cells[k] (more than lcap: only lcap were kept), their caller indices at
+ * lists[k * lcap + q], q < min(counts[k], lcap), in no particular order. */
+int tm_colony_read_neighbours(tm_session *s, int id, int32_t *counts, int32_t *lists);
 
 /* Per-phase timing with CUDA events on the session stream: phase 0 build,
  * 1 search / list-build passes, 2 list passes, 3 overflow searches and the
@@ -340,8 +360,11 @@ int tm_colony_write_vtk(tm_session *s, int id, const char *path, int rank);
  * for the default stream) and allocates nothing: its scratch is a fixed
  * 3 MiB array in device memory, held by every GPU that loads the library
  * until the process exits, which limits n to 16,777,216 cells (larger n
- * returns TM_EINVAL).  The first call on a device looks up that array's
- * address; make it before any stream capture.  All calls share the array,
+ * returns TM_EINVAL).  The first call on a device, and the first call after
+ * its context was created anew (after cudaDeviceReset, or in another
+ * context), looks up that array's address; make it before any stream
+ * capture.  Only this call's own launch failures are reported (TM_ECUDA);
+ * an error left by earlier work stays for its owner to read.  All calls share the array,
  * so calls that overlap on the GPU (other streams, other host threads)
  * race and must be serialised by the caller. */
 int tm_cic_deposit_noalloc(const double *x, const double *y, const double *z, const int *phase, int64_t n,

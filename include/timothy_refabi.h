@@ -3,7 +3,8 @@
  * The functions below have exactly the signatures of the reference functions
  * they replace, so the reference step loop (main.c:67-79, step.c:41-100)
  * links against libtimothy_gb300.so unchanged once octree.c and potential.c
- * are dropped from its build.  Each runs on the GPU
+ * are dropped from its build and the replaced functions of cells.c,
+ * patches.c and fieldgradient.c are weakened.  Each runs on the GPU
  * through the device-resident session of include/timothy_gb300.h; errors
  * end in terminate() as in the reference (utils.c:103-109).
  *
@@ -283,17 +284,15 @@ void patches_cells2envinfo(systeminfo_t systeminfo, settings_t settings, patches
  * (*cellenvdata)[f][c]; frees the patch buffers as the reference does */
 void patches_applyenv2cells(systeminfo_t systeminfo, settings_t settings, patches_t *patches,
                             cellsinfo_t *cellsinfo, grid_t *grid, cellenvdata_t ***cellenvdata);
-/* fieldgradient.c:253 -- gradient of every field (one rank) */
+/* fieldgradient.c:256 -- gradient of every field (one rank) */
 void fieldgradient(systeminfo_t systeminfo, settings_t settings, environment_t **environment, grid_t *grid);
 
-/* Releases the device session the drop-ins keep between calls (no
- * counterpart in the reference; optional at exit). */
 /* cells.c:370 -- cell cycle with mitosis of every local cell (one rank);
  * cells.c:290 -- removal of the marked cells */
 int updatecellcycles(systeminfo_t systeminfo, settings_t settings, celltype_t *celltype, cellsinfo_t *cellsinfo,
                      cellenvdata_t **cellenvdata, unsigned char *removecell, int64_t *removecount);
 void cellsdeath(int oldlnc, cellsinfo_t *cellsinfo, unsigned char *removecell, int64_t removecount);
-/* environment.c:33, 58, 131, 516 -- the fields without Hypre: allocation,
+/* environment.c:33, 56, 131, 515 -- the fields without Hypre: allocation,
  * initial values, (nothing to) set up, and the implicit diffusion step on the
  * GPU.  solverdata_t / solversettings_t (global.h:366-392, Hypre handles) are
  * never touched, so they are passed as untyped pointers. */
@@ -310,6 +309,8 @@ int tm_dropin_env_solution(int field, double *out);
 /* 1: environment_compute also copies the solution into environment[f].data
  * (the reference leaves data unchanged, environment.c:495-507) */
 void tm_dropin_set_env_writeback(int on);
+/* Releases the device session the drop-ins keep between calls (no
+ * counterpart in the reference; optional at exit). */
 void tm_dropin_shutdown(void);
 
 #ifdef __cplusplus

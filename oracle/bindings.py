@@ -28,13 +28,18 @@ _P = C.c_void_p
 _cache: dict[str, C.CDLL] = {}
 
 
-def build(ref: bool | None = None) -> None:
-    """Compile the restatement; also the reference library when its sources exist."""
+def build(ref: bool | None = None, refsrc: str | None = None) -> None:
+    """Compile the restatement; also the reference library when its sources
+    are given (``refsrc`` or the TM_REFSRC environment variable: the
+    reference's src/ directory).  ref=None builds it when they exist."""
     subprocess.run(["make", "-s", "-B", "-C", HERE, "liboracle.so"], check=True)
-    refsrc = os.environ.get("TM_REFSRC", "/root/reference/src")
+    refsrc = refsrc or os.environ.get("TM_REFSRC", "")
+    have = bool(refsrc) and os.path.isfile(os.path.join(refsrc, "octree.c"))
     if ref is None:
-        ref = os.path.isdir(refsrc)
+        ref = have
     if ref:
+        if not have:
+            raise RuntimeError("building the reference needs its src/ directory: pass refsrc= or set TM_REFSRC")
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REFSRC={refsrc}"], check=True)
 
 

@@ -25,6 +25,13 @@ import numpy as np
 H_DEFAULT = 2.5
 R0_DEFAULT = 1.0
 MEAN_NEIGHBOURS = 40.0
+# Radii of the configured colonies that give a mean of 40 neighbours within
+# h = 2.5, bisected with full-size neighbour counts: (kind, cells, seed) -> R.
+CALIBRATED_RADIUS = {
+    ("uniform", 10_000, 1): 15.256856463570728,
+    ("clustered", 1_000_000, 2): 76.3271427172167,
+    ("clustered", 16_000_000, 3): 192.68257233787858,
+}
 
 
 @dataclass
@@ -137,6 +144,17 @@ def initial_radius(kind: str, n: int, h: float = H_DEFAULT, mean: float = MEAN_N
         r = (3.0 * n / (4.0 * math.pi * rho)) ** (1.0 / 3.0)
     if kind == "clustered":
         r *= 1.35
+    return r
+
+
+def configured_radius(kind: str, n: int, seed: int) -> float:
+    """The calibrated radius of a configured colony, else the calibrated one of
+    the same generator scaled by n^(1/3)."""
+    r = CALIBRATED_RADIUS.get((kind, n, seed))
+    if r is None:
+        base = {"uniform": (10_000, CALIBRATED_RADIUS[("uniform", 10_000, 1)]),
+                "clustered": (1_000_000, CALIBRATED_RADIUS[("clustered", 1_000_000, 2)])}[kind]
+        r = base[1] * (n / base[0]) ** (1 / 3)
     return r
 
 

@@ -89,6 +89,13 @@ struct tm_arrays {
     int ncol;
     long long nslots_total;
     int want_diag;       // fill nbcount/nbhash/vcand
+    // diagnostics: the neighbour lists of sampled cells.  diag_row[off + caller
+    // index] is the cell's row in diag_nb (-1: not sampled); diag_cnt[row]
+    // counts its neighbours within h this step (zeroed at the step's start).
+    int *diag_row;
+    int *diag_cnt;
+    int *diag_nb;        // caller indices, diag_lcap per row, in no particular order
+    int diag_lcap;
 };
 
 // slot i holds a live cell of colony d (unsigned: slots below the colony's

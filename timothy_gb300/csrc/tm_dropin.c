@@ -455,7 +455,7 @@ static tm_diffusion *g_diff;
 static int64_t g_diff_gs[3];
 static int g_env_writeback;
 
-/* environment.c:33-56 without the solver's own arrays */
+/* environment.c:33-55 without the solver's own arrays */
 void environment_allocate(systeminfo_t systeminfo, settings_t settings, grid_t grid, environment_t **environment,
                           void *solverdata, void *solversettings)
 {
@@ -475,8 +475,11 @@ void environment_allocate(systeminfo_t systeminfo, settings_t settings, grid_t g
     (void)systeminfo;
 }
 
-/* environment.c:58-74: mean + rand() / RAND_MAX * variance per node in the
- * reference's order (the caller's generator advances as the reference's does) */
+/* environment.c:56-72: mean + rand() / RAND_MAX * variance per node.  The
+ * loop order and the conversion of each value are the reference's on
+ * purpose: the host program's rand() stream is consumed here, so a seeded
+ * run must take the same values in the same order, node for node, for its
+ * fields and for every later draw (cell cycle, random move) to match. */
 void environment_init(systeminfo_t systeminfo, settings_t settings, grid_t grid, environment_t **environment)
 {
     (void)systeminfo;

@@ -21,24 +21,68 @@
 // 6 int64 per block (lower x,y,z, upper x,y,z) = 3 MiB per GPU
 static __device__ __align__(256) long long g_cic_scratch[NOALLOC_MAX_BLOCKS * 6];
 
-// Host-side table of the scratch's device address, filled once per device.
-// The symbol itself is only a host-side stand-in for the device array and
-// must never be passed to a kernel.
+// Host-side table of the scratch's device address, filled once per device
+// and CUDA context.  The symbol itself is only a host-side stand-in for the
+// device array and must never be passed to a kernel.  A context that is
+// destroyed and created again (cudaDeviceReset, or a caller switching to
+// another context on the same device) loads the module anew, possibly at
+// another address, so each entry remembers the context it was taken in and is
+// looked up again when the current context differs.
+struct scratch_slot {
+    unsigned long long ctx_id;   // 0: no context identity (looked up on every call)
+    long long *ptr;
+};
 static std::mutex g_setup_mutex;
-static long long *g_scratch_dev[64];
+static scratch_slot g_scratch_dev[64];
+
+typedef int (*ctx_get_current_fn)(void **);
+typedef int (*ctx_get_id_fn)(void *, unsigned long long *);
+
+// identity of the calling thread's current context, 0 when the driver does not
+// provide one (cuCtxGetCurrent / cuCtxGetId through the runtime's entry-point
+// query, so the library need not link the driver library)
+static unsigned long long current_context_id()
+{
+    static ctx_get_current_fn get_current = nullptr;
+    static ctx_get_id_fn get_id = nullptr;
+    static bool queried = false;
+    if (!queried) {
+        void *f1 = nullptr, *f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1, q2;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) ==
+                cudaSuccess &&
+            q1 == cudaDriverEntryPointSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) == cudaSuccess &&
+            q2 == cudaDriverEntryPointSuccess) {
+            get_current = (ctx_get_current_fn)f1;
+            get_id = (ctx_get_id_fn)f2;
+        }
+        queried = true;
+    }
+    if (!get_current || !get_id) return 0;
+    void *ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+    return id;
+}
 
 static int scratch_for_current_device(long long **out)
 {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return TM_ENODEV;
+    // cudaSetDevice makes the device's context current, creating it if needed
+    if (cudaSetDevice(dev) != cudaSuccess) return TM_ECUDA;
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_dev[dev]) {
+    const unsigned long long ctx = current_context_id();
+    scratch_slot &slot = g_scratch_dev[dev];
+    if (!slot.ptr || ctx == 0 || slot.ctx_id != ctx) {
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_cic_scratch);
         if (e != cudaSuccess || !p) return TM_ECUDA;
-        g_scratch_dev[dev] = (long long *)p;
+        slot.ptr = (long long *)p;
+        slot.ctx_id = ctx;
     }
-    *out = g_scratch_dev[dev];
+    *out = slot.ptr;
     return TM_OK;
 }
 
@@ -154,13 +198,30 @@ extern "C" int tm_cic_deposit_noalloc(const double *x, const double *y, const do
     if (rc != TM_OK) return rc;
     cudaStream_t st = (cudaStream_t)stream;
     const size_t gbytes = (size_t)(gsize[0] * gsize[1] * gsize[2]) * sizeof(double);
+    // Every step's own return code is checked, not the thread's last-error
+    // state: an error left there by earlier, unrelated work is neither
+    // reported as this call's failure nor cleared.
     // patches_cells2envinfo zeroes the patch before depositing (patches.c:165-170)
     if (cudaMemsetAsync(grid, 0, gbytes, st) != cudaSuccess) return TM_ECUDA;
-    const int nblocks = n > 0 ? (int)((n + NOALLOC_BLOCK - 1) / NOALLOC_BLOCK) : 0;
-    if (nblocks > 0)
-        k_cic_noalloc<<<nblocks, NOALLOC_BLOCK, 0, st>>>(x, y, z, phase, n, dimension, lower[0], lower[1], lower[2],
-                                                        resolution, (int)gsize[0], (int)gsize[1], (int)gsize[2],
-                                                        grid, scratch);
-    k_cic_noalloc_box<<<1, 256, 0, st>>>(scratch, nblocks, dimension, (long long *)corners);
-    return cudaGetLastError() == cudaSuccess ? TM_OK : TM_ECUDA;
+    int nblocks = n > 0 ? (int)((n + NOALLOC_BLOCK - 1) / NOALLOC_BLOCK) : 0;
+    if (nblocks > 0) {
+        long long nn = (long long)n;
+        int dim = dimension;
+        double lx = lower[0], ly = lower[1], lz = lower[2];
+        float res = resolution;
+        int gx = (int)gsize[0], gy = (int)gsize[1], gz = (int)gsize[2];
+        void *args[] = {(void *)&x, (void *)&y, (void *)&z, (void *)&phase, &nn, &dim, &lx, &ly, &lz, &res,
+                        &gx, &gy, &gz, (void *)&grid, (void *)&scratch};
+        if (cudaLaunchKernel((const void *)k_cic_noalloc, dim3((unsigned)nblocks), dim3(NOALLOC_BLOCK), args, 0,
+                             st) != cudaSuccess)
+            return TM_ECUDA;
+    }
+    {
+        int dim = dimension;
+        long long *cor = (long long *)corners;
+        void *args[] = {(void *)&scratch, &nblocks, &dim, (void *)&cor};
+        if (cudaLaunchKernel((const void *)k_cic_noalloc_box, dim3(1), dim3(256), args, 0, st) != cudaSuccess)
+            return TM_ECUDA;
+    }
+    return TM_OK;
 }

@@ -192,6 +192,24 @@ __device__ __forceinline__ void pair_store(const tm_arrays &a, long long i, pair
     if (a.want_diag) a.nbhash[i] = hash;
 }
 
+// Diagnostics of one pair within h: the set's fingerprint and, for a sampled
+// cell (row >= 0), the neighbour's caller index in the cell's list.
+__device__ __forceinline__ void diag_pair(const tm_arrays &a, int row, long long j, unsigned long long &hash)
+{
+    const unsigned long long pj = (unsigned long long)a.perm[j];
+    hash += tm_mix64(pj + 1ull);
+    if (row >= 0) {
+        const int q = atomicAdd(a.diag_cnt + row, 1);
+        if (q < a.diag_lcap) a.diag_nb[(long long)row * a.diag_lcap + q] = (int)pj;
+    }
+}
+
+// sample row of cell i of colony d (diagnostics), -1 if none
+__device__ __forceinline__ int diag_row_of(const tm_arrays &a, const tm_desc &d, long long i)
+{
+    return (a.want_diag && a.diag_row) ? a.diag_row[d.off + a.perm[i]] : -1;
+}
+
 // one warp, one group of PAIR_CPW Morton-consecutive slots starting at base
 template <int PREC>
 __device__ __forceinline__ void pair_group(const tm_arrays &a, const tm_consts *K, int fallback, int lshift,
@@ -266,6 +284,7 @@ __device__ __forceinline__ void pair_group(const tm_arrays &a, const tm_consts *
 
     // FP64 data of the own cell (plain path and band rechecks)
     const double xi = live ? a.x[i] : 0.0, yi = live ? a.y[i] : 0.0, zi = live ? a.z[i] : 0.0;
+    const int drow = live ? diag_row_of(a, d, i) : -1;
     pair_acc<PREC> acc;
     acc.init();
     int cnt_nb = 0;
@@ -289,7 +308,7 @@ __device__ __forceinline__ void pair_group(const tm_arrays &a, const tm_consts *
                 if (in) {
                     cnt_nb++;
                     nbmin = min(nbmin, j);
-                    if (a.want_diag) hash += tm_mix64((unsigned long long)a.perm[j] + 1ull);
+                    if (a.want_diag) diag_pair(a, drow, j, hash);
                 }
             } else {
                 const float4 B = tB[ti];
@@ -301,7 +320,7 @@ __device__ __forceinline__ void pair_group(const tm_arrays &a, const tm_consts *
                     pair32(T, dim, dx, dy, dz, s, B.w, acc);
                     cnt_nb++;
                     nbmin = min(nbmin, j);
-                    if (a.want_diag) hash += tm_mix64((unsigned long long)a.perm[j] + 1ull);
+                    if (a.want_diag) diag_pair(a, drow, j, hash);
                 }
             }
         }
@@ -577,7 +596,7 @@ __global__ void __launch_bounds__(256) k_listbuild(tm_arrays a, const tm_consts 
 template <int PREC>
 __device__ __forceinline__ void plist_one(const tm_arrays &a, const tm_type &T, int dim, int t, long long i,
                                           float4 hi_i, float4 lo_i, int j, float4 hj, float4 lj, pair_acc<PREC> &acc,
-                                          int &cnt_nb, int &nbmin, unsigned long long &hash)
+                                          int &cnt_nb, int &nbmin, unsigned long long &hash, int drow)
 {
     bool in;
     if constexpr (PREC == 0) {
@@ -594,7 +613,7 @@ __device__ __forceinline__ void plist_one(const tm_arrays &a, const tm_type &T, 
     if (in) {
         cnt_nb++;
         nbmin = min(nbmin, PREC == 0 ? a.rank[j] : __float_as_int(lj.w));
-        if (a.want_diag) hash += tm_mix64((unsigned long long)a.perm[j] + 1ull);
+        if (a.want_diag) diag_pair(a, drow, j, hash);
     }
 }
 
@@ -622,6 +641,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_plist(tm_arrays a, const tm_con
     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
     const int cnt = __ldg(a.vcount + i);
     const long long ls = a.lstride;
+    const int drow = diag_row_of(a, d, i);
     const int *__restrict__ lst = a.vlist + i;
     int k = 0;
     for (; k + 1 < cnt; k += 2, lst += 2 * ls) {
@@ -629,13 +649,13 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_plist(tm_arrays a, const tm_con
         const int j1 = __ldg(lst + ls);
         const float4 h0 = PREC ? __ldg(hi + j0) : z4, l0 = PREC ? __ldg(lo + j0) : z4;
         const float4 h1 = PREC ? __ldg(hi + j1) : z4, l1 = PREC ? __ldg(lo + j1) : z4;
-        plist_one<PREC>(a, T, dim, t, i, hi_i, lo_i, j0, h0, l0, acc, cnt_nb, nbmin, hash);
-        plist_one<PREC>(a, T, dim, t, i, hi_i, lo_i, j1, h1, l1, acc, cnt_nb, nbmin, hash);
+        plist_one<PREC>(a, T, dim, t, i, hi_i, lo_i, j0, h0, l0, acc, cnt_nb, nbmin, hash, drow);
+        plist_one<PREC>(a, T, dim, t, i, hi_i, lo_i, j1, h1, l1, acc, cnt_nb, nbmin, hash, drow);
     }
     if (k < cnt) {
         const int j0 = __ldg(lst);
         const float4 h0 = PREC ? __ldg(hi + j0) : z4, l0 = PREC ? __ldg(lo + j0) : z4;
-        plist_one<PREC>(a, T, dim, t, i, hi_i, lo_i, j0, h0, l0, acc, cnt_nb, nbmin, hash);
+        plist_one<PREC>(a, T, dim, t, i, hi_i, lo_i, j0, h0, l0, acc, cnt_nb, nbmin, hash, drow);
     }
     pair_store<PREC>(a, i, acc, cnt_nb, nbmin, hash, false);
     // the octree walk's first pass for this cell (see k_octree_mark): walk if

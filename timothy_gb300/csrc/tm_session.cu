@@ -136,9 +136,11 @@ struct tm_session {
     unsigned char *up_stage = nullptr;    // x, y, z, size (8 B), young, ctype, phase (4 B) per slot
     unsigned char *dl_stage = nullptr;    // the downloaded fields, 8 B per slot each, and the inverse permutation
     unsigned char *up_rec = nullptr;      // an upload's cells as 48-byte records (caller order)
-    size_t up_bytes = 0, dl_bytes = 0, rec_bytes = 0;
+    double *dl_grid = nullptr;            // the grid of an asynchronous download (one colony's grid)
+    size_t up_bytes = 0, dl_bytes = 0, rec_bytes = 0, dl_grid_bytes = 0;
     cudaEvent_t ev_up_read = nullptr;     // k_upload_pack has read up_stage
     cudaEvent_t ev_dl_gathered = nullptr, ev_dl_copied = nullptr;
+    cudaEvent_t ev_dl_pos = nullptr;      // the positions of the last asynchronous download are on the host
     bool dl_pending = false, up_pending = false;
     cudaEvent_t ev_ready[2] = {nullptr, nullptr}, ev_copied[2] = {nullptr, nullptr};
     // profiling
@@ -169,6 +171,9 @@ struct tm_session {
     size_t move_cap = 0;
     tm_tuning tune{1, 1, 128, 0.1f, 64};
     cudaEvent_t tstart = nullptr, tstop = nullptr;
+    // diagnostics: sampled neighbour lists (tm_colony_sample_neighbours)
+    int diag_col = -1;
+    long long diag_ncells = 0;
 };
 
 // ---------------------------------------------------------------------------
@@ -393,6 +398,7 @@ static int enqueue_build(tm_session *s, int p, int &nk)
     CK(cudaMemsetAsync(a.bin_cursor, 0, (size_t)(nbin + 1) * sizeof(uint32_t), st));
     CK(cudaMemsetAsync(a.bigbins, 0, sizeof(int), st));
     CK(cudaMemsetAsync(a.fix_count, 0, 5 * sizeof(int), st));   // fix count and the four work counters
+    if (a.diag_cnt) CK(cudaMemsetAsync(a.diag_cnt, 0, (size_t)s->diag_ncells * sizeof(int), st));
     k_step_init<<<blocks_for(ncol, 128), 128, 0, st>>>(a);
     CK(tm_launch_bbox(a, s->K.ntypes, st));
     k_frame<<<blocks_for(ncol, 128), 128, 0, st>>>(a, s->dK);
@@ -721,7 +727,7 @@ extern "C" int tm_session_destroy(tm_session *s)
                     a.young2, a.ctype2, a.phase2, a.perm2, a.rem2, a.col, a.code, a.codes, a.bin, a.tmp, a.rank, a.hi, a.lo, a.vlist, a.vcount, a.x0,
                     a.mass, a.bin_count, a.bin_cursor, a.bin_start, a.bigbins, a.fix_count, a.fix_list, a.walk_list, a.density, a.v, a.mindist, a.fx,
                     a.fy, a.fz, a.nbcount, a.nbmin, a.nbhash, a.vcand, a.grid, a.desc, a.frame, s->scan_tmp, s->scan_tmp_slots, s->d_octsize,
-                    s->dK, s->d_scratch, s->d_scratch2, s->d_flag};
+                    s->dK, s->d_scratch, s->d_scratch2, s->d_flag, a.diag_row, a.diag_cnt, a.diag_nb};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (auto ev : s->evpool) cudaEventDestroy(ev);
@@ -743,10 +749,11 @@ extern "C" int tm_session_destroy(tm_session *s)
     if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
     if (s->h2d_stream) cudaStreamDestroy(s->h2d_stream);
     if (s->ev_h2d) cudaEventDestroy(s->ev_h2d);
-    for (cudaEvent_t e : {s->ev_up_read, s->ev_dl_gathered, s->ev_dl_copied})
+    for (cudaEvent_t e : {s->ev_up_read, s->ev_dl_gathered, s->ev_dl_copied, s->ev_dl_pos})
         if (e) cudaEventDestroy(e);
     if (s->up_stage) cudaFree(s->up_stage);
     if (s->dl_stage) cudaFree(s->dl_stage);
+    if (s->dl_grid) cudaFree(s->dl_grid);
     if (s->up_rec) cudaFree(s->up_rec);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
@@ -981,12 +988,15 @@ static int lookup(tm_session *s, int id)
     return TM_OK;
 }
 
+static void drop_sample(tm_session *s);
+
 extern "C" int tm_colony_remove(tm_session *s, int id)
 {
     int rc = lookup(s, id);
     if (rc) return rc;
     CK(cudaSetDevice(s->device));
     CK(cudaStreamSynchronize(s->stream));
+    if (s->diag_col == id) drop_sample(s);
     colony_host &c = s->cols[id];
     s->h_desc[id].active = 0;
     s->h_desc[id].n = 0;
@@ -1042,7 +1052,7 @@ static int async_io_init(tm_session *s)
     int rc = download_streams(s);
     if (rc) return rc;
     CK(cudaStreamCreateWithFlags(&s->h2d_stream, cudaStreamNonBlocking));
-    for (cudaEvent_t *e : {&s->ev_h2d, &s->ev_up_read, &s->ev_dl_gathered, &s->ev_dl_copied})
+    for (cudaEvent_t *e : {&s->ev_h2d, &s->ev_up_read, &s->ev_dl_gathered, &s->ev_dl_copied, &s->ev_dl_pos})
         CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     return TM_OK;
 }
@@ -1080,6 +1090,9 @@ extern "C" int tm_colony_upload_async(tm_session *s, int id, const tm_colony_inp
     const size_t n = (size_t)in->n;
     cudaStream_t h = s->h2d_stream;
     if (s->up_pending) CK(cudaStreamWaitEvent(h, s->ev_up_read, 0));
+    // the positions of the asynchronous download queued before this upload
+    // reach the host first, so a loop may pass them to this upload
+    if (s->dl_pending) CK(cudaStreamWaitEvent(h, s->ev_dl_pos, 0));
     CK(cudaMemcpyAsync(X + o, in->x, n * 8, cudaMemcpyHostToDevice, h));
     CK(cudaMemcpyAsync(Y + o, in->y, n * 8, cudaMemcpyHostToDevice, h));
     CK(cudaMemcpyAsync(Z + o, in->z, n * 8, cudaMemcpyHostToDevice, h));
@@ -1206,7 +1219,10 @@ static int run_step_graph(tm_session *s)
         CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
         int rc = enqueue_step(s);
         cudaError_t e = cudaStreamEndCapture(s->stream, &g);
-        if (rc) return rc;
+        if (rc) {
+            if (e == cudaSuccess) cudaGraphDestroy(g);
+            return rc;
+        }
         if (e != cudaSuccess) return tm_fail(TM_ECUDA, "graph capture: %s", cudaGetErrorString(e));
         e = cudaGraphInstantiate(&s->gexec[p], g, 0);
         cudaGraphDestroy(g);
@@ -1258,6 +1274,84 @@ extern "C" int tm_session_use_graph(tm_session *s, int on)
     if (!s) return tm_fail(TM_EINVAL, "null session");
     s->use_graph = on != 0;
     if (!on) drop_graphs(s);
+    return TM_OK;
+}
+
+extern "C" int tm_session_set_diagnostics(tm_session *s, int on)
+{
+    if (!s) return tm_fail(TM_EINVAL, "null session");
+    CK(cudaSetDevice(s->device));
+    CK(cudaStreamSynchronize(s->stream));
+    if (on && !s->A.nbhash) {
+        const long long S = ((s->cfg.max_slots + 31) / 32) * 32;
+        if (dalloc(&s->A.nbhash, S) != TM_OK || dalloc(&s->A.vcand, S) != TM_OK)
+            return tm_fail(TM_ENOMEM, "diagnostics arrays");
+        CK(cudaMemsetAsync(s->A.nbhash, 0, (size_t)S * sizeof(unsigned long long), s->stream));
+        CK(cudaMemsetAsync(s->A.vcand, 0xff, (size_t)S * sizeof(int), s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+    }
+    s->A.want_diag = on ? 1 : 0;
+    s->cfg.diagnostics = on ? 1 : 0;
+    drop_graphs(s);
+    return TM_OK;
+}
+
+static void drop_sample(tm_session *s)
+{
+    for (int **p : {&s->A.diag_row, &s->A.diag_cnt, &s->A.diag_nb})
+        if (*p) {
+            cudaFree(*p);
+            *p = nullptr;
+        }
+    s->A.diag_lcap = 0;
+    s->diag_col = -1;
+    s->diag_ncells = 0;
+}
+
+extern "C" int tm_colony_sample_neighbours(tm_session *s, int id, const int64_t *cells, int64_t ncells, int lcap)
+{
+    int rc = lookup(s, id);
+    if (rc) return rc;
+    if (ncells < 0 || (ncells > 0 && (!cells || lcap <= 0))) return tm_fail(TM_EINVAL, "bad sample");
+    if (ncells > 0 && !s->A.want_diag) return tm_fail(TM_EINVAL, "sampled neighbour lists need diagnostics on");
+    CK(cudaSetDevice(s->device));
+    CK(cudaStreamSynchronize(s->stream));
+    drop_sample(s);
+    drop_graphs(s);
+    if (ncells == 0) return TM_OK;
+    const colony_host &c = s->cols[id];
+    std::vector<int> rows((size_t)c.n, -1);
+    for (int64_t k = 0; k < ncells; k++) {
+        if (cells[k] < 0 || cells[k] >= c.n) return tm_fail(TM_EINVAL, "sampled cell %lld outside the colony",
+                                                            (long long)cells[k]);
+        rows[(size_t)cells[k]] = (int)k;
+    }
+    const long long S = ((s->cfg.max_slots + 31) / 32) * 32;
+    if (dalloc(&s->A.diag_row, S) != TM_OK || dalloc(&s->A.diag_cnt, ncells) != TM_OK ||
+        dalloc(&s->A.diag_nb, ncells * (long long)lcap) != TM_OK) {
+        drop_sample(s);
+        return tm_fail(TM_ENOMEM, "sampled neighbour lists");
+    }
+    CK(cudaMemset(s->A.diag_row, 0xff, (size_t)S * sizeof(int)));
+    if (c.n > 0) CK(cudaMemcpy(s->A.diag_row + c.off, rows.data(), (size_t)c.n * sizeof(int), cudaMemcpyHostToDevice));
+    CK(cudaMemset(s->A.diag_cnt, 0, (size_t)ncells * sizeof(int)));
+    s->A.diag_lcap = lcap;
+    s->diag_col = id;
+    s->diag_ncells = ncells;
+    return TM_OK;
+}
+
+extern "C" int tm_colony_read_neighbours(tm_session *s, int id, int32_t *counts, int32_t *lists)
+{
+    int rc = lookup(s, id);
+    if (rc) return rc;
+    if (s->diag_col != id || !counts) return tm_fail(TM_EINVAL, "no neighbour sample on this colony");
+    CK(cudaSetDevice(s->device));
+    CK(cudaStreamSynchronize(s->stream));
+    CK(cudaMemcpy(counts, s->A.diag_cnt, (size_t)s->diag_ncells * sizeof(int), cudaMemcpyDeviceToHost));
+    if (lists)
+        CK(cudaMemcpy(lists, s->A.diag_nb, (size_t)s->diag_ncells * (size_t)s->A.diag_lcap * sizeof(int),
+                      cudaMemcpyDeviceToHost));
     return TM_OK;
 }
 
@@ -1411,12 +1505,34 @@ static int download_async_queue(tm_session *s, int id, const tm_colony_output *o
         }
         CK(cudaGetLastError());
     }
+    // the grid goes through staging of its own too: the next step clears and
+    // deposits the session grid while this copy may still be running
+    const bool want_grid = out->grid && c.gridoff >= 0 && c.ngrid > 0;
+    if (want_grid) {
+        const size_t gb = sizeof(double) * (size_t)c.ngrid;
+        if (s->dl_grid_bytes < gb) {
+            CK(cudaStreamSynchronize(s->copy_stream));
+            if (s->dl_grid) CK(cudaFree(s->dl_grid));
+            s->dl_grid = nullptr;
+            s->dl_grid_bytes = 0;
+            CK(cudaMalloc((void **)&s->dl_grid, gb));
+            s->dl_grid_bytes = gb;
+        }
+        CK(cudaMemcpyAsync(s->dl_grid, a.grid + c.gridoff, gb, cudaMemcpyDeviceToDevice, s->stream));
+    }
     CK(cudaEventRecord(s->ev_dl_gathered, s->stream));
     CK(cudaStreamWaitEvent(s->copy_stream, s->ev_dl_gathered, 0));
-    for (auto &cp : copies)
-        CK(cudaMemcpyAsync(cp.first, cp.second.first, cp.second.second, cudaMemcpyDeviceToHost, s->copy_stream));
-    if (out->grid && c.gridoff >= 0)
-        CK(cudaMemcpyAsync(out->grid, a.grid + c.gridoff, sizeof(double) * (size_t)c.ngrid, cudaMemcpyDeviceToHost,
+    // positions first (the parts of x, y, z come first in the staging), then
+    // the event a following asynchronous upload waits for
+    const int npos = (out->x ? 1 : 0) + (out->y ? 1 : 0) + (out->z ? 1 : 0);
+    for (size_t k = 0; k < copies.size(); k++) {
+        CK(cudaMemcpyAsync(copies[k].first, copies[k].second.first, copies[k].second.second, cudaMemcpyDeviceToHost,
+                           s->copy_stream));
+        if ((int)k + 1 == npos) CK(cudaEventRecord(s->ev_dl_pos, s->copy_stream));
+    }
+    if (npos == 0 || copies.empty()) CK(cudaEventRecord(s->ev_dl_pos, s->copy_stream));
+    if (want_grid)
+        CK(cudaMemcpyAsync(out->grid, s->dl_grid, sizeof(double) * (size_t)c.ngrid, cudaMemcpyDeviceToHost,
                            s->copy_stream));
     CK(cudaEventRecord(s->ev_dl_copied, s->copy_stream));
     s->dl_pending = true;

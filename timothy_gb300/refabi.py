@@ -169,6 +169,20 @@ def grid_geometry(dim: int, gfh: float):
     return (sx, sx, sz), lower
 
 
+def free_patches(p):
+    """Free what patches_alloc allocated for one rank (the C library's free)."""
+    libc = C.CDLL(None)
+    libc.free.argtypes = [C.c_void_p]
+    libc.free.restype = None
+    if p.data:
+        libc.free(C.cast(p.data[0], C.c_void_p))
+    for k in ("data", "intersect", "lowercorner", "uppercorner", "lowercornerR", "uppercornerR", "size"):
+        ptr = getattr(p, k)
+        if ptr:
+            libc.free(C.cast(ptr, C.c_void_p))
+        setattr(p, k, None)
+
+
 class DropinRun:
     """The reference step loop on host celldata_t cells, through the drop-ins."""
 
@@ -275,6 +289,33 @@ class DropinRun:
         lib.octfree(C.byref(self.ci))
         aff = double3dv_t.in_dll(lib, "affShift")
         self.aff = np.array([aff.x, aff.y, aff.z, C.c_double.in_dll(lib, "affScale").value])
+
+    def step_loop(self, update: bool = True):
+        """One step of the reference loop as a host program makes it, and
+        nothing else: octbuild, patches_alloc + patches_cells2envinfo (with a
+        grid), computepotential, computeremotepotential, computegradient,
+        computeremotegradient, updatepositions, octfree (main.c:67-79,
+        step.c:41-100).  At one rank the host's own patches_applycells2env
+        then adds the patch into its grid and frees the patch buffers
+        (patches.c:321-367); here the buffers are only freed."""
+        lib = self.lib
+        ct = self.celltype
+        lib.octbuild(self.si, C.byref(self.ci), ct)
+        p = None
+        if self.cic:
+            p = patches_t()
+            lib.patches_alloc(self.si, self.st, C.byref(p), C.byref(self.ci), C.byref(self.grid))
+            lib.patches_cells2envinfo(self.si, self.st, C.byref(p), C.byref(self.ci), C.byref(self.grid))
+        lib.computepotential(self.si, C.byref(self.ci), ct, self.cc)
+        lib.computeremotepotential(self.si, C.byref(self.ci), ct, self.cc)
+        lib.computegradient(self.si, C.byref(self.ci), ct, self.cc)
+        lib.computeremotegradient(self.si, C.byref(self.ci), ct, self.cc)
+        if update:
+            lib.updatepositions(self.st, ct, C.byref(self.ci), self.removecell.ctypes.data,
+                                C.byref(self.removecount))
+        lib.octfree(C.byref(self.ci))
+        if p is not None:
+            free_patches(p)
 
     COUNT_FIELDS = ("n", "g0phase", "g1phase", "sphase", "g2phase", "mphase", "necroticphase")
 

@@ -148,6 +148,9 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "tm_session_set_tuning": (C.c_int, [P, C.POINTER(_Tuning)]),
         "tm_host_register": (C.c_int, [P, C.c_int64]),
         "tm_host_unregister": (C.c_int, [P]),
+        "tm_session_set_diagnostics": (C.c_int, [P, C.c_int]),
+        "tm_colony_sample_neighbours": (C.c_int, [P, C.c_int, P, C.c_int64, C.c_int]),
+        "tm_colony_read_neighbours": (C.c_int, [P, C.c_int, P, P]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -444,6 +447,33 @@ class Session:
 
     def profile(self, on: bool = True):
         _check(load_library().tm_session_profile(self._h, 1 if on else 0))
+
+    def set_diagnostics(self, on: bool = True):
+        """Neighbour-set fingerprints, v candidates and every cell's octree walk
+        for the following steps."""
+        _check(load_library().tm_session_set_diagnostics(self._h, 1 if on else 0))
+        self.diagnostics = bool(on)
+
+    def sample_neighbours(self, cid: int, cells, lcap: int = 512):
+        """Record, in each following step, the neighbours within h of the given
+        cells (caller indices) as the pair kernels decide them."""
+        c = np.ascontiguousarray(cells, np.int64)
+        self._sample = (cid, len(c), int(lcap))
+        _check(load_library().tm_colony_sample_neighbours(self._h, cid, _p(c) if len(c) else None, len(c),
+                                                          int(lcap)))
+
+    def read_neighbours(self, cid: int) -> list:
+        """The sampled cells' neighbour lists of the last step, each sorted
+        (caller indices)."""
+        scid, m, lcap = self._sample
+        if scid != cid:
+            raise ValueError("no neighbour sample on this colony")
+        cnt = np.zeros(max(m, 1), np.int32)
+        lst = np.zeros(max(m * lcap, 1), np.int32)
+        _check(load_library().tm_colony_read_neighbours(self._h, cid, _p(cnt), _p(lst)))
+        if np.any(cnt[:m] > lcap):
+            raise RuntimeError(f"a sampled cell has more than {lcap} neighbours")
+        return [np.sort(lst[k * lcap:k * lcap + cnt[k]]) for k in range(m)]
 
     def profile_read(self) -> dict:
         ms = np.zeros(7)
