@@ -631,7 +631,8 @@ def scale1m_record(local, steps, args):
     fscale = np.max(np.abs(np.stack([ref.fx, ref.fy, ref.fz])))
     fin = ref.mindist < 1e300
     out["parity_after_3_steps"] = {
-        "density_max_rel": float(np.max(np.abs(g["density"] - ref.density) / np.abs(ref.density))),
+        "density_max_rel": float(np.max(np.abs(g["density"] - ref.density) / np.maximum(np.abs(ref.density),
+                                                                                       1e-300))),
         "mindist_max_rel": float(np.max(np.abs(g["mindist"][fin] - ref.mindist[fin]) / ref.mindist[fin])),
         "v_max_abs": float(np.max(np.abs(g["v"] - ref.v))),
         "force_max_rel_to_max": float(max(np.max(np.abs(g[q] - getattr(ref, q))) for q in ("fx", "fy", "fz"))

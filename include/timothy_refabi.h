@@ -309,6 +309,15 @@ int tm_dropin_env_solution(int field, double *out);
 /* 1: environment_compute also copies the solution into environment[f].data
  * (the reference leaves data unchanged, environment.c:495-507) */
 void tm_dropin_set_env_writeback(int on);
+/* No counterpart in the reference.  The arithmetic of the drop-ins' pair
+ * maths from the next octbuild on: 0 = TM_PREC_FP64 (the default, the
+ * reference's own roundings) or 1 = TM_PREC_FP32C (FP32 pair maths with
+ * compensated sums, the cutoff rechecked in FP64 near h, FP64 positions;
+ * within 1e-6 of the FP64 results, identical neighbour sets); with
+ * neighbour_lists = 1 the colony keeps Verlet lists between steps as long as
+ * the host keeps the same cells in the same order (a step loop without cell
+ * divisions or removals).  Changing either releases the device session. */
+void tm_dropin_set_precision(int precision, int neighbour_lists);
 /* Releases the device session the drop-ins keep between calls (no
  * counterpart in the reference; optional at exit). */
 void tm_dropin_shutdown(void);

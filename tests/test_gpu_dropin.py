@@ -4,6 +4,7 @@ Cells are a host array of celldata_t; octbuild / patches_* / computepotential /
 computegradient / updatepositions are called through the C ABI and the
 results compared with the reference's own outputs (tests/golden).
 """
+import ctypes
 import glob
 import os
 
@@ -95,3 +96,40 @@ def test_dropin_halo_cells_are_rejected_only_with_imports():
     out = run.outputs()
     assert np.all(np.isfinite(out["density"]))
     run.shutdown()
+
+
+@pytest.mark.parametrize("lists", [False, True])
+def test_dropins_fp32c_within_tolerance(oracle_lib, lists):
+    """tm_dropin_set_precision(TM_PREC_FP32C, lists): the reference step loop
+    through the drop-ins on the FP32 + compensated path (searching the bins
+    every step, or keeping neighbour lists while the host keeps the same
+    cells), against the oracle's FP64 run of the same steps: density,
+    mindist and positions within 1e-6 relative, forces within 1e-6 of max |F|,
+    removal marks exact."""
+    from timothy_gb300 import session
+    from timothy_gb300.refabi import DropinRun
+
+    lib = session.load_library()
+    lib.tm_dropin_set_precision.argtypes = [ctypes.c_int, ctypes.c_int]
+    col = C.make_colony("clustered", 20000, 51, C.initial_radius("clustered", 20000))
+    steps = 4
+    lib.tm_dropin_set_precision(1, 1 if lists else 0)
+    try:
+        run = DropinRun(col)
+        for _ in range(steps):
+            run.step(update=True)
+        out = run.outputs()
+        run.shutdown()
+    finally:
+        lib.tm_dropin_set_precision(0, 0)
+    ref = oracle_lib.run(col, steps, which="oracle", update_mode=0)
+    for k in ("x", "y", "z"):
+        assert rel(out[k], getattr(ref, k), 1.0) <= 1e-6, k
+    pos = ref.density > 0
+    assert rel(out["density"][pos], ref.density[pos]) <= 1e-6
+    fin = ref.mindist < 1e300
+    assert rel(out["mindist"][fin], ref.mindist[fin]) <= 1e-6
+    f = np.stack([ref.fx, ref.fy, ref.fz])
+    g = np.stack([out["fx"], out["fy"], out["fz"]])
+    assert np.max(np.abs(g - f)) <= 1e-6 * np.max(np.abs(f))
+    assert np.array_equal(out["removecell"], ref.removecell)

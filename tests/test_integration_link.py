@@ -117,3 +117,31 @@ def test_shared_library_alone_does_not_replace(tmp_path, built):
     wins over the shared library's."""
     via_file, direct = _link_and_run(tmp_path, built, pic=True, static_dropins=False)
     assert (via_file, direct) == (1, 1)
+
+
+def test_remote_walk_with_imported_cells_stops_the_program():
+    """computeremotepotential with imported halo cells (numimp > 0) ends the
+    program through the reference's error exit (terminate(), else abort with
+    the message), as the GB300 path runs one MPI rank.  Run in a child
+    process; nothing touches a GPU before the check."""
+    import subprocess
+    import sys
+    import textwrap
+
+    code = textwrap.dedent(f"""
+        import ctypes, sys
+        sys.path.insert(0, {ROOT!r})
+        from timothy_gb300 import session
+        from timothy_gb300 import refabi as R
+        lib = R._bind(session.load_library())
+        si = R.systeminfo_t(); si.size = 1
+        ci = R.cellsinfo_t(); ci.localcount.n = 10
+        ct = (R.celltype_t * 1)()
+        cc = R.cellcommdata_t(); cc.numimp = 3
+        lib.computeremotepotential(si, ctypes.byref(ci), ct, cc)
+        print("returned")
+    """)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=120)
+    assert r.returncode != 0
+    assert "returned" not in r.stdout
+    assert "halo cells" in r.stderr

@@ -35,6 +35,15 @@ static int g_dim;
 static void *g_pinned;
 static size_t g_pinned_bytes;
 static systeminfo_t g_si;
+/* tm_dropin_set_precision: the pair maths of the drop-in colony and whether
+ * it keeps neighbour lists between steps */
+static int g_prec = TM_PREC_FP64;
+static int g_lists;
+/* the device colony holds the caller's cells in the caller's order (set by a
+ * step, cleared when the cell set changes), so the next octbuild may keep
+ * slots and lists */
+static int g_same_cells;
+static int64_t g_last_n = -1;
 
 static void die(const char *what, int rc, int line)
 {
@@ -83,12 +92,15 @@ static void ensure_session(int64_t n, int dim)
     cfg.device = 0;
     cfg.max_slots = cap + 64;
     cfg.max_colonies = 1;
+    cfg.list_capacity = g_lists ? 384 : 0;
     TRY("session create", tm_session_create(&g_sess, &cfg, &t));
+    g_same_cells = 0;
     g_cap = cap;
     g_dim = dim;
     tm_colony_options opt;
     memset(&opt, 0, sizeof opt);
-    opt.precision = TM_PREC_FP64;
+    opt.precision = g_prec;
+    opt.verlet = g_lists;
     opt.update_mode = TM_UPDATE_REFERENCE;
     opt.dt = 1.0;
     opt.gfh = 8.0f;
@@ -136,7 +148,12 @@ void octbuild(systeminfo_t systeminfo, cellsinfo_t *cellsinfo, celltype_t *cellt
     if (n == 0) return;                                /* octree.c:152-153 */
     ensure_session(n, cellsinfo->dimension);
     pin_cells(cellsinfo->cells, n);
-    TRY("upload", tmi_upload_aos(g_sess, g_cid, cellsinfo->cells, n, cell_layout()));
+    if (g_lists && g_same_cells && n == g_last_n)
+        TRY("upload", tmi_upload_aos_keep(g_sess, g_cid, cellsinfo->cells, n, cell_layout()));
+    else
+        TRY("upload", tmi_upload_aos(g_sess, g_cid, cellsinfo->cells, n, cell_layout()));
+    g_last_n = n;
+    g_same_cells = 1;
     push_types(cellsinfo, celltype);
     TRY("build", tmi_phase(g_sess, 0));
     tm_colony_info info;
@@ -260,6 +277,7 @@ int updatecellcycles(systeminfo_t systeminfo, settings_t settings, celltype_t *c
     ensure_session(room, settings.dimension);
     pin_cells(cellsinfo->cells, room);
     TRY("upload", tmi_upload_aos(g_sess, g_cid, cellsinfo->cells, n, cell_layout()));
+    g_same_cells = 0;   /* a fresh upload: the next octbuild uploads afresh too */
     push_types(cellsinfo, celltype);
     int maxtype = 0;
     TRY("cell types", tmi_max_ctype(g_sess, g_cid, &maxtype));
@@ -316,6 +334,7 @@ void cellsdeath(int oldlnc, cellsinfo_t *cellsinfo, unsigned char *removecell, i
         return;
     }
     ensure_session(n, cellsinfo->dimension);
+    g_same_cells = 0;
     int64_t nout = n, removed[64];
     TRY("cell removal", tmi_compact_aos(g_sess, cellsinfo->cells, n, oldlnc, removecell, &nout, removed));
     for (int t = 0; t < 8; t++)
@@ -546,6 +565,21 @@ int tm_dropin_env_solution(int field, double *out)
 
 void tm_dropin_set_env_writeback(int on) { g_env_writeback = on ? 1 : 0; }
 
+void tm_dropin_set_precision(int precision, int neighbour_lists)
+{
+    const int prec = precision == TM_PREC_FP32C ? TM_PREC_FP32C : TM_PREC_FP64;
+    const int lists = neighbour_lists ? 1 : 0;
+    if (prec == g_prec && lists == g_lists) return;
+    g_prec = prec;
+    g_lists = lists;
+    /* the next octbuild makes a session with these options */
+    if (g_sess) tm_session_destroy(g_sess);
+    g_sess = NULL;
+    g_cid = -1;
+    g_cap = 0;
+    g_same_cells = 0;
+}
+
 void tm_dropin_shutdown(void)
 {
     if (g_diff) tm_diffusion_destroy(g_diff);
@@ -557,4 +591,5 @@ void tm_dropin_shutdown(void)
     g_sess = NULL;
     g_cid = -1;
     g_cap = 0;
+    g_same_cells = 0;
 }

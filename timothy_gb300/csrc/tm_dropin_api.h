@@ -21,6 +21,10 @@ int tmi_set_types(tm_session *s, const tm_celltypes *types);
 int tmi_set_dimension(tm_session *s, int dim);
 /* caller-order AoS cells (host) -> colony state; n may not exceed the colony's slots */
 int tmi_upload_aos(tm_session *s, int cid, const void *cells, int64_t n, const tmi_aos_layout *lay);
+/* the same: with the colony's cell count unchanged the cells are taken as
+ * the same cells in the same order, keep their slots and (unless one moved
+ * too far or changed size or type) the colony's neighbour lists */
+int tmi_upload_aos_keep(tm_session *s, int cid, const void *cells, int64_t n, const tmi_aos_layout *lay);
 /* largest cell type among the uploaded cells */
 int tmi_max_ctype(tm_session *s, int cid, int *maxtype);
 /* 0 build (octbuild), 1 pair + octree walk, 2 position update, 3 CIC deposit */

@@ -122,7 +122,10 @@ __device__ __forceinline__ bool within32_at(const tm_type &T, float s, const tm_
     return dist64(a, i, j) <= T.h;
 }
 
-// FP32 + compensated pair (caller decided it is within h)
+// FP32 + compensated pair (caller decided it is within h).  The kernel
+// value's error estimate is term / (1 - u) (W ~ (1-u)^3 amplifies the FP32
+// error of 1 - u near the cutoff), formed without a division: outside
+// u = 1/2 it is ms * 2 cW (1-u)^2, inside it is bounded by 2 * term.
 __device__ __forceinline__ void pair32(const tm_type &T, int dim, float dx, float dy, float dz, float s,
                                        float sizej, pair_acc<1> &acc)
 {
@@ -136,15 +139,15 @@ __device__ __forceinline__ void pair32(const tm_type &T, int dim, float dx, floa
     const float omu = (T.hf - dist) * T.inv_hf;
     // both branches of the cubic spline, selected (no divergence)
     const bool inner = u <= 0.5f;
-    const float wk = T.cWf * (inner ? fmaf(6.0f * u * u, u - 1.0f, 1.0f) : 2.0f * omu * omu * omu);
-    const float wg = inner ? u * fmaf(3.0f, u, -2.0f) : -omu * omu;
-    const float term = T.kmassf * sizej * wk;
-    acc.dens.add(term);
-    // one-sigma rounding estimate of this term: W ~ (1-u)^3 amplifies the FP32
-    // error of (1 - u) near the cutoff
-    // (the constant 1.2e-7 part of the estimate is folded into the threshold)
-    const float ek = __fdividef(term, fmaxf(omu, 1.0e-3f));
+    const float o2 = omu * omu;
+    const float q2 = (2.0f * T.cWf) * o2;                  // 2 cW (1-u)^2
+    const float w_in = T.cWf * fmaf(6.0f * u * u, u - 1.0f, 1.0f);
+    const float wk = inner ? w_in : q2 * omu;
+    const float ms = T.kmassf * sizej;
+    acc.dens.add(ms * wk);
+    const float ek = ms * (inner ? 2.0f * w_in : q2);
     acc.err2 = fmaf(ek, ek, acc.err2);
+    const float wg = inner ? u * fmaf(3.0f, u, -2.0f) : -o2;
     const float g = wg * T.cGf * rs;
     acc.fx.add(g * dx);
     acc.fy.add(g * dy);
@@ -684,6 +687,112 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_plist(tm_arrays a, const tm_con
     }
 }
 
+// List pass of the FP32 + compensated path: LPC lanes share a cell, lane q
+// evaluating the cell's entries q, q + LPC, ... with two entries in flight
+// and the next two list indices already loading; the lanes' compensated
+// partial sums are merged by shuffles in a fixed order, so a colony's
+// results do not depend on the block shape.  With LPC = 4 a warp holds 8
+// Morton-consecutive cells, whose list lengths differ less than those of 32.
+#define PLIST_LPC 4
+template <int BLOCK, int MINB, bool DIAG>
+__global__ void __launch_bounds__(BLOCK, MINB) k_plist32(tm_arrays a, const tm_consts *K)
+{
+    constexpr int LPC = PLIST_LPC;
+    constexpr int CPW = 32 / LPC;
+    const int lane = threadIdx.x & 31;
+    const long long base = (((long long)blockIdx.x * BLOCK + threadIdx.x) >> 5) * CPW;
+    if (base >= a.nslots_total) return;            // whole warps leave together
+    const int c = a.col[base];                      // colonies are 32-aligned: one colony per warp
+    const tm_desc &d = a.desc[c];
+    if (!d.active || d.precision != 1 || d.n <= 1 || !d.verlet) return;
+    const tm_frame &f = a.frame[c];
+    if (!f.list_ok) return;                         // overflowed: the search pass evaluates
+    const long long i = base + lane / LPC;
+    const int q = lane % LPC;
+    const bool live = tm_live(i, d);
+    if (!__any_sync(FULL, live)) return;
+    const int dim = K->dim;
+    const tm_type &T = K->t[live ? a.ctype[i] : 0];
+    const float thr_lo = T.thr_lo, thr_hi = T.thr_hi;
+    const float4 hi_i = live ? a.hi[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 lo_i = live ? a.lo[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 *__restrict__ hi = a.hi;
+    const float4 *__restrict__ lo = a.lo;
+    pair_acc<1> acc;
+    acc.init();
+    int cnt_nb = 0, nbmin = 0x7fffffff;
+    unsigned long long hash = 0;
+    const int cnt = live ? __ldg(a.vcount + i) : 0;
+    const long long ls = a.lstride;
+    const int drow = (DIAG && live) ? diag_row_of(a, d, i) : -1;
+    const int *__restrict__ lst = a.vlist + i;
+    auto one = [&](int j, float4 hj, float4 lj) {
+        const float dx = (hj.x - hi_i.x) + (lj.x - lo_i.x);
+        const float dy = (hj.y - hi_i.y) + (lj.y - lo_i.y);
+        const float dz = (hj.z - hi_i.z) + (lj.z - lo_i.z);
+        const float s = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        bool in = s <= thr_lo;
+        if (!in && s <= thr_hi) in = dist64(a, i, j) <= T.h;   // FP64 only in the cutoff band
+        if (in) {
+            pair32(T, dim, dx, dy, dz, s, hj.w, acc);
+            cnt_nb++;
+            nbmin = min(nbmin, __float_as_int(lj.w));
+            if (DIAG) diag_pair(a, drow, j, hash);
+        }
+    };
+    int k = q;
+    int ja = k < cnt ? __ldg(lst + k * ls) : 0;
+    int jb = k + LPC < cnt ? __ldg(lst + (k + LPC) * ls) : 0;
+    for (; k < cnt; k += 2 * LPC) {
+        const int kn = k + 2 * LPC;
+        const int na = kn < cnt ? __ldg(lst + kn * ls) : 0;
+        const int nb = kn + LPC < cnt ? __ldg(lst + (kn + LPC) * ls) : 0;
+        const bool hasb = k + LPC < cnt;
+        const float4 ha = __ldg(hi + ja), la = __ldg(lo + ja);
+        const float4 hb = __ldg(hi + jb), lb = __ldg(lo + jb);   // jb = 0 (a valid slot) when absent
+        one(ja, ha, la);
+        if (hasb) one(jb, hb, lb);
+        ja = na;
+        jb = nb;
+    }
+    // merge the LPC partial results of each cell (fixed butterfly order)
+    for (int o = 1; o < LPC; o <<= 1) {
+        acc.dens.merge(__shfl_xor_sync(FULL, acc.dens.s, o), __shfl_xor_sync(FULL, acc.dens.c, o));
+        acc.fx.merge(__shfl_xor_sync(FULL, acc.fx.s, o), __shfl_xor_sync(FULL, acc.fx.c, o));
+        acc.fy.merge(__shfl_xor_sync(FULL, acc.fy.s, o), __shfl_xor_sync(FULL, acc.fy.c, o));
+        acc.fz.merge(__shfl_xor_sync(FULL, acc.fz.s, o), __shfl_xor_sync(FULL, acc.fz.c, o));
+        acc.mins = fminf(acc.mins, __shfl_xor_sync(FULL, acc.mins, o));
+        acc.err2 += __shfl_xor_sync(FULL, acc.err2, o);
+        cnt_nb += __shfl_xor_sync(FULL, cnt_nb, o);
+        nbmin = min(nbmin, __shfl_xor_sync(FULL, nbmin, o));
+        if (DIAG) hash += __shfl_xor_sync(FULL, hash, o);
+    }
+    if (!live || q != 0) return;
+    pair_store<1>(a, i, acc, cnt_nb, nbmin, hash, false);
+    // the octree walk's first pass for this cell (see k_octree_mark): walk if
+    // the first within-h neighbour in Morton order may overlap it
+    bool walk = cnt_nb == 0 || DIAG;
+    if (!walk) {
+        const long long m = f.ident ? (long long)nbmin : (long long)a.tmp[nbmin];
+        const float4 hm = hi[m], lm = lo[m];
+        const float dx = (hi_i.x - hm.x) + (lo_i.x - lm.x), dy = (hi_i.y - hm.y) + (lo_i.y - lm.y),
+                    dz = (hi_i.z - hm.z) + (lo_i.z - lm.z);
+        const float rs = (hi_i.w + hm.w) * 1.0001f + 1e-5f;
+        walk = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < rs * rs;
+    }
+    tm_queue_walk(a, i, cnt_nb == 0, walk);
+    if (needs_fix64(acc)) {
+        // FP64 density over the same list, the cutoff decided in FP64
+        double dens = 0.0;
+        for (int kk = 0; kk < cnt; kk++) {
+            const int j = a.vlist[(long long)kk * ls + i];
+            const double dist = dist64(a, i, j);
+            if (dist <= T.h) dens = add64(dens, dens_term64(T, dist, a.size[j]));
+        }
+        a.density[i] = dens;
+    }
+}
+
 // FP64 density of the cells flagged by the FP32 path: the same neighbour set
 // (exact FP64 cutoff) and the reference expression of potential.c:62.
 __global__ void __launch_bounds__(128) k_density_fix64(tm_arrays a, const tm_consts *K)
@@ -743,6 +852,19 @@ static unsigned pair_grid_cap(int prec)
     return (unsigned)cached[prec][dev];
 }
 
+template <bool DIAG>
+static void launch_plist32(const tm_arrays &a, const tm_consts *K, int variant, cudaStream_t st)
+{
+    // PLIST_LPC threads per slot (a warp holds 32 / PLIST_LPC cells)
+    const long long nt = a.nslots_total * PLIST_LPC;
+    switch (variant) {
+    case 2: k_plist32<128, 7, DIAG><<<(unsigned)((nt + 127) / 128), 128, 0, st>>>(a, K); break;
+    case 3: k_plist32<256, 3, DIAG><<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(a, K); break;
+    case 4: k_plist32<512, 2, DIAG><<<(unsigned)((nt + 511) / 512), 512, 0, st>>>(a, K); break;
+    default: k_plist32<256, 4, DIAG><<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(a, K); break;
+    }
+}
+
 template <int PREC>
 static void launch_plist(const tm_arrays &a, const tm_consts *K, int variant, cudaStream_t st)
 {
@@ -789,7 +911,8 @@ cudaError_t tm_launch_list(const tm_arrays &a, const tm_consts *K, int prec, con
 {
     if (a.vcap == 0 || a.nslots_total == 0) return cudaSuccess;
     if (prec == 0) launch_plist<0>(a, K, sh.list_variant, st);
-    else launch_plist<1>(a, K, sh.list_variant, st);
+    else if (a.want_diag) launch_plist32<true>(a, K, sh.list_variant, st);
+    else launch_plist32<false>(a, K, sh.list_variant, st);
     return cudaGetLastError();
 }
 

@@ -1815,6 +1815,49 @@ extern "C" int tmi_upload_aos(tm_session *s, int cid, const void *cells, int64_t
     return TM_OK;
 }
 
+// caller-order AoS cells (device staging) -> upload records (caller order)
+__global__ void k_aos_to_rec(const unsigned char *aos, tmi_aos_layout lay, long long n, int4 *rec, long long base)
+{
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const unsigned char *c = aos + k * lay.stride;
+    up_rec r;
+    r.f.x = *(const double *)(c + lay.x);
+    r.f.y = *(const double *)(c + lay.y);
+    r.f.z = *(const double *)(c + lay.z);
+    r.f.size = *(const double *)(c + lay.size);
+    r.f.young = *(const float *)(c + lay.young);
+    r.f.ctype = *(const int *)(c + lay.ctype);
+    r.f.phase = lay.phase >= 0 ? *(const int *)(c + lay.phase) : 1;
+    r.f.pad = 0;
+    int4 *d = rec + (base + k) * 3;
+    d[0] = r.v[0];
+    d[1] = r.v[1];
+    d[2] = r.v[2];
+}
+
+// The same cells in the same caller order as the colony holds: they keep
+// their slots (tm_colony_upload's rule), so neighbour lists stay valid unless
+// a cell moved too far or changed size or type.
+extern "C" int tmi_upload_aos_keep(tm_session *s, int cid, const void *cells, int64_t n, const tmi_aos_layout *lay)
+{
+    int rc = lookup(s, cid);
+    if (rc) return rc;
+    colony_host &c = s->cols[cid];
+    if (n != c.n || n == 0) return tmi_upload_aos(s, cid, cells, n, lay);
+    CK(cudaSetDevice(s->device));
+    if ((rc = tmi_reserve_stage(s, std::max<int64_t>(n * lay->stride, 8)))) return rc;
+    CK(cudaMemcpyAsync(g_stage.ptr, cells, (size_t)(n * lay->stride), cudaMemcpyHostToDevice, s->stream));
+    int4 *rec = nullptr;
+    if ((rc = upload_records(s, &rec))) return rc;
+    const tm_arrays a = view(s, s->parity);
+    k_aos_to_rec<<<blocks_for(n, 256), 256, 0, s->stream>>>((const unsigned char *)g_stage.ptr, *lay, n, rec, c.off);
+    k_upload_keep<<<blocks_for(n, 256), 256, 0, s->stream>>>(a, s->dK, cid, c.off, (int)n, lay->phase >= 0 ? 1 : 0,
+                                                            nullptr, rec, c.off);
+    CK(cudaGetLastError());
+    return TM_OK;
+}
+
 extern "C" int tmi_max_ctype(tm_session *s, int cid, int *maxtype)
 {
     int rc = lookup(s, cid);
