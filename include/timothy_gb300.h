@@ -156,6 +156,16 @@ int tm_session_list_rate(tm_session *s, double *rate, int64_t *rebuilds);
 
 /* Add a colony; its id is written to *id.  Uploads the cells. */
 int tm_colony_add(tm_session *s, const tm_colony_input *in, const tm_colony_options *opt, int *id);
+/* The same without waiting: the cells' copies and the colony's set-up are
+ * queued on the session stream behind the work already there (a step in
+ * flight keeps running), and the call returns.  Cell types are checked on
+ * the host first.  From page-locked memory the copies read in's arrays when
+ * they run, so the caller leaves them unchanged until a later
+ * tm_session_sync or a waited fence; other host memory is read during the
+ * call. */
+int tm_colony_add_async(tm_session *s, const tm_colony_input *in, const tm_colony_options *opt, int *id);
+/* Removes a colony without waiting: work queued before it still sees the
+ * colony, and its slots, bins and grid are free for colonies added after. */
 int tm_colony_remove(tm_session *s, int id);
 /* Remove the colony's cells marked for removal (outside the box after an
  * update), as cellsdeath does at one rank (cells.c:290-336): the survivors
@@ -240,6 +250,13 @@ int tm_colony_upload(tm_session *s, int id, const tm_colony_input *in);
 int tm_colony_set_active(tm_session *s, int id, int active);
 int tm_colony_download(tm_session *s, int id, const tm_colony_output *out);
 int tm_colony_stats(tm_session *s, int id, tm_colony_info *st);
+
+/* A fence after the work queued so far (session stream and the copy stream
+ * of asynchronous downloads): tm_session_wait blocks until it is done.  A
+ * host loop that waits for the fence of step k - 1 after queuing step k stays
+ * one step ahead of the device, so the device never waits for the host. */
+int tm_session_fence(tm_session *s, int64_t *fence);
+int tm_session_wait(tm_session *s, int64_t fence);
 
 /* Enqueue nsteps steps of every active colony on the session stream.
  * Returns without waiting; tm_session_sync waits and reports device errors. */

@@ -694,7 +694,30 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_plist(tm_arrays a, const tm_con
 // results do not depend on the block shape.  With LPC = 4 a warp holds 8
 // Morton-consecutive cells, whose list lengths differ less than those of 32.
 #define PLIST_LPC 4
-template <int BLOCK, int MINB, bool DIAG>
+
+// cp.async (global -> shared, through L1) and its group waits
+__device__ __forceinline__ void cpasync16(void *smem, const void *gmem)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cpasync4(void *smem, const void *gmem)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cpasync_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cpasync_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+__device__ __forceinline__ void cpasync_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// D = 0: two entries in flight in registers.  D > 0: a per-thread ring in
+// shared memory fed by cp.async keeps D entries' positions and, D entries
+// further ahead, their list indices in flight without holding registers: at
+// entry m the thread waits for the copies issued at entry m - D, evaluates
+// entry m, then issues the positions of entry m + D and the index of entry
+// m + 2 D into the slots it just consumed.
+template <int BLOCK, int MINB, int D, bool DIAG>
 __global__ void __launch_bounds__(BLOCK, MINB) k_plist32(tm_arrays a, const tm_consts *K)
 {
     constexpr int LPC = PLIST_LPC;
@@ -740,20 +763,62 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_plist32(tm_arrays a, const tm_c
             if (DIAG) diag_pair(a, drow, j, hash);
         }
     };
-    int k = q;
-    int ja = k < cnt ? __ldg(lst + k * ls) : 0;
-    int jb = k + LPC < cnt ? __ldg(lst + (k + LPC) * ls) : 0;
-    for (; k < cnt; k += 2 * LPC) {
-        const int kn = k + 2 * LPC;
-        const int na = kn < cnt ? __ldg(lst + kn * ls) : 0;
-        const int nb = kn + LPC < cnt ? __ldg(lst + (kn + LPC) * ls) : 0;
-        const bool hasb = k + LPC < cnt;
-        const float4 ha = __ldg(hi + ja), la = __ldg(lo + ja);
-        const float4 hb = __ldg(hi + jb), lb = __ldg(lo + jb);   // jb = 0 (a valid slot) when absent
-        one(ja, ha, la);
-        if (hasb) one(jb, hb, lb);
-        ja = na;
-        jb = nb;
+    if constexpr (D == 0) {
+        int k = q;
+        int ja = k < cnt ? __ldg(lst + k * ls) : 0;
+        int jb = k + LPC < cnt ? __ldg(lst + (k + LPC) * ls) : 0;
+        for (; k < cnt; k += 2 * LPC) {
+            const int kn = k + 2 * LPC;
+            const int na = kn < cnt ? __ldg(lst + kn * ls) : 0;
+            const int nb = kn + LPC < cnt ? __ldg(lst + (kn + LPC) * ls) : 0;
+            const bool hasb = k + LPC < cnt;
+            const float4 ha = __ldg(hi + ja), la = __ldg(lo + ja);
+            const float4 hb = __ldg(hi + jb), lb = __ldg(lo + jb);   // jb = 0 (a valid slot) when absent
+            one(ja, ha, la);
+            if (hasb) one(jb, hb, lb);
+            ja = na;
+            jb = nb;
+        }
+    } else {
+        // rings indexed [slot][thread], so a warp's accesses to one slot are
+        // consecutive 16-byte words (no bank conflicts)
+        __shared__ float4 rh[D][BLOCK], rl[D][BLOCK];
+        __shared__ int rj[D][BLOCK];
+        const int tid = threadIdx.x;
+        const int M = cnt > q ? (cnt - q + LPC - 1) / LPC : 0;   // this lane's entries q + LPC m
+        auto entry = [&](int m) { return lst + (long long)(q + LPC * m) * ls; };
+        int jr[D];
+#pragma unroll
+        for (int u = 0; u < D; u++) {
+            jr[u] = u < M ? __ldg(entry(u)) : 0;
+            if (u < M) {
+                cpasync16(&rh[u][tid], hi + jr[u]);
+                cpasync16(&rl[u][tid], lo + jr[u]);
+            }
+            if (D + u < M) cpasync4(&rj[u][tid], entry(D + u));
+            cpasync_commit();
+        }
+        for (int m0 = 0; m0 < M; m0 += D) {
+#pragma unroll
+            for (int u = 0; u < D; u++) {
+                const int m = m0 + u;
+                if (m < M) {
+                    cpasync_wait<D - 1>();
+                    const float4 hj = rh[u][tid], lj = rl[u][tid];
+                    one(jr[u], hj, lj);
+                    // refill slot u: positions of entry m + D, index of entry m + 2 D
+                    if (m + D < M) {
+                        const int jn = rj[u][tid];
+                        jr[u] = jn;
+                        cpasync16(&rh[u][tid], hi + jn);
+                        cpasync16(&rl[u][tid], lo + jn);
+                        if (m + 2 * D < M) cpasync4(&rj[u][tid], entry(m + 2 * D));
+                    }
+                    cpasync_commit();
+                }
+            }
+        }
+        cpasync_wait_all();
     }
     // merge the LPC partial results of each cell (fixed butterfly order)
     for (int o = 1; o < LPC; o <<= 1) {
@@ -858,10 +923,10 @@ static void launch_plist32(const tm_arrays &a, const tm_consts *K, int variant, 
     // PLIST_LPC threads per slot (a warp holds 32 / PLIST_LPC cells)
     const long long nt = a.nslots_total * PLIST_LPC;
     switch (variant) {
-    case 2: k_plist32<128, 7, DIAG><<<(unsigned)((nt + 127) / 128), 128, 0, st>>>(a, K); break;
-    case 3: k_plist32<256, 3, DIAG><<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(a, K); break;
-    case 4: k_plist32<512, 2, DIAG><<<(unsigned)((nt + 511) / 512), 512, 0, st>>>(a, K); break;
-    default: k_plist32<256, 4, DIAG><<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(a, K); break;
+    case 2: k_plist32<128, 7, 0, DIAG><<<(unsigned)((nt + 127) / 128), 128, 0, st>>>(a, K); break;
+    case 3: k_plist32<128, 7, 6, DIAG><<<(unsigned)((nt + 127) / 128), 128, 0, st>>>(a, K); break;
+    case 4: k_plist32<256, 3, 4, DIAG><<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(a, K); break;
+    default: k_plist32<128, 7, 4, DIAG><<<(unsigned)((nt + 127) / 128), 128, 0, st>>>(a, K); break;
     }
 }
 

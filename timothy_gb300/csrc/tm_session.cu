@@ -174,6 +174,10 @@ struct tm_session {
     // diagnostics: sampled neighbour lists (tm_colony_sample_neighbours)
     int diag_col = -1;
     long long diag_ncells = 0;
+    // fences (tm_session_fence): a ring of events
+    std::vector<cudaEvent_t> fence_ev;
+    cudaEvent_t fence_join = nullptr;
+    int64_t fence_next = 0;
 };
 
 // ---------------------------------------------------------------------------
@@ -512,9 +516,16 @@ static void drop_graphs(tm_session *s)
     }
 }
 
+// A colony's descriptor and frame reach the device as kernel arguments, so the
+// values are those of the call even when the host changes its copy before the
+// stream gets there (a colony removed and its entry reused without a wait).
+__global__ void k_set_desc(tm_desc *dst, tm_desc v) { *dst = v; }
+__global__ void k_set_frame(tm_frame *dst, tm_frame v) { *dst = v; }
+
 static int push_desc(tm_session *s, int c)
 {
-    CK(cudaMemcpyAsync(&s->A.desc[c], &s->h_desc[c], sizeof(tm_desc), cudaMemcpyHostToDevice, s->stream));
+    k_set_desc<<<1, 1, 0, s->stream>>>(&s->A.desc[c], s->h_desc[c]);
+    CK(cudaGetLastError());
     return TM_OK;
 }
 
@@ -731,6 +742,9 @@ extern "C" int tm_session_destroy(tm_session *s)
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (auto ev : s->evpool) cudaEventDestroy(ev);
+    for (auto ev : s->fence_ev)
+        if (ev) cudaEventDestroy(ev);
+    if (s->fence_join) cudaEventDestroy(s->fence_join);
     if (s->tstart) cudaEventDestroy(s->tstart);
     if (s->tstop) cudaEventDestroy(s->tstop);
     if (s->h_desc) cudaFreeHost(s->h_desc);
@@ -805,7 +819,10 @@ static int upload_records(tm_session *s, int4 **rec)
     return TM_OK;
 }
 
-static int copy_cells_in(tm_session *s, const colony_host &c, const tm_colony_input *in, bool keep)
+// wait = false (a new colony only, its types checked on the host): the copies
+// and kernels are queued and the call returns without waiting for them
+static int copy_cells_in(tm_session *s, const colony_host &c, const tm_colony_input *in, bool keep,
+                         bool wait = true)
 {
     const tm_arrays a = view(s, s->parity);
     const long long o = c.off;
@@ -846,6 +863,7 @@ static int copy_cells_in(tm_session *s, const colony_host &c, const tm_colony_in
         k_colony_init<<<blocks_for(c.nslots, 256), 256, 0, st>>>(a, cid, o, (int)n, c.nslots, in->phase ? 1 : 0);
     }
     CK(cudaGetLastError());
+    if (!wait && !keep) return TM_OK;
     int bad = 0;
     CK(cudaMemcpyAsync(&bad, s->d_flag, sizeof(int), cudaMemcpyDeviceToHost, st));
     // synchronous: the caller may free its buffers on return
@@ -888,7 +906,19 @@ static int auto_lcap(const tm_session *s, const tm_colony_input *in)
     return std::max(1, std::min(TM_LMAX, L));
 }
 
+static int colony_add(tm_session *s, const tm_colony_input *in, const tm_colony_options *opt, int *id, bool wait);
+
 extern "C" int tm_colony_add(tm_session *s, const tm_colony_input *in, const tm_colony_options *opt, int *id)
+{
+    return colony_add(s, in, opt, id, true);
+}
+
+extern "C" int tm_colony_add_async(tm_session *s, const tm_colony_input *in, const tm_colony_options *opt, int *id)
+{
+    return colony_add(s, in, opt, id, false);
+}
+
+static int colony_add(tm_session *s, const tm_colony_input *in, const tm_colony_options *opt, int *id, bool wait)
 {
     if (!s || !opt || !id) return tm_fail(TM_EINVAL, "null argument");
     int rc = check_input(s, in);
@@ -967,9 +997,10 @@ extern "C" int tm_colony_add(tm_session *s, const tm_colony_input *in, const tm_
     f.L = 1;
     f.nbins = 8;
     f.binscale = 2.0f;
-    CK(cudaMemcpyAsync(&s->A.frame[c], &f, sizeof f, cudaMemcpyHostToDevice, s->stream));
+    k_set_frame<<<1, 1, 0, s->stream>>>(&s->A.frame[c], f);
+    CK(cudaGetLastError());
     rc = push_desc(s, c);
-    if (rc == TM_OK) rc = copy_cells_in(s, s->cols[c], in, false);
+    if (rc == TM_OK) rc = copy_cells_in(s, s->cols[c], in, false, wait);
     if (rc != TM_OK) {
         const std::string msg = g_err;
         tm_colony_remove(s, c);
@@ -995,7 +1026,6 @@ extern "C" int tm_colony_remove(tm_session *s, int id)
     int rc = lookup(s, id);
     if (rc) return rc;
     CK(cudaSetDevice(s->device));
-    CK(cudaStreamSynchronize(s->stream));
     if (s->diag_col == id) drop_sample(s);
     colony_host &c = s->cols[id];
     s->h_desc[id].active = 0;
@@ -1003,11 +1033,13 @@ extern "C" int tm_colony_remove(tm_session *s, int id)
     rc = push_desc(s, id);
     if (rc) return rc;
     // freed slots point at the never-active entry, so no later colony that
-    // reuses this entry sees them as its own
+    // reuses this entry sees them as its own.  Nothing waits: work queued
+    // before (steps, the gathers of an asynchronous download) still sees the
+    // colony, and a colony placed in the freed ranges later is written by
+    // work queued after these kernels on the same stream.
     k_release_slots<<<blocks_for(c.nslots, 256), 256, 0, s->stream>>>(s->A.col, c.off, c.nslots,
                                                                        s->cfg.max_colonies);
     CK(cudaGetLastError());
-    CK(cudaStreamSynchronize(s->stream));
     s->slots.release(c.off / 32, c.nslots / 32);
     s->bins.release(c.binoff, c.nbin);
     if (c.gridoff >= 0) s->grids.release(c.gridoff, c.ngrid);
@@ -1352,6 +1384,39 @@ extern "C" int tm_colony_read_neighbours(tm_session *s, int id, int32_t *counts,
     if (lists)
         CK(cudaMemcpy(lists, s->A.diag_nb, (size_t)s->diag_ncells * (size_t)s->A.diag_lcap * sizeof(int),
                       cudaMemcpyDeviceToHost));
+    return TM_OK;
+}
+
+#define TM_FENCES 64
+
+extern "C" int tm_session_fence(tm_session *s, int64_t *fence)
+{
+    if (!s || !fence) return tm_fail(TM_EINVAL, "null argument");
+    CK(cudaSetDevice(s->device));
+    if (s->fence_ev.empty()) {
+        s->fence_ev.resize(TM_FENCES, nullptr);
+        for (auto &e : s->fence_ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&s->fence_join, cudaEventDisableTiming));
+    }
+    cudaEvent_t e = s->fence_ev[(size_t)(s->fence_next % TM_FENCES)];
+    if (s->copy_stream) {
+        // the work queued so far on the session stream and on the copy stream
+        CK(cudaEventRecord(s->fence_join, s->stream));
+        CK(cudaStreamWaitEvent(s->copy_stream, s->fence_join, 0));
+        CK(cudaEventRecord(e, s->copy_stream));
+    } else {
+        CK(cudaEventRecord(e, s->stream));
+    }
+    *fence = s->fence_next++;
+    return TM_OK;
+}
+
+extern "C" int tm_session_wait(tm_session *s, int64_t fence)
+{
+    if (!s || fence < 0 || fence >= s->fence_next) return tm_fail(TM_EINVAL, "no such fence");
+    CK(cudaSetDevice(s->device));
+    // a fence older than the ring is covered by the newer record in its place
+    CK(cudaEventSynchronize(s->fence_ev[(size_t)(fence % TM_FENCES)]));
     return TM_OK;
 }
 

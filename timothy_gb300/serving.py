@@ -7,8 +7,16 @@ arrival order and are admitted while the pool has room for their cells (slot
 range, bin table, colony entry); an admitted colony stays resident until its
 last step.  Every engine iteration advances all resident colonies one step in
 the same launches, so a colony admitted now steps alongside colonies that are
-part-way through theirs (continuous batching).  After the step, finished
-colonies are downloaded and removed, which frees room for the queue.
+part-way through theirs (continuous batching).  After its last step a colony's
+results are queued for download into page-locked buffers and the colony is
+removed, which frees room for the queue at once.
+
+The host keeps one step ahead of the device: admissions
+(``tm_colony_add_async``), retirements and the next step are queued behind
+the step in flight, and the host then waits only for the fence of the step
+before (``tm_session_fence``/``tm_session_wait``), when that step's retired
+results have reached the host.  The device never waits for the host's
+bookkeeping, and a request's latency ends when its results are on the host.
 
 Because a colony's results do not depend on what else is resident (per-colony
 frames, bins, lists; groups aligned to the colony's first slot), a request
@@ -126,9 +134,17 @@ class Server:
         if tuning:
             self.s.set_tuning(**tuning)
         self.s.use_graph(graph)
+        self._free_bufs: list[dict] = []
+        self._all_bufs: list[dict] = []
 
     def close(self):
+        from .session import host_unregister
+
         self.s.close()
+        for b in self._all_bufs:
+            for a in b.values():
+                host_unregister(a)
+        self._all_bufs, self._free_bufs = [], []
 
     def __enter__(self):
         return self
@@ -142,76 +158,122 @@ class Server:
         if req.colony is None:
             req.colony = source.colony(req.kind, req.n, req.seed)
         try:
-            return self.s.add_colony(req.colony, precision=self.precision, update="dt", dt=self.dt, verlet=True)
+            # queued behind the step in flight (tm_colony_add_async)
+            return self.s.add_colony(req.colony, precision=self.precision, update="dt", dt=self.dt, verlet=True,
+                                     wait=False)
         except TimothyError as e:
             if e.code == ENOMEM:
                 return None
             raise
 
+    def _buffers(self, n: int) -> dict:
+        """Page-locked host arrays for one finished colony's results (reused)."""
+        from .session import host_register
+
+        for k, b in enumerate(self._free_bufs):
+            if len(b[self.fields[0]]) >= n:
+                return self._free_bufs.pop(k)
+        cap = max(n, 1 << 16)
+        b = {f: np.zeros(cap, np.uint8 if f == "removecell" else np.float64) for f in self.fields}
+        for a in b.values():
+            host_register(a)
+        self._all_bufs.append(b)
+        return b
+
     def run(self, requests: list[Request], *, source: RequestSource | None = None, virtual: bool = False,
-            horizon: float | None = None, log=None) -> dict:
+            horizon: float | None = None, drain: bool = False, admit_window: int = 32, log=None) -> dict:
         """Serve ``requests`` (sorted by arrival).  With ``virtual`` the clock is
         the engine iteration (deterministic mixes for tests); otherwise wall time
         in seconds.  With ``horizon`` the run stops at that time, leaving later
-        arrivals and unfinished colonies out."""
+        arrivals and unfinished colonies out; with ``drain`` as well, arrivals
+        stop at the horizon and the run goes on until every request that
+        arrived before it has finished, so the latencies cover all of them.
+        Admission takes queued requests in arrival order, and looks past one
+        that does not fit (too many cells for the free slots) at most
+        ``admit_window`` places, so a large request waits for room while
+        smaller ones behind it start."""
         pending = deque(sorted(requests, key=lambda r: r.arrival))
         queue: deque[Request] = deque()
         active: dict[int, list] = {}
+        # steps queued on the device whose fence the host has not waited for,
+        # with the colonies each retired (their results travelling back)
+        inflight: deque[tuple[int, list]] = deque()
+        lag = 1
         s = self.s
         t0 = time.perf_counter()
         it = 0
         stepped_cells = 0
         resident_max = 0
         clock = (lambda: float(it)) if virtual else (lambda: time.perf_counter() - t0)
-        while pending or queue or active:
+        if drain and horizon is not None:
+            pending = deque(r for r in pending if r.arrival < horizon)
+        while pending or queue or active or inflight:
             now = clock()
-            if horizon is not None and now >= horizon:
+            if horizon is not None and now >= horizon and not drain:
                 break
             while pending and pending[0].arrival <= now:
                 queue.append(pending.popleft())
-            while queue:
-                cid = self._admit(queue[0], source)
+            # admission in arrival order, looking past requests that do not fit
+            k = 0
+            while k < min(len(queue), admit_window):
+                cid = self._admit(queue[k], source)
                 if cid is None:
-                    break
-                req = queue.popleft()
+                    k += 1
+                    continue
+                req = queue[k]
+                del queue[k]
                 req.admitted = clock()
                 active[cid] = [req, req.steps]
-            if not active:
+            if active:
+                resident_max = max(resident_max, sum(r.n for r, _ in active.values()))
+                s.step(1)
+                it += 1
+                stepped_cells += sum(r.n for r, _ in active.values())
+                # the step runs on the device: meanwhile build the cells of the
+                # requests that wait, so their admission costs only the upload
+                if source is not None:
+                    for req in list(queue)[:self.prepare_ahead]:
+                        if req.colony is None:
+                            req.colony = source.colony(req.kind, req.n, req.seed)
+                retiring = []
+                for cid in [c for c, e in active.items() if e[1] == 1]:
+                    req = active.pop(cid)[0]
+                    bufs = self._buffers(req.n)
+                    s.download_async(cid, self.fields, bufs)
+                    s.remove_colony(cid)            # queued behind the download's gathers
+                    retiring.append((req, bufs))
+                for e in active.values():
+                    e[1] -= 1
+                inflight.append((s.fence(), retiring))
+            elif not inflight:
                 if virtual:
                     it += 1
                 elif pending:
                     time.sleep(max(0.0, min(pending[0].arrival - clock(), 0.005)))
                 continue
-            resident_max = max(resident_max, sum(r.n for r, _ in active.values()))
-            s.step(1)
-            it += 1
-            stepped_cells += sum(r.n for r, _ in active.values())
-            # the step runs on the device: meanwhile build the cells of the
-            # requests that wait, so their admission costs only the upload
-            if source is not None:
-                for req in list(queue)[:self.prepare_ahead]:
-                    if req.colony is None:
-                        req.colony = source.colony(req.kind, req.n, req.seed)
-            done = []
-            for cid, entry in active.items():
-                entry[1] -= 1
-                if entry[1] == 0:
-                    done.append(cid)
-            for cid in done:
-                req = active.pop(cid)[0]
-                out = s.download(cid, self.fields)
-                req.finished = clock()
-                req.result = out if self.keep else {"density_sum": float(np.sum(out["density"]))}
-                req.colony = None if not self.keep else req.colony
-                s.remove_colony(cid)
-                if log and len(done):
-                    log(f"t={req.finished:.3f} done rid={req.rid} n={req.n} K={req.steps} lat={req.latency:.3f}")
+            # stay at most `lag` steps ahead of the device; settle everything
+            # when nothing more is queued
+            while inflight and (len(inflight) > lag or not active):
+                f, retiring = inflight.popleft()
+                s.wait(f)
+                t = clock()
+                for req, bufs in retiring:
+                    req.finished = t
+                    out = {k: bufs[k][:req.n].copy() for k in self.fields} if self.keep else None
+                    req.result = out if self.keep else {"density_sum": float(np.sum(bufs["density"][:req.n]))
+                                                        if "density" in bufs else None}
+                    req.colony = None if not self.keep else req.colony
+                    self._free_bufs.append(bufs)
+                    if log:
+                        log(f"t={req.finished:.3f} done rid={req.rid} n={req.n} K={req.steps} lat={req.latency:.3f}")
         s.sync()
         wall = clock() if not virtual else time.perf_counter() - t0
+        arrived = [r for r in requests if horizon is None or r.arrival < horizon]
         fin = [r for r in requests if not math.isnan(r.finished)]
         lat = np.array([r.latency for r in fin]) if fin else np.zeros(0)
         served = sum(r.n * r.steps for r in fin)
-        return {"requests": len(requests), "finished": len(fin), "wall_s": wall, "iterations": it,
+        return {"requests": len(requests), "arrived": len(arrived), "finished": len(fin), "wall_s": wall,
+                "iterations": it,
                 "cell_updates_finished": served, "cell_updates_stepped": stepped_cells,
                 "throughput": stepped_cells / wall if wall > 0 else 0.0,
                 "p50": float(np.percentile(lat, 50)) if len(lat) else None,

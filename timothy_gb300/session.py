@@ -149,6 +149,9 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "tm_host_register": (C.c_int, [P, C.c_int64]),
         "tm_host_unregister": (C.c_int, [P]),
         "tm_session_set_diagnostics": (C.c_int, [P, C.c_int]),
+        "tm_colony_add_async": (C.c_int, [P, C.POINTER(_Input), C.POINTER(_Options), C.POINTER(C.c_int)]),
+        "tm_session_fence": (C.c_int, [P, C.POINTER(C.c_int64)]),
+        "tm_session_wait": (C.c_int, [P, C.c_int64]),
         "tm_colony_sample_neighbours": (C.c_int, [P, C.c_int, P, C.c_int64, C.c_int]),
         "tm_colony_read_neighbours": (C.c_int, [P, C.c_int, P, P]),
     }
@@ -292,7 +295,8 @@ class Session:
         self.dim = dim
         self.diagnostics = diagnostics
         self._n = {}
-        self._keep_async = []          # arrays of queued asynchronous uploads, held until sync()
+        self._keep_async = []          # (fence id after them, arrays) of queued asynchronous uploads
+        self._fences = 0               # id of the next fence
         self._grid = {}
 
     # -- lifetime ---------------------------------------------------------
@@ -328,12 +332,17 @@ class Session:
 
     def add_colony(self, col: Colony, *, precision: str = "fp64", update: str = "reference", dt: float = 1.0,
                    cic: bool = False, gfh: float = 8.0, lcap: int = 0, reserve: int = 0, verlet: bool = False,
-                   skin: float = 0.0, rmax: int = 0) -> int:
+                   skin: float = 0.0, rmax: int = 0, wait: bool = True) -> int:
+        """Add a colony; wait=False queues it behind the work in flight
+        (tm_colony_add_async) instead of waiting for the copies."""
         inp, keep = self._input(col)
         opt = _Options(PREC[precision], UPDATE[update], float(dt), 1 if cic else 0, float(gfh), int(lcap),
                        int(reserve), 1 if verlet else 0, float(skin), int(rmax))
         cid = C.c_int(-1)
-        _check(load_library().tm_colony_add(self._h, C.byref(inp), C.byref(opt), C.byref(cid)))
+        fn = load_library().tm_colony_add if wait else load_library().tm_colony_add_async
+        _check(fn(self._h, C.byref(inp), C.byref(opt), C.byref(cid)))
+        if not wait:
+            self._keep_async.append((self._fences, keep))
         self._n[cid.value] = col.n
         if cic:
             g = int((2049.0 + 1) / gfh) + 1
@@ -358,7 +367,7 @@ class Session:
         """Queue the re-upload of the colony's cells (same n, same order); the
         arrays must stay unchanged until sync()."""
         inp, keep = self._input(col)
-        self._keep_async.append(keep)
+        self._keep_async.append((self._fences, keep))
         _check(load_library().tm_colony_upload_async(self._h, cid, C.byref(inp)))
 
     def download_async(self, cid: int, fields, out: dict):
@@ -441,6 +450,18 @@ class Session:
     def sync(self):
         _check(load_library().tm_session_sync(self._h))
         self._keep_async.clear()
+
+    def fence(self) -> int:
+        """A fence after the work queued so far (see tm_session_fence)."""
+        f = C.c_int64(-1)
+        _check(load_library().tm_session_fence(self._h, C.byref(f)))
+        self._fences = int(f.value) + 1
+        return int(f.value)
+
+    def wait(self, fence: int):
+        """Wait for a fence; the arrays of asynchronous uploads queued before it are released."""
+        _check(load_library().tm_session_wait(self._h, int(fence)))
+        self._keep_async = [(t, k) for t, k in self._keep_async if t > fence]
 
     def use_graph(self, on: bool = True):
         _check(load_library().tm_session_use_graph(self._h, 1 if on else 0))
