@@ -695,6 +695,7 @@ def main():
     ap.add_argument("--rmax", type=int, default=64, help="rebuild the neighbour lists at least every rmax steps")
     ap.add_argument("--skin", type=float, default=0.1, help="neighbour-list skin as a fraction of h (before tuning)")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (launch shapes, list skin)")
+    ap.add_argument("--list-variant", type=int, default=0, help="list kernel variant (with --no-tune; 0: default)")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched and serving forms")
     ap.add_argument("--batch-colonies", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=50)
@@ -733,6 +734,8 @@ def main():
 
         s = S.Session(col.types, dim=3, max_slots=n + 64, device=local, list_capacity=args.list_capacity)
         s.set_tuning(skin_over_h=args.skin, rmax=args.rmax)
+        if args.list_variant:
+            s.set_tuning(list_variant=args.list_variant)
         verlet = args.list_capacity > 0
 
         def add():

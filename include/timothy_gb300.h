@@ -114,6 +114,7 @@ typedef struct {
     float list_maxdisp;               /* largest cell displacement since the lists were built */
     float list_skin;                  /* the colony's list skin */
     int32_t list_age;                 /* steps since the lists were built */
+    int64_t density_fp64_cells;       /* FP32 path: cells of the last step whose density was redone in FP64 */
 } tm_colony_info;
 
 const char *tm_last_error(void);

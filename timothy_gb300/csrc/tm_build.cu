@@ -30,6 +30,7 @@ __global__ void k_step_init(tm_arrays a)
     f.nbig = 0;
     f.boundary_pairs = 0;
     f.codes_slow = 0;
+    f.fix64 = 0;
     // Neighbour lists stay valid while no pair can have come from beyond
     // h + skin to within h: every cell moved less than skin/2 since the lists
     // were built (maxdisp carries a float-rounding margin).

@@ -125,7 +125,10 @@ __device__ __forceinline__ bool within32_at(const tm_type &T, float s, const tm_
 // FP32 + compensated pair (caller decided it is within h).  The kernel
 // value's error estimate is term / (1 - u) (W ~ (1-u)^3 amplifies the FP32
 // error of 1 - u near the cutoff), formed without a division: outside
-// u = 1/2 it is ms * 2 cW (1-u)^2, inside it is bounded by 2 * term.
+// u = 1/2 it is ms * 2 cW (1-u)^2 exactly; inside, where 1 - u lies in
+// [1/2, 1], 1 / (1 - u) is bounded by the chord 3 - 2 (1 - u) (at most 12.5 %
+// above it), so cells are flagged for the FP64 density a little early,
+// never late.
 __device__ __forceinline__ void pair32(const tm_type &T, int dim, float dx, float dy, float dz, float s,
                                        float sizej, pair_acc<1> &acc)
 {
@@ -145,13 +148,35 @@ __device__ __forceinline__ void pair32(const tm_type &T, int dim, float dx, floa
     const float wk = inner ? w_in : q2 * omu;
     const float ms = T.kmassf * sizej;
     acc.dens.add(ms * wk);
-    const float ek = ms * (inner ? 2.0f * w_in : q2);
+    const float ek = ms * (inner ? w_in * fmaf(-2.0f, omu, 3.0f) : q2);
     acc.err2 = fmaf(ek, ek, acc.err2);
     const float wg = inner ? u * fmaf(3.0f, u, -2.0f) : -o2;
     const float g = wg * T.cGf * rs;
     acc.fx.add(g * dx);
     acc.fy.add(g * dy);
     if (dim == 3) acc.fz.add(g * dz);
+}
+
+// The terms of one pair within h, without the accumulation (pair32 above):
+// density term, its error estimate and the gradient factor g (force = g * d).
+__device__ __forceinline__ void pair32_terms(const tm_type &T, float s, float sizej, float &term, float &ek,
+                                             float &g)
+{
+    const float rs = rsqrtf(fmaxf(s, 1.0e-30f));
+    float dist = s * rs;
+    dist = fmaf(0.5f * rs, fmaf(-dist, dist, s), dist);
+    const float u = dist * T.inv_hf;
+    const float omu = (T.hf - dist) * T.inv_hf;
+    const bool inner = u <= 0.5f;
+    const float o2 = omu * omu;
+    const float q2 = (2.0f * T.cWf) * o2;
+    const float w_in = T.cWf * fmaf(6.0f * u * u, u - 1.0f, 1.0f);
+    const float wk = inner ? w_in : q2 * omu;
+    const float ms = T.kmassf * sizej;
+    term = ms * wk;
+    ek = ms * (inner ? w_in * fmaf(-2.0f, omu, 3.0f) : q2);
+    const float wg = inner ? u * fmaf(3.0f, u, -2.0f) : -o2;
+    g = wg * T.cGf * rs;
 }
 
 // write one cell's results (both pair kernels)
@@ -184,6 +209,7 @@ __device__ __forceinline__ void pair_store(const tm_arrays &a, long long i, pair
         if (queue && needs_fix64(acc)) {
             const int q = atomicAdd(a.fix_count, 1);
             a.fix_list[q] = (int)i;
+            atomicAdd(&a.frame[a.col[i]].fix64, 1ull);
         }
         a.mindist[i] = cnt_nb ? (double)sqrtf(acc.mins) : 1.7976931348623157e308;
         a.fx[i] = (double)acc.fx.value();
@@ -763,7 +789,57 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_plist32(tm_arrays a, const tm_c
             if (DIAG) diag_pair(a, drow, j, hash);
         }
     };
-    if constexpr (D == 0) {
+    if constexpr (D < 0) {
+        // two entries per iteration without branches on the cutoff: both
+        // entries' terms are formed, those of an entry beyond h (or absent)
+        // are zeroed, and each accumulator takes the pair's sum in one
+        // compensated add.  The pre-add rounds once per pair, an error of the
+        // same order as the compensated sum's own (eps times the sum of the
+        // magnitudes), and halves the compensated adds.
+        int k = q;
+        int ja = k < cnt ? __ldg(lst + k * ls) : 0;
+        int jb = k + LPC < cnt ? __ldg(lst + (k + LPC) * ls) : 0;
+        for (; k < cnt; k += 2 * LPC) {
+            const int kn = k + 2 * LPC;
+            const int na = kn < cnt ? __ldg(lst + kn * ls) : 0;
+            const int nb = kn + LPC < cnt ? __ldg(lst + (kn + LPC) * ls) : 0;
+            const bool hasb = k + LPC < cnt;
+            const float4 ha = __ldg(hi + ja), la = __ldg(lo + ja);
+            const float4 hb = __ldg(hi + jb), lb = __ldg(lo + jb);
+            const float dxa = (ha.x - hi_i.x) + (la.x - lo_i.x), dya = (ha.y - hi_i.y) + (la.y - lo_i.y),
+                        dza = (ha.z - hi_i.z) + (la.z - lo_i.z);
+            const float dxb = (hb.x - hi_i.x) + (lb.x - lo_i.x), dyb = (hb.y - hi_i.y) + (lb.y - lo_i.y),
+                        dzb = (hb.z - hi_i.z) + (lb.z - lo_i.z);
+            const float sa = fmaf(dxa, dxa, fmaf(dya, dya, dza * dza));
+            const float sb = fmaf(dxb, dxb, fmaf(dyb, dyb, dzb * dzb));
+            bool ina = sa <= thr_lo, inb = hasb && sb <= thr_lo;
+            if (!ina && sa <= thr_hi) ina = dist64(a, i, ja) <= T.h;            // FP64 only in the band
+            if (hasb && !inb && sb <= thr_hi) inb = dist64(a, i, jb) <= T.h;
+            float ta, ea, ga, tb, eb, gb;
+            pair32_terms(T, sa, ha.w, ta, ea, ga);
+            pair32_terms(T, sb, hb.w, tb, eb, gb);
+            ta = ina ? ta : 0.0f;
+            ea = ina ? ea : 0.0f;
+            ga = ina ? ga : 0.0f;
+            tb = inb ? tb : 0.0f;
+            eb = inb ? eb : 0.0f;
+            gb = inb ? gb : 0.0f;
+            acc.dens.add(ta + tb);
+            acc.err2 = fmaf(ea, ea, fmaf(eb, eb, acc.err2));
+            acc.fx.add(fmaf(ga, dxa, gb * dxb));
+            acc.fy.add(fmaf(ga, dya, gb * dyb));
+            if (dim == 3) acc.fz.add(fmaf(ga, dza, gb * dzb));
+            acc.mins = fminf(acc.mins, fminf(ina ? sa : 3.0e38f, inb ? sb : 3.0e38f));
+            cnt_nb += (ina ? 1 : 0) + (inb ? 1 : 0);
+            nbmin = min(nbmin, min(ina ? __float_as_int(la.w) : 0x7fffffff, inb ? __float_as_int(lb.w) : 0x7fffffff));
+            if (DIAG) {
+                if (ina) diag_pair(a, drow, ja, hash);
+                if (inb) diag_pair(a, drow, jb, hash);
+            }
+            ja = na;
+            jb = nb;
+        }
+    } else if constexpr (D == 0) {
         int k = q;
         int ja = k < cnt ? __ldg(lst + k * ls) : 0;
         int jb = k + LPC < cnt ? __ldg(lst + (k + LPC) * ls) : 0;
@@ -847,6 +923,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_plist32(tm_arrays a, const tm_c
     }
     tm_queue_walk(a, i, cnt_nb == 0, walk);
     if (needs_fix64(acc)) {
+        atomicAdd(&a.frame[c].fix64, 1ull);
         // FP64 density over the same list, the cutoff decided in FP64
         double dens = 0.0;
         for (int kk = 0; kk < cnt; kk++) {
@@ -924,9 +1001,9 @@ static void launch_plist32(const tm_arrays &a, const tm_consts *K, int variant, 
     const long long nt = a.nslots_total * PLIST_LPC;
     switch (variant) {
     case 2: k_plist32<128, 7, 0, DIAG><<<(unsigned)((nt + 127) / 128), 128, 0, st>>>(a, K); break;
-    case 3: k_plist32<128, 7, 6, DIAG><<<(unsigned)((nt + 127) / 128), 128, 0, st>>>(a, K); break;
-    case 4: k_plist32<256, 3, 4, DIAG><<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(a, K); break;
-    default: k_plist32<128, 7, 4, DIAG><<<(unsigned)((nt + 127) / 128), 128, 0, st>>>(a, K); break;
+    case 3: k_plist32<128, 7, 4, DIAG><<<(unsigned)((nt + 127) / 128), 128, 0, st>>>(a, K); break;
+    case 4: k_plist32<256, 4, -1, DIAG><<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(a, K); break;
+    default: k_plist32<128, 7, -1, DIAG><<<(unsigned)((nt + 127) / 128), 128, 0, st>>>(a, K); break;
     }
 }
 

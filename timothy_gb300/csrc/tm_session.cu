@@ -1682,6 +1682,7 @@ extern "C" int tm_colony_stats(tm_session *s, int id, tm_colony_info *st)
     st->n = c.n;
     st->list_rebuilds = (int64_t)f.rebuilds;
     st->codes_slow = (int64_t)f.codes_slow;
+    st->density_fp64_cells = (int64_t)f.fix64;
     memcpy(&st->list_maxdisp, &f.maxdisp, sizeof(float));   // stored as the float's bits
     st->list_skin = s->h_desc[id].skin;
     st->list_age = f.age;
