@@ -229,7 +229,9 @@ int tm_colony_cellcycle(tm_session *s, int id, const tm_cycle_params *p, int64_t
  * through tm_colony_upload); a cell type outside the table is read as 0 and
  * reported as TM_DEVERR_TYPES by the next tm_session_sync.  Both return once
  * the work is queued: the caller leaves in's arrays unchanged, and reads
- * out's arrays only, after tm_session_sync.  An asynchronous upload reads
+ * out's arrays only, after tm_session_sync.  With the same n, the upload's
+ * size, young, ctype and phase may be NULL: those attributes keep their
+ * values (an upload of positions only).  An asynchronous upload reads
  * its arrays only after the positions (x, y, z) of the asynchronous download
  * queued before it have reached the host, so a host loop may pass one step's
  * downloaded positions to the next step's upload without waiting; the other

@@ -1000,9 +1000,11 @@ static void launch_plist32(const tm_arrays &a, const tm_consts *K, int variant, 
     // PLIST_LPC threads per slot (a warp holds 32 / PLIST_LPC cells)
     const long long nt = a.nslots_total * PLIST_LPC;
     switch (variant) {
-    case 2: k_plist32<128, 7, 0, DIAG><<<(unsigned)((nt + 127) / 128), 128, 0, st>>>(a, K); break;
-    case 3: k_plist32<128, 7, 4, DIAG><<<(unsigned)((nt + 127) / 128), 128, 0, st>>>(a, K); break;
-    case 4: k_plist32<256, 4, -1, DIAG><<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(a, K); break;
+    // every variant accumulates alike (the paired form), so the block shape
+    // changes no result bit
+    case 2: k_plist32<256, 4, -1, DIAG><<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(a, K); break;
+    case 3: k_plist32<64, 14, -1, DIAG><<<(unsigned)((nt + 63) / 64), 64, 0, st>>>(a, K); break;
+    case 4: k_plist32<256, 3, -1, DIAG><<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(a, K); break;
     default: k_plist32<128, 7, -1, DIAG><<<(unsigned)((nt + 127) / 128), 128, 0, st>>>(a, K); break;
     }
 }

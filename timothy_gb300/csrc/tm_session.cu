@@ -101,6 +101,12 @@ struct range_alloc {
         for (auto &f : freel) s += f.second;
         return s;
     }
+    long long largest() const
+    {
+        long long m = 0;
+        for (auto &f : freel) m = std::max(m, f.second);
+        return m;
+    }
 };
 
 struct colony_host {
@@ -241,7 +247,14 @@ union up_rec {
     int4 v[3];
 };
 
-__global__ void k_upload_pack(upload_src u, int n, int has_phase, int4 *rec)
+// fields an upload carries besides the positions (the others keep their values)
+#define UP_PHASE 1
+#define UP_SIZE 2
+#define UP_YOUNG 4
+#define UP_CTYPE 8
+#define UP_ALL (UP_SIZE | UP_YOUNG | UP_CTYPE)
+
+__global__ void k_upload_pack(upload_src u, int n, int fields, int4 *rec)
 {
     const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
@@ -250,10 +263,10 @@ __global__ void k_upload_pack(upload_src u, int n, int has_phase, int4 *rec)
     r.f.x = u.x[src];
     r.f.y = u.y[src];
     r.f.z = u.z[src];
-    r.f.size = u.size[src];
-    r.f.young = u.young[src];
-    r.f.ctype = u.ctype[src];
-    r.f.phase = has_phase ? u.phase[src] : 0;
+    r.f.size = (fields & UP_SIZE) ? u.size[src] : 0.0;
+    r.f.young = (fields & UP_YOUNG) ? u.young[src] : 0.0f;
+    r.f.ctype = (fields & UP_CTYPE) ? u.ctype[src] : 0;
+    r.f.phase = (fields & UP_PHASE) ? u.phase[src] : 0;
     r.f.pad = 0;
     int4 *d = rec + src * 3;
     d[0] = r.v[0];
@@ -261,7 +274,7 @@ __global__ void k_upload_pack(upload_src u, int n, int has_phase, int4 *rec)
     d[2] = r.v[2];
 }
 
-__global__ void k_upload_keep(tm_arrays a, const tm_consts *K, int c, long long off, int n, int has_phase,
+__global__ void k_upload_keep(tm_arrays a, const tm_consts *K, int c, long long off, int n, int fields,
                               int *bad, const int4 *rec, long long base)
 {
     const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -272,21 +285,26 @@ __global__ void k_upload_keep(tm_arrays a, const tm_consts *K, int c, long long 
     r.v[0] = p[0];
     r.v[1] = p[1];
     r.v[2] = p[2];
-    const double x = r.f.x, y = r.f.y, z = r.f.z, sz = r.f.size;
-    int ct = r.f.ctype;
-    if (ct < 0 || ct >= K->ntypes) {
-        if (bad) atomicExch(bad, 1);
-        else atomicOr(&a.frame[c].error, TM_ERR_TYPES);
-        ct = 0;
+    const double x = r.f.x, y = r.f.y, z = r.f.z;
+    if (fields & UP_CTYPE) {
+        int ct = r.f.ctype;
+        if (ct < 0 || ct >= K->ntypes) {
+            if (bad) atomicExch(bad, 1);
+            else atomicOr(&a.frame[c].error, TM_ERR_TYPES);
+            ct = 0;
+        }
+        if (ct != a.ctype[s]) a.frame[c].force_rebuild = 1;
+        a.ctype[s] = ct;
     }
-    if (sz != a.size[s] || ct != a.ctype[s]) a.frame[c].force_rebuild = 1;
+    if (fields & UP_SIZE) {
+        if (r.f.size != a.size[s]) a.frame[c].force_rebuild = 1;
+        a.size[s] = r.f.size;
+    }
     a.x[s] = x;
     a.y[s] = y;
     a.z[s] = z;
-    a.size[s] = sz;
-    a.young[s] = r.f.young;
-    a.ctype[s] = ct;
-    if (has_phase) a.phase[s] = r.f.phase;
+    if (fields & UP_YOUNG) a.young[s] = r.f.young;
+    if (fields & UP_PHASE) a.phase[s] = r.f.phase;
     a.rem[s] = 0;
     if (a.desc[c].verlet && a.x0) {
         float hx, hy, hz, lx, ly, lz;
@@ -855,8 +873,10 @@ static int copy_cells_in(tm_session *s, const colony_host &c, const tm_colony_in
         int4 *rec = nullptr;
         int rc = upload_records(s, &rec);
         if (rc) return rc;
-        k_upload_pack<<<blocks_for((long long)n, 256), 256, 0, st>>>(u, (int)n, in->phase ? 1 : 0, rec);
-        k_upload_keep<<<blocks_for((long long)n, 256), 256, 0, st>>>(a, s->dK, cid, o, (int)n, in->phase ? 1 : 0,
+        k_upload_pack<<<blocks_for((long long)n, 256), 256, 0, st>>>(u, (int)n, UP_ALL | (in->phase ? UP_PHASE : 0),
+                                                                    rec);
+        k_upload_keep<<<blocks_for((long long)n, 256), 256, 0, st>>>(a, s->dK, cid, o, (int)n,
+                                                                    UP_ALL | (in->phase ? UP_PHASE : 0),
                                                                     s->d_flag, rec, o);
     } else {
         k_check_types<<<blocks_for((long long)n, 256), 256, 0, st>>>(a, s->dK, o, (int)n, s->d_flag);
@@ -920,7 +940,14 @@ extern "C" int tm_colony_add_async(tm_session *s, const tm_colony_input *in, con
 
 static int colony_add(tm_session *s, const tm_colony_input *in, const tm_colony_options *opt, int *id, bool wait)
 {
-    if (!s || !opt || !id) return tm_fail(TM_EINVAL, "null argument");
+    if (!s || !opt || !id || !in) return tm_fail(TM_EINVAL, "null argument");
+    // room first: a request that cannot fit is turned away before any pass
+    // over its cells (admission control tries many)
+    {
+        const long long want = std::max<long long>(std::max<long long>(in->n, opt->reserve), 1);
+        if ((want + 31) / 32 > s->slots.largest())
+            return tm_fail(TM_ENOMEM, "no room for %lld slots", (long long)want);
+    }
     int rc = check_input(s, in);
     if (rc) return rc;
     if (opt->precision != TM_PREC_FP64 && opt->precision != TM_PREC_FP32C) return tm_fail(TM_EINVAL, "bad precision");
@@ -1098,10 +1125,16 @@ extern "C" int tm_colony_upload_async(tm_session *s, int id, const tm_colony_inp
 {
     int rc = lookup(s, id);
     if (rc) return rc;
-    rc = check_input(s, in, false);
-    if (rc) return rc;
+    if (!in || in->n < 0 || (in->n > 0 && (!in->x || !in->y || !in->z)))
+        return tm_fail(TM_EINVAL, "bad colony input");
     colony_host &c = s->cols[id];
-    if (in->n != c.n || c.n == 0) return tm_colony_upload(s, id, in);
+    const int fields = (in->size ? UP_SIZE : 0) | (in->young ? UP_YOUNG : 0) | (in->ctype ? UP_CTYPE : 0) |
+                       (in->phase ? UP_PHASE : 0);
+    if (in->n != c.n || c.n == 0) {
+        if ((fields & UP_ALL) != UP_ALL)
+            return tm_fail(TM_EINVAL, "an upload that changes the cell count carries every field");
+        return tm_colony_upload(s, id, in);
+    }
     CK(cudaSetDevice(s->device));
     if ((rc = async_io_init(s))) return rc;
     const size_t S = (size_t)s->slots.hwm * 32 + 32, need = S * 44;
@@ -1128,9 +1161,9 @@ extern "C" int tm_colony_upload_async(tm_session *s, int id, const tm_colony_inp
     CK(cudaMemcpyAsync(X + o, in->x, n * 8, cudaMemcpyHostToDevice, h));
     CK(cudaMemcpyAsync(Y + o, in->y, n * 8, cudaMemcpyHostToDevice, h));
     CK(cudaMemcpyAsync(Z + o, in->z, n * 8, cudaMemcpyHostToDevice, h));
-    CK(cudaMemcpyAsync(SZ + o, in->size, n * 8, cudaMemcpyHostToDevice, h));
-    CK(cudaMemcpyAsync(YG + o, in->young, n * 4, cudaMemcpyHostToDevice, h));
-    CK(cudaMemcpyAsync(CT + o, in->ctype, n * 4, cudaMemcpyHostToDevice, h));
+    if (in->size) CK(cudaMemcpyAsync(SZ + o, in->size, n * 8, cudaMemcpyHostToDevice, h));
+    if (in->young) CK(cudaMemcpyAsync(YG + o, in->young, n * 4, cudaMemcpyHostToDevice, h));
+    if (in->ctype) CK(cudaMemcpyAsync(CT + o, in->ctype, n * 4, cudaMemcpyHostToDevice, h));
     if (in->phase) CK(cudaMemcpyAsync(PH + o, in->phase, n * 4, cudaMemcpyHostToDevice, h));
     CK(cudaEventRecord(s->ev_h2d, h));
     CK(cudaStreamWaitEvent(s->stream, s->ev_h2d, 0));
@@ -1138,10 +1171,10 @@ extern "C" int tm_colony_upload_async(tm_session *s, int id, const tm_colony_inp
     const upload_src u = {X, Y, Z, SZ, YG, CT, PH, o};
     int4 *rec = nullptr;
     if ((rc = upload_records(s, &rec))) return rc;
-    k_upload_pack<<<blocks_for((long long)n, 256), 256, 0, s->stream>>>(u, (int)n, in->phase ? 1 : 0, rec);
+    k_upload_pack<<<blocks_for((long long)n, 256), 256, 0, s->stream>>>(u, (int)n, fields, rec);
     CK(cudaGetLastError());
     CK(cudaEventRecord(s->ev_up_read, s->stream));   // the staging is free for the next upload's copies
-    k_upload_keep<<<blocks_for((long long)n, 256), 256, 0, s->stream>>>(a, s->dK, id, o, (int)n, in->phase ? 1 : 0,
+    k_upload_keep<<<blocks_for((long long)n, 256), 256, 0, s->stream>>>(a, s->dK, id, o, (int)n, fields,
                                                                       nullptr, rec, o);
     CK(cudaGetLastError());
     s->up_pending = true;
@@ -1918,7 +1951,8 @@ extern "C" int tmi_upload_aos_keep(tm_session *s, int cid, const void *cells, in
     if ((rc = upload_records(s, &rec))) return rc;
     const tm_arrays a = view(s, s->parity);
     k_aos_to_rec<<<blocks_for(n, 256), 256, 0, s->stream>>>((const unsigned char *)g_stage.ptr, *lay, n, rec, c.off);
-    k_upload_keep<<<blocks_for(n, 256), 256, 0, s->stream>>>(a, s->dK, cid, c.off, (int)n, lay->phase >= 0 ? 1 : 0,
+    k_upload_keep<<<blocks_for(n, 256), 256, 0, s->stream>>>(a, s->dK, cid, c.off, (int)n,
+                                                            UP_ALL | (lay->phase >= 0 ? UP_PHASE : 0),
                                                             nullptr, rec, c.off);
     CK(cudaGetLastError());
     return TM_OK;

@@ -371,6 +371,15 @@ class Session:
         self._keep_async.append((self._fences, keep))
         _check(load_library().tm_colony_upload_async(self._h, cid, C.byref(inp)))
 
+    def upload_positions_async(self, cid: int, x, y, z):
+        """Queue an upload of new positions only (same cells, same order; the
+        other attributes keep their values); the arrays must stay unchanged
+        until sync()."""
+        arrs = [np.ascontiguousarray(a, np.float64) for a in (x, y, z)]
+        inp = _Input(len(arrs[0]), *[_p(a) for a in arrs], None, None, None, None)
+        self._keep_async.append((self._fences, arrs))
+        _check(load_library().tm_colony_upload_async(self._h, cid, C.byref(inp)))
+
     def download_async(self, cid: int, fields, out: dict):
         """Queue the copy of results into out's arrays (caller order); they are
         valid after sync()."""
