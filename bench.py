@@ -49,9 +49,9 @@ UNIT = "cell-updates/s"
 B_CELL = 112
 # DRAM bytes per cell of one list-pass launch (dram__bytes_read.sum +
 # dram__bytes_write.sum over the cells of the launch), from the ncu capture
-# summarised in profiles/k_plist_fp32_clustered2m.txt; traffic grows with the
+# summarised in profiles/k_plist32_fp32_clustered2m.txt; traffic grows with the
 # cell count, so a launch over n cells moves n times this.
-TRAFFIC_PER_CELL = {"k_plist<1>": 376.1}
+TRAFFIC_PER_CELL = {"k_plist32": 370.7}
 WORKLOADS = {
     "precision16m": dict(kind="clustered", n=16_000_000, seed=3, precision="fp32c", cic=False, dt=0.01),
     "scale1m": dict(kind="clustered", n=1_000_000, seed=2, precision="fp64", cic=True, dt=0.01),
@@ -782,7 +782,7 @@ def main():
     # dominant kernel: the list pass (k_plist), one launch per step
     list_ms = prof["list_ms"] if prof["list_ms"] > 0 else prof["pair_ms"]
     achieved = B_CELL * n / (list_ms * 1e-3) / 1e9 if list_ms > 0 else None
-    kname = "k_plist<%d>" % (1 if prec == "fp32c" else 0)
+    kname = "k_plist32" if prec == "fp32c" else "k_plist<0>"
     traffic = TRAFFIC_PER_CELL.get(kname)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak if achieved else None,
@@ -887,19 +887,24 @@ def main():
             "config": {"workload": args.workload, "kind": kind, "cells": n, "seed": seed, "h": 2.5, "dt": wl["dt"],
                        "cic": wl["cic"], "precision": prec, "mean_neighbours": r4(mean_nb),
                        "max_neighbours": max_nb, "list_capacity": args.list_capacity,
-                       "tuning": (tuned.get(prec) or {}).get("tuning"),
-                       "l2": "inputs larger than L2 (state %.1f GB)" % (n * 250 / 1e9),
+                       "l2": "inputs > L2",
                        "parallelism": f"replicas x{world}"},
             "roofline": {k: (r4(v) if not isinstance(v, str) else v) for k, v in roofline.items()
-                         if k not in ("phases_ms", "traffic_unit", "peak_source")},
+                         if k not in ("phases_ms", "traffic_unit", "peak_source", "kernel")},
             "phases_ms": {k[:-3]: r4(v) for k, v in prof.items() if k.endswith("_ms") and k != "pair_ms"},
             "rebuilds": rebuilds,
-            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk}
-    line["roofline"]["peak_source"] = peak_kind
+            "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clk}
+    line["roofline"]["kernel"] = kname
+    if e2e is not None:
+        line["e2e"] = {k: r4(v) if not isinstance(v, str) else v for k, v in e2e.items() if k != "api"}
+    if cpu is not None:
+        line["cpu_baseline"] = {k: r4(v) if not isinstance(v, str) else v for k, v in cpu.items()}
+    if clk:
+        line["clocks"] = {k: r4(v) if isinstance(v, (int, float)) else v for k, v in clk.items()}
     for k in ("fp64", "fp32c_over_fp64", "error_vs_fp64", "neighbour_check"):
         if k in extra:
             v = extra[k]
-            line[k] = {q: r4(w) if not isinstance(w, str) else w for q, w in v.items()} if isinstance(v, dict) \
+            line[k] = {q: r4(w) for q, w in v.items() if not isinstance(w, str)} if isinstance(v, dict) \
                 else r4(v)
     if "scale1m" in detail:
         sc = detail["scale1m"]
@@ -918,6 +923,7 @@ def main():
                          "serving": [{"rate": r4(f["rate_per_s"]), "served": r4(f["served_cell_updates_per_s"]),
                                       "p50": r4(f["p50_s"]), "p99": r4(f["p99_s"])}
                                      for f in detail["forms"]["serving"]]}
+    detail["tuning"] = tuned
     if rank == 0:
         full = dict(line)
         full.update(detail)

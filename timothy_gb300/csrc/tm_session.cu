@@ -147,6 +147,7 @@ struct tm_session {
     cudaEvent_t ev_up_read = nullptr;     // k_upload_pack has read up_stage
     cudaEvent_t ev_dl_gathered = nullptr, ev_dl_copied = nullptr;
     cudaEvent_t ev_dl_pos = nullptr;      // the positions of the last asynchronous download are on the host
+    cudaEvent_t ev_dl_part[16] = {};      // one field of an asynchronous download gathered
     bool dl_pending = false, up_pending = false;
     cudaEvent_t ev_ready[2] = {nullptr, nullptr}, ev_copied[2] = {nullptr, nullptr};
     // profiling
@@ -783,6 +784,8 @@ extern "C" int tm_session_destroy(tm_session *s)
     if (s->ev_h2d) cudaEventDestroy(s->ev_h2d);
     for (cudaEvent_t e : {s->ev_up_read, s->ev_dl_gathered, s->ev_dl_copied, s->ev_dl_pos})
         if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : s->ev_dl_part)
+        if (e) cudaEventDestroy(e);
     if (s->up_stage) cudaFree(s->up_stage);
     if (s->dl_stage) cudaFree(s->dl_stage);
     if (s->dl_grid) cudaFree(s->dl_grid);
@@ -1113,6 +1116,7 @@ static int async_io_init(tm_session *s)
     CK(cudaStreamCreateWithFlags(&s->h2d_stream, cudaStreamNonBlocking));
     for (cudaEvent_t *e : {&s->ev_h2d, &s->ev_up_read, &s->ev_dl_gathered, &s->ev_dl_copied, &s->ev_dl_pos})
         CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    for (cudaEvent_t &e : s->ev_dl_part) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     return TM_OK;
 }
 
@@ -1578,6 +1582,10 @@ static int download_async_queue(tm_session *s, int id, const tm_colony_output *o
         {a.rem, out->removecell, 1}, {a.nbcount, out->nbcount, 4},
         {a.nbhash, a.nbhash ? (void *)out->nbhash : nullptr, 8}, {a.vcand, a.vcand ? (void *)out->vcand : nullptr, 4}};
     std::vector<std::pair<void *, std::pair<const void *, size_t>>> copies;
+    // the last of the positions asked for: a following asynchronous upload
+    // waits for it to reach the host
+    const void *last_pos = out->z ? (const void *)a.z : out->y ? (const void *)a.y : out->x ? (const void *)a.x
+                                                                                              : nullptr;
     if (c.n > 0) {
         int *iperm = (int *)(s->dl_stage + (size_t)DL_MAX_FIELDS * S * 8);
         bool inverted = false;
@@ -1599,9 +1607,14 @@ static int download_async_queue(tm_session *s, int id, const tm_colony_output *o
             else
                 k_unsort_gather<unsigned char><<<g, 256, 0, s->stream>>>((const unsigned char *)w.src, iperm, c.off,
                                                                         c.n, dst);
+            // each field travels as soon as it is gathered, the positions first
+            CK(cudaGetLastError());
+            CK(cudaEventRecord(s->ev_dl_part[part - 1], s->stream));
+            CK(cudaStreamWaitEvent(s->copy_stream, s->ev_dl_part[part - 1], 0));
+            CK(cudaMemcpyAsync(w.host, dst, (size_t)w.size * (size_t)c.n, cudaMemcpyDeviceToHost, s->copy_stream));
             copies.push_back({w.host, {(const void *)dst, (size_t)w.size * (size_t)c.n}});
+            if (w.src == last_pos) CK(cudaEventRecord(s->ev_dl_pos, s->copy_stream));
         }
-        CK(cudaGetLastError());
     }
     // the grid goes through staging of its own too: the next step clears and
     // deposits the session grid while this copy may still be running
@@ -1620,14 +1633,7 @@ static int download_async_queue(tm_session *s, int id, const tm_colony_output *o
     }
     CK(cudaEventRecord(s->ev_dl_gathered, s->stream));
     CK(cudaStreamWaitEvent(s->copy_stream, s->ev_dl_gathered, 0));
-    // positions first (the parts of x, y, z come first in the staging), then
-    // the event a following asynchronous upload waits for
     const int npos = (out->x ? 1 : 0) + (out->y ? 1 : 0) + (out->z ? 1 : 0);
-    for (size_t k = 0; k < copies.size(); k++) {
-        CK(cudaMemcpyAsync(copies[k].first, copies[k].second.first, copies[k].second.second, cudaMemcpyDeviceToHost,
-                           s->copy_stream));
-        if ((int)k + 1 == npos) CK(cudaEventRecord(s->ev_dl_pos, s->copy_stream));
-    }
     if (npos == 0 || copies.empty()) CK(cudaEventRecord(s->ev_dl_pos, s->copy_stream));
     if (want_grid)
         CK(cudaMemcpyAsync(out->grid, s->dl_grid, sizeof(double) * (size_t)c.ngrid, cudaMemcpyDeviceToHost,

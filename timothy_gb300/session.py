@@ -385,8 +385,9 @@ class Session:
         valid after sync()."""
         n = self._n[cid]
         for k in fields:
-            if k not in out or len(out[k]) < n:
-                raise ValueError(f"download_async needs an output array for {k} with {n} entries")
+            need = int(np.prod(self._grid[cid])) if k == "grid" else n
+            if k not in out or out[k].size < need or not out[k].flags.c_contiguous:
+                raise ValueError(f"download_async needs a contiguous output array for {k} with {need} entries")
         o = _Output(*[_p(out.get(k)) if k in fields else None for k, _ in _Output._fields_])
         _check(load_library().tm_colony_download_async(self._h, cid, C.byref(o)))
 
