@@ -654,29 +654,48 @@ def scale1m_record(local, steps, args):
     return out
 
 
-def dropin_record(n, kind, seed, cic, steps, warmup=1):
+def dropin_record(n, kind, seed, cic, steps, warmup=1, precision="fp64"):
     """The reference's own API: the step loop of a host program over the
     drop-ins (octbuild, patches_alloc, patches_cells2envinfo,
     computepotential, computegradient, updatepositions, octfree) on host
     celldata_t records, wall clock per step.  updatepositions draws the
-    caller's rand() for every cell as the reference does (cells.c:353-356)."""
+    caller's rand() for every cell as the reference does (cells.c:353-356).
+    precision "fp32c": tm_dropin_set_precision(TM_PREC_FP32C, lists on)."""
+    import ctypes
+
+    from timothy_gb300 import session as S
     from timothy_gb300.refabi import CELL_DTYPE, DropinRun
 
+    lib = S.load_library()
+    lib.tm_dropin_set_precision.argtypes = [ctypes.c_int, ctypes.c_int]
     col = C.make_colony(kind, n, seed, C.configured_radius(kind, n, seed))
-    run = DropinRun(col, cic=cic)
-    for _ in range(warmup):
-        run.step_loop()
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        run.step_loop()
-    dt = time.perf_counter() - t0
-    run.shutdown()
+    if precision == "fp32c":
+        lib.tm_dropin_set_precision(1, 1)
+    try:
+        run = DropinRun(col, cic=cic)
+        for _ in range(warmup):
+            run.step_loop()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            run.step_loop()
+        dt = time.perf_counter() - t0
+        # the same loop without updatepositions (its share: the host's rand()
+        # calls, the forces up, the positions and marks down, the update)
+        t1 = time.perf_counter()
+        for _ in range(steps):
+            run.step_loop(update=False)
+        dt_noupd = time.perf_counter() - t1
+        run.shutdown()
+    finally:
+        lib.tm_dropin_set_precision(0, 0)
     rec = CELL_DTYPE.itemsize
-    return {"cells": n, "kind": kind, "cic": cic, "steps": steps, "ms_per_step": dt / steps * 1e3,
+    return {"cells": n, "kind": kind, "cic": cic, "precision": precision, "steps": steps,
+            "ms_per_step": dt / steps * 1e3,
             "value": n * steps / dt, "unit": UNIT,
             # per step: the records up (octbuild); density, v, mindist and the
             # forces, then positions and removal marks down; forces and marks up
-            "h2d_bytes_per_step": n * (rec + 24 + 1), "d2h_bytes_per_step": n * (24 + 24 + 24 + 1)}
+            "h2d_bytes_per_step": n * (rec + 24 + 1), "d2h_bytes_per_step": n * (24 + 24 + 24 + 1),
+            "ms_per_step_without_updatepositions": dt_noupd / steps * 1e3}
 
 
 def main():
@@ -870,7 +889,7 @@ def main():
     if world == 1 and not args.no_dropin:
         detail["e2e_dropin"] = {"1m_cic": dropin_record(1_000_000, "clustered", 2, True, 5)}
         if n >= 16_000_000:
-            detail["e2e_dropin"]["16m"] = dropin_record(n, kind, seed, False, 2)
+            detail["e2e_dropin"]["16m"] = dropin_record(n, kind, seed, False, 3, precision=prec)
 
     if not args.no_forms and world == 1:
         detail["rows"] = {"grid_to_cell": field_rows(local, peak), "cic_deposit": cic_rows(local, peak),

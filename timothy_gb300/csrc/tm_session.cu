@@ -147,6 +147,7 @@ struct tm_session {
     cudaEvent_t ev_up_read = nullptr;     // k_upload_pack has read up_stage
     cudaEvent_t ev_dl_gathered = nullptr, ev_dl_copied = nullptr;
     cudaEvent_t ev_dl_pos = nullptr;      // the positions of the last asynchronous download are on the host
+    cudaEvent_t ev_dl_axis[3] = {};       // its x, y, z each
     cudaEvent_t ev_dl_part[16] = {};      // one field of an asynchronous download gathered
     bool dl_pending = false, up_pending = false;
     cudaEvent_t ev_ready[2] = {nullptr, nullptr}, ev_copied[2] = {nullptr, nullptr};
@@ -782,7 +783,8 @@ extern "C" int tm_session_destroy(tm_session *s)
     if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
     if (s->h2d_stream) cudaStreamDestroy(s->h2d_stream);
     if (s->ev_h2d) cudaEventDestroy(s->ev_h2d);
-    for (cudaEvent_t e : {s->ev_up_read, s->ev_dl_gathered, s->ev_dl_copied, s->ev_dl_pos})
+    for (cudaEvent_t e : {s->ev_up_read, s->ev_dl_gathered, s->ev_dl_copied, s->ev_dl_pos, s->ev_dl_axis[0],
+                          s->ev_dl_axis[1], s->ev_dl_axis[2]})
         if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : s->ev_dl_part)
         if (e) cudaEventDestroy(e);
@@ -1114,7 +1116,8 @@ static int async_io_init(tm_session *s)
     int rc = download_streams(s);
     if (rc) return rc;
     CK(cudaStreamCreateWithFlags(&s->h2d_stream, cudaStreamNonBlocking));
-    for (cudaEvent_t *e : {&s->ev_h2d, &s->ev_up_read, &s->ev_dl_gathered, &s->ev_dl_copied, &s->ev_dl_pos})
+    for (cudaEvent_t *e : {&s->ev_h2d, &s->ev_up_read, &s->ev_dl_gathered, &s->ev_dl_copied, &s->ev_dl_pos,
+                           &s->ev_dl_axis[0], &s->ev_dl_axis[1], &s->ev_dl_axis[2]})
         CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     for (cudaEvent_t &e : s->ev_dl_part) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     return TM_OK;
@@ -1159,12 +1162,16 @@ extern "C" int tm_colony_upload_async(tm_session *s, int id, const tm_colony_inp
     const size_t n = (size_t)in->n;
     cudaStream_t h = s->h2d_stream;
     if (s->up_pending) CK(cudaStreamWaitEvent(h, s->ev_up_read, 0));
-    // the positions of the asynchronous download queued before this upload
-    // reach the host first, so a loop may pass them to this upload
+    // each coordinate of the asynchronous download queued before this upload
+    // reaches the host before the same coordinate is read here, so a loop may
+    // pass them to this upload; x travels up while y and z still come down
+    double *dst3[3] = {X + o, Y + o, Z + o};
+    const double *src3[3] = {in->x, in->y, in->z};
+    for (int k = 0; k < 3; k++) {
+        if (s->dl_pending) CK(cudaStreamWaitEvent(h, s->ev_dl_axis[k], 0));
+        CK(cudaMemcpyAsync(dst3[k], src3[k], n * 8, cudaMemcpyHostToDevice, h));
+    }
     if (s->dl_pending) CK(cudaStreamWaitEvent(h, s->ev_dl_pos, 0));
-    CK(cudaMemcpyAsync(X + o, in->x, n * 8, cudaMemcpyHostToDevice, h));
-    CK(cudaMemcpyAsync(Y + o, in->y, n * 8, cudaMemcpyHostToDevice, h));
-    CK(cudaMemcpyAsync(Z + o, in->z, n * 8, cudaMemcpyHostToDevice, h));
     if (in->size) CK(cudaMemcpyAsync(SZ + o, in->size, n * 8, cudaMemcpyHostToDevice, h));
     if (in->young) CK(cudaMemcpyAsync(YG + o, in->young, n * 4, cudaMemcpyHostToDevice, h));
     if (in->ctype) CK(cudaMemcpyAsync(CT + o, in->ctype, n * 4, cudaMemcpyHostToDevice, h));
@@ -1586,6 +1593,8 @@ static int download_async_queue(tm_session *s, int id, const tm_colony_output *o
     // waits for it to reach the host
     const void *last_pos = out->z ? (const void *)a.z : out->y ? (const void *)a.y : out->x ? (const void *)a.x
                                                                                               : nullptr;
+    const void *pos3[3] = {a.x, a.y, a.z};
+    bool axis_sent[3] = {out->x && c.n > 0, out->y && c.n > 0, out->z && c.n > 0};
     if (c.n > 0) {
         int *iperm = (int *)(s->dl_stage + (size_t)DL_MAX_FIELDS * S * 8);
         bool inverted = false;
@@ -1613,6 +1622,8 @@ static int download_async_queue(tm_session *s, int id, const tm_colony_output *o
             CK(cudaStreamWaitEvent(s->copy_stream, s->ev_dl_part[part - 1], 0));
             CK(cudaMemcpyAsync(w.host, dst, (size_t)w.size * (size_t)c.n, cudaMemcpyDeviceToHost, s->copy_stream));
             copies.push_back({w.host, {(const void *)dst, (size_t)w.size * (size_t)c.n}});
+            for (int k = 0; k < 3; k++)
+                if (w.src == pos3[k]) CK(cudaEventRecord(s->ev_dl_axis[k], s->copy_stream));
             if (w.src == last_pos) CK(cudaEventRecord(s->ev_dl_pos, s->copy_stream));
         }
     }
@@ -1635,6 +1646,8 @@ static int download_async_queue(tm_session *s, int id, const tm_colony_output *o
     CK(cudaStreamWaitEvent(s->copy_stream, s->ev_dl_gathered, 0));
     const int npos = (out->x ? 1 : 0) + (out->y ? 1 : 0) + (out->z ? 1 : 0);
     if (npos == 0 || copies.empty()) CK(cudaEventRecord(s->ev_dl_pos, s->copy_stream));
+    for (int k = 0; k < 3; k++)
+        if (!axis_sent[k]) CK(cudaEventRecord(s->ev_dl_axis[k], s->copy_stream));
     if (want_grid)
         CK(cudaMemcpyAsync(out->grid, s->dl_grid, sizeof(double) * (size_t)c.ngrid, cudaMemcpyDeviceToHost,
                            s->copy_stream));
