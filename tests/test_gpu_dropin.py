@@ -141,3 +141,40 @@ def test_dropins_fp32c_within_tolerance(oracle_lib, lists):
     for k in ("x", "y", "z"):
         assert np.max(np.abs(out[k] - getattr(ref, k))) <= 2 * steps * 1e-6 * fmax, k
     assert np.array_equal(out["removecell"], ref.removecell)
+
+
+def test_updatepositions_leaves_the_callers_rand_where_rand_calls_would():
+    """updatepositions takes 3 values of the host program's rand() per cell
+    (cells.c:353-356); generated on the device from the C library's
+    generator window, they must equal those calls' values and leave the
+    generator at the same place: the next rand() after a step is the value
+    after 3 n calls, and the cells moved with randommove > 0 match a second
+    run whose draws come from rand() calls on the host."""
+    from timothy_gb300.refabi import DropinRun
+
+    libc = ctypes.CDLL(None)
+    libc.srand.argtypes = [ctypes.c_uint]
+    libc.rand.restype = ctypes.c_int
+    n = 5000
+    t = C.CellTypes.consistent(randommove=[0.05])
+    col = C.make_colony("uniform", n, 61, C.initial_radius("uniform", n), types=t)
+    libc.srand(4242)
+    run = DropinRun(col)
+    run.step(update=True)
+    after = libc.rand()
+    out = run.outputs()
+    run.shutdown()
+    libc.srand(4242)
+    draws = np.array([libc.rand() for _ in range(3 * n)], np.int64)
+    want_next = libc.rand()
+    assert after == want_next
+    # the move applied: x += F + randommove * (2 * (float)r / RAND_MAX - 1), cell by cell in order
+    r = draws.reshape(n, 3).astype(np.float32) / np.float32(2147483647)
+    step = np.float64(np.float32(0.05)) * (r.astype(np.float64) * 2.0 - 1.0)
+    ref = DropinRun(col)
+    ref.step(update=False)
+    f = ref.outputs()
+    ref.shutdown()
+    for k, ax in enumerate(("x", "y", "z")):
+        want = (getattr(col, ax) + f["f" + ax]) + step[:, k]
+        assert np.max(np.abs(out[ax] - want)) <= 1e-12 * max(1.0, np.max(np.abs(want))), ax

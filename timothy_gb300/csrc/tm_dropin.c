@@ -219,6 +219,75 @@ void computeremotegradient(systeminfo_t systeminfo, cellsinfo_t *cellsinfo, cell
     no_remote(systeminfo, cellcommdata);
 }
 
+/* The random move's rand() values without n calls of rand() on the host.
+ *
+ * updatepositions takes dim values per cell from the host program's rand()
+ * whatever the cell types' randommove (cells.c:353-356), so the generator
+ * must advance by that many values; at 16 M cells the calls alone take about
+ * a second.  The C library's rand() (glibc) is its random() generator: 31
+ * words r and a rear index, each call adding the word 28 places back
+ * (mod 31) to the oldest one and returning the sum >> 1 (the published
+ * additive generator, x_k = x_{k-31} + x_{k-3} mod 2^32).  initstate() hands
+ * back the caller's state array with the rear index stored in its first word
+ * (5 * rear + 3 for this generator type) and setstate() puts it back
+ * unchanged, so the window of the caller's generator can be read.  The
+ * window is trusted only when it predicts the next rand() exactly: one real
+ * call is made and compared (any other generator, or a rand() of its own,
+ * fails the check and the values come from rand() calls as before).  The
+ * values are then generated on the device from the window, and the window
+ * after them is written back into the caller's state array, which leaves the
+ * generator where nd calls of rand() would have left it.  The host program
+ * calls the drop-ins from one thread, as the reference does. */
+static char g_rand_scratch[128] __attribute__((aligned(8)));
+
+/* the caller's generator window, oldest word first; prev = its state array */
+static int libc_rand_window(uint32_t w[31], int32_t **prev_out)
+{
+    char *prev = initstate(1u, g_rand_scratch, sizeof g_rand_scratch);
+    if (!prev) return -1;
+    int32_t *p = (int32_t *)(void *)prev;
+    const int32_t head = p[0];
+    const int type = head % 5, rear = head / 5;
+    if (type != 3 || rear < 0 || rear >= 31) {
+        setstate(prev);
+        return -1;
+    }
+    const int front = (rear + 3) % 31;
+    for (int i = 0; i < 31; i++) w[i] = (uint32_t)p[1 + (front + i) % 31];
+    setstate(prev);
+    *prev_out = p;
+    return 0;
+}
+
+/* make w (oldest first) the caller's generator window */
+static void libc_rand_set_window(int32_t *prev, const uint32_t w[31])
+{
+    char *cur = initstate(1u, g_rand_scratch, sizeof g_rand_scratch);   /* saves the caller's position */
+    int32_t *p = (int32_t *)(void *)cur;
+    if (p != prev) {                                     /* not the array read before: leave it alone */
+        setstate(cur);
+        return;
+    }
+    p[0] = 5 * 28 + 3;                                   /* rear 28, front 0: the oldest word at index 0 */
+    for (int i = 0; i < 31; i++) p[1 + i] = (int32_t)w[i];
+    setstate(cur);
+}
+
+/* nd draws of the caller's rand() for the random move, on the device when
+ * the generator is the C library's; 0 when done, -1 when the caller must
+ * call rand() for draws[1..nd) (draws[0] is taken here in both cases) */
+static int move_draws_device(int64_t nd, int *draws)
+{
+    uint32_t w[31], end[31];
+    int32_t *prev = NULL;
+    const int have = libc_rand_window(w, &prev) == 0;
+    draws[0] = rand();
+    if (!have || draws[0] != (int)((w[0] + w[28]) >> 1)) return -1;
+    TRY("random move", tmi_set_move_draws_window(g_sess, w, nd, end));
+    libc_rand_set_window(prev, end);
+    return 0;
+}
+
 void updatepositions(settings_t settings, celltype_t *celltype, cellsinfo_t *cellsinfo, unsigned char *removecell,
                      int64_t *removecount)
 {
@@ -232,10 +301,15 @@ void updatepositions(settings_t settings, celltype_t *celltype, cellsinfo_t *cel
      * the cell types' randommove (cells.c:353-356): drawn here, so that the
      * caller's generator stays where the reference leaves it */
     const int64_t nd = n * (settings.dimension == 3 ? 3 : 2);
-    int *draws = (int *)malloc((size_t)nd * sizeof(int));
-    if (!draws) die("random move draws", -2, __LINE__);
-    for (int64_t k = 0; k < nd; k++) draws[k] = rand();
-    TRY("random move", tmi_set_move_draws(g_sess, draws, nd));
+    int first = 0;
+    int *draws = NULL;
+    if (move_draws_device(nd, &first) != 0) {
+        draws = (int *)malloc((size_t)nd * sizeof(int));
+        if (!draws) die("random move draws", -2, __LINE__);
+        draws[0] = first;
+        for (int64_t k = 1; k < nd; k++) draws[k] = rand();
+        TRY("random move", tmi_set_move_draws(g_sess, draws, nd));
+    }
     TRY("update", tmi_phase(g_sess, 2));
     TRY("sync", tm_session_sync(g_sess));
     free(draws);

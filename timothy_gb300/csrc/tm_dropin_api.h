@@ -51,6 +51,9 @@ int tmi_env2cells_patch(tm_session *s, int cid, const double *patch, int nfields
                         double **cellenv);
 /* the random move's rand() values (dim per cell, caller order); NULL clears */
 int tmi_set_move_draws(tm_session *s, const int *draws, int64_t count);
+/* the same values generated on the device from the C library's generator
+ * window w (31 words, oldest first); end receives the window after them */
+int tmi_set_move_draws_window(tm_session *s, const uint32_t w[31], int64_t count, uint32_t end[31]);
 /* updatecellcycles on host celldata_t records (after tmi_upload_aos of them);
  * counts[0..5]: change of the phase counters, counts[8 + t]: daughters of type t */
 int tmi_cycle_aos(tm_session *s, int cid, void *cells, int64_t n, int64_t cap, const tm_cycle_params *p,

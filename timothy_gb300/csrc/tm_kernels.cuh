@@ -83,4 +83,6 @@ struct tm_rand_cache {
 };
 int tm_libc_rand_device(uint32_t seed, int64_t offset, int64_t count, int *out, tm_rand_cache *cache,
                         uint32_t *d_windows, int64_t windows_cap, cudaStream_t st);
+int tm_libc_rand_from_window(const uint32_t w[31], int64_t count, int *out, uint32_t end[31], uint32_t *d_windows,
+                             int64_t windows_cap, cudaStream_t st);
 

@@ -224,27 +224,44 @@ int ensure_jumps()
 // rand() returns after offset earlier calls, into out (device); cache (31
 // words + the offset they stand at, host) lets consecutive calls continue
 // without the matrix powers
+// count values of the stream whose window is w (31 words, oldest first: the
+// next value is (w[0] + w[28]) >> 1) into out (device); end receives the
+// window after the last value
+int tm_libc_rand_from_window(const uint32_t w[31], int64_t count, int *out, uint32_t end[31], uint32_t *d_windows,
+                             int64_t windows_cap, cudaStream_t st)
+{
+    if (count <= 0) {
+        memcpy(end, w, kWin * sizeof(uint32_t));
+        return 0;
+    }
+    const int64_t nchunks = (count + kChunk - 1) / kChunk;
+    if (nchunks + 1 > windows_cap || nchunks > ((int64_t)1 << kPowers)) return -1;
+    if (ensure_jumps() != 0) return -2;
+    window31 w0;
+    memcpy(w0.w, w, sizeof w0.w);
+    uint32_t *endw = d_windows + nchunks * kWin;   // the spare window after the chunks'
+    k_rand_windows<<<(unsigned)((nchunks * 32 + 127) / 128), 128, 0, st>>>(w0, nchunks, d_windows);
+    const int threads = 128;
+    k_libc_rand<<<(unsigned)((nchunks + threads - 1) / threads), threads, 0, st>>>(d_windows, count, out, endw);
+    if (cudaGetLastError() != cudaSuccess) return -2;
+    if (cudaMemcpyAsync(end, endw, kWin * sizeof(uint32_t), cudaMemcpyDeviceToHost, st) != cudaSuccess) return -2;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return -2;
+    return 0;
+}
+
 int tm_libc_rand_device(uint32_t seed, int64_t offset, int64_t count, int *out, tm_rand_cache *cache,
                         uint32_t *d_windows, int64_t windows_cap, cudaStream_t st)
 {
     if (count <= 0) return 0;
-    const int64_t nchunks = (count + kChunk - 1) / kChunk;
-    if (nchunks + 1 > windows_cap || nchunks > ((int64_t)1 << kPowers)) return -1;
-    if (ensure_jumps() != 0) return -2;
     window31 w0;
     if (cache && cache->valid && cache->seed == seed && cache->offset == offset) {
         memcpy(w0.w, cache->window, sizeof w0.w);
     } else {
         window_at(seed, (uint64_t)offset, w0.w);
     }
-    uint32_t *endw = d_windows + nchunks * kWin;   // the spare window after the chunks'
-    k_rand_windows<<<(unsigned)((nchunks * 32 + 127) / 128), 128, 0, st>>>(w0, nchunks, d_windows);
-    const int threads = 128;
-    k_libc_rand<<<(unsigned)((nchunks + threads - 1) / threads), threads, 0, st>>>(d_windows, count, out, endw);
-    if (cudaGetLastError() != cudaSuccess) return -2;
     uint32_t end[kWin];
-    if (cudaMemcpyAsync(end, endw, sizeof end, cudaMemcpyDeviceToHost, st) != cudaSuccess) return -2;
-    if (cudaStreamSynchronize(st) != cudaSuccess) return -2;
+    const int rc = tm_libc_rand_from_window(w0.w, count, out, end, d_windows, windows_cap, st);
+    if (rc != 0) return rc;
     if (cache) {
         memcpy(cache->window, end, sizeof end);
         cache->seed = seed;

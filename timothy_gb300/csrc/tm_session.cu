@@ -2766,6 +2766,37 @@ extern "C" int tmi_set_move_draws(tm_session *s, const int *draws, int64_t count
     return TM_OK;
 }
 
+// The random move's draws generated on the device: count values of the C
+// library's stream from the window w (31 words, oldest first); end receives
+// the window after them.
+extern "C" int tmi_set_move_draws_window(tm_session *s, const uint32_t w[31], int64_t count, uint32_t end[31])
+{
+    if (!s || !w || !end || count <= 0) return tm_fail(TM_EINVAL, "bad arguments");
+    CK(cudaSetDevice(s->device));
+    if (s->move_cap < (size_t)count) {
+        if (s->move_buf) CK(cudaFree(s->move_buf));
+        s->move_buf = nullptr;
+        s->move_cap = 0;
+        int rc = dalloc(&s->move_buf, count);
+        if (rc) return rc;
+        s->move_cap = (size_t)count;
+    }
+    const int64_t chunks = (count + TM_RAND_CHUNK - 1) / TM_RAND_CHUNK + 1;
+    if (s->rand_windows_cap < chunks) {
+        if (s->rand_windows) CK(cudaFree(s->rand_windows));
+        s->rand_windows = nullptr;
+        s->rand_windows_cap = 0;
+        int rc = dalloc(&s->rand_windows, chunks * 31);
+        if (rc) return rc;
+        s->rand_windows_cap = chunks;
+    }
+    if (tm_libc_rand_from_window(w, count, s->move_buf, end, s->rand_windows, s->rand_windows_cap, s->stream) != 0)
+        return tm_fail(TM_ECUDA, "device rand() stream failed");
+    s->A.move_draws = s->move_buf;
+    drop_graphs(s);
+    return TM_OK;
+}
+
 // celldata_t byte offsets (global.h:100-120, 112-byte records)
 #define CD_PHASE 4
 #define CD_AGE 8
