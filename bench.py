@@ -270,7 +270,9 @@ def serving_form(args, device, rate, seconds):
     fin = [r for r in reqs if r.finished == r.finished]
     return {"rate_per_s": rate, "arrival_seconds": seconds, "wall_s": st["wall_s"], "requests": len(reqs),
             "finished": st["finished"], "offered_cell_updates_per_s": offered,
-            "served_cell_updates_per_s": st["throughput"], "p50_s": st["p50"], "p99_s": st["p99"],
+            "served_cell_updates_per_s": st["throughput"],
+            "served_while_arriving_cell_updates_per_s": st["throughput_during_arrivals"],
+            "p50_s": st["p50"], "p99_s": st["p99"],
             "latency_over": "every request (arrivals stop at arrival_seconds, then the queue drains)",
             "p50_by_size": _size_bins(fin), "max_resident_cells": st["max_resident_cells"],
             "pool_slots": st["pool_slots"], "pool_gb": st["pool_bytes"] / 1e9}
@@ -940,6 +942,7 @@ def main():
         fb = detail["forms"]["batched"]
         line["forms"] = {"batched_fp32c": r4(fb["fp32c"]["value"]), "batched_fp64": r4(fb["fp64"]["value"]),
                          "serving": [{"rate": r4(f["rate_per_s"]), "served": r4(f["served_cell_updates_per_s"]),
+                                      "served_while_arriving": r4(f["served_while_arriving_cell_updates_per_s"]),
                                       "p50": r4(f["p50_s"]), "p99": r4(f["p99_s"])}
                                      for f in detail["forms"]["serving"]]}
     detail["tuning"] = tuned

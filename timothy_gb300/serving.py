@@ -207,8 +207,11 @@ class Server:
         clock = (lambda: float(it)) if virtual else (lambda: time.perf_counter() - t0)
         if drain and horizon is not None:
             pending = deque(r for r in pending if r.arrival < horizon)
+        stepped_at_horizon = None
         while pending or queue or active or inflight:
             now = clock()
+            if horizon is not None and now >= horizon and stepped_at_horizon is None:
+                stepped_at_horizon = stepped_cells
             if horizon is not None and now >= horizon and not drain:
                 break
             while pending and pending[0].arrival <= now:
@@ -274,6 +277,8 @@ class Server:
         served = sum(r.n * r.steps for r in fin)
         return {"requests": len(requests), "arrived": len(arrived), "finished": len(fin), "wall_s": wall,
                 "iterations": it,
+                "throughput_during_arrivals": (stepped_at_horizon / horizon
+                                               if stepped_at_horizon is not None and horizon else None),
                 "cell_updates_finished": served, "cell_updates_stepped": stepped_cells,
                 "throughput": stepped_cells / wall if wall > 0 else 0.0,
                 "p50": float(np.percentile(lat, 50)) if len(lat) else None,
