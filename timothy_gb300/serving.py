@@ -271,13 +271,19 @@ class Server:
                         log(f"t={req.finished:.3f} done rid={req.rid} n={req.n} K={req.steps} lat={req.latency:.3f}")
         s.sync()
         wall = clock() if not virtual else time.perf_counter() - t0
+        if stepped_at_horizon is None and horizon:
+            # every request finished before the horizon: the whole run was arrivals
+            horizon_used = max(wall, 1e-9)
+            stepped_at_horizon = stepped_cells
+        else:
+            horizon_used = horizon
         arrived = [r for r in requests if horizon is None or r.arrival < horizon]
         fin = [r for r in requests if not math.isnan(r.finished)]
         lat = np.array([r.latency for r in fin]) if fin else np.zeros(0)
         served = sum(r.n * r.steps for r in fin)
         return {"requests": len(requests), "arrived": len(arrived), "finished": len(fin), "wall_s": wall,
                 "iterations": it,
-                "throughput_during_arrivals": (stepped_at_horizon / horizon
+                "throughput_during_arrivals": (stepped_at_horizon / horizon_used
                                                if stepped_at_horizon is not None and horizon else None),
                 "cell_updates_finished": served, "cell_updates_stepped": stepped_cells,
                 "throughput": stepped_cells / wall if wall > 0 else 0.0,
