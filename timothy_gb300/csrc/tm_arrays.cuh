@@ -132,6 +132,34 @@ __device__ __forceinline__ void tm_queue_walk(const tm_arrays &a, long long i, b
     }
 }
 
+// The same for kernels where several lanes share a cell: every lane of the
+// warp calls it, the cell's owner lane carries it, and the warp makes one
+// append per queue.
+__device__ __forceinline__ void tm_queue_walk_owned(const tm_arrays &a, long long i, bool owner, bool isolated,
+                                                    bool walk)
+{
+    if (owner && !walk) a.v[i] = 0.0;
+    const unsigned am = __activemask();
+    const bool wf = owner && walk && !isolated, wb = owner && walk && isolated;
+    const unsigned mf = __ballot_sync(am, wf), mb = __ballot_sync(am, wb);
+    const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    if (mf) {
+        const int leader = __ffs(mf) - 1;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(&a.work[2], __popc(mf));
+        base = __shfl_sync(am, base, leader);
+        if (wf) a.walk_list[base + __popc(mf & below)] = (int)i;
+    }
+    if (mb) {
+        const int leader = __ffs(mb) - 1;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(&a.work[3], __popc(mb));
+        base = __shfl_sync(am, base, leader);
+        if (wb) a.walk_list[a.nslots_total - 1 - (base + __popc(mb & below))] = (int)i;
+    }
+}
+
 // launch shapes chosen per session (tm_tuning)
 struct tm_shapes {
     int pair_lshift;    // candidate ranges from Morton nodes this many levels above the bins (0 or 1)

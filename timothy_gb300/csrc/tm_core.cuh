@@ -40,6 +40,7 @@ struct tm_type {
     // FP32 forms for the compensated path
     float hf, h2f, inv_hf, cWf, cGf, kmassf;   // kmassf = sc / csize
     float thr_lo, thr_hi;                      // squared-distance band around h^2
+    double inv_h, kmass;                       // 1 / h and sc / csize for the FP32 path's FP64 re-do
 };
 
 struct tm_consts {

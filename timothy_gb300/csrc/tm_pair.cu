@@ -108,6 +108,24 @@ __device__ __forceinline__ double dens_term64(const tm_type &T, double dist, dou
     return mul64(mj, (double)__double2float_rn(wk));
 }
 
+// The same term for the FP32 path's FP64 re-do of a flagged cell: u and the
+// density weight by multiplications with 1 / h and sc / csize formed on the
+// host (the FP32 path's contract is 1e-6; the re-do removes the FP32
+// cancellation in 1 - u, which these one-ulp differences do not bring back).
+__device__ __forceinline__ double dens_term64_fast(const tm_type &T, double dist, double sizej)
+{
+    const double u = dist * T.inv_h;
+    double wk;
+    if (u <= 0.5) {
+        const double six_uu = 6.0 * u * u;
+        wk = T.cW * ((1.0 - six_uu) + six_uu * u);
+    } else {
+        const double omu = 1.0 - u;
+        wk = T.cW * (2.0 * omu * omu * omu);
+    }
+    return (T.kmass * sizej) * (double)__double2float_rn(wk);
+}
+
 __device__ __forceinline__ double dist64(const tm_arrays &a, long long i, long long j)
 {
     const double dx = sub64(a.x[i], a.x[j]), dy = sub64(a.y[i], a.y[j]), dz = sub64(a.z[i], a.z[j]);
@@ -908,30 +926,39 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_plist32(tm_arrays a, const tm_c
         nbmin = min(nbmin, __shfl_xor_sync(FULL, nbmin, o));
         if (DIAG) hash += __shfl_xor_sync(FULL, hash, o);
     }
-    if (!live || q != 0) return;
-    pair_store<1>(a, i, acc, cnt_nb, nbmin, hash, false);
-    // the octree walk's first pass for this cell (see k_octree_mark): walk if
-    // the first within-h neighbour in Morton order may overlap it
-    bool walk = cnt_nb == 0 || DIAG;
-    if (!walk) {
-        const long long m = f.ident ? (long long)nbmin : (long long)a.tmp[nbmin];
-        const float4 hm = hi[m], lm = lo[m];
-        const float dx = (hi_i.x - hm.x) + (lo_i.x - lm.x), dy = (hi_i.y - hm.y) + (lo_i.y - lm.y),
-                    dz = (hi_i.z - hm.z) + (lo_i.z - lm.z);
-        const float rs = (hi_i.w + hm.w) * 1.0001f + 1e-5f;
-        walk = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < rs * rs;
+    // the merged results are the same in the cell's four lanes; lane 0 owns them
+    const bool owner = live && q == 0;
+    bool walk = false;
+    if (owner) {
+        pair_store<1>(a, i, acc, cnt_nb, nbmin, hash, false);
+        // the octree walk's first pass for this cell (see k_octree_mark): walk
+        // if the first within-h neighbour in Morton order may overlap it
+        walk = cnt_nb == 0 || DIAG;
+        if (!walk) {
+            const long long m = f.ident ? (long long)nbmin : (long long)a.tmp[nbmin];
+            const float4 hm = hi[m], lm = lo[m];
+            const float dx = (hi_i.x - hm.x) + (lo_i.x - lm.x), dy = (hi_i.y - hm.y) + (lo_i.y - lm.y),
+                        dz = (hi_i.z - hm.z) + (lo_i.z - lm.z);
+            const float rs = (hi_i.w + hm.w) * 1.0001f + 1e-5f;
+            walk = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < rs * rs;
+        }
     }
-    tm_queue_walk(a, i, cnt_nb == 0, walk);
-    if (needs_fix64(acc)) {
-        atomicAdd(&a.frame[c].fix64, 1ull);
-        // FP64 density over the same list, the cutoff decided in FP64
+    // one queue append per warp: every lane takes part, the owners carry the cells
+    tm_queue_walk_owned(a, i, owner, cnt_nb == 0, walk);
+    if (live && needs_fix64(acc)) {
+        // FP64 density over the same list, the cutoff decided in FP64, the
+        // list split over the cell's lanes and the partial sums added in a
+        // fixed order
+        const unsigned gmask = 0xfu << (lane & ~(LPC - 1));
+        if (q == 0) atomicAdd(&a.frame[c].fix64, 1ull);
         double dens = 0.0;
-        for (int kk = 0; kk < cnt; kk++) {
+        for (int kk = q; kk < cnt; kk += LPC) {
             const int j = a.vlist[(long long)kk * ls + i];
             const double dist = dist64(a, i, j);
-            if (dist <= T.h) dens = add64(dens, dens_term64(T, dist, a.size[j]));
+            if (dist <= T.h) dens += dens_term64_fast(T, dist, a.size[j]);
         }
-        a.density[i] = dens;
+        for (int o = 1; o < LPC; o <<= 1) dens = add64(dens, __shfl_xor_sync(gmask, dens, o));
+        if (q == 0) a.density[i] = dens;
     }
 }
 

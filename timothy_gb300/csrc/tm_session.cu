@@ -691,6 +691,8 @@ extern "C" int tm_session_create(tm_session **out, const tm_session_config *cfg,
         T.cWf = (float)T.cW;
         T.cGf = (float)T.cG;
         T.kmassf = (float)(T.sc / T.csize);
+        T.inv_h = 1.0 / T.h;
+        T.kmass = T.sc / T.csize;
         T.thr_lo = (float)(T.h * (1.0 - 1e-5) * T.h * (1.0 - 1e-5));
         T.thr_hi = (float)(T.h * (1.0 + 1e-5) * T.h * (1.0 + 1e-5));
         if (!(T.h > 0.0) || !(T.csize > 0.0)) {
@@ -1894,6 +1896,8 @@ extern "C" int tmi_set_types(tm_session *s, const tm_celltypes *types)
         T.cWf = (float)T.cW;
         T.cGf = (float)T.cG;
         T.kmassf = (float)(T.sc / T.csize);
+        T.inv_h = 1.0 / T.h;
+        T.kmass = T.sc / T.csize;
         T.thr_lo = (float)(T.h * (1.0 - 1e-5) * T.h * (1.0 - 1e-5));
         T.thr_hi = (float)(T.h * (1.0 + 1e-5) * T.h * (1.0 + 1e-5));
     }
