@@ -681,12 +681,11 @@ def dropin_record(n, kind, seed, cic, steps, warmup=1, precision="fp64"):
         for _ in range(steps):
             run.step_loop()
         dt = time.perf_counter() - t0
-        # the same loop without updatepositions (its share: the host's rand()
-        # calls, the forces up, the positions and marks down, the update)
-        t1 = time.perf_counter()
+        # the same loop call by call (each drop-in call returns with its results on the host)
+        calls = {k: 0.0 for k in ("octbuild", "patches", "computepotential", "computegradient", "updatepositions")}
         for _ in range(steps):
-            run.step_loop(update=False)
-        dt_noupd = time.perf_counter() - t1
+            for k, v in run.step_loop_timed().items():
+                calls[k] += v
         run.shutdown()
     finally:
         lib.tm_dropin_set_precision(0, 0)
@@ -697,7 +696,7 @@ def dropin_record(n, kind, seed, cic, steps, warmup=1, precision="fp64"):
             # per step: the records up (octbuild); density, v, mindist and the
             # forces, then positions and removal marks down; forces and marks up
             "h2d_bytes_per_step": n * (rec + 24 + 1), "d2h_bytes_per_step": n * (24 + 24 + 24 + 1),
-            "ms_per_step_without_updatepositions": dt_noupd / steps * 1e3}
+            "calls_ms": {k: v / steps * 1e3 for k, v in calls.items()}}
 
 
 def main():

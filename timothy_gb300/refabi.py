@@ -317,6 +317,39 @@ class DropinRun:
         if p is not None:
             free_patches(p)
 
+    def step_loop_timed(self) -> dict:
+        """step_loop with the wall time of each call (seconds)."""
+        import time
+
+        lib = self.lib
+        ct = self.celltype
+        out = {}
+        t = time.perf_counter()
+        lib.octbuild(self.si, C.byref(self.ci), ct)
+        out["octbuild"] = time.perf_counter() - t
+        t = time.perf_counter()
+        p = None
+        if self.cic:
+            p = patches_t()
+            lib.patches_alloc(self.si, self.st, C.byref(p), C.byref(self.ci), C.byref(self.grid))
+            lib.patches_cells2envinfo(self.si, self.st, C.byref(p), C.byref(self.ci), C.byref(self.grid))
+        out["patches"] = time.perf_counter() - t
+        t = time.perf_counter()
+        lib.computepotential(self.si, C.byref(self.ci), ct, self.cc)
+        lib.computeremotepotential(self.si, C.byref(self.ci), ct, self.cc)
+        out["computepotential"] = time.perf_counter() - t
+        t = time.perf_counter()
+        lib.computegradient(self.si, C.byref(self.ci), ct, self.cc)
+        lib.computeremotegradient(self.si, C.byref(self.ci), ct, self.cc)
+        out["computegradient"] = time.perf_counter() - t
+        t = time.perf_counter()
+        lib.updatepositions(self.st, ct, C.byref(self.ci), self.removecell.ctypes.data, C.byref(self.removecount))
+        out["updatepositions"] = time.perf_counter() - t
+        lib.octfree(C.byref(self.ci))
+        if p is not None:
+            free_patches(p)
+        return out
+
     COUNT_FIELDS = ("n", "g0phase", "g1phase", "sphase", "g2phase", "mphase", "necroticphase")
 
     def set_counts(self, counts):
