@@ -905,27 +905,32 @@ def main():
             "vs_baseline": None, "dtype": "f32+kahan (f64 positions)" if prec == "fp32c" else "f64",
             "data": "synthetic",
             "config": {"workload": args.workload, "kind": kind, "cells": n, "seed": seed, "h": 2.5, "dt": wl["dt"],
-                       "cic": wl["cic"], "precision": prec, "mean_neighbours": r4(mean_nb),
-                       "max_neighbours": max_nb, "list_capacity": args.list_capacity,
+                       "cic": wl["cic"], "mean_neighbours": r4(mean_nb), "max_neighbours": max_nb,
                        "l2": "inputs > L2",
                        "parallelism": f"replicas x{world}"},
             "roofline": {k: (r4(v) if not isinstance(v, str) else v) for k, v in roofline.items()
                          if k not in ("phases_ms", "traffic_unit", "peak_source", "kernel")},
-            "phases_ms": {k[:-3]: r4(v) for k, v in prof.items() if k.endswith("_ms") and k != "pair_ms"},
+            "phases_ms": {k[:-3]: r4(v) for k, v in prof.items() if k.endswith("_ms") and k != "pair_ms"
+                          and (k not in ("fix_ms", "cic_ms") or v > 0.05)},
             "rebuilds": rebuilds,
             "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clk}
     line["roofline"]["kernel"] = kname
     if e2e is not None:
-        line["e2e"] = {k: r4(v) if not isinstance(v, str) else v for k, v in e2e.items() if k != "api"}
+        line["e2e"] = {k: r4(v) if not isinstance(v, str) else v for k, v in e2e.items()
+                       if k not in ("api", "steps")}
     if cpu is not None:
         line["cpu_baseline"] = {k: r4(v) if not isinstance(v, str) else v for k, v in cpu.items()}
+        line["cpu_baseline"]["sample"] = cpu["sample"].split(" cells")[0] + " cells of the workload, 1 step"
     if clk:
-        line["clocks"] = {k: r4(v) if isinstance(v, (int, float)) else v for k, v in clk.items()}
+        line["clocks"] = {k: r4(v) if isinstance(v, (int, float)) else v for k, v in clk.items()
+                          if k in ("sm_mhz", "sm_max_mhz", "reasons")}
+    short = {"error_vs_fp64": ("steps", "density_max_rel", "force_max_rel_to_max", "position_max_abs"),
+             "neighbour_check": ("cells", "mismatched_cells")}
     for k in ("fp64", "fp32c_over_fp64", "error_vs_fp64", "neighbour_check"):
         if k in extra:
             v = extra[k]
-            line[k] = {q: r4(w) for q, w in v.items() if not isinstance(w, str)} if isinstance(v, dict) \
-                else r4(v)
+            line[k] = {q: r4(w) for q, w in v.items() if not isinstance(w, str) and q in short.get(k, v)} \
+                if isinstance(v, dict) else r4(v)
     if "scale1m" in detail:
         sc = detail["scale1m"]
         par = sc["parity_after_3_steps"]
@@ -935,13 +940,11 @@ def main():
                            "grid_err": r4(par["grid_max_rel_to_max"]),
                            "nb_mismatch": par["neighbour_sets_mismatched_cells"]}
     if "e2e_dropin" in detail:
-        line["e2e_dropin"] = {k: {"value": r4(v["value"]), "ms_per_step": r4(v["ms_per_step"])}
-                              for k, v in detail["e2e_dropin"].items()}
+        line["e2e_dropin"] = {k: r4(v["value"]) for k, v in detail["e2e_dropin"].items()}
     if "forms" in detail:
         fb = detail["forms"]["batched"]
         line["forms"] = {"batched_fp32c": r4(fb["fp32c"]["value"]), "batched_fp64": r4(fb["fp64"]["value"]),
                          "serving": [{"rate": r4(f["rate_per_s"]), "served": r4(f["served_cell_updates_per_s"]),
-                                      "served_while_arriving": r4(f["served_while_arriving_cell_updates_per_s"]),
                                       "p50": r4(f["p50_s"]), "p99": r4(f["p99_s"])}
                                      for f in detail["forms"]["serving"]]}
     detail["tuning"] = tuned

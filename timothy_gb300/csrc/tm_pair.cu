@@ -847,7 +847,10 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_plist32(tm_arrays a, const tm_c
             acc.fx.add(fmaf(ga, dxa, gb * dxb));
             acc.fy.add(fmaf(ga, dya, gb * dyb));
             if (dim == 3) acc.fz.add(fmaf(ga, dza, gb * dzb));
-            acc.mins = fminf(acc.mins, fminf(ina ? sa : 3.0e38f, inb ? sb : 3.0e38f));
+            // over every entry: with a neighbour within h the minimum is one of
+            // them (an entry beyond h is farther); a cell with none takes its
+            // mindist from the octree walk
+            acc.mins = fminf(acc.mins, fminf(sa, hasb ? sb : 3.0e38f));
             cnt_nb += (ina ? 1 : 0) + (inb ? 1 : 0);
             nbmin = min(nbmin, min(ina ? __float_as_int(la.w) : 0x7fffffff, inb ? __float_as_int(lb.w) : 0x7fffffff));
             if (DIAG) {
@@ -1029,7 +1032,7 @@ static void launch_plist32(const tm_arrays &a, const tm_consts *K, int variant, 
     switch (variant) {
     // every variant accumulates alike (the paired form), so the block shape
     // changes no result bit
-    case 2: k_plist32<256, 4, -1, DIAG><<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(a, K); break;
+    case 2: k_plist32<64, 16, -1, DIAG><<<(unsigned)((nt + 63) / 64), 64, 0, st>>>(a, K); break;
     case 3: k_plist32<64, 14, -1, DIAG><<<(unsigned)((nt + 63) / 64), 64, 0, st>>>(a, K); break;
     case 4: k_plist32<256, 3, -1, DIAG><<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(a, K); break;
     default: k_plist32<128, 7, -1, DIAG><<<(unsigned)((nt + 127) / 128), 128, 0, st>>>(a, K); break;
