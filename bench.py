@@ -525,11 +525,19 @@ def neighbour_check(s, cid, col, local):
     """Neighbour sets of the FP32 + compensated colony, evaluated from its
     Verlet lists (built steps before), against a plain FP64 pass that searches
     the bins on the same positions with no lists: per cell the count and the
-    fingerprint of the set within h (potential.c:39-78, dist <= h)."""
+    fingerprint of the set within h (potential.c:39-78, dist <= h).  The same
+    positions' v from a step without diagnostics (the list pass settles most
+    cells without the octree walk) against the FP64 pass's walk, which
+    diagnostics run for every cell."""
     from timothy_gb300 import session as S
 
     pos = s.download(cid, ["x", "y", "z"])
     st = s.stats(cid)
+    s.step(1)
+    s.sync()
+    fast_v = s.download(cid, ["v"])["v"]
+    walked = s.stats(cid)["walked_cells"]
+    s.upload_positions_async(cid, pos["x"], pos["y"], pos["z"])
     s.set_diagnostics(True)
     s.step(1)
     s.sync()
@@ -541,11 +549,18 @@ def neighbour_check(s, cid, col, local):
         c64 = s64.add_colony(at, precision="fp64", update="none")
         s64.step(1)
         s64.sync()
-        ref = s64.download(c64, ["nbcount", "nbhash"])
+        ref = s64.download(c64, ["nbcount", "nbhash", "v"])
     bad = (fast["nbcount"] != ref["nbcount"]) | (fast["nbhash"] != ref["nbhash"])
+    vs = float(np.max(np.abs(ref["v"])))
+    dv = np.abs(fast_v - ref["v"])
+    flips = (fast_v == 0.0) != (ref["v"] == 0.0)
     return {"cells": int(col.n), "pairs_within_h": int(np.sum(ref["nbcount"].astype(np.int64))),
             "mismatched_cells": int(np.sum(bad)), "list_age_steps": st["list_age"],
-            "against": "plain FP64 bin search on the same positions, no lists"}
+            "against": "plain FP64 bin search on the same positions, no lists",
+            "v": {"nonzero_cells": int(np.count_nonzero(ref["v"])), "walked_cells": int(walked),
+                  "max_abs_rel_to_max": float(np.max(dv) / vs) if vs > 0 else 0.0,
+                  "zero_pattern_flips": int(np.sum(flips)),
+                  "flips_above_1e-5_of_max": int(np.sum(flips & (np.abs(ref["v"]) > 1e-5 * vs)))}}
 
 
 def e2e_loop(s, cid, col, steps, positions_only=True):
@@ -670,6 +685,7 @@ def dropin_record(n, kind, seed, cic, steps, warmup=1, precision="fp64"):
 
     lib = S.load_library()
     lib.tm_dropin_set_precision.argtypes = [ctypes.c_int, ctypes.c_int]
+    lib.tm_dropin_pinned_bytes.restype = ctypes.c_int64
     col = C.make_colony(kind, n, seed, C.configured_radius(kind, n, seed))
     if precision == "fp32c":
         lib.tm_dropin_set_precision(1, 1)
@@ -677,6 +693,7 @@ def dropin_record(n, kind, seed, cic, steps, warmup=1, precision="fp64"):
         run = DropinRun(col, cic=cic)
         for _ in range(warmup):
             run.step_loop()
+        pinned = int(lib.tm_dropin_pinned_bytes())
         t0 = time.perf_counter()
         for _ in range(steps):
             run.step_loop()
@@ -696,7 +713,24 @@ def dropin_record(n, kind, seed, cic, steps, warmup=1, precision="fp64"):
             # per step: the records up (octbuild); density, v, mindist and the
             # forces, then positions and removal marks down; forces and marks up
             "h2d_bytes_per_step": n * (rec + 24 + 1), "d2h_bytes_per_step": n * (24 + 24 + 24 + 1),
+            "records_page_locked": pinned >= n * rec,
             "calls_ms": {k: v / steps * 1e3 for k, v in calls.items()}}
+
+
+def dropin_record_process(n, kind, seed, cic, steps, precision="fp64"):
+    """dropin_record in a process of its own, as a host program that links
+    the drop-ins would run: the records, their page-locking and the device
+    session start from a clean process, not from this one's other sessions
+    and registered buffers."""
+    code = ("import json, bench; print('DROPIN ' + json.dumps(bench.dropin_record("
+            f"{n}, {kind!r}, {seed}, {cic}, {steps}, precision={precision!r})))")
+    r = subprocess.run([sys.executable, "-c", code], cwd=os.path.dirname(os.path.abspath(__file__)),
+                       capture_output=True, text=True)
+    for ln in r.stdout.splitlines():
+        if ln.startswith("DROPIN "):
+            return json.loads(ln[7:])
+    return {"error": (r.stderr or r.stdout).strip().splitlines()[-1:] if (r.stderr or r.stdout) else "no output",
+            "returncode": r.returncode}
 
 
 def main():
@@ -793,7 +827,8 @@ def main():
     s.sync()
     prof = s.profile_read()
     s.profile(False)
-    rebuilds = s.stats(cid)["list_rebuilds"] - rb0
+    st_end = s.stats(cid)
+    rebuilds = st_end["list_rebuilds"] - rb0
     ms_max = dist_max(pg, ms)
     ms_per_step = ms_max / args.steps
     value = aggregate_value(n, world, args.steps, ms_max)
@@ -810,22 +845,24 @@ def main():
                 "peak_source": peak_kind, "kernel": kname, "kernel_ms": list_ms,
                 "phases_ms": {k: prof[k] for k in ("build_ms", "search_ms", "list_ms", "fix_ms", "octree_ms",
                                                    "update_ms", "cic_ms")}}
-    detail = {"roofline": dict(roofline)}
+    detail = {"roofline": dict(roofline),
+              "octree_walk": {"walked_cells_last_step": st_end["walked_cells"], "cells": n,
+                              "density_fp64_cells_last_step": st_end["density_fp64_cells"]}}
     # the compute side of the list pass (a gather-reduce: no tensor cores):
     # pairs within h per second, from this colony's own neighbour counts, and
     # the algorithmic FP32 flops of those pairs (the reference's expressions,
-    # about 83 flops per pair for density and force) against the nominal FP32
-    # rate of the part (152 SMs x 128 lanes x 2 x the maximum SM clock; no
-    # measured figure exists for it)
+    # about 83 flops per pair for density and force) against the FP32 FMA
+    # rate measured on this device (tm_measure_fp32_peak)
     nb = s.download(cid, ["nbcount"])["nbcount"]
     pairs = float(np.sum(nb.astype(np.int64)))
     if list_ms:
-        fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
+        fp32_peak = S.measure_fp32_peak(local)
         pair_rate = pairs / (list_ms * 1e-3)
         detail["roofline"]["compute"] = {
             "pairs_within_h_per_launch": pairs, "pairs_per_s": pair_rate, "algorithmic_tflops": pair_rate * 83 / 1e12,
-            "fp32_peak_tflops": fp32_peak, "fp32_peak_source": "nominal (152 SMs x 128 FP32 lanes x 2 x 2.07 GHz)",
-            "frac": pair_rate * 83 / 1e12 / fp32_peak}
+            "fp32_peak_tflops": fp32_peak,
+            "fp32_peak_source": "measured: FMA chains on every SM (tm_measure_fp32_peak)",
+            "frac": pair_rate * 83 / 1e12 / fp32_peak if fp32_peak > 0 else None}
     out_fast = s.download(cid, ["x", "y", "z", "density", "fx", "fy", "fz"]) if prec == "fp32c" else None
 
     extra = {}
@@ -888,9 +925,9 @@ def main():
     if world == 1 and not args.no_scale1m and args.workload == "precision16m":
         detail["scale1m"] = scale1m_record(local, 100, args)
     if world == 1 and not args.no_dropin:
-        detail["e2e_dropin"] = {"1m_cic": dropin_record(1_000_000, "clustered", 2, True, 5)}
+        detail["e2e_dropin"] = {"1m_cic": dropin_record_process(1_000_000, "clustered", 2, True, 5)}
         if n >= 16_000_000:
-            detail["e2e_dropin"]["16m"] = dropin_record(n, kind, seed, False, 3, precision=prec)
+            detail["e2e_dropin"]["16m"] = dropin_record_process(n, kind, seed, False, 3, precision=prec)
 
     if not args.no_forms and world == 1:
         detail["rows"] = {"grid_to_cell": field_rows(local, peak), "cic_deposit": cic_rows(local, peak),
@@ -931,6 +968,8 @@ def main():
             v = extra[k]
             line[k] = {q: r4(w) for q, w in v.items() if not isinstance(w, str) and q in short.get(k, v)} \
                 if isinstance(v, dict) else r4(v)
+    if "v" in extra.get("neighbour_check", {}):
+        line["neighbour_check"]["v_flips"] = extra["neighbour_check"]["v"]["flips_above_1e-5_of_max"]
     if "scale1m" in detail:
         sc = detail["scale1m"]
         par = sc["parity_after_3_steps"]
@@ -940,7 +979,7 @@ def main():
                            "grid_err": r4(par["grid_max_rel_to_max"]),
                            "nb_mismatch": par["neighbour_sets_mismatched_cells"]}
     if "e2e_dropin" in detail:
-        line["e2e_dropin"] = {k: r4(v["value"]) for k, v in detail["e2e_dropin"].items()}
+        line["e2e_dropin"] = {k: r4(v["value"]) if "value" in v else None for k, v in detail["e2e_dropin"].items()}
     if "forms" in detail:
         fb = detail["forms"]["batched"]
         line["forms"] = {"batched_fp32c": r4(fb["fp32c"]["value"]), "batched_fp64": r4(fb["fp64"]["value"]),

@@ -115,11 +115,16 @@ typedef struct {
     float list_skin;                  /* the colony's list skin */
     int32_t list_age;                 /* steps since the lists were built */
     int64_t density_fp64_cells;       /* FP32 path: cells of the last step whose density was redone in FP64 */
+    int64_t walked_cells;             /* cells of the last step whose v (or mindist) took the octree walk */
 } tm_colony_info;
 
 const char *tm_last_error(void);
 const char *tm_version(void);
 int tm_device_count(void);
+/* Measured FP32 FMA rate of `device` in TFLOP/s (eight independent FMA chains
+ * per thread on every SM, best of two timed launches): the compute
+ * denominator of the list pass's roofline. */
+int tm_measure_fp32_peak(int device, double *tflops);
 
 int tm_session_create(tm_session **out, const tm_session_config *cfg, const tm_celltypes *types);
 int tm_session_destroy(tm_session *s);

@@ -321,6 +321,10 @@ void tm_dropin_set_precision(int precision, int neighbour_lists);
 /* Releases the device session the drop-ins keep between calls (no
  * counterpart in the reference; optional at exit). */
 void tm_dropin_shutdown(void);
+/* No counterpart in the reference.  Bytes of the caller's cell records the
+ * drop-ins hold page-locked for their copies (0: the last registration
+ * failed and the copies run from pageable memory, at a lower rate). */
+int64_t tm_dropin_pinned_bytes(void);
 
 #ifdef __cplusplus
 }

@@ -137,3 +137,33 @@ def test_fp64_multistep_against_oracle(gpu, oracle_lib):
     assert st["octsize"] == ref.octsize
     scale = np.max(np.abs(ref.grid))
     assert np.max(np.abs(out["grid"] - ref.grid)) <= 1e-12 * scale
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+def test_dense_clump_big_bins_against_oracle(gpu, oracle_lib, precision):
+    """A clump of 1500 cells inside a cube of side 0.3 h amid a uniform colony:
+    its bins hold far more than 32 cells, so their Morton order comes from the
+    per-block bitonic sort, which also places those cells.  Octree size and
+    every output must match the oracle (the FP32 path's lists overflow there
+    and the search pass serves the colony)."""
+    base = C.make_colony("uniform", 6000, 51, C.initial_radius("uniform", 6000))
+    rng = np.random.Generator(np.random.PCG64(52))
+    k = 1500
+    clump = rng.uniform(-0.15, 0.15, size=(k, 3)) * C.H_DEFAULT
+    col = C.Colony(np.concatenate([base.x, clump[:, 0]]), np.concatenate([base.y, clump[:, 1]]),
+                   np.concatenate([base.z, clump[:, 2]]), np.concatenate([base.size, base.size[:k]]),
+                   np.concatenate([base.young, base.young[:k]]), np.concatenate([base.ctype, base.ctype[:k]]),
+                   np.concatenate([base.phase, base.phase[:k]]), base.types)
+    steps = 2 if precision == "fp64" else 1
+    out, st = gpu.run_colony(col, steps, precision=precision, update="dt", dt=0.01, verlet=True, list_capacity=384)
+    ref = oracle_lib.run(col, steps, which="oracle", update_mode=1, dt=0.01)
+    assert st["device_errors"] == 0
+    assert st["octsize"] == ref.octsize
+    r = {k2: getattr(ref, k2) for k2 in ("x", "y", "z", "density", "v", "mindist", "fx", "fy", "fz", "removecell")}
+    if precision == "fp64":
+        assert_fp64_close(out, r, col.n, "clump")
+    else:
+        pos = ref.density > 0
+        assert rel(out["density"][pos], ref.density[pos]) <= 1e-6
+        f = np.stack([ref.fx, ref.fy, ref.fz])
+        assert np.max(np.abs(np.stack([out["fx"], out["fy"], out["fz"]]) - f)) <= 1e-6 * np.max(np.abs(f))

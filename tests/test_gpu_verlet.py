@@ -173,3 +173,43 @@ def test_list_overflow_falls_back_to_search(oracle_lib, precision):
         assert rel(out["density"][pos], ref.density[pos]) <= 1e-6
         f = np.stack([ref.fx, ref.fy, ref.fz])
         assert np.max(np.abs(np.stack([out["fx"], out["fy"], out["fz"]]) - f)) <= 1e-6 * np.max(np.abs(f))
+
+
+@pytest.mark.parametrize("kind,n,seed,dim", [("clustered", 40000, 38, 3), ("uniform", 30000, 39, 3),
+                                              ("uniform", 20000, 40, 2)])
+def test_fp32_lists_walk_skip_keeps_v(kind, n, seed, dim):
+    """The list pass settles v = 0 without the octree walk when a list entry
+    inside the query box precedes the first within-h neighbour in Morton
+    order.  Diagnostics walk every cell; v must not change bit for bit, over
+    steps with and without list rebuilds."""
+    from timothy_gb300 import session as S
+
+    col = C.make_colony(kind, n, seed, C.initial_radius(kind, n, dim=dim), dim=dim)
+    fields = ["x", "y", "z", "density", "v", "mindist", "fx", "fy", "fz"]
+    a, sa = S.run_colony(col, 6, precision="fp32c", update="dt", dt=0.01, verlet=True, fields=fields)
+    b, sb = S.run_colony(col, 6, precision="fp32c", update="dt", dt=0.01, verlet=True, diagnostics=True,
+                         fields=fields)
+    for k in fields:
+        assert np.array_equal(a[k], b[k]), k
+    assert sb["walked_cells"] == col.n
+    assert sa["walked_cells"] < sb["walked_cells"]
+    assert 1 <= sa["list_rebuilds"] < 6
+
+
+def test_fp32_lists_v_against_fp64_search(oracle_lib):
+    """One step without diagnostics: v of the FP32 list path is within 1e-5
+    of max |v| of the FP64 oracle's, and zero where the oracle's is, but for
+    cells whose first neighbour barely touches them (the FP32 overlap test
+    may round the other way there)."""
+    from timothy_gb300 import session as S
+
+    col = C.make_colony("clustered", 40000, 41, C.initial_radius("clustered", 40000))
+    out, st = S.run_colony(col, 1, precision="fp32c", update="none", verlet=True, fields=["v"])
+    ref = oracle_lib.run(col, 1, which="oracle", update_mode=0)
+    vs = np.max(np.abs(ref.v))
+    assert vs > 0.0
+    assert np.max(np.abs(out["v"] - ref.v)) <= 1e-5 * vs
+    flip = (out["v"] == 0.0) != (ref.v == 0.0)
+    assert np.all(np.abs(ref.v[flip]) <= 1e-5 * vs)
+    assert np.count_nonzero(ref.v) > 0 and np.count_nonzero(out["v"]) > 0
+    assert st["walked_cells"] < col.n

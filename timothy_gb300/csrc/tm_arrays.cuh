@@ -47,6 +47,7 @@ struct tm_arrays {
     uint4 *code;         // lattice codes in the pre-sort order
     uint4 *codes;        // lattice codes in Morton order
     uint32_t *bin;       // global bin-table index of each pre-sort slot
+    int *grp;            // slots grouped by bin at their bins' Morton positions (build scratch)
     int *tmp;            // Morton position -> slot
     int *rank;           // slot -> Morton position
     float4 *hi, *lo;     // FP32 split positions (hi.w = size)
@@ -66,8 +67,14 @@ struct tm_arrays {
     // the C library's rand() values of updatepositions' random move, dim per
     // cell in the caller's order (drop-in only; null: a counter-based stream)
     const int *move_draws;
-    int *work;           // work[2], work[3]: cells queued for the octree walk
+    int *work;           // work[2], work[3]: cells queued for the octree walk; work[4]: list build's next group
     int *walk_list;
+    // worklists of 32-slot groups, wl_stride words each: entry c is the first
+    // group of colony c in the list (an exclusive prefix over the colonies),
+    // entry ncol the list's length.  List 0: colonies that rebuild this step;
+    // list 1: colonies the octree walk's first pass serves (no lists in use)
+    uint32_t *wl;
+    int wl_stride;
     // outputs (Morton order)
     double *density, *v, *mindist, *fx, *fy, *fz;
     int *nbcount;
@@ -109,13 +116,14 @@ __device__ __forceinline__ bool tm_live(long long i, const tm_desc &d)
 // Cells with neighbours within h fill the walk list from the front
 // (work[2]), isolated cells -- whose walks visit every candidate -- from the
 // back (work[3]), so warps of the walk hold walks of similar length.
-__device__ __forceinline__ void tm_queue_walk(const tm_arrays &a, long long i, bool isolated, bool walk)
+__device__ __forceinline__ void tm_queue_walk(const tm_arrays &a, int c, long long i, bool isolated, bool walk)
 {
     if (!walk) a.v[i] = 0.0;
     const unsigned am = __activemask();
     const unsigned mf = __ballot_sync(am, walk && !isolated), mb = __ballot_sync(am, walk && isolated);
     const int lane = threadIdx.x & 31;
     const unsigned below = (1u << lane) - 1u;
+    if ((mf | mb) && lane == __ffs(mf | mb) - 1) atomicAdd(&a.frame[c].walks, (unsigned long long)__popc(mf | mb));
     if (mf) {
         const int leader = __ffs(mf) - 1;
         int base = 0;
@@ -135,8 +143,8 @@ __device__ __forceinline__ void tm_queue_walk(const tm_arrays &a, long long i, b
 // The same for kernels where several lanes share a cell: every lane of the
 // warp calls it, the cell's owner lane carries it, and the warp makes one
 // append per queue.
-__device__ __forceinline__ void tm_queue_walk_owned(const tm_arrays &a, long long i, bool owner, bool isolated,
-                                                    bool walk)
+__device__ __forceinline__ void tm_queue_walk_owned(const tm_arrays &a, int c, long long i, bool owner,
+                                                    bool isolated, bool walk)
 {
     if (owner && !walk) a.v[i] = 0.0;
     const unsigned am = __activemask();
@@ -144,6 +152,7 @@ __device__ __forceinline__ void tm_queue_walk_owned(const tm_arrays &a, long lon
     const unsigned mf = __ballot_sync(am, wf), mb = __ballot_sync(am, wb);
     const int lane = threadIdx.x & 31;
     const unsigned below = (1u << lane) - 1u;
+    if ((mf | mb) && lane == __ffs(mf | mb) - 1) atomicAdd(&a.frame[c].walks, (unsigned long long)__popc(mf | mb));
     if (mf) {
         const int leader = __ffs(mf) - 1;
         int base = 0;
@@ -158,6 +167,20 @@ __device__ __forceinline__ void tm_queue_walk_owned(const tm_arrays &a, long lon
         base = __shfl_sync(am, base, leader);
         if (wb) a.walk_list[a.nslots_total - 1 - (base + __popc(mb & below))] = (int)i;
     }
+}
+
+// First slot of the q-th group of worklist wl (q below its length) and the
+// group's colony: the colony whose prefix entry is the last one <= q.
+__device__ __forceinline__ long long tm_wl_slot(const tm_arrays &a, const uint32_t *wl, uint32_t q, int &c)
+{
+    int lo = 0, hi = a.ncol;              // wl[lo] <= q < wl[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (wl[mid] <= q) lo = mid;
+        else hi = mid;
+    }
+    c = lo;
+    return a.desc[lo].off + 32ll * (long long)(q - wl[lo]);
 }
 
 // launch shapes chosen per session (tm_tuning)

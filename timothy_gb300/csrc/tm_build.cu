@@ -31,6 +31,7 @@ __global__ void k_step_init(tm_arrays a)
     f.boundary_pairs = 0;
     f.codes_slow = 0;
     f.fix64 = 0;
+    f.walks = 0;
     // Neighbour lists stay valid while no pair can have come from beyond
     // h + skin to within h: every cell moved less than skin/2 since the lists
     // were built (maxdisp carries a float-rounding margin).
@@ -74,8 +75,11 @@ __global__ void k_binbase(tm_arrays a)
 // Each warp streams BBOX_GROUPS groups of 32 slots (a group lies in one
 // colony: colonies are 32-aligned) and keeps running per-type minima and
 // maxima in registers; it reduces them across the lanes and posts them only
-// when the colony changes and at the end of its groups.
+// when the colony changes and at the end of its groups.  The positions, types
+// and colonies of BBOX_BATCH groups are loaded before any of them is used, so
+// a warp waits for memory once per batch rather than once per group.
 #define BBOX_GROUPS 16
+#define BBOX_BATCH 4
 
 template <int NT>
 __device__ __forceinline__ void bbox_post(tm_arrays &a, int c, unsigned long long (&r)[NT][6], int lane)
@@ -101,6 +105,22 @@ __device__ __forceinline__ void bbox_post(tm_arrays &a, int c, unsigned long lon
 }
 
 template <int NT>
+__device__ __forceinline__ void bbox_take(unsigned long long (&r)[NT][6], int t, double x, double y, double z)
+{
+    const unsigned long long v0 = tm_ordered(x), v1 = tm_ordered(y), v2 = tm_ordered(z);
+#pragma unroll
+    for (int tt = 0; tt < NT; tt++) {
+        if (t != tt) continue;
+        r[tt][0] = v0 < r[tt][0] ? v0 : r[tt][0];
+        r[tt][1] = v1 < r[tt][1] ? v1 : r[tt][1];
+        r[tt][2] = v2 < r[tt][2] ? v2 : r[tt][2];
+        r[tt][3] = v0 > r[tt][3] ? v0 : r[tt][3];
+        r[tt][4] = v1 > r[tt][4] ? v1 : r[tt][4];
+        r[tt][5] = v2 > r[tt][5] ? v2 : r[tt][5];
+    }
+}
+
+template <int NT>
 __global__ void __launch_bounds__(256) k_bbox(tm_arrays a, int ntypes)
 {
     const int lane = threadIdx.x & 31;
@@ -114,27 +134,49 @@ __global__ void __launch_bounds__(256) k_bbox(tm_arrays a, int ntypes)
 #pragma unroll
         for (int q = 0; q < 6; q++) r[tt][q] = q < 3 ? 0xffffffffffffffffull : 0ull;
     int cur = -1;                                   // the colony being reduced
-    for (long long g = g0; g < g1; g++) {
-        const long long s = (g << 5) + lane;
-        const int c = a.col[g << 5];                // uniform over the group
-        const tm_desc &d = a.desc[c];
-        if (!d.active) continue;
-        if (c != cur) {
-            if (cur >= 0) bbox_post<NT>(a, cur, r, lane);
-            cur = c;
-        }
-        if (s >= a.nslots_total || !tm_live(s, d)) continue;
-        const int t = a.ctype[s];
-        const unsigned long long v0 = tm_ordered(a.x[s]), v1 = tm_ordered(a.y[s]), v2 = tm_ordered(a.z[s]);
+    for (long long gb = g0; gb < g1; gb += BBOX_BATCH) {
+        double px[BBOX_BATCH], py[BBOX_BATCH], pz[BBOX_BATCH];
+        int pt[BBOX_BATCH], pc[BBOX_BATCH];
 #pragma unroll
-        for (int tt = 0; tt < NT; tt++) {
-            if (t != tt) continue;
-            r[tt][0] = v0 < r[tt][0] ? v0 : r[tt][0];
-            r[tt][1] = v1 < r[tt][1] ? v1 : r[tt][1];
-            r[tt][2] = v2 < r[tt][2] ? v2 : r[tt][2];
-            r[tt][3] = v0 > r[tt][3] ? v0 : r[tt][3];
-            r[tt][4] = v1 > r[tt][4] ? v1 : r[tt][4];
-            r[tt][5] = v2 > r[tt][5] ? v2 : r[tt][5];
+        for (int u = 0; u < BBOX_BATCH; u++) {
+            const long long g = gb + u, s = (g << 5) + lane;
+            const bool in = g < g1 && s < a.nslots_total;
+            pc[u] = g < g1 ? a.col[g << 5] : -1;    // uniform over the group
+            px[u] = in ? a.x[s] : 0.0;
+            py[u] = in ? a.y[s] : 0.0;
+            pz[u] = in ? a.z[s] : 0.0;
+            pt[u] = in ? a.ctype[s] : -1;
+        }
+        bool one = true;                            // the batch lies in one colony
+#pragma unroll
+        for (int u = 1; u < BBOX_BATCH; u++) one = one && (pc[u] == pc[0] || pc[u] < 0);
+        if (one) {
+            const int c = pc[0];
+            const tm_desc &d = a.desc[c];
+            if (!d.active) continue;
+            if (c != cur) {
+                if (cur >= 0) bbox_post<NT>(a, cur, r, lane);
+                cur = c;
+            }
+#pragma unroll
+            for (int u = 0; u < BBOX_BATCH; u++) {
+                const long long s = ((gb + u) << 5) + lane;
+                if (pc[u] >= 0 && s < a.nslots_total && tm_live(s, d)) bbox_take<NT>(r, pt[u], px[u], py[u], pz[u]);
+            }
+        } else {
+            // a colony boundary inside the batch: group by group
+#pragma unroll 1
+            for (long long g = gb; g < gb + BBOX_BATCH && g < g1; g++) {
+                const int c = a.col[g << 5];
+                const tm_desc &d = a.desc[c];
+                if (!d.active) continue;
+                if (c != cur) {
+                    if (cur >= 0) bbox_post<NT>(a, cur, r, lane);
+                    cur = c;
+                }
+                const long long s = (g << 5) + lane;
+                if (s < a.nslots_total && tm_live(s, d)) bbox_take<NT>(r, a.ctype[s], a.x[s], a.y[s], a.z[s]);
+            }
         }
     }
     if (cur >= 0) bbox_post<NT>(a, cur, r, lane);
@@ -217,12 +259,13 @@ __global__ void k_codes(tm_arrays a)
 {
     long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= a.nslots_total) return;
+    // the position loads go out with the colony's, not after it
+    const double px = a.x[s], py = a.y[s], pz = a.z[s];
     int c = a.col[s];
     const tm_desc &d = a.desc[c];
     if (!d.active || !tm_live(s, d)) return;
     const tm_frame &f = a.frame[c];
     uint4 q;
-    const double px = a.x[s], py = a.y[s], pz = a.z[s];
     long long X, Y, Z;
     const bool okx = tm_fix47(px, X), oky = tm_fix47(py, Y), okz = tm_fix47(pz, Z);
     unsigned slow = 0;
@@ -240,6 +283,9 @@ __global__ void k_codes(tm_arrays a)
     if ((int)(threadIdx.x & 31) == leader) atomicAdd(&a.bin_count[b], (uint32_t)__popc(peers));
 }
 
+// Group each colony's live slots by bin (grp holds the slots of bin b at the
+// bin's Morton positions, in no particular order); the first slot to reach a
+// bin of more than 32 cells queues it for k_binsort_big.
 __global__ void k_scatter(tm_arrays a)
 {
     long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -247,127 +293,32 @@ __global__ void k_scatter(tm_arrays a)
     int c = a.col[s];
     const tm_desc &d = a.desc[c];
     if (!d.active || !tm_live(s, d)) return;
-    uint32_t b = a.bin[s];
-    long long pos = a.frame[c].bin_base + a.bin_start[b] + atomicAdd(&a.bin_cursor[b], 1u);
-    a.rank[pos] = (int)s;   // grouped by bin; rank is free until k_gather rewrites it
-}
-
-// Sort each bin's slots by full Morton order.  k_scatter left them grouped by
-// bin in rank[]; every cell of a bin of up to 32 counts the bin's codes that
-// sort before its own (ties, an error, by position) and writes its slot at
-// that rank into tmp, so all lanes work and nothing is kept in local arrays.
-// Larger bins are queued for k_binsort_big.
-__global__ void k_binsort_small(tm_arrays a)
-{
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.nslots_total) return;
-    int c = a.col[i];
-    const tm_desc &d = a.desc[c];
-    if (!d.active || !tm_live(i, d)) return;
-    const int r = a.rank[i];
-    const uint32_t b = a.bin[r];
-    const long long st = a.frame[c].bin_base + a.bin_start[b];
-    const uint32_t cnt = a.bin_start[b + 1] - a.bin_start[b];
-    if (cnt > 32) {
-        if (st == i) {
-            atomicAdd(&a.frame[c].nbig, 1);
-            int q = atomicAdd(&a.bigbins[0], 1);
-            a.bigbins[1 + 2 * q] = (int)b;
-            a.bigbins[2 + 2 * q] = c;
-        }
-        return;
-    }
-    const uint4 key = a.code[r];
-    uint32_t rk = 0;
-    bool dup = false;
-    for (uint32_t k = 0; k < cnt; k++) {
-        const long long j = st + (long long)k;
-        if (j == i) continue;
-        const uint4 kj = a.code[a.rank[j]];
-        if (tm_morton_less(kj, key)) rk++;
-        else if (tm_code_eq(kj, key)) {
-            dup = true;
-            if (j < i) rk++;
-        }
-    }
-    if (dup) atomicOr(&a.frame[c].error, TM_ERR_CODES);
-    a.tmp[st + rk] = r;
-}
-
-// one block per large bin: bitonic sort of up to TM_BIG_BIN cells in shared memory
-__global__ void k_binsort_big(tm_arrays a)
-{
-    __shared__ uint4 key[TM_BIG_BIN];
-    __shared__ int idx[TM_BIG_BIN];
-    int nbig = a.bigbins[0];
-    for (int q = blockIdx.x; q < nbig; q += gridDim.x) {
-        uint32_t b = (uint32_t)a.bigbins[1 + 2 * q];
-        int c = a.bigbins[2 + 2 * q];
-        long long st = a.frame[c].bin_base + a.bin_start[b];
-        uint32_t cnt = a.bin_start[b + 1] - a.bin_start[b];
-        if (cnt > TM_BIG_BIN) {
-            if (threadIdx.x == 0) atomicOr(&a.frame[c].error, TM_ERR_BIGBIN);
-            continue;
-        }
-        uint32_t p2 = 1;
-        while (p2 < cnt) p2 <<= 1;
-        for (uint32_t k = threadIdx.x; k < p2; k += blockDim.x) {
-            if (k < cnt) {
-                idx[k] = a.rank[st + k];      // grouped by k_scatter
-                key[k] = a.code[idx[k]];
-            } else {
-                idx[k] = -1;
-                key[k] = make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
-            }
-        }
-        __syncthreads();
-        for (uint32_t size = 2; size <= p2; size <<= 1) {
-            for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
-                for (uint32_t k = threadIdx.x; k < p2; k += blockDim.x) {
-                    uint32_t m = k ^ stride;
-                    if (m > k) {
-                        bool up = (k & size) == 0;
-                        uint4 ka = key[k], kb = key[m];
-                        // padding keys (idx -1) sort last
-                        bool a_pad = idx[k] < 0, b_pad = idx[m] < 0;
-                        bool gt = a_pad ? !b_pad : (b_pad ? false : tm_morton_less(kb, ka));
-                        if (gt == up) {
-                            key[k] = kb;
-                            key[m] = ka;
-                            int t = idx[k];
-                            idx[k] = idx[m];
-                            idx[m] = t;
-                        }
-                    }
-                }
-                __syncthreads();
-            }
-        }
-        for (uint32_t k = threadIdx.x; k < cnt; k += blockDim.x) {
-            a.tmp[st + k] = idx[k];
-            if (k > 0 && tm_code_eq(key[k], key[k - 1])) atomicOr(&a.frame[c].error, TM_ERR_CODES);
-        }
-        __syncthreads();
+    const uint32_t b = a.bin[s];
+    const uint32_t k = atomicAdd(&a.bin_cursor[b], 1u);
+    const uint32_t b0 = a.bin_start[b];
+    a.grp[a.frame[c].bin_base + b0 + k] = (int)s;
+    if (k == 0 && a.bin_start[b + 1] - b0 > 32) {
+        atomicAdd(&a.frame[c].nbig, 1);
+        const int q = atomicAdd(&a.bigbins[0], 1);
+        a.bigbins[1 + 2 * q] = (int)b;
+        a.bigbins[2 + 2 * q] = c;
     }
 }
 
-// Morton order bookkeeping of every step, and for colonies that rebuild their
-// neighbour lists the move of the state into Morton order (into the scratch
-// buffers; k_copyback brings it back).  Positions are split for the FP32 path
-// and the FP64 density weights sc_t * (size_j / csize_t) of potential.c:62 are
+// Morton order bookkeeping of every step for the cell in slot r, whose
+// Morton position is i, and for colonies that rebuild their neighbour lists
+// the move of its state into Morton order (into the scratch buffers;
+// k_copyback brings it back).  Positions are split for the FP32 path and the
+// FP64 density weights sc_t * (size_j / csize_t) of potential.c:62 are
 // precomputed for every query type t.
-__global__ void k_gather(tm_arrays a, const tm_consts *K)
+__device__ __forceinline__ void place_one(const tm_arrays &a, const tm_consts *K, const tm_desc &d, bool rebuild,
+                                          long long r, long long i, uint4 key, double x, double y, double z,
+                                          double sz)
 {
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;   // Morton position
-    if (i >= a.nslots_total) return;
-    int c = a.col[i];
-    const tm_desc &d = a.desc[c];
-    if (!d.active || !tm_live(i, d)) return;
-    const int r = a.tmp[i];                 // slot of the cell at this position
-    a.codes[i] = a.code[r];
-    const double x = a.x[r], y = a.y[r], z = a.z[r], sz = a.size[r];
+    a.tmp[i] = (int)r;
+    a.codes[i] = key;
     long long s;                            // slot the split positions go to
-    if (a.frame[c].rebuild) {
+    if (rebuild) {
         a.x2[i] = x;
         a.y2[i] = y;
         a.z2[i] = z;
@@ -396,13 +347,107 @@ __global__ void k_gather(tm_arrays a, const tm_consts *K)
     a.lo[s] = make_float4(lx, ly, lz, __int_as_float((int)i));
 }
 
-__global__ void k_copyback(tm_arrays a)
+// One thread per slot: the cell's Morton position is its bin's first
+// position plus the number of the bin's cells whose codes sort before its own
+// (ties, an error, by slot); then the cell is placed there.  The cell's own
+// data are read in slot order; only the bin's members (up to 32, grouped by
+// k_scatter) are gathered.  Cells of larger bins are left to k_binsort_big.
+__global__ void __launch_bounds__(256) k_place(tm_arrays a, const tm_consts *K)
 {
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.nslots_total) return;
-    int c = a.col[i];
+    const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= a.nslots_total) return;
+    const double x = a.x[r], y = a.y[r], z = a.z[r], sz = a.size[r];
+    const uint4 key = a.code[r];
+    const uint32_t b = a.bin[r];
+    const int c = a.col[r];
     const tm_desc &d = a.desc[c];
-    if (!d.active || !tm_live(i, d) || !a.frame[c].rebuild) return;
+    if (!d.active || !tm_live(r, d)) return;
+    const tm_frame &f = a.frame[c];
+    const uint32_t b0 = a.bin_start[b];
+    const uint32_t cnt = a.bin_start[b + 1] - b0;
+    if (cnt > 32) return;
+    const long long st = f.bin_base + b0;
+    uint32_t rk = 0;
+    bool dup = false;
+    for (uint32_t k = 0; k < cnt; k++) {
+        const int j = a.grp[st + k];
+        if (j == (int)r) continue;
+        const uint4 kj = a.code[j];
+        if (tm_morton_less(kj, key)) rk++;
+        else if (tm_code_eq(kj, key)) {
+            dup = true;
+            if (j < (int)r) rk++;
+        }
+    }
+    if (dup) atomicOr(&a.frame[c].error, TM_ERR_CODES);
+    place_one(a, K, d, f.rebuild != 0, r, st + rk, key, x, y, z, sz);
+}
+
+// one block per large bin: bitonic sort of up to TM_BIG_BIN cells in shared
+// memory, then the cells are placed at their Morton positions
+__global__ void k_binsort_big(tm_arrays a, const tm_consts *K)
+{
+    __shared__ uint4 key[TM_BIG_BIN];
+    __shared__ int idx[TM_BIG_BIN];
+    int nbig = a.bigbins[0];
+    for (int q = blockIdx.x; q < nbig; q += gridDim.x) {
+        uint32_t b = (uint32_t)a.bigbins[1 + 2 * q];
+        int c = a.bigbins[2 + 2 * q];
+        const tm_desc &d = a.desc[c];
+        const tm_frame &f = a.frame[c];
+        long long st = f.bin_base + a.bin_start[b];
+        uint32_t cnt = a.bin_start[b + 1] - a.bin_start[b];
+        if (cnt > TM_BIG_BIN) {
+            if (threadIdx.x == 0) atomicOr(&a.frame[c].error, TM_ERR_BIGBIN);
+            continue;
+        }
+        uint32_t p2 = 1;
+        while (p2 < cnt) p2 <<= 1;
+        for (uint32_t k = threadIdx.x; k < p2; k += blockDim.x) {
+            if (k < cnt) {
+                idx[k] = a.grp[st + k];       // grouped by k_scatter
+                key[k] = a.code[idx[k]];
+            } else {
+                idx[k] = -1;
+                key[k] = make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
+            }
+        }
+        __syncthreads();
+        for (uint32_t size = 2; size <= p2; size <<= 1) {
+            for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+                for (uint32_t k = threadIdx.x; k < p2; k += blockDim.x) {
+                    uint32_t m = k ^ stride;
+                    if (m > k) {
+                        bool up = (k & size) == 0;
+                        uint4 ka = key[k], kb = key[m];
+                        // padding keys (idx -1) sort last; equal codes by slot
+                        bool a_pad = idx[k] < 0, b_pad = idx[m] < 0;
+                        bool gt = a_pad ? !b_pad
+                                        : (b_pad ? false
+                                                 : (tm_morton_less(kb, ka) || (tm_code_eq(kb, ka) && idx[m] < idx[k])));
+                        if (gt == up) {
+                            key[k] = kb;
+                            key[m] = ka;
+                            int t = idx[k];
+                            idx[k] = idx[m];
+                            idx[m] = t;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        for (uint32_t k = threadIdx.x; k < cnt; k += blockDim.x) {
+            if (k > 0 && tm_code_eq(key[k], key[k - 1])) atomicOr(&a.frame[c].error, TM_ERR_CODES);
+            const long long r = idx[k];
+            place_one(a, K, d, f.rebuild != 0, r, st + k, key[k], a.x[r], a.y[r], a.z[r], a.size[r]);
+        }
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ void copyback_one(const tm_arrays &a, long long i)
+{
     a.x[i] = a.x2[i];
     a.y[i] = a.y2[i];
     a.z[i] = a.z2[i];
@@ -412,6 +457,74 @@ __global__ void k_copyback(tm_arrays a)
     a.phase[i] = a.phase2[i];
     a.perm[i] = a.perm2[i];
     a.rem[i] = a.rem2[i];
+}
+
+// 32-slot groups of the colonies a worklist holds (see tm_arrays.wl)
+__device__ __forceinline__ uint32_t wl_groups(const tm_arrays &a, int c, int which)
+{
+    const tm_desc &d = a.desc[c];
+    const tm_frame &f = a.frame[c];
+    if (!d.active || d.n == 0) return 0;
+    const bool in = which == 0 ? f.rebuild != 0 : (d.n > 1 && (!d.verlet || !f.list_ok));
+    return in ? (uint32_t)((d.n + 31) >> 5) : 0u;
+}
+
+// One block: worklist `which` as an exclusive prefix over the colonies.  The
+// kernels that serve only some colonies in a step (the copy back and the list
+// build on rebuild steps, the walk's first pass for colonies without lists)
+// stride over the list's groups with a small grid, so a step where no colony
+// needs them costs one launch that reads the list's length, not a pass over
+// every slot.
+__global__ void __launch_bounds__(1024) k_worklist(tm_arrays a, int which)
+{
+    __shared__ uint32_t part[1024];
+    uint32_t *wl = a.wl + (long long)which * a.wl_stride;
+    const int nc = a.ncol;
+    const int per = (nc + 1023) >> 10;
+    const int c0 = (int)threadIdx.x * per;
+    const int c1 = min(c0 + per, nc);
+    uint32_t sum = 0;
+    for (int c = c0; c < c1; c++) sum += wl_groups(a, c, which);
+    part[threadIdx.x] = sum;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const uint32_t v = threadIdx.x >= (unsigned)o ? part[threadIdx.x - o] : 0u;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    uint32_t run = threadIdx.x ? part[threadIdx.x - 1] : 0u;
+    for (int c = c0; c < c1; c++) {
+        wl[c] = run;
+        run += wl_groups(a, c, which);
+    }
+    if (threadIdx.x == 1023) wl[nc] = part[1023];
+}
+
+unsigned tm_stream_grid(int block, int per_sm)
+{
+    static int sms[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < 64 && !sms[dev]) cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
+    const int nsm = (dev >= 0 && dev < 64 && sms[dev] > 0) ? sms[dev] : 152;
+    (void)block;
+    return (unsigned)(nsm * per_sm);
+}
+
+// state of the rebuilding colonies back from the gather target (worklist 0)
+__global__ void __launch_bounds__(256) k_copyback(tm_arrays a)
+{
+    const uint32_t *wl = a.wl;
+    const uint32_t total = wl[a.ncol];
+    const int lane = threadIdx.x & 31;
+    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < total;
+         q += (gridDim.x * blockDim.x) >> 5) {
+        int c;
+        const long long i = tm_wl_slot(a, wl, q, c) + lane;
+        if (!tm_live(i, a.desc[c])) continue;
+        copyback_one(a, i);
+    }
 }
 
 // ---------------------------------------------------------------------------

@@ -83,6 +83,7 @@ struct tm_frame {
     long long patch_lo[3];   // CIC patch corners (patches.c:61-132); INT_MAX/INT_MIN when empty
     long long patch_hi[3];
     unsigned long long fix64;        // FP32 cells whose density this step was redone in FP64 (diagnostic)
+    unsigned long long walks;        // cells of this step that took the octree walk (diagnostic)
 };
 
 // ---------------------------------------------------------------------------

@@ -654,6 +654,8 @@ void tm_dropin_set_precision(int precision, int neighbour_lists)
     g_same_cells = 0;
 }
 
+int64_t tm_dropin_pinned_bytes(void) { return (int64_t)g_pinned_bytes; }
+
 void tm_dropin_shutdown(void)
 {
     if (g_diff) tm_diffusion_destroy(g_diff);

@@ -8,10 +8,12 @@ __global__ void k_frame(tm_arrays a, const tm_consts *K);
 __global__ void k_codes(tm_arrays a);
 __global__ void k_binbase(tm_arrays a);
 __global__ void k_scatter(tm_arrays a);
-__global__ void k_binsort_small(tm_arrays a);
-__global__ void k_binsort_big(tm_arrays a);
-__global__ void k_gather(tm_arrays a, const tm_consts *K);
+__global__ void k_place(tm_arrays a, const tm_consts *K);
+__global__ void k_binsort_big(tm_arrays a, const tm_consts *K);
 __global__ void k_copyback(tm_arrays a);
+__global__ void k_worklist(tm_arrays a, int which);
+// blocks of a grid-stride launch: `per_sm` blocks of `block` threads per SM
+unsigned tm_stream_grid(int block, int per_sm);
 __global__ void k_octsize(tm_arrays a, unsigned long long *out);
 
 cudaError_t tm_scan_exclusive(const uint32_t *in, uint32_t *out, long long n, uint32_t *tmp, cudaStream_t st);

@@ -309,15 +309,10 @@ __device__ __forceinline__ void walk_end(const tm_arrays &a, const tm_consts *K,
 // FP32).  Cells that must walk -- those, isolated cells (mindist comes from
 // the walk) and every cell in diagnostics mode -- are queued, so the walk
 // runs with full warps.
-__global__ void __launch_bounds__(256) k_octree_mark(tm_arrays a)
+__device__ __forceinline__ void octree_mark_cell(const tm_arrays &a, int c, long long p)
 {
-    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (((p >> 5) << 5) >= a.nslots_total) return;
-    const int c = a.col[(p >> 5) << 5];                  // colonies are 32-aligned
     const tm_desc &d = a.desc[c];
-    if (!d.active || d.n <= 1) return;
     const tm_frame &f = a.frame[c];
-    if (d.verlet && f.list_ok) return;                   // done by the list kernel
     if (!tm_live(p, d)) return;
     const bool isolated = a.nbcount[p] == 0;
     bool walk = isolated || a.want_diag;
@@ -331,7 +326,22 @@ __global__ void __launch_bounds__(256) k_octree_mark(tm_arrays a)
         const float rs = (hp.w + hm.w) * 1.0001f + 1e-5f;
         walk = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < rs * rs;
     }
-    tm_queue_walk(a, p, isolated, walk);
+    tm_queue_walk(a, c, p, isolated, walk);
+}
+
+// the cells of the colonies without lists in use this step (worklist 1), a
+// warp per 32-slot group
+__global__ void __launch_bounds__(256) k_octree_mark(tm_arrays a)
+{
+    const uint32_t *wl = a.wl + a.wl_stride;
+    const uint32_t total = wl[a.ncol];
+    const int lane = threadIdx.x & 31;
+    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < total;
+         q += (gridDim.x * blockDim.x) >> 5) {
+        int c;
+        const long long p = tm_wl_slot(a, wl, q, c) + lane;
+        octree_mark_cell(a, c, p);
+    }
 }
 
 // Pass 2: the walk of every queued cell (grid-stride over both queues).  Each
@@ -368,9 +378,9 @@ __global__ void __launch_bounds__(256, 4) k_octree(tm_arrays a, const tm_consts 
 cudaError_t tm_launch_octree(const tm_arrays &a, const tm_consts *K, int block, cudaStream_t st)
 {
     if (block != 64 && block != 256) block = 128;
-    unsigned grid = (unsigned)((a.nslots_total + 255) / 256);
-    if (grid == 0) return cudaSuccess;
-    k_octree_mark<<<grid, 256, 0, st>>>(a);
+    if (a.nslots_total == 0 || a.ncol == 0) return cudaSuccess;
+    k_worklist<<<1, 1024, 0, st>>>(a, 1);
+    k_octree_mark<<<tm_stream_grid(256, 8), 256, 0, st>>>(a);
     // the queue length is known on the device only: a grid of resident size
     static int sms[64] = {};
     int dev = 0;

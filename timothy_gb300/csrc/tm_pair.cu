@@ -548,16 +548,11 @@ __global__ void __launch_bounds__(TM_WARPS_PER_BLOCK * 32) k_pair(tm_arrays a, c
 // (double-float distance) is appended to its list; the list kernel then
 // decides the cutoff exactly.  The list order (bins z, y, x, then Morton order
 // inside a bin) depends on the colony's own cells only.
-__global__ void __launch_bounds__(256) k_listbuild(tm_arrays a, const tm_consts *K)
+__device__ __forceinline__ void listbuild_cell(const tm_arrays &a, const tm_consts *K, int c, long long i)
 {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (((i >> 5) << 5) >= a.nslots_total) return;
-    const int c = a.col[(i >> 5) << 5];
     const tm_desc &d = a.desc[c];
-    if (!d.active || d.n <= 1 || !d.verlet) return;
+    if (d.n <= 1 || !d.verlet || !tm_live(i, d)) return;
     const tm_frame &f = a.frame[c];
-    if (!f.rebuild) return;
-    if (!tm_live(i, d)) return;
     const tm_type &T = K->t[a.ctype[i]];
     const float rlist = T.hf + d.skin;
     const float hr = rlist * 1.00002f + 1e-4f;
@@ -640,6 +635,27 @@ __global__ void __launch_bounds__(256) k_listbuild(tm_arrays a, const tm_consts 
         if (atomicExch(&a.frame[c].list_ok, 0) == 1) atomicAdd(&a.work[1], 1);
 }
 
+// the cells of the colonies that rebuild this step (worklist 0), a warp per
+// 32-slot group; warps take the next group from a counter (work[4]) as they
+// finish one, since groups differ widely in cost (dense regions hold more
+// candidates), and consecutive groups run at about the same time (their
+// bins and positions share the caches)
+__global__ void __launch_bounds__(256) k_listbuild(tm_arrays a, const tm_consts *K)
+{
+    const uint32_t *wl = a.wl;
+    const uint32_t total = wl[a.ncol];
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        uint32_t q = 0;
+        if (lane == 0) q = atomicAdd((unsigned *)&a.work[4], 1u);
+        q = __shfl_sync(0xffffffffu, q, 0);
+        if (q >= total) break;
+        int c;
+        const long long i = tm_wl_slot(a, wl, q, c) + lane;
+        listbuild_cell(a, K, c, i);
+    }
+}
+
 template <int PREC>
 __device__ __forceinline__ void plist_one(const tm_arrays &a, const tm_type &T, int dim, int t, long long i,
                                           float4 hi_i, float4 lo_i, int j, float4 hj, float4 lj, pair_acc<PREC> &acc,
@@ -716,7 +732,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_plist(tm_arrays a, const tm_con
         const float rs = (hi_i.w + hm.w) * 1.0001f + 1e-5f;
         walk = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < rs * rs;
     }
-    tm_queue_walk(a, i, cnt_nb == 0, walk);
+    tm_queue_walk(a, c, i, cnt_nb == 0, walk);
     if constexpr (PREC == 1) {
         if (needs_fix64(acc)) {
             // FP64 density over the same list, the cutoff decided in FP64
@@ -739,29 +755,26 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_plist(tm_arrays a, const tm_con
 // Morton-consecutive cells, whose list lengths differ less than those of 32.
 #define PLIST_LPC 4
 
-// cp.async (global -> shared, through L1) and its group waits
-__device__ __forceinline__ void cpasync16(void *smem, const void *gmem)
-{
-    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cpasync4(void *smem, const void *gmem)
-{
-    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cpasync_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cpasync_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
-__device__ __forceinline__ void cpasync_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
-
-// D = 0: two entries in flight in registers.  D > 0: a per-thread ring in
-// shared memory fed by cp.async keeps D entries' positions and, D entries
-// further ahead, their list indices in flight without holding registers: at
-// entry m the thread waits for the copies issued at entry m - D, evaluates
-// entry m, then issues the positions of entry m + D and the index of entry
-// m + 2 D into the slots it just consumed.
-template <int BLOCK, int MINB, int D, bool DIAG>
+// Each lane takes two entries per iteration (its entries q, q + LPC, then
+// q + 2 LPC, ...) with the next two list indices already loading, and forms
+// both entries' terms without branches on the cutoff: those of an entry
+// beyond h (or absent) are zeroed, and each accumulator takes the pair's sum
+// in one compensated add.  The pre-add rounds once per pair, an error of the
+// same order as the compensated sum's own (eps times the sum of the
+// magnitudes), and halves the compensated adds.
+//
+// v needs the octree walk only when no candidate precedes the first within-h
+// neighbour m in Morton order (then j* = m, see tm_octree.cu).  A list entry
+// j whose position lies inside p's query box [x - h, x + h) on every axis is
+// a candidate: its own lattice code lies in the box, so its leaf meets it.
+// The box test is taken with a margin (1e-4 h, two lattice units and the
+// float error of the split distance), so an entry that passes is inside the
+// box in the reference's FP64 lattice arithmetic too; boxmin is the least
+// Morton position of such entries, and boxmin < m means j* precedes m: j* is
+// not within h and v = 0 without a walk.  Both minima travel in one key,
+// 2 pos + 1 for an entry within h and 2 pos for one only inside the box: the
+// least key is m's (odd) unless a box entry precedes m (even).
+template <int BLOCK, int MINB, bool DIAG>
 __global__ void __launch_bounds__(BLOCK, MINB) k_plist32(tm_arrays a, const tm_consts *K)
 {
     constexpr int LPC = PLIST_LPC;
@@ -785,137 +798,65 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_plist32(tm_arrays a, const tm_c
     const float4 lo_i = live ? a.lo[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 *__restrict__ hi = a.hi;
     const float4 *__restrict__ lo = a.lo;
+    // query-box half width with the margin (a lattice unit is scale / 2^29)
+    const float hbox = T.hf * (1.0f - 1e-4f) - (float)f.scale * 3.7252903e-9f;
     pair_acc<1> acc;
     acc.init();
-    int cnt_nb = 0, nbmin = 0x7fffffff;
+    int cnt_nb = 0;
+    unsigned key = 0xffffffffu;
     unsigned long long hash = 0;
     const int cnt = live ? __ldg(a.vcount + i) : 0;
     const long long ls = a.lstride;
     const int drow = (DIAG && live) ? diag_row_of(a, d, i) : -1;
     const int *__restrict__ lst = a.vlist + i;
-    auto one = [&](int j, float4 hj, float4 lj) {
-        const float dx = (hj.x - hi_i.x) + (lj.x - lo_i.x);
-        const float dy = (hj.y - hi_i.y) + (lj.y - lo_i.y);
-        const float dz = (hj.z - hi_i.z) + (lj.z - lo_i.z);
-        const float s = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        bool in = s <= thr_lo;
-        if (!in && s <= thr_hi) in = dist64(a, i, j) <= T.h;   // FP64 only in the cutoff band
-        if (in) {
-            pair32(T, dim, dx, dy, dz, s, hj.w, acc);
-            cnt_nb++;
-            nbmin = min(nbmin, __float_as_int(lj.w));
-            if (DIAG) diag_pair(a, drow, j, hash);
+    int k = q;
+    int ja = k < cnt ? __ldg(lst + k * ls) : 0;
+    int jb = k + LPC < cnt ? __ldg(lst + (k + LPC) * ls) : 0;
+    for (; k < cnt; k += 2 * LPC) {
+        const int kn = k + 2 * LPC;
+        const int na = kn < cnt ? __ldg(lst + kn * ls) : 0;
+        const int nb = kn + LPC < cnt ? __ldg(lst + (kn + LPC) * ls) : 0;
+        const bool hasb = k + LPC < cnt;
+        const float4 ha = __ldg(hi + ja), la = __ldg(lo + ja);
+        const float4 hb = __ldg(hi + jb), lb = __ldg(lo + jb);   // jb = 0 (a valid slot) when absent
+        const float dxa = (ha.x - hi_i.x) + (la.x - lo_i.x), dya = (ha.y - hi_i.y) + (la.y - lo_i.y),
+                    dza = (ha.z - hi_i.z) + (la.z - lo_i.z);
+        const float dxb = (hb.x - hi_i.x) + (lb.x - lo_i.x), dyb = (hb.y - hi_i.y) + (lb.y - lo_i.y),
+                    dzb = (hb.z - hi_i.z) + (lb.z - lo_i.z);
+        const float sa = fmaf(dxa, dxa, fmaf(dya, dya, dza * dza));
+        const float sb = fmaf(dxb, dxb, fmaf(dyb, dyb, dzb * dzb));
+        bool ina = sa <= thr_lo, inb = hasb && sb <= thr_lo;
+        if (!ina && sa <= thr_hi) ina = dist64(a, i, ja) <= T.h;            // FP64 only in the band
+        if (hasb && !inb && sb <= thr_hi) inb = dist64(a, i, jb) <= T.h;
+        float ta, ea, ga, tb, eb, gb;
+        pair32_terms(T, sa, ha.w, ta, ea, ga);
+        pair32_terms(T, sb, hb.w, tb, eb, gb);
+        ta = ina ? ta : 0.0f;
+        ea = ina ? ea : 0.0f;
+        ga = ina ? ga : 0.0f;
+        tb = inb ? tb : 0.0f;
+        eb = inb ? eb : 0.0f;
+        gb = inb ? gb : 0.0f;
+        acc.dens.add(ta + tb);
+        acc.err2 = fmaf(ea, ea, fmaf(eb, eb, acc.err2));
+        acc.fx.add(fmaf(ga, dxa, gb * dxb));
+        acc.fy.add(fmaf(ga, dya, gb * dyb));
+        if (dim == 3) acc.fz.add(fmaf(ga, dza, gb * dzb));
+        // over every entry: with a neighbour within h the minimum is one of
+        // them (an entry beyond h is farther); a cell with none takes its
+        // mindist from the octree walk
+        acc.mins = fminf(acc.mins, fminf(sa, hasb ? sb : 3.0e38f));
+        cnt_nb += (ina ? 1 : 0) + (inb ? 1 : 0);
+        const unsigned pa = 2u * (unsigned)__float_as_int(la.w), pb = 2u * (unsigned)__float_as_int(lb.w);
+        const bool bxa = fmaxf(fabsf(dxa), fmaxf(fabsf(dya), fabsf(dza))) < hbox;
+        const bool bxb = hasb && fmaxf(fabsf(dxb), fmaxf(fabsf(dyb), fabsf(dzb))) < hbox;
+        key = min(key, min(ina ? pa + 1u : (bxa ? pa : 0xffffffffu), inb ? pb + 1u : (bxb ? pb : 0xffffffffu)));
+        if (DIAG) {
+            if (ina) diag_pair(a, drow, ja, hash);
+            if (inb) diag_pair(a, drow, jb, hash);
         }
-    };
-    if constexpr (D < 0) {
-        // two entries per iteration without branches on the cutoff: both
-        // entries' terms are formed, those of an entry beyond h (or absent)
-        // are zeroed, and each accumulator takes the pair's sum in one
-        // compensated add.  The pre-add rounds once per pair, an error of the
-        // same order as the compensated sum's own (eps times the sum of the
-        // magnitudes), and halves the compensated adds.
-        int k = q;
-        int ja = k < cnt ? __ldg(lst + k * ls) : 0;
-        int jb = k + LPC < cnt ? __ldg(lst + (k + LPC) * ls) : 0;
-        for (; k < cnt; k += 2 * LPC) {
-            const int kn = k + 2 * LPC;
-            const int na = kn < cnt ? __ldg(lst + kn * ls) : 0;
-            const int nb = kn + LPC < cnt ? __ldg(lst + (kn + LPC) * ls) : 0;
-            const bool hasb = k + LPC < cnt;
-            const float4 ha = __ldg(hi + ja), la = __ldg(lo + ja);
-            const float4 hb = __ldg(hi + jb), lb = __ldg(lo + jb);
-            const float dxa = (ha.x - hi_i.x) + (la.x - lo_i.x), dya = (ha.y - hi_i.y) + (la.y - lo_i.y),
-                        dza = (ha.z - hi_i.z) + (la.z - lo_i.z);
-            const float dxb = (hb.x - hi_i.x) + (lb.x - lo_i.x), dyb = (hb.y - hi_i.y) + (lb.y - lo_i.y),
-                        dzb = (hb.z - hi_i.z) + (lb.z - lo_i.z);
-            const float sa = fmaf(dxa, dxa, fmaf(dya, dya, dza * dza));
-            const float sb = fmaf(dxb, dxb, fmaf(dyb, dyb, dzb * dzb));
-            bool ina = sa <= thr_lo, inb = hasb && sb <= thr_lo;
-            if (!ina && sa <= thr_hi) ina = dist64(a, i, ja) <= T.h;            // FP64 only in the band
-            if (hasb && !inb && sb <= thr_hi) inb = dist64(a, i, jb) <= T.h;
-            float ta, ea, ga, tb, eb, gb;
-            pair32_terms(T, sa, ha.w, ta, ea, ga);
-            pair32_terms(T, sb, hb.w, tb, eb, gb);
-            ta = ina ? ta : 0.0f;
-            ea = ina ? ea : 0.0f;
-            ga = ina ? ga : 0.0f;
-            tb = inb ? tb : 0.0f;
-            eb = inb ? eb : 0.0f;
-            gb = inb ? gb : 0.0f;
-            acc.dens.add(ta + tb);
-            acc.err2 = fmaf(ea, ea, fmaf(eb, eb, acc.err2));
-            acc.fx.add(fmaf(ga, dxa, gb * dxb));
-            acc.fy.add(fmaf(ga, dya, gb * dyb));
-            if (dim == 3) acc.fz.add(fmaf(ga, dza, gb * dzb));
-            // over every entry: with a neighbour within h the minimum is one of
-            // them (an entry beyond h is farther); a cell with none takes its
-            // mindist from the octree walk
-            acc.mins = fminf(acc.mins, fminf(sa, hasb ? sb : 3.0e38f));
-            cnt_nb += (ina ? 1 : 0) + (inb ? 1 : 0);
-            nbmin = min(nbmin, min(ina ? __float_as_int(la.w) : 0x7fffffff, inb ? __float_as_int(lb.w) : 0x7fffffff));
-            if (DIAG) {
-                if (ina) diag_pair(a, drow, ja, hash);
-                if (inb) diag_pair(a, drow, jb, hash);
-            }
-            ja = na;
-            jb = nb;
-        }
-    } else if constexpr (D == 0) {
-        int k = q;
-        int ja = k < cnt ? __ldg(lst + k * ls) : 0;
-        int jb = k + LPC < cnt ? __ldg(lst + (k + LPC) * ls) : 0;
-        for (; k < cnt; k += 2 * LPC) {
-            const int kn = k + 2 * LPC;
-            const int na = kn < cnt ? __ldg(lst + kn * ls) : 0;
-            const int nb = kn + LPC < cnt ? __ldg(lst + (kn + LPC) * ls) : 0;
-            const bool hasb = k + LPC < cnt;
-            const float4 ha = __ldg(hi + ja), la = __ldg(lo + ja);
-            const float4 hb = __ldg(hi + jb), lb = __ldg(lo + jb);   // jb = 0 (a valid slot) when absent
-            one(ja, ha, la);
-            if (hasb) one(jb, hb, lb);
-            ja = na;
-            jb = nb;
-        }
-    } else {
-        // rings indexed [slot][thread], so a warp's accesses to one slot are
-        // consecutive 16-byte words (no bank conflicts)
-        __shared__ float4 rh[D][BLOCK], rl[D][BLOCK];
-        __shared__ int rj[D][BLOCK];
-        const int tid = threadIdx.x;
-        const int M = cnt > q ? (cnt - q + LPC - 1) / LPC : 0;   // this lane's entries q + LPC m
-        auto entry = [&](int m) { return lst + (long long)(q + LPC * m) * ls; };
-        int jr[D];
-#pragma unroll
-        for (int u = 0; u < D; u++) {
-            jr[u] = u < M ? __ldg(entry(u)) : 0;
-            if (u < M) {
-                cpasync16(&rh[u][tid], hi + jr[u]);
-                cpasync16(&rl[u][tid], lo + jr[u]);
-            }
-            if (D + u < M) cpasync4(&rj[u][tid], entry(D + u));
-            cpasync_commit();
-        }
-        for (int m0 = 0; m0 < M; m0 += D) {
-#pragma unroll
-            for (int u = 0; u < D; u++) {
-                const int m = m0 + u;
-                if (m < M) {
-                    cpasync_wait<D - 1>();
-                    const float4 hj = rh[u][tid], lj = rl[u][tid];
-                    one(jr[u], hj, lj);
-                    // refill slot u: positions of entry m + D, index of entry m + 2 D
-                    if (m + D < M) {
-                        const int jn = rj[u][tid];
-                        jr[u] = jn;
-                        cpasync16(&rh[u][tid], hi + jn);
-                        cpasync16(&rl[u][tid], lo + jn);
-                        if (m + 2 * D < M) cpasync4(&rj[u][tid], entry(m + 2 * D));
-                    }
-                    cpasync_commit();
-                }
-            }
-        }
-        cpasync_wait_all();
+        ja = na;
+        jb = nb;
     }
     // merge the LPC partial results of each cell (fixed butterfly order)
     for (int o = 1; o < LPC; o <<= 1) {
@@ -926,18 +867,23 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_plist32(tm_arrays a, const tm_c
         acc.mins = fminf(acc.mins, __shfl_xor_sync(FULL, acc.mins, o));
         acc.err2 += __shfl_xor_sync(FULL, acc.err2, o);
         cnt_nb += __shfl_xor_sync(FULL, cnt_nb, o);
-        nbmin = min(nbmin, __shfl_xor_sync(FULL, nbmin, o));
+        key = min(key, __shfl_xor_sync(FULL, key, o));
         if (DIAG) hash += __shfl_xor_sync(FULL, hash, o);
     }
+    // with cnt_nb > 0 an odd key is m's, an even one a box entry's before m
+    // (nbmin is read by the walk only, which then does not run)
+    const int nbmin = (int)(key >> 1);
     // the merged results are the same in the cell's four lanes; lane 0 owns them
     const bool owner = live && q == 0;
     bool walk = false;
     if (owner) {
         pair_store<1>(a, i, acc, cnt_nb, nbmin, hash, false);
         // the octree walk's first pass for this cell (see k_octree_mark): walk
-        // if the first within-h neighbour in Morton order may overlap it
+        // if the first within-h neighbour in Morton order may overlap it and
+        // no list entry shows a candidate before it (diagnostics walk every
+        // cell: they record j*)
         walk = cnt_nb == 0 || DIAG;
-        if (!walk) {
+        if (!walk && (key & 1u)) {
             const long long m = f.ident ? (long long)nbmin : (long long)a.tmp[nbmin];
             const float4 hm = hi[m], lm = lo[m];
             const float dx = (hi_i.x - hm.x) + (lo_i.x - lm.x), dy = (hi_i.y - hm.y) + (lo_i.y - lm.y),
@@ -947,7 +893,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_plist32(tm_arrays a, const tm_c
         }
     }
     // one queue append per warp: every lane takes part, the owners carry the cells
-    tm_queue_walk_owned(a, i, owner, cnt_nb == 0, walk);
+    tm_queue_walk_owned(a, c, i, owner, cnt_nb == 0, walk);
     if (live && needs_fix64(acc)) {
         // FP64 density over the same list, the cutoff decided in FP64, the
         // list split over the cell's lanes and the partial sums added in a
@@ -1032,10 +978,10 @@ static void launch_plist32(const tm_arrays &a, const tm_consts *K, int variant, 
     switch (variant) {
     // every variant accumulates alike (the paired form), so the block shape
     // changes no result bit
-    case 2: k_plist32<64, 16, -1, DIAG><<<(unsigned)((nt + 63) / 64), 64, 0, st>>>(a, K); break;
-    case 3: k_plist32<64, 14, -1, DIAG><<<(unsigned)((nt + 63) / 64), 64, 0, st>>>(a, K); break;
-    case 4: k_plist32<256, 3, -1, DIAG><<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(a, K); break;
-    default: k_plist32<128, 7, -1, DIAG><<<(unsigned)((nt + 127) / 128), 128, 0, st>>>(a, K); break;
+    case 2: k_plist32<64, 16, DIAG><<<(unsigned)((nt + 63) / 64), 64, 0, st>>>(a, K); break;
+    case 3: k_plist32<64, 14, DIAG><<<(unsigned)((nt + 63) / 64), 64, 0, st>>>(a, K); break;
+    case 4: k_plist32<256, 3, DIAG><<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(a, K); break;
+    default: k_plist32<128, 7, DIAG><<<(unsigned)((nt + 127) / 128), 128, 0, st>>>(a, K); break;
     }
 }
 
@@ -1076,7 +1022,7 @@ cudaError_t tm_launch_search(const tm_arrays &a, const tm_consts *K, int prec, c
 cudaError_t tm_launch_listbuild(const tm_arrays &a, const tm_consts *K, cudaStream_t st)
 {
     if (a.vcap == 0 || a.nslots_total == 0) return cudaSuccess;
-    k_listbuild<<<(unsigned)((a.nslots_total + 255) / 256), 256, 0, st>>>(a, K);
+    k_listbuild<<<tm_stream_grid(256, 16), 256, 0, st>>>(a, K);
     return cudaGetLastError();
 }
 

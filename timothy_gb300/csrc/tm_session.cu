@@ -421,7 +421,7 @@ static int enqueue_build(tm_session *s, int p, int &nk)
     CK(cudaMemsetAsync(a.bin_count, 0, (size_t)(nbin + 1) * sizeof(uint32_t), st));
     CK(cudaMemsetAsync(a.bin_cursor, 0, (size_t)(nbin + 1) * sizeof(uint32_t), st));
     CK(cudaMemsetAsync(a.bigbins, 0, sizeof(int), st));
-    CK(cudaMemsetAsync(a.fix_count, 0, 5 * sizeof(int), st));   // fix count and the four work counters
+    CK(cudaMemsetAsync(a.fix_count, 0, 6 * sizeof(int), st));   // fix count and the five work counters
     if (a.diag_cnt) CK(cudaMemsetAsync(a.diag_cnt, 0, (size_t)s->diag_ncells * sizeof(int), st));
     k_step_init<<<blocks_for(ncol, 128), 128, 0, st>>>(a);
     CK(tm_launch_bbox(a, s->K.ntypes, st));
@@ -431,12 +431,12 @@ static int enqueue_build(tm_session *s, int p, int &nk)
     CK(tm_scan_exclusive(a.bin_count, a.bin_start, nbin + 1, s->scan_tmp, st));
     k_binbase<<<blocks_for(ncol, 128), 128, 0, st>>>(a);
     k_scatter<<<blocks_for(nsl, 256), 256, 0, st>>>(a);
-    k_binsort_small<<<blocks_for(nsl, 128), 128, 0, st>>>(a);
-    k_binsort_big<<<64, 256, 0, st>>>(a);
-    k_gather<<<blocks_for(nsl, 256), 256, 0, st>>>(a, s->dK);
-    k_copyback<<<blocks_for(nsl, 256), 256, 0, st>>>(a);
+    k_place<<<blocks_for(nsl, 256), 256, 0, st>>>(a, s->dK);
+    k_binsort_big<<<64, 256, 0, st>>>(a, s->dK);
+    k_worklist<<<1, 1024, 0, st>>>(a, 0);
+    k_copyback<<<tm_stream_grid(256, 8), 256, 0, st>>>(a);
     CK(cudaGetLastError());
-    nk += 13;   // step_init, bbox, frame, codes, 3 scan passes, binbase, scatter, 2 bin sorts, gather, copyback
+    nk += 13;   // step_init, bbox, frame, codes, 3 scan passes, binbase, scatter, place, big-bin sort, worklist, copyback
     return TM_OK;
 }
 
@@ -497,7 +497,7 @@ static int enqueue_compute(tm_session *s, int &nk, bool with_marks)
     }
     if (with_marks) mark(s);
     CK(tm_launch_octree(b, s->dK, s->tune.walk_block, s->stream));
-    nk += 2;   // mark + walk
+    nk += 3;   // worklist, mark, walk
     return TM_OK;
 }
 
@@ -587,11 +587,11 @@ static int session_buffers(tm_session *s, long long S, long long B, long long G,
     AL(a.perm, S); AL(a.rem, S);
     AL(a.x2, S); AL(a.y2, S); AL(a.z2, S); AL(a.size2, S); AL(a.young2, S); AL(a.ctype2, S); AL(a.phase2, S);
     AL(a.perm2, S); AL(a.rem2, S);
-    AL(a.col, S); AL(a.code, S); AL(a.codes, S); AL(a.bin, S); AL(a.tmp, S); AL(a.rank, S); AL(a.hi, S);
+    AL(a.col, S); AL(a.code, S); AL(a.codes, S); AL(a.bin, S); AL(a.grp, S); AL(a.tmp, S); AL(a.rank, S); AL(a.hi, S);
     AL(a.lo, S);
     AL(a.mass, S * s->K.ntypes);
     AL(a.bin_count, B + 1); AL(a.bin_cursor, B + 1); AL(a.bin_start, B + 1); AL(a.bigbins, 2 * (S / 33) + 4);
-    AL(a.fix_count, 8); AL(a.fix_list, S); AL(a.walk_list, S);
+    AL(a.fix_count, 8); AL(a.fix_list, S); AL(a.walk_list, S); AL(a.wl, 2 * (C + 1));
     AL(a.density, S); AL(a.v, S); AL(a.mindist, S); AL(a.fx, S); AL(a.fy, S); AL(a.fz, S); AL(a.nbcount, S);
     AL(a.nbmin, S);
     AL(a.grid, G); AL(a.desc, C + 1); AL(a.frame, C + 1);   // entry C: never active (freed slots)
@@ -720,6 +720,7 @@ extern "C" int tm_session_create(tm_session **out, const tm_session_config *cfg,
     s->mass_types = K.ntypes;
     if (rc == TM_OK) a.work = a.fix_count + 1;
     a.lstride = S;
+    a.wl_stride = C + 1;
     a.vcap = cfg->list_capacity > 0 ? cfg->list_capacity : 0;
     if (rc == TM_OK) {
         if (cudaMallocHost((void **)&s->h_desc, sizeof(tm_desc) * (size_t)C) != cudaSuccess ||
@@ -757,8 +758,8 @@ extern "C" int tm_session_destroy(tm_session *s)
     drop_graphs(s);
     tm_arrays &a = s->A;
     void *ptrs[] = {a.x, a.y, a.z, a.size, a.young, a.ctype, a.phase, a.perm, a.rem, a.x2, a.y2, a.z2, a.size2,
-                    a.young2, a.ctype2, a.phase2, a.perm2, a.rem2, a.col, a.code, a.codes, a.bin, a.tmp, a.rank, a.hi, a.lo, a.vlist, a.vcount, a.x0,
-                    a.mass, a.bin_count, a.bin_cursor, a.bin_start, a.bigbins, a.fix_count, a.fix_list, a.walk_list, a.density, a.v, a.mindist, a.fx,
+                    a.young2, a.ctype2, a.phase2, a.perm2, a.rem2, a.col, a.code, a.codes, a.bin, a.grp, a.tmp, a.rank, a.hi, a.lo, a.vlist, a.vcount, a.x0,
+                    a.mass, a.bin_count, a.bin_cursor, a.bin_start, a.bigbins, a.fix_count, a.fix_list, a.walk_list, a.wl, a.density, a.v, a.mindist, a.fx,
                     a.fy, a.fz, a.nbcount, a.nbmin, a.nbhash, a.vcand, a.grid, a.desc, a.frame, s->scan_tmp, s->scan_tmp_slots, s->d_octsize,
                     s->dK, s->d_scratch, s->d_scratch2, s->d_flag, a.diag_row, a.diag_cnt, a.diag_nb};
     for (void *p : ptrs)
@@ -1737,6 +1738,7 @@ extern "C" int tm_colony_stats(tm_session *s, int id, tm_colony_info *st)
     st->list_rebuilds = (int64_t)f.rebuilds;
     st->codes_slow = (int64_t)f.codes_slow;
     st->density_fp64_cells = (int64_t)f.fix64;
+    st->walked_cells = (int64_t)f.walks;
     memcpy(&st->list_maxdisp, &f.maxdisp, sizeof(float));   // stored as the float's bits
     st->list_skin = s->h_desc[id].skin;
     st->list_age = f.age;

@@ -58,7 +58,7 @@ class _Info(C.Structure):
                 ("grid_size", C.c_int64 * 3), ("device_errors", C.c_uint32), ("bin_level", C.c_int),
                 ("n", C.c_int64), ("list_rebuilds", C.c_int64), ("codes_slow", C.c_int64),
                 ("list_maxdisp", C.c_float), ("list_skin", C.c_float), ("list_age", C.c_int32),
-                ("density_fp64_cells", C.c_int64)]
+                ("density_fp64_cells", C.c_int64), ("walked_cells", C.c_int64)]
 
 
 class _CycleType(C.Structure):
@@ -107,6 +107,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "tm_last_error": (C.c_char_p, []),
         "tm_version": (C.c_char_p, []),
         "tm_device_count": (C.c_int, []),
+        "tm_measure_fp32_peak": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
         "tm_session_create": (C.c_int, [C.POINTER(P), C.POINTER(_Config), C.POINTER(_CellTypes)]),
         "tm_session_destroy": (C.c_int, [P]),
         "tm_session_stream": (P, [P]),
@@ -273,6 +274,13 @@ def host_unregister(a: np.ndarray):
 
 def device_count() -> int:
     return int(load_library().tm_device_count())
+
+
+def measure_fp32_peak(device: int = 0) -> float:
+    """Measured FP32 FMA rate of the device in TFLOP/s."""
+    r = C.c_double(0.0)
+    _check(load_library().tm_measure_fp32_peak(int(device), C.byref(r)))
+    return float(r.value)
 
 
 class Session:
@@ -561,7 +569,7 @@ class Session:
                 "bin_level": int(info.bin_level), "n": int(info.n), "list_rebuilds": int(info.list_rebuilds),
                 "codes_slow": int(info.codes_slow), "list_maxdisp": float(info.list_maxdisp),
                 "list_skin": float(info.list_skin), "list_age": int(info.list_age),
-                "density_fp64_cells": int(info.density_fp64_cells)}
+                "density_fp64_cells": int(info.density_fp64_cells), "walked_cells": int(info.walked_cells)}
 
     def list_rate(self) -> tuple[float, int]:
         """(expected fraction of cells rebuilding their lists per step, rebuilds so far)."""
