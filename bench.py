@@ -51,7 +51,7 @@ B_CELL = 112
 # dram__bytes_write.sum over the cells of the launch), from the ncu capture
 # summarised in profiles/k_plist32_fp32_clustered2m.txt; traffic grows with the
 # cell count, so a launch over n cells moves n times this.
-TRAFFIC_PER_CELL = {"k_plist32": 370.7}
+TRAFFIC_PER_CELL = {"k_plist32": 370.3}
 WORKLOADS = {
     "precision16m": dict(kind="clustered", n=16_000_000, seed=3, precision="fp32c", cic=False, dt=0.01),
     "scale1m": dict(kind="clustered", n=1_000_000, seed=2, precision="fp64", cic=True, dt=0.01),
