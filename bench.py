@@ -780,6 +780,15 @@ def main():
     world, rank, local, pg = dist_setup()
     from timothy_gb300 import session as S
 
+    # the drop-in records first, each in a process of its own, before this
+    # process holds sessions and page-locked buffers of its own
+    dropin = None
+    if world == 1 and not args.no_dropin:
+        dropin = {"1m_cic": dropin_record_process(1_000_000, "clustered", 2, True, 5)}
+        if wl["n"] >= 16_000_000:
+            dropin["16m"] = dropin_record_process(wl["n"], wl["kind"], wl["seed"], False, 3,
+                                                  precision=wl["precision"])
+
     kind, n, seed = wl["kind"], wl["n"], wl["seed"]
     radius = radius_for(kind, n, seed)
     col = C.make_colony(kind, n, seed, radius)
@@ -924,10 +933,8 @@ def main():
 
     if world == 1 and not args.no_scale1m and args.workload == "precision16m":
         detail["scale1m"] = scale1m_record(local, 100, args)
-    if world == 1 and not args.no_dropin:
-        detail["e2e_dropin"] = {"1m_cic": dropin_record_process(1_000_000, "clustered", 2, True, 5)}
-        if n >= 16_000_000:
-            detail["e2e_dropin"]["16m"] = dropin_record_process(n, kind, seed, False, 3, precision=prec)
+    if dropin is not None:
+        detail["e2e_dropin"] = dropin
 
     if not args.no_forms and world == 1:
         detail["rows"] = {"grid_to_cell": field_rows(local, peak), "cic_deposit": cic_rows(local, peak),

@@ -116,6 +116,7 @@ typedef struct {
     int32_t list_age;                 /* steps since the lists were built */
     int64_t density_fp64_cells;       /* FP32 path: cells of the last step whose density was redone in FP64 */
     int64_t walked_cells;             /* cells of the last step whose v (or mindist) took the octree walk */
+    int64_t walked_isolated_cells;    /* those of them without a neighbour within h (mindist from the walk) */
 } tm_colony_info;
 
 const char *tm_last_error(void);

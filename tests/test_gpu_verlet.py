@@ -180,8 +180,10 @@ def test_list_overflow_falls_back_to_search(oracle_lib, precision):
 def test_fp32_lists_walk_skip_keeps_v(kind, n, seed, dim):
     """The list pass settles v = 0 without the octree walk when a list entry
     inside the query box precedes the first within-h neighbour in Morton
-    order.  Diagnostics walk every cell; v must not change bit for bit, over
-    steps with and without list rebuilds."""
+    order, and a cell without neighbours within h takes its mindist from its
+    list when the nearest entry is a candidate within the list's sure radius.
+    Diagnostics walk every cell; v and mindist must not change bit for bit,
+    over steps with and without list rebuilds."""
     from timothy_gb300 import session as S
 
     col = C.make_colony(kind, n, seed, C.initial_radius(kind, n, dim=dim), dim=dim)
@@ -193,6 +195,7 @@ def test_fp32_lists_walk_skip_keeps_v(kind, n, seed, dim):
         assert np.array_equal(a[k], b[k]), k
     assert sb["walked_cells"] == col.n
     assert sa["walked_cells"] < sb["walked_cells"]
+    assert sa["walked_isolated_cells"] <= sb["walked_isolated_cells"]
     assert 1 <= sa["list_rebuilds"] < 6
 
 

@@ -53,7 +53,7 @@ struct tm_arrays {
     float4 *hi, *lo;     // FP32 split positions (hi.w = size)
     double *mass;        // FP64 density weights sc_t * (size / csize_t), [type][slot]
     // bin table
-    uint32_t *bin_count, *bin_cursor, *bin_start;
+    uint32_t *bin_count, *bin_start;   // bin_count: occupancy, then the scatter's cursor
     long long nbin_total;
     int *bigbins;
     int *fix_count;      // cells whose FP32 density is redone in FP64
@@ -123,7 +123,10 @@ __device__ __forceinline__ void tm_queue_walk(const tm_arrays &a, int c, long lo
     const unsigned mf = __ballot_sync(am, walk && !isolated), mb = __ballot_sync(am, walk && isolated);
     const int lane = threadIdx.x & 31;
     const unsigned below = (1u << lane) - 1u;
-    if ((mf | mb) && lane == __ffs(mf | mb) - 1) atomicAdd(&a.frame[c].walks, (unsigned long long)__popc(mf | mb));
+    if ((mf | mb) && lane == __ffs(mf | mb) - 1) {
+        atomicAdd(&a.frame[c].walks, (unsigned long long)__popc(mf | mb));
+        if (mb) atomicAdd(&a.frame[c].walks_isolated, (unsigned long long)__popc(mb));
+    }
     if (mf) {
         const int leader = __ffs(mf) - 1;
         int base = 0;
@@ -152,7 +155,10 @@ __device__ __forceinline__ void tm_queue_walk_owned(const tm_arrays &a, int c, l
     const unsigned mf = __ballot_sync(am, wf), mb = __ballot_sync(am, wb);
     const int lane = threadIdx.x & 31;
     const unsigned below = (1u << lane) - 1u;
-    if ((mf | mb) && lane == __ffs(mf | mb) - 1) atomicAdd(&a.frame[c].walks, (unsigned long long)__popc(mf | mb));
+    if ((mf | mb) && lane == __ffs(mf | mb) - 1) {
+        atomicAdd(&a.frame[c].walks, (unsigned long long)__popc(mf | mb));
+        if (mb) atomicAdd(&a.frame[c].walks_isolated, (unsigned long long)__popc(mb));
+    }
     if (mf) {
         const int leader = __ffs(mf) - 1;
         int base = 0;

@@ -32,6 +32,7 @@ __global__ void k_step_init(tm_arrays a)
     f.codes_slow = 0;
     f.fix64 = 0;
     f.walks = 0;
+    f.walks_isolated = 0;
     // Neighbour lists stay valid while no pair can have come from beyond
     // h + skin to within h: every cell moved less than skin/2 since the lists
     // were built (maxdisp carries a float-rounding margin).
@@ -49,6 +50,7 @@ __global__ void k_step_init(tm_arrays a)
     }
     if (rb && d.active && d.n > 1 && !d.verlet) atomicAdd(&a.work[0], 1);   // colonies the search pass serves
     f.force_rebuild = 0;
+    f.disp = rb ? 0u : f.maxdisp;
     f.maxdisp = 0u;
     for (int k = 0; k < 3; k++) {
         f.patch_lo[k] = 2147483647ll;
@@ -284,8 +286,9 @@ __global__ void k_codes(tm_arrays a)
 }
 
 // Group each colony's live slots by bin (grp holds the slots of bin b at the
-// bin's Morton positions, in no particular order); the first slot to reach a
-// bin of more than 32 cells queues it for k_binsort_big.
+// bin's Morton positions, in no particular order): the count k_codes left in
+// bin_count is taken down as the cursor, and the slot that takes the last
+// place of a bin of more than 32 cells queues it for k_binsort_big.
 __global__ void k_scatter(tm_arrays a)
 {
     long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -294,7 +297,7 @@ __global__ void k_scatter(tm_arrays a)
     const tm_desc &d = a.desc[c];
     if (!d.active || !tm_live(s, d)) return;
     const uint32_t b = a.bin[s];
-    const uint32_t k = atomicAdd(&a.bin_cursor[b], 1u);
+    const uint32_t k = atomicSub(&a.bin_count[b], 1u) - 1u;
     const uint32_t b0 = a.bin_start[b];
     a.grp[a.frame[c].bin_base + b0 + k] = (int)s;
     if (k == 0 && a.bin_start[b + 1] - b0 > 32) {

@@ -78,12 +78,14 @@ struct tm_frame {
     int force_rebuild;       // set by uploads
     int ident;               // 1: slots are in this step's Morton order
     unsigned maxdisp;        // float bits of max |x - x_build| after the last update
+    unsigned disp;           // the same for the positions this step evaluates (0 on rebuild steps)
     unsigned long long rebuilds;     // rebuild steps so far (diagnostic)
     unsigned long long step_counter;
     long long patch_lo[3];   // CIC patch corners (patches.c:61-132); INT_MAX/INT_MIN when empty
     long long patch_hi[3];
     unsigned long long fix64;        // FP32 cells whose density this step was redone in FP64 (diagnostic)
     unsigned long long walks;        // cells of this step that took the octree walk (diagnostic)
+    unsigned long long walks_isolated;   // those of them without a neighbour within h
 };
 
 // ---------------------------------------------------------------------------

@@ -118,8 +118,50 @@ struct walk_state {
     const uint32_t *bst;            // the colony's bin starts
 };
 
+// distance of p to the cell in slot j as the walk takes it for mindist: FP64
+// on the plain path, from the split positions (FP32) on the compensated one
+__device__ __forceinline__ double walk_dist(const tm_arrays &a, bool fp64, long long p, long long j)
+{
+    if (fp64) {
+        const double dx = sub64(a.x[p], a.x[j]), dy = sub64(a.y[p], a.y[j]), dz = sub64(a.z[p], a.z[j]);
+        return __dsqrt_rn(add64(add64(mul64(dx, dx), mul64(dy, dy)), mul64(dz, dz)));
+    }
+    return (double)sqrtf(dist2_split(a, p, j));   // FP32 path: no FP64 work
+}
+
+// An isolated cell (no neighbour within h) walks for its mindist, the least
+// distance over the walk's candidates.  With neighbour lists in use its list
+// holds every cell nearer than R = h + skin - 2 max displacement since the
+// build: when the nearest entry is nearer than R and its lattice code lies in
+// the query box (so its leaf meets the box and it is a candidate), no
+// candidate is nearer and its distance is mindist; v = 0 (no candidate is
+// within h).  True with w.mind set; the walk is then not needed.
+__device__ __forceinline__ bool isolated_from_list(const tm_arrays &a, const tm_desc &d, const tm_frame &f,
+                                                   const tm_type &T, walk_state &w)
+{
+    const long long p = w.p;
+    const float R = (T.hf + d.skin - 2.0f * __uint_as_float(f.disp) - 2e-3f) * (1.0f - 1e-5f);
+    const int cnt = a.vcount[p];
+    double best = 1.7976931348623157e308;
+    bool cand = false;
+    for (int k = 0; k < cnt; k++) {
+        const long long j = a.vlist[(long long)k * a.lstride + p];
+        const double dist = walk_dist(a, w.fp64, p, j);
+        if (dist > best) continue;
+        const uint4 cj = a.codes[w.ident ? j : (long long)a.rank[j]];
+        const bool in = cj.x >= w.bmin[0] && cj.x < w.bmax[0] && cj.y >= w.bmin[1] && cj.y < w.bmax[1] &&
+                        cj.z >= w.bmin[2] && cj.z < w.bmax[2];
+        cand = dist < best ? in : (cand || in);
+        best = dist;
+    }
+    if (!cand || !(best < (double)R)) return false;
+    w.mind = best;
+    return true;
+}
+
 // octlocateregion and the first stack frame; false when there is nothing to
-// walk (fewer than two cells in the start node)
+// walk (fewer than two cells in the start node, or an isolated cell settled
+// from its list)
 __device__ __forceinline__ bool walk_begin(const tm_arrays &a, const tm_consts *K, long long p, walk_state &w,
                                            walk_frame *stk)
 {
@@ -150,6 +192,7 @@ __device__ __forceinline__ bool walk_begin(const tm_arrays &a, const tm_consts *
         }
         if (slow) atomicAdd(&a.frame[c].codes_slow, (unsigned long long)slow);
     }
+    if (w.isolated && !a.want_diag && d.verlet && f.list_ok && isolated_from_list(a, d, f, T, w)) return false;
 
     // octlocateregion: the highest differing bit over the three axes
     const uint32_t diff = (w.bmin[0] ^ w.bmax[0]) | (w.bmin[1] ^ w.bmax[1]) | (w.bmin[2] ^ w.bmax[2]);
@@ -249,13 +292,7 @@ __device__ __forceinline__ bool walk_step(const tm_arrays &a, walk_state &w, wal
         if (w.jstar < 0) w.jstar = k;
         if (!w.isolated) return true;
         const long long sk = w.ident ? (long long)k : (long long)a.tmp[k];
-        double dist;
-        if (w.fp64) {
-            const double dx = sub64(a.x[w.p], a.x[sk]), dy = sub64(a.y[w.p], a.y[sk]), dz = sub64(a.z[w.p], a.z[sk]);
-            dist = __dsqrt_rn(add64(add64(mul64(dx, dx), mul64(dy, dy)), mul64(dz, dz)));
-        } else {
-            dist = (double)sqrtf(dist2_split(a, w.p, sk));   // FP32 path: no FP64 work
-        }
+        const double dist = walk_dist(a, w.fp64, w.p, sk);
         w.mind = (dist < w.mind ? dist : w.mind);
         return false;
     }

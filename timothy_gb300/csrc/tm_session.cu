@@ -419,7 +419,6 @@ static int enqueue_build(tm_session *s, int p, int &nk)
     const long long nbin = s->bins.hwm;
     const int ncol = a.ncol;
     CK(cudaMemsetAsync(a.bin_count, 0, (size_t)(nbin + 1) * sizeof(uint32_t), st));
-    CK(cudaMemsetAsync(a.bin_cursor, 0, (size_t)(nbin + 1) * sizeof(uint32_t), st));
     CK(cudaMemsetAsync(a.bigbins, 0, sizeof(int), st));
     CK(cudaMemsetAsync(a.fix_count, 0, 6 * sizeof(int), st));   // fix count and the five work counters
     if (a.diag_cnt) CK(cudaMemsetAsync(a.diag_cnt, 0, (size_t)s->diag_ncells * sizeof(int), st));
@@ -590,7 +589,7 @@ static int session_buffers(tm_session *s, long long S, long long B, long long G,
     AL(a.col, S); AL(a.code, S); AL(a.codes, S); AL(a.bin, S); AL(a.grp, S); AL(a.tmp, S); AL(a.rank, S); AL(a.hi, S);
     AL(a.lo, S);
     AL(a.mass, S * s->K.ntypes);
-    AL(a.bin_count, B + 1); AL(a.bin_cursor, B + 1); AL(a.bin_start, B + 1); AL(a.bigbins, 2 * (S / 33) + 4);
+    AL(a.bin_count, B + 1); AL(a.bin_start, B + 1); AL(a.bigbins, 2 * (S / 33) + 4);
     AL(a.fix_count, 8); AL(a.fix_list, S); AL(a.walk_list, S); AL(a.wl, 2 * (C + 1));
     AL(a.density, S); AL(a.v, S); AL(a.mindist, S); AL(a.fx, S); AL(a.fy, S); AL(a.fz, S); AL(a.nbcount, S);
     AL(a.nbmin, S);
@@ -759,7 +758,7 @@ extern "C" int tm_session_destroy(tm_session *s)
     tm_arrays &a = s->A;
     void *ptrs[] = {a.x, a.y, a.z, a.size, a.young, a.ctype, a.phase, a.perm, a.rem, a.x2, a.y2, a.z2, a.size2,
                     a.young2, a.ctype2, a.phase2, a.perm2, a.rem2, a.col, a.code, a.codes, a.bin, a.grp, a.tmp, a.rank, a.hi, a.lo, a.vlist, a.vcount, a.x0,
-                    a.mass, a.bin_count, a.bin_cursor, a.bin_start, a.bigbins, a.fix_count, a.fix_list, a.walk_list, a.wl, a.density, a.v, a.mindist, a.fx,
+                    a.mass, a.bin_count, a.bin_start, a.bigbins, a.fix_count, a.fix_list, a.walk_list, a.wl, a.density, a.v, a.mindist, a.fx,
                     a.fy, a.fz, a.nbcount, a.nbmin, a.nbhash, a.vcand, a.grid, a.desc, a.frame, s->scan_tmp, s->scan_tmp_slots, s->d_octsize,
                     s->dK, s->d_scratch, s->d_scratch2, s->d_flag, a.diag_row, a.diag_cnt, a.diag_nb};
     for (void *p : ptrs)
@@ -1739,6 +1738,7 @@ extern "C" int tm_colony_stats(tm_session *s, int id, tm_colony_info *st)
     st->codes_slow = (int64_t)f.codes_slow;
     st->density_fp64_cells = (int64_t)f.fix64;
     st->walked_cells = (int64_t)f.walks;
+    st->walked_isolated_cells = (int64_t)f.walks_isolated;
     memcpy(&st->list_maxdisp, &f.maxdisp, sizeof(float));   // stored as the float's bits
     st->list_skin = s->h_desc[id].skin;
     st->list_age = f.age;

@@ -58,7 +58,8 @@ class _Info(C.Structure):
                 ("grid_size", C.c_int64 * 3), ("device_errors", C.c_uint32), ("bin_level", C.c_int),
                 ("n", C.c_int64), ("list_rebuilds", C.c_int64), ("codes_slow", C.c_int64),
                 ("list_maxdisp", C.c_float), ("list_skin", C.c_float), ("list_age", C.c_int32),
-                ("density_fp64_cells", C.c_int64), ("walked_cells", C.c_int64)]
+                ("density_fp64_cells", C.c_int64), ("walked_cells", C.c_int64),
+                ("walked_isolated_cells", C.c_int64)]
 
 
 class _CycleType(C.Structure):
@@ -569,7 +570,8 @@ class Session:
                 "bin_level": int(info.bin_level), "n": int(info.n), "list_rebuilds": int(info.list_rebuilds),
                 "codes_slow": int(info.codes_slow), "list_maxdisp": float(info.list_maxdisp),
                 "list_skin": float(info.list_skin), "list_age": int(info.list_age),
-                "density_fp64_cells": int(info.density_fp64_cells), "walked_cells": int(info.walked_cells)}
+                "density_fp64_cells": int(info.density_fp64_cells), "walked_cells": int(info.walked_cells),
+                "walked_isolated_cells": int(info.walked_isolated_cells)}
 
     def list_rate(self) -> tuple[float, int]:
         """(expected fraction of cells rebuilding their lists per step, rebuilds so far)."""
