@@ -234,6 +234,7 @@ __global__ void k_frame(tm_arrays a, const tm_consts *K)
     f.L = L;
     f.nbins = 1u << (3 * L);
     f.binscale = (float)((double)(1 << L) / sc);
+    f.units2 = (float)(sc * 3.7252902984619141e-9);
     // integer lattice path: cmul = 2^(78-ck)/scale in [2^62, 2^63)
     int es = 0;
     frexp(sc, &es);                       // sc in [2^(es-1), 2^es)

@@ -58,6 +58,7 @@ struct tm_frame {
     uint32_t nbins;      // 8^L
     float shiftf[3];     // FP32 copies for culling
     float binscale;      // 2^L / scale
+    float units2;        // two lattice units, 2 scale / 2^29 (the list pass's box margin)
     int n;               // cells in this colony
     uint32_t error;      // TM_ERR_* bits
     unsigned long long removecount;
@@ -277,6 +278,30 @@ __device__ __forceinline__ uint32_t tm_lattice_fast(double x, long long Xfx, boo
     if (ok) return c;
     slow++;
     return off == 0.0 ? tm_lattice(x, f.shift[k], f.scale) : tm_lattice_off(x, off, f.shift[k], f.scale);
+}
+
+// float -> double, exact, with integer operations only: on this part a
+// conversion issues on the FP64 pipe, which runs at a small fraction of the
+// FP32 rate; the octree walk, a chain of dependent steps, converts its FP32
+// distances this way.  (The list pass keeps the hardware conversion: there
+// the dozen integer instructions cost more than the pipe time, measured.)
+// The fields are moved into the binary64 layout (exponent rebiased by
+// 1023 - 127); subnormal floats are normalised; infinities and NaNs keep
+// their payload bits.
+__device__ __forceinline__ double tm_f2d(float f)
+{
+    const uint32_t u = __float_as_uint(f);
+    const unsigned long long sgn = (unsigned long long)(u & 0x80000000u) << 32;
+    const uint32_t e = (u >> 23) & 0xffu;
+    const unsigned long long m = u & 0x7fffffu;
+    if (e == 0u) {
+        if (m == 0ull) return __longlong_as_double((long long)sgn);
+        const int p = 31 - __clz((int)m);                       // leading one of m, value m * 2^-149
+        const unsigned long long mant = (m << (52 - p)) & 0xfffffffffffffull;
+        return __longlong_as_double((long long)(sgn | ((unsigned long long)(p + 874) << 52) | mant));
+    }
+    const unsigned long long ex = e == 255u ? 2047ull : (unsigned long long)e + 896ull;
+    return __longlong_as_double((long long)(sgn | (ex << 52) | (m << 29)));
 }
 
 // Split a double into hi (x truncated to 24 significant bits) + lo (float of

@@ -126,7 +126,7 @@ __device__ __forceinline__ double walk_dist(const tm_arrays &a, bool fp64, long 
         const double dx = sub64(a.x[p], a.x[j]), dy = sub64(a.y[p], a.y[j]), dz = sub64(a.z[p], a.z[j]);
         return __dsqrt_rn(add64(add64(mul64(dx, dx), mul64(dy, dy)), mul64(dz, dz)));
     }
-    return (double)sqrtf(dist2_split(a, p, j));   // FP32 path: no FP64 work
+    return tm_f2d(sqrtf(dist2_split(a, p, j)));   // FP32 path: no FP64 work
 }
 
 // An isolated cell (no neighbour within h) walks for its mindist, the least
@@ -329,8 +329,8 @@ __device__ __forceinline__ void walk_end(const tm_arrays &a, const tm_consts *K,
                 in = __dsqrt_rn(add64(add64(mul64(dx, dx), mul64(dy, dy)), mul64(dz, dz))) <= T.h;
             }
             if (in)
-                vv = (double)pair_potential32(dist, (float)a.size[p], a.young[p], (float)a.size[jstar],
-                                              a.young[jstar]);
+                vv = tm_f2d(pair_potential32(dist, (float)a.size[p], a.young[p], (float)a.size[jstar],
+                                             a.young[jstar]));
         }
     }
     a.v[p] = vv;

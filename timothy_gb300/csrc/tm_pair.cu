@@ -799,7 +799,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_plist32(tm_arrays a, const tm_c
     const float4 *__restrict__ hi = a.hi;
     const float4 *__restrict__ lo = a.lo;
     // query-box half width with the margin (a lattice unit is scale / 2^29)
-    const float hbox = T.hf * (1.0f - 1e-4f) - (float)f.scale * 3.7252903e-9f;
+    const float hbox = T.hf * (1.0f - 1e-4f) - f.units2;
     pair_acc<1> acc;
     acc.init();
     int cnt_nb = 0;
