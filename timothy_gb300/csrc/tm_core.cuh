@@ -41,6 +41,7 @@ struct tm_type {
     float hf, h2f, inv_hf, cWf, cGf, kmassf;   // kmassf = sc / csize
     float thr_lo, thr_hi;                      // squared-distance band around h^2
     double inv_h, kmass;                       // 1 / h and sc / csize for the FP32 path's FP64 re-do
+    double h2cut;                              // largest double d2 with sqrt(d2) <= h (the FP64 cutoff)
 };
 
 struct tm_consts {

@@ -39,8 +39,8 @@ struct pair_acc;
 
 template <>
 struct pair_acc<0> {
-    double dens, mind, fx, fy, fz;
-    __device__ void init() { dens = 0.0; mind = 1.7976931348623157e308; fx = fy = fz = 0.0; }
+    double dens, mind2, fx, fy, fz;   // mind2: least squared distance
+    __device__ void init() { dens = 0.0; mind2 = 1.7976931348623157e308; fx = fy = fz = 0.0; }
 };
 
 template <>
@@ -50,17 +50,30 @@ struct pair_acc<1> {
     __device__ void init() { dens.init(); fx.init(); fy.init(); fz.init(); mins = 3.0e38f; err2 = 0.0f; }
 };
 
-// Exact FP64 pair of potential.c:39-78 / inline.h:40-83 (density and force
-// parts; v comes from the octree walk).  Returns the distance.
-__device__ __forceinline__ double pair64(const tm_type &T, int dim, double xi, double yi, double zi, double xj,
-                                         double yj, double zj, double mj, pair_acc<0> &acc, bool &in)
+// FP64 pair of potential.c:39-78 / inline.h:40-83 (density and force parts;
+// v comes from the octree walk).  The squared distance has the reference's
+// association and roundings, and the cutoff is decided on it exactly:
+// sqrt(d2) <= h (the reference's test, with a correctly rounded square root,
+// which is monotone) holds exactly for d2 <= h2cut, the largest double whose
+// square root rounds to h or below (formed on the host), so entries beyond h
+// take no square root, and the least distance is the square root of the
+// least d2.  Within h the reference's expressions follow in FP64 with
+// separate roundings, but for u = dist * (1/h) and the force's division by
+// dist taken as one correctly rounded reciprocal: a few ulps from the
+// reference's quotients against the path's 1e-12 bound (divisions are a
+// software sequence on this part's slow FP64 pipe; measured at 16 M cells
+// the list pass went from about 140 to 104 ms; a reciprocal square root for
+// both dist and 1/dist was slower, 110 ms).
+__device__ __forceinline__ void pair64(const tm_type &T, int dim, double xi, double yi, double zi, double xj,
+                                       double yj, double zj, double mj, pair_acc<0> &acc, bool &in)
 {
     const double dx = sub64(xi, xj), dy = sub64(yi, yj), dz = sub64(zi, zj);
-    const double dist = __dsqrt_rn(add64(add64(mul64(dx, dx), mul64(dy, dy)), mul64(dz, dz)));
-    acc.mind = (dist < acc.mind ? dist : acc.mind);
-    in = dist <= T.h;
+    const double d2 = add64(add64(mul64(dx, dx), mul64(dy, dy)), mul64(dz, dz));
+    acc.mind2 = (d2 < acc.mind2 ? d2 : acc.mind2);
+    in = d2 <= T.h2cut;
     if (in) {
-        const double u = div64(dist, T.h);
+        const double dist = __dsqrt_rn(d2);
+        const double u = mul64(dist, T.inv_h);
         const double omu = sub64(1.0, u);
         double wk, wg;
         if (u <= 0.5) {
@@ -73,11 +86,11 @@ __device__ __forceinline__ double pair64(const tm_type &T, int dim, double xi, d
         }
         acc.dens = add64(acc.dens, mul64(mj, (double)__double2float_rn(wk)));
         const double wc = mul64(wg, T.cG);
-        acc.fx = add64(acc.fx, div64(mul64(wc, sub64(xj, xi)), dist));
-        acc.fy = add64(acc.fy, div64(mul64(wc, sub64(yj, yi)), dist));
-        if (dim == 3) acc.fz = add64(acc.fz, div64(mul64(wc, sub64(zj, zi)), dist));
+        const double rd = __drcp_rn(dist);
+        acc.fx = add64(acc.fx, mul64(mul64(wc, sub64(xj, xi)), rd));
+        acc.fy = add64(acc.fy, mul64(mul64(wc, sub64(yj, yi)), rd));
+        if (dim == 3) acc.fz = add64(acc.fz, mul64(mul64(wc, sub64(zj, zi)), rd));
     }
-    return dist;
 }
 
 // FP32 cutoff decision for squared distance s: FP64 only in the band
@@ -217,7 +230,7 @@ __device__ __forceinline__ void pair_store(const tm_arrays &a, long long i, pair
 {
     if constexpr (PREC == 0) {
         a.density[i] = acc.dens;
-        a.mindist[i] = acc.mind;
+        a.mindist[i] = acc.mind2 < 1.7976931348623157e308 ? __dsqrt_rn(acc.mind2) : 1.7976931348623157e308;
         a.fx[i] = acc.fx;
         a.fy[i] = acc.fy;
         a.fz[i] = acc.fz;
@@ -350,8 +363,8 @@ __device__ __forceinline__ void pair_group(const tm_arrays &a, const tm_consts *
             const int j = __float_as_int(A.w);
             if constexpr (PREC == 0) {
                 bool in;
-                const double dist = pair64(T, dim, xi, yi, zi, a.x[j], a.y[j], a.z[j],
-                                           a.mass[(long long)t * a.nslots_total + j], acc, in);
+                pair64(T, dim, xi, yi, zi, a.x[j], a.y[j], a.z[j], a.mass[(long long)t * a.nslots_total + j], acc,
+                       in);
                 if (in) {
                     cnt_nb++;
                     nbmin = min(nbmin, j);
@@ -494,8 +507,8 @@ __device__ __forceinline__ void pair_group(const tm_arrays &a, const tm_consts *
             acc.fx = add64(acc.fx, __shfl_xor_sync(FULL, acc.fx, o));
             acc.fy = add64(acc.fy, __shfl_xor_sync(FULL, acc.fy, o));
             acc.fz = add64(acc.fz, __shfl_xor_sync(FULL, acc.fz, o));
-            const double om = __shfl_xor_sync(FULL, acc.mind, o);
-            acc.mind = om < acc.mind ? om : acc.mind;
+            const double om = __shfl_xor_sync(FULL, acc.mind2, o);
+            acc.mind2 = om < acc.mind2 ? om : acc.mind2;
         } else {
             acc.dens.merge(__shfl_xor_sync(FULL, acc.dens.s, o), __shfl_xor_sync(FULL, acc.dens.c, o));
             acc.fx.merge(__shfl_xor_sync(FULL, acc.fx.s, o), __shfl_xor_sync(FULL, acc.fx.c, o));

@@ -559,6 +559,20 @@ static int dalloc(T **p, long long count)
     return TM_OK;
 }
 
+// the largest double d2 with sqrt(d2) <= h: the square root is correctly
+// rounded and monotone, so sqrt(d2) <= h exactly when d2 <= this bound
+static double cutoff_sq(double h)
+{
+    double x = h * h;
+    while (x > 0.0 && std::sqrt(x) > h) x = std::nextafter(x, 0.0);
+    for (;;) {
+        const double y = std::nextafter(x, HUGE_VAL);
+        if (!(std::sqrt(y) <= h)) break;
+        x = y;
+    }
+    return x;
+}
+
 static double host_type_const(int dim, int which, double h, double h2, double h3, double h4)
 {
     // the reference's own expressions (inline.h:45-46, 71-72)
@@ -691,6 +705,7 @@ extern "C" int tm_session_create(tm_session **out, const tm_session_config *cfg,
         T.cGf = (float)T.cG;
         T.kmassf = (float)(T.sc / T.csize);
         T.inv_h = 1.0 / T.h;
+        T.h2cut = cutoff_sq(T.h);
         T.kmass = T.sc / T.csize;
         T.thr_lo = (float)(T.h * (1.0 - 1e-5) * T.h * (1.0 - 1e-5));
         T.thr_hi = (float)(T.h * (1.0 + 1e-5) * T.h * (1.0 + 1e-5));
@@ -1899,6 +1914,7 @@ extern "C" int tmi_set_types(tm_session *s, const tm_celltypes *types)
         T.cGf = (float)T.cG;
         T.kmassf = (float)(T.sc / T.csize);
         T.inv_h = 1.0 / T.h;
+        T.h2cut = cutoff_sq(T.h);
         T.kmass = T.sc / T.csize;
         T.thr_lo = (float)(T.h * (1.0 - 1e-5) * T.h * (1.0 - 1e-5));
         T.thr_hi = (float)(T.h * (1.0 + 1e-5) * T.h * (1.0 + 1e-5));
