@@ -126,6 +126,13 @@ int tm_device_count(void);
  * per thread on every SM, best of two timed launches): the compute
  * denominator of the list pass's roofline. */
 int tm_measure_fp32_peak(int device, double *tflops);
+/* Self-check of the arithmetic the kernels form themselves: on n
+ * pseudo-random inputs each, mismatches[0] counts quotients a / b formed from
+ * RN(1/b) by an FMA correction that differ from the correctly rounded
+ * division, mismatches[1] integer double -> float roundings that differ from
+ * the hardware conversion, mismatches[2] integer float -> double conversions
+ * that do.  All three must be 0. */
+int tm_check_numerics(int device, int64_t n, uint64_t seed, int64_t *mismatches);
 
 int tm_session_create(tm_session **out, const tm_session_config *cfg, const tm_celltypes *types);
 int tm_session_destroy(tm_session *s);

@@ -305,6 +305,34 @@ __device__ __forceinline__ double tm_f2d(float f)
     return __longlong_as_double((long long)(sgn | (ex << 52) | (m << 29)));
 }
 
+// a / b rounded to nearest, given y = RN(1 / b): q = RN(a y) is within an
+// ulp of a / b, so the remainder a - b q is exact in one FMA, and
+// RN(q + (a - b q) y) is the correctly rounded quotient (Markstein's
+// correction, the division by an FMA-based reciprocal).  Three FP64
+// operations instead of a division's software sequence; the result is the
+// reference's own u = dist / h, so the kernel value rounds to the same float.
+__device__ __forceinline__ double div_by_recip(double a, double b, double y)
+{
+    const double q = __dmul_rn(a, y);
+    const double r = __fma_rn(-q, b, a);
+    return __fma_rn(r, y, q);
+}
+
+// (double)(float)w, round to nearest even, with integer operations for a w
+// whose float is normal (the hardware conversions otherwise): the 29 low
+// mantissa bits are dropped with the round-half-even carry, which runs into
+// the exponent field as it should.
+__device__ __forceinline__ double tm_round_to_float(double w)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(w);
+    const int e = (int)((b >> 52) & 0x7ff);
+    if (e < 1023 - 126 || e > 1023 + 126) return (double)__double2float_rn(w);
+    const unsigned long long low = b & 0x1fffffffull, half = 0x10000000ull;
+    unsigned long long r = b & ~0x1fffffffull;
+    if (low > half || (low == half && (b & 0x20000000ull))) r += 0x20000000ull;
+    return __longlong_as_double((long long)r);
+}
+
 // Split a double into hi (x truncated to 24 significant bits) + lo (float of
 // the remainder) with integer operations only, so no FP64 instruction runs.
 // |x| < 2^-70 flushes to zero; |x| must stay below 2^100.

@@ -39,8 +39,9 @@ struct pair_acc;
 
 template <>
 struct pair_acc<0> {
-    double dens, mind2, fx, fy, fz;   // mind2: least squared distance
-    __device__ void init() { dens = 0.0; mind2 = 1.7976931348623157e308; fx = fy = fz = 0.0; }
+    double dens, fx, fy, fz;
+    unsigned long long mind2;         // least squared distance (its bits: non-negative doubles order as integers)
+    __device__ void init() { dens = 0.0; mind2 = 0x7fefffffffffffffull; fx = fy = fz = 0.0; }
 };
 
 template <>
@@ -58,25 +59,31 @@ struct pair_acc<1> {
 // square root rounds to h or below (formed on the host), so entries beyond h
 // take no square root, and the least distance is the square root of the
 // least d2.  Within h the reference's expressions follow in FP64 with
-// separate roundings, but for u = dist * (1/h) and the force's division by
-// dist taken as one correctly rounded reciprocal: a few ulps from the
+// separate roundings: dist is the correctly rounded square root and u =
+// dist / h the correctly rounded quotient (div_by_recip), so the kernel
+// value, rounded to float as the reference does, is the reference's bit for
+// bit (a one-ulp change of u could round it to the neighbouring float, 6e-8
+// of the term).  Only the force's three divisions by dist are taken as
+// products with one correctly rounded reciprocal, a few ulps from the
 // reference's quotients against the path's 1e-12 bound (divisions are a
-// software sequence on this part's slow FP64 pipe; measured at 16 M cells
-// the list pass went from about 140 to 104 ms; a reciprocal square root for
-// both dist and 1/dist was slower, 110 ms).
+// software sequence on this part's slow FP64 pipe).  The comparisons of non-negative
+// values run on their bit patterns, the rounding of the kernel value to float
+// with integer operations (tm_round_to_float), and x_j - x_i is the negated
+// x_i - x_j (exact), so the FP64 pipe does only the arithmetic.
 __device__ __forceinline__ void pair64(const tm_type &T, int dim, double xi, double yi, double zi, double xj,
                                        double yj, double zj, double mj, pair_acc<0> &acc, bool &in)
 {
     const double dx = sub64(xi, xj), dy = sub64(yi, yj), dz = sub64(zi, zj);
     const double d2 = add64(add64(mul64(dx, dx), mul64(dy, dy)), mul64(dz, dz));
-    acc.mind2 = (d2 < acc.mind2 ? d2 : acc.mind2);
-    in = d2 <= T.h2cut;
+    const unsigned long long b2 = (unsigned long long)__double_as_longlong(d2);
+    acc.mind2 = b2 < acc.mind2 ? b2 : acc.mind2;
+    in = b2 <= (unsigned long long)__double_as_longlong(T.h2cut);
     if (in) {
         const double dist = __dsqrt_rn(d2);
-        const double u = mul64(dist, T.inv_h);
+        const double u = div_by_recip(dist, T.h, T.inv_h);
         const double omu = sub64(1.0, u);
         double wk, wg;
-        if (u <= 0.5) {
+        if ((unsigned long long)__double_as_longlong(u) <= 0x3fe0000000000000ull) {   // u <= 0.5
             const double six_uu = mul64(mul64(6.0, u), u);
             wk = mul64(T.cW, add64(sub64(1.0, six_uu), mul64(six_uu, u)));
             wg = add64(mul64(-2.0, u), mul64(mul64(3.0, u), u));
@@ -84,12 +91,12 @@ __device__ __forceinline__ void pair64(const tm_type &T, int dim, double xi, dou
             wk = mul64(T.cW, mul64(mul64(mul64(2.0, omu), omu), omu));
             wg = mul64(-omu, omu);
         }
-        acc.dens = add64(acc.dens, mul64(mj, (double)__double2float_rn(wk)));
+        acc.dens = add64(acc.dens, mul64(mj, tm_round_to_float(wk)));
         const double wc = mul64(wg, T.cG);
         const double rd = __drcp_rn(dist);
-        acc.fx = add64(acc.fx, mul64(mul64(wc, sub64(xj, xi)), rd));
-        acc.fy = add64(acc.fy, mul64(mul64(wc, sub64(yj, yi)), rd));
-        if (dim == 3) acc.fz = add64(acc.fz, mul64(mul64(wc, sub64(zj, zi)), rd));
+        acc.fx = add64(acc.fx, mul64(mul64(wc, -dx), rd));
+        acc.fy = add64(acc.fy, mul64(mul64(wc, -dy), rd));
+        if (dim == 3) acc.fz = add64(acc.fz, mul64(mul64(wc, -dz), rd));
     }
 }
 
@@ -230,7 +237,8 @@ __device__ __forceinline__ void pair_store(const tm_arrays &a, long long i, pair
 {
     if constexpr (PREC == 0) {
         a.density[i] = acc.dens;
-        a.mindist[i] = acc.mind2 < 1.7976931348623157e308 ? __dsqrt_rn(acc.mind2) : 1.7976931348623157e308;
+        a.mindist[i] = acc.mind2 < 0x7fefffffffffffffull ? __dsqrt_rn(__longlong_as_double((long long)acc.mind2))
+                                                          : 1.7976931348623157e308;
         a.fx[i] = acc.fx;
         a.fy[i] = acc.fy;
         a.fz[i] = acc.fz;
@@ -507,7 +515,7 @@ __device__ __forceinline__ void pair_group(const tm_arrays &a, const tm_consts *
             acc.fx = add64(acc.fx, __shfl_xor_sync(FULL, acc.fx, o));
             acc.fy = add64(acc.fy, __shfl_xor_sync(FULL, acc.fy, o));
             acc.fz = add64(acc.fz, __shfl_xor_sync(FULL, acc.fz, o));
-            const double om = __shfl_xor_sync(FULL, acc.mind2, o);
+            const unsigned long long om = __shfl_xor_sync(FULL, acc.mind2, o);
             acc.mind2 = om < acc.mind2 ? om : acc.mind2;
         } else {
             acc.dens.merge(__shfl_xor_sync(FULL, acc.dens.s, o), __shfl_xor_sync(FULL, acc.dens.c, o));

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include "timothy_gb300.h"
+#include "tm_core.cuh"
 
 #define PEAK_CHAINS 8
 
@@ -60,5 +61,67 @@ extern "C" int tm_measure_fp32_peak(int device, double *tflops)
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
     cudaFree(out);
+    return rc;
+}
+
+// Self-check of the arithmetic the kernels form themselves instead of calling
+// the CUDA library: the FMA-based quotient against the correctly rounded
+// division, the integer rounding of a double to float against the hardware
+// conversion, and the integer float -> double conversion against the
+// hardware one, on `n` pseudo-random inputs per check (counter-based, seed).
+
+__device__ __forceinline__ unsigned long long mix64_peak(unsigned long long x)
+{
+    x += 0x9e3779b97f4a7c15ull;
+    x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+    x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+    return x ^ (x >> 31);
+}
+
+__global__ void k_numerics_check(long long n, unsigned long long seed, unsigned long long *bad)
+{
+    unsigned long long nb[3] = {0, 0, 0};
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        const unsigned long long r0 = mix64_peak(seed ^ (unsigned long long)k), r1 = mix64_peak(r0), r2 = mix64_peak(r1);
+        // quotient: b a cutoff-like length in [0.25, 16), a in [0, b] (near b for a quarter of the draws)
+        const double b = ldexp(1.0 + (double)(r0 >> 11) * 0x1.0p-53, (int)(r1 & 7) - 2);
+        double t = (double)(r2 >> 11) * 0x1.0p-53;
+        if ((r1 >> 8 & 3) == 0) t = 1.0 - t * 1e-6;
+        const double a = __dmul_rn(b, t);
+        const double y = __drcp_rn(b);
+        if (div_by_recip(a, b, y) != __ddiv_rn(a, b)) nb[0]++;
+        // double -> float rounding: random bit patterns over the float range and halfway cases
+        unsigned long long wb = (r0 & 0x800fffffffffffffull) | ((unsigned long long)(860 + (r1 % 330)) << 52);
+        if ((r2 & 3) == 0) wb = (wb & ~0x1fffffffull) | 0x10000000ull;
+        const double w = __longlong_as_double((long long)wb);
+        const double want = (double)__double2float_rn(w);
+        const double got = tm_round_to_float(w);
+        if (__double_as_longlong(got) != __double_as_longlong(want)) nb[1]++;
+        // float -> double: every class of float bit pattern
+        const float f = __uint_as_float((unsigned)(r2 >> 32));
+        const double fd = (double)f;
+        const double fg = tm_f2d(f);
+        if (!(fd != fd && fg != fg) && __double_as_longlong(fd) != __double_as_longlong(fg)) nb[2]++;
+    }
+    for (int q = 0; q < 3; q++)
+        if (nb[q]) atomicAdd(&bad[q], nb[q]);
+}
+
+extern "C" int tm_check_numerics(int device, int64_t n, uint64_t seed, int64_t *mismatches)
+{
+    if (!mismatches || n < 0) return TM_EINVAL;
+    if (cudaSetDevice(device) != cudaSuccess) return TM_ECUDA;
+    unsigned long long *d = nullptr;
+    if (cudaMalloc((void **)&d, 3 * sizeof(unsigned long long)) != cudaSuccess) return TM_ENOMEM;
+    int rc = TM_OK;
+    unsigned long long h[3] = {0, 0, 0};
+    if (cudaMemset(d, 0, sizeof h) != cudaSuccess) rc = TM_ECUDA;
+    if (rc == TM_OK) {
+        k_numerics_check<<<1024, 256>>>((long long)n, (unsigned long long)seed, d);
+        if (cudaGetLastError() != cudaSuccess || cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost) != cudaSuccess)
+            rc = TM_ECUDA;
+    }
+    cudaFree(d);
+    for (int q = 0; q < 3; q++) mismatches[q] = (int64_t)h[q];
     return rc;
 }

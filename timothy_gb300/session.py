@@ -109,6 +109,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "tm_version": (C.c_char_p, []),
         "tm_device_count": (C.c_int, []),
         "tm_measure_fp32_peak": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
+        "tm_check_numerics": (C.c_int, [C.c_int, C.c_int64, C.c_uint64, P]),
         "tm_session_create": (C.c_int, [C.POINTER(P), C.POINTER(_Config), C.POINTER(_CellTypes)]),
         "tm_session_destroy": (C.c_int, [P]),
         "tm_session_stream": (P, [P]),
@@ -275,6 +276,14 @@ def host_unregister(a: np.ndarray):
 
 def device_count() -> int:
     return int(load_library().tm_device_count())
+
+
+def check_numerics(n: int = 1 << 24, seed: int = 1, device: int = 0) -> dict:
+    """Mismatch counts of the kernels' own arithmetic against the hardware
+    and library operations (tm_check_numerics); every count must be 0."""
+    m = np.zeros(3, np.int64)
+    _check(load_library().tm_check_numerics(int(device), int(n), int(seed), _p(m)))
+    return {"quotient": int(m[0]), "round_to_float": int(m[1]), "float_to_double": int(m[2])}
 
 
 def measure_fp32_peak(device: int = 0) -> float:
