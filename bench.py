@@ -992,7 +992,7 @@ def main():
         line["forms"] = {"batched_fp32c": r4(fb["fp32c"]["value"]), "batched_fp64": r4(fb["fp64"]["value"]),
                          "serving": [{"rate": r4(f["rate_per_s"]), "served": r4(f["served_cell_updates_per_s"]),
                                       "p50": r4(f["p50_s"]), "p99": r4(f["p99_s"])}
-                                     for f in detail["forms"]["serving"]]}
+                                     for f in detail["forms"]["serving"][:1]]}
     detail["tuning"] = tuned
     if rank == 0:
         full = dict(line)

@@ -244,13 +244,14 @@ int tm_colony_cellcycle(tm_session *s, int id, const tm_cycle_params *p, int64_t
  * the work is queued: the caller leaves in's arrays unchanged, and reads
  * out's arrays only, after tm_session_sync.  With the same n, the upload's
  * size, young, ctype and phase may be NULL: those attributes keep their
- * values (an upload of positions only).  An asynchronous upload reads each
- * of x, y, z only after the same coordinate of the asynchronous download
- * queued before it has reached the host, and its other arrays after all
- * three, so a host loop may pass one step's downloaded positions to the next
- * step's upload without waiting; x travels up while y and z still come down,
- * and the other fields of that download keep travelling while the upload
- * runs.  They
+ * values (an upload of positions only).  An asynchronous download sends each
+ * of x, y, z in eight pieces, and an asynchronous upload reads each piece of
+ * each coordinate only after the same piece of the asynchronous download
+ * queued before it has reached the host (the whole coordinate when the two
+ * cell counts differ), and its other arrays after all three, so a host loop
+ * may pass one step's downloaded positions to the next step's upload without
+ * waiting; a piece travels up while the next ones still come down, and the
+ * other fields of that download keep travelling while the upload runs.  They
  * stage through device buffers of their own, 44 and 112 bytes per slot and,
  * for a downloaded grid, one copy of the colony's grid, allocated on first
  * use (not counted by tm_session_bytes). */

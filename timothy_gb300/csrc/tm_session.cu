@@ -118,6 +118,14 @@ struct colony_host {
     int active = 1;
 };
 
+// An asynchronous download sends each coordinate in IO_CHUNKS pieces and an
+// asynchronous upload of the same cells sends each piece back as soon as it
+// is on the host, so a host loop that feeds back the positions it received
+// keeps both directions of the link busy at once.
+#define IO_CHUNKS 8
+
+static long long io_chunk_lo(long long n, int j) { return n * j / IO_CHUNKS; }
+
 struct tm_session {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -147,7 +155,8 @@ struct tm_session {
     cudaEvent_t ev_up_read = nullptr;     // k_upload_pack has read up_stage
     cudaEvent_t ev_dl_gathered = nullptr, ev_dl_copied = nullptr;
     cudaEvent_t ev_dl_pos = nullptr;      // the positions of the last asynchronous download are on the host
-    cudaEvent_t ev_dl_axis[3] = {};       // its x, y, z each
+    cudaEvent_t ev_dl_chunk[3][IO_CHUNKS] = {};   // each of its x, y, z chunks
+    long long dl_pos_n = -1;              // the cell count those positions were split by
     cudaEvent_t ev_dl_part[16] = {};      // one field of an asynchronous download gathered
     bool dl_pending = false, up_pending = false;
     cudaEvent_t ev_ready[2] = {nullptr, nullptr}, ev_copied[2] = {nullptr, nullptr};
@@ -800,9 +809,11 @@ extern "C" int tm_session_destroy(tm_session *s)
     if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
     if (s->h2d_stream) cudaStreamDestroy(s->h2d_stream);
     if (s->ev_h2d) cudaEventDestroy(s->ev_h2d);
-    for (cudaEvent_t e : {s->ev_up_read, s->ev_dl_gathered, s->ev_dl_copied, s->ev_dl_pos, s->ev_dl_axis[0],
-                          s->ev_dl_axis[1], s->ev_dl_axis[2]})
+    for (cudaEvent_t e : {s->ev_up_read, s->ev_dl_gathered, s->ev_dl_copied, s->ev_dl_pos})
         if (e) cudaEventDestroy(e);
+    for (auto &axis : s->ev_dl_chunk)
+        for (cudaEvent_t e : axis)
+            if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : s->ev_dl_part)
         if (e) cudaEventDestroy(e);
     if (s->up_stage) cudaFree(s->up_stage);
@@ -1133,9 +1144,10 @@ static int async_io_init(tm_session *s)
     int rc = download_streams(s);
     if (rc) return rc;
     CK(cudaStreamCreateWithFlags(&s->h2d_stream, cudaStreamNonBlocking));
-    for (cudaEvent_t *e : {&s->ev_h2d, &s->ev_up_read, &s->ev_dl_gathered, &s->ev_dl_copied, &s->ev_dl_pos,
-                           &s->ev_dl_axis[0], &s->ev_dl_axis[1], &s->ev_dl_axis[2]})
+    for (cudaEvent_t *e : {&s->ev_h2d, &s->ev_up_read, &s->ev_dl_gathered, &s->ev_dl_copied, &s->ev_dl_pos})
         CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    for (auto &axis : s->ev_dl_chunk)
+        for (cudaEvent_t &e : axis) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     for (cudaEvent_t &e : s->ev_dl_part) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     return TM_OK;
 }
@@ -1179,14 +1191,21 @@ extern "C" int tm_colony_upload_async(tm_session *s, int id, const tm_colony_inp
     const size_t n = (size_t)in->n;
     cudaStream_t h = s->h2d_stream;
     if (s->up_pending) CK(cudaStreamWaitEvent(h, s->ev_up_read, 0));
-    // each coordinate of the asynchronous download queued before this upload
-    // reaches the host before the same coordinate is read here, so a loop may
-    // pass them to this upload; x travels up while y and z still come down
+    // each piece of each coordinate of the asynchronous download queued
+    // before this upload reaches the host before the same piece is read here,
+    // so a loop may pass the positions it received to this upload: a piece
+    // travels up while the next ones still come down (pieces of a download of
+    // another cell count: the whole coordinate first)
     double *dst3[3] = {X + o, Y + o, Z + o};
     const double *src3[3] = {in->x, in->y, in->z};
+    const bool same_split = s->dl_pos_n == (long long)n;
     for (int k = 0; k < 3; k++) {
-        if (s->dl_pending) CK(cudaStreamWaitEvent(h, s->ev_dl_axis[k], 0));
-        CK(cudaMemcpyAsync(dst3[k], src3[k], n * 8, cudaMemcpyHostToDevice, h));
+        for (int j = 0; j < IO_CHUNKS; j++) {
+            const long long lo = io_chunk_lo((long long)n, j), hi = io_chunk_lo((long long)n, j + 1);
+            if (s->dl_pending) CK(cudaStreamWaitEvent(h, s->ev_dl_chunk[k][same_split ? j : IO_CHUNKS - 1], 0));
+            if (hi > lo)
+                CK(cudaMemcpyAsync(dst3[k] + lo, src3[k] + lo, (size_t)(hi - lo) * 8, cudaMemcpyHostToDevice, h));
+        }
     }
     if (s->dl_pending) CK(cudaStreamWaitEvent(h, s->ev_dl_pos, 0));
     if (in->size) CK(cudaMemcpyAsync(SZ + o, in->size, n * 8, cudaMemcpyHostToDevice, h));
@@ -1637,10 +1656,23 @@ static int download_async_queue(tm_session *s, int id, const tm_colony_output *o
             CK(cudaGetLastError());
             CK(cudaEventRecord(s->ev_dl_part[part - 1], s->stream));
             CK(cudaStreamWaitEvent(s->copy_stream, s->ev_dl_part[part - 1], 0));
-            CK(cudaMemcpyAsync(w.host, dst, (size_t)w.size * (size_t)c.n, cudaMemcpyDeviceToHost, s->copy_stream));
-            copies.push_back({w.host, {(const void *)dst, (size_t)w.size * (size_t)c.n}});
+            int axis = -1;
             for (int k = 0; k < 3; k++)
-                if (w.src == pos3[k]) CK(cudaEventRecord(s->ev_dl_axis[k], s->copy_stream));
+                if (w.src == pos3[k]) axis = k;
+            if (axis < 0) {
+                CK(cudaMemcpyAsync(w.host, dst, (size_t)w.size * (size_t)c.n, cudaMemcpyDeviceToHost,
+                                   s->copy_stream));
+            } else {
+                // a coordinate in pieces, each announced to a following upload
+                for (int j = 0; j < IO_CHUNKS; j++) {
+                    const long long lo = io_chunk_lo(c.n, j), hi = io_chunk_lo(c.n, j + 1);
+                    if (hi > lo)
+                        CK(cudaMemcpyAsync((double *)w.host + lo, (const double *)dst + lo, (size_t)(hi - lo) * 8,
+                                           cudaMemcpyDeviceToHost, s->copy_stream));
+                    CK(cudaEventRecord(s->ev_dl_chunk[axis][j], s->copy_stream));
+                }
+            }
+            copies.push_back({w.host, {(const void *)dst, (size_t)w.size * (size_t)c.n}});
             if (w.src == last_pos) CK(cudaEventRecord(s->ev_dl_pos, s->copy_stream));
         }
     }
@@ -1664,7 +1696,9 @@ static int download_async_queue(tm_session *s, int id, const tm_colony_output *o
     const int npos = (out->x ? 1 : 0) + (out->y ? 1 : 0) + (out->z ? 1 : 0);
     if (npos == 0 || copies.empty()) CK(cudaEventRecord(s->ev_dl_pos, s->copy_stream));
     for (int k = 0; k < 3; k++)
-        if (!axis_sent[k]) CK(cudaEventRecord(s->ev_dl_axis[k], s->copy_stream));
+        if (!axis_sent[k])
+            for (int j = 0; j < IO_CHUNKS; j++) CK(cudaEventRecord(s->ev_dl_chunk[k][j], s->copy_stream));
+    s->dl_pos_n = c.n;
     if (want_grid)
         CK(cudaMemcpyAsync(out->grid, s->dl_grid, sizeof(double) * (size_t)c.ngrid, cudaMemcpyDeviceToHost,
                            s->copy_stream));
