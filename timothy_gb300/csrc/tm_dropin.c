@@ -73,6 +73,13 @@ static void pin_cells(celldata_t *cells, int64_t n)
     }
 }
 
+/* the caller's first localcount.n records lie in the page-locked range */
+static int records_pinned(const cellsinfo_t *ci)
+{
+    return g_pinned && (void *)ci->cells == g_pinned &&
+           (size_t)ci->localcount.n * sizeof(celldata_t) <= g_pinned_bytes;
+}
+
 /* session with room for n cells and the colony's options */
 static void ensure_session(int64_t n, int dim)
 {
@@ -183,7 +190,7 @@ void computepotential(systeminfo_t systeminfo, cellsinfo_t *cellsinfo, celltype_
     TRY("pair kernel", tmi_phase(g_sess, 1));
     TRY("sync", tm_session_sync(g_sess));
     TRY("download", tmi_download_aos3(g_sess, g_cid, cellsinfo->cells, (int64_t)sizeof(celldata_t),
-                                      offsetof(celldata_t, v), 0));
+                                      offsetof(celldata_t, v), 0, records_pinned(cellsinfo)));
 }
 
 static void no_remote(systeminfo_t systeminfo, cellcommdata_t cellcommdata)
@@ -315,7 +322,7 @@ void updatepositions(settings_t settings, celltype_t *celltype, cellsinfo_t *cel
     free(draws);
     TRY("random move", tmi_set_move_draws(g_sess, NULL, 0));
     TRY("positions", tmi_download_aos3(g_sess, g_cid, cellsinfo->cells, (int64_t)sizeof(celldata_t),
-                                       offsetof(celldata_t, x), 1));
+                                       offsetof(celldata_t, x), 1, records_pinned(cellsinfo)));
     int64_t marked = 0;
     TRY("marks", tmi_download_removecell(g_sess, g_cid, removecell, &marked));
     *removecount += marked;

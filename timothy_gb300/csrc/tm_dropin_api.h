@@ -31,7 +31,8 @@ int tmi_max_ctype(tm_session *s, int cid, int *maxtype);
 int tmi_phase(tm_session *s, int which);
 /* three doubles per cell, caller order, into the host AoS at byte offset `off`:
  * which = 0 -> (v, density, mindist), 1 -> (x, y, z) */
-int tmi_download_aos3(tm_session *s, int cid, void *cells, int64_t stride, int64_t off, int which);
+/* pinned: the records are page-locked (the device writes them directly) */
+int tmi_download_aos3(tm_session *s, int cid, void *cells, int64_t stride, int64_t off, int which, int pinned);
 /* forces as packed (x, y, z) triples in caller order */
 int tmi_download_forces(tm_session *s, int cid, double *f3);
 int tmi_upload_forces(tm_session *s, int cid, const double *f3);
