@@ -169,6 +169,7 @@ struct tm_session {
     bool use_graph = false;
     bool graph_valid[2] = {false, false};
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+    long long graph_shape[2][7] = {};     // what colony adds and removes can change in a captured step
     int parity = 0;   // always 0: the state stays in place between steps
     long long launches = 0;
     int kernels_per_step = 0;
@@ -533,6 +534,30 @@ static int enqueue_step(tm_session *s)
     mark(s);
     s->kernels_per_step = nk;
     return TM_OK;
+}
+
+// The launch parameters of a step that adding or removing a colony can
+// change: the slot, bin and grid high-water marks, the colony count and which
+// paths the colonies take.  Those two operations keep the captured step when
+// these are unchanged (descriptors and frames live in device memory, so a
+// colony placed in freed ranges runs in the same launches); every other
+// change of the session drops the captured steps.
+static void graph_shape_of(const tm_session *s, long long out[7])
+{
+    bool any_cic = false, any64 = false, any32 = false;
+    for (auto &c : s->cols) {
+        if (!c.used || !c.active) continue;
+        if (c.gridoff >= 0) any_cic = true;
+        if (c.opt.precision == TM_PREC_FP64) any64 = true;
+        else any32 = true;
+    }
+    out[0] = s->slots.hwm;
+    out[1] = s->bins.hwm;
+    out[2] = s->grids.hwm;
+    out[3] = (long long)s->cols.size();
+    out[4] = any_cic;
+    out[5] = any64;
+    out[6] = any32;
 }
 
 static void drop_graphs(tm_session *s)
@@ -1067,8 +1092,7 @@ static int colony_add(tm_session *s, const tm_colony_input *in, const tm_colony_
         g_err = msg;
         return rc;
     }
-    drop_graphs(s);
-    *id = c;
+    *id = c;   // the captured step stays unless its launch shape changed (graph_shape_of)
     return TM_OK;
 }
 
@@ -1105,8 +1129,7 @@ extern "C" int tm_colony_remove(tm_session *s, int id)
     if (c.gridoff >= 0) s->grids.release(c.gridoff, c.ngrid);
     c = colony_host();
     while (!s->cols.empty() && !s->cols.back().used) s->cols.pop_back();
-    drop_graphs(s);
-    return TM_OK;
+    return TM_OK;   // the captured step stays unless its launch shape changed (graph_shape_of)
 }
 
 extern "C" int tm_colony_upload(tm_session *s, int id, const tm_colony_input *in)
@@ -1326,6 +1349,9 @@ extern "C" int tm_session_set_tuning(tm_session *s, const tm_tuning *t)
 static int run_step_graph(tm_session *s)
 {
     int p = s->parity;
+    long long shape[7];
+    graph_shape_of(s, shape);
+    if (s->graph_valid[p] && memcmp(shape, s->graph_shape[p], sizeof shape) != 0) drop_graphs(s);
     if (!s->graph_valid[p]) {
         cudaGraph_t g;
         CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
@@ -1340,6 +1366,7 @@ static int run_step_graph(tm_session *s)
         cudaGraphDestroy(g);
         if (e != cudaSuccess) return tm_fail(TM_ECUDA, "graph instantiate: %s", cudaGetErrorString(e));
         s->graph_valid[p] = true;
+        memcpy(s->graph_shape[p], shape, sizeof shape);
     }
     CK(cudaGraphLaunch(s->gexec[p], s->stream));
     return TM_OK;
