@@ -9,7 +9,7 @@ The knobs are those of ``tm_tuning`` (include/timothy_gb300.h):
 
 Each knob is tuned in turn (coordinate descent) on the colonies the session
 holds, timing steps with CUDA events on the session's stream.  Kernels that
-run every step are judged by the fastest of a few steps (a step that rebuilds
+run every step are ranked by the fastest of a few steps (a step that rebuilds
 lists is slower for reasons unrelated to the knob); the search level by the
 time of a step in which every colony rebuilds; the skin by a cost model,
 
