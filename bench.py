@@ -717,20 +717,30 @@ def dropin_record(n, kind, seed, cic, steps, warmup=1, precision="fp64"):
             "calls_ms": {k: v / steps * 1e3 for k, v in calls.items()}}
 
 
+def _record_in_process(call):
+    """Run `bench.<call>` in a process of its own and return its JSON record."""
+    code = f"import json, bench; print('RECORD ' + json.dumps(bench.{call}))"
+    r = subprocess.run([sys.executable, "-c", code], cwd=os.path.dirname(os.path.abspath(__file__)),
+                       capture_output=True, text=True)
+    for ln in r.stdout.splitlines():
+        if ln.startswith("RECORD "):
+            return json.loads(ln[7:])
+    return {"error": (r.stderr or r.stdout).strip().splitlines()[-1:] if (r.stderr or r.stdout) else "no output",
+            "returncode": r.returncode}
+
+
 def dropin_record_process(n, kind, seed, cic, steps, precision="fp64"):
     """dropin_record in a process of its own, as a host program that links
     the drop-ins would run: the records, their page-locking and the device
     session start from a clean process, not from this one's other sessions
     and registered buffers."""
-    code = ("import json, bench; print('DROPIN ' + json.dumps(bench.dropin_record("
-            f"{n}, {kind!r}, {seed}, {cic}, {steps}, precision={precision!r})))")
-    r = subprocess.run([sys.executable, "-c", code], cwd=os.path.dirname(os.path.abspath(__file__)),
-                       capture_output=True, text=True)
-    for ln in r.stdout.splitlines():
-        if ln.startswith("DROPIN "):
-            return json.loads(ln[7:])
-    return {"error": (r.stderr or r.stdout).strip().splitlines()[-1:] if (r.stderr or r.stdout) else "no output",
-            "returncode": r.returncode}
+    return _record_in_process(f"dropin_record({n}, {kind!r}, {seed}, {cic}, {steps}, precision={precision!r})")
+
+
+def serving_form_process(device, rate, seconds):
+    """serving_form in a process of its own, as a server would run: its host
+    loop does not share the interpreter with this process's other records."""
+    return _record_in_process(f"serving_form(None, {device}, {rate}, {seconds})")
 
 
 def main():
@@ -940,7 +950,7 @@ def main():
         detail["rows"] = {"grid_to_cell": field_rows(local, peak), "cic_deposit": cic_rows(local, peak),
                           "diffusion": diffusion_rows(local), "cell_cycle": cycle_rows(local)}
         forms = {"batched": batched_form(args, local)}
-        forms["serving"] = [serving_form(args, local, float(r), args.serve_seconds)
+        forms["serving"] = [serving_form_process(local, float(r), args.serve_seconds)
                             for r in args.serve_rates.split(",") if r]
         detail["forms"] = forms
 
@@ -992,7 +1002,7 @@ def main():
         line["forms"] = {"batched_fp32c": r4(fb["fp32c"]["value"]), "batched_fp64": r4(fb["fp64"]["value"]),
                          "serving": [{"rate": r4(f["rate_per_s"]), "served": r4(f["served_cell_updates_per_s"]),
                                       "p50": r4(f["p50_s"]), "p99": r4(f["p99_s"])}
-                                     for f in detail["forms"]["serving"][:1]]}
+                                     for f in [x for x in detail["forms"]["serving"] if "rate_per_s" in x][:1]]}
     detail["tuning"] = tuned
     if rank == 0:
         full = dict(line)
