@@ -216,3 +216,24 @@ def test_fp32_lists_v_against_fp64_search(oracle_lib):
     assert np.all(np.abs(ref.v[flip]) <= 1e-5 * vs)
     assert np.count_nonzero(ref.v) > 0 and np.count_nonzero(out["v"]) > 0
     assert st["walked_cells"] < col.n
+
+
+@pytest.mark.parametrize("precision", ["fp32c", "fp64"])
+def test_isolated_cells_mindist_from_lists(precision):
+    """A sparse colony (about two neighbours within h per cell): many cells
+    have none, and their mindist comes from the list when the nearest entry is
+    a sure candidate of the walk.  Diagnostics walk every cell; mindist and v
+    must not change bit for bit, and fewer isolated cells must walk."""
+    from timothy_gb300 import session as S
+
+    col = C.make_colony("uniform", 30000, 42, C.initial_radius("uniform", 30000, mean=2.0))
+    fields = ["x", "y", "z", "density", "v", "mindist", "fx", "fy", "fz"]
+    a, sa = S.run_colony(col, 4, precision=precision, update="dt", dt=0.01, verlet=True, fields=fields + ["nbcount"])
+    b, sb = S.run_colony(col, 4, precision=precision, update="dt", dt=0.01, verlet=True, diagnostics=True,
+                         fields=fields)
+    for k in fields:
+        assert np.array_equal(a[k], b[k]), k
+    isolated = int(np.sum(a["nbcount"] == 0))
+    assert isolated > 1000
+    assert sb["walked_isolated_cells"] == isolated
+    assert sa["walked_isolated_cells"] < isolated
