@@ -156,6 +156,9 @@ __device__ __forceinline__ bool isolated_from_list(const tm_arrays &a, const tm_
     }
     if (!cand || !(best < (double)R)) return false;
     w.mind = best;
+    // queued as a walk, settled without one: the colony's walk counts drop
+    atomicAdd(&a.frame[w.c].walks, ~0ull);
+    atomicAdd(&a.frame[w.c].walks_isolated, ~0ull);
     return true;
 }
 
