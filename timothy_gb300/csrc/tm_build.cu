@@ -373,7 +373,8 @@ __global__ void __launch_bounds__(256) k_place(tm_arrays a, const tm_consts *K)
     const long long st = f.bin_base + b0;
     uint32_t rk = 0;
     bool dup = false;
-    for (uint32_t k = 0; k < cnt; k++) {
+    // a bin of one cell (most of them) needs no member read
+    for (uint32_t k = 0; cnt > 1 && k < cnt; k++) {
         const int j = a.grp[st + k];
         if (j == (int)r) continue;
         const uint4 kj = a.code[j];
