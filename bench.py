@@ -720,8 +720,11 @@ def dropin_record(n, kind, seed, cic, steps, warmup=1, precision="fp64"):
 def _record_in_process(call):
     """Run `bench.<call>` in a process of its own and return its JSON record."""
     code = f"import json, bench; print('RECORD ' + json.dumps(bench.{call}))"
-    r = subprocess.run([sys.executable, "-c", code], cwd=os.path.dirname(os.path.abspath(__file__)),
-                       capture_output=True, text=True)
+    try:
+        r = subprocess.run([sys.executable, "-c", code], cwd=os.path.dirname(os.path.abspath(__file__)),
+                           capture_output=True, text=True, timeout=900)
+    except subprocess.TimeoutExpired:
+        return {"error": "no record within 900 s"}
     for ln in r.stdout.splitlines():
         if ln.startswith("RECORD "):
             return json.loads(ln[7:])
