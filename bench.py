@@ -717,14 +717,14 @@ def dropin_record(n, kind, seed, cic, steps, warmup=1, precision="fp64"):
             "calls_ms": {k: v / steps * 1e3 for k, v in calls.items()}}
 
 
-def _record_in_process(call):
+def _record_in_process(call, limit_s=900):
     """Run `bench.<call>` in a process of its own and return its JSON record."""
     code = f"import json, bench; print('RECORD ' + json.dumps(bench.{call}))"
     try:
         r = subprocess.run([sys.executable, "-c", code], cwd=os.path.dirname(os.path.abspath(__file__)),
-                           capture_output=True, text=True, timeout=900)
+                           capture_output=True, text=True, timeout=limit_s)
     except subprocess.TimeoutExpired:
-        return {"error": "no record within 900 s"}
+        return {"error": f"no record within {limit_s} s"}
     for ln in r.stdout.splitlines():
         if ln.startswith("RECORD "):
             return json.loads(ln[7:])
@@ -743,7 +743,9 @@ def dropin_record_process(n, kind, seed, cic, steps, precision="fp64"):
 def serving_form_process(device, rate, seconds):
     """serving_form in a process of its own, as a server would run: its host
     loop does not share the interpreter with this process's other records."""
-    return _record_in_process(f"serving_form(None, {device}, {rate}, {seconds})")
+    # arrivals for `seconds`, then the drain (at most about twice as long when
+    # the offered load is below twice the served rate)
+    return _record_in_process(f"serving_form(None, {device}, {rate}, {seconds})", limit_s=900 + 4 * int(seconds))
 
 
 def main():
