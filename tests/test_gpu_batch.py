@@ -119,3 +119,21 @@ def test_serving_realtime_reports_latency():
     assert stats["finished"] == len(reqs) > 10
     assert 0 < stats["p50"] <= stats["p99"]
     assert stats["throughput"] > 0
+
+
+def test_serving_from_source_matches_alone():
+    """Requests cut from a source into page-locked staging (reused once their
+    upload is done): every request's result equals the same colony alone."""
+    import numpy as np
+
+    from timothy_gb300 import serving as SV
+
+    src = SV.RequestSource(n_template=60_000, seed=9)
+    reqs = SV.poisson_requests(400.0, 0.05, seed=9, lo=2000, hi=40_000, steps=(3, 6))
+    assert len(reqs) >= 8
+    with SV.Server(max_slots=150_000, max_colonies=64, fields=("x", "y", "z", "density", "fx", "fy", "fz")) as srv:
+        stats = srv.run(reqs, source=src, virtual=True)
+    assert stats["finished"] == len(reqs)
+    for r in reqs:
+        want = SV.run_alone(src.colony(r.kind, r.n, r.seed), r.steps)
+        assert r.result["density_sum"] == float(np.sum(want["density"])), r.rid

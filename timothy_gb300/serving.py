@@ -45,6 +45,7 @@ class Request:
     arrival: float                      # seconds after the start (or engine iteration, virtual clock)
     seed: int = 0
     colony: C.Colony | None = None      # cells; built on admission when None
+    stage: dict | None = field(default=None, repr=False)   # page-locked positions the colony's cells use
     admitted: float = math.nan
     finished: float = math.nan
     result: dict | None = field(default=None, repr=False)
@@ -71,14 +72,24 @@ class RequestSource:
         self.templates = {k: C.make_colony(k, n_template, seed + i, C.initial_radius(k, n_template), types=self.types)
                           for i, k in enumerate(("uniform", "clustered"))}
 
-    def colony(self, kind: str, n: int, seed: int) -> C.Colony:
+    def colony(self, kind: str, n: int, seed: int, xyz=None) -> C.Colony:
+        """The request's cells; with ``xyz`` (three float64 arrays of at least
+        n entries) the positions are written into those arrays."""
         t = self.templates[kind]
         n = int(min(n, self.n_template))
         off = int(np.random.Generator(np.random.PCG64(seed)).integers(0, self.n_template - n + 1))
         f = (n / self.n_template) ** (1.0 / 3.0)
         sl = slice(off, off + n)
-        return C.Colony(t.x[sl] * f, t.y[sl] * f, t.z[sl] * f, t.size[sl], t.young[sl], t.ctype[sl], t.phase[sl],
+        if xyz is None:
+            pos = [t.x[sl] * f, t.y[sl] * f, t.z[sl] * f]
+        else:
+            pos = [np.multiply(src[sl], f, out=dst[:n]) for src, dst in zip((t.x, t.y, t.z), xyz)]
+        return C.Colony(pos[0], pos[1], pos[2], t.size[sl], t.young[sl], t.ctype[sl], t.phase[sl],
                         self.types, t.dim, kind, seed, t.radius * f)
+
+    def template_arrays(self) -> list:
+        """The templates' per-cell arrays that requests take slices of."""
+        return [getattr(t, k) for t in self.templates.values() for k in ("size", "young", "ctype", "phase")]
 
 
 def poisson_requests(rate: float, duration: float, *, seed: int = 7, lo: int = 1000, hi: int = 1_000_000,
@@ -136,15 +147,24 @@ class Server:
         self.s.use_graph(graph)
         self._free_bufs: list[dict] = []
         self._all_bufs: list[dict] = []
+        # page-locked positions for the cells of requests being admitted (an
+        # upload from pageable memory stages through the driver and holds the
+        # host for the copy: it was most of the host loop's time)
+        self._free_stage: list[dict] = []
+        self._all_stage: list[dict] = []
+        self._pinned_sources: list = []
 
     def close(self):
         from .session import host_unregister
 
         self.s.close()
-        for b in self._all_bufs:
+        for b in self._all_bufs + self._all_stage:
             for a in b.values():
                 host_unregister(a)
-        self._all_bufs, self._free_bufs = [], []
+        for a in self._pinned_sources:
+            host_unregister(a)
+        self._all_bufs, self._free_bufs, self._all_stage, self._free_stage = [], [], [], []
+        self._pinned_sources = []
 
     def __enter__(self):
         return self
@@ -152,11 +172,44 @@ class Server:
     def __exit__(self, *exc):
         self.close()
 
+    def _stage(self, n: int) -> dict:
+        """Page-locked position arrays for one request's cells (reused)."""
+        from .session import host_register
+
+        for k, b in enumerate(self._free_stage):
+            if len(b["x"]) >= n:
+                return self._free_stage.pop(k)
+        cap = max(n, 1 << 16)
+        b = {k: np.zeros(cap) for k in ("x", "y", "z")}
+        for a in b.values():
+            host_register(a)
+        self._all_stage.append(b)
+        return b
+
+    def _prepare(self, req: Request, source: RequestSource):
+        """Build the request's cells (into page-locked staging unless results are kept)."""
+        if self.keep:
+            req.colony = source.colony(req.kind, req.n, req.seed)
+            return
+        if not self._pinned_sources:
+            from .session import TimothyError, host_register
+
+            # the templates' other fields are sliced, not copied: lock them once
+            for a in source.template_arrays():
+                if a.flags.c_contiguous and not any(a is b for b in self._pinned_sources):
+                    try:
+                        host_register(a)
+                    except TimothyError:     # locked already (another server): the copies still work
+                        continue
+                    self._pinned_sources.append(a)
+        req.stage = self._stage(req.n)
+        req.colony = source.colony(req.kind, req.n, req.seed, (req.stage["x"], req.stage["y"], req.stage["z"]))
+
     def _admit(self, req: Request, source: RequestSource | None) -> int | None:
         from .session import TimothyError
 
         if req.colony is None:
-            req.colony = source.colony(req.kind, req.n, req.seed)
+            self._prepare(req, source)
         try:
             # queued behind the step in flight (tm_colony_add_async)
             return self.s.add_colony(req.colony, precision=self.precision, update="dt", dt=self.dt, verlet=True,
@@ -196,8 +249,9 @@ class Server:
         queue: deque[Request] = deque()
         active: dict[int, list] = {}
         # steps queued on the device whose fence the host has not waited for,
-        # with the colonies each retired (their results travelling back)
-        inflight: deque[tuple[int, list]] = deque()
+        # with the colonies each retired (their results travelling back) and
+        # the staging of the colonies admitted before it (free once it is done)
+        inflight: deque[tuple[int, list, list]] = deque()
         lag = 1
         s = self.s
         t0 = time.perf_counter()
@@ -218,6 +272,7 @@ class Server:
                 queue.append(pending.popleft())
             # admission in arrival order, looking past requests that do not fit
             k = 0
+            admitted = []
             while k < min(len(queue), admit_window):
                 cid = self._admit(queue[k], source)
                 if cid is None:
@@ -227,6 +282,7 @@ class Server:
                 del queue[k]
                 req.admitted = clock()
                 active[cid] = [req, req.steps]
+                admitted.append(req)
             if active:
                 resident_max = max(resident_max, sum(r.n for r, _ in active.values()))
                 s.step(1)
@@ -237,7 +293,7 @@ class Server:
                 if source is not None:
                     for req in list(queue)[:self.prepare_ahead]:
                         if req.colony is None:
-                            req.colony = source.colony(req.kind, req.n, req.seed)
+                            self._prepare(req, source)
                 retiring = []
                 for cid in [c for c, e in active.items() if e[1] == 1]:
                     req = active.pop(cid)[0]
@@ -247,7 +303,7 @@ class Server:
                     retiring.append((req, bufs))
                 for e in active.values():
                     e[1] -= 1
-                inflight.append((s.fence(), retiring))
+                inflight.append((s.fence(), retiring, admitted))
             elif not inflight:
                 if virtual:
                     it += 1
@@ -257,9 +313,13 @@ class Server:
             # stay at most `lag` steps ahead of the device; settle everything
             # when nothing more is queued
             while inflight and (len(inflight) > lag or not active):
-                f, retiring = inflight.popleft()
+                f, retiring, admitted_then = inflight.popleft()
                 s.wait(f)
                 t = clock()
+                for req in admitted_then:           # their uploads are done
+                    if req.stage is not None:
+                        self._free_stage.append(req.stage)
+                        req.stage = None
                 for req, bufs in retiring:
                     req.finished = t
                     out = {k: bufs[k][:req.n].copy() for k in self.fields} if self.keep else None
