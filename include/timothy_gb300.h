@@ -245,7 +245,8 @@ int tm_colony_cellcycle(tm_session *s, int id, const tm_cycle_params *p, int64_t
  * out's arrays only, after tm_session_sync.  With the same n, the upload's
  * size, young, ctype and phase may be NULL: those attributes keep their
  * values (an upload of positions only).  An asynchronous download sends each
- * of x, y, z in eight pieces, and an asynchronous upload reads each piece of
+ * of x, y, z in up to eight pieces (one per 2^20 cells), and an asynchronous
+ * upload reads each piece of
  * each coordinate only after the same piece of the asynchronous download
  * queued before it has reached the host (the whole coordinate when the two
  * cell counts differ), and its other arrays after all three, so a host loop

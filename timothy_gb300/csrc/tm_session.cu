@@ -118,13 +118,21 @@ struct colony_host {
     int active = 1;
 };
 
-// An asynchronous download sends each coordinate in IO_CHUNKS pieces and an
-// asynchronous upload of the same cells sends each piece back as soon as it
-// is on the host, so a host loop that feeds back the positions it received
-// keeps both directions of the link busy at once.
+// An asynchronous download sends each coordinate in pieces (up to IO_CHUNKS,
+// one per 2^20 cells: small colonies go in one, their copies being cheaper
+// than the calls that queue them) and an asynchronous upload of the same
+// cells sends each piece back as soon as it is on the host, so a host loop
+// that feeds back the positions it received keeps both directions of the
+// link busy at once.
 #define IO_CHUNKS 8
 
-static long long io_chunk_lo(long long n, int j) { return n * j / IO_CHUNKS; }
+static int io_pieces(long long n)
+{
+    const long long p = n >> 20;
+    return p < 1 ? 1 : (p > IO_CHUNKS ? IO_CHUNKS : (int)p);
+}
+
+static long long io_chunk_lo(long long n, int j) { return n * j / io_pieces(n); }
 
 struct tm_session {
     int device = 0;
@@ -1222,8 +1230,9 @@ extern "C" int tm_colony_upload_async(tm_session *s, int id, const tm_colony_inp
     double *dst3[3] = {X + o, Y + o, Z + o};
     const double *src3[3] = {in->x, in->y, in->z};
     const bool same_split = s->dl_pos_n == (long long)n;
+    const int pieces = io_pieces((long long)n);
     for (int k = 0; k < 3; k++) {
-        for (int j = 0; j < IO_CHUNKS; j++) {
+        for (int j = 0; j < pieces; j++) {
             const long long lo = io_chunk_lo((long long)n, j), hi = io_chunk_lo((long long)n, j + 1);
             if (s->dl_pending) CK(cudaStreamWaitEvent(h, s->ev_dl_chunk[k][same_split ? j : IO_CHUNKS - 1], 0));
             if (hi > lo)
@@ -1691,13 +1700,17 @@ static int download_async_queue(tm_session *s, int id, const tm_colony_output *o
                                    s->copy_stream));
             } else {
                 // a coordinate in pieces, each announced to a following upload
-                for (int j = 0; j < IO_CHUNKS; j++) {
+                // (the last event marks the whole coordinate, for an upload of
+                // another cell count)
+                const int pieces = io_pieces(c.n);
+                for (int j = 0; j < pieces; j++) {
                     const long long lo = io_chunk_lo(c.n, j), hi = io_chunk_lo(c.n, j + 1);
                     if (hi > lo)
                         CK(cudaMemcpyAsync((double *)w.host + lo, (const double *)dst + lo, (size_t)(hi - lo) * 8,
                                            cudaMemcpyDeviceToHost, s->copy_stream));
                     CK(cudaEventRecord(s->ev_dl_chunk[axis][j], s->copy_stream));
                 }
+                if (pieces < IO_CHUNKS) CK(cudaEventRecord(s->ev_dl_chunk[axis][IO_CHUNKS - 1], s->copy_stream));
             }
             copies.push_back({w.host, {(const void *)dst, (size_t)w.size * (size_t)c.n}});
             if (w.src == last_pos) CK(cudaEventRecord(s->ev_dl_pos, s->copy_stream));
@@ -1723,8 +1736,10 @@ static int download_async_queue(tm_session *s, int id, const tm_colony_output *o
     const int npos = (out->x ? 1 : 0) + (out->y ? 1 : 0) + (out->z ? 1 : 0);
     if (npos == 0 || copies.empty()) CK(cudaEventRecord(s->ev_dl_pos, s->copy_stream));
     for (int k = 0; k < 3; k++)
-        if (!axis_sent[k])
-            for (int j = 0; j < IO_CHUNKS; j++) CK(cudaEventRecord(s->ev_dl_chunk[k][j], s->copy_stream));
+        if (!axis_sent[k]) {
+            for (int j = 0; j < io_pieces(c.n); j++) CK(cudaEventRecord(s->ev_dl_chunk[k][j], s->copy_stream));
+            CK(cudaEventRecord(s->ev_dl_chunk[k][IO_CHUNKS - 1], s->copy_stream));
+        }
     s->dl_pos_n = c.n;
     if (want_grid)
         CK(cudaMemcpyAsync(out->grid, s->dl_grid, sizeof(double) * (size_t)c.ngrid, cudaMemcpyDeviceToHost,
