@@ -36,6 +36,21 @@ def test_request_source_keeps_density():
     assert not np.array_equal(a.x, b.x)
 
 
+def test_request_source_into_staging_matches_allocation():
+    """Cells cut into caller-provided (page-locked) position arrays are the
+    same values as the allocating path; the other fields are template views."""
+    src = SV.RequestSource(n_template=40_000, seed=3)
+    stage = [np.full(9000, np.nan) for _ in range(3)]
+    for kind, n, seed in (("uniform", 5000, 11), ("clustered", 8000, 12)):
+        a = src.colony(kind, n, seed)
+        b = src.colony(kind, n, seed, stage)
+        for k in ("x", "y", "z", "size", "young", "ctype", "phase"):
+            assert np.array_equal(getattr(a, k), getattr(b, k)), (kind, k)
+        assert np.shares_memory(b.x, stage[0]) and np.shares_memory(b.z, stage[2])
+        assert any(np.shares_memory(b.size, t) for t in src.template_arrays())
+        assert b.n == n and a.radius == b.radius
+
+
 def test_make_batch_sizes_kinds_seeds():
     cols = B.make_batch(40, seed=4, lo=1000, hi=20_000)
     n = np.array([c.n for c in cols])
